@@ -1,0 +1,109 @@
+"""Synthetic circuit workloads.
+
+* ``code_circuit(family, distance, rounds, p)`` loads a committed circuit of one of the reference's
+  generated code families (rotated/unrotated surface code, repetition code, color code), produced by
+  the reference's own generator with all four noise knobs (after_clifford_depolarization,
+  before_round_data_depolarization, before_measure_flip_probability, after_reset_flip_probability)
+  set to 0.001, and substitutes the requested probability.  The templates live in
+  tests/golden/circuits/ and are made by tests/golden/make_golden.py.
+* ``random_clifford_circuit`` builds the random-Clifford correctness workload: layers drawn uniformly
+  from {H, S, CX, CZ, SWAP, ISWAP, MPP (2-4 body), M, R, MR}, DEPOLARIZE1/2 after each gate layer with
+  p in [1e-4, 1e-2], and every measurement result annotated as its own DETECTOR.
+"""
+
+import math
+import os
+import random
+
+_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CIRCUIT_DIR = os.path.join(_ROOT, "tests", "golden", "circuits")
+
+FAMILIES = {
+    "surface_code:rotated_memory_z": "surface_rz",
+    "surface_code:rotated_memory_x": "surface_rx",
+    "surface_code:unrotated_memory_z": "surface_uz",
+    "repetition_code:memory": "rep",
+    "color_code:memory_xyz": "color",
+}
+
+TEMPLATE_P = "0.001"
+
+
+def template_path(family: str, distance: int, rounds: int) -> str:
+    return os.path.join(CIRCUIT_DIR, f"{FAMILIES[family]}_d{distance}_r{rounds}.stim")
+
+
+def format_p(p: float) -> str:
+    if p == 0:
+        return "0"
+    s = repr(float(p))
+    return s
+
+
+def code_circuit(family: str, distance: int, rounds: int, p: float) -> str:
+    """The generated code circuit with every noise probability set to p."""
+    path = template_path(family, distance, rounds)
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"no committed template for {family} d={distance} r={rounds}: {path}")
+    with open(path) as f:
+        text = f.read()
+    return text.replace("(" + TEMPLATE_P + ")", "(" + format_p(p) + ")")
+
+
+def random_clifford_circuit(num_qubits: int, depth: int, seed: int, p_lo: float = 1e-4,
+                            p_hi: float = 1e-2) -> str:
+    rng = random.Random(seed)
+    gates = ["H", "S", "CX", "CZ", "SWAP", "ISWAP", "MPP", "M", "R", "MR"]
+    lines = []
+
+    def p_draw():
+        return math.exp(rng.uniform(math.log(p_lo), math.log(p_hi)))
+
+    def subset():
+        return [q for q in range(num_qubits) if rng.random() < 0.5]
+
+    def pairs():
+        qs = list(range(num_qubits))
+        rng.shuffle(qs)
+        k = rng.randint(1, num_qubits // 2)
+        return [(qs[2 * i], qs[2 * i + 1]) for i in range(k)]
+
+    for _ in range(depth):
+        g = gates[rng.randrange(len(gates))]
+        if g in ("H", "S"):
+            qs = subset()
+            if not qs:
+                continue
+            lines.append(g + " " + " ".join(map(str, qs)))
+            lines.append(f"DEPOLARIZE1({p_draw():.6g}) " + " ".join(map(str, qs)))
+        elif g in ("CX", "CZ", "SWAP", "ISWAP"):
+            ps = pairs()
+            flat = " ".join(f"{a} {b}" for a, b in ps)
+            lines.append(g + " " + flat)
+            lines.append(f"DEPOLARIZE2({p_draw():.6g}) " + flat)
+        elif g == "MPP":
+            qs = list(range(num_qubits))
+            rng.shuffle(qs)
+            prods = []
+            i = 0
+            while i + 4 <= len(qs) and rng.random() < 0.9:
+                w = rng.randint(2, 4)
+                terms = [rng.choice("XYZ") + str(q) for q in qs[i:i + w]]
+                i += w
+                prods.append(("!" if rng.random() < 0.25 else "") + "*".join(terms))
+            if not prods:
+                continue
+            lines.append("MPP " + " ".join(prods))
+            n = len(prods)
+            for k in range(n):
+                lines.append(f"DETECTOR rec[-{n - k}]")
+        else:
+            qs = subset()
+            if not qs:
+                continue
+            lines.append(g + " " + " ".join(map(str, qs)))
+            if g in ("M", "MR"):
+                n = len(qs)
+                for k in range(n):
+                    lines.append(f"DETECTOR rec[-{n - k}]")
+    return "\n".join(lines) + "\n"

@@ -1,0 +1,119 @@
+"""Regenerates the golden fixtures under tests/golden/ from the REFERENCE itself.
+
+Run in a container where the reference tree exists (it is never copied into this repository):
+
+    make -C oracle ref                 # builds oracle/_ref/stim and oracle/_ref/ref_inject from the
+                                       # reference's own sources
+    python tests/golden/make_golden.py
+
+It writes
+  * tests/golden/circuits/*.stim  circuits made by the reference's generator (`stim gen`) with all four
+                                  noise knobs at 0.001 (stim_gb300.workloads substitutes other p);
+  * tests/golden/<case>.npz       for each case: the circuit text, seed, shot count, and the
+                                  detection events, observable flips and measurement flips that the
+                                  reference's FrameSimulator produced when fed the injected random
+                                  stream of stim_gb300/csrc/gfs_contract.h (oracle/ref_inject.cc), plus
+                                  the reference sample from the reference's TableauSimulator.
+"""
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from stim_gb300 import workloads  # noqa: E402
+
+STIM = os.path.join(ROOT, "oracle", "_ref", "stim")
+REF_INJECT = os.path.join(ROOT, "oracle", "_ref", "ref_inject")
+
+GEN = {
+    "surface_code:rotated_memory_z": ("surface_code", "rotated_memory_z", list(range(3, 27, 2))),
+    "surface_code:rotated_memory_x": ("surface_code", "rotated_memory_x", list(range(3, 23, 2))),
+    "surface_code:unrotated_memory_z": ("surface_code", "unrotated_memory_z", [3, 5]),
+    "repetition_code:memory": ("repetition_code", "memory", list(range(3, 53, 2))),
+    "color_code:memory_xyz": ("color_code", "memory_xyz", list(range(3, 17, 2))),
+}
+
+
+def gen_templates():
+    os.makedirs(workloads.CIRCUIT_DIR, exist_ok=True)
+    p = workloads.TEMPLATE_P
+    for family, (code, task, ds) in GEN.items():
+        for d in ds:
+            out = subprocess.run(
+                [STIM, "gen", "--code", code, "--task", task, "--distance", str(d), "--rounds", str(d),
+                 "--after_clifford_depolarization", p, "--before_round_data_depolarization", p,
+                 "--before_measure_flip_probability", p, "--after_reset_flip_probability", p],
+                check=True, capture_output=True, text=True).stdout
+            with open(workloads.template_path(family, d, d), "w") as f:
+                f.write(out)
+
+
+def run_ref(text: str, seed: int, shots: int):
+    with tempfile.TemporaryDirectory() as td:
+        cpath = os.path.join(td, "c.stim")
+        opath = os.path.join(td, "o.bin")
+        with open(cpath, "w") as f:
+            f.write(text)
+        subprocess.run([REF_INJECT, cpath, str(seed), str(shots), opath], check=True)
+        raw = open(opath, "rb").read()
+    assert raw[:8] == b"GFSREF01"
+    s, D, O, M = [int(v) for v in np.frombuffer(raw[8:40], dtype=np.uint64)]
+    off = 40
+    out = {}
+    for name, n in (("dets", D), ("obs", O), ("meas", M)):
+        nb = (n + 7) // 8
+        out[name] = np.frombuffer(raw[off:off + s * nb], dtype=np.uint8).reshape(s, nb).copy()
+        off += s * nb
+    out["ref_sample"] = np.frombuffer(raw[off:off + (M + 7) // 8], dtype=np.uint8).copy()
+    out["num_detectors"], out["num_observables"], out["num_measurements"] = D, O, M
+    return out
+
+
+def hand(name):
+    with open(os.path.join(HERE, "hand", name + ".stim")) as f:
+        return f.read()
+
+
+def cases():
+    cc = workloads.code_circuit
+    rc = workloads.random_clifford_circuit
+    return [
+        ("surface_rz_d3_r3_p0.001", cc("surface_code:rotated_memory_z", 3, 3, 0.001), 0, 4096),
+        ("surface_rz_d3_r3_p0.05", cc("surface_code:rotated_memory_z", 3, 3, 0.05), 1, 1024),
+        ("surface_rx_d5_r5_p0.01", cc("surface_code:rotated_memory_x", 5, 5, 0.01), 2, 1024),
+        ("surface_rx_d11_r11_p0.005", cc("surface_code:rotated_memory_x", 11, 11, 0.005), 3, 512),
+        ("surface_rx_d11_r11_p0", cc("surface_code:rotated_memory_x", 11, 11, 0.0), 4, 256),
+        ("surface_uz_d5_r5_p0.02", cc("surface_code:unrotated_memory_z", 5, 5, 0.02), 5, 512),
+        ("rep_d9_r9_p0.02", cc("repetition_code:memory", 9, 9, 0.02), 6, 1024),
+        ("color_d5_r5_p0.01", cc("color_code:memory_xyz", 5, 5, 0.01), 7, 1024),
+        ("all_gates_s5", hand("all_gates"), 5, 1024),
+        ("all_gates_s6_384", hand("all_gates"), 6, 384),
+        ("all_gates_s7_200", hand("all_gates"), 7, 200),
+        ("feedback", hand("feedback"), 8, 1024),
+        ("pauli_channels", hand("pauli_channels"), 9, 1024),
+        ("obs_data_1001", hand("obs_data"), 10, 1001),
+        ("random_clifford_n64_d200_s1", rc(64, 200, 1), 11, 512),
+        ("random_clifford_n64_d200_s2", rc(64, 200, 2), 12, 512),
+        ("random_clifford_n128_d200_s3", rc(128, 200, 3), 13, 256),
+        ("random_clifford_n300_d60_s4", rc(300, 60, 4), 14, 256),
+    ]
+
+
+def main():
+    gen_templates()
+    for name, text, seed, shots in cases():
+        out = run_ref(text, seed, shots)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), circuit=np.array(text), seed=np.uint64(seed),
+                            shots=np.uint64(shots), **out)
+        print(name, out["num_detectors"], out["num_measurements"], shots)
+
+
+if __name__ == "__main__":
+    main()
