@@ -1,0 +1,318 @@
+"""Benchmark: detection-event Gbit/s of the bulk detection sampler.
+
+Workload (one step): 2^20 shots of the rotated surface code memory-Z experiment, distance 25, 25 rounds
+(1249 qubits, 15,600 detectors + 1 observable, REPEAT block kept as a loop), p = 1e-3 on all four noise
+knobs, generated by the reference's generator (tests/golden/circuits/surface_rz_d25_r25.stim).  This is
+one 2^20-shot chunk of the 2^24-shot streamed configuration.
+
+  value : device-resident Gbit/s = shots x (detectors + observables) / time of the frame kernel plus the
+          shot-major transpose, output left in HBM (CUDA events on the library's stream).
+  e2e   : the same metric through the public API (CompiledDetectorSampler.sample(..., bit_packed=True,
+          separate_observables=True)) into host numpy arrays, device->host copy included.
+
+`--impl reference` times the CPU reference implementation of the path on the host cores: the oracle port
+(oracle/stim_oracle.c, a 64-bit-word restatement of the reference's FrameSimulator) with all host threads,
+on a bounded sample of the same workload per step.
+"""
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "detection-event Gbit/s at d=25 r=25 (surface_code:rotated_memory_z, p=1e-3)"
+UNIT = "Gbit/s"
+WORKLOAD = dict(family="surface_code:rotated_memory_z", distance=25, rounds=25, p=0.001)
+
+
+def circuit_text():
+    from stim_gb300 import workloads
+
+    return workloads.code_circuit(WORKLOAD["family"], WORKLOAD["distance"], WORKLOAD["rounds"], WORKLOAD["p"])
+
+
+def algorithmic_work(text):
+    """Per-shot shared-memory frame-bit accesses and random bits, with the per-gate rules:
+    1q Clifford = read 2 + write 2 (H) or 1 (S-like); CX/CZ = read 4 + write 2; other 2q = 8; M = 3;
+    MR = 4; R = 2; DETECTOR with k record refs = k + 1; a noise hit = 4 (8 for DEPOLARIZE2);
+    random bits = 1 per M/MR/R target plus one per qubit at the start of a shot."""
+    acc = 0.0
+    rbits = 0.0
+    hits = 0.0
+    mult = [1]
+    for line in text.splitlines():
+        line = line.split("#")[0].strip()
+        if not line:
+            continue
+        if line.startswith("REPEAT"):
+            mult.append(mult[-1] * int(line.split()[1]))
+            continue
+        if line == "}":
+            mult.pop()
+            continue
+        m = re.match(r"([A-Z_0-9]+)(?:\(([^)]*)\))?\s*(.*)", line)
+        g, args, targets = m.group(1), m.group(2), m.group(3).split()
+        k = mult[-1]
+        n = len(targets)
+        if g in ("H", "H_YZ", "SQRT_X", "SQRT_Y"):
+            acc += k * n * 4
+        elif g in ("S", "S_DAG", "H_XY"):
+            acc += k * n * 3
+        elif g in ("CX", "CZ", "CY"):
+            acc += k * (n // 2) * 6
+        elif g in ("SWAP", "ISWAP"):
+            acc += k * (n // 2) * 8
+        elif g in ("M", "MX"):
+            acc += k * n * 3
+            rbits += k * n
+        elif g in ("MR", "MRX"):
+            acc += k * n * 4
+            rbits += k * n
+        elif g in ("R", "RX"):
+            acc += k * n * 2
+            rbits += k * n
+        elif g == "DETECTOR":
+            acc += k * (n + 1)
+        elif g in ("X_ERROR", "Z_ERROR", "DEPOLARIZE1"):
+            hits += k * n * float(args)
+            acc += k * n * float(args) * 4
+        elif g == "DEPOLARIZE2":
+            hits += k * (n // 2) * float(args)
+            acc += k * (n // 2) * float(args) * 8
+    return acc, rbits, hits
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) >= 9:
+                for name, v in zip(names, r[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def cpu_baseline(text, D, O, shots, threads):
+    from oracle.oracle import OracleCircuit
+
+    c = OracleCircuit(text)
+    c.sample(min(shots, 1024), 1, threads=threads)  # warm
+    t0 = time.perf_counter()
+    c.sample(shots, 2, threads=threads)
+    dt = time.perf_counter() - t0
+    return shots * (D + O) / dt / 1e9, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle.oracle import OracleCircuit
+
+    text = circuit_text()
+    c = OracleCircuit(text)
+    D, O = c.num_detectors, c.num_observables
+    threads = os.cpu_count() or 1
+    sample_shots = args.cpu_shots
+    for _ in range(args.warmup):
+        c.sample(sample_shots, 0, threads=threads)
+    times = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        c.sample(sample_shots, 1 + k, threads=threads)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = args.steps * sample_shots * (D + O) / total / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 bitwise",
+        "data": "synthetic (reference-generated circuit, seeded shots)",
+        "config": {"workload": "surface_code:rotated_memory_z d=25 r=25 p=1e-3", "shots_per_step": sample_shots,
+                   "note": "oracle port (oracle/stim_oracle.c) on host cores; the reference tree is not present here"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{sample_shots} shots per step x {args.steps} steps, 64-bit words"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "p50_ms": 1e3 * statistics.median(times),
+        "p99_ms": 1e3 * sorted(times)[min(len(times) - 1, int(math.ceil(0.99 * len(times))) - 1)],
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    import stim_gb300
+    from stim_gb300 import _native
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    text = circuit_text()
+    circ = stim_gb300.Circuit(text)
+    D, O = circ.num_detectors, circ.num_observables
+    shots = args.shots
+    sampler = circ.compile_detector_sampler(seed=args.seed + rank, device=local)
+    if args.shape:
+        b, t = [int(x) for x in args.shape.split(",")]
+        sampler.set_launch_shape(b, t)
+    drow, orow = (D + 7) // 8, (O + 7) // 8
+    dets = torch.empty((shots, drow), dtype=torch.uint8, device=f"cuda:{local}")
+    obs = torch.empty((shots, orow), dtype=torch.uint8, device=f"cuda:{local}")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    L = _native.lib()
+    flags = _native.BIT_PACKED
+
+    def device_step():
+        _native.check(L.gfs_sample_detections_device(sampler._h, shots, flags, dets.data_ptr(), drow,
+                                                     obs.data_ptr(), orow))
+        return sampler.last_timings()
+
+    for _ in range(args.warmup):
+        device_step()
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    frame_ms, step_ms, launches = [], [], 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()  # outputs exceed L2 anyway; also evict them between steps
+        t = device_step()
+        frame_ms.append(t["frame_ms"])
+        step_ms.append(t["frame_ms"] + t["transpose_ms"])
+        launches += t["frame_launches"] + t["transpose_launches"]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    dev_s = sum(step_ms) / 1e3
+    if world > 1:
+        tt = torch.tensor([dev_s], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        dev_s = float(tt.item())
+    value = world * args.steps * shots * (D + O) / dev_s / 1e9
+
+    # End to end through the public API into host numpy arrays.
+    e2e_times = []
+    for k in range(args.e2e_steps + 1):
+        t1 = time.perf_counter()
+        sampler.sample(shots, bit_packed=True, separate_observables=True)
+        if k:
+            e2e_times.append(time.perf_counter() - t1)
+    e2e_s = sum(e2e_times)
+    e2e_value = world * len(e2e_times) * shots * (D + O) / e2e_s / 1e9
+
+    acc_bits, rbits, hits = algorithmic_work(text)
+    frame_avg_s = statistics.mean(frame_ms) / 1e3
+    achieved_gbs = acc_bits / 8 * shots / frame_avg_s / 1e9
+    smem_peak = _native.measure_smem_peak(local) / 1e9
+
+    if rank == 0:
+        cb_value, cb_s = cpu_baseline(text, D, O, args.cpu_shots, os.cpu_count() or 1)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32 bitwise",
+            "data": "synthetic (reference-generated circuit, seeded shots)",
+            "config": {"workload": "surface_code:rotated_memory_z d=25 r=25 p=1e-3", "shots_per_step": shots,
+                       "detectors": D, "observables": O, "launch_shape": sampler.launch_shape(),
+                       "l2": "outputs (2 GB/step) exceed L2; a 256 MiB buffer is also rewritten between steps",
+                       "parallelism": f"replicas by shot range x{world}"},
+            "p50_ms": statistics.median(step_ms), "p99_ms": sorted(step_ms)[-1],
+            "wall_ms_per_step": 1e3 * wall / args.steps,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": shots * (drow + orow),
+                    "ms_per_step": 1e3 * e2e_s / max(1, len(e2e_times))},
+            "gpu_launches": launches,
+            "roofline": {"bound": "smem", "achieved": achieved_gbs, "peak": smem_peak, "unit": "GB/s",
+                         "frac": achieved_gbs / smem_peak, "traffic": None,
+                         "basis": f"{acc_bits:.0f} frame-bit accesses/shot x {shots} shots per frame-kernel launch; "
+                                  "peak = project shared-memory probe (gfs_measure_smem_peak)"},
+            "cpu_baseline": {"value": cb_value, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                             "sample": f"{args.cpu_shots} shots of the same workload ({cb_s:.1f} s), oracle port"},
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--shots", type=int, default=1 << 20)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-shots", type=int, default=1 << 15)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--shape", default="")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,125 @@
+/*
+ * stim_gb300.h -- C ABI of the GB300 frame sampler (libstim_gb300.so).
+ *
+ * Plain pointers and sizes only.  Every entry point returns a gfs_status; on failure
+ * gfs_last_error() returns a thread-local message whose text matches the reference's exception
+ * message for the same condition.  No C++ exception crosses this boundary.
+ *
+ * The boundary replaces stim::FrameSimulator<W> as held by the reference's compiled samplers:
+ *   - CompiledDetectorSampler  (src/stim/py/compiled_detector_sampler.pybind.h:28-54,
+ *                               compiled_detector_sampler.pybind.cc:28-86)
+ *   - CompiledMeasurementSampler (src/stim/py/compiled_measurement_sampler.pybind.cc:31-83)
+ * and the batch drivers they call (src/stim/simulators/frame_simulator_util.inl:21-35, 290-315).
+ */
+#ifndef STIM_GB300_H
+#define STIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gfs_status {
+    GFS_OK = 0,
+    GFS_ERR_INVALID_ARGUMENT = 1, /* reference: std::invalid_argument -> ValueError */
+    GFS_ERR_OUT_OF_RANGE = 2,     /* reference: std::out_of_range -> IndexError (e.g. measure_record_batch.inl:84-92) */
+    GFS_ERR_CUDA = 3,             /* a CUDA runtime call failed or no device is present */
+    GFS_ERR_OUT_OF_MEMORY = 4,
+    GFS_ERR_INTERNAL = 5
+} gfs_status;
+
+typedef struct gfs_circuit gfs_circuit; /* parsed circuit (host) */
+typedef struct gfs_sampler gfs_sampler; /* lowered program + device state + random stream position */
+
+/* Sampling modes. */
+#define GFS_MODE_DETECTIONS 0u   /* CompiledDetectorSampler */
+#define GFS_MODE_MEASUREMENTS 1u /* CompiledMeasurementSampler */
+
+/* Layout flags of gfs_sample_detections (compiled_detector_sampler.pybind.cc:216-322). */
+#define GFS_PREPEND_OBSERVABLES 1u
+#define GFS_APPEND_OBSERVABLES 2u
+#define GFS_BIT_PACKED 4u
+
+/* Thread-local message of the last failed call on this thread. */
+const char *gfs_last_error(void);
+
+/* Library / device information.  out[0] = device count. */
+gfs_status gfs_device_count(int *out);
+
+/*
+ * Parses .stim text (replaces stim::Circuit(text), src/stim/circuit/circuit.cc:302-310).
+ * stats[0..5] = num_qubits, num_measurements, num_detectors, num_observables, max_lookback,
+ * number of instructions with REPEAT unrolled.
+ */
+gfs_status gfs_circuit_parse(const char *text, size_t len, gfs_circuit **out);
+gfs_status gfs_circuit_stats(const gfs_circuit *c, uint64_t *stats6);
+void gfs_circuit_free(gfs_circuit *c);
+
+/*
+ * Lowers the circuit for `mode` and uploads it to CUDA device `device`; the random stream starts at
+ * shot 0 of `seed` (replaces the sampler constructors, compiled_detector_sampler.pybind.cc:28-32,151-154
+ * and compiled_measurement_sampler.pybind.cc:63-83).  Successive sample calls continue the stream.
+ */
+gfs_status gfs_sampler_create(const gfs_circuit *c, uint32_t mode, uint64_t seed, int device, gfs_sampler **out);
+void gfs_sampler_free(gfs_sampler *s);
+
+/*
+ * Detection events of `shots` shots into caller-owned HOST memory (mirrors sample(shots,
+ * prepend_observables, append_observables, bit_packed, dets_out, obs_out), compiled_detector_sampler.pybind.cc:34-86).
+ * dets: shots rows of `dets_stride` bytes holding the detectors (with observables prepended/appended per
+ * flags), bit-packed little-endian when GFS_BIT_PACKED, else one 0/1 byte per bit.  obs (may be NULL):
+ * the observables alone, same packing, `obs_stride` bytes per shot.
+ */
+gfs_status gfs_sample_detections(gfs_sampler *s, uint64_t shots, uint32_t flags, uint8_t *dets, uint64_t dets_stride,
+                                 uint8_t *obs, uint64_t obs_stride);
+
+/*
+ * Measurement results into caller-owned HOST memory (mirrors CompiledMeasurementSampler.sample,
+ * compiled_measurement_sampler.pybind.cc:31-35 -> frame_simulator_util.inl:290-315).  ref_sample: the
+ * reference sample, ceil(num_measurements/8) bytes bit-packed, XORed into every shot; NULL = all zero
+ * (skip_reference_sample=True).
+ */
+gfs_status gfs_sample_measurements(gfs_sampler *s, uint64_t shots, uint32_t flags, const uint8_t *ref_sample,
+                                   uint8_t *out, uint64_t out_stride);
+
+/*
+ * Same as gfs_sample_detections but the outputs are DEVICE pointers on the sampler's device (for callers
+ * that keep results in HBM, e.g. a decoder on the same GPU).  The call returns when the results are
+ * written.
+ */
+gfs_status gfs_sample_detections_device(gfs_sampler *s, uint64_t shots, uint32_t flags, void *dets,
+                                        uint64_t dets_stride, void *obs, uint64_t obs_stride);
+
+/*
+ * Device timings (milliseconds, CUDA events on the sampler's stream) of the last sample call:
+ * out[0] = frame kernel, out[1] = transpose kernel(s), out[2] = device->host copies, out[3] = whole call.
+ * counts[0] = frame-kernel launches, counts[1] = transpose launches.
+ */
+gfs_status gfs_sampler_last_timings(const gfs_sampler *s, double *out4, uint64_t *counts2);
+
+/*
+ * Launch shape: blocks_per_cta in {1, 2, 4} (128-shot blocks held in one CTA's shared memory),
+ * threads per CTA (multiple of 32, <= 256), grid CTAs (0 = one full wave of resident CTAs).
+ * Fails when the circuit's state does not fit shared memory with that many blocks.
+ */
+gfs_status gfs_sampler_set_shape(gfs_sampler *s, int blocks_per_cta, int threads, int grid);
+gfs_status gfs_sampler_get_shape(const gfs_sampler *s, int *blocks_per_cta, int *threads, int *grid,
+                                 uint64_t *smem_bytes);
+
+/*
+ * Measures the shared-memory load+store throughput of `device` with a project-written probe kernel
+ * (bytes per second summed over all SMs).  The frame kernel's roofline denominator.  No counterpart in
+ * the reference (it has no GPU code).
+ */
+gfs_status gfs_measure_smem_peak(int device, double *bytes_per_s);
+
+/* Maximum shots per device chunk (bounds HBM use); 0 restores the default. */
+gfs_status gfs_sampler_set_chunk_shots(gfs_sampler *s, uint64_t shots);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* STIM_GB300_H */

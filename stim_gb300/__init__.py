@@ -1,0 +1,220 @@
+"""GB300 frame sampler: a drop-in for the reference's bulk detection-event and measurement samplers.
+
+Mirrors the Python surface of the reference's compiled samplers:
+
+* ``Circuit.compile_detector_sampler(*, seed=None)`` (src/stim/circuit/circuit.pybind.cc:827-831)
+  -> ``CompiledDetectorSampler.sample(shots, *, prepend_observables, append_observables,
+  separate_observables, bit_packed, dets_out, obs_out)`` (src/stim/py/compiled_detector_sampler.pybind.cc:34-86,
+  216-322);
+* ``Circuit.compile_sampler(*, skip_reference_sample=False, seed=None, reference_sample=None)``
+  (circuit.pybind.cc:588-595, compiled_measurement_sampler.pybind.cc:63-83) -> ``.sample(shots, *, bit_packed)``.
+
+Everything runs through the C ABI of libstim_gb300.so on a CUDA device.  Random streams are the
+counter-based contract of csrc/gfs_contract.h: the same seed gives the same shots on every run, every
+slicing and every GPU, but not the reference's mt19937_64 stream (which the reference itself documents as
+unstable across versions and machines).
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import _native
+from ._native import check, lib
+
+__all__ = ["Circuit", "CompiledDetectorSampler", "CompiledMeasurementSampler", "device_count"]
+
+
+def device_count() -> int:
+    return _native.device_count()
+
+
+def _seed_value(seed):
+    if seed is None:
+        return int.from_bytes(os.urandom(8), "little")
+    if isinstance(seed, bool) or not isinstance(seed, (int, np.integer)) or not (0 <= int(seed) < 2**64):
+        raise ValueError("Expected seed to be None or a 64 bit unsigned integer.")
+    return int(seed)
+
+
+class Circuit:
+    """A parsed .stim circuit (parsing happens in the library's C++ host code)."""
+
+    def __init__(self, text: str = ""):
+        if not isinstance(text, str):
+            text = str(text)
+        self._text = text
+        h = ctypes.c_void_p()
+        data = text.encode()
+        check(lib().gfs_circuit_parse(data, len(data), ctypes.byref(h)))
+        self._h = h
+        s = (ctypes.c_uint64 * 6)()
+        check(lib().gfs_circuit_stats(self._h, s))
+        (self.num_qubits, self.num_measurements, self.num_detectors, self.num_observables,
+         self.max_lookback, self.num_instructions_unrolled) = [int(v) for v in s]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().gfs_circuit_free(h)
+            self._h = None
+
+    def __str__(self):
+        return self._text
+
+    def __repr__(self):
+        return f"stim_gb300.Circuit({self._text!r})"
+
+    def compile_detector_sampler(self, *, seed=None, device: int = 0) -> "CompiledDetectorSampler":
+        return CompiledDetectorSampler(self, seed=seed, device=device)
+
+    def compile_sampler(self, *, skip_reference_sample: bool = False, seed=None, reference_sample=None,
+                        device: int = 0) -> "CompiledMeasurementSampler":
+        return CompiledMeasurementSampler(self, skip_reference_sample=skip_reference_sample, seed=seed,
+                                          reference_sample=reference_sample, device=device)
+
+
+class _SamplerBase:
+    _mode = None
+
+    def __init__(self, circuit, seed, device):
+        if not isinstance(circuit, Circuit):
+            circuit = Circuit(str(circuit))
+        self._circuit = circuit
+        h = ctypes.c_void_p()
+        check(lib().gfs_sampler_create(circuit._h, self._mode, _seed_value(seed), int(device), ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().gfs_sampler_free(h)
+            self._h = None
+
+    # -- tuning / introspection (no counterpart in the reference) --
+    def set_launch_shape(self, blocks_per_cta: int, threads: int = 256, grid: int = 0):
+        check(lib().gfs_sampler_set_shape(self._h, blocks_per_cta, threads, grid))
+
+    def launch_shape(self):
+        b, t, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        sm = ctypes.c_uint64()
+        check(lib().gfs_sampler_get_shape(self._h, ctypes.byref(b), ctypes.byref(t), ctypes.byref(g),
+                                          ctypes.byref(sm)))
+        return {"blocks_per_cta": b.value, "threads": t.value, "grid": g.value, "smem_bytes": sm.value}
+
+    def set_chunk_shots(self, shots: int):
+        check(lib().gfs_sampler_set_chunk_shots(self._h, int(shots)))
+
+    def last_timings(self):
+        t = (ctypes.c_double * 4)()
+        c = (ctypes.c_uint64 * 2)()
+        check(lib().gfs_sampler_last_timings(self._h, t, c))
+        return {"frame_ms": t[0], "transpose_ms": t[1], "copy_ms": t[2], "total_ms": t[3],
+                "frame_launches": int(c[0]), "transpose_launches": int(c[1])}
+
+
+def _out_array(out, shape, packed):
+    dtype = np.uint8 if packed else np.bool_
+    if out is None:
+        return np.empty(shape, dtype=dtype), None
+    if not isinstance(out, np.ndarray) or out.dtype != dtype:
+        raise ValueError("Output buffer wasn't a numpy.ndarray[%s]." % ("np.uint8" if packed else "np.bool_"))
+    if out.ndim != 2:
+        raise ValueError("Output buffer wasn't two dimensional.")
+    if tuple(out.shape) != tuple(shape):
+        raise ValueError(f"Expected output buffer to have shape=({shape[0]}, {shape[1]}) but its shape is "
+                         f"({out.shape[0]}, {out.shape[1]}).")
+    if out.flags.c_contiguous or (out.shape[1] <= 1 and out.strides[0] > 0):
+        return out, None
+    return np.empty(shape, dtype=dtype), out
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class CompiledDetectorSampler(_SamplerBase):
+    """Samples detection events and observable flips (replaces CompiledDetectorSampler + FrameSimulator)."""
+
+    _mode = _native.MODE_DETECTIONS
+
+    def __init__(self, circuit, *, seed=None, device: int = 0):
+        super().__init__(circuit, seed, device)
+
+    def sample(self, shots: int, *, prepend_observables: bool = False, append_observables: bool = False,
+               separate_observables: bool = False, bit_packed: bool = False, dets_out=None, obs_out=None):
+        if separate_observables and (append_observables or prepend_observables):
+            raise ValueError("Can't specify separate_observables=True with append_observables=True or "
+                             "prepend_observables=True")
+        shots = int(shots)
+        if shots < 0:
+            raise ValueError("shots must be non-negative")
+        c = self._circuit
+        D, O = c.num_detectors, c.num_observables
+        nd = D + (O if prepend_observables else 0) + (O if append_observables else 0)
+        width = (lambda n: (n + 7) // 8) if bit_packed else (lambda n: n)
+        dets, dets_user = _out_array(dets_out, (shots, width(nd)), bit_packed)
+        want_obs = separate_observables or obs_out is not None
+        obs = obs_user = None
+        if want_obs:
+            obs, obs_user = _out_array(obs_out, (shots, width(O)), bit_packed)
+        flags = ((_native.PREPEND_OBSERVABLES if prepend_observables else 0)
+                 | (_native.APPEND_OBSERVABLES if append_observables else 0)
+                 | (_native.BIT_PACKED if bit_packed else 0))
+        if shots:
+            check(lib().gfs_sample_detections(
+                self._h, shots, flags, _ptr(dets), dets.strides[0] if dets.size else max(1, dets.shape[1]),
+                _ptr(obs) if obs is not None else None,
+                (obs.strides[0] if obs.size else max(1, obs.shape[1])) if obs is not None else 0))
+        if dets_user is not None:
+            dets_user[...] = dets
+            dets = dets_user
+        if obs_user is not None:
+            obs_user[...] = obs
+            obs = obs_user
+        if separate_observables:
+            return dets, obs
+        return dets
+
+
+class CompiledMeasurementSampler(_SamplerBase):
+    """Samples measurement results = reference sample XOR frame flips (replaces CompiledMeasurementSampler)."""
+
+    _mode = _native.MODE_MEASUREMENTS
+
+    def __init__(self, circuit, *, skip_reference_sample: bool = False, seed=None, reference_sample=None,
+                 device: int = 0):
+        super().__init__(circuit, seed, device)
+        M = self._circuit.num_measurements
+        if reference_sample is not None:
+            if skip_reference_sample:
+                raise ValueError("skip_reference_sample = True but reference_sample is not None.")
+            ref = np.asarray(reference_sample)
+            if ref.dtype == np.bool_:
+                if ref.shape != (M,):
+                    raise ValueError("reference_sample has the wrong number of bits")
+                ref = np.packbits(ref, bitorder="little")
+            elif ref.dtype == np.uint8:
+                if ref.shape != ((M + 7) // 8,):
+                    raise ValueError("reference_sample has the wrong number of bytes")
+            else:
+                raise ValueError("reference_sample must be a numpy bool or uint8 array")
+            self._ref = np.ascontiguousarray(ref, dtype=np.uint8)
+        elif skip_reference_sample:
+            self._ref = None
+        else:
+            raise NotImplementedError(
+                "computing the reference sample on the host is not available yet; pass reference_sample= "
+                "(e.g. stim.Circuit(text).reference_sample()) or skip_reference_sample=True")
+
+    def sample(self, shots: int, *, bit_packed: bool = False):
+        shots = int(shots)
+        M = self._circuit.num_measurements
+        out = np.empty((shots, (M + 7) // 8 if bit_packed else M), dtype=np.uint8 if bit_packed else np.bool_)
+        if shots:
+            check(lib().gfs_sample_measurements(
+                self._h, shots, _native.BIT_PACKED if bit_packed else 0,
+                _ptr(self._ref) if self._ref is not None else None, _ptr(out),
+                out.strides[0] if out.size else max(1, out.shape[1])))
+        return out

@@ -1,0 +1,103 @@
+"""ctypes binding of libstim_gb300.so (include/stim_gb300.h).
+
+The product path has exactly one implementation: the CUDA library.  If it cannot be built or loaded,
+or there is no CUDA device, calls raise; there is no CPU fallback.
+"""
+
+import ctypes
+import os
+import threading
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_lock = threading.Lock()
+_lib = None
+
+GFS_OK = 0
+GFS_ERR_INVALID_ARGUMENT = 1
+GFS_ERR_OUT_OF_RANGE = 2
+GFS_ERR_CUDA = 3
+GFS_ERR_OUT_OF_MEMORY = 4
+GFS_ERR_INTERNAL = 5
+
+MODE_DETECTIONS = 0
+MODE_MEASUREMENTS = 1
+
+PREPEND_OBSERVABLES = 1
+APPEND_OBSERVABLES = 2
+BIT_PACKED = 4
+
+_vp = ctypes.c_void_p
+_u64 = ctypes.c_uint64
+
+
+def _declare(L):
+    L.gfs_last_error.restype = ctypes.c_char_p
+    L.gfs_last_error.argtypes = []
+    sigs = {
+        "gfs_device_count": [ctypes.POINTER(ctypes.c_int)],
+        "gfs_circuit_parse": [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(_vp)],
+        "gfs_circuit_stats": [_vp, ctypes.POINTER(_u64)],
+        "gfs_sampler_create": [_vp, ctypes.c_uint32, _u64, ctypes.c_int, ctypes.POINTER(_vp)],
+        "gfs_sample_detections": [_vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64],
+        "gfs_sample_detections_device": [_vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64],
+        "gfs_sample_measurements": [_vp, _u64, ctypes.c_uint32, _vp, _vp, _u64],
+        "gfs_sampler_last_timings": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_u64)],
+        "gfs_sampler_set_shape": [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+        "gfs_sampler_get_shape": [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                  ctypes.POINTER(ctypes.c_int), ctypes.POINTER(_u64)],
+        "gfs_sampler_set_chunk_shots": [_vp, _u64],
+        "gfs_measure_smem_peak": [ctypes.c_int, ctypes.POINTER(ctypes.c_double)],
+    }
+    for name, args in sigs.items():
+        f = getattr(L, name)
+        f.restype = ctypes.c_int
+        f.argtypes = args
+    for name in ("gfs_circuit_free", "gfs_sampler_free"):
+        f = getattr(L, name)
+        f.restype = None
+        f.argtypes = [_vp]
+
+
+def library_path() -> str:
+    return os.path.join(_HERE, "_lib", "libstim_gb300.so")
+
+
+def lib():
+    """Loads (building first if needed) the CUDA library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            from . import build as _build
+            path = _build.build()
+            L = ctypes.CDLL(path)
+            _declare(L)
+            _lib = L
+    return _lib
+
+
+def check(status: int):
+    if status == GFS_OK:
+        return
+    msg = lib().gfs_last_error().decode(errors="replace")
+    if status == GFS_ERR_INVALID_ARGUMENT:
+        raise ValueError(msg)
+    if status == GFS_ERR_OUT_OF_RANGE:
+        raise IndexError(msg)
+    if status == GFS_ERR_OUT_OF_MEMORY:
+        raise MemoryError(msg)
+    raise RuntimeError(msg)
+
+
+def measure_smem_peak(device: int = 0) -> float:
+    """Shared-memory load+store bytes/s of the device, from the library's probe kernel."""
+    v = ctypes.c_double(0)
+    check(lib().gfs_measure_smem_peak(int(device), ctypes.byref(v)))
+    return v.value
+
+
+def device_count() -> int:
+    n = ctypes.c_int(0)
+    check(lib().gfs_device_count(ctypes.byref(n)))
+    return n.value

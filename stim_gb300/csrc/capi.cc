@@ -1,0 +1,533 @@
+// C ABI (include/stim_gb300.h) and the host runtime behind it: device copies of the lowered program,
+// chunked launches of the frame and transpose kernels on a per-sampler stream, and error mapping.
+#include "../../include/stim_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+
+#include "circuit.h"
+#include "kernels.h"
+#include "lower.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+struct CudaError : std::runtime_error {
+    cudaError_t code;
+    CudaError(cudaError_t c, const char *what) : std::runtime_error(std::string(what) + ": " + cudaGetErrorString(c)), code(c) {
+    }
+};
+
+void ck(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) {
+        throw CudaError(e, what);
+    }
+}
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t n = 0;
+    int device = -1;
+    void ensure(size_t bytes, int dev) {
+        if (bytes <= n && p) {
+            return;
+        }
+        release();
+        if (bytes == 0) {
+            return;
+        }
+        ck(cudaMalloc(&p, bytes), "cudaMalloc");
+        n = bytes;
+        device = dev;
+    }
+    void release() {
+        if (p) {
+            cudaFree(p);
+        }
+        p = nullptr;
+        n = 0;
+    }
+    ~DevBuf() {
+        release();
+    }
+};
+
+template <typename T>
+void upload(DevBuf &b, const std::vector<T> &v, int dev, cudaStream_t s) {
+    size_t bytes = std::max<size_t>(v.size() * sizeof(T), 16);
+    b.ensure(bytes, dev);
+    if (!v.empty()) {
+        ck(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), "upload");
+    }
+}
+
+gfs_status fail(gfs_status st, const std::string &msg) {
+    g_err = msg;
+    return st;
+}
+
+template <typename F>
+gfs_status guarded(F f) {
+    try {
+        f();
+        return GFS_OK;
+    } catch (const std::out_of_range &e) {
+        return fail(GFS_ERR_OUT_OF_RANGE, e.what());
+    } catch (const std::invalid_argument &e) {
+        return fail(GFS_ERR_INVALID_ARGUMENT, e.what());
+    } catch (const CudaError &e) {
+        return fail(e.code == cudaErrorMemoryAllocation ? GFS_ERR_OUT_OF_MEMORY : GFS_ERR_CUDA, e.what());
+    } catch (const std::bad_alloc &) {
+        return fail(GFS_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (const std::exception &e) {
+        return fail(GFS_ERR_INTERNAL, e.what());
+    }
+}
+
+}  // namespace
+
+struct gfs_circuit {
+    gfs::Circuit circuit;
+    gfs::CircuitStats stats;
+};
+
+struct gfs_sampler {
+    int device = 0;
+    uint32_t mode = 0;
+    uint64_t seed = 0;
+    uint64_t next_block = 0;
+    gfs::Program prog;
+    DevBuf d_ops, d_pool, d_tables, d_chans, d_orig, d_status;
+    DevBuf det_tmp, obs_tmp, meas_tmp, out_tmp, ref_bits;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    gfs::LaunchShape shape{};
+    int num_sms = 0;
+    uint64_t chunk_shots = 0;
+    double t_frame = 0, t_transpose = 0, t_copy = 0, t_total = 0;
+    uint64_t n_frame = 0, n_transpose = 0;
+
+    ~gfs_sampler() {
+        if (stream) {
+            cudaSetDevice(device);
+            cudaStreamSynchronize(stream);
+            for (auto &e : ev) {
+                if (e) {
+                    cudaEventDestroy(e);
+                }
+            }
+            cudaStreamDestroy(stream);
+        }
+    }
+
+    size_t smem_for(int bpc) const {
+        return gfs::frame_smem_bytes(prog.num_rows, prog.ring, (uint32_t)prog.num_observables, bpc);
+    }
+
+    void choose_shape(int bpc, int threads, int grid) {
+        cudaDeviceProp prop;
+        ck(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+        num_sms = prop.multiProcessorCount;
+        size_t smem = smem_for(bpc);
+        if (smem > (size_t)prop.sharedMemPerBlockOptin) {
+            throw std::invalid_argument("circuit state (" + std::to_string(smem) +
+                                        " bytes) does not fit in shared memory with " + std::to_string(bpc) +
+                                        " blocks per CTA");
+        }
+        if (threads <= 0 || threads > 256 || threads % 32) {
+            throw std::invalid_argument("threads per CTA must be a multiple of 32 in [32, 256]");
+        }
+        gfs::LaunchShape s{bpc, threads, 1, smem};
+        int per_sm = 0;
+        ck(gfs::frame_kernel_max_ctas_per_sm(s, &per_sm), "occupancy");
+        if (per_sm < 1) {
+            throw std::invalid_argument("frame kernel cannot be resident with this launch shape");
+        }
+        s.grid = grid > 0 ? grid : per_sm * num_sms;
+        shape = s;
+    }
+
+    void init(const gfs_circuit *c, uint32_t m, uint64_t sd, int dev) {
+        device = dev;
+        mode = m;
+        seed = sd;
+        prog = gfs::lower(c->circuit, m == GFS_MODE_MEASUREMENTS ? gfs::SampleMode::MEASUREMENTS
+                                                               : gfs::SampleMode::DETECTIONS);
+        int count = 0;
+        ck(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
+        if (dev < 0 || dev >= count) {
+            throw std::invalid_argument("no CUDA device " + std::to_string(dev));
+        }
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (auto &e : ev) {
+            ck(cudaEventCreate(&e), "cudaEventCreate");
+        }
+        upload(d_ops, prog.ops, device, stream);
+        upload(d_pool, prog.pool, device, stream);
+        upload(d_tables, prog.tables, device, stream);
+        upload(d_chans, prog.chans, device, stream);
+        upload(d_orig, prog.qubit_orig, device, stream);
+        d_status.ensure(16, device);
+        ck(cudaMemsetAsync(d_status.p, 0, 16, stream), "memset");
+        int bpc = 1;
+        choose_shape(bpc, 256, 0);
+        ck(cudaStreamSynchronize(stream), "upload sync");
+    }
+
+    uint64_t per_block_bytes(uint64_t out_row_bytes) const {
+        uint64_t rows = prog.num_detectors + prog.num_observables + (mode == GFS_MODE_MEASUREMENTS ? prog.num_measurements : 0);
+        return rows * 16 + 128 * out_row_bytes;
+    }
+
+    uint64_t chunk_blocks(uint64_t out_row_bytes) const {
+        uint64_t bpc = (uint64_t)shape.blocks_per_cta;
+        if (chunk_shots) {
+            uint64_t b = std::max<uint64_t>(1, chunk_shots / 128);
+            return ((b + bpc - 1) / bpc) * bpc;
+        }
+        uint64_t budget = (uint64_t)3 << 30;
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+            budget = std::min<uint64_t>(budget, free_b / 3);
+        }
+        uint64_t b = std::max<uint64_t>(1, budget / std::max<uint64_t>(1, per_block_bytes(out_row_bytes)));
+        uint64_t wave = (uint64_t)shape.grid * bpc;
+        if (b > wave) {
+            b = (b / wave) * wave;
+        }
+        return std::max<uint64_t>(bpc, (b / bpc) * bpc);
+    }
+
+    void reset_timings() {
+        t_frame = t_transpose = t_copy = t_total = 0;
+        n_frame = n_transpose = 0;
+    }
+
+    float elapsed(int a, int b) {
+        float ms = 0;
+        ck(cudaEventElapsedTime(&ms, ev[a], ev[b]), "cudaEventElapsedTime");
+        return ms;
+    }
+
+    // Runs the frame kernel for nblk blocks starting at stream block `block0`; results land in the tmp buffers.
+    void run_frame(uint64_t nblk, uint64_t block0) {
+        uint64_t bpc = (uint64_t)shape.blocks_per_cta;
+        uint64_t nslices = (nblk + bpc - 1) / bpc;
+        uint64_t alloc_blocks = nslices * bpc;
+        det_tmp.ensure(std::max<uint64_t>(16, alloc_blocks * prog.num_detectors * 16), device);
+        obs_tmp.ensure(std::max<uint64_t>(16, alloc_blocks * prog.num_observables * 16), device);
+        if (mode == GFS_MODE_MEASUREMENTS) {
+            meas_tmp.ensure(std::max<uint64_t>(16, alloc_blocks * prog.num_measurements * 16), device);
+        }
+        gfs::KernelArgs a{};
+        a.ops = (const gfs::DevOp *)d_ops.p;
+        a.pool = (const uint32_t *)d_pool.p;
+        a.tables = (const uint32_t *)d_tables.p;
+        a.chans = (const gfs::DevChan *)d_chans.p;
+        a.qubit_orig = (const uint32_t *)d_orig.p;
+        a.nrows = prog.num_rows;
+        a.ring = prog.ring;
+        a.nobs = (uint32_t)prog.num_observables;
+        a.nslices = (uint32_t)nslices;
+        a.ndet = prog.num_detectors;
+        a.nmeas = prog.num_measurements;
+        a.seed = seed;
+        a.block0 = block0;
+        a.det_out = (uint4 *)det_tmp.p;
+        a.obs_out = (uint4 *)obs_tmp.p;
+        a.meas_out = (uint4 *)meas_tmp.p;
+        a.status = (uint32_t *)d_status.p;
+        gfs::LaunchShape s = shape;
+        s.grid = (int)std::min<uint64_t>((uint64_t)shape.grid, nslices);
+        ck(gfs::launch_frame_kernel(a, s, stream), "frame kernel launch");
+        n_frame++;
+    }
+
+    void transpose(const uint4 *s0, uint64_t n0, const uint4 *s1, uint64_t n1, const uint4 *s2, uint64_t n2,
+                   const uint8_t *xr, uint64_t nshots, uint8_t *out, uint64_t stride, bool packed) {
+        gfs::TransposeArgs t{};
+        t.src0 = s0;
+        t.n0 = n0;
+        t.src1 = s1;
+        t.n1 = n1;
+        t.src2 = s2;
+        t.n2 = n2;
+        t.xor_rows = xr;
+        t.nshots = nshots;
+        t.out = out;
+        t.out_stride = stride;
+        t.bit_packed = packed ? 1 : 0;
+        ck(gfs::launch_transpose(t, stream), "transpose launch");
+        n_transpose++;
+    }
+
+    void check_status() {
+        uint32_t st = 0;
+        ck(cudaMemcpy(&st, d_status.p, 4, cudaMemcpyDeviceToHost), "status read");
+        if (st) {
+            cudaMemset(d_status.p, 0, 4);
+            throw std::runtime_error("frame kernel reported error status " + std::to_string(st));
+        }
+    }
+
+    // Shared driver for detections (host or device destinations).
+    void detections(uint64_t shots, uint32_t flags, uint8_t *dets, uint64_t dstride, uint8_t *obs, uint64_t ostride,
+                    bool device_out) {
+        bool packed = flags & GFS_BIT_PACKED;
+        uint64_t D = prog.num_detectors, O = prog.num_observables;
+        uint64_t nd = D + ((flags & GFS_PREPEND_OBSERVABLES) ? O : 0) + ((flags & GFS_APPEND_OBSERVABLES) ? O : 0);
+        uint64_t drow = packed ? (nd + 7) / 8 : nd;
+        uint64_t orow = packed ? (O + 7) / 8 : O;
+        if (dets && dstride < drow) {
+            throw std::invalid_argument("dets row stride too small");
+        }
+        if (obs && ostride < orow) {
+            throw std::invalid_argument("obs row stride too small");
+        }
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        reset_timings();
+        ck(cudaEventRecord(ev[0], stream), "event");
+        uint64_t cb = chunk_blocks(drow + orow);
+        uint64_t done = 0;
+        while (done < shots) {
+            uint64_t cs = std::min<uint64_t>(shots - done, cb * 128);
+            uint64_t nblk = (cs + 127) / 128;
+            ck(cudaEventRecord(ev[1], stream), "event");
+            run_frame(nblk, next_block);
+            ck(cudaEventRecord(ev[2], stream), "event");
+            const uint4 *dt = (const uint4 *)det_tmp.p, *ot = (const uint4 *)obs_tmp.p;
+            uint8_t *dd = nullptr, *od = nullptr;
+            if (device_out) {
+                dd = dets ? dets + done * dstride : nullptr;
+                od = obs ? obs + done * ostride : nullptr;
+            } else {
+                out_tmp.ensure(std::max<uint64_t>(16, cs * (drow + orow)), device);
+                dd = (uint8_t *)out_tmp.p;
+                od = (uint8_t *)out_tmp.p + cs * drow;
+            }
+            uint64_t ds = device_out ? dstride : drow, os = device_out ? ostride : orow;
+            if (dets) {
+                if ((flags & GFS_PREPEND_OBSERVABLES) && (flags & GFS_APPEND_OBSERVABLES)) {
+                    transpose(ot, O, dt, D, ot, O, nullptr, cs, dd, ds, packed);
+                } else if (flags & GFS_PREPEND_OBSERVABLES) {
+                    transpose(ot, O, dt, D, nullptr, 0, nullptr, cs, dd, ds, packed);
+                } else if (flags & GFS_APPEND_OBSERVABLES) {
+                    transpose(dt, D, ot, O, nullptr, 0, nullptr, cs, dd, ds, packed);
+                } else {
+                    transpose(dt, D, nullptr, 0, nullptr, 0, nullptr, cs, dd, ds, packed);
+                }
+            }
+            if (obs) {
+                transpose(ot, O, nullptr, 0, nullptr, 0, nullptr, cs, od, os, packed);
+            }
+            ck(cudaEventRecord(ev[3], stream), "event");
+            if (!device_out) {
+                if (dets && drow) {
+                    ck(cudaMemcpy2DAsync(dets + done * dstride, dstride, dd, drow, drow, cs, cudaMemcpyDeviceToHost,
+                                         stream),
+                       "copy dets");
+                }
+                if (obs && orow) {
+                    ck(cudaMemcpy2DAsync(obs + done * ostride, ostride, od, orow, orow, cs, cudaMemcpyDeviceToHost,
+                                         stream),
+                       "copy obs");
+                }
+            }
+            ck(cudaStreamSynchronize(stream), "sample");
+            t_frame += elapsed(1, 2);
+            t_transpose += elapsed(2, 3);
+            check_status();
+            next_block += nblk;
+            done += cs;
+        }
+        ck(cudaEventRecord(ev[1], stream), "event");
+        ck(cudaStreamSynchronize(stream), "sample");
+        t_total = elapsed(0, 1);
+        t_copy = std::max(0.0, t_total - t_frame - t_transpose);
+    }
+
+    void measurements(uint64_t shots, uint32_t flags, const uint8_t *ref, uint8_t *out, uint64_t stride) {
+        if (mode != GFS_MODE_MEASUREMENTS) {
+            throw std::invalid_argument("sampler was not created in measurement mode");
+        }
+        bool packed = flags & GFS_BIT_PACKED;
+        uint64_t M = prog.num_measurements;
+        uint64_t row = packed ? (M + 7) / 8 : M;
+        if (stride < row) {
+            throw std::invalid_argument("output row stride too small");
+        }
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        reset_timings();
+        const uint8_t *dref = nullptr;
+        if (ref && M) {
+            ref_bits.ensure((M + 7) / 8, device);
+            ck(cudaMemcpyAsync(ref_bits.p, ref, (M + 7) / 8, cudaMemcpyHostToDevice, stream), "ref upload");
+            dref = (const uint8_t *)ref_bits.p;
+        }
+        ck(cudaEventRecord(ev[0], stream), "event");
+        uint64_t cb = chunk_blocks(row);
+        uint64_t done = 0;
+        while (done < shots) {
+            uint64_t cs = std::min<uint64_t>(shots - done, cb * 128);
+            uint64_t nblk = (cs + 127) / 128;
+            ck(cudaEventRecord(ev[1], stream), "event");
+            run_frame(nblk, next_block);
+            ck(cudaEventRecord(ev[2], stream), "event");
+            out_tmp.ensure(std::max<uint64_t>(16, cs * row), device);
+            transpose((const uint4 *)meas_tmp.p, M, nullptr, 0, nullptr, 0, dref, cs, (uint8_t *)out_tmp.p, row, packed);
+            ck(cudaEventRecord(ev[3], stream), "event");
+            if (row) {
+                ck(cudaMemcpy2DAsync(out + done * stride, stride, out_tmp.p, row, row, cs, cudaMemcpyDeviceToHost, stream),
+                   "copy meas");
+            }
+            ck(cudaStreamSynchronize(stream), "sample");
+            t_frame += elapsed(1, 2);
+            t_transpose += elapsed(2, 3);
+            check_status();
+            next_block += nblk;
+            done += cs;
+        }
+        ck(cudaEventRecord(ev[1], stream), "event");
+        ck(cudaStreamSynchronize(stream), "sample");
+        t_total = elapsed(0, 1);
+        t_copy = std::max(0.0, t_total - t_frame - t_transpose);
+    }
+};
+
+extern "C" {
+
+const char *gfs_last_error(void) {
+    return g_err.c_str();
+}
+
+gfs_status gfs_device_count(int *out) {
+    return guarded([&] {
+        int n = 0;
+        cudaError_t e = cudaGetDeviceCount(&n);
+        if (e != cudaSuccess) {
+            n = 0;
+            cudaGetLastError();
+        }
+        *out = n;
+    });
+}
+
+gfs_status gfs_circuit_parse(const char *text, size_t len, gfs_circuit **out) {
+    *out = nullptr;
+    return guarded([&] {
+        auto c = std::make_unique<gfs_circuit>();
+        c->circuit = gfs::Circuit::parse(std::string_view(text, len));
+        c->stats = c->circuit.stats();
+        *out = c.release();
+    });
+}
+
+gfs_status gfs_circuit_stats(const gfs_circuit *c, uint64_t *s) {
+    return guarded([&] {
+        s[0] = c->stats.num_qubits;
+        s[1] = c->stats.num_measurements;
+        s[2] = c->stats.num_detectors;
+        s[3] = c->stats.num_observables;
+        s[4] = c->stats.max_lookback;
+        s[5] = c->stats.num_instances;
+    });
+}
+
+void gfs_circuit_free(gfs_circuit *c) {
+    delete c;
+}
+
+gfs_status gfs_sampler_create(const gfs_circuit *c, uint32_t mode, uint64_t seed, int device, gfs_sampler **out) {
+    *out = nullptr;
+    return guarded([&] {
+        if (mode != GFS_MODE_DETECTIONS && mode != GFS_MODE_MEASUREMENTS) {
+            throw std::invalid_argument("unknown sampling mode");
+        }
+        auto s = std::make_unique<gfs_sampler>();
+        s->init(c, mode, seed, device);
+        *out = s.release();
+    });
+}
+
+void gfs_sampler_free(gfs_sampler *s) {
+    delete s;
+}
+
+gfs_status gfs_sample_detections(gfs_sampler *s, uint64_t shots, uint32_t flags, uint8_t *dets, uint64_t dets_stride,
+                                 uint8_t *obs, uint64_t obs_stride) {
+    return guarded([&] {
+        if (s->mode != GFS_MODE_DETECTIONS) {
+            throw std::invalid_argument("sampler was not created in detection mode");
+        }
+        s->detections(shots, flags, dets, dets_stride, obs, obs_stride, false);
+    });
+}
+
+gfs_status gfs_sample_detections_device(gfs_sampler *s, uint64_t shots, uint32_t flags, void *dets,
+                                        uint64_t dets_stride, void *obs, uint64_t obs_stride) {
+    return guarded([&] {
+        if (s->mode != GFS_MODE_DETECTIONS) {
+            throw std::invalid_argument("sampler was not created in detection mode");
+        }
+        s->detections(shots, flags, (uint8_t *)dets, dets_stride, (uint8_t *)obs, obs_stride, true);
+    });
+}
+
+gfs_status gfs_sample_measurements(gfs_sampler *s, uint64_t shots, uint32_t flags, const uint8_t *ref_sample,
+                                   uint8_t *out, uint64_t out_stride) {
+    return guarded([&] { s->measurements(shots, flags, ref_sample, out, out_stride); });
+}
+
+gfs_status gfs_sampler_last_timings(const gfs_sampler *s, double *out4, uint64_t *counts2) {
+    return guarded([&] {
+        out4[0] = s->t_frame;
+        out4[1] = s->t_transpose;
+        out4[2] = s->t_copy;
+        out4[3] = s->t_total;
+        if (counts2) {
+            counts2[0] = s->n_frame;
+            counts2[1] = s->n_transpose;
+        }
+    });
+}
+
+gfs_status gfs_sampler_set_shape(gfs_sampler *s, int blocks_per_cta, int threads, int grid) {
+    return guarded([&] {
+        if (blocks_per_cta != 1 && blocks_per_cta != 2 && blocks_per_cta != 4) {
+            throw std::invalid_argument("blocks_per_cta must be 1, 2 or 4");
+        }
+        ck(cudaSetDevice(s->device), "cudaSetDevice");
+        s->choose_shape(blocks_per_cta, threads, grid);
+    });
+}
+
+gfs_status gfs_sampler_get_shape(const gfs_sampler *s, int *blocks_per_cta, int *threads, int *grid,
+                                 uint64_t *smem_bytes) {
+    return guarded([&] {
+        *blocks_per_cta = s->shape.blocks_per_cta;
+        *threads = s->shape.threads;
+        *grid = s->shape.grid;
+        *smem_bytes = s->shape.smem;
+    });
+}
+
+gfs_status gfs_measure_smem_peak(int device, double *bytes_per_s) {
+    return guarded([&] {
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        ck(gfs::measure_smem_peak(bytes_per_s), "shared-memory probe");
+    });
+}
+
+gfs_status gfs_sampler_set_chunk_shots(gfs_sampler *s, uint64_t shots) {
+    return guarded([&] { s->chunk_shots = shots; });
+}
+
+}  // extern "C"

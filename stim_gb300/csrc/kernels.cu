@@ -1,0 +1,743 @@
+// Frame-sampling kernels for sm_103a.
+//
+// frame_kernel: one CTA owns a slice of B x 128 shots at a time (persistent, grid-stride over slices).
+// Its X/Z Pauli frames ([row][block] uint4, 128 shots per uint4), the measurement ring, the observable
+// accumulators and the correlated-error flags live in shared memory for the whole circuit.  The CTA
+// walks the device program (program.h): every op spreads its independent units over the threads,
+// updates 128 shots per unit with 128-bit shared-memory loads/stores and bitwise logic, and ends with
+// one __syncthreads().  Noise is sampled from the counter-based stream of gfs_contract.h: a thread owns
+// a segment of 8 units x 128 shots and skips geometrically to its hits, which it applies with shared
+// atomics.  Detection events stream to global memory as [block][detector] uint4 rows.
+//
+// transpose_kernel: turns [block][row] bit-rows into shot-major bytes with a 32x32 warp-ballot transpose
+// per word, replacing the reference's bit-by-bit numpy conversion (numpy.pybind.cc:20-63) and
+// simd_bit_table::transpose_into (simd_bit_table.inl:192-208).
+#include <cstdio>
+
+#include "gfs_contract.h"
+#include "kernels.h"
+
+namespace gfs {
+
+__device__ __forceinline__ uint4 x4(uint4 a, uint4 b) {
+    return make_uint4(a.x ^ b.x, a.y ^ b.y, a.z ^ b.z, a.w ^ b.w);
+}
+__device__ __forceinline__ uint4 zero4() {
+    return make_uint4(0, 0, 0, 0);
+}
+__device__ __forceinline__ uint4 u4(gfs_u32x4 v) {
+    return make_uint4(v.v[0], v.v[1], v.v[2], v.v[3]);
+}
+__device__ __forceinline__ uint32_t wrap(uint32_t s, uint32_t L) {
+    return s >= L ? s - L : s;
+}
+__device__ __forceinline__ void atomic_xor_bit(uint4 *base, uint32_t idx, uint32_t shot) {
+    atomicXor(reinterpret_cast<uint32_t *>(base + idx) + (shot >> 5), 1u << (shot & 31));
+}
+__device__ __forceinline__ void atomic_or_bit(uint4 *base, uint32_t idx, uint32_t shot) {
+    atomicOr(reinterpret_cast<uint32_t *>(base + idx) + (shot >> 5), 1u << (shot & 31));
+}
+
+// Two-qubit frame rules (frame_simulator.inl:386-630), one 32-bit word at a time.
+__device__ __forceinline__ void rule2(uint32_t sub, uint32_t &x1, uint32_t &z1, uint32_t &x2, uint32_t &z2) {
+    switch (sub) {
+        case K2_CX:
+            z1 ^= z2;
+            x2 ^= x1;
+            break;
+        case K2_CY:
+            z1 ^= x2 ^ z2;
+            z2 ^= x1;
+            x2 ^= x1;
+            break;
+        case K2_CZ:
+            z1 ^= x2;
+            z2 ^= x1;
+            break;
+        case K2_XCX:
+            x1 ^= z2;
+            x2 ^= z1;
+            break;
+        case K2_XCY:
+            x1 ^= x2 ^ z2;
+            x2 ^= z1;
+            z2 ^= z1;
+            break;
+        case K2_YCX:
+            x2 ^= x1 ^ z1;
+            x1 ^= z2;
+            z1 ^= z2;
+            break;
+        case K2_YCY: {
+            uint32_t y1 = x1 ^ z1, y2 = x2 ^ z2;
+            x1 ^= y2;
+            z1 ^= y2;
+            x2 ^= y1;
+            z2 ^= y1;
+            break;
+        }
+        case K2_SWAP: {
+            uint32_t t = x1;
+            x1 = x2;
+            x2 = t;
+            t = z1;
+            z1 = z2;
+            z2 = t;
+            break;
+        }
+        case K2_ISWAP: {
+            uint32_t dx = x1 ^ x2;
+            uint32_t t1 = z1 ^ dx, t2 = z2 ^ dx;
+            z1 = t2;
+            z2 = t1;
+            uint32_t t = x1;
+            x1 = x2;
+            x2 = t;
+            break;
+        }
+        case K2_CXSWAP:
+            z2 ^= z1;
+            z1 ^= z2;
+            x1 ^= x2;
+            x2 ^= x1;
+            break;
+        case K2_CZSWAP: {
+            uint32_t t = x1;
+            x1 = x2;
+            x2 = t;
+            t = z1;
+            z1 = z2;
+            z2 = t;
+            z1 ^= x2;
+            z2 ^= x1;
+            break;
+        }
+        case K2_SWAPCX:
+            z1 ^= z2;
+            z2 ^= z1;
+            x2 ^= x1;
+            x1 ^= x2;
+            break;
+        case K2_SQRT_XX: {
+            uint32_t dz = z1 ^ z2;
+            x1 ^= dz;
+            x2 ^= dz;
+            break;
+        }
+        case K2_SQRT_YY: {
+            uint32_t d = x1 ^ z1 ^ x2 ^ z2;
+            x1 ^= d;
+            z1 ^= d;
+            x2 ^= d;
+            z2 ^= d;
+            break;
+        }
+        case K2_SQRT_ZZ: {
+            uint32_t dx = x1 ^ x2;
+            z1 ^= dx;
+            z2 ^= dx;
+            break;
+        }
+        default:
+            break;
+    }
+}
+
+__device__ __forceinline__ void rule2v(uint32_t sub, uint4 &x1, uint4 &z1, uint4 &x2, uint4 &z2) {
+    rule2(sub, x1.x, z1.x, x2.x, z2.x);
+    rule2(sub, x1.y, z1.y, x2.y, z2.y);
+    rule2(sub, x1.z, z1.z, x2.z, z2.z);
+    rule2(sub, x1.w, z1.w, x2.w, z2.w);
+}
+
+__device__ __forceinline__ void apply_pauli_atomic(uint4 *X, uint4 *Z, uint32_t idx, uint32_t shot, uint32_t v) {
+    if (v == 1 || v == 2) {
+        atomic_xor_bit(X, idx, shot);
+    }
+    if (v == 2 || v == 3) {
+        atomic_xor_bit(Z, idx, shot);
+    }
+}
+
+template <int B>
+__global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
+    extern __shared__ uint4 sm[];
+    const uint32_t nr = p.nrows, L = p.ring, NO = p.nobs;
+    uint4 *X = sm;
+    uint4 *Z = X + (size_t)nr * B;
+    uint4 *R = Z + (size_t)nr * B;
+    uint4 *O = R + (size_t)L * B;
+    uint4 *OCC = O + (size_t)NO * B;
+    uint4 *MSK = OCC + B;
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t *pool = p.pool;
+
+    for (uint32_t slice = blockIdx.x; slice < p.nslices; slice += gridDim.x) {
+        const uint64_t lb0 = (uint64_t)slice * B;
+        const uint64_t gb0 = p.block0 + lb0;
+
+        for (uint32_t i = tid; i < nr * B; i += nt) {
+            uint32_t r = i / B, blk = i % B;
+            X[i] = zero4();
+            Z[i] = u4(gfs_row_bits(p.seed, GFS_P_RESET, 0, __ldg(p.qubit_orig + r), (uint32_t)(gb0 + blk)));
+        }
+        for (uint32_t i = tid; i < NO * B; i += nt) {
+            O[i] = zero4();
+        }
+        for (uint32_t i = tid; i < B; i += nt) {
+            OCC[i] = zero4();
+        }
+        __syncthreads();
+
+        uint32_t rec = 0;
+        uint64_t det_base = 0, meas_base = 0, inst_base = 0;
+        int depth = 0;
+        uint32_t loop_pc[kMaxLoopDepth + 1];
+        uint64_t loop_left[kMaxLoopDepth + 1], loop_base[kMaxLoopDepth + 1], loop_stride[kMaxLoopDepth + 1];
+        uint32_t pc = 0;
+
+        for (;;) {
+            const DevOp op = p.ops[pc];
+            const uint32_t code = op.code & 0xFFu, sub = op.code >> 8;
+            const uint64_t inst = inst_base + op.inst;
+            const uint32_t n = op.n, a = op.a;
+            if (code == OP_END) {
+                break;
+            }
+            if (code == OP_LOOP_BEGIN) {
+                if (depth >= kMaxLoopDepth) {
+                    if (tid == 0) {
+                        atomicOr(p.status, 1u);
+                    }
+                    break;
+                }
+                loop_pc[depth] = pc;
+                loop_left[depth] = (uint64_t)op.a | ((uint64_t)op.b << 32);
+                loop_base[depth] = inst_base;
+                loop_stride[depth] = (uint64_t)op.c | ((uint64_t)op.d << 32);
+                depth++;
+                inst_base = inst;
+                pc++;
+                continue;
+            }
+            if (code == OP_LOOP_END) {
+                int d = depth - 1;
+                if (--loop_left[d] > 0) {
+                    inst_base += loop_stride[d];
+                    pc = loop_pc[d] + 1;
+                } else {
+                    inst_base = loop_base[d];
+                    depth = d;
+                    pc++;
+                }
+                continue;
+            }
+
+            switch (code) {
+                case OP_1Q:
+                    for (uint32_t i = tid; i < n * B; i += nt) {
+                        uint32_t u = i / B, blk = i % B;
+                        uint32_t idx = __ldg(pool + a + u) * B + blk;
+                        uint4 x = X[idx], z = Z[idx];
+                        switch (sub) {
+                            case K1_H_XZ:
+                                X[idx] = z;
+                                Z[idx] = x;
+                                break;
+                            case K1_H_XY:
+                                Z[idx] = x4(z, x);
+                                break;
+                            case K1_H_YZ:
+                                X[idx] = x4(x, z);
+                                break;
+                            case K1_C_XYZ:
+                                x = x4(x, z);
+                                X[idx] = x;
+                                Z[idx] = x4(z, x);
+                                break;
+                            default:  // K1_C_ZYX
+                                z = x4(z, x);
+                                Z[idx] = z;
+                                X[idx] = x4(x, z);
+                                break;
+                        }
+                    }
+                    break;
+
+                case OP_2Q:
+                    for (uint32_t i = tid; i < n * B; i += nt) {
+                        uint32_t u = i / B, blk = i % B;
+                        uint32_t i1 = __ldg(pool + a + 2 * u) * B + blk;
+                        uint32_t i2 = __ldg(pool + a + 2 * u + 1) * B + blk;
+                        if (sub == K2_CX) {
+                            uint4 z1 = Z[i1], z2 = Z[i2], x1 = X[i1], x2 = X[i2];
+                            Z[i1] = x4(z1, z2);
+                            X[i2] = x4(x2, x1);
+                        } else if (sub == K2_CZ) {
+                            uint4 z1 = Z[i1], z2 = Z[i2], x1 = X[i1], x2 = X[i2];
+                            Z[i1] = x4(z1, x2);
+                            Z[i2] = x4(z2, x1);
+                        } else {
+                            uint4 x1 = X[i1], z1 = Z[i1], x2 = X[i2], z2 = Z[i2];
+                            rule2v(sub, x1, z1, x2, z2);
+                            X[i1] = x1;
+                            Z[i1] = z1;
+                            X[i2] = x2;
+                            Z[i2] = z2;
+                        }
+                    }
+                    break;
+
+                case OP_FEEDBACK:
+                    for (uint32_t i = tid; i < n * B; i += nt) {
+                        uint32_t u = i / B, blk = i % B;
+                        uint32_t k = __ldg(pool + a + 2 * u);
+                        uint32_t rm = __ldg(pool + a + 2 * u + 1);
+                        uint32_t idx = (rm & kRowMask) * B + blk;
+                        uint4 v = R[wrap(rec + L - k, L) * B + blk];
+                        if ((rm >> 24) & kFeedbackX) {
+                            X[idx] = x4(X[idx], v);
+                        }
+                        if ((rm >> 24) & kFeedbackZ) {
+                            Z[idx] = x4(Z[idx], v);
+                        }
+                    }
+                    break;
+
+                case OP_MEASURE:
+                    for (uint32_t i = tid; i < n * B; i += nt) {
+                        uint32_t u = i / B, blk = i % B;
+                        uint32_t idx = __ldg(pool + a + u) * B + blk;
+                        uint32_t slot = wrap(rec + u, L) * B + blk;
+                        uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, op.b + u, (uint32_t)(gb0 + blk)));
+                        uint4 x = X[idx], z = Z[idx];
+                        switch (sub) {
+                            case KM_M:
+                                R[slot] = x;
+                                Z[idx] = r;
+                                break;
+                            case KM_MX:
+                                R[slot] = z;
+                                X[idx] = r;
+                                break;
+                            case KM_MY:
+                                R[slot] = x4(x, z);
+                                X[idx] = x4(x4(x, z), r);
+                                Z[idx] = r;
+                                break;
+                            case KM_MR:
+                                R[slot] = x;
+                                X[idx] = zero4();
+                                Z[idx] = r;
+                                break;
+                            case KM_MRX:
+                                R[slot] = z;
+                                Z[idx] = zero4();
+                                X[idx] = r;
+                                break;
+                            default:  // KM_MRY
+                                R[slot] = x4(x, z);
+                                Z[idx] = r;
+                                X[idx] = r;
+                                break;
+                        }
+                    }
+                    rec = wrap(rec + n, L);
+                    break;
+
+                case OP_RESET:
+                    for (uint32_t i = tid; i < n * B; i += nt) {
+                        uint32_t u = i / B, blk = i % B;
+                        uint32_t idx = __ldg(pool + a + u) * B + blk;
+                        uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, op.b + u, (uint32_t)(gb0 + blk)));
+                        if (sub == KR_R) {
+                            X[idx] = zero4();
+                            Z[idx] = r;
+                        } else if (sub == KR_RX) {
+                            X[idx] = r;
+                            Z[idx] = zero4();
+                        } else {
+                            X[idx] = r;
+                            Z[idx] = r;
+                        }
+                    }
+                    break;
+
+                case OP_RECORD_ZERO:
+                    for (uint32_t i = tid; i < n * B; i += nt) {
+                        uint32_t u = i / B, blk = i % B;
+                        R[wrap(rec + u, L) * B + blk] = zero4();
+                    }
+                    rec = wrap(rec + n, L);
+                    break;
+
+                case OP_MNOISE:
+                case OP_NOISE:
+                case OP_HERALD: {
+                    const DevChan &ch = p.chans[op.b];
+                    const uint32_t *T = p.tables + ch.table;
+                    const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
+                    const uint32_t purpose = code == OP_MNOISE ? GFS_P_MNOISE : GFS_P_NOISE;
+                    for (uint32_t i = tid; i < nseg * B; i += nt) {
+                        uint32_t g = i / B, blk = i % B;
+                        uint32_t u0 = g * GFS_SEG_UNITS;
+                        uint32_t nu = min(GFS_SEG_UNITS, n - u0);
+                        int32_t trials = (int32_t)(nu * GFS_BLOCK_SHOTS);
+                        gfs_stream st;
+                        gfs_stream_init(&st, p.seed, purpose, inst, g, (uint32_t)(gb0 + blk));
+                        int32_t pos = -1;
+                        while ((pos = gfs_next_hit(&st, T, ch.inv_c, pos, trials, ch.always)) >= 0) {
+                            uint32_t u = u0 + (uint32_t)pos / GFS_BLOCK_SHOTS;
+                            uint32_t shot = (uint32_t)pos % GFS_BLOCK_SHOTS;
+                            if (code == OP_MNOISE) {
+                                atomic_xor_bit(R, wrap(rec + L - n + u, L) * B + blk, shot);
+                            } else if (code == OP_HERALD) {
+                                uint32_t c = gfs_stream_next(&st);
+                                uint32_t idx = __ldg(pool + a + u) * B + blk;
+                                atomic_or_bit(R, wrap(rec + L - n + u, L) * B + blk, shot);
+                                if (sub == 0) {
+                                    if (c & 1) {
+                                        atomic_xor_bit(X, idx, shot);
+                                    }
+                                    if (c & 2) {
+                                        atomic_xor_bit(Z, idx, shot);
+                                    }
+                                } else {
+                                    apply_pauli_atomic(X, Z, idx, shot, gfs_choice_weighted(c, ch.cum, 4));
+                                }
+                            } else {
+                                switch (sub) {
+                                    case KN_X:
+                                        atomic_xor_bit(X, __ldg(pool + a + u) * B + blk, shot);
+                                        break;
+                                    case KN_Y: {
+                                        uint32_t idx = __ldg(pool + a + u) * B + blk;
+                                        atomic_xor_bit(X, idx, shot);
+                                        atomic_xor_bit(Z, idx, shot);
+                                        break;
+                                    }
+                                    case KN_Z:
+                                        atomic_xor_bit(Z, __ldg(pool + a + u) * B + blk, shot);
+                                        break;
+                                    case KN_DEP1: {
+                                        uint32_t v = 1 + gfs_choice_uniform(gfs_stream_next(&st), 3);
+                                        apply_pauli_atomic(X, Z, __ldg(pool + a + u) * B + blk, shot,
+                                                           v == 1 ? 1 : (v == 2 ? 3 : 2));
+                                        break;
+                                    }
+                                    case KN_PC1: {
+                                        uint32_t v = 1 + gfs_choice_weighted(gfs_stream_next(&st), ch.cum, 3);
+                                        apply_pauli_atomic(X, Z, __ldg(pool + a + u) * B + blk, shot, v);
+                                        break;
+                                    }
+                                    case KN_DEP2: {
+                                        uint32_t v = 1 + gfs_choice_uniform(gfs_stream_next(&st), 15);
+                                        uint32_t i1 = __ldg(pool + a + 2 * u) * B + blk;
+                                        uint32_t i2 = __ldg(pool + a + 2 * u + 1) * B + blk;
+                                        if (v & 1) atomic_xor_bit(X, i1, shot);
+                                        if (v & 2) atomic_xor_bit(Z, i1, shot);
+                                        if (v & 4) atomic_xor_bit(X, i2, shot);
+                                        if (v & 8) atomic_xor_bit(Z, i2, shot);
+                                        break;
+                                    }
+                                    default: {  // KN_PC2
+                                        uint32_t v = 1 + gfs_choice_weighted(gfs_stream_next(&st), ch.cum, 15);
+                                        uint32_t i1 = __ldg(pool + a + 2 * u) * B + blk;
+                                        uint32_t i2 = __ldg(pool + a + 2 * u + 1) * B + blk;
+                                        apply_pauli_atomic(X, Z, i1, shot, v >> 2);
+                                        apply_pauli_atomic(X, Z, i2, shot, v & 3);
+                                        break;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                    break;
+                }
+
+                case OP_CORR_MASK: {
+                    const DevChan &ch = p.chans[op.b];
+                    for (uint32_t blk = tid; blk < (uint32_t)B; blk += nt) {
+                        uint32_t m[4] = {0, 0, 0, 0};
+                        if (ch.active) {
+                            gfs_stream st;
+                            gfs_stream_init(&st, p.seed, GFS_P_NOISE, inst, 0, (uint32_t)(gb0 + blk));
+                            int32_t pos = -1;
+                            while ((pos = gfs_next_hit(&st, p.tables + ch.table, ch.inv_c, pos,
+                                                       (int32_t)GFS_BLOCK_SHOTS, ch.always)) >= 0) {
+                                m[pos >> 5] |= 1u << (pos & 31);
+                            }
+                        }
+                        uint4 occ = sub == 0 ? zero4() : OCC[blk];
+                        uint4 mk = make_uint4(m[0] & ~occ.x, m[1] & ~occ.y, m[2] & ~occ.z, m[3] & ~occ.w);
+                        OCC[blk] = make_uint4(occ.x | mk.x, occ.y | mk.y, occ.z | mk.z, occ.w | mk.w);
+                        MSK[blk] = mk;
+                    }
+                    break;
+                }
+
+                case OP_CORR_APPLY:
+                    for (uint32_t i = tid; i < n * B; i += nt) {
+                        uint32_t u = i / B, blk = i % B;
+                        uint32_t rm = __ldg(pool + a + u);
+                        uint32_t idx = (rm & kRowMask) * B + blk;
+                        uint4 mk = MSK[blk];
+                        if ((rm >> 24) & 1) {
+                            X[idx] = x4(X[idx], mk);
+                        }
+                        if ((rm >> 24) & 2) {
+                            Z[idx] = x4(Z[idx], mk);
+                        }
+                    }
+                    break;
+
+                case OP_DETECTORS:
+                    for (uint32_t i = tid; i < n * B; i += nt) {
+                        uint32_t u = i / B, blk = i % B;
+                        uint32_t s = __ldg(pool + a + u), e = __ldg(pool + a + u + 1);
+                        uint4 acc = zero4();
+                        for (uint32_t j = s; j < e; j++) {
+                            uint32_t k = __ldg(pool + j);
+                            acc = x4(acc, R[wrap(rec + L - k, L) * B + blk]);
+                        }
+                        p.det_out[(lb0 + blk) * p.ndet + det_base + u] = acc;
+                    }
+                    det_base += n;
+                    break;
+
+                case OP_OBS:
+                    for (uint32_t i = tid; i < n * B; i += nt) {
+                        uint32_t u = i / B, blk = i % B;
+                        uint32_t t = __ldg(pool + a + u);
+                        uint4 v;
+                        if (t & kTermRecord) {
+                            v = R[wrap(rec + L - (t & kRowMask), L) * B + blk];
+                        } else {
+                            uint32_t idx = (t & kRowMask) * B + blk;
+                            v = zero4();
+                            if (t & kTermX) {
+                                v = x4(v, Z[idx]);
+                            }
+                            if (t & kTermZ) {
+                                v = x4(v, X[idx]);
+                            }
+                        }
+                        uint32_t *o = reinterpret_cast<uint32_t *>(O + (size_t)op.b * B + blk);
+                        if (v.x) atomicXor(o + 0, v.x);
+                        if (v.y) atomicXor(o + 1, v.y);
+                        if (v.z) atomicXor(o + 2, v.z);
+                        if (v.w) atomicXor(o + 3, v.w);
+                    }
+                    break;
+
+                case OP_EMIT:
+                    for (uint32_t i = tid; i < n * B; i += nt) {
+                        uint32_t u = i / B, blk = i % B;
+                        p.meas_out[(lb0 + blk) * p.nmeas + meas_base + u] = R[wrap(rec + L - n + u, L) * B + blk];
+                    }
+                    meas_base += n;
+                    break;
+
+                default:
+                    if (tid == 0) {
+                        atomicOr(p.status, 2u);
+                    }
+                    break;
+            }
+            __syncthreads();
+            pc++;
+        }
+
+        for (uint32_t i = tid; i < NO * B; i += nt) {
+            uint32_t k = i / B, blk = i % B;
+            p.obs_out[(lb0 + blk) * NO + k] = O[i];
+        }
+        __syncthreads();
+    }
+}
+
+size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta) {
+    return ((size_t)2 * nrows + ring + nobs + 2) * (size_t)blocks_per_cta * sizeof(uint4);
+}
+
+template <int B>
+static cudaError_t launch_b(const KernelArgs &args, const LaunchShape &s, cudaStream_t stream) {
+    cudaError_t e = cudaFuncSetAttribute(frame_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    frame_kernel<B><<<s.grid, s.threads, s.smem, stream>>>(args);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_frame_kernel(const KernelArgs &args, const LaunchShape &shape, cudaStream_t stream) {
+    switch (shape.blocks_per_cta) {
+        case 1:
+            return launch_b<1>(args, shape, stream);
+        case 2:
+            return launch_b<2>(args, shape, stream);
+        case 4:
+            return launch_b<4>(args, shape, stream);
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+template <int B>
+static cudaError_t occ_b(const LaunchShape &s, int *out) {
+    cudaError_t e = cudaFuncSetAttribute(frame_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, frame_kernel<B>, s.threads, s.smem);
+}
+
+cudaError_t frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out) {
+    switch (shape.blocks_per_cta) {
+        case 1:
+            return occ_b<1>(shape, out);
+        case 2:
+            return occ_b<2>(shape, out);
+        case 4:
+            return occ_b<4>(shape, out);
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Shot-major output.  One warp per (128-shot block, 32 concatenated rows); 8 warps of a CTA cover 256
+// consecutive rows of the same block so that each shot's output bytes are written by one CTA.
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) transpose_kernel(const TransposeArgs t) {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t blk = blockIdx.x;
+    const uint64_t total = t.n0 + t.n1 + t.n2;
+    const uint64_t r0 = ((uint64_t)blockIdx.y * 8 + warp) * 32;
+    if (r0 >= total) {
+        return;
+    }
+    const uint64_t r = r0 + lane;
+    uint4 v = zero4();
+    if (r < t.n0) {
+        v = t.src0[blk * t.n0 + r];
+    } else if (r < t.n0 + t.n1) {
+        v = t.src1[blk * t.n1 + (r - t.n0)];
+    } else if (r < total) {
+        v = t.src2[blk * t.n2 + (r - t.n0 - t.n1)];
+    }
+    if (t.xor_rows && r < total && ((t.xor_rows[r >> 3] >> (r & 7)) & 1)) {
+        v = x4(v, make_uint4(~0u, ~0u, ~0u, ~0u));
+    }
+    const uint32_t words[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int w = 0; w < 4; w++) {
+        uint32_t mine = 0;
+#pragma unroll
+        for (int i = 0; i < 32; i++) {
+            uint32_t b = __ballot_sync(0xFFFFFFFFu, (words[w] >> i) & 1u);
+            if (lane == (uint32_t)i) {
+                mine = b;
+            }
+        }
+        uint64_t shot = blk * 128 + (uint64_t)w * 32 + lane;
+        if (shot >= t.nshots) {
+            continue;
+        }
+        uint8_t *row = t.out + shot * t.out_stride;
+        uint64_t nvalid = total - r0 < 32 ? total - r0 : 32;
+        if (t.bit_packed) {
+            uint64_t nbytes = (nvalid + 7) / 8;
+            for (uint64_t j = 0; j < nbytes; j++) {
+                row[r0 / 8 + j] = (uint8_t)(mine >> (8 * j));
+            }
+        } else {
+            for (uint64_t j = 0; j < nvalid; j++) {
+                row[r0 + j] = (uint8_t)((mine >> j) & 1u);
+            }
+        }
+    }
+}
+
+cudaError_t launch_transpose(const TransposeArgs &args, cudaStream_t stream) {
+    uint64_t total = args.n0 + args.n1 + args.n2;
+    if (total == 0 || args.nshots == 0) {
+        return cudaSuccess;
+    }
+    uint64_t nblk = (args.nshots + 127) / 128;
+    uint64_t ngroups = (total + 31) / 32;
+    dim3 grid((unsigned)nblk, (unsigned)((ngroups + 7) / 8));
+    if (grid.y > 65535) {
+        return cudaErrorInvalidValue;
+    }
+    transpose_kernel<<<grid, 256, 0, stream>>>(args);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------------------
+// Shared-memory throughput probe: every thread streams 128-bit load/XOR/store passes over a 64 KiB
+// shared buffer with conflict-free addressing (consecutive lanes touch consecutive 16-byte words).
+// Reports the bytes moved (loads + stores) per second over all SMs: the denominator of the frame
+// kernel's shared-memory roofline.
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) smem_probe_kernel(uint32_t iters, uint32_t *sink) {
+    extern __shared__ uint4 buf[];
+    const uint32_t n = 4096;  // 64 KiB of uint4
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        buf[i] = make_uint4(i, i * 3u, i * 5u, i * 7u);
+    }
+    __syncthreads();
+    uint4 acc = zero4();
+    uint32_t idx = threadIdx.x;
+    for (uint32_t it = 0; it < iters; it++) {
+#pragma unroll 8
+        for (uint32_t k = 0; k < 8; k++) {
+            uint32_t j = (idx + k * blockDim.x) & (n - 1);
+            uint4 v = buf[j];
+            acc = x4(acc, v);
+            buf[j] = x4(v, make_uint4(it, k, it ^ k, 1u));
+        }
+    }
+    if ((acc.x ^ acc.y ^ acc.z ^ acc.w) == 0x9E3779B9u) {
+        atomicAdd(sink, 1u);
+    }
+}
+
+cudaError_t measure_smem_peak(double *bytes_per_s) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, dev);
+    if (e != cudaSuccess) return e;
+    const size_t smem = 4096 * sizeof(uint4);
+    e = cudaFuncSetAttribute(smem_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, smem_probe_kernel, 512, smem);
+    if (e != cudaSuccess) return e;
+    int grid = prop.multiProcessorCount * (per_sm > 0 ? per_sm : 1);
+    uint32_t *sink = nullptr;
+    e = cudaMalloc(&sink, 4);
+    if (e != cudaSuccess) return e;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const uint32_t iters = 4096;
+    smem_probe_kernel<<<grid, 512, smem>>>(64, sink);  // warm-up
+    cudaEventRecord(a);
+    smem_probe_kernel<<<grid, 512, smem>>>(iters, sink);
+    cudaEventRecord(b);
+    e = cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(sink);
+    if (e != cudaSuccess) return e;
+    double bytes = (double)grid * 512.0 * iters * 8.0 * 2.0 * sizeof(uint4);
+    *bytes_per_s = bytes / (ms * 1e-3);
+    return cudaGetLastError();
+}
+
+}  // namespace gfs

@@ -1,0 +1,63 @@
+// Launch interface of the frame-sampling kernels (kernels.cu).  Host code only sees plain pointers.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "program.h"
+
+namespace gfs {
+
+struct KernelArgs {
+    const DevOp *ops;
+    const uint32_t *pool;
+    const uint32_t *tables;
+    const DevChan *chans;
+    const uint32_t *qubit_orig;
+    uint32_t nrows;
+    uint32_t ring;
+    uint32_t nobs;
+    uint32_t nslices;  // slices of `blocks_per_cta` 128-shot blocks in this launch
+    uint64_t ndet;
+    uint64_t nmeas;
+    uint64_t seed;
+    uint64_t block0;   // stream position (global 128-shot block index) of local block 0
+    uint4 *det_out;    // [local block][ndet] (may be null when ndet == 0)
+    uint4 *obs_out;    // [local block][nobs]
+    uint4 *meas_out;   // [local block][nmeas] (measurement mode only)
+    uint32_t *status;  // device error word, 0 = ok
+};
+
+struct LaunchShape {
+    int blocks_per_cta;  // 1, 2 or 4 blocks of 128 shots per CTA
+    int threads;         // threads per CTA
+    int grid;            // CTAs (persistent: each walks slices grid-stride)
+    size_t smem;         // dynamic shared memory bytes
+};
+
+size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta);
+cudaError_t launch_frame_kernel(const KernelArgs &args, const LaunchShape &shape, cudaStream_t stream);
+cudaError_t frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out);
+
+// Transposes [local block][rows] bit-rows (128 shots per entry) of up to three sources, concatenated
+// (src0 rows, then src1, then src2), into shot-major output rows.  `xor_rows` (optional) is a bit vector over the
+// concatenated rows that is XORed into every shot (the reference sample of measurement sampling).
+struct TransposeArgs {
+    const uint4 *src0;
+    uint64_t n0;
+    const uint4 *src1;
+    uint64_t n1;
+    const uint4 *src2;
+    uint64_t n2;
+    const uint8_t *xor_rows;
+    uint64_t nshots;
+    uint8_t *out;
+    uint64_t out_stride;  // bytes between consecutive shots in `out`
+    int bit_packed;       // 1: little-endian bit-packed bytes; 0: one byte (0/1) per bit
+};
+cudaError_t launch_transpose(const TransposeArgs &args, cudaStream_t stream);
+
+// Shared-memory load+store throughput of the current device (bytes per second over all SMs).
+cudaError_t measure_smem_peak(double *bytes_per_s);
+
+}  // namespace gfs

@@ -1,0 +1,807 @@
+// Lowering of a parsed circuit into the device program.
+//
+// Decompositions follow the reference exactly where they change which frame bits exist at a
+// randomization point: MPP (gate_decomposition.cc:88-161), SPP/SPP_DAG (gate_decomposition.cc:163-250),
+// MXX/MYY/MZZ (frame_simulator.inl:841-902 with decompose_pair_instruction_into_disjoint_segments,
+// gate_decomposition.cc:319-347).  Instructions whose targets repeat are split into runs of distinct
+// targets so the kernel may process every unit of an op in parallel with the reference's sequential
+// result (frame_simulator.inl:278 notes the same hazard for MR).
+#include "lower.h"
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <stdexcept>
+#include <unordered_map>
+#include <unordered_set>
+
+#include "gfs_contract.h"
+
+namespace gfs {
+namespace {
+
+struct Lowerer {
+    const Circuit &root;
+    SampleMode mode;
+    Program prog;
+    std::vector<int32_t> row_of;  // qubit -> row
+    std::map<std::vector<double>, uint32_t> chan_cache;
+    uint64_t meas_seen = 0;  // results before this point on the first pass through every loop
+    uint64_t max_results_per_inst = 0;
+
+    // pending detector group
+    std::vector<std::vector<uint32_t>> pending_dets;
+    uint64_t pending_inst = 0;
+
+    Lowerer(const Circuit &c, SampleMode m) : root(c), mode(m) {
+    }
+
+    uint32_t row(uint32_t t) const {
+        return (uint32_t)row_of[t & GFS_T_VALUE_MASK];
+    }
+
+    void collect_qubits(const Circuit &c, std::vector<uint8_t> &used) {
+        for (const auto &op : c.ops) {
+            if (op.gate == GFS_REPEAT) {
+                collect_qubits(c.blocks[op.block], used);
+                continue;
+            }
+            if (op.gate == GFS_MPAD) {
+                continue;
+            }
+            for (auto t : op.targets) {
+                if (t & (GFS_T_RECORD | GFS_T_SWEEP | GFS_T_COMBINER)) {
+                    continue;
+                }
+                used[t & GFS_T_VALUE_MASK] = 1;
+            }
+        }
+    }
+
+    uint32_t channel(double p, const std::vector<double> &weights) {
+        std::vector<double> key = weights;
+        key.push_back(p);
+        auto it = chan_cache.find(key);
+        if (it != chan_cache.end()) {
+            return it->second;
+        }
+        DevChan ch{};
+        ch.active = p > 0;
+        ch.always = p >= 1;
+        ch.table = 0;
+        ch.inv_c = 0;
+        if (ch.active && !ch.always) {
+            ch.table = (uint32_t)prog.tables.size();
+            prog.tables.resize(prog.tables.size() + GFS_SEG_TRIALS + 1);
+            gfs_build_gap_table(p, prog.tables.data() + ch.table);
+            ch.inv_c = gfs_inv_c(p);
+        }
+        if (!weights.empty()) {
+            gfs_build_choice_table(weights.data(), (uint32_t)weights.size(), ch.cum);
+        }
+        uint32_t id = (uint32_t)prog.chans.size();
+        prog.chans.push_back(ch);
+        chan_cache[key] = id;
+        return id;
+    }
+
+    DevOp &emit(uint32_t code, uint32_t sub, uint32_t n, uint64_t inst) {
+        DevOp op{};
+        op.code = code | (sub << 8);
+        op.n = n;
+        op.a = (uint32_t)prog.pool.size();
+        op.inst = inst;
+        prog.ops.push_back(op);
+        return prog.ops.back();
+    }
+
+    void check_lookback(uint32_t k) {
+        if (k == 0) {
+            throw std::out_of_range("Lookback must be non-zero.");
+        }
+        if (k > meas_seen) {
+            throw std::out_of_range("Referred to a measurement record before the beginning of time.");
+        }
+    }
+
+    // ---- runs of distinct rows ----
+    template <typename F>
+    void distinct_runs(const std::vector<uint32_t> &rows, size_t stride, F flush) {
+        std::unordered_set<uint32_t> seen;
+        size_t start = 0;
+        for (size_t k = 0; k < rows.size(); k += stride) {
+            bool clash = false;
+            for (size_t j = 0; j < stride; j++) {
+                if (seen.count(rows[k + j])) {
+                    clash = true;
+                }
+            }
+            if (clash) {
+                flush(start, k);
+                seen.clear();
+                start = k;
+            }
+            for (size_t j = 0; j < stride; j++) {
+                seen.insert(rows[k + j]);
+            }
+        }
+        if (start < rows.size()) {
+            flush(start, rows.size());
+        }
+    }
+
+    void emit_1q(uint32_t sub, const std::vector<uint32_t> &rows, uint64_t inst) {
+        distinct_runs(rows, 1, [&](size_t a, size_t b) {
+            emit(OP_1Q, sub, (uint32_t)(b - a), inst);
+            prog.pool.insert(prog.pool.end(), rows.begin() + a, rows.begin() + b);
+        });
+    }
+
+    void emit_2q(uint32_t sub, const std::vector<uint32_t> &rows, uint64_t inst) {
+        distinct_runs(rows, 2, [&](size_t a, size_t b) {
+            emit(OP_2Q, sub, (uint32_t)((b - a) / 2), inst);
+            prog.pool.insert(prog.pool.end(), rows.begin() + a, rows.begin() + b);
+        });
+    }
+
+    void emit_measure(uint32_t sub, const std::vector<uint32_t> &rows, uint32_t unit0, uint64_t inst) {
+        distinct_runs(rows, 1, [&](size_t a, size_t b) {
+            DevOp &op = emit(OP_MEASURE, sub, (uint32_t)(b - a), inst);
+            op.b = unit0 + (uint32_t)a;
+            prog.pool.insert(prog.pool.end(), rows.begin() + a, rows.begin() + b);
+        });
+    }
+
+    void emit_results_tail(const Instruction &op, uint64_t nres, uint64_t inst) {
+        if (!op.args.empty() && op.args[0] > 0 && nres) {
+            DevOp &d = emit(OP_MNOISE, 0, (uint32_t)nres, inst);
+            d.b = channel(op.args[0], {});
+        }
+        if (mode == SampleMode::MEASUREMENTS && nres) {
+            emit(OP_EMIT, 0, (uint32_t)nres, inst);
+        }
+        meas_seen += nres;
+        max_results_per_inst = std::max(max_results_per_inst, nres);
+    }
+
+    void flush_detectors() {
+        if (pending_dets.empty()) {
+            return;
+        }
+        uint32_t n = (uint32_t)pending_dets.size();
+        emit(OP_DETECTORS, 0, n, pending_inst);
+        size_t base = prog.pool.size();
+        prog.pool.resize(base + n + 1);
+        for (uint32_t i = 0; i < n; i++) {
+            prog.pool[base + i] = (uint32_t)prog.pool.size();
+            prog.pool.insert(prog.pool.end(), pending_dets[i].begin(), pending_dets[i].end());
+        }
+        prog.pool[base + n] = (uint32_t)prog.pool.size();
+        prog.num_detectors += n;
+        pending_dets.clear();
+    }
+
+    // ---- two-qubit gates with classical controls ----
+    void lower_two_qubit(const Instruction &op, uint64_t inst) {
+        uint32_t sub = 0;
+        bool reverse = false;
+        switch (op.gate) {
+            case GFS_CX: sub = K2_CX; break;
+            case GFS_CY: sub = K2_CY; break;
+            case GFS_CZ: sub = K2_CZ; break;
+            case GFS_XCZ: sub = K2_CX; reverse = true; break;
+            case GFS_YCZ: sub = K2_CY; reverse = true; break;
+            case GFS_XCX: sub = K2_XCX; break;
+            case GFS_XCY: sub = K2_XCY; break;
+            case GFS_YCX: sub = K2_YCX; break;
+            case GFS_YCY: sub = K2_YCY; break;
+            case GFS_SWAP: sub = K2_SWAP; break;
+            case GFS_ISWAP:
+            case GFS_ISWAP_DAG: sub = K2_ISWAP; break;
+            case GFS_CXSWAP: sub = K2_CXSWAP; break;
+            case GFS_SWAPCX: sub = K2_SWAPCX; break;
+            case GFS_CZSWAP: sub = K2_CZSWAP; break;
+            case GFS_SQRT_XX:
+            case GFS_SQRT_XX_DAG: sub = K2_SQRT_XX; break;
+            case GFS_SQRT_YY:
+            case GFS_SQRT_YY_DAG: sub = K2_SQRT_YY; break;
+            case GFS_SQRT_ZZ:
+            case GFS_SQRT_ZZ_DAG: sub = K2_SQRT_ZZ; break;
+            default: throw std::invalid_argument("not a two-qubit gate");
+        }
+        // Split into runs; a run is either all quantum pairs or all feedback, with distinct rows.
+        std::vector<uint32_t> qrows;
+        std::vector<uint32_t> fb;  // lookback, row|mask
+        std::unordered_set<uint32_t> seen;
+        auto flush = [&]() {
+            if (!qrows.empty()) {
+                emit(OP_2Q, sub, (uint32_t)(qrows.size() / 2), inst);
+                prog.pool.insert(prog.pool.end(), qrows.begin(), qrows.end());
+                qrows.clear();
+            }
+            if (!fb.empty()) {
+                emit(OP_FEEDBACK, 0, (uint32_t)(fb.size() / 2), inst);
+                prog.pool.insert(prog.pool.end(), fb.begin(), fb.end());
+                fb.clear();
+            }
+            seen.clear();
+        };
+        for (size_t k = 0; k < op.targets.size(); k += 2) {
+            uint32_t c = op.targets[k] & ~GFS_T_INVERTED, t = op.targets[k + 1] & ~GFS_T_INVERTED;
+            if (reverse) {
+                std::swap(c, t);
+            }
+            bool cb = c & (GFS_T_RECORD | GFS_T_SWEEP), tb = t & (GFS_T_RECORD | GFS_T_SWEEP);
+            if (!cb && !tb) {
+                uint32_t r1 = row(c), r2 = row(t);
+                if (!fb.empty() || seen.count(r1) || seen.count(r2)) {
+                    flush();
+                }
+                seen.insert(r1);
+                seen.insert(r2);
+                qrows.push_back(r1);
+                qrows.push_back(r2);
+                continue;
+            }
+            uint32_t bit, q, mask;
+            if (sub == K2_CZ) {
+                if (cb && tb) {
+                    continue;  // both classical: no effect
+                }
+                bit = cb ? c : t;
+                q = cb ? t : c;
+                mask = kFeedbackZ;
+            } else if (tb) {
+                throw std::invalid_argument(std::string(sub == K2_CX ? "Controlled X" : "Controlled Y") +
+                                            " had a bit as its target, instead of its control.");
+            } else {
+                bit = c;
+                q = t;
+                mask = sub == K2_CX ? kFeedbackX : (kFeedbackX | kFeedbackZ);
+            }
+            if (bit & GFS_T_SWEEP) {
+                continue;  // sweep bits read as zero in the samplers
+            }
+            uint32_t k_back = bit & GFS_T_VALUE_MASK;
+            check_lookback(k_back);
+            uint32_t r = row(q);
+            if (!qrows.empty() || seen.count(r)) {
+                flush();
+            }
+            seen.insert(r);
+            fb.push_back(k_back);
+            fb.push_back(r | (mask << 24));
+        }
+        flush();
+    }
+
+    // ---- Pauli products (MPP, SPP) ----
+    struct Product {
+        std::vector<uint32_t> qubits;  // sorted, active
+        std::vector<uint8_t> x, z;
+        std::vector<uint32_t> bits;
+    };
+
+    std::vector<Product> read_products(const Instruction &op, const char *gname) {
+        std::vector<Product> out;
+        size_t k = 0;
+        while (k < op.targets.size()) {
+            size_t end = k + 1;
+            while (end < op.targets.size() && (op.targets[end] & GFS_T_COMBINER)) {
+                end += 2;
+            }
+            std::map<uint32_t, std::pair<uint8_t, uint8_t>> acc;
+            bool imag = false;
+            Product p;
+            for (size_t j = k; j < end; j += 2) {
+                uint32_t t = op.targets[j];
+                if (t & (GFS_T_PAULI_X | GFS_T_PAULI_Z)) {
+                    uint32_t q = t & GFS_T_VALUE_MASK;
+                    uint8_t nx = (t & GFS_T_PAULI_X) ? 1 : 0, nz = (t & GFS_T_PAULI_Z) ? 1 : 0;
+                    auto &e = acc[q];
+                    if ((e.first & nz) ^ (e.second & nx)) {
+                        imag = !imag;
+                    }
+                    e.first ^= nx;
+                    e.second ^= nz;
+                } else if (t & (GFS_T_RECORD | GFS_T_SWEEP)) {
+                    p.bits.push_back(t);
+                } else {
+                    throw std::invalid_argument(std::string("Found an unsupported target in ") + gname + ".");
+                }
+            }
+            if (imag) {
+                throw std::invalid_argument(std::string("Acted on an anti-Hermitian operator (e.g. X0*Z0 instead of Y0) in ") +
+                                            gname + ".");
+            }
+            for (auto &e : acc) {
+                if (e.second.first || e.second.second) {
+                    p.qubits.push_back(e.first);
+                    p.x.push_back(e.second.first);
+                    p.z.push_back(e.second.second);
+                }
+            }
+            out.push_back(std::move(p));
+            k = end;
+        }
+        return out;
+    }
+
+    // Emits the CX pairs (control, target) as layers in which every row appears at most once.  All
+    // pairs passed here commute with one another (distinct controls, targets never controls).
+    void emit_cx_layers(const std::vector<std::pair<uint32_t, uint32_t>> &pairs, uint64_t inst) {
+        std::vector<std::pair<uint32_t, uint32_t>> rest = pairs;
+        while (!rest.empty()) {
+            std::unordered_set<uint32_t> used;
+            std::vector<uint32_t> layer;
+            std::vector<std::pair<uint32_t, uint32_t>> next;
+            for (auto &pr : rest) {
+                if (used.count(pr.first) || used.count(pr.second)) {
+                    next.push_back(pr);
+                } else {
+                    used.insert(pr.first);
+                    used.insert(pr.second);
+                    layer.push_back(pr.first);
+                    layer.push_back(pr.second);
+                }
+            }
+            emit(OP_2Q, K2_CX, (uint32_t)(layer.size() / 2), inst);
+            prog.pool.insert(prog.pool.end(), layer.begin(), layer.end());
+            rest.swap(next);
+        }
+    }
+
+    void lower_mpp(const Instruction &op, uint64_t inst) {
+        auto prods = read_products(op, "MPP");
+        uint32_t result = 0;
+        std::vector<uint32_t> hxz, hyz, meas;
+        std::vector<std::pair<uint32_t, uint32_t>> cnot;
+        std::unordered_set<uint32_t> merged;
+        uint32_t group_first = 0;
+        auto flush = [&]() {
+            if (meas.empty()) {
+                return;
+            }
+            if (!hxz.empty()) emit_1q(K1_H_XZ, hxz, inst);
+            if (!hyz.empty()) emit_1q(K1_H_YZ, hyz, inst);
+            if (!cnot.empty()) emit_cx_layers(cnot, inst);
+            emit_measure(KM_M, meas, group_first, inst);
+            if (!cnot.empty()) emit_cx_layers(cnot, inst);
+            if (!hyz.empty()) emit_1q(K1_H_YZ, hyz, inst);
+            if (!hxz.empty()) emit_1q(K1_H_XZ, hxz, inst);
+            hxz.clear();
+            hyz.clear();
+            meas.clear();
+            cnot.clear();
+            merged.clear();
+        };
+        for (auto &p : prods) {
+            if (p.qubits.empty()) {
+                flush();
+                emit(OP_RECORD_ZERO, 0, 1, inst);
+                result++;
+                continue;
+            }
+            bool overlap = false;
+            for (auto q : p.qubits) {
+                overlap |= merged.count(q) > 0;
+            }
+            if (overlap) {
+                flush();
+            }
+            if (meas.empty()) {
+                group_first = result;
+            }
+            for (size_t j = 0; j < p.qubits.size(); j++) {
+                uint32_t r = row_of[p.qubits[j]];
+                merged.insert(p.qubits[j]);
+                if (p.x[j]) {
+                    (p.z[j] ? hyz : hxz).push_back(r);
+                }
+                if (j == 0) {
+                    meas.push_back(r);
+                } else {
+                    cnot.push_back({r, (uint32_t)row_of[p.qubits[0]]});
+                }
+            }
+            result++;
+        }
+        flush();
+        emit_results_tail(op, result, inst);
+    }
+
+    void lower_spp(const Instruction &op, uint64_t inst) {
+        auto prods = read_products(op, op.gate == GFS_SPP ? "SPP" : "SPP_DAG");
+        for (auto &p : prods) {
+            if (p.qubits.empty()) {
+                continue;
+            }
+            std::vector<uint32_t> hxz, hyz;
+            uint32_t focus = (uint32_t)row_of[p.qubits[0]];
+            for (size_t j = 0; j < p.qubits.size(); j++) {
+                uint32_t r = row_of[p.qubits[j]];
+                if (p.x[j]) {
+                    (p.z[j] ? hyz : hxz).push_back(r);
+                }
+            }
+            auto cx_all = [&]() {
+                for (size_t j = 1; j < p.qubits.size(); j++) {
+                    emit(OP_2Q, K2_CX, 1, inst);
+                    prog.pool.push_back((uint32_t)row_of[p.qubits[j]]);
+                    prog.pool.push_back(focus);
+                }
+                for (auto b : p.bits) {
+                    if (b & GFS_T_SWEEP) {
+                        continue;
+                    }
+                    check_lookback(b & GFS_T_VALUE_MASK);
+                    emit(OP_FEEDBACK, 0, 1, inst);
+                    prog.pool.push_back(b & GFS_T_VALUE_MASK);
+                    prog.pool.push_back(focus | (kFeedbackX << 24));
+                }
+            };
+            if (!hxz.empty()) emit_1q(K1_H_XZ, hxz, inst);
+            if (!hyz.empty()) emit_1q(K1_H_YZ, hyz, inst);
+            cx_all();
+            emit_1q(K1_H_XY, {focus}, inst);
+            cx_all();
+            if (!hyz.empty()) emit_1q(K1_H_YZ, hyz, inst);
+            if (!hxz.empty()) emit_1q(K1_H_XZ, hxz, inst);
+        }
+    }
+
+    void lower_pair_measure(const Instruction &op, uint64_t inst) {
+        uint32_t conj = op.gate == GFS_MYY ? K2_CY : K2_CX;
+        bool reverse = op.gate == GFS_MZZ;
+        uint32_t mk = op.gate == GFS_MXX ? KM_MX : op.gate == GFS_MYY ? KM_MY : KM_M;
+        uint32_t result = 0;
+        std::unordered_set<uint32_t> used;
+        size_t flushed = 0;
+        auto flush = [&](size_t end) {
+            std::vector<uint32_t> pr, first;
+            for (size_t k = flushed; k < end; k += 2) {
+                uint32_t a = row(op.targets[k]), b = row(op.targets[k + 1]);
+                if (reverse) {
+                    pr.push_back(b);
+                    pr.push_back(a);
+                } else {
+                    pr.push_back(a);
+                    pr.push_back(b);
+                }
+                first.push_back(a);
+            }
+            emit_2q(conj, pr, inst);
+            emit_measure(mk, first, result, inst);
+            emit_2q(conj, pr, inst);
+            result += (uint32_t)first.size();
+            used.clear();
+            flushed = end;
+        };
+        for (size_t k = 0; k < op.targets.size(); k += 2) {
+            uint32_t q0 = op.targets[k] & GFS_T_VALUE_MASK, q1 = op.targets[k + 1] & GFS_T_VALUE_MASK;
+            if (used.count(q0) || used.count(q1)) {
+                flush(k);
+            }
+            used.insert(q0);
+            used.insert(q1);
+        }
+        if (flushed < op.targets.size()) {
+            flush(op.targets.size());
+        }
+        emit_results_tail(op, result, inst);
+    }
+
+    void lower_instruction(const Instruction &op, uint64_t inst) {
+        gfs_gate g = op.gate;
+        if (g == GFS_DETECTOR) {
+            if (pending_dets.empty()) {
+                pending_inst = inst;
+            }
+            std::vector<uint32_t> lbs;
+            for (auto t : op.targets) {
+                uint32_t k = t & GFS_T_VALUE_MASK;
+                check_lookback(k);
+                lbs.push_back(k);
+            }
+            pending_dets.push_back(std::move(lbs));
+            return;
+        }
+        switch (g) {
+            case GFS_TICK:
+            case GFS_QUBIT_COORDS:
+            case GFS_SHIFT_COORDS:
+            case GFS_I:
+            case GFS_X:
+            case GFS_Y:
+            case GFS_Z:
+            case GFS_II:
+            case GFS_I_ERROR:
+            case GFS_II_ERROR:
+                return;
+            default:
+                break;
+        }
+        if (g == GFS_OBSERVABLE_INCLUDE) {
+            uint32_t k_obs = (uint32_t)op.args[0];
+            std::vector<uint32_t> terms;
+            for (auto t : op.targets) {
+                if (t & GFS_T_RECORD) {
+                    check_lookback(t & GFS_T_VALUE_MASK);
+                    terms.push_back((t & GFS_T_VALUE_MASK) | kTermRecord);
+                } else {
+                    uint32_t term = row(t);
+                    if (t & GFS_T_PAULI_X) term |= kTermX;
+                    if (t & GFS_T_PAULI_Z) term |= kTermZ;
+                    terms.push_back(term);
+                }
+            }
+            if (!terms.empty()) {
+                DevOp &d = emit(OP_OBS, 0, (uint32_t)terms.size(), inst);
+                d.b = k_obs;
+                prog.pool.insert(prog.pool.end(), terms.begin(), terms.end());
+            }
+            return;
+        }
+        flush_detectors();
+        std::vector<uint32_t> rows;
+        for (auto t : op.targets) {
+            if (!(t & (GFS_T_RECORD | GFS_T_SWEEP | GFS_T_COMBINER))) {
+                rows.push_back(row(t));
+            }
+        }
+        switch (g) {
+            case GFS_H:
+            case GFS_H_NXZ:
+            case GFS_SQRT_Y:
+            case GFS_SQRT_Y_DAG:
+                emit_1q(K1_H_XZ, rows, inst);
+                return;
+            case GFS_S:
+            case GFS_S_DAG:
+            case GFS_H_XY:
+            case GFS_H_NXY:
+                emit_1q(K1_H_XY, rows, inst);
+                return;
+            case GFS_SQRT_X:
+            case GFS_SQRT_X_DAG:
+            case GFS_H_YZ:
+            case GFS_H_NYZ:
+                emit_1q(K1_H_YZ, rows, inst);
+                return;
+            case GFS_C_XYZ:
+            case GFS_C_NXYZ:
+            case GFS_C_XNYZ:
+            case GFS_C_XYNZ:
+                emit_1q(K1_C_XYZ, rows, inst);
+                return;
+            case GFS_C_ZYX:
+            case GFS_C_NZYX:
+            case GFS_C_ZNYX:
+            case GFS_C_ZYNX:
+                emit_1q(K1_C_ZYX, rows, inst);
+                return;
+            case GFS_M:
+            case GFS_MX:
+            case GFS_MY:
+            case GFS_MR:
+            case GFS_MRX:
+            case GFS_MRY: {
+                uint32_t sub = g == GFS_M    ? KM_M
+                               : g == GFS_MX ? KM_MX
+                               : g == GFS_MY ? KM_MY
+                               : g == GFS_MR ? KM_MR
+                               : g == GFS_MRX ? KM_MRX
+                                              : KM_MRY;
+                emit_measure(sub, rows, 0, inst);
+                emit_results_tail(op, rows.size(), inst);
+                return;
+            }
+            case GFS_R:
+            case GFS_RX:
+            case GFS_RY: {
+                uint32_t sub = g == GFS_R ? KR_R : g == GFS_RX ? KR_RX : KR_RY;
+                distinct_runs(rows, 1, [&](size_t a, size_t b) {
+                    DevOp &d = emit(OP_RESET, sub, (uint32_t)(b - a), inst);
+                    d.b = (uint32_t)a;
+                    prog.pool.insert(prog.pool.end(), rows.begin() + a, rows.begin() + b);
+                });
+                return;
+            }
+            case GFS_MPAD: {
+                emit(OP_RECORD_ZERO, 0, (uint32_t)op.targets.size(), inst);
+                emit_results_tail(op, op.targets.size(), inst);
+                return;
+            }
+            case GFS_MPP:
+                lower_mpp(op, inst);
+                return;
+            case GFS_SPP:
+            case GFS_SPP_DAG:
+                lower_spp(op, inst);
+                return;
+            case GFS_MXX:
+            case GFS_MYY:
+            case GFS_MZZ:
+                lower_pair_measure(op, inst);
+                return;
+            case GFS_X_ERROR:
+            case GFS_Y_ERROR:
+            case GFS_Z_ERROR:
+            case GFS_DEPOLARIZE1:
+            case GFS_DEPOLARIZE2: {
+                double p = op.args[0];
+                if (!(p > 0) || rows.empty()) {
+                    return;
+                }
+                uint32_t sub = g == GFS_X_ERROR   ? KN_X
+                               : g == GFS_Y_ERROR ? KN_Y
+                               : g == GFS_Z_ERROR ? KN_Z
+                               : g == GFS_DEPOLARIZE1 ? KN_DEP1
+                                                      : KN_DEP2;
+                uint32_t n = (uint32_t)(sub == KN_DEP2 ? rows.size() / 2 : rows.size());
+                DevOp &d = emit(OP_NOISE, sub, n, inst);
+                d.b = channel(p, {});
+                prog.pool.insert(prog.pool.end(), rows.begin(), rows.end());
+                return;
+            }
+            case GFS_PAULI_CHANNEL_1:
+            case GFS_PAULI_CHANNEL_2: {
+                double p = 0;
+                for (double w : op.args) p += w;
+                if (!(p > 0) || rows.empty()) {
+                    return;
+                }
+                uint32_t sub = g == GFS_PAULI_CHANNEL_1 ? KN_PC1 : KN_PC2;
+                uint32_t n = (uint32_t)(sub == KN_PC2 ? rows.size() / 2 : rows.size());
+                DevOp &d = emit(OP_NOISE, sub, n, inst);
+                d.b = channel(p, op.args);
+                prog.pool.insert(prog.pool.end(), rows.begin(), rows.end());
+                return;
+            }
+            case GFS_E:
+            case GFS_ELSE_CORRELATED_ERROR: {
+                DevOp &m = emit(OP_CORR_MASK, g == GFS_E ? 0 : 1, 1, inst);
+                m.b = channel(op.args[0], {});
+                std::map<uint32_t, uint32_t> xz;
+                for (auto t : op.targets) {
+                    uint32_t r = row(t);
+                    uint32_t v = ((t & GFS_T_PAULI_X) ? 1u : 0u) | ((t & GFS_T_PAULI_Z) ? 2u : 0u);
+                    xz[r] ^= v;
+                }
+                std::vector<uint32_t> units;
+                for (auto &e : xz) {
+                    if (e.second) {
+                        units.push_back(e.first | (e.second << 24));
+                    }
+                }
+                if (!units.empty()) {
+                    emit(OP_CORR_APPLY, 0, (uint32_t)units.size(), inst);
+                    prog.pool.insert(prog.pool.end(), units.begin(), units.end());
+                }
+                return;
+            }
+            case GFS_HERALDED_ERASE:
+            case GFS_HERALDED_PAULI_CHANNEL_1: {
+                uint32_t n = (uint32_t)rows.size();
+                emit(OP_RECORD_ZERO, 0, n, inst);
+                double p = 0;
+                std::vector<double> w;
+                if (g == GFS_HERALDED_ERASE) {
+                    p = op.args[0];
+                } else {
+                    w = op.args;
+                    for (double v : w) p += v;
+                }
+                if (p > 0 && n) {
+                    DevOp &d = emit(OP_HERALD, g == GFS_HERALDED_ERASE ? 0 : 1, n, inst);
+                    d.b = channel(p, w);
+                    prog.pool.insert(prog.pool.end(), rows.begin(), rows.end());
+                }
+                if (mode == SampleMode::MEASUREMENTS && n) {
+                    emit(OP_EMIT, 0, n, inst);
+                }
+                meas_seen += n;
+                max_results_per_inst = std::max<uint64_t>(max_results_per_inst, n);
+                return;
+            }
+            default:
+                break;
+        }
+        if (gate_info(g).flags & GFS_F_PAIRS) {
+            lower_two_qubit(op, inst);
+            return;
+        }
+        throw std::invalid_argument(std::string("Not implemented in the GPU frame sampler: ") + gate_info(g).name);
+    }
+
+    std::unordered_map<const Circuit *, uint64_t> inst_memo;
+    uint64_t instances(const Circuit &c) {
+        auto it = inst_memo.find(&c);
+        if (it != inst_memo.end()) {
+            return it->second;
+        }
+        uint64_t v = c.stats().num_instances;
+        inst_memo[&c] = v;
+        return v;
+    }
+
+    uint64_t results_of(const Circuit &c) {
+        return c.stats().num_measurements;
+    }
+
+    void lower_block(const Circuit &c, uint32_t depth) {
+        prog.max_loop_depth = std::max(prog.max_loop_depth, depth);
+        if (depth > (uint32_t)kMaxLoopDepth) {
+            throw std::invalid_argument("REPEAT blocks nested deeper than the GPU sampler supports");
+        }
+        uint64_t flat = 0;
+        for (const auto &op : c.ops) {
+            if (op.gate == GFS_REPEAT) {
+                flush_detectors();
+                const Circuit &body = c.blocks[op.block];
+                uint64_t stride = instances(body);
+                size_t begin = prog.ops.size();
+                DevOp &lb = emit(OP_LOOP_BEGIN, 0, 0, flat);
+                lb.a = (uint32_t)op.reps;
+                lb.b = (uint32_t)(op.reps >> 32);
+                lb.c = (uint32_t)stride;
+                lb.d = (uint32_t)(stride >> 32);
+                uint64_t seen_before = meas_seen;
+                lower_block(body, depth + 1);
+                flush_detectors();
+                uint32_t body_len = (uint32_t)(prog.ops.size() - begin - 1);
+                prog.ops[begin].n = body_len;
+                DevOp &le = emit(OP_LOOP_END, 0, body_len, flat);
+                (void)le;
+                // The body was lowered against the first iteration's record length; later iterations
+                // only see more results.
+                uint64_t per_iter = meas_seen - seen_before;
+                meas_seen = seen_before + per_iter * op.reps;
+                flat += op.reps * stride;
+            } else {
+                lower_instruction(op, flat);
+                flat += 1;
+            }
+        }
+    }
+
+    void run() {
+        prog.stats = root.stats();
+        std::vector<uint8_t> used(prog.stats.num_qubits + 1, 0);
+        collect_qubits(root, used);
+        row_of.assign(used.size(), -1);
+        for (size_t q = 0; q < used.size(); q++) {
+            if (used[q]) {
+                row_of[q] = (int32_t)prog.qubit_orig.size();
+                prog.qubit_orig.push_back((uint32_t)q);
+            }
+        }
+        prog.num_rows = (uint32_t)prog.qubit_orig.size();
+        if (prog.num_rows > kRowMask) {
+            throw std::invalid_argument("too many qubits for the GPU frame sampler");
+        }
+        lower_block(root, 0);
+        flush_detectors();
+        emit(OP_END, 0, 0, 0);
+        prog.num_observables = prog.stats.num_observables;
+        prog.num_measurements = prog.stats.num_measurements;
+        uint64_t ring = std::max<uint64_t>(std::max<uint64_t>(prog.stats.max_lookback, max_results_per_inst), 1);
+        if (ring > (1u << 24)) {
+            throw std::invalid_argument("measurement record window too large for the GPU frame sampler");
+        }
+        prog.ring = (uint32_t)ring;
+        if (prog.num_detectors != prog.stats.num_detectors) {
+            throw std::logic_error("detector count mismatch in lowering");
+        }
+    }
+};
+
+}  // namespace
+
+Program lower(const Circuit &circuit, SampleMode mode) {
+    Lowerer l(circuit, mode);
+    l.run();
+    return std::move(l.prog);
+}
+
+}  // namespace gfs

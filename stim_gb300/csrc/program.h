@@ -1,0 +1,79 @@
+// Device instruction stream of the frame-sampling kernel.
+//
+// The host lowers a parsed circuit into this compact program once per (circuit, mode).  REPEAT blocks stay
+// loops (LOOP_BEGIN / LOOP_END with a repetition count), so a 25-round surface code is ~30 ops per round
+// body instead of the reference's per-iteration re-walk of the instruction list (circuit.h:180-193).
+// Every op acts on "units" (targets, pairs, detectors, terms) that are independent of one another, so
+// the kernel spreads units over threads and puts one CTA barrier between consecutive ops.
+#pragma once
+
+#include <cstdint>
+
+namespace gfs {
+
+enum OpCode : uint32_t {
+    OP_END = 0,
+    OP_LOOP_BEGIN,   // n = body length in ops; a,b = reps lo/hi; c,d = instances per iteration lo/hi
+    OP_LOOP_END,     // n = body length in ops
+    OP_1Q,           // sub = K1_*; pool[a+i] = row
+    OP_2Q,           // sub = K2_*; pool[a+2i], pool[a+2i+1] = rows
+    OP_FEEDBACK,     // pool[a+2i] = lookback, pool[a+2i+1] = row | mask<<24 (1 = x, 2 = z)
+    OP_MEASURE,      // sub = KM_*; pool[a+i] = row; b = first randomization unit
+    OP_RESET,        // sub = KR_*; pool[a+i] = row; b = first randomization unit
+    OP_RECORD_ZERO,  // append n zero results (MPAD, herald slots)
+    OP_MNOISE,       // flip the last n results; b = channel
+    OP_NOISE,        // sub = KN_*; pool[a + i*(1 or 2)] = rows; b = channel
+    OP_CORR_MASK,    // sub = 0 (E: clear the occurred flags first) / 1 (ELSE); b = channel
+    OP_CORR_APPLY,   // pool[a+i] = row | xz<<24
+    OP_HERALD,       // sub = 0 HERALDED_ERASE / 1 HERALDED_PAULI_CHANNEL_1; pool[a+i] = row; b = channel;
+                     // the herald results are the last n results (already zeroed)
+    OP_DETECTORS,    // n detectors; pool[a+i] .. pool[a+i+1] = absolute pool range of lookbacks
+    OP_OBS,          // b = observable index; pool[a+i] = term (rec: k | 1<<31; Pauli: row | X<<30 | Z<<29)
+    OP_EMIT,         // copy the last n results to the measurement output
+};
+
+enum : uint32_t { K1_H_XZ = 0, K1_H_XY, K1_H_YZ, K1_C_XYZ, K1_C_ZYX };
+enum : uint32_t {
+    K2_CX = 0,
+    K2_CY,
+    K2_CZ,
+    K2_XCX,
+    K2_XCY,
+    K2_YCX,
+    K2_YCY,
+    K2_SWAP,
+    K2_ISWAP,
+    K2_CXSWAP,
+    K2_CZSWAP,
+    K2_SWAPCX,
+    K2_SQRT_XX,
+    K2_SQRT_YY,
+    K2_SQRT_ZZ,
+};
+enum : uint32_t { KM_M = 0, KM_MX, KM_MY, KM_MR, KM_MRX, KM_MRY };
+enum : uint32_t { KR_R = 0, KR_RX, KR_RY };
+enum : uint32_t { KN_X = 0, KN_Y, KN_Z, KN_DEP1, KN_PC1, KN_DEP2, KN_PC2 };
+
+struct alignas(16) DevOp {
+    uint32_t code;  // OpCode | sub << 8
+    uint32_t n;
+    uint32_t a, b, c, d;
+    uint64_t inst;  // instance offset of the source instruction within the enclosing loop iteration
+};
+static_assert(sizeof(DevOp) == 32, "DevOp layout");
+
+// A noise channel: hit probability p (gap table) plus the Pauli choice thresholds.
+struct alignas(16) DevChan {
+    uint32_t table;   // offset of T[0..1024] in the table pool
+    uint32_t active;  // p > 0
+    uint32_t always;  // p >= 1
+    float inv_c;
+    uint64_t cum[16];
+};
+
+constexpr uint32_t kFeedbackX = 1, kFeedbackZ = 2;
+constexpr uint32_t kTermRecord = 1u << 31, kTermX = 1u << 30, kTermZ = 1u << 29;
+constexpr uint32_t kRowMask = (1u << 24) - 1;
+constexpr int kMaxLoopDepth = 16;
+
+}  // namespace gfs

@@ -1,0 +1,85 @@
+"""C ABI checks that need no GPU: the library loads, exports every declared symbol, parses circuits
+with the reference's statistics and errors, and refuses to sample without a device (no CPU fallback)."""
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import stim_gb300
+from conftest import GOLDEN_DIR, ROOT, golden_names
+from oracle.oracle import OracleCircuit
+from stim_gb300 import _native, workloads
+
+
+def declared_symbols():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if f.endswith(".h"):
+            text = open(os.path.join(inc, f)).read()
+            names |= set(re.findall(r"\b(gfs_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    L = _native.lib()
+    syms = declared_symbols()
+    assert len(syms) >= 14
+    for name in syms:
+        assert hasattr(L, name), name
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_parse_stats_match_reference(name):
+    g = dict(np.load(os.path.join(GOLDEN_DIR, name + ".npz")))
+    c = stim_gb300.Circuit(str(g["circuit"]))
+    assert c.num_detectors == int(g["num_detectors"])
+    assert c.num_observables == int(g["num_observables"])
+    assert c.num_measurements == int(g["num_measurements"])
+    o = OracleCircuit(str(g["circuit"]))
+    assert c.num_qubits == o.num_qubits
+    assert c.max_lookback == o.max_lookback
+    assert c.num_instructions_unrolled == o.num_instances
+
+
+def test_parse_large_surface_code():
+    c = stim_gb300.Circuit(workloads.code_circuit("surface_code:rotated_memory_z", 25, 25, 0.001))
+    assert (c.num_qubits, c.num_measurements, c.num_detectors, c.num_observables, c.max_lookback) == (
+        1324, 16225, 15600, 1, 1248)
+
+
+@pytest.mark.parametrize("text,err", [
+    ("H 0\nCX 0", ValueError),
+    ("X_ERROR(1.5) 0", ValueError),
+    ("NOT_A_GATE 0", ValueError),
+    ("REPEAT 0 {\nH 0\n}", ValueError),
+    ("REPEAT 2 {\nH 0\n", ValueError),
+    ("}", ValueError),
+    ("H 0 rec[-1]", ValueError),
+    ("CX 0 0", ValueError),
+    ("MPP X0*", ValueError),
+    ("DEPOLARIZE1(0.1, 0.2) 0", ValueError),
+    ("H0", ValueError),
+])
+def test_parse_errors(text, err):
+    with pytest.raises(err):
+        stim_gb300.Circuit(text)
+    with pytest.raises(ValueError):
+        OracleCircuit(text)
+
+
+def test_parse_fuses_like_the_reference():
+    c = stim_gb300.Circuit("H 0\nH 1\nX_ERROR(0.1) 0\nX_ERROR(0.1) 1\nX_ERROR(0.2) 2\nTICK\nTICK\nREPEAT 3 {\nH 0\n}\nH 1")
+    o = OracleCircuit("H 0\nH 1\nX_ERROR(0.1) 0\nX_ERROR(0.1) 1\nX_ERROR(0.2) 2\nTICK\nTICK\nREPEAT 3 {\nH 0\n}\nH 1")
+    assert c.num_instructions_unrolled == o.num_instances == 1 + 1 + 1 + 2 + 3 + 1
+
+
+def test_sampling_without_gpu_raises_instead_of_falling_back():
+    if _native.device_count() > 0:
+        pytest.skip("a CUDA device is present")
+    c = stim_gb300.Circuit("X_ERROR(1) 0\nM 0\nDETECTOR rec[-1]")
+    with pytest.raises((RuntimeError, ValueError)):
+        c.compile_detector_sampler(seed=1)

@@ -1,0 +1,163 @@
+"""Parity of the CUDA path (through the C ABI) with the reference and the oracle.
+
+* golden fixtures: outputs of the reference's own FrameSimulator on the injected stream, bit-exact;
+* larger sizes: the CPU oracle on the same seeds, bit-exact;
+* invariants: chunking, launch shape and stream continuation do not change any bit;
+* noiseless circuits give exactly zero detection events.
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+import stim_gb300
+from conftest import GOLDEN_DIR, golden_names
+from oracle.oracle import OracleCircuit
+from stim_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLDEN_DIR, name + ".npz")))
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_detections_match_reference_golden(name):
+    g = load(name)
+    c = stim_gb300.Circuit(str(g["circuit"]))
+    s = c.compile_detector_sampler(seed=int(g["seed"]))
+    d, o = s.sample(int(g["shots"]), separate_observables=True, bit_packed=True)
+    np.testing.assert_array_equal(d, g["dets"])
+    np.testing.assert_array_equal(o, g["obs"])
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_measurements_match_reference_golden(name):
+    g = load(name)
+    c = stim_gb300.Circuit(str(g["circuit"]))
+    s = c.compile_sampler(skip_reference_sample=True, seed=int(g["seed"]))
+    m = s.sample(int(g["shots"]), bit_packed=True)
+    np.testing.assert_array_equal(m, g["meas"])
+    s2 = c.compile_sampler(reference_sample=g["ref_sample"], seed=int(g["seed"]))
+    m2 = s2.sample(int(g["shots"]), bit_packed=True)
+    np.testing.assert_array_equal(m2, g["meas"] ^ g["ref_sample"][None, :])
+
+
+def _unpack(a, n):
+    return np.unpackbits(a, axis=1, bitorder="little")[:, :n].astype(np.bool_)
+
+
+def test_layout_flags_match_packed_golden():
+    g = load("all_gates_s5")
+    c = stim_gb300.Circuit(str(g["circuit"]))
+    D, O, shots, seed = c.num_detectors, c.num_observables, int(g["shots"]), int(g["seed"])
+    dets = _unpack(g["dets"], D)
+    obs = _unpack(g["obs"], O)
+    cases = [
+        (dict(), dets),
+        (dict(append_observables=True), np.concatenate([dets, obs], axis=1)),
+        (dict(prepend_observables=True), np.concatenate([obs, dets], axis=1)),
+        (dict(prepend_observables=True, append_observables=True), np.concatenate([obs, dets, obs], axis=1)),
+    ]
+    for kw, want in cases:
+        for packed in (False, True):
+            s = c.compile_detector_sampler(seed=seed)
+            got = s.sample(shots, bit_packed=packed, **kw)
+            if packed:
+                got = _unpack(got, want.shape[1])
+            np.testing.assert_array_equal(got, want, err_msg=str((kw, packed)))
+
+
+def test_manual_output_buffers():
+    text = """
+        X_ERROR(1) 0
+        M 0
+        DETECTOR
+        DETECTOR
+        DETECTOR rec[-1]
+        DETECTOR rec[-1]
+        DETECTOR rec[-1]
+        DETECTOR
+        DETECTOR
+        DETECTOR rec[-1]
+        DETECTOR rec[-1]
+        OBSERVABLE_INCLUDE(0) rec[-1]
+    """
+    s = stim_gb300.Circuit(text).compile_detector_sampler()
+    for bad in [np.zeros((17, 8), np.bool_), np.zeros((17, 10), np.bool_), np.zeros((18, 9), np.bool_),
+                np.zeros((17, 9), np.uint8)]:
+        with pytest.raises(ValueError):
+            s.sample(shots=17, dets_out=bad)
+    buf = np.zeros((17, 9), dtype=np.bool_)
+    assert s.sample(shots=17, dets_out=buf) is buf
+    assert np.array_equal(buf, [[0, 0, 1, 1, 1, 0, 0, 1, 1]] * 17)
+    buf = np.zeros((17, 2), dtype=np.uint8)
+    assert s.sample(shots=17, dets_out=buf, bit_packed=True) is buf
+    assert np.array_equal(buf, [[0b10011100, 0b1]] * 17)
+    buf = np.zeros((2, 17), dtype=np.uint8).transpose()
+    assert s.sample(shots=17, dets_out=buf, bit_packed=True) is buf
+    assert np.array_equal(buf, [[0b10011100, 0b1]] * 17)
+    obs = np.zeros((17, 1), dtype=np.bool_)
+    s.sample(shots=17, obs_out=obs)
+    assert obs.all()
+
+
+def test_separate_with_append_raises():
+    s = stim_gb300.Circuit("M 0\nDETECTOR rec[-1]").compile_detector_sampler()
+    with pytest.raises(ValueError):
+        s.sample(10, separate_observables=True, append_observables=True)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+@pytest.mark.parametrize("p", [0.001, 0.005])
+def test_surface_d11_matches_oracle(seed, p):
+    text = workloads.code_circuit("surface_code:rotated_memory_x", 11, 11, p)
+    shots = 8192
+    gd, go = stim_gb300.Circuit(text).compile_detector_sampler(seed=seed).sample(
+        shots, separate_observables=True, bit_packed=True)
+    od, oo, _ = OracleCircuit(text).sample(shots, seed, threads=8)
+    np.testing.assert_array_equal(gd, od)
+    np.testing.assert_array_equal(go, oo)
+
+
+def test_noiseless_surface_d11_gives_zero_detection_events():
+    text = workloads.code_circuit("surface_code:rotated_memory_x", 11, 11, 0.0)
+    d = stim_gb300.Circuit(text).compile_detector_sampler(seed=5).sample(1 << 18, bit_packed=True)
+    assert not d.any()
+
+
+@pytest.mark.parametrize("n,depth,seed", [(64, 200, 21), (128, 200, 22), (256, 200, 23), (512, 200, 24)])
+def test_random_clifford_matches_oracle(n, depth, seed):
+    text = workloads.random_clifford_circuit(n, depth, seed)
+    shots = 2048
+    gd, go = stim_gb300.Circuit(text).compile_detector_sampler(seed=seed).sample(
+        shots, separate_observables=True, bit_packed=True)
+    od, oo, _ = OracleCircuit(text).sample(shots, seed, threads=8)
+    np.testing.assert_array_equal(gd, od)
+    np.testing.assert_array_equal(go, oo)
+
+
+def test_chunking_shape_and_continuation_do_not_change_bits():
+    text = workloads.code_circuit("surface_code:rotated_memory_z", 5, 5, 0.01)
+    c = stim_gb300.Circuit(text)
+    ref = c.compile_detector_sampler(seed=9).sample(4096, bit_packed=True)
+    for shape in [(1, 256), (2, 256), (4, 256), (1, 128), (2, 64)]:
+        s = c.compile_detector_sampler(seed=9)
+        s.set_launch_shape(*shape)
+        np.testing.assert_array_equal(s.sample(4096, bit_packed=True), ref, err_msg=str(shape))
+    s = c.compile_detector_sampler(seed=9)
+    s.set_chunk_shots(384)
+    np.testing.assert_array_equal(s.sample(4096, bit_packed=True), ref)
+    s = c.compile_detector_sampler(seed=9)
+    a = s.sample(1024, bit_packed=True)
+    b = s.sample(3072, bit_packed=True)
+    np.testing.assert_array_equal(np.concatenate([a, b]), ref)
+
+
+def test_lookback_errors_match_reference():
+    with pytest.raises(IndexError):
+        stim_gb300.Circuit("M 0\nDETECTOR rec[-2]").compile_detector_sampler()
+    with pytest.raises(ValueError):
+        stim_gb300.Circuit("M 0\nCX 0 rec[-1]").compile_detector_sampler()
