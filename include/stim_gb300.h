@@ -58,6 +58,14 @@ gfs_status gfs_circuit_stats(const gfs_circuit *c, uint64_t *stats6);
 void gfs_circuit_free(gfs_circuit *c);
 
 /*
+ * Lowers the circuit for `mode` on the host only (no device needed) and reports the program:
+ * info[0] = device ops, [1] = pool words, [2] = compacted qubit rows, [3] = measurement ring rows,
+ * [4] = noise channels, [5] = deepest REPEAT nesting, [6] = shared-memory bytes per 128-shot block,
+ * [7] = detectors.  Fails with the same errors as gfs_sampler_create's lowering step.
+ */
+gfs_status gfs_program_info(const gfs_circuit *c, uint32_t mode, uint64_t *info8);
+
+/*
  * Lowers the circuit for `mode` and uploads it to CUDA device `device`; the random stream starts at
  * shot 0 of `seed` (replaces the sampler constructors, compiled_detector_sampler.pybind.cc:28-32,151-154
  * and compiled_measurement_sampler.pybind.cc:63-83).  Successive sample calls continue the stream.

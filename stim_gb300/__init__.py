@@ -66,6 +66,14 @@ class Circuit:
     def __repr__(self):
         return f"stim_gb300.Circuit({self._text!r})"
 
+    def program_info(self, mode: str = "detections") -> dict:
+        """Lowers the circuit on the host (no GPU needed) and describes the device program."""
+        info = (ctypes.c_uint64 * 8)()
+        m = _native.MODE_MEASUREMENTS if mode == "measurements" else _native.MODE_DETECTIONS
+        check(lib().gfs_program_info(self._h, m, info))
+        keys = ["ops", "pool_words", "rows", "ring", "channels", "loop_depth", "smem_bytes_per_block", "detectors"]
+        return dict(zip(keys, [int(v) for v in info]))
+
     def compile_detector_sampler(self, *, seed=None, device: int = 0) -> "CompiledDetectorSampler":
         return CompiledDetectorSampler(self, seed=seed, device=device)
 

@@ -37,6 +37,7 @@ def _declare(L):
         "gfs_device_count": [ctypes.POINTER(ctypes.c_int)],
         "gfs_circuit_parse": [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(_vp)],
         "gfs_circuit_stats": [_vp, ctypes.POINTER(_u64)],
+        "gfs_program_info": [_vp, ctypes.c_uint32, ctypes.POINTER(_u64)],
         "gfs_sampler_create": [_vp, ctypes.c_uint32, _u64, ctypes.c_int, ctypes.POINTER(_vp)],
         "gfs_sample_detections": [_vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64],
         "gfs_sample_detections_device": [_vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64],

@@ -445,6 +445,24 @@ void gfs_circuit_free(gfs_circuit *c) {
     delete c;
 }
 
+gfs_status gfs_program_info(const gfs_circuit *c, uint32_t mode, uint64_t *info8) {
+    return guarded([&] {
+        if (mode != GFS_MODE_DETECTIONS && mode != GFS_MODE_MEASUREMENTS) {
+            throw std::invalid_argument("unknown sampling mode");
+        }
+        gfs::Program p = gfs::lower(c->circuit, mode == GFS_MODE_MEASUREMENTS ? gfs::SampleMode::MEASUREMENTS
+                                                                           : gfs::SampleMode::DETECTIONS);
+        info8[0] = p.ops.size();
+        info8[1] = p.pool.size();
+        info8[2] = p.num_rows;
+        info8[3] = p.ring;
+        info8[4] = p.chans.size();
+        info8[5] = p.max_loop_depth;
+        info8[6] = gfs::frame_smem_bytes(p.num_rows, p.ring, (uint32_t)p.num_observables, 1);
+        info8[7] = p.num_detectors;
+    });
+}
+
 gfs_status gfs_sampler_create(const gfs_circuit *c, uint32_t mode, uint64_t seed, int device, gfs_sampler **out) {
     *out = nullptr;
     return guarded([&] {

@@ -27,6 +27,8 @@ struct Lowerer {
     std::vector<int32_t> row_of;  // qubit -> row
     std::map<std::vector<double>, uint32_t> chan_cache;
     uint64_t meas_seen = 0;  // results before this point on the first pass through every loop
+    uint64_t mult = 1;       // product of the repetition counts of the enclosing loops
+    uint64_t dets_unrolled = 0;
     uint64_t max_results_per_inst = 0;
 
     // pending detector group
@@ -177,7 +179,7 @@ struct Lowerer {
             prog.pool.insert(prog.pool.end(), pending_dets[i].begin(), pending_dets[i].end());
         }
         prog.pool[base + n] = (uint32_t)prog.pool.size();
-        prog.num_detectors += n;
+        dets_unrolled += (uint64_t)n * mult;
         pending_dets.clear();
     }
 
@@ -747,8 +749,11 @@ struct Lowerer {
                 lb.c = (uint32_t)stride;
                 lb.d = (uint32_t)(stride >> 32);
                 uint64_t seen_before = meas_seen;
+                uint64_t saved_mult = mult;
+                mult = (op.reps && mult > UINT64_MAX / op.reps) ? UINT64_MAX : mult * op.reps;
                 lower_block(body, depth + 1);
                 flush_detectors();
+                mult = saved_mult;
                 uint32_t body_len = (uint32_t)(prog.ops.size() - begin - 1);
                 prog.ops[begin].n = body_len;
                 DevOp &le = emit(OP_LOOP_END, 0, body_len, flat);
@@ -783,6 +788,7 @@ struct Lowerer {
         lower_block(root, 0);
         flush_detectors();
         emit(OP_END, 0, 0, 0);
+        prog.num_detectors = prog.stats.num_detectors;
         prog.num_observables = prog.stats.num_observables;
         prog.num_measurements = prog.stats.num_measurements;
         uint64_t ring = std::max<uint64_t>(std::max<uint64_t>(prog.stats.max_lookback, max_results_per_inst), 1);
@@ -790,7 +796,7 @@ struct Lowerer {
             throw std::invalid_argument("measurement record window too large for the GPU frame sampler");
         }
         prog.ring = (uint32_t)ring;
-        if (prog.num_detectors != prog.stats.num_detectors) {
+        if (dets_unrolled != prog.stats.num_detectors) {
             throw std::logic_error("detector count mismatch in lowering");
         }
     }

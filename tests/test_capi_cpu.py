@@ -83,3 +83,23 @@ def test_sampling_without_gpu_raises_instead_of_falling_back():
     c = stim_gb300.Circuit("X_ERROR(1) 0\nM 0\nDETECTOR rec[-1]")
     with pytest.raises((RuntimeError, ValueError)):
         c.compile_detector_sampler(seed=1)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_lowering_succeeds_on_host(name):
+    g = dict(np.load(os.path.join(GOLDEN_DIR, name + ".npz")))
+    c = stim_gb300.Circuit(str(g["circuit"]))
+    for mode in ("detections", "measurements"):
+        info = c.program_info(mode)
+        assert info["detectors"] == c.num_detectors
+        assert info["rows"] <= c.num_qubits
+        assert info["ring"] >= max(1, c.max_lookback)
+
+
+def test_lowering_keeps_repeat_as_loops():
+    c = stim_gb300.Circuit(workloads.code_circuit("surface_code:rotated_memory_z", 25, 25, 0.001))
+    info = c.program_info()
+    assert info["loop_depth"] == 1
+    assert info["rows"] == 1249
+    assert info["ops"] < 200  # the 24-round body is emitted once, not unrolled
+    assert info["smem_bytes_per_block"] <= 64 * 1024
