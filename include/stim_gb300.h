@@ -101,6 +101,29 @@ gfs_status gfs_sample_detections_device(gfs_sampler *s, uint64_t shots, uint32_t
                                         uint64_t dets_stride, void *obs, uint64_t obs_stride);
 
 /*
+ * Allocation-free variant of gfs_sample_detections_device.  No counterpart in the reference.
+ *
+ * For callers that must not allocate or free device memory while they sample: for example a real-time
+ * decoding loop whose HBM is reserved up front by its own pool allocator, or a loop that cannot afford
+ * cudaMalloc/cudaFree's implicit device synchronization and latency.  Each call allocates nothing:
+ * the frame kernel's scratch (16 bytes per 128-shot block per detector or observable) lives in a
+ * fixed 64 MiB file-scope __device__ array (stim_gb300/csrc/noalloc.cu) that every GPU loading the
+ * library holds until the process exits, and the outputs are the caller's device buffers, as in
+ * gfs_sample_detections_device.  Creating the sampler (gfs_sampler_create) still allocates the lowered
+ * program once, at set-up.
+ *
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress, with that
+ * device current); make that first call before any stream capture.  Circuits needing more than 64 MiB
+ * of scratch for one CTA's slice of shots are rejected with GFS_ERR_INVALID_ARGUMENT.  Larger shot
+ * counts are processed in chunks that fit.  All calls share the array and it keeps the last call's
+ * contents (nothing in it needs to start at zero: every scratch row is written before it is read).
+ * Calls from this process to one device are serialized by a lock; calls that overlap on the GPU by
+ * other means (e.g. another copy of the library in the same process) race on the array.
+ */
+gfs_status gfs_sample_detections_device_noalloc(gfs_sampler *s, uint64_t shots, uint32_t flags, void *dets,
+                                                uint64_t dets_stride, void *obs, uint64_t obs_stride);
+
+/*
  * Device timings (milliseconds, CUDA events on the sampler's stream) of the last sample call:
  * out[0] = frame kernel, out[1] = transpose kernel(s), out[2] = device->host copies, out[3] = whole call.
  * counts[0] = frame-kernel launches, counts[1] = transpose launches.

@@ -14,6 +14,7 @@
 #include "circuit.h"
 #include "kernels.h"
 #include "lower.h"
+#include "noalloc.h"
 
 namespace {
 
@@ -402,6 +403,107 @@ struct gfs_sampler {
     }
 };
 
+namespace {
+
+// Allocation-free detection sampling into caller-owned device buffers: the frame kernel's scratch is the
+// fixed array of noalloc.cu instead of cudaMalloc'd buffers; everything else is as in
+// gfs_sample_detections_device.  Calls on one device are serialized by a process-wide lock.
+void detections_noalloc(gfs_sampler *s, uint64_t shots, uint32_t flags, uint8_t *dets, uint64_t dstride, uint8_t *obs,
+                        uint64_t ostride) {
+    if (s->mode != GFS_MODE_DETECTIONS) {
+        throw std::invalid_argument("sampler was not created in detection mode");
+    }
+    bool packed = flags & GFS_BIT_PACKED;
+    uint64_t D = s->prog.num_detectors, O = s->prog.num_observables;
+    uint64_t nd = D + ((flags & GFS_PREPEND_OBSERVABLES) ? O : 0) + ((flags & GFS_APPEND_OBSERVABLES) ? O : 0);
+    uint64_t drow = packed ? (nd + 7) / 8 : nd;
+    uint64_t orow = packed ? (O + 7) / 8 : O;
+    if (dets && dstride < drow) {
+        throw std::invalid_argument("dets row stride too small");
+    }
+    if (obs && ostride < orow) {
+        throw std::invalid_argument("obs row stride too small");
+    }
+    uint64_t bpc = (uint64_t)s->shape.blocks_per_cta;
+    uint64_t per_block = (D + O) * sizeof(uint4);
+    uint64_t cap_blocks = per_block ? (uint64_t)(gfs::kNoAllocScratchBytes / per_block) : ((uint64_t)1 << 40);
+    cap_blocks = (cap_blocks / bpc) * bpc;
+    if (cap_blocks == 0) {
+        throw std::invalid_argument(
+            "the circuit needs " + std::to_string(per_block * bpc) + " bytes of scratch per " +
+            std::to_string(128 * bpc) + "-shot slice (" + std::to_string(D) + " detectors + " + std::to_string(O) +
+            " observables), more than the " + std::to_string(gfs::kNoAllocScratchBytes) +
+            " bytes the allocation-free entry point holds; use gfs_sample_detections_device instead");
+    }
+    ck(cudaSetDevice(s->device), "cudaSetDevice");
+    std::lock_guard<std::mutex> lock(gfs::noalloc_device_lock(s->device));
+    void *scratch = nullptr;
+    ck(gfs::noalloc_scratch_address(s->device, &scratch), "scratch address");
+    uint4 *det_s = (uint4 *)scratch;
+    uint4 *obs_s = det_s + cap_blocks * D;
+    s->reset_timings();
+    ck(cudaEventRecord(s->ev[0], s->stream), "event");
+    uint64_t done = 0;
+    while (done < shots) {
+        uint64_t cs = std::min<uint64_t>(shots - done, cap_blocks * 128);
+        uint64_t nblk = (cs + 127) / 128;
+        uint64_t nslices = (nblk + bpc - 1) / bpc;
+        gfs::KernelArgs a{};
+        a.ops = (const gfs::DevOp *)s->d_ops.p;
+        a.pool = (const uint32_t *)s->d_pool.p;
+        a.tables = (const uint32_t *)s->d_tables.p;
+        a.chans = (const gfs::DevChan *)s->d_chans.p;
+        a.qubit_orig = (const uint32_t *)s->d_orig.p;
+        a.nrows = s->prog.num_rows;
+        a.ring = s->prog.ring;
+        a.nobs = (uint32_t)O;
+        a.nslices = (uint32_t)nslices;
+        a.ndet = D;
+        a.nmeas = 0;
+        a.seed = s->seed;
+        a.block0 = s->next_block;
+        a.det_out = det_s;
+        a.obs_out = obs_s;
+        a.meas_out = nullptr;
+        a.status = (uint32_t *)s->d_status.p;
+        gfs::LaunchShape shape = s->shape;
+        shape.grid = (int)std::min<uint64_t>((uint64_t)s->shape.grid, nslices);
+        ck(cudaEventRecord(s->ev[1], s->stream), "event");
+        ck(gfs::launch_frame_kernel(a, shape, s->stream), "frame kernel launch");
+        s->n_frame++;
+        ck(cudaEventRecord(s->ev[2], s->stream), "event");
+        uint8_t *dd = dets ? dets + done * dstride : nullptr;
+        uint8_t *od = obs ? obs + done * ostride : nullptr;
+        if (dets) {
+            if ((flags & GFS_PREPEND_OBSERVABLES) && (flags & GFS_APPEND_OBSERVABLES)) {
+                s->transpose(obs_s, O, det_s, D, obs_s, O, nullptr, cs, dd, dstride, packed);
+            } else if (flags & GFS_PREPEND_OBSERVABLES) {
+                s->transpose(obs_s, O, det_s, D, nullptr, 0, nullptr, cs, dd, dstride, packed);
+            } else if (flags & GFS_APPEND_OBSERVABLES) {
+                s->transpose(det_s, D, obs_s, O, nullptr, 0, nullptr, cs, dd, dstride, packed);
+            } else {
+                s->transpose(det_s, D, nullptr, 0, nullptr, 0, nullptr, cs, dd, dstride, packed);
+            }
+        }
+        if (obs) {
+            s->transpose(obs_s, O, nullptr, 0, nullptr, 0, nullptr, cs, od, ostride, packed);
+        }
+        ck(cudaEventRecord(s->ev[3], s->stream), "event");
+        ck(cudaStreamSynchronize(s->stream), "sample");
+        s->t_frame += s->elapsed(1, 2);
+        s->t_transpose += s->elapsed(2, 3);
+        s->check_status();
+        s->next_block += nblk;
+        done += cs;
+    }
+    ck(cudaEventRecord(s->ev[1], s->stream), "event");
+    ck(cudaStreamSynchronize(s->stream), "sample");
+    s->t_total = s->elapsed(0, 1);
+    s->t_copy = 0;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *gfs_last_error(void) {
@@ -497,6 +599,11 @@ gfs_status gfs_sample_detections_device(gfs_sampler *s, uint64_t shots, uint32_t
         }
         s->detections(shots, flags, (uint8_t *)dets, dets_stride, (uint8_t *)obs, obs_stride, true);
     });
+}
+
+gfs_status gfs_sample_detections_device_noalloc(gfs_sampler *s, uint64_t shots, uint32_t flags, void *dets,
+                                                uint64_t dets_stride, void *obs, uint64_t obs_stride) {
+    return guarded([&] { detections_noalloc(s, shots, flags, (uint8_t *)dets, dets_stride, (uint8_t *)obs, obs_stride); });
 }
 
 gfs_status gfs_sample_measurements(gfs_sampler *s, uint64_t shots, uint32_t flags, const uint8_t *ref_sample,
