@@ -259,7 +259,7 @@ def run_gpu(args):
         if k:
             e2e_times.append(time.perf_counter() - t1)
     e2e_s = sum(e2e_times)
-    e2e_value = world * len(e2e_times) * shots * (D + O) / e2e_s / 1e9
+    e2e_value = world * len(e2e_times) * shots * (D + O) / e2e_s / 1e9 if e2e_times else None
 
     acc_bits, rbits, hits = algorithmic_work(text)
     frame_avg_s = statistics.mean(frame_ms) / 1e3

@@ -49,6 +49,14 @@ const char *gfs_last_error(void);
 gfs_status gfs_device_count(int *out);
 
 /*
+ * Device facts used by the runtime: info[0] = SMs, [1] = opt-in shared memory per CTA (bytes),
+ * [2] = shared memory per SM, [3] = pageable host memory access (1 when kernels may write ordinary host
+ * memory, as on Grace-based systems), [4] = that access uses host page tables, [5] = SM clock (kHz),
+ * [6] = compute capability x 10, [7] = L2 bytes.
+ */
+gfs_status gfs_device_info(int device, int64_t *info8);
+
+/*
  * Parses .stim text (replaces stim::Circuit(text), src/stim/circuit/circuit.cc:302-310).
  * stats[0..5] = num_qubits, num_measurements, num_detectors, num_observables, max_lookback,
  * number of instructions with REPEAT unrolled.

@@ -35,6 +35,7 @@ def _declare(L):
     L.gfs_last_error.argtypes = []
     sigs = {
         "gfs_device_count": [ctypes.POINTER(ctypes.c_int)],
+        "gfs_device_info": [ctypes.c_int, ctypes.POINTER(ctypes.c_int64)],
         "gfs_circuit_parse": [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(_vp)],
         "gfs_circuit_stats": [_vp, ctypes.POINTER(_u64)],
         "gfs_program_info": [_vp, ctypes.c_uint32, ctypes.POINTER(_u64)],
@@ -97,6 +98,14 @@ def measure_smem_peak(device: int = 0) -> float:
     v = ctypes.c_double(0)
     check(lib().gfs_measure_smem_peak(int(device), ctypes.byref(v)))
     return v.value
+
+
+def device_info(device: int = 0) -> dict:
+    v = (ctypes.c_int64 * 8)()
+    check(lib().gfs_device_info(int(device), v))
+    keys = ["sms", "smem_per_cta_optin", "smem_per_sm", "pageable_memory_access",
+            "pageable_uses_host_page_tables", "sm_clock_khz", "cc", "l2_bytes"]
+    return dict(zip(keys, [int(x) for x in v]))
 
 
 def device_count() -> int:

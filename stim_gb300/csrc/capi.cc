@@ -522,6 +522,25 @@ gfs_status gfs_device_count(int *out) {
     });
 }
 
+gfs_status gfs_device_info(int device, int64_t *info8) {
+    return guarded([&] {
+        cudaDeviceProp prop;
+        ck(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+        int v = 0;
+        info8[0] = prop.multiProcessorCount;
+        info8[1] = (int64_t)prop.sharedMemPerBlockOptin;
+        info8[2] = (int64_t)prop.sharedMemPerMultiprocessor;
+        ck(cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, device), "attribute");
+        info8[3] = v;
+        ck(cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device), "attribute");
+        info8[4] = v;
+        ck(cudaDeviceGetAttribute(&v, cudaDevAttrClockRate, device), "attribute");
+        info8[5] = v;
+        info8[6] = prop.major * 10 + prop.minor;
+        info8[7] = (int64_t)prop.l2CacheSize;
+    });
+}
+
 gfs_status gfs_circuit_parse(const char *text, size_t len, gfs_circuit **out) {
     *out = nullptr;
     return guarded([&] {
