@@ -12,6 +12,7 @@
 #include <string>
 
 #include "circuit.h"
+#include "gfs_contract.h"
 #include "kernels.h"
 #include "lower.h"
 #include "noalloc.h"
@@ -67,6 +68,10 @@ void upload(DevBuf &b, const std::vector<T> &v, int dev, cudaStream_t s) {
     if (!v.empty()) {
         ck(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), "upload");
     }
+}
+
+uint64_t pad32(uint64_t n) {
+    return (n + 31) & ~(uint64_t)31;
 }
 
 gfs_status fail(gfs_status st, const std::string &msg) {
@@ -128,8 +133,14 @@ struct gfs_sampler {
         }
     }
 
+    // Gap tables go to shared memory when they are small (up to 4 distinct probabilities).
+    uint32_t smem_table_words() const {
+        return prog.tables.size() <= 4 * (GFS_SEG_TRIALS + 1) ? (uint32_t)prog.tables.size() : 0;
+    }
+
     size_t smem_for(int bpc) const {
-        return gfs::frame_smem_bytes(prog.num_rows, prog.ring, (uint32_t)prog.num_observables, bpc);
+        return gfs::frame_smem_bytes(prog.num_rows, prog.ring, (uint32_t)prog.num_observables, bpc,
+                                     smem_table_words());
     }
 
     void choose_shape(int bpc, int threads, int grid) {
@@ -246,6 +257,7 @@ struct gfs_sampler {
         a.obs_out = (uint4 *)obs_tmp.p;
         a.meas_out = (uint4 *)meas_tmp.p;
         a.status = (uint32_t *)d_status.p;
+        a.smem_table_words = smem_table_words();
         gfs::LaunchShape s = shape;
         s.grid = (int)std::min<uint64_t>((uint64_t)shape.grid, nslices);
         ck(gfs::launch_frame_kernel(a, s, stream), "frame kernel launch");
@@ -310,11 +322,12 @@ struct gfs_sampler {
                 dd = dets ? dets + done * dstride : nullptr;
                 od = obs ? obs + done * ostride : nullptr;
             } else {
-                out_tmp.ensure(std::max<uint64_t>(16, cs * (drow + orow)), device);
+                out_tmp.ensure(std::max<uint64_t>(16, cs * (pad32(drow) + pad32(orow))), device);
                 dd = (uint8_t *)out_tmp.p;
-                od = (uint8_t *)out_tmp.p + cs * drow;
+                od = (uint8_t *)out_tmp.p + cs * pad32(drow);
             }
-            uint64_t ds = device_out ? dstride : drow, os = device_out ? ostride : orow;
+            // Staging rows are padded to 32 bytes so the transpose writes whole sectors.
+            uint64_t ds = device_out ? dstride : pad32(drow), os = device_out ? ostride : pad32(orow);
             if (dets) {
                 if ((flags & GFS_PREPEND_OBSERVABLES) && (flags & GFS_APPEND_OBSERVABLES)) {
                     transpose(ot, O, dt, D, ot, O, nullptr, cs, dd, ds, packed);
@@ -332,12 +345,12 @@ struct gfs_sampler {
             ck(cudaEventRecord(ev[3], stream), "event");
             if (!device_out) {
                 if (dets && drow) {
-                    ck(cudaMemcpy2DAsync(dets + done * dstride, dstride, dd, drow, drow, cs, cudaMemcpyDeviceToHost,
+                    ck(cudaMemcpy2DAsync(dets + done * dstride, dstride, dd, ds, drow, cs, cudaMemcpyDeviceToHost,
                                          stream),
                        "copy dets");
                 }
                 if (obs && orow) {
-                    ck(cudaMemcpy2DAsync(obs + done * ostride, ostride, od, orow, orow, cs, cudaMemcpyDeviceToHost,
+                    ck(cudaMemcpy2DAsync(obs + done * ostride, ostride, od, os, orow, cs, cudaMemcpyDeviceToHost,
                                          stream),
                        "copy obs");
                 }
@@ -382,11 +395,13 @@ struct gfs_sampler {
             ck(cudaEventRecord(ev[1], stream), "event");
             run_frame(nblk, next_block);
             ck(cudaEventRecord(ev[2], stream), "event");
-            out_tmp.ensure(std::max<uint64_t>(16, cs * row), device);
-            transpose((const uint4 *)meas_tmp.p, M, nullptr, 0, nullptr, 0, dref, cs, (uint8_t *)out_tmp.p, row, packed);
+            out_tmp.ensure(std::max<uint64_t>(16, cs * pad32(row)), device);
+            transpose((const uint4 *)meas_tmp.p, M, nullptr, 0, nullptr, 0, dref, cs, (uint8_t *)out_tmp.p, pad32(row),
+                      packed);
             ck(cudaEventRecord(ev[3], stream), "event");
             if (row) {
-                ck(cudaMemcpy2DAsync(out + done * stride, stride, out_tmp.p, row, row, cs, cudaMemcpyDeviceToHost, stream),
+                ck(cudaMemcpy2DAsync(out + done * stride, stride, out_tmp.p, pad32(row), row, cs,
+                                     cudaMemcpyDeviceToHost, stream),
                    "copy meas");
             }
             ck(cudaStreamSynchronize(stream), "sample");
@@ -466,6 +481,7 @@ void detections_noalloc(gfs_sampler *s, uint64_t shots, uint32_t flags, uint8_t 
         a.obs_out = obs_s;
         a.meas_out = nullptr;
         a.status = (uint32_t *)s->d_status.p;
+        a.smem_table_words = s->smem_table_words();
         gfs::LaunchShape shape = s->shape;
         shape.grid = (int)std::min<uint64_t>((uint64_t)s->shape.grid, nslices);
         ck(cudaEventRecord(s->ev[1], s->stream), "event");
@@ -579,7 +595,7 @@ gfs_status gfs_program_info(const gfs_circuit *c, uint32_t mode, uint64_t *info8
         info8[3] = p.ring;
         info8[4] = p.chans.size();
         info8[5] = p.max_loop_depth;
-        info8[6] = gfs::frame_smem_bytes(p.num_rows, p.ring, (uint32_t)p.num_observables, 1);
+        info8[6] = gfs::frame_smem_bytes(p.num_rows, p.ring, (uint32_t)p.num_observables, 1, 0);
         info8[7] = p.num_detectors;
     });
 }

@@ -105,8 +105,8 @@ GFS_HD gfs_u32x4 gfs_row_bits(uint64_t seed, uint32_t purpose, uint64_t instance
 typedef struct gfs_stream {
     uint32_t k0, k1, c0, c1, c2, c3base;
     uint32_t group;
-    uint32_t idx;
-    gfs_u32x4 buf;
+    uint32_t left;              /* draws left in b0..b3 */
+    uint32_t b0, b1, b2, b3;    /* next draws, in order (kept in registers: no indexed access) */
 } gfs_stream;
 
 GFS_HD void gfs_stream_init(gfs_stream *s, uint64_t seed, uint32_t purpose, uint64_t instance, uint32_t segment,
@@ -118,16 +118,26 @@ GFS_HD void gfs_stream_init(gfs_stream *s, uint64_t seed, uint32_t purpose, uint
     s->c2 = (uint32_t)instance;
     s->c3base = gfs_c3(purpose, instance, 0);
     s->group = 0;
-    s->idx = 4;
+    s->left = 0;
+    s->b0 = s->b1 = s->b2 = s->b3 = 0;
 }
 
 GFS_HD uint32_t gfs_stream_next(gfs_stream *s) {
-    if (s->idx == 4) {
-        s->buf = gfs_philox(s->k0, s->k1, s->c0, s->c1, s->c2, s->c3base | (s->group & 0xFFFFFu));
+    if (s->left == 0) {
+        gfs_u32x4 r = gfs_philox(s->k0, s->k1, s->c0, s->c1, s->c2, s->c3base | (s->group & 0xFFFFFu));
+        s->b0 = r.v[0];
+        s->b1 = r.v[1];
+        s->b2 = r.v[2];
+        s->b3 = r.v[3];
         s->group++;
-        s->idx = 0;
+        s->left = 4;
     }
-    return s->buf.v[s->idx++];
+    uint32_t out = s->b0;
+    s->b0 = s->b1;
+    s->b1 = s->b2;
+    s->b2 = s->b3;
+    s->left--;
+    return out;
 }
 
 /*

@@ -171,6 +171,15 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
     uint4 *MSK = OCC + B;
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
     const uint32_t *pool = p.pool;
+    // Gap tables are read on every noise hit; keep them in shared memory when the launch reserved room.
+    const uint32_t *tables = p.tables;
+    if (p.smem_table_words) {
+        uint32_t *st = reinterpret_cast<uint32_t *>(MSK + B);
+        for (uint32_t i = tid; i < p.smem_table_words; i += nt) {
+            st[i] = __ldg(p.tables + i);
+        }
+        tables = st;
+    }
 
     for (uint32_t slice = blockIdx.x; slice < p.nslices; slice += gridDim.x) {
         const uint64_t lb0 = (uint64_t)slice * B;
@@ -375,7 +384,7 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                 case OP_NOISE:
                 case OP_HERALD: {
                     const DevChan &ch = p.chans[op.b];
-                    const uint32_t *T = p.tables + ch.table;
+                    const uint32_t *T = tables + ch.table;
                     const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
                     const uint32_t purpose = code == OP_MNOISE ? GFS_P_MNOISE : GFS_P_NOISE;
                     for (uint32_t i = tid; i < nseg * B; i += nt) {
@@ -463,7 +472,7 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                             gfs_stream st;
                             gfs_stream_init(&st, p.seed, GFS_P_NOISE, inst, 0, (uint32_t)(gb0 + blk));
                             int32_t pos = -1;
-                            while ((pos = gfs_next_hit(&st, p.tables + ch.table, ch.inv_c, pos,
+                            while ((pos = gfs_next_hit(&st, tables + ch.table, ch.inv_c, pos,
                                                        (int32_t)GFS_BLOCK_SHOTS, ch.always)) >= 0) {
                                 m[pos >> 5] |= 1u << (pos & 31);
                             }
@@ -556,8 +565,9 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
     }
 }
 
-size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta) {
-    return ((size_t)2 * nrows + ring + nobs + 2) * (size_t)blocks_per_cta * sizeof(uint4);
+size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words) {
+    return ((size_t)2 * nrows + ring + nobs + 2) * (size_t)blocks_per_cta * sizeof(uint4) +
+           (size_t)table_words * sizeof(uint32_t);
 }
 
 template <int B>
@@ -659,12 +669,102 @@ __global__ void __launch_bounds__(256) transpose_kernel(const TransposeArgs t) {
     }
 }
 
+// Bit-packed shot-major output, tiled: a CTA of 256 threads owns (one 128-shot block, 256 concatenated
+// rows).  Each thread loads one row's uint4; each warp ballot-transposes its 32 rows into 4-byte words per
+// shot and stages them in shared memory; then thread pairs write each shot's 32 output bytes.  When the
+// destination row and stride are 16-byte aligned the writes are full 16-byte stores covering whole
+// 32-byte sectors; otherwise the widest aligned stores (8, 4, 2 or 1 bytes) are used.
+__device__ __forceinline__ uint4 load_concat(const TransposeArgs &t, uint64_t blk, uint64_t r, uint64_t total) {
+    uint4 v = zero4();
+    if (r < t.n0) {
+        v = t.src0[blk * t.n0 + r];
+    } else if (r < t.n0 + t.n1) {
+        v = t.src1[blk * t.n1 + (r - t.n0)];
+    } else if (r < total) {
+        v = t.src2[blk * t.n2 + (r - t.n0 - t.n1)];
+    }
+    if (t.xor_rows && r < total && ((t.xor_rows[r >> 3] >> (r & 7)) & 1)) {
+        v = x4(v, make_uint4(~0u, ~0u, ~0u, ~0u));
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(256) transpose_tile_kernel(const TransposeArgs t) {
+    __shared__ uint32_t tile[128][9];  // [shot][4-byte word of the 32-byte chunk], padded against conflicts
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint64_t blk = blockIdx.x;
+    const uint64_t total = t.n0 + t.n1 + t.n2;
+    const uint64_t r0 = (uint64_t)blockIdx.y * 256;
+    const uint4 v = load_concat(t, blk, r0 + tid, total);
+    const uint32_t words[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int w = 0; w < 4; w++) {
+        uint32_t mine = 0;
+#pragma unroll
+        for (int i = 0; i < 32; i++) {
+            uint32_t b = __ballot_sync(0xFFFFFFFFu, (words[w] >> i) & 1u);
+            if (lane == (uint32_t)i) {
+                mine = b;
+            }
+        }
+        tile[w * 32 + lane][warp] = mine;
+    }
+    __syncthreads();
+    const uint32_t s = tid >> 1, half = tid & 1;
+    const uint64_t shot = blk * 128 + s;
+    if (shot >= t.nshots) {
+        return;
+    }
+    const uint64_t row_bytes = (total + 7) / 8;
+    const uint64_t off = r0 / 8 + 16 * half;
+    if (off >= row_bytes) {
+        return;
+    }
+    const uint64_t n = row_bytes - off < 16 ? row_bytes - off : 16;
+    uint8_t *dst = t.out + shot * t.out_stride + off;
+    const uint32_t *src = &tile[s][4 * half];
+    if (n == 16 && ((uintptr_t)dst & 15) == 0) {
+        *reinterpret_cast<uint4 *>(dst) = make_uint4(src[0], src[1], src[2], src[3]);
+    } else if (n == 16 && ((uintptr_t)dst & 7) == 0) {
+        reinterpret_cast<uint2 *>(dst)[0] = make_uint2(src[0], src[1]);
+        reinterpret_cast<uint2 *>(dst)[1] = make_uint2(src[2], src[3]);
+    } else if (((uintptr_t)dst & 3) == 0) {
+        uint64_t k = 0;
+        for (; k + 4 <= n; k += 4) {
+            *reinterpret_cast<uint32_t *>(dst + k) = src[k / 4];
+        }
+        for (; k < n; k++) {
+            dst[k] = (uint8_t)(src[k / 4] >> (8 * (k & 3)));
+        }
+    } else if (((uintptr_t)dst & 1) == 0) {
+        uint64_t k = 0;
+        for (; k + 2 <= n; k += 2) {
+            *reinterpret_cast<uint16_t *>(dst + k) = (uint16_t)(src[k / 4] >> (8 * (k & 3)));
+        }
+        for (; k < n; k++) {
+            dst[k] = (uint8_t)(src[k / 4] >> (8 * (k & 3)));
+        }
+    } else {
+        for (uint64_t k = 0; k < n; k++) {
+            dst[k] = (uint8_t)(src[k / 4] >> (8 * (k & 3)));
+        }
+    }
+}
+
 cudaError_t launch_transpose(const TransposeArgs &args, cudaStream_t stream) {
     uint64_t total = args.n0 + args.n1 + args.n2;
     if (total == 0 || args.nshots == 0) {
         return cudaSuccess;
     }
     uint64_t nblk = (args.nshots + 127) / 128;
+    if (args.bit_packed) {
+        dim3 grid((unsigned)nblk, (unsigned)((total + 255) / 256));
+        if (grid.y > 65535) {
+            return cudaErrorInvalidValue;
+        }
+        transpose_tile_kernel<<<grid, 256, 0, stream>>>(args);
+        return cudaGetLastError();
+    }
     uint64_t ngroups = (total + 31) / 32;
     dim3 grid((unsigned)nblk, (unsigned)((ngroups + 7) / 8));
     if (grid.y > 65535) {
