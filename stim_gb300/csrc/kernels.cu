@@ -159,6 +159,102 @@ __device__ __forceinline__ void apply_pauli_atomic(uint4 *X, uint4 *Z, uint32_t 
     }
 }
 
+// Pauli pattern of a noise hit: bit0 = X on the unit's (first) row, bit1 = Z on it, bits 2-3 the same for
+// the second row of a pair; for measurement flips bit0 = flip.
+__device__ __forceinline__ uint32_t pauli_xz(uint32_t v) {  // 0=I 1=X 2=Y 3=Z
+    return (v == 1 || v == 2 ? 1u : 0u) | (v == 2 || v == 3 ? 2u : 0u);
+}
+
+// Draws the Pauli of one hit, consuming the channel's choice draw when it has one.  DEPOLARIZE1/2 keep
+// the reference's bit layout of 1 + rng() % 3 / % 15 (frame_simulator.inl:663-690).
+__device__ __forceinline__ uint32_t hit_bits(uint32_t code, uint32_t sub, const DevChan &ch, gfs_stream *st) {
+    if (code == OP_MNOISE) {
+        return 1;
+    }
+    switch (sub) {
+        case KN_X:
+            return 1;
+        case KN_Y:
+            return 3;
+        case KN_Z:
+            return 2;
+        case KN_DEP1:
+            return 1 + gfs_choice_uniform(gfs_stream_next(st), 3);
+        case KN_PC1:
+            return pauli_xz(1 + gfs_choice_weighted(gfs_stream_next(st), ch.cum, 3));
+        case KN_DEP2:
+            return 1 + gfs_choice_uniform(gfs_stream_next(st), 15);
+        default: {  // KN_PC2
+            uint32_t v = 1 + gfs_choice_weighted(gfs_stream_next(st), ch.cum, 15);
+            return pauli_xz(v >> 2) | (pauli_xz(v & 3) << 2);
+        }
+    }
+}
+
+template <int B>
+__device__ __forceinline__ void apply_hit(uint32_t code, uint32_t sub, uint32_t n, const uint32_t *pool, uint32_t a,
+                                          uint32_t u, uint32_t blk, uint32_t shot, uint32_t bits, uint4 *X, uint4 *Z,
+                                          uint4 *R, uint32_t rec, uint32_t L) {
+    if (code == OP_MNOISE) {
+        atomic_xor_bit(R, wrap(rec + L - n + u, L) * B + blk, shot);
+        return;
+    }
+    const bool pair = sub == KN_DEP2 || sub == KN_PC2;
+    const uint32_t i1 = __ldg(pool + a + (pair ? 2 * u : u)) * B + blk;
+    if (bits & 1) {
+        atomic_xor_bit(X, i1, shot);
+    }
+    if (bits & 2) {
+        atomic_xor_bit(Z, i1, shot);
+    }
+    if (pair && (bits & 12)) {
+        const uint32_t i2 = __ldg(pool + a + 2 * u + 1) * B + blk;
+        if (bits & 4) {
+            atomic_xor_bit(X, i2, shot);
+        }
+        if (bits & 8) {
+            atomic_xor_bit(Z, i2, shot);
+        }
+    }
+}
+
+// Hit list of one noise op, generated one phase ahead (see frame_kernel).
+constexpr uint32_t kHitCap = 1024;
+struct HitList {
+    uint2 *entries;  // {unit, shot | bits << 8 | blk << 16}
+    uint32_t *count; // [2], alternating per generation
+    uint32_t *overflow;
+};
+
+template <int B>
+__device__ __forceinline__ void generate_hits(const KernelArgs &p, const uint32_t *tables, const DevOp &op,
+                                              uint64_t inst, uint64_t gb0, HitList h, uint32_t par, uint32_t first,
+                                              uint32_t nt) {
+    const uint32_t code = op.code & 0xFFu, sub = op.code >> 8, n = op.n;
+    const DevChan &ch = p.chans[op.b];
+    const uint32_t *T = tables + ch.table;
+    const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
+    const uint32_t purpose = code == OP_MNOISE ? GFS_P_MNOISE : GFS_P_NOISE;
+    for (uint32_t i = first; i < nseg * B; i += nt) {
+        uint32_t g = i / B, blk = i % B;
+        uint32_t u0 = g * GFS_SEG_UNITS;
+        uint32_t nu = min(GFS_SEG_UNITS, n - u0);
+        gfs_stream st;
+        gfs_stream_init(&st, p.seed, purpose, inst, g, (uint32_t)(gb0 + blk));
+        int32_t pos = -1;
+        while ((pos = gfs_next_hit(&st, T, ch.inv_c, pos, (int32_t)(nu * GFS_BLOCK_SHOTS), ch.always)) >= 0) {
+            uint32_t bits = hit_bits(code, sub, ch, &st);
+            uint32_t slot = atomicAdd(h.count + par, 1u);
+            if (slot < kHitCap) {
+                h.entries[slot] = make_uint2(u0 + (uint32_t)pos / GFS_BLOCK_SHOTS,
+                                             ((uint32_t)pos % GFS_BLOCK_SHOTS) | (bits << 8) | (blk << 16));
+            } else {
+                h.overflow[par] = 1;
+            }
+        }
+    }
+}
+
 template <int B>
 __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
     extern __shared__ uint4 sm[];
@@ -173,13 +269,17 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
     const uint32_t *pool = p.pool;
     // Gap tables are read on every noise hit; keep them in shared memory when the launch reserved room.
     const uint32_t *tables = p.tables;
+    uint32_t *st_tables = reinterpret_cast<uint32_t *>(MSK + B);
     if (p.smem_table_words) {
-        uint32_t *st = reinterpret_cast<uint32_t *>(MSK + B);
         for (uint32_t i = tid; i < p.smem_table_words; i += nt) {
-            st[i] = __ldg(p.tables + i);
+            st_tables[i] = __ldg(p.tables + i);
         }
-        tables = st;
+        tables = st_tables;
     }
+    HitList hits;
+    hits.entries = reinterpret_cast<uint2 *>(st_tables + ((p.smem_table_words + 3) & ~3u));
+    hits.count = reinterpret_cast<uint32_t *>(hits.entries + kHitCap);
+    hits.overflow = hits.count + 2;
 
     for (uint32_t slice = blockIdx.x; slice < p.nslices; slice += gridDim.x) {
         const uint64_t lb0 = (uint64_t)slice * B;
@@ -196,9 +296,14 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
         for (uint32_t i = tid; i < B; i += nt) {
             OCC[i] = zero4();
         }
+        if (tid < 4) {
+            hits.count[tid] = 0;  // count[0..1], overflow[0..1]
+        }
         __syncthreads();
 
         uint32_t rec = 0;
+        uint32_t par = 0;      // parity of the hit list the next generation fills
+        bool pregen = false;   // the current op's hits were generated during the previous phase
         uint64_t det_base = 0, meas_base = 0, inst_base = 0;
         int depth = 0;
         uint32_t loop_pc[kMaxLoopDepth + 1];
@@ -381,8 +486,24 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                     break;
 
                 case OP_MNOISE:
-                case OP_NOISE:
-                case OP_HERALD: {
+                case OP_NOISE: {
+                    if (pregen) {
+                        const uint32_t nh = hits.count[par ^ 1];
+                        const bool overflowed = hits.overflow[par ^ 1] != 0;
+                        if (tid == 0) {
+                            hits.count[par] = 0;  // free the other list for the next generation
+                            hits.overflow[par] = 0;
+                        }
+                        if (!overflowed) {
+                            for (uint32_t i = tid; i < nh; i += nt) {
+                                uint2 e = hits.entries[i];
+                                apply_hit<B>(code, sub, n, pool, a, e.x, e.y >> 16, e.y & 0xFFu, (e.y >> 8) & 0xFFu,
+                                             X, Z, R, rec, L);
+                            }
+                            break;
+                        }
+                    }
+                    // Direct mode: walk every segment of this op now.
                     const DevChan &ch = p.chans[op.b];
                     const uint32_t *T = tables + ch.table;
                     const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
@@ -391,73 +512,46 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                         uint32_t g = i / B, blk = i % B;
                         uint32_t u0 = g * GFS_SEG_UNITS;
                         uint32_t nu = min(GFS_SEG_UNITS, n - u0);
-                        int32_t trials = (int32_t)(nu * GFS_BLOCK_SHOTS);
                         gfs_stream st;
                         gfs_stream_init(&st, p.seed, purpose, inst, g, (uint32_t)(gb0 + blk));
                         int32_t pos = -1;
-                        while ((pos = gfs_next_hit(&st, T, ch.inv_c, pos, trials, ch.always)) >= 0) {
+                        while ((pos = gfs_next_hit(&st, T, ch.inv_c, pos, (int32_t)(nu * GFS_BLOCK_SHOTS),
+                                                   ch.always)) >= 0) {
+                            uint32_t bits = hit_bits(code, sub, ch, &st);
+                            apply_hit<B>(code, sub, n, pool, a, u0 + (uint32_t)pos / GFS_BLOCK_SHOTS, blk,
+                                         (uint32_t)pos % GFS_BLOCK_SHOTS, bits, X, Z, R, rec, L);
+                        }
+                    }
+                    break;
+                }
+
+                case OP_HERALD: {
+                    const DevChan &ch = p.chans[op.b];
+                    const uint32_t *T = tables + ch.table;
+                    const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
+                    for (uint32_t i = tid; i < nseg * B; i += nt) {
+                        uint32_t g = i / B, blk = i % B;
+                        uint32_t u0 = g * GFS_SEG_UNITS;
+                        uint32_t nu = min(GFS_SEG_UNITS, n - u0);
+                        gfs_stream st;
+                        gfs_stream_init(&st, p.seed, GFS_P_NOISE, inst, g, (uint32_t)(gb0 + blk));
+                        int32_t pos = -1;
+                        while ((pos = gfs_next_hit(&st, T, ch.inv_c, pos, (int32_t)(nu * GFS_BLOCK_SHOTS),
+                                                   ch.always)) >= 0) {
                             uint32_t u = u0 + (uint32_t)pos / GFS_BLOCK_SHOTS;
                             uint32_t shot = (uint32_t)pos % GFS_BLOCK_SHOTS;
-                            if (code == OP_MNOISE) {
-                                atomic_xor_bit(R, wrap(rec + L - n + u, L) * B + blk, shot);
-                            } else if (code == OP_HERALD) {
-                                uint32_t c = gfs_stream_next(&st);
-                                uint32_t idx = __ldg(pool + a + u) * B + blk;
-                                atomic_or_bit(R, wrap(rec + L - n + u, L) * B + blk, shot);
-                                if (sub == 0) {
-                                    if (c & 1) {
-                                        atomic_xor_bit(X, idx, shot);
-                                    }
-                                    if (c & 2) {
-                                        atomic_xor_bit(Z, idx, shot);
-                                    }
-                                } else {
-                                    apply_pauli_atomic(X, Z, idx, shot, gfs_choice_weighted(c, ch.cum, 4));
+                            uint32_t c = gfs_stream_next(&st);
+                            uint32_t idx = __ldg(pool + a + u) * B + blk;
+                            atomic_or_bit(R, wrap(rec + L - n + u, L) * B + blk, shot);
+                            if (sub == 0) {
+                                if (c & 1) {
+                                    atomic_xor_bit(X, idx, shot);
+                                }
+                                if (c & 2) {
+                                    atomic_xor_bit(Z, idx, shot);
                                 }
                             } else {
-                                switch (sub) {
-                                    case KN_X:
-                                        atomic_xor_bit(X, __ldg(pool + a + u) * B + blk, shot);
-                                        break;
-                                    case KN_Y: {
-                                        uint32_t idx = __ldg(pool + a + u) * B + blk;
-                                        atomic_xor_bit(X, idx, shot);
-                                        atomic_xor_bit(Z, idx, shot);
-                                        break;
-                                    }
-                                    case KN_Z:
-                                        atomic_xor_bit(Z, __ldg(pool + a + u) * B + blk, shot);
-                                        break;
-                                    case KN_DEP1: {
-                                        uint32_t v = 1 + gfs_choice_uniform(gfs_stream_next(&st), 3);
-                                        apply_pauli_atomic(X, Z, __ldg(pool + a + u) * B + blk, shot,
-                                                           v == 1 ? 1 : (v == 2 ? 3 : 2));
-                                        break;
-                                    }
-                                    case KN_PC1: {
-                                        uint32_t v = 1 + gfs_choice_weighted(gfs_stream_next(&st), ch.cum, 3);
-                                        apply_pauli_atomic(X, Z, __ldg(pool + a + u) * B + blk, shot, v);
-                                        break;
-                                    }
-                                    case KN_DEP2: {
-                                        uint32_t v = 1 + gfs_choice_uniform(gfs_stream_next(&st), 15);
-                                        uint32_t i1 = __ldg(pool + a + 2 * u) * B + blk;
-                                        uint32_t i2 = __ldg(pool + a + 2 * u + 1) * B + blk;
-                                        if (v & 1) atomic_xor_bit(X, i1, shot);
-                                        if (v & 2) atomic_xor_bit(Z, i1, shot);
-                                        if (v & 4) atomic_xor_bit(X, i2, shot);
-                                        if (v & 8) atomic_xor_bit(Z, i2, shot);
-                                        break;
-                                    }
-                                    default: {  // KN_PC2
-                                        uint32_t v = 1 + gfs_choice_weighted(gfs_stream_next(&st), ch.cum, 15);
-                                        uint32_t i1 = __ldg(pool + a + 2 * u) * B + blk;
-                                        uint32_t i2 = __ldg(pool + a + 2 * u + 1) * B + blk;
-                                        apply_pauli_atomic(X, Z, i1, shot, v >> 2);
-                                        apply_pauli_atomic(X, Z, i2, shot, v & 3);
-                                        break;
-                                    }
-                                }
+                                apply_pauli_atomic(X, Z, idx, shot, gfs_choice_weighted(c, ch.cum, 4));
                             }
                         }
                     }
@@ -553,6 +647,22 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                     }
                     break;
             }
+            // Look-ahead: when the next op is noise, generate its hits now (noise draws do not depend on the
+            // frames), spread over the threads with the least work in this phase, so the noise op itself
+            // only applies a short hit list.  Not across loop boundaries and not from a noise op's phase.
+            {
+                const bool this_noise = code == OP_NOISE || code == OP_MNOISE;
+                pregen = false;
+                if (!this_noise) {
+                    const DevOp nx = p.ops[pc + 1];
+                    const uint32_t ncode = nx.code & 0xFFu;
+                    if (ncode == OP_NOISE || ncode == OP_MNOISE) {
+                        generate_hits<B>(p, tables, nx, inst_base + nx.inst, gb0, hits, par, nt - 1 - tid, nt);
+                        par ^= 1;
+                        pregen = true;
+                    }
+                }
+            }
             __syncthreads();
             pc++;
         }
@@ -567,7 +677,7 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
 
 size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words) {
     return ((size_t)2 * nrows + ring + nobs + 2) * (size_t)blocks_per_cta * sizeof(uint4) +
-           (size_t)table_words * sizeof(uint32_t);
+           (size_t)((table_words + 3) & ~3u) * sizeof(uint32_t) + kHitCap * sizeof(uint2) + 4 * sizeof(uint32_t);
 }
 
 template <int B>
