@@ -102,4 +102,4 @@ def test_lowering_keeps_repeat_as_loops():
     assert info["loop_depth"] == 1
     assert info["rows"] == 1249
     assert info["ops"] < 200  # the 24-round body is emitted once, not unrolled
-    assert info["smem_bytes_per_block"] <= 64 * 1024
+    assert 3 * info["smem_bytes_per_block"] <= 227 * 1024  # three CTAs per SM
