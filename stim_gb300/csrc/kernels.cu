@@ -218,41 +218,9 @@ __device__ __forceinline__ void apply_hit(uint32_t code, uint32_t sub, uint32_t 
     }
 }
 
-// Hit list of one noise op, generated one phase ahead (see frame_kernel).
-constexpr uint32_t kHitCap = 1024;
-struct HitList {
-    uint2 *entries;  // {unit, shot | bits << 8 | blk << 16}
-    uint32_t *count; // [2], alternating per generation
-    uint32_t *overflow;
-};
-
-template <int B>
-__device__ __forceinline__ void generate_hits(const KernelArgs &p, const uint32_t *tables, const DevOp &op,
-                                              uint64_t inst, uint64_t gb0, HitList h, uint32_t par, uint32_t first,
-                                              uint32_t nt) {
-    const uint32_t code = op.code & 0xFFu, sub = op.code >> 8, n = op.n;
-    const DevChan &ch = p.chans[op.b];
-    const uint32_t *T = tables + ch.table;
-    const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
-    const uint32_t purpose = code == OP_MNOISE ? GFS_P_MNOISE : GFS_P_NOISE;
-    for (uint32_t i = first; i < nseg * B; i += nt) {
-        uint32_t g = i / B, blk = i % B;
-        uint32_t u0 = g * GFS_SEG_UNITS;
-        uint32_t nu = min(GFS_SEG_UNITS, n - u0);
-        gfs_stream st;
-        gfs_stream_init(&st, p.seed, purpose, inst, g, (uint32_t)(gb0 + blk));
-        int32_t pos = -1;
-        while ((pos = gfs_next_hit(&st, T, ch.inv_c, pos, (int32_t)(nu * GFS_BLOCK_SHOTS), ch.always)) >= 0) {
-            uint32_t bits = hit_bits(code, sub, ch, &st);
-            uint32_t slot = atomicAdd(h.count + par, 1u);
-            if (slot < kHitCap) {
-                h.entries[slot] = make_uint2(u0 + (uint32_t)pos / GFS_BLOCK_SHOTS,
-                                             ((uint32_t)pos % GFS_BLOCK_SHOTS) | (bits << 8) | (blk << 16));
-            } else {
-                h.overflow[par] = 1;
-            }
-        }
-    }
+// Hit entries of batched noise ops: unit (17 bits) | shot << 17 | Pauli bits << 24 | block << 28.
+__device__ __forceinline__ uint32_t pack_hit(uint32_t u, uint32_t shot, uint32_t bits, uint32_t blk) {
+    return u | (shot << 17) | (bits << 24) | (blk << 28);
 }
 
 template <int B>
@@ -276,10 +244,10 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
         }
         tables = st_tables;
     }
-    HitList hits;
-    hits.entries = reinterpret_cast<uint2 *>(st_tables + ((p.smem_table_words + 3) & ~3u));
-    hits.count = reinterpret_cast<uint32_t *>(hits.entries + kHitCap);
-    hits.overflow = hits.count + 2;
+    // Hit lists of the current region's batched noise ops, then their counters and overflow flags.
+    uint32_t *hit_list = st_tables + ((p.smem_table_words + 3) & ~3u);
+    uint32_t *hit_count = hit_list + ((p.hit_list_entries * B + 3) & ~3u);
+    uint32_t *hit_overflow = hit_count + kMaxBatchedNoiseOps;
 
     for (uint32_t slice = blockIdx.x; slice < p.nslices; slice += gridDim.x) {
         const uint64_t lb0 = (uint64_t)slice * B;
@@ -296,14 +264,9 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
         for (uint32_t i = tid; i < B; i += nt) {
             OCC[i] = zero4();
         }
-        if (tid < 4) {
-            hits.count[tid] = 0;  // count[0..1], overflow[0..1]
-        }
         __syncthreads();
 
         uint32_t rec = 0;
-        uint32_t par = 0;      // parity of the hit list the next generation fills
-        bool pregen = false;   // the current op's hits were generated during the previous phase
         uint64_t det_base = 0, meas_base = 0, inst_base = 0;
         int depth = 0;
         uint32_t loop_pc[kMaxLoopDepth + 1];
@@ -487,18 +450,15 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
 
                 case OP_MNOISE:
                 case OP_NOISE: {
-                    if (pregen) {
-                        const uint32_t nh = hits.count[par ^ 1];
-                        const bool overflowed = hits.overflow[par ^ 1] != 0;
-                        if (tid == 0) {
-                            hits.count[par] = 0;  // free the other list for the next generation
-                            hits.overflow[par] = 0;
-                        }
-                        if (!overflowed) {
+                    if (op.c) {  // hits generated by the region's OP_NOISE_BATCH
+                        const uint32_t j = op.c - 1;
+                        const uint32_t off = (op.d & 0xFFFFu) * B, cap = (op.d >> 16) * B;
+                        if (!hit_overflow[j]) {
+                            const uint32_t nh = min(hit_count[j], cap);
                             for (uint32_t i = tid; i < nh; i += nt) {
-                                uint2 e = hits.entries[i];
-                                apply_hit<B>(code, sub, n, pool, a, e.x, e.y >> 16, e.y & 0xFFu, (e.y >> 8) & 0xFFu,
-                                             X, Z, R, rec, L);
+                                uint32_t e = hit_list[off + i];
+                                apply_hit<B>(code, sub, n, pool, a, e & 0x1FFFFu, e >> 28, (e >> 17) & 0x7Fu,
+                                             (e >> 24) & 0xFu, X, Z, R, rec, L);
                             }
                             break;
                         }
@@ -552,6 +512,44 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                                 }
                             } else {
                                 apply_pauli_atomic(X, Z, idx, shot, gfs_choice_weighted(c, ch.cum, 4));
+                            }
+                        }
+                    }
+                    break;
+                }
+
+                case OP_NOISE_BATCH: {
+                    if (tid < n) {
+                        hit_count[tid] = 0;
+                        hit_overflow[tid] = 0;
+                    }
+                    __syncthreads();
+                    const uint32_t total = __ldg(pool + a + 4 * n) * B;
+                    for (uint32_t i = tid; i < total; i += nt) {
+                        const uint32_t gf = i / B, blk = i % B;
+                        uint32_t j = 0;
+                        while (j + 1 < n && __ldg(pool + a + 4 * (j + 1) + 3) <= gf) {
+                            j++;
+                        }
+                        const uint32_t g = gf - __ldg(pool + a + 4 * j + 3);
+                        const DevOp nop = p.ops[pc + __ldg(pool + a + 4 * j)];
+                        const uint32_t ncode = nop.code & 0xFFu, nsub = nop.code >> 8;
+                        const DevChan &ch = p.chans[nop.b];
+                        const uint32_t off = (nop.d & 0xFFFFu) * B, cap = (nop.d >> 16) * B;
+                        const uint32_t u0 = g * GFS_SEG_UNITS, nu = min(GFS_SEG_UNITS, nop.n - u0);
+                        gfs_stream st;
+                        gfs_stream_init(&st, p.seed, ncode == OP_MNOISE ? GFS_P_MNOISE : GFS_P_NOISE,
+                                        inst_base + nop.inst, g, (uint32_t)(gb0 + blk));
+                        int32_t pos = -1;
+                        while ((pos = gfs_next_hit(&st, tables + ch.table, ch.inv_c, pos,
+                                                   (int32_t)(nu * GFS_BLOCK_SHOTS), ch.always)) >= 0) {
+                            const uint32_t bits = hit_bits(ncode, nsub, ch, &st);
+                            const uint32_t slot = atomicAdd(hit_count + j, 1u);
+                            if (slot < cap) {
+                                hit_list[off + slot] = pack_hit(u0 + (uint32_t)pos / GFS_BLOCK_SHOTS,
+                                                                (uint32_t)pos % GFS_BLOCK_SHOTS, bits, blk);
+                            } else {
+                                hit_overflow[j] = 1;
                             }
                         }
                     }
@@ -647,22 +645,6 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                     }
                     break;
             }
-            // Look-ahead: when the next op is noise, generate its hits now (noise draws do not depend on the
-            // frames), spread over the threads with the least work in this phase, so the noise op itself
-            // only applies a short hit list.  Not across loop boundaries and not from a noise op's phase.
-            {
-                const bool this_noise = code == OP_NOISE || code == OP_MNOISE;
-                pregen = false;
-                if (!this_noise) {
-                    const DevOp nx = p.ops[pc + 1];
-                    const uint32_t ncode = nx.code & 0xFFu;
-                    if (ncode == OP_NOISE || ncode == OP_MNOISE) {
-                        generate_hits<B>(p, tables, nx, inst_base + nx.inst, gb0, hits, par, nt - 1 - tid, nt);
-                        par ^= 1;
-                        pregen = true;
-                    }
-                }
-            }
             __syncthreads();
             pc++;
         }
@@ -675,9 +657,12 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
     }
 }
 
-size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words) {
+size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words,
+                        uint32_t hit_list_entries) {
     return ((size_t)2 * nrows + ring + nobs + 2) * (size_t)blocks_per_cta * sizeof(uint4) +
-           (size_t)((table_words + 3) & ~3u) * sizeof(uint32_t) + kHitCap * sizeof(uint2) + 4 * sizeof(uint32_t);
+           (size_t)((table_words + 3) & ~3u) * sizeof(uint32_t) +
+           (size_t)((hit_list_entries * blocks_per_cta + 3) & ~3u) * sizeof(uint32_t) +
+           2 * kMaxBatchedNoiseOps * sizeof(uint32_t);
 }
 
 template <int B>

@@ -770,6 +770,109 @@ struct Lowerer {
         }
     }
 
+    // Expected-hit bound for one 128-shot block of a noise op: mean + 6 sigma + 8.
+    static uint32_t hit_capacity(uint64_t trials, double p) {
+        double mean = (double)trials * p;
+        double cap = mean + 6.0 * std::sqrt(mean * (1.0 - p)) + 8.0;
+        return cap > 1e9 ? 1000000000u : (uint32_t)std::ceil(cap);
+    }
+
+    // Hit probability of a noise op's channel (the sum of its weights for multi-outcome channels).
+    double op_probability(const DevOp &op) const {
+        const DevChan &ch = prog.chans[op.b];
+        if (ch.always) {
+            return 1.0;
+        }
+        // 1 - T[1] / 2^32 recovers p to 2^-32; good enough for a capacity bound.
+        return 1.0 - (double)prog.tables[ch.table + 1] / 4294967296.0;
+    }
+
+    // Inserts an OP_NOISE_BATCH at the start of every straight-line region (the body of a loop iteration,
+    // or the code between loop boundaries) that holds noise ops, and rewrites loop body lengths.
+    void insert_noise_batches() {
+        std::vector<DevOp> in;
+        in.swap(prog.ops);
+        std::vector<DevOp> out;
+        std::vector<size_t> open_loops;  // positions of LOOP_BEGIN in `out`
+        size_t i = 0;
+        while (i < in.size()) {
+            uint32_t code = in[i].code & 0xFFu;
+            if (code == OP_LOOP_BEGIN) {
+                open_loops.push_back(out.size());
+                out.push_back(in[i++]);
+                continue;
+            }
+            if (code == OP_LOOP_END) {
+                size_t b = open_loops.back();
+                open_loops.pop_back();
+                uint32_t len = (uint32_t)(out.size() - b - 1);
+                out[b].n = len;
+                DevOp e = in[i++];
+                e.n = len;
+                out.push_back(e);
+                continue;
+            }
+            // region [i, j): until the next loop boundary or the end
+            size_t j = i;
+            while (j < in.size()) {
+                uint32_t c = in[j].code & 0xFFu;
+                if (c == OP_LOOP_BEGIN || c == OP_LOOP_END || c == OP_END) {
+                    break;
+                }
+                j++;
+            }
+            std::vector<size_t> noise;
+            uint64_t total_cap = 0;
+            for (size_t k = i; k < j && noise.size() < kMaxBatchedNoiseOps; k++) {
+                uint32_t c = in[k].code & 0xFFu;
+                if ((c == OP_NOISE || c == OP_MNOISE) && in[k].n <= kMaxBatchUnits) {
+                    uint32_t cap = hit_capacity((uint64_t)in[k].n * GFS_BLOCK_SHOTS, op_probability(in[k]));
+                    if (total_cap + cap > kMaxBatchCapacity) {
+                        continue;
+                    }
+                    total_cap += cap;
+                    noise.push_back(k);
+                }
+            }
+            if (!noise.empty()) {
+                DevOp batch{};
+                batch.code = OP_NOISE_BATCH;
+                batch.n = (uint32_t)noise.size();
+                batch.a = (uint32_t)prog.pool.size();
+                batch.inst = 0;
+                size_t batch_pos = out.size();
+                uint32_t off = 0, seg = 0;
+                for (size_t q = 0; q < noise.size(); q++) {
+                    DevOp &op = in[noise[q]];
+                    uint32_t cap = hit_capacity((uint64_t)op.n * GFS_BLOCK_SHOTS, op_probability(op));
+                    uint32_t pc_off = (uint32_t)(noise[q] - i + 1);  // relative to the batch op
+                    prog.pool.push_back(pc_off);
+                    prog.pool.push_back(off);
+                    prog.pool.push_back(cap);
+                    prog.pool.push_back(seg);
+                    op.c = (uint32_t)q + 1;
+                    op.d = off | (cap << 16);
+                    off += cap;
+                    seg += (op.n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
+                }
+                prog.pool.push_back(seg);  // total segments (per block)
+                batch.b = off;             // entries per block
+                prog.hit_list_entries = std::max(prog.hit_list_entries, off);
+                (void)batch_pos;
+                out.push_back(batch);
+            }
+            for (size_t k = i; k < j; k++) {
+                out.push_back(in[k]);
+            }
+            if (j < in.size() && (in[j].code & 0xFFu) == OP_END) {
+                out.push_back(in[j]);
+                j++;
+            }
+            i = j;
+        }
+        prog.ops.swap(out);
+    }
+
     void run() {
         prog.stats = root.stats();
         std::vector<uint8_t> used(prog.stats.num_qubits + 1, 0);
@@ -788,6 +891,7 @@ struct Lowerer {
         lower_block(root, 0);
         flush_detectors();
         emit(OP_END, 0, 0, 0);
+        insert_noise_batches();
         prog.num_detectors = prog.stats.num_detectors;
         prog.num_observables = prog.stats.num_observables;
         prog.num_measurements = prog.stats.num_measurements;

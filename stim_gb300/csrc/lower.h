@@ -23,6 +23,7 @@ struct Program {
     uint64_t num_observables = 0;
     uint64_t num_measurements = 0;
     uint32_t max_loop_depth = 0;
+    uint32_t hit_list_entries = 0;  // largest region hit list, entries per 128-shot block
     CircuitStats stats;
 };
 

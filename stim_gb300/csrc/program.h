@@ -30,6 +30,9 @@ enum OpCode : uint32_t {
     OP_DETECTORS,    // n detectors; pool[a+i] .. pool[a+i+1] = absolute pool range of lookbacks
     OP_OBS,          // b = observable index; pool[a+i] = term (rec: k | 1<<31; Pauli: row | X<<30 | Z<<29)
     OP_EMIT,         // copy the last n results to the measurement output
+    OP_NOISE_BATCH,  // generate the hits of the n noise ops of this straight-line region into their
+                     // shared-memory hit lists; pool[a + 4j ..] = {pc offset, list offset, capacity,
+                     // segment prefix} per op j (capacities and offsets per 128-shot block)
 };
 
 enum : uint32_t { K1_H_XZ = 0, K1_H_XY, K1_H_YZ, K1_C_XYZ, K1_C_ZYX };
@@ -75,5 +78,9 @@ constexpr uint32_t kFeedbackX = 1, kFeedbackZ = 2;
 constexpr uint32_t kTermRecord = 1u << 31, kTermX = 1u << 30, kTermZ = 1u << 29;
 constexpr uint32_t kRowMask = (1u << 24) - 1;
 constexpr int kMaxLoopDepth = 16;
+constexpr uint32_t kMaxBatchedNoiseOps = 32;     // noise ops per region whose hits are generated in a batch
+constexpr uint32_t kMaxBatchUnits = 1u << 17;    // units of a batched op (hit entries hold 17-bit units)
+constexpr uint32_t kMaxBatchCapacity = 2048;     // hit-list entries of a region, per 128-shot block
+// A noise op whose hits were generated by the region's OP_NOISE_BATCH carries c = its index + 1.
 
 }  // namespace gfs
