@@ -342,26 +342,46 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                     break;
 
                 case OP_2Q:
+                    if (sub == K2_CX || sub == K2_CZ) {
+                        // Two independent pairs per iteration: both pairs' loads are in flight together.
+                        const uint32_t items = n * B;
+                        for (uint32_t i = tid; i < items; i += 2 * nt) {
+                            const uint32_t i2b = i + nt;
+                            const bool two = i2b < items;
+                            const uint32_t ua = i / B, ba = i % B;
+                            const uint32_t ub = two ? i2b / B : ua, bb = two ? i2b % B : ba;
+                            const uint32_t a1 = __ldg(pool + a + 2 * ua) * B + ba, a2 = __ldg(pool + a + 2 * ua + 1) * B + ba;
+                            const uint32_t b1 = __ldg(pool + a + 2 * ub) * B + bb, b2 = __ldg(pool + a + 2 * ub + 1) * B + bb;
+                            uint4 az1 = Z[a1], az2 = Z[a2], ax1 = X[a1], ax2 = X[a2];
+                            uint4 bz1 = Z[b1], bz2 = Z[b2], bx1 = X[b1], bx2 = X[b2];
+                            if (sub == K2_CX) {
+                                Z[a1] = x4(az1, az2);
+                                X[a2] = x4(ax2, ax1);
+                                if (two) {
+                                    Z[b1] = x4(bz1, bz2);
+                                    X[b2] = x4(bx2, bx1);
+                                }
+                            } else {
+                                Z[a1] = x4(az1, ax2);
+                                Z[a2] = x4(az2, ax1);
+                                if (two) {
+                                    Z[b1] = x4(bz1, bx2);
+                                    Z[b2] = x4(bz2, bx1);
+                                }
+                            }
+                        }
+                        break;
+                    }
                     for (uint32_t i = tid; i < n * B; i += nt) {
                         uint32_t u = i / B, blk = i % B;
                         uint32_t i1 = __ldg(pool + a + 2 * u) * B + blk;
                         uint32_t i2 = __ldg(pool + a + 2 * u + 1) * B + blk;
-                        if (sub == K2_CX) {
-                            uint4 z1 = Z[i1], z2 = Z[i2], x1 = X[i1], x2 = X[i2];
-                            Z[i1] = x4(z1, z2);
-                            X[i2] = x4(x2, x1);
-                        } else if (sub == K2_CZ) {
-                            uint4 z1 = Z[i1], z2 = Z[i2], x1 = X[i1], x2 = X[i2];
-                            Z[i1] = x4(z1, x2);
-                            Z[i2] = x4(z2, x1);
-                        } else {
-                            uint4 x1 = X[i1], z1 = Z[i1], x2 = X[i2], z2 = Z[i2];
-                            rule2v(sub, x1, z1, x2, z2);
-                            X[i1] = x1;
-                            Z[i1] = z1;
-                            X[i2] = x2;
-                            Z[i2] = z2;
-                        }
+                        uint4 x1 = X[i1], z1 = Z[i1], x2 = X[i2], z2 = Z[i2];
+                        rule2v(sub, x1, z1, x2, z2);
+                        X[i1] = x1;
+                        Z[i1] = z1;
+                        X[i2] = x2;
+                        Z[i2] = z2;
                     }
                     break;
 
@@ -525,14 +545,22 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                     }
                     __syncthreads();
                     const uint32_t total = __ldg(pool + a + 4 * n) * B;
+                    // A thread's segment index only grows, so the op it belongs to is tracked incrementally.
+                    uint32_t j = 0, seg_lo = 0, seg_hi = n > 1 ? __ldg(pool + a + 4 + 3) : 0xFFFFFFFFu;
+                    DevOp nop = p.ops[pc + __ldg(pool + a)];
                     for (uint32_t i = tid; i < total; i += nt) {
                         const uint32_t gf = i / B, blk = i % B;
-                        uint32_t j = 0;
-                        while (j + 1 < n && __ldg(pool + a + 4 * (j + 1) + 3) <= gf) {
+                        bool moved = false;
+                        while (gf >= seg_hi) {
                             j++;
+                            seg_lo = seg_hi;
+                            seg_hi = j + 1 < n ? __ldg(pool + a + 4 * (j + 1) + 3) : 0xFFFFFFFFu;
+                            moved = true;
                         }
-                        const uint32_t g = gf - __ldg(pool + a + 4 * j + 3);
-                        const DevOp nop = p.ops[pc + __ldg(pool + a + 4 * j)];
+                        if (moved) {
+                            nop = p.ops[pc + __ldg(pool + a + 4 * j)];
+                        }
+                        const uint32_t g = gf - seg_lo;
                         const uint32_t ncode = nop.code & 0xFFu, nsub = nop.code >> 8;
                         const DevChan &ch = p.chans[nop.b];
                         const uint32_t off = (nop.d & 0xFFFFu) * B, cap = (nop.d >> 16) * B;
@@ -544,7 +572,17 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                         while ((pos = gfs_next_hit(&st, tables + ch.table, ch.inv_c, pos,
                                                    (int32_t)(nu * GFS_BLOCK_SHOTS), ch.always)) >= 0) {
                             const uint32_t bits = hit_bits(ncode, nsub, ch, &st);
-                            const uint32_t slot = atomicAdd(hit_count + j, 1u);
+                            // Warp-aggregated slot allocation: one shared atomic per (warp, op).
+                            const uint32_t active = __activemask();
+                            const uint32_t same = __match_any_sync(active, j);
+                            const uint32_t lane = tid & 31u;
+                            const uint32_t leader = (uint32_t)__ffs(same) - 1u;
+                            uint32_t base = 0;
+                            if (lane == leader) {
+                                base = atomicAdd(hit_count + j, (uint32_t)__popc(same));
+                            }
+                            base = __shfl_sync(same, base, (int)leader);
+                            const uint32_t slot = base + (uint32_t)__popc(same & ((1u << lane) - 1u));
                             if (slot < cap) {
                                 hit_list[off + slot] = pack_hit(u0 + (uint32_t)pos / GFS_BLOCK_SHOTS,
                                                                 (uint32_t)pos % GFS_BLOCK_SHOTS, bits, blk);
