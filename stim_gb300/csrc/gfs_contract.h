@@ -20,21 +20,24 @@
  *                   (adjacent fusable instructions fused exactly as the reference parser does)
  *   unit        a target (1-qubit channels), a target pair (2-qubit channels), a measurement
  *               result (noisy measurements, heralds), or the single unit of E/ELSE_CORRELATED_ERROR
- *   segment     units [8g, 8g+8) x the 128 shots of a block; trial tau = (u - 8g) * 128 + shot
+ *   unit row    one unit x the 128 shots of a block: 128 Bernoulli trials, trial t = shot t of the block
  *
  *   Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",
  *   SC'11) with key (lo32(seed), hi32(seed)) and counter
- *       c0 = b, c1 = unit-or-segment, c2 = lo32(i), c3 = purpose<<28 | (hi bits of i)<<20 | draw group
+ *       c0 = b, c1 = unit, quad or qubit, c2 = lo32(i), c3 = purpose<<28 | (bits 32..39 of i)<<20 | group
  *
- *   RESET   purpose 1: z of qubit q at the start of a shot = Philox(b, q, 0, 1<<28)
- *   RAND    purpose 2: the randomized row of result/target r of instance i = Philox(b, r, i, ...)
- *   NOISE   purpose 3: a sequential stream of 32-bit draws per segment, 4 per Philox call
- *   MNOISE  purpose 4: the same for measurement-result flips (M(p), MR(p), MPP(p), ...)
+ *   RESET       purpose 1: z of qubit q at the start of a shot = Philox(b, q, 0, 1<<28)
+ *   RAND        purpose 2: the randomized row of result/target r of instance i = Philox(b, r, i, 2<<28)
+ *   NOISE       purpose 3: first draws; word k of Philox(b, u >> 2, i, 3<<28) is the first draw of unit u
+ *                          with u & 3 == k (one Philox call serves a quad of four units)
+ *   NOISE_UNIT  purpose 4: follow-up draws of unit u: words 0..3 of Philox(b, u, i, 4<<28 | g), g = 0, 1, ...
+ *   MNOISE / MNOISE_UNIT  purposes 5 / 6: the same for measurement-result flips (M(p), MR(p), MPP(p), ...)
  *
- *   A segment's hits: pos = -1; repeat { pos += 1 + G(next draw); if pos >= trials: stop; hit(pos);
- *   if the channel picks a Pauli: choice = next draw }.  G(u) = max{k : u < T[k]} with
+ *   The hits of a unit row: pos = G(first draw); while pos < 128 { hit(pos) [+ one follow-up draw for
+ *   the Pauli, when the channel chooses one]; room = 127 - pos; if room == 0 stop; w = next follow-up
+ *   draw; if w < T[room] stop; pos += 1 + G(w) }, with G(u) = max{k : u < T[k]} (capped at 128) and
  *   T[k] = floor((1-p)^k * 2^32) computed in 64-bit fixed point, so P(G >= k) = (1-p)^k.
- *   p == 0 draws nothing and hits nothing; p >= 1 hits every trial without gap draws.
+ *   p == 0 draws nothing and hits nothing; p >= 1 hits every trial, with no gap draws.
  */
 #ifndef GFS_CONTRACT_H
 #define GFS_CONTRACT_H
@@ -51,13 +54,15 @@
 #endif
 
 #define GFS_BLOCK_SHOTS 128u
-#define GFS_SEG_UNITS 8u
-#define GFS_SEG_TRIALS (GFS_BLOCK_SHOTS * GFS_SEG_UNITS)
+#define GFS_QUAD 4u                           /* units sharing one Philox call for their first draws */
+#define GFS_TABLE_LEN (GFS_BLOCK_SHOTS + 1u) /* T[0..128] */
 
 #define GFS_P_RESET 1u
 #define GFS_P_RAND 2u
 #define GFS_P_NOISE 3u
-#define GFS_P_MNOISE 4u
+#define GFS_P_NOISE_UNIT 4u
+#define GFS_P_MNOISE 5u
+#define GFS_P_MNOISE_UNIT 6u
 
 typedef struct gfs_u32x4 {
     uint32_t v[4];
@@ -140,14 +145,19 @@ GFS_HD uint32_t gfs_stream_next(gfs_stream *s) {
     return out;
 }
 
+/* First draws of the four units 4q..4q+3 of a noise instruction instance in one block. */
+GFS_HD gfs_u32x4 gfs_first_draws(uint64_t seed, uint32_t purpose, uint64_t instance, uint32_t quad, uint32_t block) {
+    return gfs_philox((uint32_t)seed, (uint32_t)(seed >> 32), block, quad, (uint32_t)instance,
+                      gfs_c3(purpose, instance, 0));
+}
+
 /*
- * Gap lookup.  `table` holds T[1..GFS_SEG_TRIALS] (index 0 unused).  `est` is any starting guess;
- * the two walks below make the answer the unique k with u < T[k] (T[0] = 2^32) and u >= T[k+1],
- * capped at GFS_SEG_TRIALS, whatever the guess was.
+ * G(u) = max{k <= maxk : u < T[k]} (T[0] = 2^32).  `est` is any starting guess; the two walks make the
+ * answer exact whatever the guess.  `table` holds T[0..GFS_BLOCK_SHOTS] (index 0 unused).
  */
-GFS_HD uint32_t gfs_gap_fixup(uint32_t u, const uint32_t *table, int32_t est) {
-    int32_t k = est < 0 ? 0 : (est > (int32_t)GFS_SEG_TRIALS ? (int32_t)GFS_SEG_TRIALS : est);
-    while (k < (int32_t)GFS_SEG_TRIALS && u < table[k + 1]) {
+GFS_HD uint32_t gfs_gap_fixup(uint32_t u, const uint32_t *table, int32_t est, int32_t maxk) {
+    int32_t k = est < 0 ? 0 : (est > maxk ? maxk : est);
+    while (k < maxk && u < table[k + 1]) {
         k++;
     }
     while (k > 0 && u >= table[k]) {
@@ -156,24 +166,7 @@ GFS_HD uint32_t gfs_gap_fixup(uint32_t u, const uint32_t *table, int32_t est) {
     return (uint32_t)k;
 }
 
-/*
- * Next hit of a segment after position `pos` (start with pos = -1), or -1 when the segment has no
- * further hits.  `always` marks p >= 1 (every trial hits, no draws); `inv_c` = 1 / -log2(1-p) only
- * seeds the lookup, so host and device may compute it with different log2 approximations.
- */
-GFS_HD int32_t gfs_next_hit(gfs_stream *s, const uint32_t *table, float inv_c, int32_t pos, int32_t trials,
-                            int always) {
-    if (always) {
-        return pos + 1 < trials ? pos + 1 : -1;
-    }
-    int32_t room = trials - pos - 1; /* a gap >= room leaves the segment */
-    if (room <= 0) {
-        return -1;
-    }
-    uint32_t u = gfs_stream_next(s);
-    if (u < table[room]) {
-        return -1;
-    }
+GFS_HD int32_t gfs_gap_estimate(uint32_t u, float inv_c) {
 #if defined(__CUDA_ARCH__)
     float lg = __log2f((float)u + 0.5f);
 #else
@@ -183,11 +176,26 @@ GFS_HD int32_t gfs_next_hit(gfs_stream *s, const uint32_t *table, float inv_c, i
     if (!(e >= 0.0f)) { /* also catches NaN */
         e = 0.0f;
     }
-    if (e > (float)GFS_SEG_TRIALS) {
-        e = (float)GFS_SEG_TRIALS;
+    if (e > (float)GFS_BLOCK_SHOTS) {
+        e = (float)GFS_BLOCK_SHOTS;
     }
-    uint32_t g = gfs_gap_fixup(u, table, (int32_t)e);
-    return pos + 1 + (int32_t)g;
+    return (int32_t)e;
+}
+
+/* Position of the first hit of a unit row from its first draw; GFS_BLOCK_SHOTS when there is none. */
+GFS_HD uint32_t gfs_first_hit(uint32_t u, const uint32_t *table, float inv_c) {
+    if (u < table[GFS_BLOCK_SHOTS]) {
+        return GFS_BLOCK_SHOTS;
+    }
+    return gfs_gap_fixup(u, table, gfs_gap_estimate(u, inv_c), (int32_t)GFS_BLOCK_SHOTS - 1);
+}
+
+/* Gap before the next hit when `room` trials remain (room >= 1); returns room when there is none. */
+GFS_HD uint32_t gfs_next_gap(uint32_t w, const uint32_t *table, float inv_c, uint32_t room) {
+    if (w < table[room]) {
+        return room;
+    }
+    return gfs_gap_fixup(w, table, gfs_gap_estimate(w, inv_c), (int32_t)room - 1);
 }
 
 /* Choice helpers. */
@@ -206,7 +214,7 @@ GFS_HD uint32_t gfs_choice_weighted(uint32_t c, const uint64_t *cum, uint32_t n)
 
 #if !defined(__CUDA_ARCH__)
 /*
- * Host-only: the threshold table T[0..GFS_SEG_TRIALS] for probability p in (0, 1).
+ * Host-only: the threshold table T[0..GFS_BLOCK_SHOTS] for probability p in (0, 1).
  * (1-p) is converted once to 0.64 fixed point; powers are formed by 64x64->128 multiplies,
  * so every platform computes the same table from the same double p.
  */
@@ -223,7 +231,7 @@ static inline void gfs_build_gap_table(double p, uint32_t *table) {
     }
     uint64_t A = UINT64_MAX;
     table[0] = UINT32_MAX;
-    for (uint32_t k = 1; k <= GFS_SEG_TRIALS; k++) {
+    for (uint32_t k = 1; k <= GFS_BLOCK_SHOTS; k++) {
         A = (uint64_t)(((unsigned __int128)A * (unsigned __int128)Q) >> 64);
         table[k] = (uint32_t)(A >> 32);
     }

@@ -150,29 +150,18 @@ __device__ __forceinline__ void rule2v(uint32_t sub, uint4 &x1, uint4 &z1, uint4
     rule2(sub, x1.w, z1.w, x2.w, z2.w);
 }
 
-__device__ __forceinline__ void apply_pauli_atomic(uint4 *X, uint4 *Z, uint32_t idx, uint32_t shot, uint32_t v) {
-    if (v == 1 || v == 2) {
-        atomic_xor_bit(X, idx, shot);
-    }
-    if (v == 2 || v == 3) {
-        atomic_xor_bit(Z, idx, shot);
-    }
-}
-
 // Pauli pattern of a noise hit: bit0 = X on the unit's (first) row, bit1 = Z on it, bits 2-3 the same for
-// the second row of a pair; for measurement flips bit0 = flip.
+// the second row of a pair; for measurement flips (KN_FLIP) bit0 = flip.
 __device__ __forceinline__ uint32_t pauli_xz(uint32_t v) {  // 0=I 1=X 2=Y 3=Z
     return (v == 1 || v == 2 ? 1u : 0u) | (v == 2 || v == 3 ? 2u : 0u);
 }
 
 // Draws the Pauli of one hit, consuming the channel's choice draw when it has one.  DEPOLARIZE1/2 keep
 // the reference's bit layout of 1 + rng() % 3 / % 15 (frame_simulator.inl:663-690).
-__device__ __forceinline__ uint32_t hit_bits(uint32_t code, uint32_t sub, const DevChan &ch, gfs_stream *st) {
-    if (code == OP_MNOISE) {
-        return 1;
-    }
-    switch (sub) {
+__device__ __forceinline__ uint32_t hit_bits(uint32_t kind, const DevChan &ch, gfs_stream *st) {
+    switch (kind) {
         case KN_X:
+        case KN_FLIP:
             return 1;
         case KN_Y:
             return 3;
@@ -191,40 +180,231 @@ __device__ __forceinline__ uint32_t hit_bits(uint32_t code, uint32_t sub, const 
     }
 }
 
-template <int B>
-__device__ __forceinline__ void apply_hit(uint32_t code, uint32_t sub, uint32_t n, const uint32_t *pool, uint32_t a,
-                                          uint32_t u, uint32_t blk, uint32_t shot, uint32_t bits, uint4 *X, uint4 *Z,
-                                          uint4 *R, uint32_t rec, uint32_t L) {
-    if (code == OP_MNOISE) {
-        atomic_xor_bit(R, wrap(rec + L - n + u, L) * B + blk, shot);
-        return;
+__device__ __forceinline__ void set_bit4(uint4 &m, uint32_t pos) {
+    const uint32_t b = 1u << (pos & 31), w = pos >> 5;
+    m.x ^= w == 0 ? b : 0u;
+    m.y ^= w == 1 ? b : 0u;
+    m.z ^= w == 2 ? b : 0u;
+    m.w ^= w == 3 ? b : 0u;
+}
+
+// The hits of one unit row (the 128 shots of a block), following gfs_contract.h: `first` is the unit's
+// word of its quad's first-draw Philox call; follow-up draws come from the unit's own stream.
+// f(pos, stream) is called for each hit.  Returns the number of hits.
+template <typename F>
+__device__ __forceinline__ uint32_t walk_unit(uint32_t first, const DevChan &ch, const uint32_t *T, uint64_t seed,
+                                              uint32_t purpose_unit, uint64_t inst, uint32_t unit, uint32_t block,
+                                              F f) {
+    uint32_t pos = ch.always ? 0u : gfs_first_hit(first, T, ch.inv_c);
+    if (pos >= GFS_BLOCK_SHOTS) {
+        return 0;
     }
-    const bool pair = sub == KN_DEP2 || sub == KN_PC2;
-    const uint32_t i1 = __ldg(pool + a + (pair ? 2 * u : u)) * B + blk;
-    if (bits & 1) {
-        atomic_xor_bit(X, i1, shot);
-    }
-    if (bits & 2) {
-        atomic_xor_bit(Z, i1, shot);
-    }
-    if (pair && (bits & 12)) {
-        const uint32_t i2 = __ldg(pool + a + 2 * u + 1) * B + blk;
-        if (bits & 4) {
-            atomic_xor_bit(X, i2, shot);
+    gfs_stream st;
+    gfs_stream_init(&st, seed, purpose_unit, inst, unit, block);
+    uint32_t count = 0;
+    for (;;) {
+        f(pos, &st);
+        count++;
+        if (pos + 1 >= GFS_BLOCK_SHOTS) {
+            break;
         }
-        if (bits & 8) {
-            atomic_xor_bit(Z, i2, shot);
+        const uint32_t room = GFS_BLOCK_SHOTS - 1 - pos;
+        const uint32_t gap = ch.always ? 0u : gfs_next_gap(gfs_stream_next(&st), T, ch.inv_c, room);
+        if (gap >= room) {
+            break;
+        }
+        pos += 1 + gap;
+    }
+    return count;
+}
+
+struct Masks {
+    uint4 x1, z1, x2, z2;
+};
+
+// Noise masks of one unit row; returns false when the row has no hit (the common case at small p).
+__device__ __forceinline__ bool unit_masks(uint32_t first, uint32_t kind, const DevChan &ch, const uint32_t *T,
+                                           uint64_t seed, uint32_t purpose_unit, uint64_t inst, uint32_t unit,
+                                           uint32_t block, Masks &m) {
+    m.x1 = m.z1 = m.x2 = m.z2 = zero4();
+    return walk_unit(first, ch, T, seed, purpose_unit, inst, unit, block, [&](uint32_t pos, gfs_stream *st) {
+               const uint32_t bits = hit_bits(kind, ch, st);
+               if (bits & 1) set_bit4(m.x1, pos);
+               if (bits & 2) set_bit4(m.z1, pos);
+               if (bits & 4) set_bit4(m.x2, pos);
+               if (bits & 8) set_bit4(m.z2, pos);
+           }) != 0;
+}
+
+__device__ __forceinline__ uint32_t word_of(const gfs_u32x4 &v, uint32_t k) {
+    return k == 0 ? v.v[0] : k == 1 ? v.v[1] : k == 2 ? v.v[2] : v.v[3];
+}
+
+__device__ __forceinline__ void atomic_xor4(uint4 *base, uint32_t idx, uint4 m) {
+    uint32_t *w = reinterpret_cast<uint32_t *>(base + idx);
+    if (m.x) atomicXor(w + 0, m.x);
+    if (m.y) atomicXor(w + 1, m.y);
+    if (m.z) atomicXor(w + 2, m.z);
+    if (m.w) atomicXor(w + 3, m.w);
+}
+
+// A noise channel fused into a gate op: DevOp c (after the gate) / d (before it).
+struct Fused {
+    const DevChan *ch;  // null when absent
+    uint32_t kind;
+    uint64_t inst;
+};
+
+__device__ __forceinline__ Fused decode_fused(const KernelArgs &p, uint32_t v, uint64_t inst) {
+    Fused f;
+    const uint32_t c = v & kFusedChanMask;
+    f.ch = c ? &p.chans[c - 1] : nullptr;
+    f.kind = (v >> 20) & 0xFu;
+    f.inst = inst + (int64_t)(int8_t)(v >> 24);
+    return f;
+}
+
+// Applies the one-qubit frame rule of a K1_* gate.
+__device__ __forceinline__ void rule1(uint32_t sub, uint4 &x, uint4 &z) {
+    switch (sub) {
+        case K1_H_XZ: {
+            uint4 t = x;
+            x = z;
+            z = t;
+            break;
+        }
+        case K1_H_XY:
+            z = x4(z, x);
+            break;
+        case K1_H_YZ:
+            x = x4(x, z);
+            break;
+        case K1_C_XYZ:
+            x = x4(x, z);
+            z = x4(z, x);
+            break;
+        default:  // K1_C_ZYX
+            z = x4(z, x);
+            x = x4(x, z);
+            break;
+    }
+}
+
+// Gate op with noise fused before and/or after it.  The op's units are its instruction's units (the
+// lowering fuses only single-run instructions whose noise targets are the same list), so the noise of
+// unit u is keyed exactly as the standalone noise instruction would be.  A thread takes a quad of four
+// units, whose first draws come from one Philox call per fused channel, and updates their rows in
+// registers: no atomics, no extra phase.
+template <int B>
+__device__ __forceinline__ void fused_gate(const KernelArgs &p, const DevOp &op, uint32_t code, uint32_t sub,
+                                           uint64_t inst, uint64_t gb0, const uint32_t *tables, uint4 *X, uint4 *Z,
+                                           uint4 *R, uint32_t rec, uint32_t L, uint32_t tid, uint32_t nt) {
+    const uint32_t n = op.n, a = op.a;
+    const Fused pre = decode_fused(p, op.d, inst), post = decode_fused(p, op.c, inst);
+    const bool pair = code == OP_2Q;
+    const uint32_t nquads = (n + GFS_QUAD - 1) / GFS_QUAD;
+    for (uint32_t item = tid; item < nquads * B; item += nt) {
+        const uint32_t q = item / B, blk = item % B;
+        const uint32_t block = (uint32_t)(gb0 + blk);
+        gfs_u32x4 fpre{}, fpost{};
+        if (pre.ch) {
+            fpre = gfs_first_draws(p.seed, GFS_P_NOISE, pre.inst, q, block);
+        }
+        if (post.ch) {
+            fpost = gfs_first_draws(p.seed, GFS_P_NOISE, post.inst, q, block);
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < GFS_QUAD; k++) {
+            const uint32_t u = q * GFS_QUAD + k;
+            if (u >= n) {
+                break;
+            }
+            const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
+            const uint32_t i2 = pair ? __ldg(p.pool + a + 2 * u + 1) * B + blk : i1;
+            uint4 x1 = X[i1], z1 = Z[i1];
+            uint4 x2 = zero4(), z2 = zero4();
+            if (pair) {
+                x2 = X[i2];
+                z2 = Z[i2];
+            }
+            Masks m;
+            if (pre.ch && unit_masks(word_of(fpre, k), pre.kind, *pre.ch, tables + pre.ch->table, p.seed,
+                                     GFS_P_NOISE_UNIT, pre.inst, u, block, m)) {
+                x1 = x4(x1, m.x1);
+                z1 = x4(z1, m.z1);
+                x2 = x4(x2, m.x2);
+                z2 = x4(z2, m.z2);
+            }
+            if (code == OP_1Q) {
+                rule1(sub, x1, z1);
+            } else if (code == OP_2Q) {
+                rule2v(sub, x1, z1, x2, z2);
+            } else {
+                const uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, op.b + u, block));
+                if (code == OP_MEASURE) {
+                    const uint32_t slot = wrap(rec + u, L) * B + blk;
+                    switch (sub) {
+                        case KM_M:
+                            R[slot] = x1;
+                            z1 = r;
+                            break;
+                        case KM_MX:
+                            R[slot] = z1;
+                            x1 = r;
+                            break;
+                        case KM_MY:
+                            R[slot] = x4(x1, z1);
+                            x1 = x4(x4(x1, z1), r);
+                            z1 = r;
+                            break;
+                        case KM_MR:
+                            R[slot] = x1;
+                            x1 = zero4();
+                            z1 = r;
+                            break;
+                        case KM_MRX:
+                            R[slot] = z1;
+                            z1 = zero4();
+                            x1 = r;
+                            break;
+                        default:  // KM_MRY
+                            R[slot] = x4(x1, z1);
+                            z1 = r;
+                            x1 = r;
+                            break;
+                    }
+                } else {  // OP_RESET
+                    if (sub == KR_R) {
+                        x1 = zero4();
+                        z1 = r;
+                    } else if (sub == KR_RX) {
+                        x1 = r;
+                        z1 = zero4();
+                    } else {
+                        x1 = r;
+                        z1 = r;
+                    }
+                }
+            }
+            if (post.ch && unit_masks(word_of(fpost, k), post.kind, *post.ch, tables + post.ch->table, p.seed,
+                                      GFS_P_NOISE_UNIT, post.inst, u, block, m)) {
+                x1 = x4(x1, m.x1);
+                z1 = x4(z1, m.z1);
+                x2 = x4(x2, m.x2);
+                z2 = x4(z2, m.z2);
+            }
+            X[i1] = x1;
+            Z[i1] = z1;
+            if (pair) {
+                X[i2] = x2;
+                Z[i2] = z2;
+            }
         }
     }
 }
 
-// Hit entries of batched noise ops: unit (17 bits) | shot << 17 | Pauli bits << 24 | block << 28.
-__device__ __forceinline__ uint32_t pack_hit(uint32_t u, uint32_t shot, uint32_t bits, uint32_t blk) {
-    return u | (shot << 17) | (bits << 24) | (blk << 28);
-}
-
 template <int B>
-__global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
+__global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
     extern __shared__ uint4 sm[];
     const uint32_t nr = p.nrows, L = p.ring, NO = p.nobs;
     uint4 *X = sm;
@@ -235,7 +415,7 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
     uint4 *MSK = OCC + B;
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
     const uint32_t *pool = p.pool;
-    // Gap tables are read on every noise hit; keep them in shared memory when the launch reserved room.
+    // Gap tables are read on every noise draw; keep them in shared memory when the launch reserved room.
     const uint32_t *tables = p.tables;
     uint32_t *st_tables = reinterpret_cast<uint32_t *>(MSK + B);
     if (p.smem_table_words) {
@@ -244,10 +424,6 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
         }
         tables = st_tables;
     }
-    // Hit lists of the current region's batched noise ops, then their counters and overflow flags.
-    uint32_t *hit_list = st_tables + ((p.smem_table_words + 3) & ~3u);
-    uint32_t *hit_count = hit_list + ((p.hit_list_entries * B + 3) & ~3u);
-    uint32_t *hit_overflow = hit_count + kMaxBatchedNoiseOps;
 
     for (uint32_t slice = blockIdx.x; slice < p.nslices; slice += gridDim.x) {
         const uint64_t lb0 = (uint64_t)slice * B;
@@ -310,6 +486,16 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                 continue;
             }
 
+            if ((code == OP_1Q || code == OP_2Q || code == OP_MEASURE || code == OP_RESET) && (op.c | op.d)) {
+                fused_gate<B>(p, op, code, sub, inst, gb0, tables, X, Z, R, rec, L, tid, nt);
+                if (code == OP_MEASURE) {
+                    rec = wrap(rec + n, L);
+                }
+                __syncthreads();
+                pc++;
+                continue;
+            }
+
             switch (code) {
                 case OP_1Q:
                     for (uint32_t i = tid; i < n * B; i += nt) {
@@ -327,15 +513,10 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                             case K1_H_YZ:
                                 X[idx] = x4(x, z);
                                 break;
-                            case K1_C_XYZ:
-                                x = x4(x, z);
+                            default:
+                                rule1(sub, x, z);
                                 X[idx] = x;
-                                Z[idx] = x4(z, x);
-                                break;
-                            default:  // K1_C_ZYX
-                                z = x4(z, x);
                                 Z[idx] = z;
-                                X[idx] = x4(x, z);
                                 break;
                         }
                     }
@@ -468,38 +649,44 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                     rec = wrap(rec + n, L);
                     break;
 
-                case OP_MNOISE:
-                case OP_NOISE: {
-                    if (op.c) {  // hits generated by the region's OP_NOISE_BATCH
-                        const uint32_t j = op.c - 1;
-                        const uint32_t off = (op.d & 0xFFFFu) * B, cap = (op.d >> 16) * B;
-                        if (!hit_overflow[j]) {
-                            const uint32_t nh = min(hit_count[j], cap);
-                            for (uint32_t i = tid; i < nh; i += nt) {
-                                uint32_t e = hit_list[off + i];
-                                apply_hit<B>(code, sub, n, pool, a, e & 0x1FFFFu, e >> 28, (e >> 17) & 0x7Fu,
-                                             (e >> 24) & 0xFu, X, Z, R, rec, L);
-                            }
-                            break;
-                        }
-                    }
-                    // Direct mode: walk every segment of this op now.
+                case OP_NOISE:
+                case OP_MNOISE: {
+                    // Standalone noise: quads of units; rows may repeat within an instruction, so the
+                    // (rare) nonzero masks are applied with shared atomics.
                     const DevChan &ch = p.chans[op.b];
                     const uint32_t *T = tables + ch.table;
-                    const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
-                    const uint32_t purpose = code == OP_MNOISE ? GFS_P_MNOISE : GFS_P_NOISE;
-                    for (uint32_t i = tid; i < nseg * B; i += nt) {
-                        uint32_t g = i / B, blk = i % B;
-                        uint32_t u0 = g * GFS_SEG_UNITS;
-                        uint32_t nu = min(GFS_SEG_UNITS, n - u0);
-                        gfs_stream st;
-                        gfs_stream_init(&st, p.seed, purpose, inst, g, (uint32_t)(gb0 + blk));
-                        int32_t pos = -1;
-                        while ((pos = gfs_next_hit(&st, T, ch.inv_c, pos, (int32_t)(nu * GFS_BLOCK_SHOTS),
-                                                   ch.always)) >= 0) {
-                            uint32_t bits = hit_bits(code, sub, ch, &st);
-                            apply_hit<B>(code, sub, n, pool, a, u0 + (uint32_t)pos / GFS_BLOCK_SHOTS, blk,
-                                         (uint32_t)pos % GFS_BLOCK_SHOTS, bits, X, Z, R, rec, L);
+                    const bool meas = code == OP_MNOISE;
+                    const bool pair = !meas && (sub == KN_DEP2 || sub == KN_PC2);
+                    const uint32_t kind = meas ? KN_FLIP : sub;
+                    const uint32_t nquads = (n + GFS_QUAD - 1) / GFS_QUAD;
+                    for (uint32_t item = tid; item < nquads * B; item += nt) {
+                        const uint32_t q = item / B, blk = item % B;
+                        const uint32_t block = (uint32_t)(gb0 + blk);
+                        const gfs_u32x4 first =
+                            gfs_first_draws(p.seed, meas ? GFS_P_MNOISE : GFS_P_NOISE, inst, q, block);
+#pragma unroll
+                        for (uint32_t k = 0; k < GFS_QUAD; k++) {
+                            const uint32_t u = q * GFS_QUAD + k;
+                            if (u >= n) {
+                                break;
+                            }
+                            Masks m;
+                            if (!unit_masks(word_of(first, k), kind, ch, T, p.seed,
+                                            meas ? GFS_P_MNOISE_UNIT : GFS_P_NOISE_UNIT, inst, u, block, m)) {
+                                continue;
+                            }
+                            if (meas) {
+                                atomic_xor4(R, wrap(rec + L - n + u, L) * B + blk, m.x1);
+                                continue;
+                            }
+                            const uint32_t i1 = __ldg(pool + a + (pair ? 2 * u : u)) * B + blk;
+                            atomic_xor4(X, i1, m.x1);
+                            atomic_xor4(Z, i1, m.z1);
+                            if (pair) {
+                                const uint32_t i2 = __ldg(pool + a + 2 * u + 1) * B + blk;
+                                atomic_xor4(X, i2, m.x2);
+                                atomic_xor4(Z, i2, m.z2);
+                            }
                         }
                     }
                     break;
@@ -508,87 +695,26 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                 case OP_HERALD: {
                     const DevChan &ch = p.chans[op.b];
                     const uint32_t *T = tables + ch.table;
-                    const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
-                    for (uint32_t i = tid; i < nseg * B; i += nt) {
-                        uint32_t g = i / B, blk = i % B;
-                        uint32_t u0 = g * GFS_SEG_UNITS;
-                        uint32_t nu = min(GFS_SEG_UNITS, n - u0);
-                        gfs_stream st;
-                        gfs_stream_init(&st, p.seed, GFS_P_NOISE, inst, g, (uint32_t)(gb0 + blk));
-                        int32_t pos = -1;
-                        while ((pos = gfs_next_hit(&st, T, ch.inv_c, pos, (int32_t)(nu * GFS_BLOCK_SHOTS),
-                                                   ch.always)) >= 0) {
-                            uint32_t u = u0 + (uint32_t)pos / GFS_BLOCK_SHOTS;
-                            uint32_t shot = (uint32_t)pos % GFS_BLOCK_SHOTS;
-                            uint32_t c = gfs_stream_next(&st);
-                            uint32_t idx = __ldg(pool + a + u) * B + blk;
-                            atomic_or_bit(R, wrap(rec + L - n + u, L) * B + blk, shot);
-                            if (sub == 0) {
-                                if (c & 1) {
-                                    atomic_xor_bit(X, idx, shot);
-                                }
-                                if (c & 2) {
-                                    atomic_xor_bit(Z, idx, shot);
-                                }
-                            } else {
-                                apply_pauli_atomic(X, Z, idx, shot, gfs_choice_weighted(c, ch.cum, 4));
+                    const uint32_t nquads = (n + GFS_QUAD - 1) / GFS_QUAD;
+                    for (uint32_t item = tid; item < nquads * B; item += nt) {
+                        const uint32_t q = item / B, blk = item % B;
+                        const uint32_t block = (uint32_t)(gb0 + blk);
+                        const gfs_u32x4 first = gfs_first_draws(p.seed, GFS_P_NOISE, inst, q, block);
+                        for (uint32_t k = 0; k < GFS_QUAD; k++) {
+                            const uint32_t u = q * GFS_QUAD + k;
+                            if (u >= n) {
+                                break;
                             }
-                        }
-                    }
-                    break;
-                }
-
-                case OP_NOISE_BATCH: {
-                    if (tid < n) {
-                        hit_count[tid] = 0;
-                        hit_overflow[tid] = 0;
-                    }
-                    __syncthreads();
-                    const uint32_t total = __ldg(pool + a + 4 * n) * B;
-                    // A thread's segment index only grows, so the op it belongs to is tracked incrementally.
-                    uint32_t j = 0, seg_lo = 0, seg_hi = n > 1 ? __ldg(pool + a + 4 + 3) : 0xFFFFFFFFu;
-                    DevOp nop = p.ops[pc + __ldg(pool + a)];
-                    for (uint32_t i = tid; i < total; i += nt) {
-                        const uint32_t gf = i / B, blk = i % B;
-                        bool moved = false;
-                        while (gf >= seg_hi) {
-                            j++;
-                            seg_lo = seg_hi;
-                            seg_hi = j + 1 < n ? __ldg(pool + a + 4 * (j + 1) + 3) : 0xFFFFFFFFu;
-                            moved = true;
-                        }
-                        if (moved) {
-                            nop = p.ops[pc + __ldg(pool + a + 4 * j)];
-                        }
-                        const uint32_t g = gf - seg_lo;
-                        const uint32_t ncode = nop.code & 0xFFu, nsub = nop.code >> 8;
-                        const DevChan &ch = p.chans[nop.b];
-                        const uint32_t off = (nop.d & 0xFFFFu) * B, cap = (nop.d >> 16) * B;
-                        const uint32_t u0 = g * GFS_SEG_UNITS, nu = min(GFS_SEG_UNITS, nop.n - u0);
-                        gfs_stream st;
-                        gfs_stream_init(&st, p.seed, ncode == OP_MNOISE ? GFS_P_MNOISE : GFS_P_NOISE,
-                                        inst_base + nop.inst, g, (uint32_t)(gb0 + blk));
-                        int32_t pos = -1;
-                        while ((pos = gfs_next_hit(&st, tables + ch.table, ch.inv_c, pos,
-                                                   (int32_t)(nu * GFS_BLOCK_SHOTS), ch.always)) >= 0) {
-                            const uint32_t bits = hit_bits(ncode, nsub, ch, &st);
-                            // Warp-aggregated slot allocation: one shared atomic per (warp, op).
-                            const uint32_t active = __activemask();
-                            const uint32_t same = __match_any_sync(active, j);
-                            const uint32_t lane = tid & 31u;
-                            const uint32_t leader = (uint32_t)__ffs(same) - 1u;
-                            uint32_t base = 0;
-                            if (lane == leader) {
-                                base = atomicAdd(hit_count + j, (uint32_t)__popc(same));
-                            }
-                            base = __shfl_sync(same, base, (int)leader);
-                            const uint32_t slot = base + (uint32_t)__popc(same & ((1u << lane) - 1u));
-                            if (slot < cap) {
-                                hit_list[off + slot] = pack_hit(u0 + (uint32_t)pos / GFS_BLOCK_SHOTS,
-                                                                (uint32_t)pos % GFS_BLOCK_SHOTS, bits, blk);
-                            } else {
-                                hit_overflow[j] = 1;
-                            }
+                            const uint32_t idx = __ldg(pool + a + u) * B + blk;
+                            const uint32_t slot = wrap(rec + L - n + u, L) * B + blk;
+                            walk_unit(word_of(first, k), ch, T, p.seed, GFS_P_NOISE_UNIT, inst, u, block,
+                                      [&](uint32_t pos, gfs_stream *st) {
+                                          const uint32_t c = gfs_stream_next(st);
+                                          atomic_or_bit(R, slot, pos);
+                                          const uint32_t v = sub == 0 ? (c & 3u) : pauli_xz(gfs_choice_weighted(c, ch.cum, 4));
+                                          if (v & 1) atomic_xor_bit(X, idx, pos);
+                                          if (v & 2) atomic_xor_bit(Z, idx, pos);
+                                      });
                         }
                     }
                     break;
@@ -597,18 +723,16 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                 case OP_CORR_MASK: {
                     const DevChan &ch = p.chans[op.b];
                     for (uint32_t blk = tid; blk < (uint32_t)B; blk += nt) {
-                        uint32_t m[4] = {0, 0, 0, 0};
+                        Masks m;
+                        m.x1 = zero4();
                         if (ch.active) {
-                            gfs_stream st;
-                            gfs_stream_init(&st, p.seed, GFS_P_NOISE, inst, 0, (uint32_t)(gb0 + blk));
-                            int32_t pos = -1;
-                            while ((pos = gfs_next_hit(&st, tables + ch.table, ch.inv_c, pos,
-                                                       (int32_t)GFS_BLOCK_SHOTS, ch.always)) >= 0) {
-                                m[pos >> 5] |= 1u << (pos & 31);
-                            }
+                            const uint32_t block = (uint32_t)(gb0 + blk);
+                            const gfs_u32x4 first = gfs_first_draws(p.seed, GFS_P_NOISE, inst, 0, block);
+                            unit_masks(first.v[0], KN_X, ch, tables + ch.table, p.seed, GFS_P_NOISE_UNIT, inst, 0,
+                                       block, m);
                         }
                         uint4 occ = sub == 0 ? zero4() : OCC[blk];
-                        uint4 mk = make_uint4(m[0] & ~occ.x, m[1] & ~occ.y, m[2] & ~occ.z, m[3] & ~occ.w);
+                        uint4 mk = make_uint4(m.x1.x & ~occ.x, m.x1.y & ~occ.y, m.x1.z & ~occ.z, m.x1.w & ~occ.w);
                         OCC[blk] = make_uint4(occ.x | mk.x, occ.y | mk.y, occ.z | mk.z, occ.w | mk.w);
                         MSK[blk] = mk;
                     }
@@ -661,11 +785,7 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
                                 v = x4(v, X[idx]);
                             }
                         }
-                        uint32_t *o = reinterpret_cast<uint32_t *>(O + (size_t)op.b * B + blk);
-                        if (v.x) atomicXor(o + 0, v.x);
-                        if (v.y) atomicXor(o + 1, v.y);
-                        if (v.z) atomicXor(o + 2, v.z);
-                        if (v.w) atomicXor(o + 3, v.w);
+                        atomic_xor4(O, op.b * B + blk, v);
                     }
                     break;
 
@@ -695,12 +815,9 @@ __global__ void __launch_bounds__(256) frame_kernel(const KernelArgs p) {
     }
 }
 
-size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words,
-                        uint32_t hit_list_entries) {
+size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words) {
     return ((size_t)2 * nrows + ring + nobs + 2) * (size_t)blocks_per_cta * sizeof(uint4) +
-           (size_t)((table_words + 3) & ~3u) * sizeof(uint32_t) +
-           (size_t)((hit_list_entries * blocks_per_cta + 3) & ~3u) * sizeof(uint32_t) +
-           2 * kMaxBatchedNoiseOps * sizeof(uint32_t);
+           (size_t)((table_words + 3) & ~3u) * sizeof(uint32_t);
 }
 
 template <int B>

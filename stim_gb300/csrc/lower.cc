@@ -74,7 +74,7 @@ struct Lowerer {
         ch.inv_c = 0;
         if (ch.active && !ch.always) {
             ch.table = (uint32_t)prog.tables.size();
-            prog.tables.resize(prog.tables.size() + GFS_SEG_TRIALS + 1);
+            prog.tables.resize(prog.tables.size() + GFS_TABLE_LEN);
             gfs_build_gap_table(p, prog.tables.data() + ch.table);
             ch.inv_c = gfs_inv_c(p);
         }
@@ -493,6 +493,158 @@ struct Lowerer {
         emit_results_tail(op, result, inst);
     }
 
+    // ---- noise fused into adjacent gates ----
+    struct Fuse {
+        const Instruction *pre = nullptr;   // noise instruction just before the gate (instance inst - 1)
+        const Instruction *post = nullptr;  // noise instruction just after it (instance inst + 1)
+    };
+
+    static bool noise_1q(gfs_gate g) {
+        return g == GFS_X_ERROR || g == GFS_Y_ERROR || g == GFS_Z_ERROR || g == GFS_DEPOLARIZE1 ||
+               g == GFS_PAULI_CHANNEL_1;
+    }
+    static bool noise_2q(gfs_gate g) {
+        return g == GFS_DEPOLARIZE2 || g == GFS_PAULI_CHANNEL_2;
+    }
+    static bool gate_1q_fusable(gfs_gate g) {
+        switch (g) {
+            case GFS_H: case GFS_H_NXZ: case GFS_SQRT_Y: case GFS_SQRT_Y_DAG: case GFS_S: case GFS_S_DAG:
+            case GFS_H_XY: case GFS_H_NXY: case GFS_SQRT_X: case GFS_SQRT_X_DAG: case GFS_H_YZ: case GFS_H_NYZ:
+            case GFS_C_XYZ: case GFS_C_NXYZ: case GFS_C_XNYZ: case GFS_C_XYNZ: case GFS_C_ZYX: case GFS_C_NZYX:
+            case GFS_C_ZNYX: case GFS_C_ZYNX: case GFS_M: case GFS_MX: case GFS_MY: case GFS_MR: case GFS_MRX:
+            case GFS_MRY: case GFS_R: case GFS_RX: case GFS_RY:
+                return true;
+            default:
+                return false;
+        }
+    }
+    static bool gate_2q_fusable(gfs_gate g) {
+        switch (g) {
+            case GFS_CX: case GFS_CY: case GFS_CZ: case GFS_XCX: case GFS_XCY: case GFS_YCX: case GFS_YCY:
+            case GFS_SWAP: case GFS_ISWAP: case GFS_ISWAP_DAG: case GFS_CXSWAP: case GFS_SWAPCX: case GFS_CZSWAP:
+            case GFS_SQRT_XX: case GFS_SQRT_XX_DAG: case GFS_SQRT_YY: case GFS_SQRT_YY_DAG: case GFS_SQRT_ZZ:
+            case GFS_SQRT_ZZ_DAG:
+                return true;
+            default:
+                return false;
+        }
+    }
+
+    static double noise_p(const Instruction &n) {
+        if (n.gate == GFS_PAULI_CHANNEL_1 || n.gate == GFS_PAULI_CHANNEL_2) {
+            double p = 0;
+            for (double w : n.args) p += w;
+            return p;
+        }
+        return n.args.empty() ? 0.0 : n.args[0];
+    }
+
+    // Whether noise instruction `n` may be fused into gate instruction `g` (same units, distinct rows).
+    bool fusable(const Instruction &n, const Instruction &g) const {
+        if (!(noise_p(n) > 0)) {
+            return false;
+        }
+        bool one = noise_1q(n.gate) && gate_1q_fusable(g.gate);
+        bool two = noise_2q(n.gate) && gate_2q_fusable(g.gate);
+        if (!one && !two) {
+            return false;
+        }
+        if (n.targets.size() != g.targets.size()) {
+            return false;
+        }
+        std::unordered_set<uint32_t> seen;
+        for (size_t k = 0; k < g.targets.size(); k++) {
+            uint32_t gt = g.targets[k] & ~GFS_T_INVERTED, nt = n.targets[k];
+            if (gt != nt || (gt & (GFS_T_RECORD | GFS_T_SWEEP | GFS_T_COMBINER))) {
+                return false;
+            }
+            if (!seen.insert(gt).second) {
+                return false;
+            }
+        }
+        return true;
+    }
+
+    uint32_t fused_word(const Instruction *n, int delta) {
+        if (!n) {
+            return 0;
+        }
+        uint32_t kind;
+        std::vector<double> weights;
+        switch (n->gate) {
+            case GFS_X_ERROR: kind = KN_X; break;
+            case GFS_Y_ERROR: kind = KN_Y; break;
+            case GFS_Z_ERROR: kind = KN_Z; break;
+            case GFS_DEPOLARIZE1: kind = KN_DEP1; break;
+            case GFS_DEPOLARIZE2: kind = KN_DEP2; break;
+            case GFS_PAULI_CHANNEL_1: kind = KN_PC1; weights = n->args; break;
+            default: kind = KN_PC2; weights = n->args; break;
+        }
+        uint32_t ch = channel(noise_p(*n), weights);
+        if (ch + 1 > kFusedChanMask) {
+            throw std::invalid_argument("too many distinct noise channels for the GPU frame sampler");
+        }
+        return (ch + 1) | (kind << 20) | ((uint32_t)(uint8_t)(int8_t)delta << 24);
+    }
+
+    // Emits a gate instruction with fused noise as a single op.
+    void lower_fused(const Instruction &op, uint64_t inst, const Fuse &f) {
+        std::vector<uint32_t> rows;
+        for (auto t : op.targets) {
+            rows.push_back(row(t));
+        }
+        uint32_t code, sub;
+        uint32_t n = (uint32_t)rows.size();
+        gfs_gate g = op.gate;
+        if (gate_2q_fusable(g)) {
+            code = OP_2Q;
+            n /= 2;
+            switch (g) {
+                case GFS_CX: sub = K2_CX; break;
+                case GFS_CY: sub = K2_CY; break;
+                case GFS_CZ: sub = K2_CZ; break;
+                case GFS_XCX: sub = K2_XCX; break;
+                case GFS_XCY: sub = K2_XCY; break;
+                case GFS_YCX: sub = K2_YCX; break;
+                case GFS_YCY: sub = K2_YCY; break;
+                case GFS_SWAP: sub = K2_SWAP; break;
+                case GFS_ISWAP: case GFS_ISWAP_DAG: sub = K2_ISWAP; break;
+                case GFS_CXSWAP: sub = K2_CXSWAP; break;
+                case GFS_SWAPCX: sub = K2_SWAPCX; break;
+                case GFS_CZSWAP: sub = K2_CZSWAP; break;
+                case GFS_SQRT_XX: case GFS_SQRT_XX_DAG: sub = K2_SQRT_XX; break;
+                case GFS_SQRT_YY: case GFS_SQRT_YY_DAG: sub = K2_SQRT_YY; break;
+                default: sub = K2_SQRT_ZZ; break;
+            }
+        } else {
+            switch (g) {
+                case GFS_H: case GFS_H_NXZ: case GFS_SQRT_Y: case GFS_SQRT_Y_DAG: code = OP_1Q; sub = K1_H_XZ; break;
+                case GFS_S: case GFS_S_DAG: case GFS_H_XY: case GFS_H_NXY: code = OP_1Q; sub = K1_H_XY; break;
+                case GFS_SQRT_X: case GFS_SQRT_X_DAG: case GFS_H_YZ: case GFS_H_NYZ: code = OP_1Q; sub = K1_H_YZ; break;
+                case GFS_C_XYZ: case GFS_C_NXYZ: case GFS_C_XNYZ: case GFS_C_XYNZ: code = OP_1Q; sub = K1_C_XYZ; break;
+                case GFS_C_ZYX: case GFS_C_NZYX: case GFS_C_ZNYX: case GFS_C_ZYNX: code = OP_1Q; sub = K1_C_ZYX; break;
+                case GFS_M: code = OP_MEASURE; sub = KM_M; break;
+                case GFS_MX: code = OP_MEASURE; sub = KM_MX; break;
+                case GFS_MY: code = OP_MEASURE; sub = KM_MY; break;
+                case GFS_MR: code = OP_MEASURE; sub = KM_MR; break;
+                case GFS_MRX: code = OP_MEASURE; sub = KM_MRX; break;
+                case GFS_MRY: code = OP_MEASURE; sub = KM_MRY; break;
+                case GFS_R: code = OP_RESET; sub = KR_R; break;
+                case GFS_RX: code = OP_RESET; sub = KR_RX; break;
+                default: code = OP_RESET; sub = KR_RY; break;
+            }
+        }
+        uint32_t post = fused_word(f.post, +1), pre = fused_word(f.pre, -1);
+        DevOp &d = emit(code, sub, n, inst);
+        d.b = 0;
+        d.c = post;
+        d.d = pre;
+        prog.pool.insert(prog.pool.end(), rows.begin(), rows.end());
+        if (code == OP_MEASURE) {
+            emit_results_tail(op, n, inst);
+        }
+    }
+
     void lower_instruction(const Instruction &op, uint64_t inst) {
         gfs_gate g = op.gate;
         if (g == GFS_DETECTOR) {
@@ -737,7 +889,35 @@ struct Lowerer {
             throw std::invalid_argument("REPEAT blocks nested deeper than the GPU sampler supports");
         }
         uint64_t flat = 0;
-        for (const auto &op : c.ops) {
+        std::vector<uint8_t> consumed(c.ops.size(), 0);
+        for (size_t k = 0; k < c.ops.size(); k++) {
+            const auto &op = c.ops[k];
+            if (consumed[k]) {  // noise fused into a neighbouring gate
+                flat += 1;
+                continue;
+            }
+            if (op.gate != GFS_REPEAT && k + 1 < c.ops.size() && (noise_1q(op.gate) || noise_2q(op.gate)) &&
+                c.ops[k + 1].gate != GFS_REPEAT && fusable(op, c.ops[k + 1])) {
+                consumed[k] = 1;  // lowered as the pre-noise of the next instruction
+                flat += 1;
+                continue;
+            }
+            if (op.gate != GFS_REPEAT && (gate_1q_fusable(op.gate) || gate_2q_fusable(op.gate))) {
+                Fuse f;
+                if (k > 0 && consumed[k - 1] && c.ops[k - 1].gate != GFS_REPEAT && fusable(c.ops[k - 1], op)) {
+                    f.pre = &c.ops[k - 1];
+                }
+                if (k + 1 < c.ops.size() && c.ops[k + 1].gate != GFS_REPEAT && fusable(c.ops[k + 1], op)) {
+                    f.post = &c.ops[k + 1];
+                    consumed[k + 1] = 1;
+                }
+                if (f.pre || f.post) {
+                    flush_detectors();
+                    lower_fused(op, flat, f);
+                    flat += 1;
+                    continue;
+                }
+            }
             if (op.gate == GFS_REPEAT) {
                 flush_detectors();
                 const Circuit &body = c.blocks[op.block];
@@ -770,109 +950,6 @@ struct Lowerer {
         }
     }
 
-    // Expected-hit bound for one 128-shot block of a noise op: mean + 6 sigma + 8.
-    static uint32_t hit_capacity(uint64_t trials, double p) {
-        double mean = (double)trials * p;
-        double cap = mean + 6.0 * std::sqrt(mean * (1.0 - p)) + 8.0;
-        return cap > 1e9 ? 1000000000u : (uint32_t)std::ceil(cap);
-    }
-
-    // Hit probability of a noise op's channel (the sum of its weights for multi-outcome channels).
-    double op_probability(const DevOp &op) const {
-        const DevChan &ch = prog.chans[op.b];
-        if (ch.always) {
-            return 1.0;
-        }
-        // 1 - T[1] / 2^32 recovers p to 2^-32; good enough for a capacity bound.
-        return 1.0 - (double)prog.tables[ch.table + 1] / 4294967296.0;
-    }
-
-    // Inserts an OP_NOISE_BATCH at the start of every straight-line region (the body of a loop iteration,
-    // or the code between loop boundaries) that holds noise ops, and rewrites loop body lengths.
-    void insert_noise_batches() {
-        std::vector<DevOp> in;
-        in.swap(prog.ops);
-        std::vector<DevOp> out;
-        std::vector<size_t> open_loops;  // positions of LOOP_BEGIN in `out`
-        size_t i = 0;
-        while (i < in.size()) {
-            uint32_t code = in[i].code & 0xFFu;
-            if (code == OP_LOOP_BEGIN) {
-                open_loops.push_back(out.size());
-                out.push_back(in[i++]);
-                continue;
-            }
-            if (code == OP_LOOP_END) {
-                size_t b = open_loops.back();
-                open_loops.pop_back();
-                uint32_t len = (uint32_t)(out.size() - b - 1);
-                out[b].n = len;
-                DevOp e = in[i++];
-                e.n = len;
-                out.push_back(e);
-                continue;
-            }
-            // region [i, j): until the next loop boundary or the end
-            size_t j = i;
-            while (j < in.size()) {
-                uint32_t c = in[j].code & 0xFFu;
-                if (c == OP_LOOP_BEGIN || c == OP_LOOP_END || c == OP_END) {
-                    break;
-                }
-                j++;
-            }
-            std::vector<size_t> noise;
-            uint64_t total_cap = 0;
-            for (size_t k = i; k < j && noise.size() < kMaxBatchedNoiseOps; k++) {
-                uint32_t c = in[k].code & 0xFFu;
-                if ((c == OP_NOISE || c == OP_MNOISE) && in[k].n <= kMaxBatchUnits) {
-                    uint32_t cap = hit_capacity((uint64_t)in[k].n * GFS_BLOCK_SHOTS, op_probability(in[k]));
-                    if (total_cap + cap > kMaxBatchCapacity) {
-                        continue;
-                    }
-                    total_cap += cap;
-                    noise.push_back(k);
-                }
-            }
-            if (!noise.empty()) {
-                DevOp batch{};
-                batch.code = OP_NOISE_BATCH;
-                batch.n = (uint32_t)noise.size();
-                batch.a = (uint32_t)prog.pool.size();
-                batch.inst = 0;
-                size_t batch_pos = out.size();
-                uint32_t off = 0, seg = 0;
-                for (size_t q = 0; q < noise.size(); q++) {
-                    DevOp &op = in[noise[q]];
-                    uint32_t cap = hit_capacity((uint64_t)op.n * GFS_BLOCK_SHOTS, op_probability(op));
-                    uint32_t pc_off = (uint32_t)(noise[q] - i + 1);  // relative to the batch op
-                    prog.pool.push_back(pc_off);
-                    prog.pool.push_back(off);
-                    prog.pool.push_back(cap);
-                    prog.pool.push_back(seg);
-                    op.c = (uint32_t)q + 1;
-                    op.d = off | (cap << 16);
-                    off += cap;
-                    seg += (op.n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
-                }
-                prog.pool.push_back(seg);  // total segments (per block)
-                batch.b = off;             // entries per block
-                prog.hit_list_entries = std::max(prog.hit_list_entries, off);
-                (void)batch_pos;
-                out.push_back(batch);
-            }
-            for (size_t k = i; k < j; k++) {
-                out.push_back(in[k]);
-            }
-            if (j < in.size() && (in[j].code & 0xFFu) == OP_END) {
-                out.push_back(in[j]);
-                j++;
-            }
-            i = j;
-        }
-        prog.ops.swap(out);
-    }
-
     void run() {
         prog.stats = root.stats();
         std::vector<uint8_t> used(prog.stats.num_qubits + 1, 0);
@@ -891,7 +968,6 @@ struct Lowerer {
         lower_block(root, 0);
         flush_detectors();
         emit(OP_END, 0, 0, 0);
-        insert_noise_batches();
         prog.num_detectors = prog.stats.num_detectors;
         prog.num_observables = prog.stats.num_observables;
         prog.num_measurements = prog.stats.num_measurements;

@@ -14,7 +14,7 @@ enum class SampleMode { DETECTIONS, MEASUREMENTS };
 struct Program {
     std::vector<DevOp> ops;
     std::vector<uint32_t> pool;
-    std::vector<uint32_t> tables;  // gap tables, GFS_SEG_TRIALS + 1 entries each
+    std::vector<uint32_t> tables;  // gap tables, GFS_TABLE_LEN entries each
     std::vector<DevChan> chans;
     std::vector<uint32_t> qubit_orig;  // compacted row -> circuit qubit index (keys the reset stream)
     uint32_t num_rows = 0;             // compacted qubits
@@ -23,7 +23,6 @@ struct Program {
     uint64_t num_observables = 0;
     uint64_t num_measurements = 0;
     uint32_t max_loop_depth = 0;
-    uint32_t hit_list_entries = 0;  // largest region hit list, entries per 128-shot block
     CircuitStats stats;
 };
 

@@ -30,10 +30,13 @@ enum OpCode : uint32_t {
     OP_DETECTORS,    // n detectors; pool[a+i] .. pool[a+i+1] = absolute pool range of lookbacks
     OP_OBS,          // b = observable index; pool[a+i] = term (rec: k | 1<<31; Pauli: row | X<<30 | Z<<29)
     OP_EMIT,         // copy the last n results to the measurement output
-    OP_NOISE_BATCH,  // generate the hits of the n noise ops of this straight-line region into their
-                     // shared-memory hit lists; pool[a + 4j ..] = {pc offset, list offset, capacity,
-                     // segment prefix} per op j (capacities and offsets per 128-shot block)
 };
+
+// Noise fused into a gate op (OP_1Q, OP_2Q, OP_MEASURE, OP_RESET): DevOp c = noise after the gate,
+// d = noise before it.  Bits 0..19: channel index + 1 (0 = none); bits 20..23: KN_* kind; bits 24..31:
+// signed offset of the noise instruction's instance from the gate's.  The lowering fuses a noise
+// instruction only into an adjacent single-run gate with the same target list, so unit u of the gate
+// is unit u of the noise instruction.
 
 enum : uint32_t { K1_H_XZ = 0, K1_H_XY, K1_H_YZ, K1_C_XYZ, K1_C_ZYX };
 enum : uint32_t {
@@ -55,7 +58,8 @@ enum : uint32_t {
 };
 enum : uint32_t { KM_M = 0, KM_MX, KM_MY, KM_MR, KM_MRX, KM_MRY };
 enum : uint32_t { KR_R = 0, KR_RX, KR_RY };
-enum : uint32_t { KN_X = 0, KN_Y, KN_Z, KN_DEP1, KN_PC1, KN_DEP2, KN_PC2 };
+enum : uint32_t { KN_X = 0, KN_Y, KN_Z, KN_DEP1, KN_PC1, KN_DEP2, KN_PC2, KN_FLIP };
+constexpr uint32_t kFusedChanMask = (1u << 20) - 1;
 
 struct alignas(16) DevOp {
     uint32_t code;  // OpCode | sub << 8
@@ -78,9 +82,5 @@ constexpr uint32_t kFeedbackX = 1, kFeedbackZ = 2;
 constexpr uint32_t kTermRecord = 1u << 31, kTermX = 1u << 30, kTermZ = 1u << 29;
 constexpr uint32_t kRowMask = (1u << 24) - 1;
 constexpr int kMaxLoopDepth = 16;
-constexpr uint32_t kMaxBatchedNoiseOps = 32;     // noise ops per region whose hits are generated in a batch
-constexpr uint32_t kMaxBatchUnits = 1u << 17;    // units of a batched op (hit entries hold 17-bit units)
-constexpr uint32_t kMaxBatchCapacity = 2048;     // hit-list entries of a region, per 128-shot block
-// A noise op whose hits were generated by the region's OP_NOISE_BATCH carries c = its index + 1.
 
 }  // namespace gfs

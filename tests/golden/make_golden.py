@@ -99,6 +99,8 @@ def cases():
         ("feedback", hand("feedback"), 8, 1024),
         ("pauli_channels", hand("pauli_channels"), 9, 1024),
         ("obs_data_1001", hand("obs_data"), 10, 1001),
+        ("fusion", hand("fusion"), 15, 1024),
+        ("fusion_200", hand("fusion"), 16, 200),
         ("random_clifford_n64_d200_s1", rc(64, 200, 1), 11, 512),
         ("random_clifford_n64_d200_s2", rc(64, 200, 2), 12, 512),
         ("random_clifford_n128_d200_s3", rc(128, 200, 3), 13, 256),
