@@ -222,18 +222,32 @@ struct Masks {
     uint4 x1, z1, x2, z2;
 };
 
+// Noise masks of a unit row that has at least one hit (kept out of line: at small p the hit path is rare,
+// and inlining it into every gate form multiplies the kernel's code size).
+__device__ __noinline__ void unit_masks_slow(uint32_t first, uint32_t kind, const DevChan *ch, const uint32_t *T,
+                                             uint64_t seed, uint32_t purpose_unit, uint64_t inst, uint32_t unit,
+                                             uint32_t block, Masks *out) {
+    Masks m;
+    m.x1 = m.z1 = m.x2 = m.z2 = zero4();
+    walk_unit(first, *ch, T, seed, purpose_unit, inst, unit, block, [&](uint32_t pos, gfs_stream *st) {
+        const uint32_t bits = hit_bits(kind, *ch, st);
+        if (bits & 1) set_bit4(m.x1, pos);
+        if (bits & 2) set_bit4(m.z1, pos);
+        if (bits & 4) set_bit4(m.x2, pos);
+        if (bits & 8) set_bit4(m.z2, pos);
+    });
+    *out = m;
+}
+
 // Noise masks of one unit row; returns false when the row has no hit (the common case at small p).
 __device__ __forceinline__ bool unit_masks(uint32_t first, uint32_t kind, const DevChan &ch, const uint32_t *T,
                                            uint64_t seed, uint32_t purpose_unit, uint64_t inst, uint32_t unit,
                                            uint32_t block, Masks &m) {
-    m.x1 = m.z1 = m.x2 = m.z2 = zero4();
-    return walk_unit(first, ch, T, seed, purpose_unit, inst, unit, block, [&](uint32_t pos, gfs_stream *st) {
-               const uint32_t bits = hit_bits(kind, ch, st);
-               if (bits & 1) set_bit4(m.x1, pos);
-               if (bits & 2) set_bit4(m.z1, pos);
-               if (bits & 4) set_bit4(m.x2, pos);
-               if (bits & 8) set_bit4(m.z2, pos);
-           }) != 0;
+    if (!ch.always && first < T[GFS_BLOCK_SHOTS]) {
+        return false;
+    }
+    unit_masks_slow(first, kind, &ch, T, seed, purpose_unit, inst, unit, block, &m);
+    return true;
 }
 
 __device__ __forceinline__ uint32_t word_of(const gfs_u32x4 &v, uint32_t k) {
@@ -313,7 +327,6 @@ __device__ __forceinline__ void fused_gate(const KernelArgs &p, const DevOp &op,
         if (post.ch) {
             fpost = gfs_first_draws(p.seed, GFS_P_NOISE, post.inst, q, block);
         }
-#pragma unroll
         for (uint32_t k = 0; k < GFS_QUAD; k++) {
             const uint32_t u = q * GFS_QUAD + k;
             if (u >= n) {
@@ -664,7 +677,6 @@ __global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
                         const uint32_t block = (uint32_t)(gb0 + blk);
                         const gfs_u32x4 first =
                             gfs_first_draws(p.seed, meas ? GFS_P_MNOISE : GFS_P_NOISE, inst, q, block);
-#pragma unroll
                         for (uint32_t k = 0; k < GFS_QUAD; k++) {
                             const uint32_t u = q * GFS_QUAD + k;
                             if (u >= n) {
