@@ -222,11 +222,21 @@ struct Masks {
     uint4 x1, z1, x2, z2;
 };
 
-// Noise masks of a unit row that has at least one hit (kept out of line: at small p the hit path is rare,
-// and inlining it into every gate form multiplies the kernel's code size).
-__device__ __noinline__ void unit_masks_slow(uint32_t first, uint32_t kind, const DevChan *ch, const uint32_t *T,
-                                             uint64_t seed, uint32_t purpose_unit, uint64_t inst, uint32_t unit,
-                                             uint32_t block, Masks *out) {
+__device__ __forceinline__ void atomic_xor4(uint4 *base, uint32_t idx, uint4 m) {
+    uint32_t *w = reinterpret_cast<uint32_t *>(base + idx);
+    if (m.x) atomicXor(w + 0, m.x);
+    if (m.y) atomicXor(w + 1, m.y);
+    if (m.z) atomicXor(w + 2, m.z);
+    if (m.w) atomicXor(w + 3, m.w);
+}
+
+// Applies the noise of a unit row that has at least one hit straight to its shared-memory rows.  Kept out of
+// line: at small p this path is rare, and keeping the masks out of the gate loops keeps their register
+// pressure low.  `atomic` for standalone noise ops, whose rows may repeat within an instruction.
+__device__ __noinline__ void apply_unit_noise(uint32_t first, uint32_t kind, const DevChan *ch, const uint32_t *T,
+                                              uint64_t seed, uint32_t purpose_unit, uint64_t inst, uint32_t unit,
+                                              uint32_t block, uint4 *X, uint4 *Z, uint32_t i1, uint32_t i2,
+                                              bool pair, bool atomic) {
     Masks m;
     m.x1 = m.z1 = m.x2 = m.z2 = zero4();
     walk_unit(first, *ch, T, seed, purpose_unit, inst, unit, block, [&](uint32_t pos, gfs_stream *st) {
@@ -236,31 +246,32 @@ __device__ __noinline__ void unit_masks_slow(uint32_t first, uint32_t kind, cons
         if (bits & 4) set_bit4(m.x2, pos);
         if (bits & 8) set_bit4(m.z2, pos);
     });
-    *out = m;
+    if (atomic) {
+        atomic_xor4(X, i1, m.x1);
+        atomic_xor4(Z, i1, m.z1);
+        if (pair) {
+            atomic_xor4(X, i2, m.x2);
+            atomic_xor4(Z, i2, m.z2);
+        }
+    } else {
+        X[i1] = x4(X[i1], m.x1);
+        Z[i1] = x4(Z[i1], m.z1);
+        if (pair) {
+            X[i2] = x4(X[i2], m.x2);
+            Z[i2] = x4(Z[i2], m.z2);
+        }
+    }
 }
 
-// Noise masks of one unit row; returns false when the row has no hit (the common case at small p).
-__device__ __forceinline__ bool unit_masks(uint32_t first, uint32_t kind, const DevChan &ch, const uint32_t *T,
-                                           uint64_t seed, uint32_t purpose_unit, uint64_t inst, uint32_t unit,
-                                           uint32_t block, Masks &m) {
-    if (!ch.always && first < T[GFS_BLOCK_SHOTS]) {
-        return false;
-    }
-    unit_masks_slow(first, kind, &ch, T, seed, purpose_unit, inst, unit, block, &m);
-    return true;
+// Whether a unit row has any hit, from its first draw.
+__device__ __forceinline__ bool row_hit(uint32_t first, const DevChan &ch, const uint32_t *T) {
+    return ch.always || first >= T[GFS_BLOCK_SHOTS];
 }
 
 __device__ __forceinline__ uint32_t word_of(const gfs_u32x4 &v, uint32_t k) {
     return k == 0 ? v.v[0] : k == 1 ? v.v[1] : k == 2 ? v.v[2] : v.v[3];
 }
 
-__device__ __forceinline__ void atomic_xor4(uint4 *base, uint32_t idx, uint4 m) {
-    uint32_t *w = reinterpret_cast<uint32_t *>(base + idx);
-    if (m.x) atomicXor(w + 0, m.x);
-    if (m.y) atomicXor(w + 1, m.y);
-    if (m.z) atomicXor(w + 2, m.z);
-    if (m.w) atomicXor(w + 3, m.w);
-}
 
 // A noise channel fused into a gate op: DevOp c (after the gate) / d (before it).
 struct Fused {
@@ -320,97 +331,92 @@ __device__ __forceinline__ void fused_gate(const KernelArgs &p, const DevOp &op,
     for (uint32_t item = tid; item < nquads * B; item += nt) {
         const uint32_t q = item / B, blk = item % B;
         const uint32_t block = (uint32_t)(gb0 + blk);
-        gfs_u32x4 fpre{}, fpost{};
+        const uint32_t u0 = q * GFS_QUAD, un = min(GFS_QUAD, n - u0);
+        // 1. noise before the gate (rare hits, applied in place)
         if (pre.ch) {
-            fpre = gfs_first_draws(p.seed, GFS_P_NOISE, pre.inst, q, block);
-        }
-        if (post.ch) {
-            fpost = gfs_first_draws(p.seed, GFS_P_NOISE, post.inst, q, block);
-        }
-        for (uint32_t k = 0; k < GFS_QUAD; k++) {
-            const uint32_t u = q * GFS_QUAD + k;
-            if (u >= n) {
-                break;
-            }
-            const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
-            const uint32_t i2 = pair ? __ldg(p.pool + a + 2 * u + 1) * B + blk : i1;
-            uint4 x1 = X[i1], z1 = Z[i1];
-            uint4 x2 = zero4(), z2 = zero4();
-            if (pair) {
-                x2 = X[i2];
-                z2 = Z[i2];
-            }
-            Masks m;
-            if (pre.ch && unit_masks(word_of(fpre, k), pre.kind, *pre.ch, tables + pre.ch->table, p.seed,
-                                     GFS_P_NOISE_UNIT, pre.inst, u, block, m)) {
-                x1 = x4(x1, m.x1);
-                z1 = x4(z1, m.z1);
-                x2 = x4(x2, m.x2);
-                z2 = x4(z2, m.z2);
-            }
-            if (code == OP_1Q) {
-                rule1(sub, x1, z1);
-            } else if (code == OP_2Q) {
-                rule2v(sub, x1, z1, x2, z2);
-            } else {
-                const uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, op.b + u, block));
-                if (code == OP_MEASURE) {
-                    const uint32_t slot = wrap(rec + u, L) * B + blk;
-                    switch (sub) {
-                        case KM_M:
-                            R[slot] = x1;
-                            z1 = r;
-                            break;
-                        case KM_MX:
-                            R[slot] = z1;
-                            x1 = r;
-                            break;
-                        case KM_MY:
-                            R[slot] = x4(x1, z1);
-                            x1 = x4(x4(x1, z1), r);
-                            z1 = r;
-                            break;
-                        case KM_MR:
-                            R[slot] = x1;
-                            x1 = zero4();
-                            z1 = r;
-                            break;
-                        case KM_MRX:
-                            R[slot] = z1;
-                            z1 = zero4();
-                            x1 = r;
-                            break;
-                        default:  // KM_MRY
-                            R[slot] = x4(x1, z1);
-                            z1 = r;
-                            x1 = r;
-                            break;
-                    }
-                } else {  // OP_RESET
-                    if (sub == KR_R) {
-                        x1 = zero4();
-                        z1 = r;
-                    } else if (sub == KR_RX) {
-                        x1 = r;
-                        z1 = zero4();
-                    } else {
-                        x1 = r;
-                        z1 = r;
-                    }
+            const uint32_t *T = tables + pre.ch->table;
+            const gfs_u32x4 f = gfs_first_draws(p.seed, GFS_P_NOISE, pre.inst, q, block);
+            for (uint32_t k = 0; k < un; k++) {
+                const uint32_t w = word_of(f, k);
+                if (row_hit(w, *pre.ch, T)) {
+                    const uint32_t u = u0 + k;
+                    const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
+                    const uint32_t i2 = pair ? __ldg(p.pool + a + 2 * u + 1) * B + blk : i1;
+                    apply_unit_noise(w, pre.kind, pre.ch, T, p.seed, GFS_P_NOISE_UNIT, pre.inst, u, block, X, Z, i1,
+                                     i2, pair, false);
                 }
             }
-            if (post.ch && unit_masks(word_of(fpost, k), post.kind, *post.ch, tables + post.ch->table, p.seed,
-                                      GFS_P_NOISE_UNIT, post.inst, u, block, m)) {
-                x1 = x4(x1, m.x1);
-                z1 = x4(z1, m.z1);
-                x2 = x4(x2, m.x2);
-                z2 = x4(z2, m.z2);
-            }
-            X[i1] = x1;
-            Z[i1] = z1;
-            if (pair) {
+        }
+        // 2. the gate
+        for (uint32_t k = 0; k < un; k++) {
+            const uint32_t u = u0 + k;
+            const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
+            if (code == OP_2Q) {
+                const uint32_t i2 = __ldg(p.pool + a + 2 * u + 1) * B + blk;
+                uint4 x1 = X[i1], z1 = Z[i1], x2 = X[i2], z2 = Z[i2];
+                rule2v(sub, x1, z1, x2, z2);
+                X[i1] = x1;
+                Z[i1] = z1;
                 X[i2] = x2;
                 Z[i2] = z2;
+            } else if (code == OP_1Q) {
+                uint4 x = X[i1], z = Z[i1];
+                rule1(sub, x, z);
+                X[i1] = x;
+                Z[i1] = z;
+            } else if (code == OP_MEASURE) {
+                const uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, op.b + u, block));
+                const uint32_t slot = wrap(rec + u, L) * B + blk;
+                const uint4 x = X[i1], z = Z[i1];
+                switch (sub) {
+                    case KM_M:
+                        R[slot] = x;
+                        Z[i1] = r;
+                        break;
+                    case KM_MX:
+                        R[slot] = z;
+                        X[i1] = r;
+                        break;
+                    case KM_MY:
+                        R[slot] = x4(x, z);
+                        X[i1] = x4(x4(x, z), r);
+                        Z[i1] = r;
+                        break;
+                    case KM_MR:
+                        R[slot] = x;
+                        X[i1] = zero4();
+                        Z[i1] = r;
+                        break;
+                    case KM_MRX:
+                        R[slot] = z;
+                        Z[i1] = zero4();
+                        X[i1] = r;
+                        break;
+                    default:  // KM_MRY
+                        R[slot] = x4(x, z);
+                        Z[i1] = r;
+                        X[i1] = r;
+                        break;
+                }
+            } else {  // OP_RESET
+                const uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, op.b + u, block));
+                X[i1] = sub == KR_R ? zero4() : r;
+                Z[i1] = sub == KR_RX ? zero4() : r;
+            }
+        }
+        // 3. noise after the gate
+        if (post.ch) {
+            const uint32_t *T = tables + post.ch->table;
+            const gfs_u32x4 f = gfs_first_draws(p.seed, GFS_P_NOISE, post.inst, q, block);
+            for (uint32_t k = 0; k < un; k++) {
+                const uint32_t w = word_of(f, k);
+                if (row_hit(w, *post.ch, T)) {
+                    const uint32_t u = u0 + k;
+                    const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
+                    const uint32_t i2 = pair ? __ldg(p.pool + a + 2 * u + 1) * B + blk : i1;
+                    apply_unit_noise(w, post.kind, post.ch, T, p.seed, GFS_P_NOISE_UNIT, post.inst, u, block, X, Z,
+                                     i1, i2, pair, false);
+                }
             }
         }
     }
@@ -665,40 +671,34 @@ __global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
                 case OP_NOISE:
                 case OP_MNOISE: {
                     // Standalone noise: quads of units; rows may repeat within an instruction, so the
-                    // (rare) nonzero masks are applied with shared atomics.
+                    // (rare) rows with hits are applied with shared atomics.
                     const DevChan &ch = p.chans[op.b];
                     const uint32_t *T = tables + ch.table;
                     const bool meas = code == OP_MNOISE;
                     const bool pair = !meas && (sub == KN_DEP2 || sub == KN_PC2);
-                    const uint32_t kind = meas ? KN_FLIP : sub;
                     const uint32_t nquads = (n + GFS_QUAD - 1) / GFS_QUAD;
                     for (uint32_t item = tid; item < nquads * B; item += nt) {
                         const uint32_t q = item / B, blk = item % B;
                         const uint32_t block = (uint32_t)(gb0 + blk);
-                        const gfs_u32x4 first =
-                            gfs_first_draws(p.seed, meas ? GFS_P_MNOISE : GFS_P_NOISE, inst, q, block);
-                        for (uint32_t k = 0; k < GFS_QUAD; k++) {
-                            const uint32_t u = q * GFS_QUAD + k;
-                            if (u >= n) {
-                                break;
-                            }
-                            Masks m;
-                            if (!unit_masks(word_of(first, k), kind, ch, T, p.seed,
-                                            meas ? GFS_P_MNOISE_UNIT : GFS_P_NOISE_UNIT, inst, u, block, m)) {
+                        const gfs_u32x4 f = gfs_first_draws(p.seed, meas ? GFS_P_MNOISE : GFS_P_NOISE, inst, q, block);
+                        const uint32_t u0 = q * GFS_QUAD, un = min(GFS_QUAD, n - u0);
+                        for (uint32_t k = 0; k < un; k++) {
+                            const uint32_t w = word_of(f, k);
+                            if (!row_hit(w, ch, T)) {
                                 continue;
                             }
+                            const uint32_t u = u0 + k;
                             if (meas) {
-                                atomic_xor4(R, wrap(rec + L - n + u, L) * B + blk, m.x1);
+                                // A flipped result: X mask of a KN_FLIP walk applied to the result's ring row.
+                                const uint32_t slot = wrap(rec + L - n + u, L) * B + blk;
+                                apply_unit_noise(w, KN_FLIP, &ch, T, p.seed, GFS_P_MNOISE_UNIT, inst, u, block, R, R,
+                                                 slot, slot, false, true);
                                 continue;
                             }
                             const uint32_t i1 = __ldg(pool + a + (pair ? 2 * u : u)) * B + blk;
-                            atomic_xor4(X, i1, m.x1);
-                            atomic_xor4(Z, i1, m.z1);
-                            if (pair) {
-                                const uint32_t i2 = __ldg(pool + a + 2 * u + 1) * B + blk;
-                                atomic_xor4(X, i2, m.x2);
-                                atomic_xor4(Z, i2, m.z2);
-                            }
+                            const uint32_t i2 = pair ? __ldg(pool + a + 2 * u + 1) * B + blk : i1;
+                            apply_unit_noise(w, sub, &ch, T, p.seed, GFS_P_NOISE_UNIT, inst, u, block, X, Z, i1, i2,
+                                             pair, true);
                         }
                     }
                     break;
@@ -735,16 +735,15 @@ __global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
                 case OP_CORR_MASK: {
                     const DevChan &ch = p.chans[op.b];
                     for (uint32_t blk = tid; blk < (uint32_t)B; blk += nt) {
-                        Masks m;
-                        m.x1 = zero4();
+                        uint4 hits = zero4();
                         if (ch.active) {
                             const uint32_t block = (uint32_t)(gb0 + blk);
                             const gfs_u32x4 first = gfs_first_draws(p.seed, GFS_P_NOISE, inst, 0, block);
-                            unit_masks(first.v[0], KN_X, ch, tables + ch.table, p.seed, GFS_P_NOISE_UNIT, inst, 0,
-                                       block, m);
+                            walk_unit(first.v[0], ch, tables + ch.table, p.seed, GFS_P_NOISE_UNIT, inst, 0, block,
+                                      [&](uint32_t pos, gfs_stream *) { set_bit4(hits, pos); });
                         }
                         uint4 occ = sub == 0 ? zero4() : OCC[blk];
-                        uint4 mk = make_uint4(m.x1.x & ~occ.x, m.x1.y & ~occ.y, m.x1.z & ~occ.z, m.x1.w & ~occ.w);
+                        uint4 mk = make_uint4(hits.x & ~occ.x, hits.y & ~occ.y, hits.z & ~occ.z, hits.w & ~occ.w);
                         OCC[blk] = make_uint4(occ.x | mk.x, occ.y | mk.y, occ.z | mk.z, occ.w | mk.w);
                         MSK[blk] = mk;
                     }

@@ -889,27 +889,30 @@ struct Lowerer {
             throw std::invalid_argument("REPEAT blocks nested deeper than the GPU sampler supports");
         }
         uint64_t flat = 0;
-        std::vector<uint8_t> consumed(c.ops.size(), 0);
+        // 0: lowered on its own; 1: noise fused after the previous instruction; 2: noise fused before the next.
+        std::vector<uint8_t> fused(c.ops.size(), 0);
         for (size_t k = 0; k < c.ops.size(); k++) {
             const auto &op = c.ops[k];
-            if (consumed[k]) {  // noise fused into a neighbouring gate
+            if (fused[k]) {  // noise lowered as part of a neighbouring gate
                 flat += 1;
                 continue;
             }
             if (op.gate != GFS_REPEAT && k + 1 < c.ops.size() && (noise_1q(op.gate) || noise_2q(op.gate)) &&
-                c.ops[k + 1].gate != GFS_REPEAT && fusable(op, c.ops[k + 1])) {
-                consumed[k] = 1;  // lowered as the pre-noise of the next instruction
+                c.ops[k + 1].gate != GFS_REPEAT && (gate_1q_fusable(c.ops[k + 1].gate) ||
+                                                     gate_2q_fusable(c.ops[k + 1].gate)) &&
+                fusable(op, c.ops[k + 1])) {
+                fused[k] = 2;
                 flat += 1;
                 continue;
             }
             if (op.gate != GFS_REPEAT && (gate_1q_fusable(op.gate) || gate_2q_fusable(op.gate))) {
                 Fuse f;
-                if (k > 0 && consumed[k - 1] && c.ops[k - 1].gate != GFS_REPEAT && fusable(c.ops[k - 1], op)) {
+                if (k > 0 && fused[k - 1] == 2) {
                     f.pre = &c.ops[k - 1];
                 }
                 if (k + 1 < c.ops.size() && c.ops[k + 1].gate != GFS_REPEAT && fusable(c.ops[k + 1], op)) {
                     f.post = &c.ops[k + 1];
-                    consumed[k + 1] = 1;
+                    fused[k + 1] = 1;
                 }
                 if (f.pre || f.post) {
                     flush_detectors();
