@@ -320,6 +320,64 @@ __device__ __forceinline__ void rule1(uint32_t sub, uint4 &x, uint4 &z) {
 // unit u is keyed exactly as the standalone noise instruction would be.  A thread takes a quad of four
 // units, whose first draws come from one Philox call per fused channel, and updates their rows in
 // registers: no atomics, no extra phase.
+// Applies the noise of the rows with hits among a warp's quads.  Each lane holds one quad of units (the
+// four first draws `f` of one channel, `un` valid units, 0 for an idle lane).  Rows with hits (about 12% at
+// p = 1e-3) are dealt out to the lanes with ballots and shuffles, so the warp walks them side by side in
+// one converged pass instead of once per unit with most lanes idle.  Must be called by all 32 lanes; the
+// rows it touches belong to this warp's quads, so a __syncwarp() before it orders it after their gate.
+template <int B>
+__device__ __forceinline__ void warp_noise(const KernelArgs &p, const Fused &fz, const gfs_u32x4 &f, uint32_t un,
+                                           uint32_t q, uint32_t blk, uint64_t gb0, const uint32_t *tables,
+                                           uint4 *X, uint4 *Z, uint4 *R, uint32_t rec, uint32_t L, uint32_t n,
+                                           uint32_t a, bool pair, bool meas, bool atomic) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t *T = tables + fz.ch->table;
+    uint32_t m[GFS_QUAD], total = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < GFS_QUAD; k++) {
+        const bool h = k < un && row_hit(word_of(f, k), *fz.ch, T);
+        m[k] = __ballot_sync(0xFFFFFFFFu, h);
+        total += (uint32_t)__popc(m[k]);
+    }
+    for (uint32_t e0 = 0; e0 < total; e0 += 32) {
+        const uint32_t e = e0 + lane;
+        uint32_t k = 0, i = e;
+        while (k + 1 < GFS_QUAD && i >= (uint32_t)__popc(m[k])) {
+            i -= (uint32_t)__popc(m[k]);
+            k++;
+        }
+        const bool valid = e < total;
+        const uint32_t src = valid ? __fns(m[k], 0, (int)i + 1) : lane;
+        const uint32_t w0 = __shfl_sync(0xFFFFFFFFu, f.v[0], (int)src);
+        const uint32_t w1 = __shfl_sync(0xFFFFFFFFu, f.v[1], (int)src);
+        const uint32_t w2 = __shfl_sync(0xFFFFFFFFu, f.v[2], (int)src);
+        const uint32_t w3 = __shfl_sync(0xFFFFFFFFu, f.v[3], (int)src);
+        const uint32_t qs = __shfl_sync(0xFFFFFFFFu, q, (int)src);
+        const uint32_t bs = __shfl_sync(0xFFFFFFFFu, blk, (int)src);
+        if (!valid) {
+            continue;
+        }
+        const uint32_t w = k == 0 ? w0 : k == 1 ? w1 : k == 2 ? w2 : w3;
+        const uint32_t u = qs * GFS_QUAD + k;
+        const uint32_t block = (uint32_t)(gb0 + bs);
+        if (meas) {
+            const uint32_t slot = wrap(rec + L - n + u, L) * B + bs;
+            apply_unit_noise(w, KN_FLIP, fz.ch, T, p.seed, GFS_P_MNOISE_UNIT, fz.inst, u, block, R, R, slot, slot,
+                             false, atomic);
+        } else {
+            const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + bs;
+            const uint32_t i2 = pair ? __ldg(p.pool + a + 2 * u + 1) * B + bs : i1;
+            apply_unit_noise(w, fz.kind, fz.ch, T, p.seed, GFS_P_NOISE_UNIT, fz.inst, u, block, X, Z, i1, i2, pair,
+                             atomic);
+        }
+    }
+}
+
+// Gate op with noise fused before and/or after it.  The op's units are its instruction's units (the
+// lowering fuses only single-run instructions whose noise targets are the same list), so the noise of
+// unit u is keyed exactly as the standalone noise instruction would be.  Each lane takes a quad of four
+// units, whose first draws come from one Philox call per fused channel; the warp applies the rare rows
+// with hits together (warp_noise), then the gate runs over the quad, then the post-noise rows.
 template <int B>
 __device__ __forceinline__ void fused_gate(const KernelArgs &p, const DevOp &op, uint32_t code, uint32_t sub,
                                            uint64_t inst, uint64_t gb0, const uint32_t *tables, uint4 *X, uint4 *Z,
@@ -328,26 +386,22 @@ __device__ __forceinline__ void fused_gate(const KernelArgs &p, const DevOp &op,
     const Fused pre = decode_fused(p, op.d, inst), post = decode_fused(p, op.c, inst);
     const bool pair = code == OP_2Q;
     const uint32_t nquads = (n + GFS_QUAD - 1) / GFS_QUAD;
-    for (uint32_t item = tid; item < nquads * B; item += nt) {
-        const uint32_t q = item / B, blk = item % B;
+    const uint32_t total = nquads * B;
+    const uint32_t lane = tid & 31u;
+    for (uint32_t item0 = tid - lane; item0 < total; item0 += nt) {  // warp-uniform trip count
+        const uint32_t item = item0 + lane;
+        const bool valid = item < total;
+        const uint32_t q = valid ? item / B : 0, blk = valid ? item % B : 0;
         const uint32_t block = (uint32_t)(gb0 + blk);
-        const uint32_t u0 = q * GFS_QUAD, un = min(GFS_QUAD, n - u0);
-        // 1. noise before the gate (rare hits, applied in place)
+        const uint32_t u0 = q * GFS_QUAD, un = valid ? min(GFS_QUAD, n - u0) : 0;
         if (pre.ch) {
-            const uint32_t *T = tables + pre.ch->table;
-            const gfs_u32x4 f = gfs_first_draws(p.seed, GFS_P_NOISE, pre.inst, q, block);
-            for (uint32_t k = 0; k < un; k++) {
-                const uint32_t w = word_of(f, k);
-                if (row_hit(w, *pre.ch, T)) {
-                    const uint32_t u = u0 + k;
-                    const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
-                    const uint32_t i2 = pair ? __ldg(p.pool + a + 2 * u + 1) * B + blk : i1;
-                    apply_unit_noise(w, pre.kind, pre.ch, T, p.seed, GFS_P_NOISE_UNIT, pre.inst, u, block, X, Z, i1,
-                                     i2, pair, false);
-                }
+            gfs_u32x4 f{};
+            if (valid) {
+                f = gfs_first_draws(p.seed, GFS_P_NOISE, pre.inst, q, block);
             }
+            warp_noise<B>(p, pre, f, un, q, blk, gb0, tables, X, Z, R, rec, L, n, a, pair, false, false);
+            __syncwarp();
         }
-        // 2. the gate
         for (uint32_t k = 0; k < un; k++) {
             const uint32_t u = u0 + k;
             const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
@@ -404,20 +458,13 @@ __device__ __forceinline__ void fused_gate(const KernelArgs &p, const DevOp &op,
                 Z[i1] = sub == KR_RX ? zero4() : r;
             }
         }
-        // 3. noise after the gate
         if (post.ch) {
-            const uint32_t *T = tables + post.ch->table;
-            const gfs_u32x4 f = gfs_first_draws(p.seed, GFS_P_NOISE, post.inst, q, block);
-            for (uint32_t k = 0; k < un; k++) {
-                const uint32_t w = word_of(f, k);
-                if (row_hit(w, *post.ch, T)) {
-                    const uint32_t u = u0 + k;
-                    const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
-                    const uint32_t i2 = pair ? __ldg(p.pool + a + 2 * u + 1) * B + blk : i1;
-                    apply_unit_noise(w, post.kind, post.ch, T, p.seed, GFS_P_NOISE_UNIT, post.inst, u, block, X, Z,
-                                     i1, i2, pair, false);
-                }
+            gfs_u32x4 f{};
+            if (valid) {
+                f = gfs_first_draws(p.seed, GFS_P_NOISE, post.inst, q, block);
             }
+            __syncwarp();
+            warp_noise<B>(p, post, f, un, q, blk, gb0, tables, X, Z, R, rec, L, n, a, pair, false, false);
         }
     }
 }
@@ -670,36 +717,28 @@ __global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
 
                 case OP_NOISE:
                 case OP_MNOISE: {
-                    // Standalone noise: quads of units; rows may repeat within an instruction, so the
-                    // (rare) rows with hits are applied with shared atomics.
-                    const DevChan &ch = p.chans[op.b];
-                    const uint32_t *T = tables + ch.table;
+                    // Standalone noise: a quad of units per lane; rows may repeat within an instruction, so
+                    // the rows with hits are applied with shared atomics.
                     const bool meas = code == OP_MNOISE;
+                    Fused fz;
+                    fz.ch = &p.chans[op.b];
+                    fz.kind = meas ? (uint32_t)KN_FLIP : sub;
+                    fz.inst = inst;
                     const bool pair = !meas && (sub == KN_DEP2 || sub == KN_PC2);
                     const uint32_t nquads = (n + GFS_QUAD - 1) / GFS_QUAD;
-                    for (uint32_t item = tid; item < nquads * B; item += nt) {
-                        const uint32_t q = item / B, blk = item % B;
-                        const uint32_t block = (uint32_t)(gb0 + blk);
-                        const gfs_u32x4 f = gfs_first_draws(p.seed, meas ? GFS_P_MNOISE : GFS_P_NOISE, inst, q, block);
-                        const uint32_t u0 = q * GFS_QUAD, un = min(GFS_QUAD, n - u0);
-                        for (uint32_t k = 0; k < un; k++) {
-                            const uint32_t w = word_of(f, k);
-                            if (!row_hit(w, ch, T)) {
-                                continue;
-                            }
-                            const uint32_t u = u0 + k;
-                            if (meas) {
-                                // A flipped result: X mask of a KN_FLIP walk applied to the result's ring row.
-                                const uint32_t slot = wrap(rec + L - n + u, L) * B + blk;
-                                apply_unit_noise(w, KN_FLIP, &ch, T, p.seed, GFS_P_MNOISE_UNIT, inst, u, block, R, R,
-                                                 slot, slot, false, true);
-                                continue;
-                            }
-                            const uint32_t i1 = __ldg(pool + a + (pair ? 2 * u : u)) * B + blk;
-                            const uint32_t i2 = pair ? __ldg(pool + a + 2 * u + 1) * B + blk : i1;
-                            apply_unit_noise(w, sub, &ch, T, p.seed, GFS_P_NOISE_UNIT, inst, u, block, X, Z, i1, i2,
-                                             pair, true);
+                    const uint32_t total = nquads * B;
+                    const uint32_t lane = tid & 31u;
+                    for (uint32_t item0 = tid - lane; item0 < total; item0 += nt) {
+                        const uint32_t item = item0 + lane;
+                        const bool valid = item < total;
+                        const uint32_t q = valid ? item / B : 0, blk = valid ? item % B : 0;
+                        gfs_u32x4 f{};
+                        if (valid) {
+                            f = gfs_first_draws(p.seed, meas ? GFS_P_MNOISE : GFS_P_NOISE, inst, q,
+                                                (uint32_t)(gb0 + blk));
                         }
+                        const uint32_t un = valid ? min(GFS_QUAD, n - q * GFS_QUAD) : 0;
+                        warp_noise<B>(p, fz, f, un, q, blk, gb0, tables, X, Z, R, rec, L, n, a, pair, meas, true);
                     }
                     break;
                 }
