@@ -95,7 +95,7 @@ struct Injector {
         }
     }
 
-    // Unit-row walk of the contract; calls hit(unit, shot, stream) for each hit.
+    // Segment walk of the contract; calls hit(unit, shot, stream) for each hit.
     template <typename HIT>
     void for_hits(double p, uint32_t purpose, size_t num_units, HIT hit) {
         if (!(p > 0) || num_units == 0) {
@@ -108,27 +108,19 @@ struct Injector {
             gfs_build_gap_table(p, table.data());
             inv_c = gfs_inv_c(p);
         }
-        uint32_t purpose_unit = purpose == GFS_P_MNOISE ? GFS_P_MNOISE_UNIT : GFS_P_NOISE_UNIT;
+        size_t nseg = (num_units + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
         for (size_t b = 0; b < blocks; b++) {
-            for (size_t u = 0; u < num_units; u++) {
-                gfs_u32x4 first = gfs_first_draws(seed, purpose, instance, (uint32_t)(u / GFS_QUAD), (uint32_t)b);
-                uint32_t pos = always ? 0 : gfs_first_hit(first.v[u % GFS_QUAD], table.data(), inv_c);
-                if (pos >= GFS_BLOCK_SHOTS) {
-                    continue;
-                }
+            for (size_t g = 0; g < nseg; g++) {
+                size_t u0 = g * GFS_SEG_UNITS;
+                size_t nu = std::min<size_t>(GFS_SEG_UNITS, num_units - u0);
+                int32_t trials = (int32_t)(nu * GFS_BLOCK_SHOTS);
                 gfs_stream s;
-                gfs_stream_init(&s, seed, purpose_unit, instance, (uint32_t)u, (uint32_t)b);
-                for (;;) {
-                    hit(u, b * GFS_BLOCK_SHOTS + pos, &s);
-                    if (pos + 1 >= GFS_BLOCK_SHOTS) {
-                        break;
-                    }
-                    uint32_t room = GFS_BLOCK_SHOTS - 1 - pos;
-                    uint32_t gap = always ? 0 : gfs_next_gap(gfs_stream_next(&s), table.data(), inv_c, room);
-                    if (gap >= room) {
-                        break;
-                    }
-                    pos += 1 + gap;
+                gfs_stream_init(&s, seed, purpose, instance, (uint32_t)g, (uint32_t)b);
+                int32_t pos = -1;
+                while ((pos = gfs_next_hit(&s, table.data(), inv_c, pos, trials, always)) >= 0) {
+                    size_t unit = u0 + (size_t)pos / GFS_BLOCK_SHOTS;
+                    size_t shot = b * GFS_BLOCK_SHOTS + (size_t)pos % GFS_BLOCK_SHOTS;
+                    hit(unit, shot, &s);
                 }
             }
         }

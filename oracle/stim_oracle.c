@@ -858,34 +858,24 @@ static uint64_t *new_result(osim *s) {
 /* hit callback context */
 typedef void (*hit_fn)(osim *s, const oinst *op, size_t unit, size_t shot, gfs_stream *st, void *ctx);
 
-/* The hits of every unit row of a noise instruction (contract in gfs_contract.h). */
+/* The hits of every segment of a noise instruction (contract in gfs_contract.h). */
 static void walk_hits(osim *s, const oinst *op, uint32_t purpose, size_t nunits, hit_fn fn, void *ctx) {
     const ochan *ch = &op->ch;
     if (!ch->active || nunits == 0) {
         return;
     }
-    uint32_t purpose_unit = purpose == GFS_P_MNOISE ? GFS_P_MNOISE_UNIT : GFS_P_NOISE_UNIT;
+    size_t nseg = (nunits + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
     for (size_t b = 0; b < s->nblocks; b++) {
-        uint32_t block = (uint32_t)(s->first_block + b);
-        for (size_t u = 0; u < nunits; u++) {
-            gfs_u32x4 first = gfs_first_draws(s->seed, purpose, s->inst, (uint32_t)(u / GFS_QUAD), block);
-            uint32_t pos = ch->always ? 0 : gfs_first_hit(first.v[u % GFS_QUAD], ch->table, ch->inv_c);
-            if (pos >= GFS_BLOCK_SHOTS) {
-                continue;
-            }
+        for (size_t g = 0; g < nseg; g++) {
+            size_t u0 = g * GFS_SEG_UNITS;
+            size_t nu = nunits - u0 < GFS_SEG_UNITS ? nunits - u0 : GFS_SEG_UNITS;
+            int32_t trials = (int32_t)(nu * GFS_BLOCK_SHOTS);
             gfs_stream st;
-            gfs_stream_init(&st, s->seed, purpose_unit, s->inst, (uint32_t)u, block);
-            for (;;) {
-                fn(s, op, u, b * GFS_BLOCK_SHOTS + pos, &st, ctx);
-                if (pos + 1 >= GFS_BLOCK_SHOTS) {
-                    break;
-                }
-                uint32_t room = GFS_BLOCK_SHOTS - 1 - pos;
-                uint32_t gap = ch->always ? 0 : gfs_next_gap(gfs_stream_next(&st), ch->table, ch->inv_c, room);
-                if (gap >= room) {
-                    break;
-                }
-                pos += 1 + gap;
+            gfs_stream_init(&st, s->seed, purpose, s->inst, (uint32_t)g, (uint32_t)(s->first_block + b));
+            int32_t pos = -1;
+            while ((pos = gfs_next_hit(&st, ch->table, ch->inv_c, pos, trials, ch->always)) >= 0) {
+                fn(s, op, u0 + (size_t)pos / GFS_BLOCK_SHOTS, b * GFS_BLOCK_SHOTS + (size_t)pos % GFS_BLOCK_SHOTS,
+                   &st, ctx);
             }
         }
     }

@@ -20,24 +20,23 @@
  *                   (adjacent fusable instructions fused exactly as the reference parser does)
  *   unit        a target (1-qubit channels), a target pair (2-qubit channels), a measurement
  *               result (noisy measurements, heralds), or the single unit of E/ELSE_CORRELATED_ERROR
- *   unit row    one unit x the 128 shots of a block: 128 Bernoulli trials, trial t = shot t of the block
+ *   segment     units [4g, 4g+4) x the 128 shots of a block; trial tau = (u - 4g) * 128 + shot
  *
  *   Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",
  *   SC'11) with key (lo32(seed), hi32(seed)) and counter
- *       c0 = b, c1 = unit, quad or qubit, c2 = lo32(i), c3 = purpose<<28 | (bits 32..39 of i)<<20 | group
+ *       c0 = b, c1 = segment or qubit or result, c2 = lo32(i), c3 = purpose<<28 | (bits 32..39 of i)<<20 | group
  *
- *   RESET       purpose 1: z of qubit q at the start of a shot = Philox(b, q, 0, 1<<28)
- *   RAND        purpose 2: the randomized row of result/target r of instance i = Philox(b, r, i, 2<<28)
- *   NOISE       purpose 3: first draws; word k of Philox(b, u >> 2, i, 3<<28) is the first draw of unit u
- *                          with u & 3 == k (one Philox call serves a quad of four units)
- *   NOISE_UNIT  purpose 4: follow-up draws of unit u: words 0..3 of Philox(b, u, i, 4<<28 | g), g = 0, 1, ...
- *   MNOISE / MNOISE_UNIT  purposes 5 / 6: the same for measurement-result flips (M(p), MR(p), MPP(p), ...)
+ *   RESET   purpose 1: z of qubit q at the start of a shot = Philox(b, q, 0, 1<<28)
+ *   RAND    purpose 2: the randomized row of result/target r of instance i = Philox(b, r, i, 2<<28)
+ *   NOISE   purpose 3: a sequential stream of 32-bit draws per segment, 4 per Philox call (group 0, 1, ...)
+ *   MNOISE  purpose 4: the same for measurement-result flips (M(p), MR(p), MPP(p), ...)
  *
- *   The hits of a unit row: pos = G(first draw); while pos < 128 { hit(pos) [+ one follow-up draw for
- *   the Pauli, when the channel chooses one]; room = 127 - pos; if room == 0 stop; w = next follow-up
- *   draw; if w < T[room] stop; pos += 1 + G(w) }, with G(u) = max{k : u < T[k]} (capped at 128) and
+ *   A segment's hits: pos = -1; repeat { pos += 1 + G(next draw); if pos >= trials: stop; hit(pos);
+ *   if the channel picks a Pauli: choice = next draw }.  G(u) = max{k : u < T[k]} with
  *   T[k] = floor((1-p)^k * 2^32) computed in 64-bit fixed point, so P(G >= k) = (1-p)^k.
- *   p == 0 draws nothing and hits nothing; p >= 1 hits every trial, with no gap draws.
+ *   p == 0 draws nothing and hits nothing; p >= 1 hits every trial without gap draws.
+ *   A segment is exactly the four units one GPU lane updates, so at small p one Philox call per lane
+ *   and segment usually decides everything.
  */
 #ifndef GFS_CONTRACT_H
 #define GFS_CONTRACT_H
@@ -54,15 +53,14 @@
 #endif
 
 #define GFS_BLOCK_SHOTS 128u
-#define GFS_QUAD 4u                           /* units sharing one Philox call for their first draws */
-#define GFS_TABLE_LEN (GFS_BLOCK_SHOTS + 1u) /* T[0..128] */
+#define GFS_SEG_UNITS 4u
+#define GFS_SEG_TRIALS (GFS_BLOCK_SHOTS * GFS_SEG_UNITS)
+#define GFS_TABLE_LEN (GFS_SEG_TRIALS + 1u) /* T[0..512] */
 
 #define GFS_P_RESET 1u
 #define GFS_P_RAND 2u
 #define GFS_P_NOISE 3u
-#define GFS_P_NOISE_UNIT 4u
-#define GFS_P_MNOISE 5u
-#define GFS_P_MNOISE_UNIT 6u
+#define GFS_P_MNOISE 4u
 
 typedef struct gfs_u32x4 {
     uint32_t v[4];
@@ -145,15 +143,9 @@ GFS_HD uint32_t gfs_stream_next(gfs_stream *s) {
     return out;
 }
 
-/* First draws of the four units 4q..4q+3 of a noise instruction instance in one block. */
-GFS_HD gfs_u32x4 gfs_first_draws(uint64_t seed, uint32_t purpose, uint64_t instance, uint32_t quad, uint32_t block) {
-    return gfs_philox((uint32_t)seed, (uint32_t)(seed >> 32), block, quad, (uint32_t)instance,
-                      gfs_c3(purpose, instance, 0));
-}
-
 /*
  * G(u) = max{k <= maxk : u < T[k]} (T[0] = 2^32).  `est` is any starting guess; the two walks make the
- * answer exact whatever the guess.  `table` holds T[0..GFS_BLOCK_SHOTS] (index 0 unused).
+ * answer exact whatever the guess.  `table` holds T[0..GFS_SEG_TRIALS] (index 0 unused).
  */
 GFS_HD uint32_t gfs_gap_fixup(uint32_t u, const uint32_t *table, int32_t est, int32_t maxk) {
     int32_t k = est < 0 ? 0 : (est > maxk ? maxk : est);
@@ -166,7 +158,24 @@ GFS_HD uint32_t gfs_gap_fixup(uint32_t u, const uint32_t *table, int32_t est, in
     return (uint32_t)k;
 }
 
-GFS_HD int32_t gfs_gap_estimate(uint32_t u, float inv_c) {
+/*
+ * Next hit of a segment after position `pos` (start with pos = -1), or -1 when the segment has no
+ * further hits.  `always` marks p >= 1 (every trial hits, no draws); `inv_c` = 1 / -log2(1-p) only
+ * seeds the lookup, so host and device may compute it with different log2 approximations.
+ */
+GFS_HD int32_t gfs_next_hit(gfs_stream *s, const uint32_t *table, float inv_c, int32_t pos, int32_t trials,
+                            int always) {
+    if (always) {
+        return pos + 1 < trials ? pos + 1 : -1;
+    }
+    int32_t room = trials - pos - 1; /* a gap >= room leaves the segment */
+    if (room <= 0) {
+        return -1;
+    }
+    uint32_t u = gfs_stream_next(s);
+    if (u < table[room]) {
+        return -1;
+    }
 #if defined(__CUDA_ARCH__)
     float lg = __log2f((float)u + 0.5f);
 #else
@@ -176,26 +185,11 @@ GFS_HD int32_t gfs_gap_estimate(uint32_t u, float inv_c) {
     if (!(e >= 0.0f)) { /* also catches NaN */
         e = 0.0f;
     }
-    if (e > (float)GFS_BLOCK_SHOTS) {
-        e = (float)GFS_BLOCK_SHOTS;
+    if (e > (float)room) {
+        e = (float)room;
     }
-    return (int32_t)e;
-}
-
-/* Position of the first hit of a unit row from its first draw; GFS_BLOCK_SHOTS when there is none. */
-GFS_HD uint32_t gfs_first_hit(uint32_t u, const uint32_t *table, float inv_c) {
-    if (u < table[GFS_BLOCK_SHOTS]) {
-        return GFS_BLOCK_SHOTS;
-    }
-    return gfs_gap_fixup(u, table, gfs_gap_estimate(u, inv_c), (int32_t)GFS_BLOCK_SHOTS - 1);
-}
-
-/* Gap before the next hit when `room` trials remain (room >= 1); returns room when there is none. */
-GFS_HD uint32_t gfs_next_gap(uint32_t w, const uint32_t *table, float inv_c, uint32_t room) {
-    if (w < table[room]) {
-        return room;
-    }
-    return gfs_gap_fixup(w, table, gfs_gap_estimate(w, inv_c), (int32_t)room - 1);
+    uint32_t g = gfs_gap_fixup(u, table, (int32_t)e, room - 1);
+    return pos + 1 + (int32_t)g;
 }
 
 /* Choice helpers. */
@@ -214,7 +208,7 @@ GFS_HD uint32_t gfs_choice_weighted(uint32_t c, const uint64_t *cum, uint32_t n)
 
 #if !defined(__CUDA_ARCH__)
 /*
- * Host-only: the threshold table T[0..GFS_BLOCK_SHOTS] for probability p in (0, 1).
+ * Host-only: the threshold table T[0..GFS_SEG_TRIALS] for probability p in (0, 1).
  * (1-p) is converted once to 0.64 fixed point; powers are formed by 64x64->128 multiplies,
  * so every platform computes the same table from the same double p.
  */
@@ -231,7 +225,7 @@ static inline void gfs_build_gap_table(double p, uint32_t *table) {
     }
     uint64_t A = UINT64_MAX;
     table[0] = UINT32_MAX;
-    for (uint32_t k = 1; k <= GFS_BLOCK_SHOTS; k++) {
+    for (uint32_t k = 1; k <= GFS_SEG_TRIALS; k++) {
         A = (uint64_t)(((unsigned __int128)A * (unsigned __int128)Q) >> 64);
         table[k] = (uint32_t)(A >> 32);
     }

@@ -6,8 +6,10 @@
 // walks the device program (program.h): every op spreads its independent units over the threads,
 // updates 128 shots per unit with 128-bit shared-memory loads/stores and bitwise logic, and ends with
 // one __syncthreads().  Noise is sampled from the counter-based stream of gfs_contract.h: a thread owns
-// a segment of 8 units x 128 shots and skips geometrically to its hits, which it applies with shared
-// atomics.  Detection events stream to global memory as [block][detector] uint4 rows.
+// a segment of 4 units x 128 shots and skips geometrically to its hits.  Noise next to a gate on the
+// same targets is fused into the gate op (the thread's segment is the four units it updates, so the hits
+// go straight into its own rows); other noise ops apply their hits with shared atomics.  Detection events
+// stream to global memory as [block][detector] uint4 rows.
 //
 // transpose_kernel: turns [block][row] bit-rows into shot-major bytes with a 32x32 warp-ballot transpose
 // per word, replacing the reference's bit-by-bit numpy conversion (numpy.pybind.cc:20-63) and
@@ -180,47 +182,29 @@ __device__ __forceinline__ uint32_t hit_bits(uint32_t kind, const DevChan &ch, g
     }
 }
 
-__device__ __forceinline__ void set_bit4(uint4 &m, uint32_t pos) {
-    const uint32_t b = 1u << (pos & 31), w = pos >> 5;
-    m.x ^= w == 0 ? b : 0u;
-    m.y ^= w == 1 ? b : 0u;
-    m.z ^= w == 2 ? b : 0u;
-    m.w ^= w == 3 ? b : 0u;
-}
-
-// The hits of one unit row (the 128 shots of a block), following gfs_contract.h: `first` is the unit's
-// word of its quad's first-draw Philox call; follow-up draws come from the unit's own stream.
-// f(pos, stream) is called for each hit.  Returns the number of hits.
+// The hits of one segment (units [4g, 4g+4) x the 128 shots of a block), following gfs_contract.h:
+// f(k, shot, stream) is called for each hit, on unit 4g + k at `shot`.  At small p the first Philox
+// call of the segment usually shows there is no hit at all.
 template <typename F>
-__device__ __forceinline__ uint32_t walk_unit(uint32_t first, const DevChan &ch, const uint32_t *T, uint64_t seed,
-                                              uint32_t purpose_unit, uint64_t inst, uint32_t unit, uint32_t block,
-                                              F f) {
-    uint32_t pos = ch.always ? 0u : gfs_first_hit(first, T, ch.inv_c);
-    if (pos >= GFS_BLOCK_SHOTS) {
-        return 0;
-    }
+__device__ __forceinline__ void walk_segment(const DevChan &ch, const uint32_t *T, uint64_t seed, uint32_t purpose,
+                                             uint64_t inst, uint32_t seg, uint32_t block, uint32_t nunits, F f) {
     gfs_stream st;
-    gfs_stream_init(&st, seed, purpose_unit, inst, unit, block);
-    uint32_t count = 0;
-    for (;;) {
-        f(pos, &st);
-        count++;
-        if (pos + 1 >= GFS_BLOCK_SHOTS) {
-            break;
-        }
-        const uint32_t room = GFS_BLOCK_SHOTS - 1 - pos;
-        const uint32_t gap = ch.always ? 0u : gfs_next_gap(gfs_stream_next(&st), T, ch.inv_c, room);
-        if (gap >= room) {
-            break;
-        }
-        pos += 1 + gap;
+    gfs_stream_init(&st, seed, purpose, inst, seg, block);
+    const int32_t trials = (int32_t)(nunits * GFS_BLOCK_SHOTS);
+    int32_t pos = -1;
+    while ((pos = gfs_next_hit(&st, T, ch.inv_c, pos, trials, ch.always)) >= 0) {
+        f((uint32_t)pos >> 7, (uint32_t)pos & 127u, &st);
     }
-    return count;
 }
 
-struct Masks {
-    uint4 x1, z1, x2, z2;
-};
+__device__ __forceinline__ void flip_bit(uint4 *base, uint32_t idx, uint32_t shot, bool atomic) {
+    uint32_t *w = reinterpret_cast<uint32_t *>(base + idx) + (shot >> 5);
+    if (atomic) {
+        atomicXor(w, 1u << (shot & 31));
+    } else {
+        *w ^= 1u << (shot & 31);
+    }
+}
 
 __device__ __forceinline__ void atomic_xor4(uint4 *base, uint32_t idx, uint4 m) {
     uint32_t *w = reinterpret_cast<uint32_t *>(base + idx);
@@ -230,48 +214,14 @@ __device__ __forceinline__ void atomic_xor4(uint4 *base, uint32_t idx, uint4 m) 
     if (m.w) atomicXor(w + 3, m.w);
 }
 
-// Applies the noise of a unit row that has at least one hit straight to its shared-memory rows.  Kept out of
-// line: at small p this path is rare, and keeping the masks out of the gate loops keeps their register
-// pressure low.  `atomic` for standalone noise ops, whose rows may repeat within an instruction.
-__device__ __noinline__ void apply_unit_noise(uint32_t first, uint32_t kind, const DevChan *ch, const uint32_t *T,
-                                              uint64_t seed, uint32_t purpose_unit, uint64_t inst, uint32_t unit,
-                                              uint32_t block, uint4 *X, uint4 *Z, uint32_t i1, uint32_t i2,
-                                              bool pair, bool atomic) {
-    Masks m;
-    m.x1 = m.z1 = m.x2 = m.z2 = zero4();
-    walk_unit(first, *ch, T, seed, purpose_unit, inst, unit, block, [&](uint32_t pos, gfs_stream *st) {
-        const uint32_t bits = hit_bits(kind, *ch, st);
-        if (bits & 1) set_bit4(m.x1, pos);
-        if (bits & 2) set_bit4(m.z1, pos);
-        if (bits & 4) set_bit4(m.x2, pos);
-        if (bits & 8) set_bit4(m.z2, pos);
-    });
-    if (atomic) {
-        atomic_xor4(X, i1, m.x1);
-        atomic_xor4(Z, i1, m.z1);
-        if (pair) {
-            atomic_xor4(X, i2, m.x2);
-            atomic_xor4(Z, i2, m.z2);
-        }
-    } else {
-        X[i1] = x4(X[i1], m.x1);
-        Z[i1] = x4(Z[i1], m.z1);
-        if (pair) {
-            X[i2] = x4(X[i2], m.x2);
-            Z[i2] = x4(Z[i2], m.z2);
-        }
-    }
+// Applies the Pauli `bits` of one hit (bit0 = X / bit1 = Z on the first row, bits 2-3 on the second).
+__device__ __forceinline__ void apply_bits(uint4 *X, uint4 *Z, uint32_t i1, uint32_t i2, uint32_t shot,
+                                           uint32_t bits, bool atomic) {
+    if (bits & 1) flip_bit(X, i1, shot, atomic);
+    if (bits & 2) flip_bit(Z, i1, shot, atomic);
+    if (bits & 4) flip_bit(X, i2, shot, atomic);
+    if (bits & 8) flip_bit(Z, i2, shot, atomic);
 }
-
-// Whether a unit row has any hit, from its first draw.
-__device__ __forceinline__ bool row_hit(uint32_t first, const DevChan &ch, const uint32_t *T) {
-    return ch.always || first >= T[GFS_BLOCK_SHOTS];
-}
-
-__device__ __forceinline__ uint32_t word_of(const gfs_u32x4 &v, uint32_t k) {
-    return k == 0 ? v.v[0] : k == 1 ? v.v[1] : k == 2 ? v.v[2] : v.v[3];
-}
-
 
 // A noise channel fused into a gate op: DevOp c (after the gate) / d (before it).
 struct Fused {
@@ -317,67 +267,10 @@ __device__ __forceinline__ void rule1(uint32_t sub, uint4 &x, uint4 &z) {
 
 // Gate op with noise fused before and/or after it.  The op's units are its instruction's units (the
 // lowering fuses only single-run instructions whose noise targets are the same list), so the noise of
-// unit u is keyed exactly as the standalone noise instruction would be.  A thread takes a quad of four
-// units, whose first draws come from one Philox call per fused channel, and updates their rows in
-// registers: no atomics, no extra phase.
-// Applies the noise of the rows with hits among a warp's quads.  Each lane holds one quad of units (the
-// four first draws `f` of one channel, `un` valid units, 0 for an idle lane).  Rows with hits (about 12% at
-// p = 1e-3) are dealt out to the lanes with ballots and shuffles, so the warp walks them side by side in
-// one converged pass instead of once per unit with most lanes idle.  Must be called by all 32 lanes; the
-// rows it touches belong to this warp's quads, so a __syncwarp() before it orders it after their gate.
-template <int B>
-__device__ __forceinline__ void warp_noise(const KernelArgs &p, const Fused &fz, const gfs_u32x4 &f, uint32_t un,
-                                           uint32_t q, uint32_t blk, uint64_t gb0, const uint32_t *tables,
-                                           uint4 *X, uint4 *Z, uint4 *R, uint32_t rec, uint32_t L, uint32_t n,
-                                           uint32_t a, bool pair, bool meas, bool atomic) {
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t *T = tables + fz.ch->table;
-    uint32_t m[GFS_QUAD], total = 0;
-#pragma unroll
-    for (uint32_t k = 0; k < GFS_QUAD; k++) {
-        const bool h = k < un && row_hit(word_of(f, k), *fz.ch, T);
-        m[k] = __ballot_sync(0xFFFFFFFFu, h);
-        total += (uint32_t)__popc(m[k]);
-    }
-    for (uint32_t e0 = 0; e0 < total; e0 += 32) {
-        const uint32_t e = e0 + lane;
-        uint32_t k = 0, i = e;
-        while (k + 1 < GFS_QUAD && i >= (uint32_t)__popc(m[k])) {
-            i -= (uint32_t)__popc(m[k]);
-            k++;
-        }
-        const bool valid = e < total;
-        const uint32_t src = valid ? __fns(m[k], 0, (int)i + 1) : lane;
-        const uint32_t w0 = __shfl_sync(0xFFFFFFFFu, f.v[0], (int)src);
-        const uint32_t w1 = __shfl_sync(0xFFFFFFFFu, f.v[1], (int)src);
-        const uint32_t w2 = __shfl_sync(0xFFFFFFFFu, f.v[2], (int)src);
-        const uint32_t w3 = __shfl_sync(0xFFFFFFFFu, f.v[3], (int)src);
-        const uint32_t qs = __shfl_sync(0xFFFFFFFFu, q, (int)src);
-        const uint32_t bs = __shfl_sync(0xFFFFFFFFu, blk, (int)src);
-        if (!valid) {
-            continue;
-        }
-        const uint32_t w = k == 0 ? w0 : k == 1 ? w1 : k == 2 ? w2 : w3;
-        const uint32_t u = qs * GFS_QUAD + k;
-        const uint32_t block = (uint32_t)(gb0 + bs);
-        if (meas) {
-            const uint32_t slot = wrap(rec + L - n + u, L) * B + bs;
-            apply_unit_noise(w, KN_FLIP, fz.ch, T, p.seed, GFS_P_MNOISE_UNIT, fz.inst, u, block, R, R, slot, slot,
-                             false, atomic);
-        } else {
-            const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + bs;
-            const uint32_t i2 = pair ? __ldg(p.pool + a + 2 * u + 1) * B + bs : i1;
-            apply_unit_noise(w, fz.kind, fz.ch, T, p.seed, GFS_P_NOISE_UNIT, fz.inst, u, block, X, Z, i1, i2, pair,
-                             atomic);
-        }
-    }
-}
-
-// Gate op with noise fused before and/or after it.  The op's units are its instruction's units (the
-// lowering fuses only single-run instructions whose noise targets are the same list), so the noise of
-// unit u is keyed exactly as the standalone noise instruction would be.  Each lane takes a quad of four
-// units, whose first draws come from one Philox call per fused channel; the warp applies the rare rows
-// with hits together (warp_noise), then the gate runs over the quad, then the post-noise rows.
+// unit u is keyed exactly as the standalone noise instruction would be.  Each lane takes one noise
+// segment (four units x 128 shots): it walks the pre-noise hits into those units' shared-memory rows,
+// applies the gate to the four units, then walks the post-noise hits.  The rows are the lane's own, so
+// there are no atomics and no extra phase.
 template <int B>
 __device__ __forceinline__ void fused_gate(const KernelArgs &p, const DevOp &op, uint32_t code, uint32_t sub,
                                            uint64_t inst, uint64_t gb0, const uint32_t *tables, uint4 *X, uint4 *Z,
@@ -385,22 +278,21 @@ __device__ __forceinline__ void fused_gate(const KernelArgs &p, const DevOp &op,
     const uint32_t n = op.n, a = op.a;
     const Fused pre = decode_fused(p, op.d, inst), post = decode_fused(p, op.c, inst);
     const bool pair = code == OP_2Q;
-    const uint32_t nquads = (n + GFS_QUAD - 1) / GFS_QUAD;
-    const uint32_t total = nquads * B;
-    const uint32_t lane = tid & 31u;
-    for (uint32_t item0 = tid - lane; item0 < total; item0 += nt) {  // warp-uniform trip count
-        const uint32_t item = item0 + lane;
-        const bool valid = item < total;
-        const uint32_t q = valid ? item / B : 0, blk = valid ? item % B : 0;
+    const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
+    for (uint32_t item = tid; item < nseg * B; item += nt) {
+        const bool valid = true;
+        const uint32_t q = item / B, blk = item % B;
         const uint32_t block = (uint32_t)(gb0 + blk);
-        const uint32_t u0 = q * GFS_QUAD, un = valid ? min(GFS_QUAD, n - u0) : 0;
-        if (pre.ch) {
-            gfs_u32x4 f{};
-            if (valid) {
-                f = gfs_first_draws(p.seed, GFS_P_NOISE, pre.inst, q, block);
-            }
-            warp_noise<B>(p, pre, f, un, q, blk, gb0, tables, X, Z, R, rec, L, n, a, pair, false, false);
-            __syncwarp();
+        const uint32_t u0 = q * GFS_SEG_UNITS, un = min(GFS_SEG_UNITS, n - u0);
+        if (pre.ch && valid) {
+            walk_segment(*pre.ch, tables + pre.ch->table, p.seed, GFS_P_NOISE, pre.inst, q, block, un,
+                         [&](uint32_t k, uint32_t shot, gfs_stream *st) {
+                             const uint32_t bits = hit_bits(pre.kind, *pre.ch, st);
+                             const uint32_t u = u0 + k;
+                             const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
+                             const uint32_t i2 = pair ? __ldg(p.pool + a + 2 * u + 1) * B + blk : i1;
+                             apply_bits(X, Z, i1, i2, shot, bits, false);
+                         });
         }
         for (uint32_t k = 0; k < un; k++) {
             const uint32_t u = u0 + k;
@@ -458,13 +350,15 @@ __device__ __forceinline__ void fused_gate(const KernelArgs &p, const DevOp &op,
                 Z[i1] = sub == KR_RX ? zero4() : r;
             }
         }
-        if (post.ch) {
-            gfs_u32x4 f{};
-            if (valid) {
-                f = gfs_first_draws(p.seed, GFS_P_NOISE, post.inst, q, block);
-            }
-            __syncwarp();
-            warp_noise<B>(p, post, f, un, q, blk, gb0, tables, X, Z, R, rec, L, n, a, pair, false, false);
+        if (post.ch && valid) {
+            walk_segment(*post.ch, tables + post.ch->table, p.seed, GFS_P_NOISE, post.inst, q, block, un,
+                         [&](uint32_t k, uint32_t shot, gfs_stream *st) {
+                             const uint32_t bits = hit_bits(post.kind, *post.ch, st);
+                             const uint32_t u = u0 + k;
+                             const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
+                             const uint32_t i2 = pair ? __ldg(p.pool + a + 2 * u + 1) * B + blk : i1;
+                             apply_bits(X, Z, i1, i2, shot, bits, false);
+                         });
         }
     }
 }
@@ -717,28 +611,29 @@ __global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
 
                 case OP_NOISE:
                 case OP_MNOISE: {
-                    // Standalone noise: a quad of units per lane; rows may repeat within an instruction, so
-                    // the rows with hits are applied with shared atomics.
+                    // Standalone noise: one segment per lane; rows may repeat within an instruction, so hits
+                    // are applied with shared atomics.
                     const bool meas = code == OP_MNOISE;
-                    Fused fz;
-                    fz.ch = &p.chans[op.b];
-                    fz.kind = meas ? (uint32_t)KN_FLIP : sub;
-                    fz.inst = inst;
+                    const DevChan &ch = p.chans[op.b];
+                    const uint32_t *T = tables + ch.table;
                     const bool pair = !meas && (sub == KN_DEP2 || sub == KN_PC2);
-                    const uint32_t nquads = (n + GFS_QUAD - 1) / GFS_QUAD;
-                    const uint32_t total = nquads * B;
-                    const uint32_t lane = tid & 31u;
-                    for (uint32_t item0 = tid - lane; item0 < total; item0 += nt) {
-                        const uint32_t item = item0 + lane;
-                        const bool valid = item < total;
-                        const uint32_t q = valid ? item / B : 0, blk = valid ? item % B : 0;
-                        gfs_u32x4 f{};
-                        if (valid) {
-                            f = gfs_first_draws(p.seed, meas ? GFS_P_MNOISE : GFS_P_NOISE, inst, q,
-                                                (uint32_t)(gb0 + blk));
-                        }
-                        const uint32_t un = valid ? min(GFS_QUAD, n - q * GFS_QUAD) : 0;
-                        warp_noise<B>(p, fz, f, un, q, blk, gb0, tables, X, Z, R, rec, L, n, a, pair, meas, true);
+                    const uint32_t kind = meas ? (uint32_t)KN_FLIP : sub;
+                    const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
+                    for (uint32_t item = tid; item < nseg * B; item += nt) {
+                        const uint32_t g = item / B, blk = item % B;
+                        const uint32_t u0 = g * GFS_SEG_UNITS;
+                        walk_segment(ch, T, p.seed, meas ? GFS_P_MNOISE : GFS_P_NOISE, inst, g, (uint32_t)(gb0 + blk),
+                                     min(GFS_SEG_UNITS, n - u0), [&](uint32_t k, uint32_t shot, gfs_stream *st) {
+                                         const uint32_t u = u0 + k;
+                                         if (meas) {
+                                             flip_bit(R, wrap(rec + L - n + u, L) * B + blk, shot, true);
+                                             return;
+                                         }
+                                         const uint32_t bits = hit_bits(kind, ch, st);
+                                         const uint32_t i1 = __ldg(pool + a + (pair ? 2 * u : u)) * B + blk;
+                                         const uint32_t i2 = pair ? __ldg(pool + a + 2 * u + 1) * B + blk : i1;
+                                         apply_bits(X, Z, i1, i2, shot, bits, true);
+                                     });
                     }
                     break;
                 }
@@ -746,27 +641,20 @@ __global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
                 case OP_HERALD: {
                     const DevChan &ch = p.chans[op.b];
                     const uint32_t *T = tables + ch.table;
-                    const uint32_t nquads = (n + GFS_QUAD - 1) / GFS_QUAD;
-                    for (uint32_t item = tid; item < nquads * B; item += nt) {
-                        const uint32_t q = item / B, blk = item % B;
-                        const uint32_t block = (uint32_t)(gb0 + blk);
-                        const gfs_u32x4 first = gfs_first_draws(p.seed, GFS_P_NOISE, inst, q, block);
-                        for (uint32_t k = 0; k < GFS_QUAD; k++) {
-                            const uint32_t u = q * GFS_QUAD + k;
-                            if (u >= n) {
-                                break;
-                            }
-                            const uint32_t idx = __ldg(pool + a + u) * B + blk;
-                            const uint32_t slot = wrap(rec + L - n + u, L) * B + blk;
-                            walk_unit(word_of(first, k), ch, T, p.seed, GFS_P_NOISE_UNIT, inst, u, block,
-                                      [&](uint32_t pos, gfs_stream *st) {
-                                          const uint32_t c = gfs_stream_next(st);
-                                          atomic_or_bit(R, slot, pos);
-                                          const uint32_t v = sub == 0 ? (c & 3u) : pauli_xz(gfs_choice_weighted(c, ch.cum, 4));
-                                          if (v & 1) atomic_xor_bit(X, idx, pos);
-                                          if (v & 2) atomic_xor_bit(Z, idx, pos);
-                                      });
-                        }
+                    const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
+                    for (uint32_t item = tid; item < nseg * B; item += nt) {
+                        const uint32_t g = item / B, blk = item % B;
+                        const uint32_t u0 = g * GFS_SEG_UNITS;
+                        walk_segment(ch, T, p.seed, GFS_P_NOISE, inst, g, (uint32_t)(gb0 + blk),
+                                     min(GFS_SEG_UNITS, n - u0), [&](uint32_t k, uint32_t shot, gfs_stream *st) {
+                                         const uint32_t u = u0 + k;
+                                         const uint32_t c = gfs_stream_next(st);
+                                         const uint32_t idx = __ldg(pool + a + u) * B + blk;
+                                         atomic_or_bit(R, wrap(rec + L - n + u, L) * B + blk, shot);
+                                         const uint32_t v =
+                                             sub == 0 ? (c & 3u) : pauli_xz(gfs_choice_weighted(c, ch.cum, 4));
+                                         apply_bits(X, Z, idx, idx, shot, v, true);
+                                     });
                     }
                     break;
                 }
@@ -774,13 +662,14 @@ __global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
                 case OP_CORR_MASK: {
                     const DevChan &ch = p.chans[op.b];
                     for (uint32_t blk = tid; blk < (uint32_t)B; blk += nt) {
-                        uint4 hits = zero4();
+                        uint32_t hw[4] = {0, 0, 0, 0};
                         if (ch.active) {
-                            const uint32_t block = (uint32_t)(gb0 + blk);
-                            const gfs_u32x4 first = gfs_first_draws(p.seed, GFS_P_NOISE, inst, 0, block);
-                            walk_unit(first.v[0], ch, tables + ch.table, p.seed, GFS_P_NOISE_UNIT, inst, 0, block,
-                                      [&](uint32_t pos, gfs_stream *) { set_bit4(hits, pos); });
+                            walk_segment(ch, tables + ch.table, p.seed, GFS_P_NOISE, inst, 0, (uint32_t)(gb0 + blk), 1,
+                                         [&](uint32_t, uint32_t shot, gfs_stream *) {
+                                             hw[shot >> 5] |= 1u << (shot & 31);
+                                         });
                         }
+                        const uint4 hits = make_uint4(hw[0], hw[1], hw[2], hw[3]);
                         uint4 occ = sub == 0 ? zero4() : OCC[blk];
                         uint4 mk = make_uint4(hits.x & ~occ.x, hits.y & ~occ.y, hits.z & ~occ.z, hits.w & ~occ.w);
                         OCC[blk] = make_uint4(occ.x | mk.x, occ.y | mk.y, occ.z | mk.z, occ.w | mk.w);
