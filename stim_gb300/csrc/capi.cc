@@ -138,9 +138,14 @@ struct gfs_sampler {
         return prog.tables.size() <= 32 * GFS_TABLE_LEN ? (uint32_t)prog.tables.size() : 0;
     }
 
+    // Small op streams go to shared memory too (every thread reads every op).
+    uint32_t smem_ops() const {
+        return prog.ops.size() <= 256 ? (uint32_t)prog.ops.size() : 0;
+    }
+
     size_t smem_for(int bpc) const {
         return gfs::frame_smem_bytes(prog.num_rows, prog.ring, (uint32_t)prog.num_observables, bpc,
-                                     smem_table_words());
+                                     smem_table_words(), smem_ops());
     }
 
     void choose_shape(int bpc, int threads, int grid) {
@@ -258,6 +263,7 @@ struct gfs_sampler {
         a.meas_out = (uint4 *)meas_tmp.p;
         a.status = (uint32_t *)d_status.p;
         a.smem_table_words = smem_table_words();
+        a.smem_ops = smem_ops();
         gfs::LaunchShape s = shape;
         s.grid = (int)std::min<uint64_t>((uint64_t)shape.grid, nslices);
         ck(gfs::launch_frame_kernel(a, s, stream), "frame kernel launch");
@@ -482,6 +488,7 @@ void detections_noalloc(gfs_sampler *s, uint64_t shots, uint32_t flags, uint8_t 
         a.meas_out = nullptr;
         a.status = (uint32_t *)s->d_status.p;
         a.smem_table_words = s->smem_table_words();
+        a.smem_ops = s->smem_ops();
         gfs::LaunchShape shape = s->shape;
         shape.grid = (int)std::min<uint64_t>((uint64_t)s->shape.grid, nslices);
         ck(cudaEventRecord(s->ev[1], s->stream), "event");
@@ -596,7 +603,8 @@ gfs_status gfs_program_info(const gfs_circuit *c, uint32_t mode, uint64_t *info8
         info8[4] = p.chans.size();
         info8[5] = p.max_loop_depth;
         info8[6] = gfs::frame_smem_bytes(p.num_rows, p.ring, (uint32_t)p.num_observables, 1,
-                                         p.tables.size() <= 32 * GFS_TABLE_LEN ? (uint32_t)p.tables.size() : 0);
+                                         p.tables.size() <= 32 * GFS_TABLE_LEN ? (uint32_t)p.tables.size() : 0,
+                                         p.ops.size() <= 256 ? (uint32_t)p.ops.size() : 0);
         info8[7] = p.num_detectors;
     });
 }

@@ -271,6 +271,74 @@ __device__ __forceinline__ void rule1(uint32_t sub, uint4 &x, uint4 &z) {
 // segment (four units x 128 shots): it walks the pre-noise hits into those units' shared-memory rows,
 // applies the gate to the four units, then walks the post-noise hits.  The rows are the lane's own, so
 // there are no atomics and no extra phase.
+// The gate of one unit of a fused op (noise is applied separately, in place, by the segment owner).
+template <int B>
+__device__ __forceinline__ void gate_unit(const KernelArgs &p, uint32_t code, uint32_t sub, uint32_t a, uint32_t rb,
+                                          uint64_t inst, uint32_t u, uint32_t blk, uint32_t block, uint4 *X, uint4 *Z,
+                                          uint4 *R, uint32_t rec, uint32_t L) {
+    const bool pair = code == OP_2Q;
+    const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
+    if (pair) {
+        const uint32_t i2 = __ldg(p.pool + a + 2 * u + 1) * B + blk;
+        uint4 x1 = X[i1], z1 = Z[i1], x2 = X[i2], z2 = Z[i2];
+        rule2v(sub, x1, z1, x2, z2);
+        X[i1] = x1;
+        Z[i1] = z1;
+        X[i2] = x2;
+        Z[i2] = z2;
+    } else if (code == OP_1Q) {
+        uint4 x = X[i1], z = Z[i1];
+        rule1(sub, x, z);
+        X[i1] = x;
+        Z[i1] = z;
+    } else if (code == OP_MEASURE) {
+        const uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, rb + u, block));
+        const uint32_t slot = wrap(rec + u, L) * B + blk;
+        const uint4 x = X[i1], z = Z[i1];
+        switch (sub) {
+            case KM_M:
+                R[slot] = x;
+                Z[i1] = r;
+                break;
+            case KM_MX:
+                R[slot] = z;
+                X[i1] = r;
+                break;
+            case KM_MY:
+                R[slot] = x4(x, z);
+                X[i1] = x4(x4(x, z), r);
+                Z[i1] = r;
+                break;
+            case KM_MR:
+                R[slot] = x;
+                X[i1] = zero4();
+                Z[i1] = r;
+                break;
+            case KM_MRX:
+                R[slot] = z;
+                Z[i1] = zero4();
+                X[i1] = r;
+                break;
+            default:  // KM_MRY
+                R[slot] = x4(x, z);
+                Z[i1] = r;
+                X[i1] = r;
+                break;
+        }
+    } else {  // OP_RESET
+        const uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, rb + u, block));
+        X[i1] = sub == KR_R ? zero4() : r;
+        Z[i1] = sub == KR_RX ? zero4() : r;
+    }
+}
+
+// Gate op with noise fused before and/or after it.  The op's units are its instruction's units (the
+// lowering fuses only single-run instructions whose noise targets are the same list), so the noise of
+// unit u is keyed exactly as the standalone noise instruction would be.  A warp takes 32 noise segments
+// (four units x 128 shots each): every lane walks its segment's pre-noise hits into those units'
+// shared-memory rows; after a __syncwarp the warp applies the gate to the 128 units with consecutive lanes
+// on consecutive units (so quarter-warps touch distinct banks); after another __syncwarp each lane walks
+// its post-noise hits.  All rows stay within the warp: no atomics, no extra CTA phase.
 template <int B>
 __device__ __forceinline__ void fused_gate(const KernelArgs &p, const DevOp &op, uint32_t code, uint32_t sub,
                                            uint64_t inst, uint64_t gb0, const uint32_t *tables, uint4 *X, uint4 *Z,
@@ -279,87 +347,52 @@ __device__ __forceinline__ void fused_gate(const KernelArgs &p, const DevOp &op,
     const Fused pre = decode_fused(p, op.d, inst), post = decode_fused(p, op.c, inst);
     const bool pair = code == OP_2Q;
     const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
-    for (uint32_t item = tid; item < nseg * B; item += nt) {
-        const bool valid = true;
+    const uint32_t items = nseg * B;  // (segment, block) pairs
+    const uint32_t lane = tid & 31u;
+    for (uint32_t item0 = tid - lane; item0 < items; item0 += nt) {  // warp-uniform trip count
+        const uint32_t item = item0 + lane;
+        const bool valid = item < items;
         const uint32_t q = item / B, blk = item % B;
+        const uint32_t u0 = q * GFS_SEG_UNITS;
+        const uint32_t un = valid ? min(GFS_SEG_UNITS, n - u0) : 0;
         const uint32_t block = (uint32_t)(gb0 + blk);
-        const uint32_t u0 = q * GFS_SEG_UNITS, un = min(GFS_SEG_UNITS, n - u0);
-        if (pre.ch && valid) {
-            walk_segment(*pre.ch, tables + pre.ch->table, p.seed, GFS_P_NOISE, pre.inst, q, block, un,
-                         [&](uint32_t k, uint32_t shot, gfs_stream *st) {
-                             const uint32_t bits = hit_bits(pre.kind, *pre.ch, st);
-                             const uint32_t u = u0 + k;
-                             const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
-                             const uint32_t i2 = pair ? __ldg(p.pool + a + 2 * u + 1) * B + blk : i1;
-                             apply_bits(X, Z, i1, i2, shot, bits, false);
-                         });
+        if (pre.ch) {
+            if (un) {
+                walk_segment(*pre.ch, tables + pre.ch->table, p.seed, GFS_P_NOISE, pre.inst, q, block, un,
+                             [&](uint32_t k, uint32_t shot, gfs_stream *st) {
+                                 const uint32_t bits = hit_bits(pre.kind, *pre.ch, st);
+                                 const uint32_t u = u0 + k;
+                                 const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
+                                 const uint32_t i2 = pair ? __ldg(p.pool + a + 2 * u + 1) * B + blk : i1;
+                                 apply_bits(X, Z, i1, i2, shot, bits, false);
+                             });
+            }
+            __syncwarp();
         }
-        for (uint32_t k = 0; k < un; k++) {
-            const uint32_t u = u0 + k;
-            const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
-            if (code == OP_2Q) {
-                const uint32_t i2 = __ldg(p.pool + a + 2 * u + 1) * B + blk;
-                uint4 x1 = X[i1], z1 = Z[i1], x2 = X[i2], z2 = Z[i2];
-                rule2v(sub, x1, z1, x2, z2);
-                X[i1] = x1;
-                Z[i1] = z1;
-                X[i2] = x2;
-                Z[i2] = z2;
-            } else if (code == OP_1Q) {
-                uint4 x = X[i1], z = Z[i1];
-                rule1(sub, x, z);
-                X[i1] = x;
-                Z[i1] = z;
-            } else if (code == OP_MEASURE) {
-                const uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, op.b + u, block));
-                const uint32_t slot = wrap(rec + u, L) * B + blk;
-                const uint4 x = X[i1], z = Z[i1];
-                switch (sub) {
-                    case KM_M:
-                        R[slot] = x;
-                        Z[i1] = r;
-                        break;
-                    case KM_MX:
-                        R[slot] = z;
-                        X[i1] = r;
-                        break;
-                    case KM_MY:
-                        R[slot] = x4(x, z);
-                        X[i1] = x4(x4(x, z), r);
-                        Z[i1] = r;
-                        break;
-                    case KM_MR:
-                        R[slot] = x;
-                        X[i1] = zero4();
-                        Z[i1] = r;
-                        break;
-                    case KM_MRX:
-                        R[slot] = z;
-                        Z[i1] = zero4();
-                        X[i1] = r;
-                        break;
-                    default:  // KM_MRY
-                        R[slot] = x4(x, z);
-                        Z[i1] = r;
-                        X[i1] = r;
-                        break;
-                }
-            } else {  // OP_RESET
-                const uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, op.b + u, block));
-                X[i1] = sub == KR_R ? zero4() : r;
-                Z[i1] = sub == KR_RX ? zero4() : r;
+        // The warp's items cover units [item0 / B * 4, ...) of B blocks: 128 (unit, block) gate items.
+        const uint32_t ubase = (item0 / B) * GFS_SEG_UNITS;
+#pragma unroll
+        for (uint32_t m = 0; m < GFS_SEG_UNITS; m++) {
+            const uint32_t j = m * 32 + lane;  // (unit, block) gate item of this warp, blocks fastest
+            const uint32_t u = ubase + j / B, gb = j % B;
+            if (u < n && (item0 + (j / B) / GFS_SEG_UNITS * B + gb) < items) {
+                gate_unit<B>(p, code, sub, a, op.b, inst, u, gb, (uint32_t)(gb0 + gb), X, Z, R, rec, L);
             }
         }
-        if (post.ch && valid) {
-            walk_segment(*post.ch, tables + post.ch->table, p.seed, GFS_P_NOISE, post.inst, q, block, un,
-                         [&](uint32_t k, uint32_t shot, gfs_stream *st) {
-                             const uint32_t bits = hit_bits(post.kind, *post.ch, st);
-                             const uint32_t u = u0 + k;
-                             const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
-                             const uint32_t i2 = pair ? __ldg(p.pool + a + 2 * u + 1) * B + blk : i1;
-                             apply_bits(X, Z, i1, i2, shot, bits, false);
-                         });
+        if (post.ch) {
+            __syncwarp();
+            if (un) {
+                walk_segment(*post.ch, tables + post.ch->table, p.seed, GFS_P_NOISE, post.inst, q, block, un,
+                             [&](uint32_t k, uint32_t shot, gfs_stream *st) {
+                                 const uint32_t bits = hit_bits(post.kind, *post.ch, st);
+                                 const uint32_t u = u0 + k;
+                                 const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
+                                 const uint32_t i2 = pair ? __ldg(p.pool + a + 2 * u + 1) * B + blk : i1;
+                                 apply_bits(X, Z, i1, i2, shot, bits, false);
+                             });
+            }
         }
+        __syncwarp();
     }
 }
 
@@ -383,6 +416,17 @@ __global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
             st_tables[i] = __ldg(p.tables + i);
         }
         tables = st_tables;
+    }
+    // The op stream is read by every thread at every op; keep it in shared memory when it is small.
+    const DevOp *ops = p.ops;
+    if (p.smem_ops) {
+        DevOp *so = reinterpret_cast<DevOp *>(st_tables + ((p.smem_table_words + 3) & ~3u));
+        const uint4 *src = reinterpret_cast<const uint4 *>(p.ops);
+        uint4 *dst = reinterpret_cast<uint4 *>(so);
+        for (uint32_t i = tid; i < p.smem_ops * (sizeof(DevOp) / sizeof(uint4)); i += nt) {
+            dst[i] = __ldg(src + i);
+        }
+        ops = so;
     }
 
     for (uint32_t slice = blockIdx.x; slice < p.nslices; slice += gridDim.x) {
@@ -410,7 +454,7 @@ __global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
         uint32_t pc = 0;
 
         for (;;) {
-            const DevOp op = p.ops[pc];
+            const DevOp op = ops[pc];
             const uint32_t code = op.code & 0xFFu, sub = op.code >> 8;
             const uint64_t inst = inst_base + op.inst;
             const uint32_t n = op.n, a = op.a;
@@ -754,9 +798,10 @@ __global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
     }
 }
 
-size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words) {
+size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words,
+                        uint32_t smem_ops) {
     return ((size_t)2 * nrows + ring + nobs + 2) * (size_t)blocks_per_cta * sizeof(uint4) +
-           (size_t)((table_words + 3) & ~3u) * sizeof(uint32_t);
+           (size_t)((table_words + 3) & ~3u) * sizeof(uint32_t) + (size_t)smem_ops * sizeof(DevOp);
 }
 
 template <int B>

@@ -27,6 +27,7 @@ struct KernelArgs {
     uint4 *meas_out;   // [local block][nmeas] (measurement mode only)
     uint32_t *status;  // device error word, 0 = ok
     uint32_t smem_table_words;  // > 0: copy the first smem_table_words of `tables` into shared memory
+    uint32_t smem_ops;          // > 0: copy the op stream (this many ops) into shared memory
 };
 
 struct LaunchShape {
@@ -36,7 +37,8 @@ struct LaunchShape {
     size_t smem;         // dynamic shared memory bytes
 };
 
-size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words);
+size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words,
+                        uint32_t smem_ops);
 cudaError_t launch_frame_kernel(const KernelArgs &args, const LaunchShape &shape, cudaStream_t stream);
 cudaError_t frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out);
 
