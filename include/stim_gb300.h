@@ -148,6 +148,13 @@ gfs_status gfs_sampler_get_shape(const gfs_sampler *s, int *blocks_per_cta, int 
                                  uint64_t *smem_bytes);
 
 /*
+ * Where the measurement record window lives: 0 = shared memory, 1 = a per-CTA region of a global
+ * (L2-resident) buffer, which frees shared memory for more resident CTAs; -1 = choose automatically (the
+ * default).  Results do not depend on it.
+ */
+gfs_status gfs_sampler_set_ring_placement(gfs_sampler *s, int placement);
+
+/*
  * Measures the shared-memory load+store throughput of `device` with a project-written probe kernel
  * (bytes per second summed over all SMs).  The frame kernel's roofline denominator.  No counterpart in
  * the reference (it has no GPU code).

@@ -111,6 +111,10 @@ class _SamplerBase:
                                           ctypes.byref(sm)))
         return {"blocks_per_cta": b.value, "threads": t.value, "grid": g.value, "smem_bytes": sm.value}
 
+    def set_ring_placement(self, placement: int):
+        """-1 automatic, 0 shared memory, 1 global memory (per-CTA, L2-resident)."""
+        check(lib().gfs_sampler_set_ring_placement(self._h, int(placement)))
+
     def set_chunk_shots(self, shots: int):
         check(lib().gfs_sampler_set_chunk_shots(self._h, int(shots)))
 

@@ -111,11 +111,12 @@ struct gfs_sampler {
     uint64_t next_block = 0;
     gfs::Program prog;
     DevBuf d_ops, d_pool, d_tables, d_chans, d_orig, d_status;
-    DevBuf det_tmp, obs_tmp, meas_tmp, out_tmp, ref_bits;
+    DevBuf det_tmp, obs_tmp, meas_tmp, out_tmp, ref_bits, ring_buf;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     gfs::LaunchShape shape{};
     int num_sms = 0;
+    int ring_pref = -1;  // -1 automatic, 0 shared memory, 1 global memory
     uint64_t chunk_shots = 0;
     double t_frame = 0, t_transpose = 0, t_copy = 0, t_total = 0;
     uint64_t n_frame = 0, n_transpose = 0;
@@ -143,16 +144,34 @@ struct gfs_sampler {
         return prog.ops.size() <= 256 ? (uint32_t)prog.ops.size() : 0;
     }
 
-    size_t smem_for(int bpc) const {
-        return gfs::frame_smem_bytes(prog.num_rows, prog.ring, (uint32_t)prog.num_observables, bpc,
-                                     smem_table_words(), smem_ops());
+    size_t smem_for(int bpc, bool ring_global) const {
+        return gfs::frame_smem_bytes(prog.num_rows, ring_global ? 0 : prog.ring, (uint32_t)prog.num_observables,
+                                     bpc, smem_table_words(), smem_ops());
     }
 
-    void choose_shape(int bpc, int threads, int grid) {
+    // ring: 0 = shared memory, 1 = global memory, -1 = whichever keeps more 128-shot blocks resident per SM.
+    void choose_shape(int bpc, int threads, int grid, int ring = -1) {
         cudaDeviceProp prop;
         ck(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
         num_sms = prop.multiProcessorCount;
-        size_t smem = smem_for(bpc);
+        if (ring < 0) {
+            auto resident = [&](bool g) {
+                gfs::LaunchShape t{bpc, threads, 1, smem_for(bpc, g), g};
+                if (t.smem > (size_t)prop.sharedMemPerBlockOptin) {
+                    return 0;
+                }
+                int per = 0;
+                if (gfs::frame_kernel_max_ctas_per_sm(t, &per) != cudaSuccess) {
+                    cudaGetLastError();
+                    return 0;
+                }
+                return per * bpc;
+            };
+            int in_smem = resident(false), in_global = resident(true);
+            ring = (in_smem == 0 || in_global * 2 >= in_smem * 3) ? 1 : 0;
+        }
+        const bool ring_global = ring == 1;
+        size_t smem = smem_for(bpc, ring_global);
         if (smem > (size_t)prop.sharedMemPerBlockOptin) {
             throw std::invalid_argument("circuit state (" + std::to_string(smem) +
                                         " bytes) does not fit in shared memory with " + std::to_string(bpc) +
@@ -161,7 +180,7 @@ struct gfs_sampler {
         if (threads <= 0 || threads > 256 || threads % 32) {
             throw std::invalid_argument("threads per CTA must be a multiple of 32 in [32, 256]");
         }
-        gfs::LaunchShape s{bpc, threads, 1, smem};
+        gfs::LaunchShape s{bpc, threads, 1, smem, ring_global};
         int per_sm = 0;
         ck(gfs::frame_kernel_max_ctas_per_sm(s, &per_sm), "occupancy");
         if (per_sm < 1) {
@@ -195,7 +214,7 @@ struct gfs_sampler {
         d_status.ensure(16, device);
         ck(cudaMemsetAsync(d_status.p, 0, 16, stream), "memset");
         int bpc = 1;
-        choose_shape(bpc, 256, 0);
+        choose_shape(bpc, 256, 0, ring_pref);
         ck(cudaStreamSynchronize(stream), "upload sync");
     }
 
@@ -264,6 +283,11 @@ struct gfs_sampler {
         a.status = (uint32_t *)d_status.p;
         a.smem_table_words = smem_table_words();
         a.smem_ops = smem_ops();
+        a.ring_global = nullptr;
+        if (shape.ring_global) {
+            ring_buf.ensure((uint64_t)shape.grid * (uint64_t)shape.blocks_per_cta * prog.ring * sizeof(uint4), device);
+            a.ring_global = (uint4 *)ring_buf.p;
+        }
         gfs::LaunchShape s = shape;
         s.grid = (int)std::min<uint64_t>((uint64_t)shape.grid, nslices);
         ck(gfs::launch_frame_kernel(a, s, stream), "frame kernel launch");
@@ -489,7 +513,19 @@ void detections_noalloc(gfs_sampler *s, uint64_t shots, uint32_t flags, uint8_t 
         a.status = (uint32_t *)s->d_status.p;
         a.smem_table_words = s->smem_table_words();
         a.smem_ops = s->smem_ops();
+        a.ring_global = nullptr;  // this path allocates nothing: the ring stays in shared memory
         gfs::LaunchShape shape = s->shape;
+        if (shape.ring_global) {
+            shape.ring_global = false;
+            shape.smem = s->smem_for(shape.blocks_per_cta, false);
+            int per_sm = 0;
+            ck(gfs::frame_kernel_max_ctas_per_sm(shape, &per_sm), "occupancy");
+            if (per_sm < 1) {
+                throw std::invalid_argument("the circuit's measurement ring does not fit in shared memory, which the "
+                                            "allocation-free entry point requires");
+            }
+            shape.grid = per_sm * s->num_sms;
+        }
         shape.grid = (int)std::min<uint64_t>((uint64_t)s->shape.grid, nslices);
         ck(cudaEventRecord(s->ev[1], s->stream), "event");
         ck(gfs::launch_frame_kernel(a, shape, s->stream), "frame kernel launch");
@@ -674,7 +710,18 @@ gfs_status gfs_sampler_set_shape(gfs_sampler *s, int blocks_per_cta, int threads
             throw std::invalid_argument("blocks_per_cta must be 1, 2 or 4");
         }
         ck(cudaSetDevice(s->device), "cudaSetDevice");
-        s->choose_shape(blocks_per_cta, threads, grid);
+        s->choose_shape(blocks_per_cta, threads, grid, s->ring_pref);
+    });
+}
+
+gfs_status gfs_sampler_set_ring_placement(gfs_sampler *s, int placement) {
+    return guarded([&] {
+        if (placement < -1 || placement > 1) {
+            throw std::invalid_argument("ring placement must be -1 (automatic), 0 (shared memory) or 1 (global memory)");
+        }
+        ck(cudaSetDevice(s->device), "cudaSetDevice");
+        s->ring_pref = placement;
+        s->choose_shape(s->shape.blocks_per_cta, s->shape.threads, 0, placement);
     });
 }
 

@@ -402,8 +402,10 @@ __global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
     const uint32_t nr = p.nrows, L = p.ring, NO = p.nobs;
     uint4 *X = sm;
     uint4 *Z = X + (size_t)nr * B;
-    uint4 *R = Z + (size_t)nr * B;
-    uint4 *O = R + (size_t)L * B;
+    // The measurement ring lives in shared memory, or (for large rings, to fit more CTAs per SM) in this
+    // CTA's own region of a global scratch buffer, which stays L2-resident.
+    uint4 *R = p.ring_global ? p.ring_global + (size_t)blockIdx.x * L * B : Z + (size_t)nr * B;
+    uint4 *O = p.ring_global ? Z + (size_t)nr * B : R + (size_t)L * B;
     uint4 *OCC = O + (size_t)NO * B;
     uint4 *MSK = OCC + B;
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
@@ -800,6 +802,7 @@ __global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
 
 size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words,
                         uint32_t smem_ops) {
+    // `ring` = measurement-ring rows held in shared memory (0 when the ring is in global memory).
     return ((size_t)2 * nrows + ring + nobs + 2) * (size_t)blocks_per_cta * sizeof(uint4) +
            (size_t)((table_words + 3) & ~3u) * sizeof(uint32_t) + (size_t)smem_ops * sizeof(DevOp);
 }

@@ -28,6 +28,7 @@ struct KernelArgs {
     uint32_t *status;  // device error word, 0 = ok
     uint32_t smem_table_words;  // > 0: copy the first smem_table_words of `tables` into shared memory
     uint32_t smem_ops;          // > 0: copy the op stream (this many ops) into shared memory
+    uint4 *ring_global;         // non-null: measurement ring in global memory, [CTA][ring row][block]
 };
 
 struct LaunchShape {
@@ -35,6 +36,7 @@ struct LaunchShape {
     int threads;         // threads per CTA
     int grid;            // CTAs (persistent: each walks slices grid-stride)
     size_t smem;         // dynamic shared memory bytes
+    bool ring_global;    // measurement ring in global memory (per-CTA region) instead of shared memory
 };
 
 size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words,
