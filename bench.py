@@ -142,15 +142,33 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
-def cpu_baseline(text, D, O, shots, threads):
+def cpu_baseline(text, D, O, chunk, threads, min_s, max_s):
+    """The oracle port on the host cores: consecutive `chunk`-shot calls until at least `min_s` seconds of
+    CPU work (at most `max_s`) have been timed.  Returns (Gbit/s, seconds, shots)."""
     from oracle.oracle import OracleCircuit
 
     c = OracleCircuit(text)
-    c.sample(min(shots, 1024), 1, threads=threads)  # warm
+    c.sample(min(chunk, 1024), 1, threads=threads)  # warm
+    shots = 0
     t0 = time.perf_counter()
-    c.sample(shots, 2, threads=threads)
-    dt = time.perf_counter() - t0
-    return shots * (D + O) / dt / 1e9, dt
+    while True:
+        c.sample(chunk, 2, first_shot=shots, threads=threads)
+        shots += chunk
+        dt = time.perf_counter() - t0
+        if dt >= min_s or dt + dt / (shots // chunk) > max_s:
+            break
+    return shots * (D + O) / dt / 1e9, dt, shots
+
+
+def _measured_hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            v = json.load(f).get("hbm_gbs")
+            if v:
+                return float(v)
+    except (OSError, ValueError):
+        pass
+    return 6800.0
 
 
 def run_reference(args):
@@ -163,7 +181,7 @@ def run_reference(args):
     c = OracleCircuit(text)
     D, O = c.num_detectors, c.num_observables
     threads = os.cpu_count() or 1
-    sample_shots = args.cpu_shots
+    sample_shots = args.ref_shots
     for _ in range(args.warmup):
         c.sample(sample_shots, 0, threads=threads)
     times = []
@@ -179,7 +197,8 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 bitwise",
         "data": "synthetic (reference-generated circuit, seeded shots)",
         "config": {"workload": "surface_code:rotated_memory_z d=25 r=25 p=1e-3", "shots_per_step": sample_shots,
-                   "note": "oracle port (oracle/stim_oracle.c) on host cores; the reference tree is not present here"},
+                   "note": "oracle port (oracle/stim_oracle.c, pthreads over 1024-shot batches, 64-bit words) on "
+                           "the host cores; the reference's own sources are not available on this machine"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{sample_shots} shots per step x {args.steps} steps, 64-bit words"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -251,13 +270,18 @@ def run_gpu(args):
         dev_s = float(tt.item())
     value = world * args.steps * shots * (D + O) / dev_s / 1e9
 
-    # End to end through the public API into host numpy arrays.
+    # End to end through the public API into host numpy arrays that the caller reuses between requests
+    # (dets_out= / obs_out=, as a streaming caller does); the first call touches their pages.
+    host_dets = np.empty((shots, drow), dtype=np.uint8)
+    host_obs = np.empty((shots, orow), dtype=np.uint8)
     e2e_times = []
+    e2e_parts = []
     for k in range(args.e2e_steps + 1):
         t1 = time.perf_counter()
-        sampler.sample(shots, bit_packed=True, separate_observables=True)
+        sampler.sample(shots, bit_packed=True, separate_observables=True, dets_out=host_dets, obs_out=host_obs)
         if k:
             e2e_times.append(time.perf_counter() - t1)
+            e2e_parts.append(sampler.last_timings())
     e2e_s = sum(e2e_times)
     e2e_value = world * len(e2e_times) * shots * (D + O) / e2e_s / 1e9 if e2e_times else None
 
@@ -265,9 +289,14 @@ def run_gpu(args):
     frame_avg_s = statistics.mean(frame_ms) / 1e3
     achieved_gbs = acc_bits / 8 * shots / frame_avg_s / 1e9
     smem_peak = _native.measure_smem_peak(local) / 1e9
+    # Transpose: reads the detector-major rows (16 bytes per row per 128 shots) and writes the shot-major rows.
+    tr_ms = statistics.mean(t - f for t, f in zip(step_ms, frame_ms))
+    tr_bytes = shots * ((D + O) / 8 + drow + orow)
+    hbm_peak = _measured_hbm_peak()
 
     if rank == 0:
-        cb_value, cb_s = cpu_baseline(text, D, O, args.cpu_shots, os.cpu_count() or 1)
+        cb_value, cb_s, cb_shots = cpu_baseline(text, D, O, args.cpu_chunk, os.cpu_count() or 1, args.cpu_seconds,
+                                                3 * args.cpu_seconds)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
@@ -281,14 +310,25 @@ def run_gpu(args):
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": shots * (drow + orow),
-                    "ms_per_step": 1e3 * e2e_s / max(1, len(e2e_times))},
+                    "ms_per_step": 1e3 * e2e_s / max(1, len(e2e_times)),
+                    "p50_ms": 1e3 * statistics.median(e2e_times) if e2e_times else None,
+                    "p99_ms": 1e3 * max(e2e_times) if e2e_times else None,
+                    "api": "CompiledDetectorSampler.sample(shots, bit_packed=True, separate_observables=True, "
+                           "dets_out=, obs_out=) into reused host numpy arrays",
+                    "device_ms": {k: statistics.mean(p[k] for p in e2e_parts) for k in
+                                  ("frame_ms", "transpose_ms", "copy_ms", "total_ms")} if e2e_parts else None},
             "gpu_launches": launches,
             "roofline": {"bound": "smem", "achieved": achieved_gbs, "peak": smem_peak, "unit": "GB/s",
                          "frac": achieved_gbs / smem_peak, "traffic": None,
                          "basis": f"{acc_bits:.0f} frame-bit accesses/shot x {shots} shots per frame-kernel launch; "
                                   "peak = project shared-memory probe (gfs_measure_smem_peak)"},
+            "roofline_transpose": {"bound": "hbm", "achieved": tr_bytes / (tr_ms / 1e3) / 1e9, "peak": hbm_peak,
+                                   "unit": "GB/s", "frac": tr_bytes / (tr_ms / 1e3) / 1e9 / hbm_peak,
+                                   "basis": "detector-major rows read + shot-major rows written per step; "
+                                            "peak = measured HBM copy bandwidth"},
             "cpu_baseline": {"value": cb_value, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-                             "sample": f"{args.cpu_shots} shots of the same workload ({cb_s:.1f} s), oracle port"},
+                             "sample": f"{cb_shots} shots of the same workload in {args.cpu_chunk}-shot calls "
+                                       f"({cb_s:.1f} s), oracle port (64-bit words, pthreads)"},
             "clocks": clk,
         }
         print(json.dumps(line))
@@ -304,7 +344,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--shots", type=int, default=1 << 20)
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-shots", type=int, default=1 << 15)
+    ap.add_argument("--cpu-chunk", type=int, default=1 << 16)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-shots", type=int, default=1 << 20)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--shape", default="")
     args = ap.parse_args()

@@ -113,7 +113,9 @@ struct gfs_sampler {
     DevBuf d_ops, d_pool, d_tables, d_chans, d_orig, d_status;
     DevBuf det_tmp, obs_tmp, meas_tmp, out_tmp, ref_bits, ring_buf;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // device->host copies of host-destination chunks
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t pev[2][4] = {};  // per pipeline slot: chunk start, frame done, transpose done, copy done
     gfs::LaunchShape shape{};
     int num_sms = 0;
     int ring_pref = -1;  // -1 automatic, 0 shared memory, 1 global memory
@@ -125,9 +127,20 @@ struct gfs_sampler {
         if (stream) {
             cudaSetDevice(device);
             cudaStreamSynchronize(stream);
+            if (copy_stream) {
+                cudaStreamSynchronize(copy_stream);
+                cudaStreamDestroy(copy_stream);
+            }
             for (auto &e : ev) {
                 if (e) {
                     cudaEventDestroy(e);
+                }
+            }
+            for (auto &slot : pev) {
+                for (auto &e : slot) {
+                    if (e) {
+                        cudaEventDestroy(e);
+                    }
                 }
             }
             cudaStreamDestroy(stream);
@@ -203,8 +216,14 @@ struct gfs_sampler {
         }
         ck(cudaSetDevice(device), "cudaSetDevice");
         ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        ck(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
         for (auto &e : ev) {
             ck(cudaEventCreate(&e), "cudaEventCreate");
+        }
+        for (auto &slot : pev) {
+            for (auto &e : slot) {
+                ck(cudaEventCreate(&e), "cudaEventCreate");
+            }
         }
         upload(d_ops, prog.ops, device, stream);
         upload(d_pool, prog.pool, device, stream);
@@ -321,6 +340,113 @@ struct gfs_sampler {
         }
     }
 
+    // Chunk size (in 128-shot blocks) for host destinations: at least four chunks for requests of four or
+    // more full waves, so that copies overlap kernels, within the device memory budget.
+    uint64_t host_chunk_blocks(uint64_t nblk_total, uint64_t slot_row_bytes) const {
+        uint64_t cb = chunk_blocks(2 * slot_row_bytes);
+        if (chunk_shots) {
+            return cb;
+        }
+        uint64_t wave = (uint64_t)shape.grid * (uint64_t)shape.blocks_per_cta;
+        uint64_t quarter = (nblk_total + 3) / 4;
+        uint64_t target = std::max<uint64_t>(wave, ((quarter + wave - 1) / wave) * wave);
+        return std::min<uint64_t>(cb, target);
+    }
+
+    // Host destinations.  Chunk k is sampled and transposed on `stream` into slot k % 2 of a device
+    // staging buffer; its device->host copy runs on `copy_stream` while chunk k + 1's kernels run.  The
+    // copy of chunk k is issued only after chunk k + 1's kernels are queued, because a copy into pageable
+    // memory may hold the calling thread until it completes.
+    template <typename Produce, typename Copy>
+    void host_pipeline(uint64_t shots, uint64_t slot_row_bytes, Produce produce, Copy copy) {
+        uint64_t nblk_total = (shots + 127) / 128;
+        uint64_t cb = host_chunk_blocks(nblk_total, slot_row_bytes);
+        uint64_t slot_bytes = cb * 128 * slot_row_bytes;
+        out_tmp.ensure(std::max<uint64_t>(16, 2 * slot_bytes), device);
+        uint8_t *slots[2] = {(uint8_t *)out_tmp.p, (uint8_t *)out_tmp.p + slot_bytes};
+        struct Chunk {
+            uint64_t done, cs;
+        };
+        Chunk inflight[2] = {};
+        bool used[2] = {false, false};
+        auto account = [&](int slot) {
+            // The copy of this slot's chunk has completed, so its kernel events have too.
+            ck(cudaEventSynchronize(pev[slot][3]), "chunk copy");
+            float ms = 0;
+            ck(cudaEventElapsedTime(&ms, pev[slot][0], pev[slot][1]), "cudaEventElapsedTime");
+            t_frame += ms;
+            ck(cudaEventElapsedTime(&ms, pev[slot][1], pev[slot][2]), "cudaEventElapsedTime");
+            t_transpose += ms;
+            used[slot] = false;
+        };
+        auto issue_copy = [&](int slot) {
+            ck(cudaStreamWaitEvent(copy_stream, pev[slot][2], 0), "cudaStreamWaitEvent");
+            copy(inflight[slot].done, inflight[slot].cs, slots[slot]);
+            ck(cudaEventRecord(pev[slot][3], copy_stream), "event");
+        };
+        ck(cudaEventRecord(ev[0], stream), "event");
+        uint64_t done = 0;
+        int k = 0, prev = -1;
+        while (done < shots) {
+            const int slot = k & 1;
+            if (used[slot]) {
+                account(slot);
+            }
+            uint64_t cs = std::min<uint64_t>(shots - done, cb * 128);
+            uint64_t nblk = (cs + 127) / 128;
+            ck(cudaEventRecord(pev[slot][0], stream), "event");
+            run_frame(nblk, next_block);
+            ck(cudaEventRecord(pev[slot][1], stream), "event");
+            produce(done, cs, slots[slot]);
+            ck(cudaEventRecord(pev[slot][2], stream), "event");
+            inflight[slot] = Chunk{done, cs};
+            used[slot] = true;
+            if (prev >= 0) {
+                issue_copy(prev);
+            }
+            prev = slot;
+            next_block += nblk;
+            done += cs;
+            k++;
+        }
+        if (prev >= 0) {
+            issue_copy(prev);
+        }
+        ck(cudaEventRecord(ev[1], copy_stream), "event");
+        for (int slot = 0; slot < 2; slot++) {
+            if (used[slot]) {
+                account(slot);
+            }
+        }
+        ck(cudaStreamSynchronize(stream), "sample");
+        ck(cudaEventSynchronize(ev[1]), "sample");
+        t_total = elapsed(0, 1);
+        t_copy = std::max(0.0, t_total - t_frame - t_transpose);
+        check_status();
+    }
+
+    // Enqueues the transposes of one chunk's detection events (and observables) into dd / od.
+    void transpose_detections(uint32_t flags, uint64_t cs, uint8_t *dd, uint64_t ds, uint8_t *od, uint64_t os,
+                              bool want_dets, bool want_obs) {
+        bool packed = flags & GFS_BIT_PACKED;
+        uint64_t D = prog.num_detectors, O = prog.num_observables;
+        const uint4 *dt = (const uint4 *)det_tmp.p, *ot = (const uint4 *)obs_tmp.p;
+        if (want_dets) {
+            if ((flags & GFS_PREPEND_OBSERVABLES) && (flags & GFS_APPEND_OBSERVABLES)) {
+                transpose(ot, O, dt, D, ot, O, nullptr, cs, dd, ds, packed);
+            } else if (flags & GFS_PREPEND_OBSERVABLES) {
+                transpose(ot, O, dt, D, nullptr, 0, nullptr, cs, dd, ds, packed);
+            } else if (flags & GFS_APPEND_OBSERVABLES) {
+                transpose(dt, D, ot, O, nullptr, 0, nullptr, cs, dd, ds, packed);
+            } else {
+                transpose(dt, D, nullptr, 0, nullptr, 0, nullptr, cs, dd, ds, packed);
+            }
+        }
+        if (want_obs) {
+            transpose(ot, O, nullptr, 0, nullptr, 0, nullptr, cs, od, os, packed);
+        }
+    }
+
     // Shared driver for detections (host or device destinations).
     void detections(uint64_t shots, uint32_t flags, uint8_t *dets, uint64_t dstride, uint8_t *obs, uint64_t ostride,
                     bool device_out) {
@@ -337,6 +463,28 @@ struct gfs_sampler {
         }
         ck(cudaSetDevice(device), "cudaSetDevice");
         reset_timings();
+        if (!device_out) {
+            // Staging rows are padded to 32 bytes so the transpose writes whole sectors.
+            const uint64_t ds = pad32(drow), os = pad32(orow);
+            host_pipeline(
+                shots, ds + os,
+                [&](uint64_t, uint64_t cs, uint8_t *buf) {
+                    transpose_detections(flags, cs, buf, ds, buf + cs * ds, os, dets != nullptr, obs != nullptr);
+                },
+                [&](uint64_t done, uint64_t cs, uint8_t *buf) {
+                    if (dets && drow) {
+                        ck(cudaMemcpy2DAsync(dets + done * dstride, dstride, buf, ds, drow, cs,
+                                             cudaMemcpyDeviceToHost, copy_stream),
+                           "copy dets");
+                    }
+                    if (obs && orow) {
+                        ck(cudaMemcpy2DAsync(obs + done * ostride, ostride, buf + cs * ds, os, orow, cs,
+                                             cudaMemcpyDeviceToHost, copy_stream),
+                           "copy obs");
+                    }
+                });
+            return;
+        }
         ck(cudaEventRecord(ev[0], stream), "event");
         uint64_t cb = chunk_blocks(drow + orow);
         uint64_t done = 0;
@@ -346,45 +494,9 @@ struct gfs_sampler {
             ck(cudaEventRecord(ev[1], stream), "event");
             run_frame(nblk, next_block);
             ck(cudaEventRecord(ev[2], stream), "event");
-            const uint4 *dt = (const uint4 *)det_tmp.p, *ot = (const uint4 *)obs_tmp.p;
-            uint8_t *dd = nullptr, *od = nullptr;
-            if (device_out) {
-                dd = dets ? dets + done * dstride : nullptr;
-                od = obs ? obs + done * ostride : nullptr;
-            } else {
-                out_tmp.ensure(std::max<uint64_t>(16, cs * (pad32(drow) + pad32(orow))), device);
-                dd = (uint8_t *)out_tmp.p;
-                od = (uint8_t *)out_tmp.p + cs * pad32(drow);
-            }
-            // Staging rows are padded to 32 bytes so the transpose writes whole sectors.
-            uint64_t ds = device_out ? dstride : pad32(drow), os = device_out ? ostride : pad32(orow);
-            if (dets) {
-                if ((flags & GFS_PREPEND_OBSERVABLES) && (flags & GFS_APPEND_OBSERVABLES)) {
-                    transpose(ot, O, dt, D, ot, O, nullptr, cs, dd, ds, packed);
-                } else if (flags & GFS_PREPEND_OBSERVABLES) {
-                    transpose(ot, O, dt, D, nullptr, 0, nullptr, cs, dd, ds, packed);
-                } else if (flags & GFS_APPEND_OBSERVABLES) {
-                    transpose(dt, D, ot, O, nullptr, 0, nullptr, cs, dd, ds, packed);
-                } else {
-                    transpose(dt, D, nullptr, 0, nullptr, 0, nullptr, cs, dd, ds, packed);
-                }
-            }
-            if (obs) {
-                transpose(ot, O, nullptr, 0, nullptr, 0, nullptr, cs, od, os, packed);
-            }
+            transpose_detections(flags, cs, dets ? dets + done * dstride : nullptr, dstride,
+                                 obs ? obs + done * ostride : nullptr, ostride, dets != nullptr, obs != nullptr);
             ck(cudaEventRecord(ev[3], stream), "event");
-            if (!device_out) {
-                if (dets && drow) {
-                    ck(cudaMemcpy2DAsync(dets + done * dstride, dstride, dd, ds, drow, cs, cudaMemcpyDeviceToHost,
-                                         stream),
-                       "copy dets");
-                }
-                if (obs && orow) {
-                    ck(cudaMemcpy2DAsync(obs + done * ostride, ostride, od, os, orow, cs, cudaMemcpyDeviceToHost,
-                                         stream),
-                       "copy obs");
-                }
-            }
             ck(cudaStreamSynchronize(stream), "sample");
             t_frame += elapsed(1, 2);
             t_transpose += elapsed(2, 3);
@@ -416,35 +528,19 @@ struct gfs_sampler {
             ck(cudaMemcpyAsync(ref_bits.p, ref, (M + 7) / 8, cudaMemcpyHostToDevice, stream), "ref upload");
             dref = (const uint8_t *)ref_bits.p;
         }
-        ck(cudaEventRecord(ev[0], stream), "event");
-        uint64_t cb = chunk_blocks(row);
-        uint64_t done = 0;
-        while (done < shots) {
-            uint64_t cs = std::min<uint64_t>(shots - done, cb * 128);
-            uint64_t nblk = (cs + 127) / 128;
-            ck(cudaEventRecord(ev[1], stream), "event");
-            run_frame(nblk, next_block);
-            ck(cudaEventRecord(ev[2], stream), "event");
-            out_tmp.ensure(std::max<uint64_t>(16, cs * pad32(row)), device);
-            transpose((const uint4 *)meas_tmp.p, M, nullptr, 0, nullptr, 0, dref, cs, (uint8_t *)out_tmp.p, pad32(row),
-                      packed);
-            ck(cudaEventRecord(ev[3], stream), "event");
-            if (row) {
-                ck(cudaMemcpy2DAsync(out + done * stride, stride, out_tmp.p, pad32(row), row, cs,
-                                     cudaMemcpyDeviceToHost, stream),
-                   "copy meas");
-            }
-            ck(cudaStreamSynchronize(stream), "sample");
-            t_frame += elapsed(1, 2);
-            t_transpose += elapsed(2, 3);
-            check_status();
-            next_block += nblk;
-            done += cs;
-        }
-        ck(cudaEventRecord(ev[1], stream), "event");
-        ck(cudaStreamSynchronize(stream), "sample");
-        t_total = elapsed(0, 1);
-        t_copy = std::max(0.0, t_total - t_frame - t_transpose);
+        const uint64_t rs = pad32(row);
+        host_pipeline(
+            shots, rs,
+            [&](uint64_t, uint64_t cs, uint8_t *buf) {
+                transpose((const uint4 *)meas_tmp.p, M, nullptr, 0, nullptr, 0, dref, cs, buf, rs, packed);
+            },
+            [&](uint64_t done, uint64_t cs, uint8_t *buf) {
+                if (row) {
+                    ck(cudaMemcpy2DAsync(out + done * stride, stride, buf, rs, row, cs, cudaMemcpyDeviceToHost,
+                                         copy_stream),
+                       "copy meas");
+                }
+            });
     }
 };
 

@@ -11,8 +11,8 @@
 // go straight into its own rows); other noise ops apply their hits with shared atomics.  Detection events
 // stream to global memory as [block][detector] uint4 rows.
 //
-// transpose_kernel: turns [block][row] bit-rows into shot-major bytes with a 32x32 warp-ballot transpose
-// per word, replacing the reference's bit-by-bit numpy conversion (numpy.pybind.cc:20-63) and
+// transpose_tile_kernel: turns [block][row] bit-rows into shot-major bytes with 32x32 shuffle-butterfly
+// bit transposes, replacing the reference's bit-by-bit numpy conversion (numpy.pybind.cc:20-63) and
 // simd_bit_table::transpose_into (simd_bit_table.inl:192-208).
 #include <cstdio>
 
@@ -852,65 +852,13 @@ cudaError_t frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out) {
     }
 }
 
-// ------------------------------------------------------------------------------------------------
-// Shot-major output.  One warp per (128-shot block, 32 concatenated rows); 8 warps of a CTA cover 256
-// consecutive rows of the same block so that each shot's output bytes are written by one CTA.
-// ------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) transpose_kernel(const TransposeArgs t) {
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint64_t blk = blockIdx.x;
-    const uint64_t total = t.n0 + t.n1 + t.n2;
-    const uint64_t r0 = ((uint64_t)blockIdx.y * 8 + warp) * 32;
-    if (r0 >= total) {
-        return;
-    }
-    const uint64_t r = r0 + lane;
-    uint4 v = zero4();
-    if (r < t.n0) {
-        v = t.src0[blk * t.n0 + r];
-    } else if (r < t.n0 + t.n1) {
-        v = t.src1[blk * t.n1 + (r - t.n0)];
-    } else if (r < total) {
-        v = t.src2[blk * t.n2 + (r - t.n0 - t.n1)];
-    }
-    if (t.xor_rows && r < total && ((t.xor_rows[r >> 3] >> (r & 7)) & 1)) {
-        v = x4(v, make_uint4(~0u, ~0u, ~0u, ~0u));
-    }
-    const uint32_t words[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-    for (int w = 0; w < 4; w++) {
-        uint32_t mine = 0;
-#pragma unroll
-        for (int i = 0; i < 32; i++) {
-            uint32_t b = __ballot_sync(0xFFFFFFFFu, (words[w] >> i) & 1u);
-            if (lane == (uint32_t)i) {
-                mine = b;
-            }
-        }
-        uint64_t shot = blk * 128 + (uint64_t)w * 32 + lane;
-        if (shot >= t.nshots) {
-            continue;
-        }
-        uint8_t *row = t.out + shot * t.out_stride;
-        uint64_t nvalid = total - r0 < 32 ? total - r0 : 32;
-        if (t.bit_packed) {
-            uint64_t nbytes = (nvalid + 7) / 8;
-            for (uint64_t j = 0; j < nbytes; j++) {
-                row[r0 / 8 + j] = (uint8_t)(mine >> (8 * j));
-            }
-        } else {
-            for (uint64_t j = 0; j < nvalid; j++) {
-                row[r0 + j] = (uint8_t)((mine >> j) & 1u);
-            }
-        }
-    }
-}
-
-// Bit-packed shot-major output, tiled: a CTA of 256 threads owns (one 128-shot block, 256 concatenated
-// rows).  Each thread loads one row's uint4; each warp ballot-transposes its 32 rows into 4-byte words per
-// shot and stages them in shared memory; then thread pairs write each shot's 32 output bytes.  When the
-// destination row and stride are 16-byte aligned the writes are full 16-byte stores covering whole
-// 32-byte sectors; otherwise the widest aligned stores (8, 4, 2 or 1 bytes) are used.
+// Shot-major output, tiled: a CTA of 256 threads owns (one 128-shot block, 1024 concatenated rows).
+// Phase 1: each warp loads 4 groups of 32 rows (one uint4 = 128 shots per row) and turns every 32x32 bit
+// block around with a five-stage shuffle butterfly (recursive exchange of off-diagonal sub-blocks), leaving
+// lane l with 32 rows of shot 32w + l; the words are staged in shared memory as [shot][32 words].
+// Phase 2: each warp writes whole shot rows of the tile (128 bytes bit-packed, 1024 bytes unpacked) with
+// coalesced 4-byte stores; a destination that is not 4-byte aligned is written as aligned words assembled
+// with funnel shifts, and only the two partial words at the ends use byte stores.
 __device__ __forceinline__ uint4 load_concat(const TransposeArgs &t, uint64_t blk, uint64_t r, uint64_t total) {
     uint4 v = zero4();
     if (r < t.n0) {
@@ -926,89 +874,111 @@ __device__ __forceinline__ uint4 load_concat(const TransposeArgs &t, uint64_t bl
     return v;
 }
 
+// Lane r holds row r of a 32x32 bit matrix (bit c = column c); afterwards lane c holds column c.
+__device__ __forceinline__ uint32_t transpose32(uint32_t x, uint32_t lane) {
+    const uint32_t lo[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const uint32_t s = 16u >> k, m = lo[k];
+        const uint32_t y = __shfl_xor_sync(0xFFFFFFFFu, x, s);
+        x = (lane & s) ? ((x & ~m) | ((y >> s) & m)) : ((x & m) | ((y & m) << s));
+    }
+    return x;
+}
+
+constexpr uint32_t kTileRows = 1024, kTileWords = kTileRows / 32;
+
+// Word j of a shot's output chunk: the packed bits themselves, or four 0/1 bytes per nibble unpacked.
+__device__ __forceinline__ uint32_t chunk_word(const uint32_t *row, int32_t j, int packed) {
+    if (packed) {
+        return row[j];
+    }
+    const uint32_t v = (row[j >> 3] >> (4 * (j & 7))) & 0xFu;
+    return (v & 1u) | ((v >> 1) & 1u) << 8 | ((v >> 2) & 1u) << 16 | ((v >> 3) & 1u) << 24;
+}
+
 __global__ void __launch_bounds__(256) transpose_tile_kernel(const TransposeArgs t) {
-    __shared__ uint32_t tile[128][9];  // [shot][4-byte word of the 32-byte chunk], padded against conflicts
+    __shared__ uint32_t tile[128][kTileWords + 1];  // [shot][32-row word], padded against bank conflicts
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint64_t blk = blockIdx.x;
+    // Row tiles vary fastest across the grid, so the CTAs writing the pieces of the same shot rows run
+    // together and the 32-byte sectors they share are completed in L2 before eviction.
+    const uint64_t blk = blockIdx.y;
     const uint64_t total = t.n0 + t.n1 + t.n2;
-    const uint64_t r0 = (uint64_t)blockIdx.y * 256;
-    const uint4 v = load_concat(t, blk, r0 + tid, total);
-    const uint32_t words[4] = {v.x, v.y, v.z, v.w};
+    const uint64_t r0 = (uint64_t)blockIdx.x * kTileRows;
 #pragma unroll
-    for (int w = 0; w < 4; w++) {
-        uint32_t mine = 0;
+    for (uint32_t g = 0; g < 4; g++) {
+        const uint64_t r = r0 + 128 * warp + 32 * g + lane;
+        const uint4 v = load_concat(t, blk, r, total);
+        const uint32_t words[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-        for (int i = 0; i < 32; i++) {
-            uint32_t b = __ballot_sync(0xFFFFFFFFu, (words[w] >> i) & 1u);
-            if (lane == (uint32_t)i) {
-                mine = b;
-            }
+        for (uint32_t w = 0; w < 4; w++) {
+            tile[32 * w + lane][4 * warp + g] = transpose32(words[w], lane);
         }
-        tile[w * 32 + lane][warp] = mine;
     }
     __syncthreads();
-    const uint32_t s = tid >> 1, half = tid & 1;
-    const uint64_t shot = blk * 128 + s;
-    if (shot >= t.nshots) {
-        return;
-    }
-    const uint64_t row_bytes = (total + 7) / 8;
-    const uint64_t off = r0 / 8 + 16 * half;
-    if (off >= row_bytes) {
-        return;
-    }
-    const uint64_t n = row_bytes - off < 16 ? row_bytes - off : 16;
-    uint8_t *dst = t.out + shot * t.out_stride + off;
-    const uint32_t *src = &tile[s][4 * half];
-    if (n == 16 && ((uintptr_t)dst & 15) == 0) {
-        *reinterpret_cast<uint4 *>(dst) = make_uint4(src[0], src[1], src[2], src[3]);
-    } else if (n == 16 && ((uintptr_t)dst & 7) == 0) {
-        reinterpret_cast<uint2 *>(dst)[0] = make_uint2(src[0], src[1]);
-        reinterpret_cast<uint2 *>(dst)[1] = make_uint2(src[2], src[3]);
-    } else if (((uintptr_t)dst & 3) == 0) {
-        uint64_t k = 0;
-        for (; k + 4 <= n; k += 4) {
-            *reinterpret_cast<uint32_t *>(dst + k) = src[k / 4];
+    const uint64_t rows = total - r0 < kTileRows ? total - r0 : kTileRows;
+    const int packed = t.bit_packed;
+    const int32_t nbytes = (int32_t)(packed ? (rows + 7) / 8 : rows);
+    const uint64_t col = packed ? r0 / 8 : r0;
+    for (uint32_t s = warp; s < 128; s += 8) {
+        const uint64_t shot = blk * 128 + s;
+        if (shot >= t.nshots) {
+            break;
         }
-        for (; k < n; k++) {
-            dst[k] = (uint8_t)(src[k / 4] >> (8 * (k & 3)));
-        }
-    } else if (((uintptr_t)dst & 1) == 0) {
-        uint64_t k = 0;
-        for (; k + 2 <= n; k += 2) {
-            *reinterpret_cast<uint16_t *>(dst + k) = (uint16_t)(src[k / 4] >> (8 * (k & 3)));
-        }
-        for (; k < n; k++) {
-            dst[k] = (uint8_t)(src[k / 4] >> (8 * (k & 3)));
-        }
-    } else {
-        for (uint64_t k = 0; k < n; k++) {
-            dst[k] = (uint8_t)(src[k / 4] >> (8 * (k & 3)));
+        const uint32_t *row = tile[s];
+        uint8_t *dst = t.out + shot * t.out_stride + col;
+        const int32_t m = (int32_t)((uintptr_t)dst & 3);
+        uint32_t *base = reinterpret_cast<uint32_t *>(dst - m);
+        const int32_t nq = (m + nbytes + 3) / 4;
+        for (int32_t q = (int32_t)lane; q < nq; q += 32) {
+            const int32_t b0 = 4 * q - m;  // chunk byte held by byte 0 of aligned word q
+            if (b0 >= 0 && b0 + 4 <= nbytes) {
+                uint32_t val;
+                if (m == 0) {
+                    val = chunk_word(row, q, packed);
+                } else {
+                    val = __funnelshift_r(chunk_word(row, q - 1, packed), chunk_word(row, q, packed), 8 * (4 - m));
+                }
+                base[q] = val;
+            } else {
+                uint8_t *bytes = reinterpret_cast<uint8_t *>(base + q);
+                for (int32_t i = 0; i < 4; i++) {
+                    const int32_t b = b0 + i;
+                    if (b >= 0 && b < nbytes) {
+                        bytes[i] = (uint8_t)(chunk_word(row, b >> 2, packed) >> (8 * (b & 3)));
+                    }
+                }
+            }
         }
     }
 }
 
 cudaError_t launch_transpose(const TransposeArgs &args, cudaStream_t stream) {
-    uint64_t total = args.n0 + args.n1 + args.n2;
+    const uint64_t total = args.n0 + args.n1 + args.n2;
     if (total == 0 || args.nshots == 0) {
         return cudaSuccess;
     }
-    uint64_t nblk = (args.nshots + 127) / 128;
-    if (args.bit_packed) {
-        dim3 grid((unsigned)nblk, (unsigned)((total + 255) / 256));
-        if (grid.y > 65535) {
-            return cudaErrorInvalidValue;
-        }
-        transpose_tile_kernel<<<grid, 256, 0, stream>>>(args);
-        return cudaGetLastError();
-    }
-    uint64_t ngroups = (total + 31) / 32;
-    dim3 grid((unsigned)nblk, (unsigned)((ngroups + 7) / 8));
-    if (grid.y > 65535) {
+    const uint64_t tiles = (total + kTileRows - 1) / kTileRows;
+    if (tiles > 0x7FFFFFFFull) {
         return cudaErrorInvalidValue;
     }
-    transpose_kernel<<<grid, 256, 0, stream>>>(args);
-    return cudaGetLastError();
+    const uint64_t nblk = (args.nshots + 127) / 128;
+    const uint64_t per_launch = 65535;  // grid.y limit; larger requests are split by 128-shot block
+    for (uint64_t b0 = 0; b0 < nblk; b0 += per_launch) {
+        TransposeArgs t = args;
+        t.src0 = args.src0 ? args.src0 + b0 * args.n0 : nullptr;
+        t.src1 = args.src1 ? args.src1 + b0 * args.n1 : nullptr;
+        t.src2 = args.src2 ? args.src2 + b0 * args.n2 : nullptr;
+        t.out = args.out + b0 * 128 * args.out_stride;
+        t.nshots = args.nshots - b0 * 128;
+        const uint64_t nb = nblk - b0 < per_launch ? nblk - b0 : per_launch;
+        transpose_tile_kernel<<<dim3((unsigned)tiles, (unsigned)nb), 256, 0, stream>>>(t);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            return e;
+        }
+    }
+    return cudaSuccess;
 }
 
 // ------------------------------------------------------------------------------------------------
