@@ -164,6 +164,45 @@ gfs_status gfs_measure_smem_peak(int device, double *bytes_per_s);
 /* Maximum shots per device chunk (bounds HBM use); 0 restores the default. */
 gfs_status gfs_sampler_set_chunk_shots(gfs_sampler *s, uint64_t shots);
 
+/*
+ * Launch-shape autotuner: times the frame kernel on `trial_shots` shots (0 = 2^18) for each candidate
+ * shape (blocks per CTA x threads x ring placement) that fits and keeps the fastest; *best_ms (may be
+ * null) receives its time.  The sampler's stream position does not move and results never depend on the
+ * shape.  No counterpart in the reference (its CPU sampler has no launch shape).
+ */
+gfs_status gfs_sampler_autotune(gfs_sampler *s, uint64_t trial_shots, double *best_ms);
+
+/*
+ * Batched sampling: the next shots of many detection samplers in ONE persistent frame-kernel launch
+ * (work items = (circuit, 128-shot slice), claimed dynamically by the CTAs, most expensive circuits
+ * first), followed by each circuit's transpose; the launch sequence is captured as a CUDA graph and
+ * replayed while shot counts, destinations and launch shape stay the same.  Entry j returns exactly what
+ * gfs_sample_detections(samplers[j], shots[j], ...) would have returned at that point, and advances that
+ * sampler the same way (a sampler listed twice continues its stream from the first entry to the second).
+ * The samplers must stay alive, on one device, and unused elsewhere while the batch is in use.
+ * No counterpart in the reference, whose nearest equivalent is one CompiledDetectorSampler per circuit
+ * (src/stim/py/compiled_detector_sampler.pybind.cc:216-322).
+ */
+typedef struct gfs_batch gfs_batch;
+gfs_status gfs_batch_create(gfs_sampler *const *samplers, size_t n, gfs_batch **out);
+void gfs_batch_free(gfs_batch *b);
+/* dets[j] / obs[j]: device pointers (null skips that output); strides in bytes per shot. */
+gfs_status gfs_batch_sample_detections_device(gfs_batch *b, const uint64_t *shots, uint32_t flags, void *const *dets,
+                                              const uint64_t *dets_stride, void *const *obs,
+                                              const uint64_t *obs_stride);
+/* Same with host destinations (copied out of a device staging arena). */
+gfs_status gfs_batch_sample_detections(gfs_batch *b, const uint64_t *shots, uint32_t flags, uint8_t *const *dets,
+                                       const uint64_t *dets_stride, uint8_t *const *obs, const uint64_t *obs_stride);
+/* Launch shape of the batched kernel (ring_placement as in gfs_sampler_set_ring_placement). */
+gfs_status gfs_batch_set_shape(gfs_batch *b, int blocks_per_cta, int threads, int ring_placement);
+gfs_status gfs_batch_get_shape(const gfs_batch *b, int *blocks_per_cta, int *threads, int *grid, uint64_t *smem_bytes,
+                               int *ring_global);
+/* Times each candidate shape on these shot counts (samplers do not advance) and keeps the fastest. */
+gfs_status gfs_batch_autotune(gfs_batch *b, const uint64_t *shots, double *best_ms);
+/* out4: frame, transposes, host copies, whole call (ms); counts4: frame launches, transpose launches,
+ * graph launches, graph builds (cumulative). */
+gfs_status gfs_batch_last_timings(const gfs_batch *b, double *out4, uint64_t *counts4);
+
 #ifdef __cplusplus
 }
 #endif

@@ -118,6 +118,13 @@ class _SamplerBase:
     def set_chunk_shots(self, shots: int):
         check(lib().gfs_sampler_set_chunk_shots(self._h, int(shots)))
 
+    def autotune(self, trial_shots: int = 0) -> float:
+        """Times the frame kernel for each candidate launch shape and keeps the fastest (results never
+        depend on the shape; the stream position does not move).  Returns the best time in ms."""
+        ms = ctypes.c_double()
+        check(lib().gfs_sampler_autotune(self._h, int(trial_shots), ctypes.byref(ms)))
+        return ms.value
+
     def last_timings(self):
         t = (ctypes.c_double * 4)()
         c = (ctypes.c_uint64 * 2)()
@@ -230,3 +237,119 @@ class CompiledMeasurementSampler(_SamplerBase):
                 _ptr(self._ref) if self._ref is not None else None, _ptr(out),
                 out.strides[0] if out.size else max(1, out.shape[1])))
         return out
+
+
+class BatchSampler:
+    """The next shots of many detection samplers in one persistent kernel launch (replayed as a CUDA graph).
+
+    Entry j of a call returns exactly what ``samplers[j].sample(shots[j], ...)`` would have returned at that
+    point and advances that sampler the same way.  No counterpart in the reference, where each circuit has
+    its own CompiledDetectorSampler (compiled_detector_sampler.pybind.cc:216-322).
+    """
+
+    def __init__(self, samplers):
+        self._samplers = list(samplers)
+        if not self._samplers:
+            raise ValueError("a batch needs at least one sampler")
+        for s in self._samplers:
+            if not isinstance(s, CompiledDetectorSampler):
+                raise ValueError("BatchSampler takes CompiledDetectorSampler objects")
+        arr = (ctypes.c_void_p * len(self._samplers))(*[s._h.value for s in self._samplers])
+        h = ctypes.c_void_p()
+        check(lib().gfs_batch_create(arr, len(self._samplers), ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().gfs_batch_free(h)
+            self._h = None
+
+    def __len__(self):
+        return len(self._samplers)
+
+    def _shots(self, shots):
+        shots = [int(x) for x in shots]
+        if len(shots) != len(self._samplers):
+            raise ValueError("need one shot count per sampler")
+        if any(x < 0 for x in shots):
+            raise ValueError("shots must be non-negative")
+        return (ctypes.c_uint64 * len(shots))(*shots), shots
+
+    def _rows(self, flags_packed, prepend, append):
+        out = []
+        for s in self._samplers:
+            c = s._circuit
+            D, O = c.num_detectors, c.num_observables
+            nd = D + (O if prepend else 0) + (O if append else 0)
+            out.append(((nd + 7) // 8, (O + 7) // 8) if flags_packed else (nd, O))
+        return out
+
+    def sample(self, shots, *, bit_packed: bool = False, prepend_observables: bool = False,
+               append_observables: bool = False, separate_observables: bool = False):
+        """Returns a list with one entry per sampler, shaped like CompiledDetectorSampler.sample's result."""
+        if separate_observables and (append_observables or prepend_observables):
+            raise ValueError("Can't specify separate_observables=True with append_observables=True or "
+                             "prepend_observables=True")
+        cshots, shots = self._shots(shots)
+        n = len(shots)
+        rows = self._rows(bit_packed, prepend_observables, append_observables)
+        dtype = np.uint8 if bit_packed else np.bool_
+        dets = [np.empty((k, r[0]), dtype=dtype) for k, r in zip(shots, rows)]
+        obs = [np.empty((k, r[1]), dtype=dtype) for k, r in zip(shots, rows)] if separate_observables else None
+        flags = ((_native.PREPEND_OBSERVABLES if prepend_observables else 0)
+                 | (_native.APPEND_OBSERVABLES if append_observables else 0)
+                 | (_native.BIT_PACKED if bit_packed else 0))
+        dptr = (ctypes.c_void_p * n)(*[d.ctypes.data if d.size else None for d in dets])
+        dstr = (ctypes.c_uint64 * n)(*[max(1, d.strides[0]) if d.size else max(1, d.shape[1]) for d in dets])
+        if obs is not None:
+            optr = (ctypes.c_void_p * n)(*[o.ctypes.data if o.size else None for o in obs])
+            ostr = (ctypes.c_uint64 * n)(*[max(1, o.strides[0]) if o.size else max(1, o.shape[1]) for o in obs])
+        else:
+            optr = ostr = None
+        check(lib().gfs_batch_sample_detections(self._h, cshots, flags, dptr, dstr, optr, ostr))
+        if separate_observables:
+            return list(zip(dets, obs))
+        return dets
+
+    def sample_device(self, shots, dets_ptrs, dets_strides, obs_ptrs=None, obs_strides=None, *,
+                      bit_packed: bool = True, prepend_observables: bool = False, append_observables: bool = False):
+        """Writes each circuit's shot-major rows to caller-owned device buffers (raw device pointers)."""
+        cshots, shots = self._shots(shots)
+        n = len(shots)
+        flags = ((_native.PREPEND_OBSERVABLES if prepend_observables else 0)
+                 | (_native.APPEND_OBSERVABLES if append_observables else 0)
+                 | (_native.BIT_PACKED if bit_packed else 0))
+        dptr = (ctypes.c_void_p * n)(*[int(p) if p else None for p in dets_ptrs])
+        dstr = (ctypes.c_uint64 * n)(*[int(x) for x in dets_strides])
+        optr = ostr = None
+        if obs_ptrs is not None:
+            optr = (ctypes.c_void_p * n)(*[int(p) if p else None for p in obs_ptrs])
+            ostr = (ctypes.c_uint64 * n)(*[int(x) for x in obs_strides])
+        check(lib().gfs_batch_sample_detections_device(self._h, cshots, flags, dptr, dstr, optr, ostr))
+
+    def set_launch_shape(self, blocks_per_cta: int, threads: int = 256, ring_placement: int = -1):
+        check(lib().gfs_batch_set_shape(self._h, int(blocks_per_cta), int(threads), int(ring_placement)))
+
+    def launch_shape(self):
+        b, t, g, r = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        sm = ctypes.c_uint64()
+        check(lib().gfs_batch_get_shape(self._h, ctypes.byref(b), ctypes.byref(t), ctypes.byref(g),
+                                        ctypes.byref(sm), ctypes.byref(r)))
+        return {"blocks_per_cta": b.value, "threads": t.value, "grid": g.value, "smem_bytes": sm.value,
+                "ring_global": bool(r.value)}
+
+    def autotune(self, shots) -> float:
+        """Times each candidate launch shape on these shot counts and keeps the fastest; returns its ms."""
+        cshots, _ = self._shots(shots)
+        ms = ctypes.c_double()
+        check(lib().gfs_batch_autotune(self._h, cshots, ctypes.byref(ms)))
+        return ms.value
+
+    def last_timings(self):
+        t = (ctypes.c_double * 4)()
+        c = (ctypes.c_uint64 * 4)()
+        check(lib().gfs_batch_last_timings(self._h, t, c))
+        return {"frame_ms": t[0], "transpose_ms": t[1], "copy_ms": t[2], "total_ms": t[3],
+                "frame_launches": int(c[0]), "transpose_launches": int(c[1]), "graph_launches": int(c[2]),
+                "graph_builds": int(c[3])}

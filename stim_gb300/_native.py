@@ -51,12 +51,23 @@ def _declare(L):
         "gfs_sampler_set_chunk_shots": [_vp, _u64],
         "gfs_sampler_set_ring_placement": [_vp, ctypes.c_int],
         "gfs_measure_smem_peak": [ctypes.c_int, ctypes.POINTER(ctypes.c_double)],
+        "gfs_sampler_autotune": [_vp, _u64, ctypes.POINTER(ctypes.c_double)],
+        "gfs_batch_create": [ctypes.POINTER(_vp), ctypes.c_size_t, ctypes.POINTER(_vp)],
+        "gfs_batch_sample_detections_device": [_vp, ctypes.POINTER(_u64), ctypes.c_uint32, ctypes.POINTER(_vp),
+                                               ctypes.POINTER(_u64), ctypes.POINTER(_vp), ctypes.POINTER(_u64)],
+        "gfs_batch_sample_detections": [_vp, ctypes.POINTER(_u64), ctypes.c_uint32, ctypes.POINTER(_vp),
+                                        ctypes.POINTER(_u64), ctypes.POINTER(_vp), ctypes.POINTER(_u64)],
+        "gfs_batch_set_shape": [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+        "gfs_batch_get_shape": [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(_u64), ctypes.POINTER(ctypes.c_int)],
+        "gfs_batch_autotune": [_vp, ctypes.POINTER(_u64), ctypes.POINTER(ctypes.c_double)],
+        "gfs_batch_last_timings": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_u64)],
     }
     for name, args in sigs.items():
         f = getattr(L, name)
         f.restype = ctypes.c_int
         f.argtypes = args
-    for name in ("gfs_circuit_free", "gfs_sampler_free"):
+    for name in ("gfs_circuit_free", "gfs_sampler_free", "gfs_batch_free"):
         f = getattr(L, name)
         f.restype = None
         f.argtypes = [_vp]

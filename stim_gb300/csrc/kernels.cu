@@ -396,31 +396,41 @@ __device__ __forceinline__ void fused_gate(const KernelArgs &p, const DevOp &op,
     }
 }
 
+// Shared-memory layout of a CTA holding B blocks of 128 shots: X and Z frames [row][block], the
+// measurement ring [ring row][block] (unless it is in global memory), observable accumulators, the
+// correlated-error flags and mask, then the gap tables and the op stream when they are cached.
+struct FrameState {
+    uint4 *X, *Z, *R, *O, *OCC, *MSK;
+    const uint32_t *tables;
+    const DevOp *ops;
+};
+
+// Lays out shared memory for circuit `p` and copies its gap tables and op stream in; the copies are
+// visible after the next __syncthreads() (the first one in frame_slice).
 template <int B>
-__global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
-    extern __shared__ uint4 sm[];
+__device__ __forceinline__ FrameState frame_state(const KernelArgs &p, uint4 *sm) {
+    FrameState st;
     const uint32_t nr = p.nrows, L = p.ring, NO = p.nobs;
-    uint4 *X = sm;
-    uint4 *Z = X + (size_t)nr * B;
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    st.X = sm;
+    st.Z = st.X + (size_t)nr * B;
     // The measurement ring lives in shared memory, or (for large rings, to fit more CTAs per SM) in this
     // CTA's own region of a global scratch buffer, which stays L2-resident.
-    uint4 *R = p.ring_global ? p.ring_global + (size_t)blockIdx.x * L * B : Z + (size_t)nr * B;
-    uint4 *O = p.ring_global ? Z + (size_t)nr * B : R + (size_t)L * B;
-    uint4 *OCC = O + (size_t)NO * B;
-    uint4 *MSK = OCC + B;
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    const uint32_t *pool = p.pool;
+    st.R = p.ring_global ? p.ring_global + (size_t)blockIdx.x * p.ring_cta_stride : st.Z + (size_t)nr * B;
+    st.O = p.ring_global ? st.Z + (size_t)nr * B : st.R + (size_t)L * B;
+    st.OCC = st.O + (size_t)NO * B;
+    st.MSK = st.OCC + B;
     // Gap tables are read on every noise draw; keep them in shared memory when the launch reserved room.
-    const uint32_t *tables = p.tables;
-    uint32_t *st_tables = reinterpret_cast<uint32_t *>(MSK + B);
+    st.tables = p.tables;
+    uint32_t *st_tables = reinterpret_cast<uint32_t *>(st.MSK + B);
     if (p.smem_table_words) {
         for (uint32_t i = tid; i < p.smem_table_words; i += nt) {
             st_tables[i] = __ldg(p.tables + i);
         }
-        tables = st_tables;
+        st.tables = st_tables;
     }
     // The op stream is read by every thread at every op; keep it in shared memory when it is small.
-    const DevOp *ops = p.ops;
+    st.ops = p.ops;
     if (p.smem_ops) {
         DevOp *so = reinterpret_cast<DevOp *>(st_tables + ((p.smem_table_words + 3) & ~3u));
         const uint4 *src = reinterpret_cast<const uint4 *>(p.ops);
@@ -428,375 +438,439 @@ __global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
         for (uint32_t i = tid; i < p.smem_ops * (sizeof(DevOp) / sizeof(uint4)); i += nt) {
             dst[i] = __ldg(src + i);
         }
-        ops = so;
+        st.ops = so;
     }
+    return st;
+}
 
-    for (uint32_t slice = blockIdx.x; slice < p.nslices; slice += gridDim.x) {
-        const uint64_t lb0 = (uint64_t)slice * B;
-        const uint64_t gb0 = p.block0 + lb0;
+// Samples slice `slice` (blocks slice*B .. slice*B+B-1 of this launch) of circuit `p` from the start of
+// the circuit to its end, leaving detection events, observables and measurements in global memory.
+template <int B>
+__device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameState &st, uint32_t slice) {
+    const uint32_t nr = p.nrows, L = p.ring, NO = p.nobs;
+    uint4 *const X = st.X, *const Z = st.Z, *const R = st.R, *const O = st.O, *const OCC = st.OCC,
+               *const MSK = st.MSK;
+    const uint32_t *const tables = st.tables;
+    const DevOp *const ops = st.ops;
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t *pool = p.pool;
+    const uint64_t lb0 = (uint64_t)slice * B;
+    const uint64_t gb0 = p.block0 + lb0;
 
-        for (uint32_t i = tid; i < nr * B; i += nt) {
-            uint32_t r = i / B, blk = i % B;
-            X[i] = zero4();
-            Z[i] = u4(gfs_row_bits(p.seed, GFS_P_RESET, 0, __ldg(p.qubit_orig + r), (uint32_t)(gb0 + blk)));
+    for (uint32_t i = tid; i < nr * B; i += nt) {
+        uint32_t r = i / B, blk = i % B;
+        X[i] = zero4();
+        Z[i] = u4(gfs_row_bits(p.seed, GFS_P_RESET, 0, __ldg(p.qubit_orig + r), (uint32_t)(gb0 + blk)));
+    }
+    for (uint32_t i = tid; i < NO * B; i += nt) {
+        O[i] = zero4();
+    }
+    for (uint32_t i = tid; i < B; i += nt) {
+        OCC[i] = zero4();
+    }
+    __syncthreads();
+
+    uint32_t rec = 0;
+    uint64_t det_base = 0, meas_base = 0, inst_base = 0;
+    int depth = 0;
+    uint32_t loop_pc[kMaxLoopDepth + 1];
+    uint64_t loop_left[kMaxLoopDepth + 1], loop_base[kMaxLoopDepth + 1], loop_stride[kMaxLoopDepth + 1];
+    uint32_t pc = 0;
+
+    for (;;) {
+        const DevOp op = ops[pc];
+        const uint32_t code = op.code & 0xFFu, sub = op.code >> 8;
+        const uint64_t inst = inst_base + op.inst;
+        const uint32_t n = op.n, a = op.a;
+        if (code == OP_END) {
+            break;
         }
-        for (uint32_t i = tid; i < NO * B; i += nt) {
-            O[i] = zero4();
-        }
-        for (uint32_t i = tid; i < B; i += nt) {
-            OCC[i] = zero4();
-        }
-        __syncthreads();
-
-        uint32_t rec = 0;
-        uint64_t det_base = 0, meas_base = 0, inst_base = 0;
-        int depth = 0;
-        uint32_t loop_pc[kMaxLoopDepth + 1];
-        uint64_t loop_left[kMaxLoopDepth + 1], loop_base[kMaxLoopDepth + 1], loop_stride[kMaxLoopDepth + 1];
-        uint32_t pc = 0;
-
-        for (;;) {
-            const DevOp op = ops[pc];
-            const uint32_t code = op.code & 0xFFu, sub = op.code >> 8;
-            const uint64_t inst = inst_base + op.inst;
-            const uint32_t n = op.n, a = op.a;
-            if (code == OP_END) {
+        if (code == OP_LOOP_BEGIN) {
+            if (depth >= kMaxLoopDepth) {
+                if (tid == 0) {
+                    atomicOr(p.status, 1u);
+                }
                 break;
             }
-            if (code == OP_LOOP_BEGIN) {
-                if (depth >= kMaxLoopDepth) {
-                    if (tid == 0) {
-                        atomicOr(p.status, 1u);
-                    }
-                    break;
-                }
-                loop_pc[depth] = pc;
-                loop_left[depth] = (uint64_t)op.a | ((uint64_t)op.b << 32);
-                loop_base[depth] = inst_base;
-                loop_stride[depth] = (uint64_t)op.c | ((uint64_t)op.d << 32);
-                depth++;
-                inst_base = inst;
+            loop_pc[depth] = pc;
+            loop_left[depth] = (uint64_t)op.a | ((uint64_t)op.b << 32);
+            loop_base[depth] = inst_base;
+            loop_stride[depth] = (uint64_t)op.c | ((uint64_t)op.d << 32);
+            depth++;
+            inst_base = inst;
+            pc++;
+            continue;
+        }
+        if (code == OP_LOOP_END) {
+            int d = depth - 1;
+            if (--loop_left[d] > 0) {
+                inst_base += loop_stride[d];
+                pc = loop_pc[d] + 1;
+            } else {
+                inst_base = loop_base[d];
+                depth = d;
                 pc++;
-                continue;
             }
-            if (code == OP_LOOP_END) {
-                int d = depth - 1;
-                if (--loop_left[d] > 0) {
-                    inst_base += loop_stride[d];
-                    pc = loop_pc[d] + 1;
-                } else {
-                    inst_base = loop_base[d];
-                    depth = d;
-                    pc++;
-                }
-                continue;
-            }
+            continue;
+        }
 
-            if ((code == OP_1Q || code == OP_2Q || code == OP_MEASURE || code == OP_RESET) && (op.c | op.d)) {
-                fused_gate<B>(p, op, code, sub, inst, gb0, tables, X, Z, R, rec, L, tid, nt);
-                if (code == OP_MEASURE) {
-                    rec = wrap(rec + n, L);
-                }
-                __syncthreads();
-                pc++;
-                continue;
-            }
-
-            switch (code) {
-                case OP_1Q:
-                    for (uint32_t i = tid; i < n * B; i += nt) {
-                        uint32_t u = i / B, blk = i % B;
-                        uint32_t idx = __ldg(pool + a + u) * B + blk;
-                        uint4 x = X[idx], z = Z[idx];
-                        switch (sub) {
-                            case K1_H_XZ:
-                                X[idx] = z;
-                                Z[idx] = x;
-                                break;
-                            case K1_H_XY:
-                                Z[idx] = x4(z, x);
-                                break;
-                            case K1_H_YZ:
-                                X[idx] = x4(x, z);
-                                break;
-                            default:
-                                rule1(sub, x, z);
-                                X[idx] = x;
-                                Z[idx] = z;
-                                break;
-                        }
-                    }
-                    break;
-
-                case OP_2Q:
-                    if (sub == K2_CX || sub == K2_CZ) {
-                        // Two independent pairs per iteration: both pairs' loads are in flight together.
-                        const uint32_t items = n * B;
-                        for (uint32_t i = tid; i < items; i += 2 * nt) {
-                            const uint32_t i2b = i + nt;
-                            const bool two = i2b < items;
-                            const uint32_t ua = i / B, ba = i % B;
-                            const uint32_t ub = two ? i2b / B : ua, bb = two ? i2b % B : ba;
-                            const uint32_t a1 = __ldg(pool + a + 2 * ua) * B + ba, a2 = __ldg(pool + a + 2 * ua + 1) * B + ba;
-                            const uint32_t b1 = __ldg(pool + a + 2 * ub) * B + bb, b2 = __ldg(pool + a + 2 * ub + 1) * B + bb;
-                            uint4 az1 = Z[a1], az2 = Z[a2], ax1 = X[a1], ax2 = X[a2];
-                            uint4 bz1 = Z[b1], bz2 = Z[b2], bx1 = X[b1], bx2 = X[b2];
-                            if (sub == K2_CX) {
-                                Z[a1] = x4(az1, az2);
-                                X[a2] = x4(ax2, ax1);
-                                if (two) {
-                                    Z[b1] = x4(bz1, bz2);
-                                    X[b2] = x4(bx2, bx1);
-                                }
-                            } else {
-                                Z[a1] = x4(az1, ax2);
-                                Z[a2] = x4(az2, ax1);
-                                if (two) {
-                                    Z[b1] = x4(bz1, bx2);
-                                    Z[b2] = x4(bz2, bx1);
-                                }
-                            }
-                        }
-                        break;
-                    }
-                    for (uint32_t i = tid; i < n * B; i += nt) {
-                        uint32_t u = i / B, blk = i % B;
-                        uint32_t i1 = __ldg(pool + a + 2 * u) * B + blk;
-                        uint32_t i2 = __ldg(pool + a + 2 * u + 1) * B + blk;
-                        uint4 x1 = X[i1], z1 = Z[i1], x2 = X[i2], z2 = Z[i2];
-                        rule2v(sub, x1, z1, x2, z2);
-                        X[i1] = x1;
-                        Z[i1] = z1;
-                        X[i2] = x2;
-                        Z[i2] = z2;
-                    }
-                    break;
-
-                case OP_FEEDBACK:
-                    for (uint32_t i = tid; i < n * B; i += nt) {
-                        uint32_t u = i / B, blk = i % B;
-                        uint32_t k = __ldg(pool + a + 2 * u);
-                        uint32_t rm = __ldg(pool + a + 2 * u + 1);
-                        uint32_t idx = (rm & kRowMask) * B + blk;
-                        uint4 v = R[wrap(rec + L - k, L) * B + blk];
-                        if ((rm >> 24) & kFeedbackX) {
-                            X[idx] = x4(X[idx], v);
-                        }
-                        if ((rm >> 24) & kFeedbackZ) {
-                            Z[idx] = x4(Z[idx], v);
-                        }
-                    }
-                    break;
-
-                case OP_MEASURE:
-                    for (uint32_t i = tid; i < n * B; i += nt) {
-                        uint32_t u = i / B, blk = i % B;
-                        uint32_t idx = __ldg(pool + a + u) * B + blk;
-                        uint32_t slot = wrap(rec + u, L) * B + blk;
-                        uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, op.b + u, (uint32_t)(gb0 + blk)));
-                        uint4 x = X[idx], z = Z[idx];
-                        switch (sub) {
-                            case KM_M:
-                                R[slot] = x;
-                                Z[idx] = r;
-                                break;
-                            case KM_MX:
-                                R[slot] = z;
-                                X[idx] = r;
-                                break;
-                            case KM_MY:
-                                R[slot] = x4(x, z);
-                                X[idx] = x4(x4(x, z), r);
-                                Z[idx] = r;
-                                break;
-                            case KM_MR:
-                                R[slot] = x;
-                                X[idx] = zero4();
-                                Z[idx] = r;
-                                break;
-                            case KM_MRX:
-                                R[slot] = z;
-                                Z[idx] = zero4();
-                                X[idx] = r;
-                                break;
-                            default:  // KM_MRY
-                                R[slot] = x4(x, z);
-                                Z[idx] = r;
-                                X[idx] = r;
-                                break;
-                        }
-                    }
-                    rec = wrap(rec + n, L);
-                    break;
-
-                case OP_RESET:
-                    for (uint32_t i = tid; i < n * B; i += nt) {
-                        uint32_t u = i / B, blk = i % B;
-                        uint32_t idx = __ldg(pool + a + u) * B + blk;
-                        uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, op.b + u, (uint32_t)(gb0 + blk)));
-                        if (sub == KR_R) {
-                            X[idx] = zero4();
-                            Z[idx] = r;
-                        } else if (sub == KR_RX) {
-                            X[idx] = r;
-                            Z[idx] = zero4();
-                        } else {
-                            X[idx] = r;
-                            Z[idx] = r;
-                        }
-                    }
-                    break;
-
-                case OP_RECORD_ZERO:
-                    for (uint32_t i = tid; i < n * B; i += nt) {
-                        uint32_t u = i / B, blk = i % B;
-                        R[wrap(rec + u, L) * B + blk] = zero4();
-                    }
-                    rec = wrap(rec + n, L);
-                    break;
-
-                case OP_NOISE:
-                case OP_MNOISE: {
-                    // Standalone noise: one segment per lane; rows may repeat within an instruction, so hits
-                    // are applied with shared atomics.
-                    const bool meas = code == OP_MNOISE;
-                    const DevChan &ch = p.chans[op.b];
-                    const uint32_t *T = tables + ch.table;
-                    const bool pair = !meas && (sub == KN_DEP2 || sub == KN_PC2);
-                    const uint32_t kind = meas ? (uint32_t)KN_FLIP : sub;
-                    const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
-                    for (uint32_t item = tid; item < nseg * B; item += nt) {
-                        const uint32_t g = item / B, blk = item % B;
-                        const uint32_t u0 = g * GFS_SEG_UNITS;
-                        walk_segment(ch, T, p.seed, meas ? GFS_P_MNOISE : GFS_P_NOISE, inst, g, (uint32_t)(gb0 + blk),
-                                     min(GFS_SEG_UNITS, n - u0), [&](uint32_t k, uint32_t shot, gfs_stream *st) {
-                                         const uint32_t u = u0 + k;
-                                         if (meas) {
-                                             flip_bit(R, wrap(rec + L - n + u, L) * B + blk, shot, true);
-                                             return;
-                                         }
-                                         const uint32_t bits = hit_bits(kind, ch, st);
-                                         const uint32_t i1 = __ldg(pool + a + (pair ? 2 * u : u)) * B + blk;
-                                         const uint32_t i2 = pair ? __ldg(pool + a + 2 * u + 1) * B + blk : i1;
-                                         apply_bits(X, Z, i1, i2, shot, bits, true);
-                                     });
-                    }
-                    break;
-                }
-
-                case OP_HERALD: {
-                    const DevChan &ch = p.chans[op.b];
-                    const uint32_t *T = tables + ch.table;
-                    const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
-                    for (uint32_t item = tid; item < nseg * B; item += nt) {
-                        const uint32_t g = item / B, blk = item % B;
-                        const uint32_t u0 = g * GFS_SEG_UNITS;
-                        walk_segment(ch, T, p.seed, GFS_P_NOISE, inst, g, (uint32_t)(gb0 + blk),
-                                     min(GFS_SEG_UNITS, n - u0), [&](uint32_t k, uint32_t shot, gfs_stream *st) {
-                                         const uint32_t u = u0 + k;
-                                         const uint32_t c = gfs_stream_next(st);
-                                         const uint32_t idx = __ldg(pool + a + u) * B + blk;
-                                         atomic_or_bit(R, wrap(rec + L - n + u, L) * B + blk, shot);
-                                         const uint32_t v =
-                                             sub == 0 ? (c & 3u) : pauli_xz(gfs_choice_weighted(c, ch.cum, 4));
-                                         apply_bits(X, Z, idx, idx, shot, v, true);
-                                     });
-                    }
-                    break;
-                }
-
-                case OP_CORR_MASK: {
-                    const DevChan &ch = p.chans[op.b];
-                    for (uint32_t blk = tid; blk < (uint32_t)B; blk += nt) {
-                        uint32_t hw[4] = {0, 0, 0, 0};
-                        if (ch.active) {
-                            walk_segment(ch, tables + ch.table, p.seed, GFS_P_NOISE, inst, 0, (uint32_t)(gb0 + blk), 1,
-                                         [&](uint32_t, uint32_t shot, gfs_stream *) {
-                                             hw[shot >> 5] |= 1u << (shot & 31);
-                                         });
-                        }
-                        const uint4 hits = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-                        uint4 occ = sub == 0 ? zero4() : OCC[blk];
-                        uint4 mk = make_uint4(hits.x & ~occ.x, hits.y & ~occ.y, hits.z & ~occ.z, hits.w & ~occ.w);
-                        OCC[blk] = make_uint4(occ.x | mk.x, occ.y | mk.y, occ.z | mk.z, occ.w | mk.w);
-                        MSK[blk] = mk;
-                    }
-                    break;
-                }
-
-                case OP_CORR_APPLY:
-                    for (uint32_t i = tid; i < n * B; i += nt) {
-                        uint32_t u = i / B, blk = i % B;
-                        uint32_t rm = __ldg(pool + a + u);
-                        uint32_t idx = (rm & kRowMask) * B + blk;
-                        uint4 mk = MSK[blk];
-                        if ((rm >> 24) & 1) {
-                            X[idx] = x4(X[idx], mk);
-                        }
-                        if ((rm >> 24) & 2) {
-                            Z[idx] = x4(Z[idx], mk);
-                        }
-                    }
-                    break;
-
-                case OP_DETECTORS:
-                    for (uint32_t i = tid; i < n * B; i += nt) {
-                        uint32_t u = i / B, blk = i % B;
-                        uint32_t s = __ldg(pool + a + u), e = __ldg(pool + a + u + 1);
-                        uint4 acc = zero4();
-                        for (uint32_t j = s; j < e; j++) {
-                            uint32_t k = __ldg(pool + j);
-                            acc = x4(acc, R[wrap(rec + L - k, L) * B + blk]);
-                        }
-                        p.det_out[(lb0 + blk) * p.ndet + det_base + u] = acc;
-                    }
-                    det_base += n;
-                    break;
-
-                case OP_OBS:
-                    for (uint32_t i = tid; i < n * B; i += nt) {
-                        uint32_t u = i / B, blk = i % B;
-                        uint32_t t = __ldg(pool + a + u);
-                        uint4 v;
-                        if (t & kTermRecord) {
-                            v = R[wrap(rec + L - (t & kRowMask), L) * B + blk];
-                        } else {
-                            uint32_t idx = (t & kRowMask) * B + blk;
-                            v = zero4();
-                            if (t & kTermX) {
-                                v = x4(v, Z[idx]);
-                            }
-                            if (t & kTermZ) {
-                                v = x4(v, X[idx]);
-                            }
-                        }
-                        atomic_xor4(O, op.b * B + blk, v);
-                    }
-                    break;
-
-                case OP_EMIT:
-                    for (uint32_t i = tid; i < n * B; i += nt) {
-                        uint32_t u = i / B, blk = i % B;
-                        p.meas_out[(lb0 + blk) * p.nmeas + meas_base + u] = R[wrap(rec + L - n + u, L) * B + blk];
-                    }
-                    meas_base += n;
-                    break;
-
-                default:
-                    if (tid == 0) {
-                        atomicOr(p.status, 2u);
-                    }
-                    break;
+        if ((code == OP_1Q || code == OP_2Q || code == OP_MEASURE || code == OP_RESET) && (op.c | op.d)) {
+            fused_gate<B>(p, op, code, sub, inst, gb0, tables, X, Z, R, rec, L, tid, nt);
+            if (code == OP_MEASURE) {
+                rec = wrap(rec + n, L);
             }
             __syncthreads();
             pc++;
+            continue;
         }
 
-        for (uint32_t i = tid; i < NO * B; i += nt) {
-            uint32_t k = i / B, blk = i % B;
-            p.obs_out[(lb0 + blk) * NO + k] = O[i];
+        switch (code) {
+            case OP_1Q:
+                for (uint32_t i = tid; i < n * B; i += nt) {
+                    uint32_t u = i / B, blk = i % B;
+                    uint32_t idx = __ldg(pool + a + u) * B + blk;
+                    uint4 x = X[idx], z = Z[idx];
+                    switch (sub) {
+                        case K1_H_XZ:
+                            X[idx] = z;
+                            Z[idx] = x;
+                            break;
+                        case K1_H_XY:
+                            Z[idx] = x4(z, x);
+                            break;
+                        case K1_H_YZ:
+                            X[idx] = x4(x, z);
+                            break;
+                        default:
+                            rule1(sub, x, z);
+                            X[idx] = x;
+                            Z[idx] = z;
+                            break;
+                    }
+                }
+                break;
+
+            case OP_2Q:
+                if (sub == K2_CX || sub == K2_CZ) {
+                    // Two independent pairs per iteration: both pairs' loads are in flight together.
+                    const uint32_t items = n * B;
+                    for (uint32_t i = tid; i < items; i += 2 * nt) {
+                        const uint32_t i2b = i + nt;
+                        const bool two = i2b < items;
+                        const uint32_t ua = i / B, ba = i % B;
+                        const uint32_t ub = two ? i2b / B : ua, bb = two ? i2b % B : ba;
+                        const uint32_t a1 = __ldg(pool + a + 2 * ua) * B + ba, a2 = __ldg(pool + a + 2 * ua + 1) * B + ba;
+                        const uint32_t b1 = __ldg(pool + a + 2 * ub) * B + bb, b2 = __ldg(pool + a + 2 * ub + 1) * B + bb;
+                        uint4 az1 = Z[a1], az2 = Z[a2], ax1 = X[a1], ax2 = X[a2];
+                        uint4 bz1 = Z[b1], bz2 = Z[b2], bx1 = X[b1], bx2 = X[b2];
+                        if (sub == K2_CX) {
+                            Z[a1] = x4(az1, az2);
+                            X[a2] = x4(ax2, ax1);
+                            if (two) {
+                                Z[b1] = x4(bz1, bz2);
+                                X[b2] = x4(bx2, bx1);
+                            }
+                        } else {
+                            Z[a1] = x4(az1, ax2);
+                            Z[a2] = x4(az2, ax1);
+                            if (two) {
+                                Z[b1] = x4(bz1, bx2);
+                                Z[b2] = x4(bz2, bx1);
+                            }
+                        }
+                    }
+                    break;
+                }
+                for (uint32_t i = tid; i < n * B; i += nt) {
+                    uint32_t u = i / B, blk = i % B;
+                    uint32_t i1 = __ldg(pool + a + 2 * u) * B + blk;
+                    uint32_t i2 = __ldg(pool + a + 2 * u + 1) * B + blk;
+                    uint4 x1 = X[i1], z1 = Z[i1], x2 = X[i2], z2 = Z[i2];
+                    rule2v(sub, x1, z1, x2, z2);
+                    X[i1] = x1;
+                    Z[i1] = z1;
+                    X[i2] = x2;
+                    Z[i2] = z2;
+                }
+                break;
+
+            case OP_FEEDBACK:
+                for (uint32_t i = tid; i < n * B; i += nt) {
+                    uint32_t u = i / B, blk = i % B;
+                    uint32_t k = __ldg(pool + a + 2 * u);
+                    uint32_t rm = __ldg(pool + a + 2 * u + 1);
+                    uint32_t idx = (rm & kRowMask) * B + blk;
+                    uint4 v = R[wrap(rec + L - k, L) * B + blk];
+                    if ((rm >> 24) & kFeedbackX) {
+                        X[idx] = x4(X[idx], v);
+                    }
+                    if ((rm >> 24) & kFeedbackZ) {
+                        Z[idx] = x4(Z[idx], v);
+                    }
+                }
+                break;
+
+            case OP_MEASURE:
+                for (uint32_t i = tid; i < n * B; i += nt) {
+                    uint32_t u = i / B, blk = i % B;
+                    uint32_t idx = __ldg(pool + a + u) * B + blk;
+                    uint32_t slot = wrap(rec + u, L) * B + blk;
+                    uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, op.b + u, (uint32_t)(gb0 + blk)));
+                    uint4 x = X[idx], z = Z[idx];
+                    switch (sub) {
+                        case KM_M:
+                            R[slot] = x;
+                            Z[idx] = r;
+                            break;
+                        case KM_MX:
+                            R[slot] = z;
+                            X[idx] = r;
+                            break;
+                        case KM_MY:
+                            R[slot] = x4(x, z);
+                            X[idx] = x4(x4(x, z), r);
+                            Z[idx] = r;
+                            break;
+                        case KM_MR:
+                            R[slot] = x;
+                            X[idx] = zero4();
+                            Z[idx] = r;
+                            break;
+                        case KM_MRX:
+                            R[slot] = z;
+                            Z[idx] = zero4();
+                            X[idx] = r;
+                            break;
+                        default:  // KM_MRY
+                            R[slot] = x4(x, z);
+                            Z[idx] = r;
+                            X[idx] = r;
+                            break;
+                    }
+                }
+                rec = wrap(rec + n, L);
+                break;
+
+            case OP_RESET:
+                for (uint32_t i = tid; i < n * B; i += nt) {
+                    uint32_t u = i / B, blk = i % B;
+                    uint32_t idx = __ldg(pool + a + u) * B + blk;
+                    uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, op.b + u, (uint32_t)(gb0 + blk)));
+                    if (sub == KR_R) {
+                        X[idx] = zero4();
+                        Z[idx] = r;
+                    } else if (sub == KR_RX) {
+                        X[idx] = r;
+                        Z[idx] = zero4();
+                    } else {
+                        X[idx] = r;
+                        Z[idx] = r;
+                    }
+                }
+                break;
+
+            case OP_RECORD_ZERO:
+                for (uint32_t i = tid; i < n * B; i += nt) {
+                    uint32_t u = i / B, blk = i % B;
+                    R[wrap(rec + u, L) * B + blk] = zero4();
+                }
+                rec = wrap(rec + n, L);
+                break;
+
+            case OP_NOISE:
+            case OP_MNOISE: {
+                // Standalone noise: one segment per lane; rows may repeat within an instruction, so hits
+                // are applied with shared atomics.
+                const bool meas = code == OP_MNOISE;
+                const DevChan &ch = p.chans[op.b];
+                const uint32_t *T = tables + ch.table;
+                const bool pair = !meas && (sub == KN_DEP2 || sub == KN_PC2);
+                const uint32_t kind = meas ? (uint32_t)KN_FLIP : sub;
+                const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
+                for (uint32_t item = tid; item < nseg * B; item += nt) {
+                    const uint32_t g = item / B, blk = item % B;
+                    const uint32_t u0 = g * GFS_SEG_UNITS;
+                    walk_segment(ch, T, p.seed, meas ? GFS_P_MNOISE : GFS_P_NOISE, inst, g, (uint32_t)(gb0 + blk),
+                                 min(GFS_SEG_UNITS, n - u0), [&](uint32_t k, uint32_t shot, gfs_stream *st) {
+                                     const uint32_t u = u0 + k;
+                                     if (meas) {
+                                         flip_bit(R, wrap(rec + L - n + u, L) * B + blk, shot, true);
+                                         return;
+                                     }
+                                     const uint32_t bits = hit_bits(kind, ch, st);
+                                     const uint32_t i1 = __ldg(pool + a + (pair ? 2 * u : u)) * B + blk;
+                                     const uint32_t i2 = pair ? __ldg(pool + a + 2 * u + 1) * B + blk : i1;
+                                     apply_bits(X, Z, i1, i2, shot, bits, true);
+                                 });
+                }
+                break;
+            }
+
+            case OP_HERALD: {
+                const DevChan &ch = p.chans[op.b];
+                const uint32_t *T = tables + ch.table;
+                const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
+                for (uint32_t item = tid; item < nseg * B; item += nt) {
+                    const uint32_t g = item / B, blk = item % B;
+                    const uint32_t u0 = g * GFS_SEG_UNITS;
+                    walk_segment(ch, T, p.seed, GFS_P_NOISE, inst, g, (uint32_t)(gb0 + blk),
+                                 min(GFS_SEG_UNITS, n - u0), [&](uint32_t k, uint32_t shot, gfs_stream *st) {
+                                     const uint32_t u = u0 + k;
+                                     const uint32_t c = gfs_stream_next(st);
+                                     const uint32_t idx = __ldg(pool + a + u) * B + blk;
+                                     atomic_or_bit(R, wrap(rec + L - n + u, L) * B + blk, shot);
+                                     const uint32_t v =
+                                         sub == 0 ? (c & 3u) : pauli_xz(gfs_choice_weighted(c, ch.cum, 4));
+                                     apply_bits(X, Z, idx, idx, shot, v, true);
+                                 });
+                }
+                break;
+            }
+
+            case OP_CORR_MASK: {
+                const DevChan &ch = p.chans[op.b];
+                for (uint32_t blk = tid; blk < (uint32_t)B; blk += nt) {
+                    uint32_t hw[4] = {0, 0, 0, 0};
+                    if (ch.active) {
+                        walk_segment(ch, tables + ch.table, p.seed, GFS_P_NOISE, inst, 0, (uint32_t)(gb0 + blk), 1,
+                                     [&](uint32_t, uint32_t shot, gfs_stream *) {
+                                         hw[shot >> 5] |= 1u << (shot & 31);
+                                     });
+                    }
+                    const uint4 hits = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                    uint4 occ = sub == 0 ? zero4() : OCC[blk];
+                    uint4 mk = make_uint4(hits.x & ~occ.x, hits.y & ~occ.y, hits.z & ~occ.z, hits.w & ~occ.w);
+                    OCC[blk] = make_uint4(occ.x | mk.x, occ.y | mk.y, occ.z | mk.z, occ.w | mk.w);
+                    MSK[blk] = mk;
+                }
+                break;
+            }
+
+            case OP_CORR_APPLY:
+                for (uint32_t i = tid; i < n * B; i += nt) {
+                    uint32_t u = i / B, blk = i % B;
+                    uint32_t rm = __ldg(pool + a + u);
+                    uint32_t idx = (rm & kRowMask) * B + blk;
+                    uint4 mk = MSK[blk];
+                    if ((rm >> 24) & 1) {
+                        X[idx] = x4(X[idx], mk);
+                    }
+                    if ((rm >> 24) & 2) {
+                        Z[idx] = x4(Z[idx], mk);
+                    }
+                }
+                break;
+
+            case OP_DETECTORS:
+                for (uint32_t i = tid; i < n * B; i += nt) {
+                    uint32_t u = i / B, blk = i % B;
+                    uint32_t s = __ldg(pool + a + u), e = __ldg(pool + a + u + 1);
+                    uint4 acc = zero4();
+                    for (uint32_t j = s; j < e; j++) {
+                        uint32_t k = __ldg(pool + j);
+                        acc = x4(acc, R[wrap(rec + L - k, L) * B + blk]);
+                    }
+                    p.det_out[(lb0 + blk) * p.ndet + det_base + u] = acc;
+                }
+                det_base += n;
+                break;
+
+            case OP_OBS:
+                for (uint32_t i = tid; i < n * B; i += nt) {
+                    uint32_t u = i / B, blk = i % B;
+                    uint32_t t = __ldg(pool + a + u);
+                    uint4 v;
+                    if (t & kTermRecord) {
+                        v = R[wrap(rec + L - (t & kRowMask), L) * B + blk];
+                    } else {
+                        uint32_t idx = (t & kRowMask) * B + blk;
+                        v = zero4();
+                        if (t & kTermX) {
+                            v = x4(v, Z[idx]);
+                        }
+                        if (t & kTermZ) {
+                            v = x4(v, X[idx]);
+                        }
+                    }
+                    atomic_xor4(O, op.b * B + blk, v);
+                }
+                break;
+
+            case OP_EMIT:
+                for (uint32_t i = tid; i < n * B; i += nt) {
+                    uint32_t u = i / B, blk = i % B;
+                    p.meas_out[(lb0 + blk) * p.nmeas + meas_base + u] = R[wrap(rec + L - n + u, L) * B + blk];
+                }
+                meas_base += n;
+                break;
+
+            default:
+                if (tid == 0) {
+                    atomicOr(p.status, 2u);
+                }
+                break;
         }
         __syncthreads();
+        pc++;
+    }
+
+    for (uint32_t i = tid; i < NO * B; i += nt) {
+        uint32_t k = i / B, blk = i % B;
+        p.obs_out[(lb0 + blk) * NO + k] = O[i];
+    }
+    __syncthreads();
+}
+
+template <int B>
+__global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
+    extern __shared__ uint4 sm[];
+    const FrameState st = frame_state<B>(p, sm);
+    for (uint32_t slice = blockIdx.x; slice < p.nslices; slice += gridDim.x) {
+        frame_slice<B>(p, st, slice);
+    }
+}
+
+// Many circuits in one persistent launch: work items are (circuit, slice) pairs numbered circuit by
+// circuit (b.slice_prefix[j] = first item of circuit j); CTAs claim items from a global counter, so
+// expensive and cheap circuits balance across the SMs.  A CTA reloads the circuit's descriptor, gap tables
+// and op stream only when its next item belongs to another circuit.
+template <int B>
+__global__ void __launch_bounds__(256, 3) batch_frame_kernel(const BatchArgs b) {
+    extern __shared__ uint4 sm[];
+    __shared__ KernelArgs cur;
+    __shared__ uint32_t s_item, s_circ;
+    uint32_t have = 0xFFFFFFFFu;
+    FrameState st{};
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const uint32_t item = atomicAdd(b.counter, 1u);
+            s_item = item;
+            if (item < b.total_slices) {
+                uint32_t lo = 0, hi = b.ncircuits;  // last j with slice_prefix[j] <= item
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) / 2;
+                    if (b.slice_prefix[mid] <= item) {
+                        lo = mid;
+                    } else {
+                        hi = mid;
+                    }
+                }
+                s_circ = lo;
+                if (lo != have) {
+                    cur = b.circuits[lo];
+                }
+            }
+        }
+        __syncthreads();
+        const uint32_t item = s_item, j = s_circ;
+        if (item >= b.total_slices) {
+            break;
+        }
+        if (j != have) {
+            st = frame_state<B>(cur, sm);
+            have = j;
+        }
+        frame_slice<B>(cur, st, item - b.slice_prefix[j]);
     }
 }
 
@@ -825,6 +899,53 @@ cudaError_t launch_frame_kernel(const KernelArgs &args, const LaunchShape &shape
             return launch_b<2>(args, shape, stream);
         case 4:
             return launch_b<4>(args, shape, stream);
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+template <int B>
+static cudaError_t launch_batch_b(const BatchArgs &args, const LaunchShape &s, cudaStream_t stream) {
+    cudaError_t e = cudaFuncSetAttribute(batch_frame_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)s.smem);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    batch_frame_kernel<B><<<s.grid, s.threads, s.smem, stream>>>(args);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_frame_kernel(const BatchArgs &args, const LaunchShape &shape, cudaStream_t stream) {
+    switch (shape.blocks_per_cta) {
+        case 1:
+            return launch_batch_b<1>(args, shape, stream);
+        case 2:
+            return launch_batch_b<2>(args, shape, stream);
+        case 4:
+            return launch_batch_b<4>(args, shape, stream);
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+template <int B>
+static cudaError_t occ_batch_b(const LaunchShape &s, int *out) {
+    cudaError_t e = cudaFuncSetAttribute(batch_frame_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)s.smem);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, batch_frame_kernel<B>, s.threads, s.smem);
+}
+
+cudaError_t batch_frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out) {
+    switch (shape.blocks_per_cta) {
+        case 1:
+            return occ_batch_b<1>(shape, out);
+        case 2:
+            return occ_batch_b<2>(shape, out);
+        case 4:
+            return occ_batch_b<4>(shape, out);
         default:
             return cudaErrorInvalidValue;
     }

@@ -29,6 +29,17 @@ struct KernelArgs {
     uint32_t smem_table_words;  // > 0: copy the first smem_table_words of `tables` into shared memory
     uint32_t smem_ops;          // > 0: copy the op stream (this many ops) into shared memory
     uint4 *ring_global;         // non-null: measurement ring in global memory, [CTA][ring row][block]
+    uint64_t ring_cta_stride;   // uint4 entries between consecutive CTAs' regions of ring_global
+};
+
+// Several circuits in one launch (batch_frame_kernel): circuit j owns work items
+// slice_prefix[j] .. slice_prefix[j+1]-1, one per slice of its shots.
+struct BatchArgs {
+    const KernelArgs *circuits;
+    const uint32_t *slice_prefix;  // ncircuits + 1 entries
+    uint32_t ncircuits;
+    uint32_t total_slices;
+    uint32_t *counter;             // next unclaimed work item; zero before the launch
 };
 
 struct LaunchShape {
@@ -43,6 +54,8 @@ size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks
                         uint32_t smem_ops);
 cudaError_t launch_frame_kernel(const KernelArgs &args, const LaunchShape &shape, cudaStream_t stream);
 cudaError_t frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out);
+cudaError_t launch_batch_frame_kernel(const BatchArgs &args, const LaunchShape &shape, cudaStream_t stream);
+cudaError_t batch_frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out);
 
 // Transposes [local block][rows] bit-rows (128 shots per entry) of up to three sources, concatenated
 // (src0 rows, then src1, then src2), into shot-major output rows.  `xor_rows` (optional) is a bit vector over the

@@ -94,6 +94,9 @@ struct Lowerer {
         op.a = (uint32_t)prog.pool.size();
         op.inst = inst;
         prog.ops.push_back(op);
+        // Cost estimate per 128-shot block: units processed plus a fixed per-op overhead, times repetitions.
+        const double w = ((double)n + 64.0) * (double)mult;
+        prog.work = prog.work + w > 1e18 ? 1e18 : prog.work + w;
         return prog.ops.back();
     }
 

@@ -23,6 +23,7 @@ struct Program {
     uint64_t num_observables = 0;
     uint64_t num_measurements = 0;
     uint32_t max_loop_depth = 0;
+    double work = 0;  // estimated cost of one 128-shot block (orders circuits in a batched launch)
     CircuitStats stats;
 };
 

@@ -1,0 +1,588 @@
+// Host runtime shared by the C ABI entry points: CUDA error mapping, device buffers, and the sampler
+// object (lowered program on the device, stream, launch shape, chunked kernel launches).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/stim_gb300.h"
+#include "circuit.h"
+#include "gfs_contract.h"
+#include "kernels.h"
+#include "lower.h"
+
+namespace gfs_rt {
+
+extern thread_local std::string g_err;
+
+struct CudaError : std::runtime_error {
+    cudaError_t code;
+    CudaError(cudaError_t c, const char *what) : std::runtime_error(std::string(what) + ": " + cudaGetErrorString(c)), code(c) {
+    }
+};
+
+inline void ck(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) {
+        throw CudaError(e, what);
+    }
+}
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t n = 0;
+    int device = -1;
+    void ensure(size_t bytes, int dev) {
+        if (bytes <= n && p) {
+            return;
+        }
+        release();
+        if (bytes == 0) {
+            return;
+        }
+        ck(cudaMalloc(&p, bytes), "cudaMalloc");
+        n = bytes;
+        device = dev;
+    }
+    void release() {
+        if (p) {
+            cudaFree(p);
+        }
+        p = nullptr;
+        n = 0;
+    }
+    ~DevBuf() {
+        release();
+    }
+};
+
+template <typename T>
+void upload(DevBuf &b, const std::vector<T> &v, int dev, cudaStream_t s) {
+    size_t bytes = std::max<size_t>(v.size() * sizeof(T), 16);
+    b.ensure(bytes, dev);
+    if (!v.empty()) {
+        ck(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), "upload");
+    }
+}
+
+inline uint64_t pad32(uint64_t n) {
+    return (n + 31) & ~(uint64_t)31;
+}
+
+inline gfs_status fail(gfs_status st, const std::string &msg) {
+    g_err = msg;
+    return st;
+}
+
+template <typename F>
+gfs_status guarded(F f) {
+    try {
+        f();
+        return GFS_OK;
+    } catch (const std::out_of_range &e) {
+        return fail(GFS_ERR_OUT_OF_RANGE, e.what());
+    } catch (const std::invalid_argument &e) {
+        return fail(GFS_ERR_INVALID_ARGUMENT, e.what());
+    } catch (const CudaError &e) {
+        return fail(e.code == cudaErrorMemoryAllocation ? GFS_ERR_OUT_OF_MEMORY : GFS_ERR_CUDA, e.what());
+    } catch (const std::bad_alloc &) {
+        return fail(GFS_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (const std::exception &e) {
+        return fail(GFS_ERR_INTERNAL, e.what());
+    }
+}
+
+}  // namespace gfs_rt
+
+// Internal header: the runtime's own translation units use these helpers unqualified.
+using namespace gfs_rt;
+
+struct gfs_circuit {
+    gfs::Circuit circuit;
+    gfs::CircuitStats stats;
+};
+
+struct gfs_sampler {
+    using DevBuf = gfs_rt::DevBuf;
+    int device = 0;
+    uint32_t mode = 0;
+    uint64_t seed = 0;
+    uint64_t next_block = 0;
+    gfs::Program prog;
+    DevBuf d_ops, d_pool, d_tables, d_chans, d_orig, d_status;
+    DevBuf det_tmp, obs_tmp, meas_tmp, out_tmp, ref_bits, ring_buf;
+    cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // device->host copies of host-destination chunks
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t pev[2][4] = {};  // per pipeline slot: chunk start, frame done, transpose done, copy done
+    gfs::LaunchShape shape{};
+    int num_sms = 0;
+    int ring_pref = -1;  // -1 automatic, 0 shared memory, 1 global memory
+    uint64_t chunk_shots = 0;
+    double t_frame = 0, t_transpose = 0, t_copy = 0, t_total = 0;
+    uint64_t n_frame = 0, n_transpose = 0;
+
+    ~gfs_sampler() {
+        if (stream) {
+            cudaSetDevice(device);
+            cudaStreamSynchronize(stream);
+            if (copy_stream) {
+                cudaStreamSynchronize(copy_stream);
+                cudaStreamDestroy(copy_stream);
+            }
+            for (auto &e : ev) {
+                if (e) {
+                    cudaEventDestroy(e);
+                }
+            }
+            for (auto &slot : pev) {
+                for (auto &e : slot) {
+                    if (e) {
+                        cudaEventDestroy(e);
+                    }
+                }
+            }
+            cudaStreamDestroy(stream);
+        }
+    }
+
+    // Gap tables go to shared memory when they are small (up to 32 distinct probabilities).
+    uint32_t smem_table_words() const {
+        return prog.tables.size() <= 32 * GFS_TABLE_LEN ? (uint32_t)prog.tables.size() : 0;
+    }
+
+    // Small op streams go to shared memory too (every thread reads every op).
+    uint32_t smem_ops() const {
+        return prog.ops.size() <= 256 ? (uint32_t)prog.ops.size() : 0;
+    }
+
+    size_t smem_for(int bpc, bool ring_global) const {
+        return gfs::frame_smem_bytes(prog.num_rows, ring_global ? 0 : prog.ring, (uint32_t)prog.num_observables,
+                                     bpc, smem_table_words(), smem_ops());
+    }
+
+    // ring: 0 = shared memory, 1 = global memory, -1 = whichever keeps more 128-shot blocks resident per SM.
+    void choose_shape(int bpc, int threads, int grid, int ring = -1) {
+        cudaDeviceProp prop;
+        ck(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+        num_sms = prop.multiProcessorCount;
+        if (ring < 0) {
+            auto resident = [&](bool g) {
+                gfs::LaunchShape t{bpc, threads, 1, smem_for(bpc, g), g};
+                if (t.smem > (size_t)prop.sharedMemPerBlockOptin) {
+                    return 0;
+                }
+                int per = 0;
+                if (gfs::frame_kernel_max_ctas_per_sm(t, &per) != cudaSuccess) {
+                    cudaGetLastError();
+                    return 0;
+                }
+                return per * bpc;
+            };
+            int in_smem = resident(false), in_global = resident(true);
+            ring = (in_smem == 0 || in_global * 2 >= in_smem * 3) ? 1 : 0;
+        }
+        const bool ring_global = ring == 1;
+        size_t smem = smem_for(bpc, ring_global);
+        if (smem > (size_t)prop.sharedMemPerBlockOptin) {
+            throw std::invalid_argument("circuit state (" + std::to_string(smem) +
+                                        " bytes) does not fit in shared memory with " + std::to_string(bpc) +
+                                        " blocks per CTA");
+        }
+        if (threads <= 0 || threads > 256 || threads % 32) {
+            throw std::invalid_argument("threads per CTA must be a multiple of 32 in [32, 256]");
+        }
+        gfs::LaunchShape s{bpc, threads, 1, smem, ring_global};
+        int per_sm = 0;
+        ck(gfs::frame_kernel_max_ctas_per_sm(s, &per_sm), "occupancy");
+        if (per_sm < 1) {
+            throw std::invalid_argument("frame kernel cannot be resident with this launch shape");
+        }
+        s.grid = grid > 0 ? grid : per_sm * num_sms;
+        shape = s;
+    }
+
+    void init(const gfs_circuit *c, uint32_t m, uint64_t sd, int dev) {
+        device = dev;
+        mode = m;
+        seed = sd;
+        prog = gfs::lower(c->circuit, m == GFS_MODE_MEASUREMENTS ? gfs::SampleMode::MEASUREMENTS
+                                                               : gfs::SampleMode::DETECTIONS);
+        int count = 0;
+        ck(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
+        if (dev < 0 || dev >= count) {
+            throw std::invalid_argument("no CUDA device " + std::to_string(dev));
+        }
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        ck(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (auto &e : ev) {
+            ck(cudaEventCreate(&e), "cudaEventCreate");
+        }
+        for (auto &slot : pev) {
+            for (auto &e : slot) {
+                ck(cudaEventCreate(&e), "cudaEventCreate");
+            }
+        }
+        upload(d_ops, prog.ops, device, stream);
+        upload(d_pool, prog.pool, device, stream);
+        upload(d_tables, prog.tables, device, stream);
+        upload(d_chans, prog.chans, device, stream);
+        upload(d_orig, prog.qubit_orig, device, stream);
+        d_status.ensure(16, device);
+        ck(cudaMemsetAsync(d_status.p, 0, 16, stream), "memset");
+        int bpc = 1;
+        choose_shape(bpc, 256, 0, ring_pref);
+        ck(cudaStreamSynchronize(stream), "upload sync");
+    }
+
+    uint64_t per_block_bytes(uint64_t out_row_bytes) const {
+        uint64_t rows = prog.num_detectors + prog.num_observables + (mode == GFS_MODE_MEASUREMENTS ? prog.num_measurements : 0);
+        return rows * 16 + 128 * out_row_bytes;
+    }
+
+    uint64_t chunk_blocks(uint64_t out_row_bytes) const {
+        uint64_t bpc = (uint64_t)shape.blocks_per_cta;
+        if (chunk_shots) {
+            uint64_t b = std::max<uint64_t>(1, chunk_shots / 128);
+            return ((b + bpc - 1) / bpc) * bpc;
+        }
+        uint64_t budget = (uint64_t)3 << 30;
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+            budget = std::min<uint64_t>(budget, free_b / 3);
+        }
+        uint64_t b = std::max<uint64_t>(1, budget / std::max<uint64_t>(1, per_block_bytes(out_row_bytes)));
+        uint64_t wave = (uint64_t)shape.grid * bpc;
+        if (b > wave) {
+            b = (b / wave) * wave;
+        }
+        return std::max<uint64_t>(bpc, (b / bpc) * bpc);
+    }
+
+    void reset_timings() {
+        t_frame = t_transpose = t_copy = t_total = 0;
+        n_frame = n_transpose = 0;
+    }
+
+    float elapsed(int a, int b) {
+        float ms = 0;
+        ck(cudaEventElapsedTime(&ms, ev[a], ev[b]), "cudaEventElapsedTime");
+        return ms;
+    }
+
+    // Runs the frame kernel for nblk blocks starting at stream block `block0`; results land in the tmp buffers.
+    void run_frame(uint64_t nblk, uint64_t block0) {
+        uint64_t bpc = (uint64_t)shape.blocks_per_cta;
+        uint64_t nslices = (nblk + bpc - 1) / bpc;
+        uint64_t alloc_blocks = nslices * bpc;
+        det_tmp.ensure(std::max<uint64_t>(16, alloc_blocks * prog.num_detectors * 16), device);
+        obs_tmp.ensure(std::max<uint64_t>(16, alloc_blocks * prog.num_observables * 16), device);
+        if (mode == GFS_MODE_MEASUREMENTS) {
+            meas_tmp.ensure(std::max<uint64_t>(16, alloc_blocks * prog.num_measurements * 16), device);
+        }
+        gfs::KernelArgs a{};
+        a.ops = (const gfs::DevOp *)d_ops.p;
+        a.pool = (const uint32_t *)d_pool.p;
+        a.tables = (const uint32_t *)d_tables.p;
+        a.chans = (const gfs::DevChan *)d_chans.p;
+        a.qubit_orig = (const uint32_t *)d_orig.p;
+        a.nrows = prog.num_rows;
+        a.ring = prog.ring;
+        a.nobs = (uint32_t)prog.num_observables;
+        a.nslices = (uint32_t)nslices;
+        a.ndet = prog.num_detectors;
+        a.nmeas = prog.num_measurements;
+        a.seed = seed;
+        a.block0 = block0;
+        a.det_out = (uint4 *)det_tmp.p;
+        a.obs_out = (uint4 *)obs_tmp.p;
+        a.meas_out = (uint4 *)meas_tmp.p;
+        a.status = (uint32_t *)d_status.p;
+        a.smem_table_words = smem_table_words();
+        a.smem_ops = smem_ops();
+        a.ring_global = nullptr;
+        if (shape.ring_global) {
+            ring_buf.ensure((uint64_t)shape.grid * (uint64_t)shape.blocks_per_cta * prog.ring * sizeof(uint4), device);
+            a.ring_global = (uint4 *)ring_buf.p;
+            a.ring_cta_stride = (uint64_t)shape.blocks_per_cta * prog.ring;
+        }
+        gfs::LaunchShape s = shape;
+        s.grid = (int)std::min<uint64_t>((uint64_t)shape.grid, nslices);
+        ck(gfs::launch_frame_kernel(a, s, stream), "frame kernel launch");
+        n_frame++;
+    }
+
+    void transpose(const uint4 *s0, uint64_t n0, const uint4 *s1, uint64_t n1, const uint4 *s2, uint64_t n2,
+                   const uint8_t *xr, uint64_t nshots, uint8_t *out, uint64_t stride, bool packed) {
+        gfs::TransposeArgs t{};
+        t.src0 = s0;
+        t.n0 = n0;
+        t.src1 = s1;
+        t.n1 = n1;
+        t.src2 = s2;
+        t.n2 = n2;
+        t.xor_rows = xr;
+        t.nshots = nshots;
+        t.out = out;
+        t.out_stride = stride;
+        t.bit_packed = packed ? 1 : 0;
+        ck(gfs::launch_transpose(t, stream), "transpose launch");
+        n_transpose++;
+    }
+
+    void check_status() {
+        uint32_t st = 0;
+        ck(cudaMemcpy(&st, d_status.p, 4, cudaMemcpyDeviceToHost), "status read");
+        if (st) {
+            cudaMemset(d_status.p, 0, 4);
+            throw std::runtime_error("frame kernel reported error status " + std::to_string(st));
+        }
+    }
+
+    // Times the frame kernel on `trial_shots` shots for each candidate launch shape and keeps the fastest.
+    // The stream position does not move (the trial's results are discarded).
+    double autotune(uint64_t trial_shots) {
+        struct Cand {
+            int bpc, threads, ring;
+        };
+        const Cand cands[] = {{1, 256, 0}, {1, 256, 1}, {1, 128, 0}, {1, 128, 1}, {2, 256, 0},
+                              {2, 256, 1}, {2, 128, 0}, {2, 128, 1}, {4, 256, 0}, {4, 256, 1}};
+        const gfs::LaunchShape before = shape;
+        const uint64_t nblk = std::max<uint64_t>(1, (trial_shots + 127) / 128);
+        double best = -1;
+        gfs::LaunchShape best_shape = shape;
+        for (const Cand &c : cands) {
+            try {
+                choose_shape(c.bpc, c.threads, 0, c.ring);
+            } catch (const std::invalid_argument &) {
+                continue;
+            }
+            float total = 0;
+            for (int rep = 0; rep < 2; rep++) {
+                ck(cudaEventRecord(ev[1], stream), "event");
+                run_frame(nblk, next_block);
+                ck(cudaEventRecord(ev[2], stream), "event");
+                ck(cudaStreamSynchronize(stream), "autotune");
+                total = (float)elapsed(1, 2);
+            }
+            check_status();
+            if (best < 0 || total < best) {
+                best = total;
+                best_shape = shape;
+            }
+        }
+        shape = best < 0 ? before : best_shape;
+        return best;
+    }
+
+    // Chunk size (in 128-shot blocks) for host destinations: at least four chunks for requests of four or
+    // more full waves, so that copies overlap kernels, within the device memory budget.
+    uint64_t host_chunk_blocks(uint64_t nblk_total, uint64_t slot_row_bytes) const {
+        uint64_t cb = chunk_blocks(2 * slot_row_bytes);
+        if (chunk_shots) {
+            return cb;
+        }
+        uint64_t wave = (uint64_t)shape.grid * (uint64_t)shape.blocks_per_cta;
+        uint64_t quarter = (nblk_total + 3) / 4;
+        uint64_t target = std::max<uint64_t>(wave, ((quarter + wave - 1) / wave) * wave);
+        return std::min<uint64_t>(cb, target);
+    }
+
+    // Host destinations.  Chunk k is sampled and transposed on `stream` into slot k % 2 of a device
+    // staging buffer; its device->host copy runs on `copy_stream` while chunk k + 1's kernels run.  The
+    // copy of chunk k is issued only after chunk k + 1's kernels are queued, because a copy into pageable
+    // memory may hold the calling thread until it completes.
+    template <typename Produce, typename Copy>
+    void host_pipeline(uint64_t shots, uint64_t slot_row_bytes, Produce produce, Copy copy) {
+        uint64_t nblk_total = (shots + 127) / 128;
+        uint64_t cb = host_chunk_blocks(nblk_total, slot_row_bytes);
+        uint64_t slot_bytes = cb * 128 * slot_row_bytes;
+        out_tmp.ensure(std::max<uint64_t>(16, 2 * slot_bytes), device);
+        uint8_t *slots[2] = {(uint8_t *)out_tmp.p, (uint8_t *)out_tmp.p + slot_bytes};
+        struct Chunk {
+            uint64_t done, cs;
+        };
+        Chunk inflight[2] = {};
+        bool used[2] = {false, false};
+        auto account = [&](int slot) {
+            // The copy of this slot's chunk has completed, so its kernel events have too.
+            ck(cudaEventSynchronize(pev[slot][3]), "chunk copy");
+            float ms = 0;
+            ck(cudaEventElapsedTime(&ms, pev[slot][0], pev[slot][1]), "cudaEventElapsedTime");
+            t_frame += ms;
+            ck(cudaEventElapsedTime(&ms, pev[slot][1], pev[slot][2]), "cudaEventElapsedTime");
+            t_transpose += ms;
+            used[slot] = false;
+        };
+        auto issue_copy = [&](int slot) {
+            ck(cudaStreamWaitEvent(copy_stream, pev[slot][2], 0), "cudaStreamWaitEvent");
+            copy(inflight[slot].done, inflight[slot].cs, slots[slot]);
+            ck(cudaEventRecord(pev[slot][3], copy_stream), "event");
+        };
+        ck(cudaEventRecord(ev[0], stream), "event");
+        uint64_t done = 0;
+        int k = 0, prev = -1;
+        while (done < shots) {
+            const int slot = k & 1;
+            if (used[slot]) {
+                account(slot);
+            }
+            uint64_t cs = std::min<uint64_t>(shots - done, cb * 128);
+            uint64_t nblk = (cs + 127) / 128;
+            ck(cudaEventRecord(pev[slot][0], stream), "event");
+            run_frame(nblk, next_block);
+            ck(cudaEventRecord(pev[slot][1], stream), "event");
+            produce(done, cs, slots[slot]);
+            ck(cudaEventRecord(pev[slot][2], stream), "event");
+            inflight[slot] = Chunk{done, cs};
+            used[slot] = true;
+            if (prev >= 0) {
+                issue_copy(prev);
+            }
+            prev = slot;
+            next_block += nblk;
+            done += cs;
+            k++;
+        }
+        if (prev >= 0) {
+            issue_copy(prev);
+        }
+        ck(cudaEventRecord(ev[1], copy_stream), "event");
+        for (int slot = 0; slot < 2; slot++) {
+            if (used[slot]) {
+                account(slot);
+            }
+        }
+        ck(cudaStreamSynchronize(stream), "sample");
+        ck(cudaEventSynchronize(ev[1]), "sample");
+        t_total = elapsed(0, 1);
+        t_copy = std::max(0.0, t_total - t_frame - t_transpose);
+        check_status();
+    }
+
+    // Enqueues the transposes of one chunk's detection events (and observables) into dd / od.
+    void transpose_detections(uint32_t flags, uint64_t cs, uint8_t *dd, uint64_t ds, uint8_t *od, uint64_t os,
+                              bool want_dets, bool want_obs) {
+        bool packed = flags & GFS_BIT_PACKED;
+        uint64_t D = prog.num_detectors, O = prog.num_observables;
+        const uint4 *dt = (const uint4 *)det_tmp.p, *ot = (const uint4 *)obs_tmp.p;
+        if (want_dets) {
+            if ((flags & GFS_PREPEND_OBSERVABLES) && (flags & GFS_APPEND_OBSERVABLES)) {
+                transpose(ot, O, dt, D, ot, O, nullptr, cs, dd, ds, packed);
+            } else if (flags & GFS_PREPEND_OBSERVABLES) {
+                transpose(ot, O, dt, D, nullptr, 0, nullptr, cs, dd, ds, packed);
+            } else if (flags & GFS_APPEND_OBSERVABLES) {
+                transpose(dt, D, ot, O, nullptr, 0, nullptr, cs, dd, ds, packed);
+            } else {
+                transpose(dt, D, nullptr, 0, nullptr, 0, nullptr, cs, dd, ds, packed);
+            }
+        }
+        if (want_obs) {
+            transpose(ot, O, nullptr, 0, nullptr, 0, nullptr, cs, od, os, packed);
+        }
+    }
+
+    // Shared driver for detections (host or device destinations).
+    void detections(uint64_t shots, uint32_t flags, uint8_t *dets, uint64_t dstride, uint8_t *obs, uint64_t ostride,
+                    bool device_out) {
+        bool packed = flags & GFS_BIT_PACKED;
+        uint64_t D = prog.num_detectors, O = prog.num_observables;
+        uint64_t nd = D + ((flags & GFS_PREPEND_OBSERVABLES) ? O : 0) + ((flags & GFS_APPEND_OBSERVABLES) ? O : 0);
+        uint64_t drow = packed ? (nd + 7) / 8 : nd;
+        uint64_t orow = packed ? (O + 7) / 8 : O;
+        if (dets && dstride < drow) {
+            throw std::invalid_argument("dets row stride too small");
+        }
+        if (obs && ostride < orow) {
+            throw std::invalid_argument("obs row stride too small");
+        }
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        reset_timings();
+        if (!device_out) {
+            // Staging rows are padded to 32 bytes so the transpose writes whole sectors.
+            const uint64_t ds = pad32(drow), os = pad32(orow);
+            host_pipeline(
+                shots, ds + os,
+                [&](uint64_t, uint64_t cs, uint8_t *buf) {
+                    transpose_detections(flags, cs, buf, ds, buf + cs * ds, os, dets != nullptr, obs != nullptr);
+                },
+                [&](uint64_t done, uint64_t cs, uint8_t *buf) {
+                    if (dets && drow) {
+                        ck(cudaMemcpy2DAsync(dets + done * dstride, dstride, buf, ds, drow, cs,
+                                             cudaMemcpyDeviceToHost, copy_stream),
+                           "copy dets");
+                    }
+                    if (obs && orow) {
+                        ck(cudaMemcpy2DAsync(obs + done * ostride, ostride, buf + cs * ds, os, orow, cs,
+                                             cudaMemcpyDeviceToHost, copy_stream),
+                           "copy obs");
+                    }
+                });
+            return;
+        }
+        ck(cudaEventRecord(ev[0], stream), "event");
+        uint64_t cb = chunk_blocks(drow + orow);
+        uint64_t done = 0;
+        while (done < shots) {
+            uint64_t cs = std::min<uint64_t>(shots - done, cb * 128);
+            uint64_t nblk = (cs + 127) / 128;
+            ck(cudaEventRecord(ev[1], stream), "event");
+            run_frame(nblk, next_block);
+            ck(cudaEventRecord(ev[2], stream), "event");
+            transpose_detections(flags, cs, dets ? dets + done * dstride : nullptr, dstride,
+                                 obs ? obs + done * ostride : nullptr, ostride, dets != nullptr, obs != nullptr);
+            ck(cudaEventRecord(ev[3], stream), "event");
+            ck(cudaStreamSynchronize(stream), "sample");
+            t_frame += elapsed(1, 2);
+            t_transpose += elapsed(2, 3);
+            check_status();
+            next_block += nblk;
+            done += cs;
+        }
+        ck(cudaEventRecord(ev[1], stream), "event");
+        ck(cudaStreamSynchronize(stream), "sample");
+        t_total = elapsed(0, 1);
+        t_copy = std::max(0.0, t_total - t_frame - t_transpose);
+    }
+
+    void measurements(uint64_t shots, uint32_t flags, const uint8_t *ref, uint8_t *out, uint64_t stride) {
+        if (mode != GFS_MODE_MEASUREMENTS) {
+            throw std::invalid_argument("sampler was not created in measurement mode");
+        }
+        bool packed = flags & GFS_BIT_PACKED;
+        uint64_t M = prog.num_measurements;
+        uint64_t row = packed ? (M + 7) / 8 : M;
+        if (stride < row) {
+            throw std::invalid_argument("output row stride too small");
+        }
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        reset_timings();
+        const uint8_t *dref = nullptr;
+        if (ref && M) {
+            ref_bits.ensure((M + 7) / 8, device);
+            ck(cudaMemcpyAsync(ref_bits.p, ref, (M + 7) / 8, cudaMemcpyHostToDevice, stream), "ref upload");
+            dref = (const uint8_t *)ref_bits.p;
+        }
+        const uint64_t rs = pad32(row);
+        host_pipeline(
+            shots, rs,
+            [&](uint64_t, uint64_t cs, uint8_t *buf) {
+                transpose((const uint4 *)meas_tmp.p, M, nullptr, 0, nullptr, 0, dref, cs, buf, rs, packed);
+            },
+            [&](uint64_t done, uint64_t cs, uint8_t *buf) {
+                if (row) {
+                    ck(cudaMemcpy2DAsync(out + done * stride, stride, buf, rs, row, cs, cudaMemcpyDeviceToHost,
+                                         copy_stream),
+                       "copy meas");
+                }
+            });
+    }
+};
+

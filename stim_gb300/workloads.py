@@ -107,3 +107,21 @@ def random_clifford_circuit(num_qubits: int, depth: int, seed: int, p_lo: float 
                 for k in range(n):
                     lines.append(f"DETECTOR rec[-{n - k}]")
     return "\n".join(lines) + "\n"
+
+
+def batched_workload(num_circuits: int = 256, seed: int = 2024, d_choices=tuple(range(3, 19, 2)),
+                     p_lo: float = 1e-4, p_hi: float = 1e-2, shots_lo: int = 1 << 12, shots_hi: int = 1 << 20):
+    """The many-circuit workload: rotated surface-code memory-Z circuits with d drawn uniformly from
+    d_choices and rounds = d, p log-uniform in [p_lo, p_hi], shot counts log-uniform in [shots_lo,
+    shots_hi], and one sampling seed per circuit; all draws come from a generator seeded with `seed`.
+    Returns a list of dicts with keys text, distance, p, shots, seed."""
+    rng = random.Random(seed)
+    out = []
+    for _ in range(num_circuits):
+        d = d_choices[rng.randrange(len(d_choices))]
+        p = math.exp(rng.uniform(math.log(p_lo), math.log(p_hi)))
+        p = float(f"{p:.4g}")
+        shots = int(round(math.exp(rng.uniform(math.log(shots_lo), math.log(shots_hi)))))
+        out.append({"text": code_circuit("surface_code:rotated_memory_z", d, d, p), "distance": d, "p": p,
+                    "shots": shots, "seed": rng.randrange(1 << 62)})
+    return out
