@@ -250,14 +250,15 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    frame_ms, step_ms, launches = [], [], 0
+    frame_ms, noise_ms, step_ms, launches = [], [], [], 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
         flush.zero_()  # outputs exceed L2 anyway; also evict them between steps
         t = device_step()
         frame_ms.append(t["frame_ms"])
-        step_ms.append(t["frame_ms"] + t["transpose_ms"])
-        launches += t["frame_launches"] + t["transpose_launches"]
+        noise_ms.append(t["noise_ms"])
+        step_ms.append(t["frame_ms"] + t["noise_ms"] + t["transpose_ms"])
+        launches += t["frame_launches"] + t["noise_launches"] + t["transpose_launches"]
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     if world > 1:
@@ -290,11 +291,12 @@ def run_gpu(args):
     achieved_gbs = acc_bits / 8 * shots / frame_avg_s / 1e9
     smem_peak = _native.measure_smem_peak(local) / 1e9
     # Transpose: reads the detector-major rows (16 bytes per row per 128 shots) and writes the shot-major rows.
-    tr_ms = statistics.mean(t - f for t, f in zip(step_ms, frame_ms))
+    tr_ms = statistics.mean(t - f - z for t, f, z in zip(step_ms, frame_ms, noise_ms))
     tr_bytes = shots * ((D + O) / 8 + drow + orow)
     hbm_peak = _measured_hbm_peak()
 
     batched = run_batched(args, local) if args.batched else None
+    serving = run_serving(args, local) if args.serve_seconds > 0 else None
 
     if rank == 0:
         cb_value, cb_s, cb_shots = cpu_baseline(text, D, O, args.cpu_chunk, os.cpu_count() or 1, args.cpu_seconds,
@@ -309,6 +311,8 @@ def run_gpu(args):
                        "l2": "outputs (2 GB/step) exceed L2; a 256 MiB buffer is also rewritten between steps",
                        "parallelism": f"replicas by shot range x{world}"},
             "p50_ms": statistics.median(step_ms), "p99_ms": sorted(step_ms)[-1],
+            "kernel_ms": {"frame": statistics.mean(frame_ms), "noise": statistics.mean(noise_ms),
+                          "transpose": tr_ms},
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": shots * (drow + orow),
@@ -318,7 +322,8 @@ def run_gpu(args):
                     "api": "CompiledDetectorSampler.sample(shots, bit_packed=True, separate_observables=True, "
                            "dets_out=, obs_out=) into reused host numpy arrays",
                     "device_ms": {k: statistics.mean(p[k] for p in e2e_parts) for k in
-                                  ("frame_ms", "transpose_ms", "copy_ms", "total_ms")} if e2e_parts else None},
+                                  ("frame_ms", "noise_ms", "transpose_ms", "copy_ms", "total_ms")}
+                    if e2e_parts else None},
             "gpu_launches": launches,
             "roofline": {"bound": "smem", "achieved": achieved_gbs, "peak": smem_peak, "unit": "GB/s",
                          "frac": achieved_gbs / smem_peak, "traffic": None,
@@ -333,6 +338,7 @@ def run_gpu(args):
                                        f"({cb_s:.1f} s), oracle port (64-bit words, pthreads)"},
             "clocks": clk,
             "batched": batched,
+            "serving": serving,
         }
         print(json.dumps(line))
     if world > 1:
@@ -405,6 +411,110 @@ def run_batched(args, local):
     }
 
 
+def run_serving(args, local):
+    """Open-loop serving: Poisson arrivals at --serve-rate requests/s for --serve-seconds, each request a
+    generated code circuit (repetition d 3..51, rotated surface X/Z d 3..21, color d 3..15; rounds = d;
+    p log-uniform [1e-4, 1e-2] on a 16-per-decade grid; shots log-uniform [2^10, 2^22]; own seed),
+    submitted to the continuous-batching server with bit-packed results in device memory.  Latency is
+    measured from each request's scheduled arrival to its completion, so client back-pressure (a full
+    result arena) counts against it."""
+    import collections
+
+    import torch
+
+    import stim_gb300
+    from stim_gb300 import workloads
+
+    wl = workloads.serving_workload(rate=args.serve_rate, seconds=args.serve_seconds, seed=7)
+    texts, dims = {}, {}
+    for w in wl:
+        key = (w["family"], w["distance"], w["p"])
+        if key not in texts:
+            t = workloads.code_circuit(w["family"], w["distance"], w["distance"], w["p"])
+            c = stim_gb300.Circuit(t)
+            texts[key] = t
+            dims[key] = (c.num_detectors, c.num_observables)
+    arena_bytes = args.serve_arena_gb << 30
+    arena = torch.empty(arena_bytes, dtype=torch.uint8, device=f"cuda:{local}")
+    base = arena.data_ptr()
+    server = stim_gb300.Server(device=local, hbm_budget=args.serve_hbm_gb << 30, max_chunk_shots=1 << 18)
+    for key, t in texts.items():  # warm the device-side circuit cache
+        D, O = dims[key]
+        server.submit_device(t, 0, seed=0, dets_ptr=base, dets_stride=(D + 7) // 8).result()
+    outstanding = collections.deque()  # (request, start, size): results held in the arena, oldest first
+    head = 0
+    lat = []
+    bits = 0
+
+    def retire(block):
+        while outstanding and (block or outstanding[0][0].done()):
+            r = outstanding.popleft()[0]
+            r.result()
+            lat.append(r.latency_ms + r._client_delay_ms)
+            block = False
+
+    def alloc(size):
+        # Ring allocation in the result arena; waits for the oldest request when there is no room.  The
+        # strict comparisons keep head != tail while the ring is wrapped.
+        nonlocal head
+        if size >= arena_bytes:
+            raise ValueError("request larger than the result arena")
+        while True:
+            if not outstanding:
+                head = 0
+            if not outstanding or head >= outstanding[0][1]:
+                tail = outstanding[0][1] if outstanding else arena_bytes
+                if head + size <= arena_bytes:
+                    start = head
+                    break
+                if size < tail and outstanding:
+                    start = 0
+                    break
+            elif head + size < outstanding[0][1]:
+                start = head
+                break
+            retire(True)
+        head = start + size
+        return start
+
+    t0 = time.perf_counter()
+    for w in wl:
+        key = (w["family"], w["distance"], w["p"])
+        D, O = dims[key]
+        drow, orow = (D + 7) // 8, (O + 7) // 8
+        size = (w["shots"] * (drow + orow) + 255) & ~255
+        now = time.perf_counter() - t0
+        if now < w["t"]:
+            time.sleep(w["t"] - now)
+        start = alloc(size)
+        sub = time.perf_counter() - t0
+        r = server.submit_device(texts[key], w["shots"], seed=w["seed"], dets_ptr=base + start, dets_stride=drow,
+                                 obs_ptr=base + start + w["shots"] * drow, obs_stride=orow)
+        r._client_delay_ms = max(0.0, 1e3 * (sub - w["t"]))
+        outstanding.append((r, start, size))
+        bits += w["shots"] * (D + O)
+        retire(False)
+    while outstanding:
+        retire(True)
+    wall = time.perf_counter() - t0
+    st = server.stats()
+    server.close()
+    lat.sort()
+    offered = sum(w["shots"] * sum(dims[(w["family"], w["distance"], w["p"])]) for w in wl) / args.serve_seconds
+    return {
+        "workload": f"Poisson {args.serve_rate:g} req/s for {args.serve_seconds:g} s; repetition d3-51, surface "
+                    "X/Z d3-21, color d3-15, rounds = d, p log-uniform [1e-4, 1e-2] (16 per decade), shots "
+                    "log-uniform [2^10, 2^22], per-request seed; bit-packed results in device memory",
+        "requests": len(wl), "distinct_circuits": len(texts),
+        "gbits": bits / wall / 1e9, "offered_gbits": offered / 1e9,
+        "p50_ms": lat[len(lat) // 2] if lat else None,
+        "p99_ms": lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)] if lat else None,
+        "wall_s": wall, "batches": st["batches"], "chunks_per_batch": st["chunks_per_batch"],
+        "cache_hits": st["cache_hits"], "cache_misses": st["cache_misses"],
+        "latency_basis": "scheduled arrival to completion (server completion time plus client submit delay)",
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -420,6 +530,10 @@ def main():
     ap.add_argument("--shape", default="")
     ap.add_argument("--batched", type=int, default=1)
     ap.add_argument("--batch-circuits", type=int, default=256)
+    ap.add_argument("--serve-seconds", type=float, default=2.0)
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-arena-gb", type=int, default=48)
+    ap.add_argument("--serve-hbm-gb", type=int, default=16)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

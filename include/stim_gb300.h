@@ -72,6 +72,17 @@ void gfs_circuit_free(gfs_circuit *c);
  * [7] = detectors.  Fails with the same errors as gfs_sampler_create's lowering step.
  */
 gfs_status gfs_program_info(const gfs_circuit *c, uint32_t mode, uint64_t *info8);
+/*
+ * The circuit's reference sample: its noiseless version run once on a host stabilizer tableau with every
+ * random measurement outcome forced to 0, bit-packed little-endian into out[0 .. (measurements+7)/8).
+ * Replaces TableauSimulator<W>::reference_sample_circuit (src/stim/simulators/tableau_simulator.inl:
+ * 1435-1438) behind Circuit.reference_sample() and compile_sampler() (src/stim/circuit/circuit.pybind.cc,
+ * src/stim/py/compiled_measurement_sampler.pybind.cc:63-83).  Host only, no GPU needed.
+ */
+gfs_status gfs_circuit_reference_sample(const gfs_circuit *c, uint8_t *out, uint64_t nbytes);
+/* Noise occurrences met by one pass over the lowered program (loops unrolled) and the expected number of
+ * noise hits per 128-shot block: the sizes of the hit lists (host only, no GPU needed). */
+gfs_status gfs_program_noise(const gfs_circuit *c, uint32_t mode, uint64_t *occurrences, double *hits_per_block);
 
 /*
  * Lowers the circuit for `mode` and uploads it to CUDA device `device`; the random stream starts at
@@ -165,6 +176,22 @@ gfs_status gfs_measure_smem_peak(int device, double *bytes_per_s);
 gfs_status gfs_sampler_set_chunk_shots(gfs_sampler *s, uint64_t shots);
 
 /*
+ * Noise generation: 1 (default, -1 = automatic) draws every noise hit of a chunk in a separate kernel
+ * into a list that the frame kernel then applies; 0 draws noise inside the frame kernel.  Results are
+ * identical either way.  No counterpart in the reference.
+ */
+gfs_status gfs_sampler_set_noise_mode(gfs_sampler *s, int mode);
+/* Noise-kernel time (ms) of the last sample call; gfs_sampler_last_timings' frame time excludes it. */
+gfs_status gfs_sampler_last_noise_ms(const gfs_sampler *s, double *ms);
+/* Hit-list region capacity in records per noise occurrence and slice (0 = automatic: expected hits plus a
+ * wide margin).  A chunk whose hits do not fit is redone with inline noise, with identical results; a
+ * small capacity exercises that. */
+gfs_status gfs_sampler_set_hit_capacity(gfs_sampler *s, uint64_t records);
+/* Kernel launches of the last sample call: frame, transpose, noise; plus hit-list overflows (chunks redone
+ * with inline noise) over the sampler's life. */
+gfs_status gfs_sampler_last_counts(const gfs_sampler *s, uint64_t *counts4);
+
+/*
  * Launch-shape autotuner: times the frame kernel on `trial_shots` shots (0 = 2^18) for each candidate
  * shape (blocks per CTA x threads x ring placement) that fits and keeps the fastest; *best_ms (may be
  * null) receives its time.  The sampler's stream position does not move and results never depend on the
@@ -202,6 +229,34 @@ gfs_status gfs_batch_autotune(gfs_batch *b, const uint64_t *shots, double *best_
 /* out4: frame, transposes, host copies, whole call (ms); counts4: frame launches, transpose launches,
  * graph launches, graph builds (cumulative). */
 gfs_status gfs_batch_last_timings(const gfs_batch *b, double *out4, uint64_t *counts4);
+
+/*
+ * Request server with continuous batching on one device.  A worker thread keeps lowered circuits in a
+ * device-resident cache keyed by circuit text, cuts requests into chunks of at most max_chunk_shots
+ * (0 = 2^18) shots, and admits chunks first come first served into the next batched launch while the
+ * batch's device-memory footprint stays within half of hbm_budget_bytes (0 = 8 GiB; two batches are in
+ * flight at a time).  Request `ticket` returns exactly
+ * Circuit(text).compile_detector_sampler(seed=seed).sample(shots, flags...), whatever it was batched
+ * with.  Destinations are host memory (device_out = 0; copied out of device staging) or device memory
+ * (device_out = 1) and must stay valid until gfs_server_wait reports the request done.
+ * No counterpart in the reference (src/stim/py/compiled_detector_sampler.pybind.cc:216-322 is the
+ * per-request call this replaces).
+ */
+typedef struct gfs_server gfs_server;
+gfs_status gfs_server_create(int device, uint64_t hbm_budget_bytes, uint64_t max_chunk_shots, gfs_server **out);
+/* Drains the queue, then stops the worker. */
+void gfs_server_free(gfs_server *s);
+gfs_status gfs_server_submit(gfs_server *s, const char *text, size_t len, uint64_t shots, uint64_t seed,
+                             uint32_t flags, int device_out, void *dets, uint64_t dets_stride, void *obs,
+                             uint64_t obs_stride, uint64_t *ticket);
+/* Waits up to timeout_s seconds (< 0: forever).  *done = 1 once the request finished; its status is the
+ * request's own (an error message when it failed).  A finished ticket is collected and cannot be waited
+ * on again.  *latency_ms (may be null) = submit to completion. */
+gfs_status gfs_server_wait(gfs_server *s, uint64_t ticket, double timeout_s, int *done, double *latency_ms);
+/* out12: completed, failed, p50 latency ms, p99 latency ms, aggregate Gbit/s (detection + observable bits
+ * of completed requests / first submit to last completion), batches, mean chunks per batch, cache hits,
+ * cache misses, longest queue, bits completed, seconds spanned. */
+gfs_status gfs_server_stats(gfs_server *s, double *out12);
 
 #ifdef __cplusplus
 }

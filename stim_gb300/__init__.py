@@ -23,7 +23,7 @@ import numpy as np
 from . import _native
 from ._native import check, lib
 
-__all__ = ["Circuit", "CompiledDetectorSampler", "CompiledMeasurementSampler", "device_count"]
+__all__ = ["Circuit", "CompiledDetectorSampler", "CompiledMeasurementSampler", "BatchSampler", "Server", "device_count"]
 
 
 def device_count() -> int:
@@ -72,7 +72,22 @@ class Circuit:
         m = _native.MODE_MEASUREMENTS if mode == "measurements" else _native.MODE_DETECTIONS
         check(lib().gfs_program_info(self._h, m, info))
         keys = ["ops", "pool_words", "rows", "ring", "channels", "loop_depth", "smem_bytes_per_block", "detectors"]
-        return dict(zip(keys, [int(v) for v in info]))
+        out = dict(zip(keys, [int(v) for v in info]))
+        occ, hits = ctypes.c_uint64(), ctypes.c_double()
+        check(lib().gfs_program_noise(self._h, m, ctypes.byref(occ), ctypes.byref(hits)))
+        out["noise_occurrences"] = occ.value
+        out["hits_per_block"] = hits.value
+        return out
+
+    def reference_sample(self, *, bit_packed: bool = False) -> np.ndarray:
+        """The noiseless run with random outcomes forced to 0 (the reference's Circuit.reference_sample),
+        computed on the host."""
+        M = self.num_measurements
+        out = np.zeros((M + 7) // 8, dtype=np.uint8)
+        check(lib().gfs_circuit_reference_sample(self._h, _ptr(out) if out.size else None, out.size))
+        if bit_packed:
+            return out
+        return np.unpackbits(out, bitorder="little")[:M].astype(np.bool_)
 
     def compile_detector_sampler(self, *, seed=None, device: int = 0) -> "CompiledDetectorSampler":
         return CompiledDetectorSampler(self, seed=seed, device=device)
@@ -125,12 +140,21 @@ class _SamplerBase:
         check(lib().gfs_sampler_autotune(self._h, int(trial_shots), ctypes.byref(ms)))
         return ms.value
 
+    def set_noise_mode(self, mode: int):
+        """-1 automatic, 0 noise drawn inside the frame kernel, 1 noise drawn into hit lists by a separate
+        kernel.  Results are identical."""
+        check(lib().gfs_sampler_set_noise_mode(self._h, int(mode)))
+
     def last_timings(self):
         t = (ctypes.c_double * 4)()
-        c = (ctypes.c_uint64 * 2)()
-        check(lib().gfs_sampler_last_timings(self._h, t, c))
-        return {"frame_ms": t[0], "transpose_ms": t[1], "copy_ms": t[2], "total_ms": t[3],
-                "frame_launches": int(c[0]), "transpose_launches": int(c[1])}
+        c = (ctypes.c_uint64 * 4)()
+        check(lib().gfs_sampler_last_timings(self._h, t, None))
+        check(lib().gfs_sampler_last_counts(self._h, c))
+        nm = ctypes.c_double()
+        check(lib().gfs_sampler_last_noise_ms(self._h, ctypes.byref(nm)))
+        return {"frame_ms": t[0], "noise_ms": nm.value, "transpose_ms": t[1], "copy_ms": t[2], "total_ms": t[3],
+                "frame_launches": int(c[0]), "transpose_launches": int(c[1]), "noise_launches": int(c[2]),
+                "hit_overflows": int(c[3])}
 
 
 def _out_array(out, shape, packed):
@@ -223,9 +247,7 @@ class CompiledMeasurementSampler(_SamplerBase):
         elif skip_reference_sample:
             self._ref = None
         else:
-            raise NotImplementedError(
-                "computing the reference sample on the host is not available yet; pass reference_sample= "
-                "(e.g. stim.Circuit(text).reference_sample()) or skip_reference_sample=True")
+            self._ref = self._circuit.reference_sample(bit_packed=True)
 
     def sample(self, shots: int, *, bit_packed: bool = False):
         shots = int(shots)
@@ -353,3 +375,116 @@ class BatchSampler:
         return {"frame_ms": t[0], "transpose_ms": t[1], "copy_ms": t[2], "total_ms": t[3],
                 "frame_launches": int(c[0]), "transpose_launches": int(c[1]), "graph_launches": int(c[2]),
                 "graph_builds": int(c[3])}
+
+
+class ServerRequest:
+    """A submitted request; ``result()`` waits and returns what
+    ``Circuit(text).compile_detector_sampler(seed=seed).sample(shots, ...)`` returns."""
+
+    def __init__(self, server, ticket, dets, obs, separate):
+        self._server = server
+        self._ticket = ticket
+        self._dets = dets
+        self._obs = obs
+        self._separate = separate
+        self._done = False
+        self.latency_ms = None
+
+    def done(self, timeout: float = 0.0) -> bool:
+        if not self._done:
+            d = ctypes.c_int()
+            lat = ctypes.c_double()
+            check(lib().gfs_server_wait(self._server._h, self._ticket, float(timeout), ctypes.byref(d),
+                                        ctypes.byref(lat)))
+            if d.value:
+                self._done = True
+                self.latency_ms = lat.value
+        return self._done
+
+    def result(self, timeout: float = -1.0):
+        if not self.done(timeout):
+            raise TimeoutError("request not finished")
+        if self._dets is None:
+            return None
+        if self._separate:
+            return self._dets, self._obs
+        return self._dets
+
+
+class Server:
+    """Continuous-batching request server on one device (see gfs_server_* in include/stim_gb300.h)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 8 << 30, max_chunk_shots: int = 1 << 18):
+        h = ctypes.c_void_p()
+        check(lib().gfs_server_create(int(device), int(hbm_budget), int(max_chunk_shots), ctypes.byref(h)))
+        self._h = h
+        self._texts = {}
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().gfs_server_free(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _text(self, circuit):
+        t = circuit if isinstance(circuit, (str, bytes)) else str(circuit)
+        return t.encode() if isinstance(t, str) else t
+
+    def submit(self, circuit, shots: int, *, seed: int, bit_packed: bool = False, prepend_observables: bool = False,
+               append_observables: bool = False, separate_observables: bool = False, num_detectors: int = None,
+               num_observables: int = None) -> ServerRequest:
+        """Queues a detection-sampling request with host (numpy) results."""
+        if separate_observables and (append_observables or prepend_observables):
+            raise ValueError("Can't specify separate_observables=True with append_observables=True or "
+                             "prepend_observables=True")
+        text = self._text(circuit)
+        if num_detectors is None or num_observables is None:
+            c = circuit if isinstance(circuit, Circuit) else self._texts.get(text)
+            if c is None:
+                c = Circuit(text.decode())
+                self._texts[text] = c
+            num_detectors, num_observables = c.num_detectors, c.num_observables
+        D, O = int(num_detectors), int(num_observables)
+        nd = D + (O if prepend_observables else 0) + (O if append_observables else 0)
+        width = (lambda n: (n + 7) // 8) if bit_packed else (lambda n: n)
+        dtype = np.uint8 if bit_packed else np.bool_
+        shots = int(shots)
+        dets = np.empty((shots, width(nd)), dtype=dtype)
+        obs = np.empty((shots, width(O)), dtype=dtype) if separate_observables else None
+        flags = ((_native.PREPEND_OBSERVABLES if prepend_observables else 0)
+                 | (_native.APPEND_OBSERVABLES if append_observables else 0)
+                 | (_native.BIT_PACKED if bit_packed else 0))
+        t = ctypes.c_uint64()
+        check(lib().gfs_server_submit(
+            self._h, text, len(text), shots, _seed_value(seed), flags, 0,
+            _ptr(dets) if dets.size else None, max(1, dets.strides[0]) if dets.size else max(1, dets.shape[1]),
+            (_ptr(obs) if obs.size else None) if obs is not None else None,
+            (max(1, obs.strides[0]) if obs.size else max(1, obs.shape[1])) if obs is not None else 0,
+            ctypes.byref(t)))
+        return ServerRequest(self, t.value, dets, obs, separate_observables)
+
+    def submit_device(self, circuit, shots: int, *, seed: int, dets_ptr: int, dets_stride: int, obs_ptr: int = 0,
+                      obs_stride: int = 0, bit_packed: bool = True) -> ServerRequest:
+        """Queues a request whose bit-packed (or unpacked) results go to caller-owned device memory."""
+        text = self._text(circuit)
+        t = ctypes.c_uint64()
+        check(lib().gfs_server_submit(self._h, text, len(text), int(shots), _seed_value(seed),
+                                      _native.BIT_PACKED if bit_packed else 0, 1, int(dets_ptr) or None,
+                                      int(dets_stride), int(obs_ptr) or None, int(obs_stride), ctypes.byref(t)))
+        return ServerRequest(self, t.value, None, None, False)
+
+    def stats(self) -> dict:
+        o = (ctypes.c_double * 12)()
+        check(lib().gfs_server_stats(self._h, o))
+        keys = ["completed", "failed", "p50_ms", "p99_ms", "gbits", "batches", "chunks_per_batch", "cache_hits",
+                "cache_misses", "max_queue", "bits", "seconds"]
+        return dict(zip(keys, list(o)))

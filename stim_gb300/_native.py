@@ -39,6 +39,8 @@ def _declare(L):
         "gfs_circuit_parse": [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(_vp)],
         "gfs_circuit_stats": [_vp, ctypes.POINTER(_u64)],
         "gfs_program_info": [_vp, ctypes.c_uint32, ctypes.POINTER(_u64)],
+        "gfs_circuit_reference_sample": [_vp, _vp, _u64],
+        "gfs_program_noise": [_vp, ctypes.c_uint32, ctypes.POINTER(_u64), ctypes.POINTER(ctypes.c_double)],
         "gfs_sampler_create": [_vp, ctypes.c_uint32, _u64, ctypes.c_int, ctypes.POINTER(_vp)],
         "gfs_sample_detections": [_vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64],
         "gfs_sample_detections_device": [_vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64],
@@ -52,6 +54,10 @@ def _declare(L):
         "gfs_sampler_set_ring_placement": [_vp, ctypes.c_int],
         "gfs_measure_smem_peak": [ctypes.c_int, ctypes.POINTER(ctypes.c_double)],
         "gfs_sampler_autotune": [_vp, _u64, ctypes.POINTER(ctypes.c_double)],
+        "gfs_sampler_set_noise_mode": [_vp, ctypes.c_int],
+        "gfs_sampler_set_hit_capacity": [_vp, _u64],
+        "gfs_sampler_last_noise_ms": [_vp, ctypes.POINTER(ctypes.c_double)],
+        "gfs_sampler_last_counts": [_vp, ctypes.POINTER(_u64)],
         "gfs_batch_create": [ctypes.POINTER(_vp), ctypes.c_size_t, ctypes.POINTER(_vp)],
         "gfs_batch_sample_detections_device": [_vp, ctypes.POINTER(_u64), ctypes.c_uint32, ctypes.POINTER(_vp),
                                                ctypes.POINTER(_u64), ctypes.POINTER(_vp), ctypes.POINTER(_u64)],
@@ -62,12 +68,17 @@ def _declare(L):
                                 ctypes.POINTER(ctypes.c_int), ctypes.POINTER(_u64), ctypes.POINTER(ctypes.c_int)],
         "gfs_batch_autotune": [_vp, ctypes.POINTER(_u64), ctypes.POINTER(ctypes.c_double)],
         "gfs_batch_last_timings": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_u64)],
+        "gfs_server_create": [ctypes.c_int, _u64, _u64, ctypes.POINTER(_vp)],
+        "gfs_server_submit": [_vp, ctypes.c_char_p, ctypes.c_size_t, _u64, _u64, ctypes.c_uint32, ctypes.c_int,
+                              _vp, _u64, _vp, _u64, ctypes.POINTER(_u64)],
+        "gfs_server_wait": [_vp, _u64, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)],
+        "gfs_server_stats": [_vp, ctypes.POINTER(ctypes.c_double)],
     }
     for name, args in sigs.items():
         f = getattr(L, name)
         f.restype = ctypes.c_int
         f.argtypes = args
-    for name in ("gfs_circuit_free", "gfs_sampler_free", "gfs_batch_free"):
+    for name in ("gfs_circuit_free", "gfs_sampler_free", "gfs_batch_free", "gfs_server_free"):
         f = getattr(L, name)
         f.restype = None
         f.argtypes = [_vp]

@@ -5,6 +5,7 @@
 #include <mutex>
 
 #include "noalloc.h"
+#include "tableau.h"
 
 namespace gfs_rt {
 thread_local std::string g_err;
@@ -76,7 +77,7 @@ void detections_noalloc(gfs_sampler *s, uint64_t shots, uint32_t flags, uint8_t 
         a.smem_table_words = s->smem_table_words();
         a.smem_ops = s->smem_ops();
         a.ring_global = nullptr;  // this path allocates nothing: the ring stays in shared memory
-        gfs::LaunchShape shape = s->shape;
+        gfs::LaunchShape shape = s->shape_inline;  // no hit lists: they would need allocations
         if (shape.ring_global) {
             shape.ring_global = false;
             shape.smem = s->smem_for(shape.blocks_per_cta, false);
@@ -88,7 +89,7 @@ void detections_noalloc(gfs_sampler *s, uint64_t shots, uint32_t flags, uint8_t 
             }
             shape.grid = per_sm * s->num_sms;
         }
-        shape.grid = (int)std::min<uint64_t>((uint64_t)s->shape.grid, nslices);
+        shape.grid = (int)std::min<uint64_t>((uint64_t)shape.grid, nslices);
         ck(cudaEventRecord(s->ev[1], s->stream), "event");
         ck(gfs::launch_frame_kernel(a, shape, s->stream), "frame kernel launch");
         s->n_frame++;
@@ -207,6 +208,29 @@ gfs_status gfs_program_info(const gfs_circuit *c, uint32_t mode, uint64_t *info8
     });
 }
 
+gfs_status gfs_circuit_reference_sample(const gfs_circuit *c, uint8_t *out, uint64_t nbytes) {
+    return guarded([&] {
+        const std::vector<uint8_t> bits = gfs::reference_sample(c->circuit);
+        if (nbytes < bits.size()) {
+            throw std::invalid_argument("reference sample buffer too small");
+        }
+        std::memset(out, 0, nbytes);
+        std::memcpy(out, bits.data(), bits.size());
+    });
+}
+
+gfs_status gfs_program_noise(const gfs_circuit *c, uint32_t mode, uint64_t *occurrences, double *hits_per_block) {
+    return guarded([&] {
+        if (mode != GFS_MODE_DETECTIONS && mode != GFS_MODE_MEASUREMENTS) {
+            throw std::invalid_argument("unknown sampling mode");
+        }
+        gfs::Program p = gfs::lower(c->circuit, mode == GFS_MODE_MEASUREMENTS ? gfs::SampleMode::MEASUREMENTS
+                                                                           : gfs::SampleMode::DETECTIONS);
+        *occurrences = p.noise_occurrences;
+        *hits_per_block = p.hits_per_block;
+    });
+}
+
 gfs_status gfs_sampler_create(const gfs_circuit *c, uint32_t mode, uint64_t seed, int device, gfs_sampler **out) {
     *out = nullptr;
     return guarded([&] {
@@ -306,6 +330,37 @@ gfs_status gfs_measure_smem_peak(int device, double *bytes_per_s) {
 
 gfs_status gfs_sampler_set_chunk_shots(gfs_sampler *s, uint64_t shots) {
     return guarded([&] { s->chunk_shots = shots; });
+}
+
+gfs_status gfs_sampler_set_noise_mode(gfs_sampler *s, int mode) {
+    return guarded([&] {
+        if (mode < -1 || mode > 1) {
+            throw std::invalid_argument("noise mode must be -1 (automatic), 0 (inline) or 1 (hit lists when possible)");
+        }
+        ck(cudaSetDevice(s->device), "cudaSetDevice");
+        s->hits_pref = mode;
+        s->choose_shape(s->shape.blocks_per_cta, s->shape.threads, 0, s->shape.ring_global ? 1 : 0);
+    });
+}
+
+gfs_status gfs_sampler_last_noise_ms(const gfs_sampler *s, double *ms) {
+    return guarded([&] { *ms = s->t_noise; });
+}
+
+gfs_status gfs_sampler_set_hit_capacity(gfs_sampler *s, uint64_t records) {
+    return guarded([&] {
+        s->hit_capacity_override = records;
+        s->occs_blocks = 0;  // re-plan the regions
+    });
+}
+
+gfs_status gfs_sampler_last_counts(const gfs_sampler *s, uint64_t *counts4) {
+    return guarded([&] {
+        counts4[0] = s->n_frame;
+        counts4[1] = s->n_transpose;
+        counts4[2] = s->n_noise;
+        counts4[3] = s->n_hit_overflows;
+    });
 }
 
 gfs_status gfs_sampler_autotune(gfs_sampler *s, uint64_t trial_shots, double *best_ms) {

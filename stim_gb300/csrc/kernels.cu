@@ -396,6 +396,160 @@ __device__ __forceinline__ void fused_gate(const KernelArgs &p, const DevOp &op,
     }
 }
 
+// ------------------------------------------------------------------------------------------------
+// Precomputed noise.  noise_kernel walks the program once per slice, exactly as the frame kernel does,
+// and draws every noise occurrence's hits (same contract, same streams) into a list of 64-bit records;
+// the frame kernel in hit-list mode then only XORs the recorded bits into its shared-memory frames.
+// This takes the Philox/geometric-skip work, its register pressure and its lane imbalance out of the
+// frame kernel, whose CTAs wait on a barrier after every op.
+//
+// Record: bits 0..23 row (measurement flips: result index within the instruction), 24..47 second row
+// (heralds: result index), 48..51 Pauli bits (X, Z on the first row, X, Z on the second), 52..60 shot
+// within the slice (block * 128 + shot).  Records of one occurrence are contiguous but unordered (XOR
+// and OR commute).
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t hit_record(uint32_t a, uint32_t b, uint32_t bits, uint32_t s9) {
+    return (uint64_t)(a & kRowMask) | ((uint64_t)(b & kRowMask) << 24) | ((uint64_t)(bits & 15u) << 48) |
+           ((uint64_t)s9 << 52);
+}
+
+// Occurrence kinds (how the frame kernel applies a record).
+enum : uint32_t { OCC_PAULI = 0, OCC_FLIP, OCC_HERALD, OCC_CORR };
+
+// Calls f(record) for every hit of one noise occurrence of `op` in this slice's B blocks: which = 0 for a
+// noise op, 1 for the noise fused before a gate (op.d), 2 for the noise fused after it (op.c).
+template <int B, typename F>
+__device__ __forceinline__ void occurrence_hits(const KernelArgs &p, const uint32_t *tables, const DevOp &op,
+                                                uint32_t which, uint64_t inst, uint64_t gb0, uint32_t tid,
+                                                uint32_t nt, F f) {
+    const uint32_t code = op.code & 0xFFu, sub = op.code >> 8;
+    const uint32_t a = op.a;
+    const DevChan *ch;
+    uint32_t kind, purpose = GFS_P_NOISE, n = op.n;
+    bool pair = false;
+    uint64_t oinst = inst;
+    if (which) {
+        const uint32_t w = which == 1 ? op.d : op.c;
+        ch = &p.chans[(w & kFusedChanMask) - 1];
+        kind = (w >> 20) & 0xFu;
+        oinst = inst + (int64_t)(int8_t)(w >> 24);
+        pair = code == OP_2Q;
+    } else {
+        ch = &p.chans[op.b];
+        kind = sub;
+        if (code == OP_NOISE) {
+            pair = sub == KN_DEP2 || sub == KN_PC2;
+        } else if (code == OP_MNOISE) {
+            purpose = GFS_P_MNOISE;
+            kind = KN_FLIP;
+        } else if (code == OP_CORR_MASK) {
+            n = 1;
+        }
+    }
+    if (!ch->active) {
+        return;
+    }
+    const uint32_t *T = tables + ch->table;
+    const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
+    for (uint32_t item = tid; item < nseg * B; item += nt) {
+        const uint32_t g = item / B, blk = item % B;
+        const uint32_t u0 = g * GFS_SEG_UNITS;
+        walk_segment(*ch, T, p.seed, purpose, oinst, g, (uint32_t)(gb0 + blk), min(GFS_SEG_UNITS, n - u0),
+                     [&](uint32_t k, uint32_t shot, gfs_stream *st) {
+                         const uint32_t u = u0 + k, s9 = blk * 128 + shot;
+                         if (!which && code == OP_MNOISE) {
+                             f(hit_record(u, 0, 1, s9));
+                         } else if (!which && code == OP_CORR_MASK) {
+                             f(hit_record(0, 0, 0, s9));
+                         } else if (!which && code == OP_HERALD) {
+                             const uint32_t c = gfs_stream_next(st);
+                             const uint32_t v = sub == 0 ? (c & 3u) : pauli_xz(gfs_choice_weighted(c, ch->cum, 4));
+                             f(hit_record(__ldg(p.pool + a + u), u, v, s9));
+                         } else {
+                             const uint32_t bits = hit_bits(kind, *ch, st);
+                             const uint32_t r1 = __ldg(p.pool + a + (pair ? 2 * u : u));
+                             const uint32_t r2 = pair ? __ldg(p.pool + a + 2 * u + 1) : r1;
+                             f(hit_record(r1, r2, bits, s9));
+                         }
+                     });
+    }
+}
+
+// One warp per (slice, occurrence): the lanes walk the occurrence's segments and write each hit into the
+// occurrence's region of the slice, counting with a shared-memory cursor.  No barriers: occurrences and
+// slices are independent streams.
+template <int B>
+__global__ void __launch_bounds__(256) noise_kernel(const KernelArgs p) {
+    __shared__ uint32_t cursor[8];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint64_t w = (uint64_t)blockIdx.x * 8 + warp;
+    if (w >= (uint64_t)p.nslices * p.n_occ) {
+        return;
+    }
+    const uint32_t slice = (uint32_t)(w / p.n_occ), k = (uint32_t)(w % p.n_occ);
+    const NoiseOcc oc = p.occs[k];
+    const DevOp op = p.ops[oc.pc];
+    const uint64_t gb0 = p.block0 + (uint64_t)slice * B;
+    uint64_t *region = p.hits + (uint64_t)slice * p.slice_cap + oc.off;
+    if (lane == 0) {
+        cursor[warp] = 0;
+    }
+    __syncwarp();
+    occurrence_hits<B>(p, p.tables, op, oc.which, oc.inst, gb0, lane, 32u, [&](uint64_t r) {
+        const uint32_t pos = atomicAdd(&cursor[warp], 1u);
+        if (pos < oc.cap) {
+            region[pos] = r;
+        }
+    });
+    __syncwarp();
+    if (lane == 0) {
+        uint32_t c = cursor[warp];
+        if (c > oc.cap) {
+            atomicOr(p.status, 4u);
+            c = 0;
+        }
+        p.hit_count[w] = c;
+    }
+}
+
+// Applies the records of occurrence `occ` of this slice: Pauli flips into the frames, measurement flips
+// into the ring, heralds into the ring and frames; correlated-error hits are OR-ed into MSK (the caller
+// clears it first and derives the mask afterwards).
+template <int B>
+__device__ __forceinline__ void apply_hits(const KernelArgs &p, uint32_t slice, uint32_t occ, uint32_t kind,
+                                           uint4 *X, uint4 *Z, uint4 *R, uint4 *MSK, uint32_t rec, uint32_t L,
+                                           uint32_t n, uint32_t tid, uint32_t nt) {
+    if (occ >= p.n_occ) {  // the host counted fewer occurrences than the program has
+        if (tid == 0) {
+            atomicOr(p.status, 2u);
+        }
+        return;
+    }
+    const uint32_t count = p.hit_count[(uint64_t)slice * p.n_occ + occ];
+    const uint64_t *h = p.hits + (uint64_t)slice * p.slice_cap + p.occs[occ].off;
+    for (uint32_t i = tid; i < count; i += nt) {
+        const uint64_t r = __ldg(reinterpret_cast<const unsigned long long *>(h + i));
+        const uint32_t ra = (uint32_t)r & kRowMask, rb = (uint32_t)(r >> 24) & kRowMask;
+        const uint32_t bits = (uint32_t)(r >> 48) & 15u, s9 = (uint32_t)(r >> 52) & 511u;
+        const uint32_t blk = s9 >> 7, shot = s9 & 127u;
+        switch (kind) {
+            case OCC_PAULI:
+                apply_bits(X, Z, ra * B + blk, rb * B + blk, shot, bits, true);
+                break;
+            case OCC_FLIP:
+                flip_bit(R, wrap(rec + L - n + ra, L) * B + blk, shot, true);
+                break;
+            case OCC_HERALD:
+                atomic_or_bit(R, wrap(rec + L - n + rb, L) * B + blk, shot);
+                apply_bits(X, Z, ra * B + blk, ra * B + blk, shot, bits, true);
+                break;
+            default:  // OCC_CORR
+                atomic_or_bit(MSK, blk, shot);
+                break;
+        }
+    }
+}
+
 // Shared-memory layout of a CTA holding B blocks of 128 shots: X and Z frames [row][block], the
 // measurement ring [ring row][block] (unless it is in global memory), observable accumulators, the
 // correlated-error flags and mask, then the gap tables and the op stream when they are cached.
@@ -445,7 +599,7 @@ __device__ __forceinline__ FrameState frame_state(const KernelArgs &p, uint4 *sm
 
 // Samples slice `slice` (blocks slice*B .. slice*B+B-1 of this launch) of circuit `p` from the start of
 // the circuit to its end, leaving detection events, observables and measurements in global memory.
-template <int B>
+template <int B, bool HITS>
 __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameState &st, uint32_t slice) {
     const uint32_t nr = p.nrows, L = p.ring, NO = p.nobs;
     uint4 *const X = st.X, *const Z = st.Z, *const R = st.R, *const O = st.O, *const OCC = st.OCC,
@@ -470,7 +624,7 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
     }
     __syncthreads();
 
-    uint32_t rec = 0;
+    uint32_t rec = 0, occ = 0;
     uint64_t det_base = 0, meas_base = 0, inst_base = 0;
     int depth = 0;
     uint32_t loop_pc[kMaxLoopDepth + 1];
@@ -514,7 +668,8 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
             continue;
         }
 
-        if ((code == OP_1Q || code == OP_2Q || code == OP_MEASURE || code == OP_RESET) && (op.c | op.d)) {
+        const bool gate = code == OP_1Q || code == OP_2Q || code == OP_MEASURE || code == OP_RESET;
+        if (!HITS && gate && (op.c | op.d)) {
             fused_gate<B>(p, op, code, sub, inst, gb0, tables, X, Z, R, rec, L, tid, nt);
             if (code == OP_MEASURE) {
                 rec = wrap(rec + n, L);
@@ -522,6 +677,10 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
             __syncthreads();
             pc++;
             continue;
+        }
+        if (HITS && gate && (op.d & kFusedChanMask)) {  // noise before the gate
+            apply_hits<B>(p, slice, occ++, OCC_PAULI, X, Z, R, MSK, rec, L, n, tid, nt);
+            __syncthreads();
         }
 
         switch (code) {
@@ -679,6 +838,11 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
 
             case OP_NOISE:
             case OP_MNOISE: {
+                if (HITS) {
+                    apply_hits<B>(p, slice, occ++, code == OP_MNOISE ? OCC_FLIP : OCC_PAULI, X, Z, R, MSK, rec, L, n,
+                                  tid, nt);
+                    break;
+                }
                 // Standalone noise: one segment per lane; rows may repeat within an instruction, so hits
                 // are applied with shared atomics.
                 const bool meas = code == OP_MNOISE;
@@ -707,6 +871,10 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
             }
 
             case OP_HERALD: {
+                if (HITS) {
+                    apply_hits<B>(p, slice, occ++, OCC_HERALD, X, Z, R, MSK, rec, L, n, tid, nt);
+                    break;
+                }
                 const DevChan &ch = p.chans[op.b];
                 const uint32_t *T = tables + ch.table;
                 const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
@@ -728,6 +896,22 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
             }
 
             case OP_CORR_MASK: {
+                if (HITS) {
+                    for (uint32_t blk = tid; blk < (uint32_t)B; blk += nt) {
+                        MSK[blk] = zero4();
+                    }
+                    __syncthreads();
+                    apply_hits<B>(p, slice, occ++, OCC_CORR, X, Z, R, MSK, rec, L, n, tid, nt);
+                    __syncthreads();
+                    for (uint32_t blk = tid; blk < (uint32_t)B; blk += nt) {
+                        const uint4 hits = MSK[blk];
+                        const uint4 oc = sub == 0 ? zero4() : OCC[blk];
+                        const uint4 mk = make_uint4(hits.x & ~oc.x, hits.y & ~oc.y, hits.z & ~oc.z, hits.w & ~oc.w);
+                        OCC[blk] = make_uint4(oc.x | mk.x, oc.y | mk.y, oc.z | mk.z, oc.w | mk.w);
+                        MSK[blk] = mk;
+                    }
+                    break;
+                }
                 const DevChan &ch = p.chans[op.b];
                 for (uint32_t blk = tid; blk < (uint32_t)B; blk += nt) {
                     uint32_t hw[4] = {0, 0, 0, 0};
@@ -810,6 +994,10 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
                 }
                 break;
         }
+        if (HITS && gate && (op.c & kFusedChanMask)) {  // noise after the gate
+            __syncthreads();
+            apply_hits<B>(p, slice, occ++, OCC_PAULI, X, Z, R, MSK, rec, L, n, tid, nt);
+        }
         __syncthreads();
         pc++;
     }
@@ -821,12 +1009,14 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
     __syncthreads();
 }
 
-template <int B>
-__global__ void __launch_bounds__(256, 3) frame_kernel(const KernelArgs p) {
+// Hit-list mode draws no noise in the frame kernel, which leaves room for a fourth resident CTA per SM
+// (64 registers a thread) when shared memory allows it.
+template <int B, bool HITS>
+__global__ void __launch_bounds__(256, HITS ? 4 : 3) frame_kernel(const KernelArgs p) {
     extern __shared__ uint4 sm[];
     const FrameState st = frame_state<B>(p, sm);
     for (uint32_t slice = blockIdx.x; slice < p.nslices; slice += gridDim.x) {
-        frame_slice<B>(p, st, slice);
+        frame_slice<B, HITS>(p, st, slice);
     }
 }
 
@@ -870,7 +1060,7 @@ __global__ void __launch_bounds__(256, 3) batch_frame_kernel(const BatchArgs b) 
             st = frame_state<B>(cur, sm);
             have = j;
         }
-        frame_slice<B>(cur, st, item - b.slice_prefix[j]);
+        frame_slice<B, false>(cur, st, item - b.slice_prefix[j]);
     }
 }
 
@@ -881,24 +1071,56 @@ size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks
            (size_t)((table_words + 3) & ~3u) * sizeof(uint32_t) + (size_t)smem_ops * sizeof(DevOp);
 }
 
-template <int B>
+template <int B, bool H>
 static cudaError_t launch_b(const KernelArgs &args, const LaunchShape &s, cudaStream_t stream) {
-    cudaError_t e = cudaFuncSetAttribute(frame_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(frame_kernel<B, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
     if (e != cudaSuccess) {
         return e;
     }
-    frame_kernel<B><<<s.grid, s.threads, s.smem, stream>>>(args);
+    frame_kernel<B, H><<<s.grid, s.threads, s.smem, stream>>>(args);
     return cudaGetLastError();
 }
 
 cudaError_t launch_frame_kernel(const KernelArgs &args, const LaunchShape &shape, cudaStream_t stream) {
+    const bool h = args.hits != nullptr;
+    if (h != shape.hits) {
+        return cudaErrorInvalidValue;
+    }
     switch (shape.blocks_per_cta) {
         case 1:
-            return launch_b<1>(args, shape, stream);
+            return h ? launch_b<1, true>(args, shape, stream) : launch_b<1, false>(args, shape, stream);
         case 2:
-            return launch_b<2>(args, shape, stream);
+            return h ? launch_b<2, true>(args, shape, stream) : launch_b<2, false>(args, shape, stream);
         case 4:
-            return launch_b<4>(args, shape, stream);
+            return h ? launch_b<4, true>(args, shape, stream) : launch_b<4, false>(args, shape, stream);
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+template <int B>
+static cudaError_t launch_noise_b(const KernelArgs &args, cudaStream_t stream) {
+    const uint64_t warps = (uint64_t)args.nslices * args.n_occ;
+    const uint64_t blocks = (warps + 7) / 8;
+    if (blocks > 0x7FFFFFFFull) {
+        return cudaErrorInvalidValue;
+    }
+    noise_kernel<B><<<(unsigned)blocks, 256, 0, stream>>>(args);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_noise_kernel(const KernelArgs &args, int blocks_per_cta, cudaStream_t stream) {
+    if (!args.hits || !args.hit_count || !args.occs || args.n_occ == 0) {
+        return cudaErrorInvalidValue;
+    }
+    switch (blocks_per_cta) {
+        case 1:
+            return launch_noise_b<1>(args, stream);
+        case 2:
+            return launch_noise_b<2>(args, stream);
+        case 4:
+            return launch_noise_b<4>(args, stream);
         default:
             return cudaErrorInvalidValue;
     }
@@ -951,23 +1173,25 @@ cudaError_t batch_frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *ou
     }
 }
 
-template <int B>
+template <int B, bool H>
 static cudaError_t occ_b(const LaunchShape &s, int *out) {
-    cudaError_t e = cudaFuncSetAttribute(frame_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(frame_kernel<B, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
     if (e != cudaSuccess) {
         return e;
     }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, frame_kernel<B>, s.threads, s.smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, frame_kernel<B, H>, s.threads, s.smem);
 }
 
 cudaError_t frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out) {
+    const bool h = shape.hits;
     switch (shape.blocks_per_cta) {
         case 1:
-            return occ_b<1>(shape, out);
+            return h ? occ_b<1, true>(shape, out) : occ_b<1, false>(shape, out);
         case 2:
-            return occ_b<2>(shape, out);
+            return h ? occ_b<2, true>(shape, out) : occ_b<2, false>(shape, out);
         case 4:
-            return occ_b<4>(shape, out);
+            return h ? occ_b<4, true>(shape, out) : occ_b<4, false>(shape, out);
         default:
             return cudaErrorInvalidValue;
     }

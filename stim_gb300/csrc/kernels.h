@@ -30,6 +30,14 @@ struct KernelArgs {
     uint32_t smem_ops;          // > 0: copy the op stream (this many ops) into shared memory
     uint4 *ring_global;         // non-null: measurement ring in global memory, [CTA][ring row][block]
     uint64_t ring_cta_stride;   // uint4 entries between consecutive CTAs' regions of ring_global
+    // Precomputed noise (noise_kernel, then frame_kernel in hit-list mode); hits == null: the frame kernel
+    // draws its noise inline.
+    uint64_t *hits;          // hit records (see hit_record() in kernels.cu): slice s's region starts at
+                             // s * slice_cap, occurrence k's records at occs[k].off within it
+    uint32_t *hit_count;     // [slice][occurrence] records written
+    const NoiseOcc *occs;    // the program's noise occurrences in order
+    uint32_t n_occ;
+    uint64_t slice_cap;      // records per slice region
 };
 
 // Several circuits in one launch (batch_frame_kernel): circuit j owns work items
@@ -48,11 +56,17 @@ struct LaunchShape {
     int grid;            // CTAs (persistent: each walks slices grid-stride)
     size_t smem;         // dynamic shared memory bytes
     bool ring_global;    // measurement ring in global memory (per-CTA region) instead of shared memory
+    bool hits = false;   // hit-list mode (noise precomputed by noise_kernel)
 };
 
 size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words,
                         uint32_t smem_ops);
+// Frame kernel; in hit-list mode (args.hits != null) noise_kernel must have run on the same arguments.
 cudaError_t launch_frame_kernel(const KernelArgs &args, const LaunchShape &shape, cudaStream_t stream);
+// Draws every noise hit of every slice into args.hits / args.hit_count: one warp per (slice, occurrence).
+// Sets status bit 4 when an occurrence's records do not fit its region (the chunk must then be redone
+// with inline noise).
+cudaError_t launch_noise_kernel(const KernelArgs &args, int blocks_per_cta, cudaStream_t stream);
 cudaError_t frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out);
 cudaError_t launch_batch_frame_kernel(const BatchArgs &args, const LaunchShape &shape, cudaStream_t stream);
 cudaError_t batch_frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out);

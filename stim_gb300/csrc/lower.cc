@@ -83,6 +83,7 @@ struct Lowerer {
         }
         uint32_t id = (uint32_t)prog.chans.size();
         prog.chans.push_back(ch);
+        prog.chan_p.push_back(p);
         chan_cache[key] = id;
         return id;
     }
@@ -956,6 +957,114 @@ struct Lowerer {
         }
     }
 
+    // Counts noise occurrences and expected hits with loop multiplicities (the noise kernel and the frame
+    // kernel meet the occurrences in exactly this order), and lists them when there are not too many.
+    void count_noise() {
+        auto chan_hits = [&](uint32_t ch, uint64_t units) {
+            double pr = std::min(1.0, std::max(0.0, prog.chan_p[ch]));
+            return (double)units * GFS_BLOCK_SHOTS * pr;
+        };
+        // Occurrences and expected hits of op `op` (in the order pre, op, post).
+        auto op_noise = [&](const DevOp &op, auto emit_occ) {
+            const uint32_t code = op.code & 0xFFu;
+            switch (code) {
+                case OP_1Q:
+                case OP_2Q:
+                case OP_MEASURE:
+                case OP_RESET:
+                    if (op.d & kFusedChanMask) {
+                        emit_occ(1u, chan_hits((op.d & kFusedChanMask) - 1, op.n));
+                    }
+                    if (op.c & kFusedChanMask) {
+                        emit_occ(2u, chan_hits((op.c & kFusedChanMask) - 1, op.n));
+                    }
+                    break;
+                case OP_NOISE:
+                case OP_MNOISE:
+                case OP_HERALD:
+                    emit_occ(0u, chan_hits(op.b, op.n));
+                    break;
+                case OP_CORR_MASK:
+                    emit_occ(0u, chan_hits(op.b, 1));
+                    break;
+                default:
+                    break;
+            }
+        };
+        // Totals with multiplicities.
+        std::vector<double> mult_stack{1.0};
+        double occ = 0, hits = 0;
+        for (const DevOp &op : prog.ops) {
+            const uint32_t code = op.code & 0xFFu;
+            const double m = mult_stack.back();
+            if (code == OP_LOOP_BEGIN) {
+                mult_stack.push_back(m * (double)((uint64_t)op.a | ((uint64_t)op.b << 32)));
+            } else if (code == OP_LOOP_END) {
+                if (mult_stack.size() > 1) {
+                    mult_stack.pop_back();
+                }
+            } else {
+                op_noise(op, [&](uint32_t, double h) {
+                    occ += m;
+                    hits += m * h;
+                });
+            }
+        }
+        prog.noise_occurrences = occ > 1e18 ? (uint64_t)1e18 : (uint64_t)occ;
+        prog.hits_per_block = hits;
+        prog.occs.clear();
+        prog.occ_hits_per_block.clear();
+        if (prog.noise_occurrences == 0 || prog.noise_occurrences > kMaxNoiseOccurrences) {
+            return;
+        }
+        // The list, walking the program the way the kernels do (same instance arithmetic).
+        struct Loop {
+            uint32_t pc;
+            uint64_t left, base, stride;
+        };
+        std::vector<Loop> loops;
+        uint64_t inst_base = 0;
+        for (uint32_t pc = 0; pc < prog.ops.size();) {
+            const DevOp &op = prog.ops[pc];
+            const uint32_t code = op.code & 0xFFu;
+            const uint64_t inst = inst_base + op.inst;
+            if (code == OP_END) {
+                break;
+            }
+            if (code == OP_LOOP_BEGIN) {
+                loops.push_back({pc, (uint64_t)op.a | ((uint64_t)op.b << 32), inst_base,
+                                 (uint64_t)op.c | ((uint64_t)op.d << 32)});
+                inst_base = inst;
+                pc++;
+                continue;
+            }
+            if (code == OP_LOOP_END) {
+                Loop &l = loops.back();
+                if (--l.left > 0) {
+                    inst_base += l.stride;
+                    pc = l.pc + 1;
+                } else {
+                    inst_base = l.base;
+                    loops.pop_back();
+                    pc++;
+                }
+                continue;
+            }
+            op_noise(op, [&](uint32_t which, double h) {
+                NoiseOcc o{};
+                o.pc = pc;
+                o.which = which;
+                o.inst = inst;
+                prog.occs.push_back(o);
+                prog.occ_hits_per_block.push_back(h);
+            });
+            pc++;
+        }
+        if (prog.occs.size() != prog.noise_occurrences) {
+            throw std::logic_error("noise occurrence count mismatch");
+        }
+    }
+
     void run() {
         prog.stats = root.stats();
         std::vector<uint8_t> used(prog.stats.num_qubits + 1, 0);
@@ -974,6 +1083,7 @@ struct Lowerer {
         lower_block(root, 0);
         flush_detectors();
         emit(OP_END, 0, 0, 0);
+        count_noise();
         prog.num_detectors = prog.stats.num_detectors;
         prog.num_observables = prog.stats.num_observables;
         prog.num_measurements = prog.stats.num_measurements;
@@ -989,6 +1099,28 @@ struct Lowerer {
 };
 
 }  // namespace
+
+uint64_t plan_hit_regions(std::vector<NoiseOcc> &occs, const std::vector<double> &hits_per_block, uint32_t blocks,
+                          uint64_t cap_override) {
+    uint64_t off = 0;
+    for (size_t k = 0; k < occs.size(); k++) {
+        const double mean = hits_per_block[k] * blocks;
+        double cap = std::ceil(mean + 8.0 * std::sqrt(mean) + 32.0);
+        cap = std::min(cap, (double)blocks * GFS_BLOCK_SHOTS * (double)(1u << 24));  // at most every trial
+        uint64_t c = (uint64_t)cap;
+        if (cap_override) {
+            c = std::min<uint64_t>(c, cap_override);
+        }
+        c = (c + 1) & ~(uint64_t)1;
+        if (off + c > 0xFFFFFFFFull) {
+            throw std::invalid_argument("hit-list region too large");
+        }
+        occs[k].off = (uint32_t)off;
+        occs[k].cap = (uint32_t)c;
+        off += c;
+    }
+    return off;
+}
 
 Program lower(const Circuit &circuit, SampleMode mode) {
     Lowerer l(circuit, mode);

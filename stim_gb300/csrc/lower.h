@@ -24,11 +24,30 @@ struct Program {
     uint64_t num_measurements = 0;
     uint32_t max_loop_depth = 0;
     double work = 0;  // estimated cost of one 128-shot block (orders circuits in a batched launch)
+    std::vector<double> chan_p;  // hit probability of each channel
+
+    // Noise occurrences (a noise instruction instance, or the noise fused before/after a gate) met by one
+    // pass over the program, loops unrolled, and the expected number of hits per 128-shot block.
+    uint64_t noise_occurrences = 0;
+    double hits_per_block = 0;
+    // The occurrences in order with their expected hits per 128-shot block (empty when there are more
+    // than kMaxNoiseOccurrences).
+    std::vector<NoiseOcc> occs;
+    std::vector<double> occ_hits_per_block;
     CircuitStats stats;
 };
 
 // Throws std::invalid_argument (bad circuit) or std::out_of_range (lookback before the beginning of
 // time), mirroring the reference's errors for the same circuits.
 Program lower(const Circuit &circuit, SampleMode mode);
+
+constexpr uint64_t kMaxNoiseOccurrences = 1u << 16;
+
+// Fills each occurrence's region (off, cap) for slices of `blocks` 128-shot blocks: the expected hits
+// plus a margin of eight standard deviations and 32 records (an overflow is detected by the noise kernel
+// and the chunk redone inline).  cap_override > 0 caps every region (used to exercise that path).
+// Returns the records per slice region.
+uint64_t plan_hit_regions(std::vector<NoiseOcc> &occs, const std::vector<double> &hits_per_block, uint32_t blocks,
+                          uint64_t cap_override);
 
 }  // namespace gfs

@@ -78,6 +78,19 @@ struct alignas(16) DevChan {
     uint64_t cum[16];
 };
 
+// One noise occurrence of the program (a noise op, or the noise fused before / after a gate op) met by a
+// pass over the program with loops unrolled: the op, the instance it runs as, and where its hit records
+// go inside a slice's region of the hit list.
+struct alignas(16) NoiseOcc {
+    uint32_t pc;     // op index
+    uint32_t which;  // 0 noise op, 1 noise fused before the gate (op.d), 2 after it (op.c)
+    uint64_t inst;   // instance of the op (loop iteration applied)
+    uint32_t off;    // first record within the slice region (even, so regions start on 16 bytes)
+    uint32_t cap;    // records reserved
+    uint32_t pad[2];
+};
+static_assert(sizeof(NoiseOcc) == 32, "NoiseOcc layout");
+
 constexpr uint32_t kFeedbackX = 1, kFeedbackZ = 2;
 constexpr uint32_t kTermRecord = 1u << 31, kTermX = 1u << 30, kTermZ = 1u << 29;
 constexpr uint32_t kRowMask = (1u << 24) - 1;

@@ -121,12 +121,24 @@ struct gfs_sampler {
     cudaStream_t copy_stream = nullptr;  // device->host copies of host-destination chunks
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t pev[2][4] = {};  // per pipeline slot: chunk start, frame done, transpose done, copy done
+    cudaEvent_t ev_noise[3][2] = {};  // around a noise kernel launch: device path, pipeline slots 0 and 1
+    int cur_slot = -1;                // pipeline slot of the chunk being enqueued (-1: device path)
+    bool noise_pending[3] = {false, false, false};
+    double t_noise = 0;
     gfs::LaunchShape shape{};
     int num_sms = 0;
     int ring_pref = -1;  // -1 automatic, 0 shared memory, 1 global memory
+    int hits_pref = -1;  // noise drawn by noise_kernel into hit lists: -1 automatic, 0 never, 1 when possible
+    bool force_inline = false;  // set while a chunk is redone after its hit list overflowed
+    gfs::LaunchShape shape_inline{};  // the same shape for the inline-noise frame kernel
+    DevBuf hit_buf, hit_count, d_occs;
+    int occs_blocks = 0;          // blocks per slice the uploaded occurrence regions were planned for
+    uint64_t slice_cap = 0;       // records per slice region
+    uint64_t n_hit_overflows = 0;
+    uint64_t hit_capacity_override = 0;  // records per occurrence region (0 = from the expected hits)
     uint64_t chunk_shots = 0;
     double t_frame = 0, t_transpose = 0, t_copy = 0, t_total = 0;
-    uint64_t n_frame = 0, n_transpose = 0;
+    uint64_t n_frame = 0, n_transpose = 0, n_noise = 0;
 
     ~gfs_sampler() {
         if (stream) {
@@ -143,6 +155,13 @@ struct gfs_sampler {
             }
             for (auto &slot : pev) {
                 for (auto &e : slot) {
+                    if (e) {
+                        cudaEventDestroy(e);
+                    }
+                }
+            }
+            for (auto &pair : ev_noise) {
+                for (auto &e : pair) {
                     if (e) {
                         cudaEventDestroy(e);
                     }
@@ -167,6 +186,12 @@ struct gfs_sampler {
                                      bpc, smem_table_words(), smem_ops());
     }
 
+    // Hit-list mode needs at least one noise occurrence and a bounded number of them per pass (the index
+    // holds one entry per slice and occurrence).
+    bool hits_possible() const {
+        return hits_pref != 0 && !prog.occs.empty();
+    }
+
     // ring: 0 = shared memory, 1 = global memory, -1 = whichever keeps more 128-shot blocks resident per SM.
     void choose_shape(int bpc, int threads, int grid, int ring = -1) {
         cudaDeviceProp prop;
@@ -175,6 +200,7 @@ struct gfs_sampler {
         if (ring < 0) {
             auto resident = [&](bool g) {
                 gfs::LaunchShape t{bpc, threads, 1, smem_for(bpc, g), g};
+                t.hits = hits_possible();
                 if (t.smem > (size_t)prop.sharedMemPerBlockOptin) {
                     return 0;
                 }
@@ -199,13 +225,18 @@ struct gfs_sampler {
             throw std::invalid_argument("threads per CTA must be a multiple of 32 in [32, 256]");
         }
         gfs::LaunchShape s{bpc, threads, 1, smem, ring_global};
-        int per_sm = 0;
+        gfs::LaunchShape si = s;
+        s.hits = hits_possible();
+        int per_sm = 0, per_sm_inline = 0;
         ck(gfs::frame_kernel_max_ctas_per_sm(s, &per_sm), "occupancy");
-        if (per_sm < 1) {
+        ck(gfs::frame_kernel_max_ctas_per_sm(si, &per_sm_inline), "occupancy");
+        if (per_sm < 1 || per_sm_inline < 1) {
             throw std::invalid_argument("frame kernel cannot be resident with this launch shape");
         }
         s.grid = grid > 0 ? grid : per_sm * num_sms;
+        si.grid = grid > 0 ? grid : per_sm_inline * num_sms;
         shape = s;
+        shape_inline = si;
     }
 
     void init(const gfs_circuit *c, uint32_t m, uint64_t sd, int dev) {
@@ -230,6 +261,11 @@ struct gfs_sampler {
                 ck(cudaEventCreate(&e), "cudaEventCreate");
             }
         }
+        for (auto &pair : ev_noise) {
+            for (auto &e : pair) {
+                ck(cudaEventCreate(&e), "cudaEventCreate");
+            }
+        }
         upload(d_ops, prog.ops, device, stream);
         upload(d_pool, prog.pool, device, stream);
         upload(d_tables, prog.tables, device, stream);
@@ -244,7 +280,12 @@ struct gfs_sampler {
 
     uint64_t per_block_bytes(uint64_t out_row_bytes) const {
         uint64_t rows = prog.num_detectors + prog.num_observables + (mode == GFS_MODE_MEASUREMENTS ? prog.num_measurements : 0);
-        return rows * 16 + 128 * out_row_bytes;
+        uint64_t b = rows * 16 + 128 * out_row_bytes;
+        if (shape.hits) {
+            // Region capacity runs above the expected hits; estimate it generously.
+            b += (uint64_t)(prog.hits_per_block * 8 * 2.5) + 64 * 8 * prog.noise_occurrences + prog.noise_occurrences * 4;
+        }
+        return b;
     }
 
     uint64_t chunk_blocks(uint64_t out_row_bytes) const {
@@ -267,8 +308,25 @@ struct gfs_sampler {
     }
 
     void reset_timings() {
-        t_frame = t_transpose = t_copy = t_total = 0;
-        n_frame = n_transpose = 0;
+        t_frame = t_transpose = t_copy = t_total = t_noise = 0;
+        n_frame = n_transpose = n_noise = 0;
+        noise_pending[0] = noise_pending[1] = noise_pending[2] = false;
+    }
+
+    // Adds the noise kernel time of the chunk last enqueued in `slot` (-1: device path) once the stream has
+    // passed it, and returns it.
+    double account_noise(int slot) {
+        const int i = slot + 1;
+        float ms = 0;
+        if (noise_pending[i]) {
+            if (cudaEventElapsedTime(&ms, ev_noise[i][0], ev_noise[i][1]) != cudaSuccess) {
+                cudaGetLastError();
+                ms = 0;
+            }
+            noise_pending[i] = false;
+            t_noise += ms;
+        }
+        return ms;
     }
 
     float elapsed(int a, int b) {
@@ -278,8 +336,11 @@ struct gfs_sampler {
     }
 
     // Runs the frame kernel for nblk blocks starting at stream block `block0`; results land in the tmp buffers.
+    // Runs the frame kernel for nblk blocks starting at stream block `block0`; results land in the tmp buffers.
+    // In hit-list mode noise_kernel runs first and draws the chunk's noise into hit_buf.
     void run_frame(uint64_t nblk, uint64_t block0) {
-        uint64_t bpc = (uint64_t)shape.blocks_per_cta;
+        const gfs::LaunchShape &sh = (shape.hits && !force_inline) ? shape : shape_inline;
+        uint64_t bpc = (uint64_t)sh.blocks_per_cta;
         uint64_t nslices = (nblk + bpc - 1) / bpc;
         uint64_t alloc_blocks = nslices * bpc;
         det_tmp.ensure(std::max<uint64_t>(16, alloc_blocks * prog.num_detectors * 16), device);
@@ -308,13 +369,36 @@ struct gfs_sampler {
         a.smem_table_words = smem_table_words();
         a.smem_ops = smem_ops();
         a.ring_global = nullptr;
-        if (shape.ring_global) {
-            ring_buf.ensure((uint64_t)shape.grid * (uint64_t)shape.blocks_per_cta * prog.ring * sizeof(uint4), device);
+        if (sh.ring_global) {
+            ring_buf.ensure((uint64_t)sh.grid * (uint64_t)sh.blocks_per_cta * prog.ring * sizeof(uint4), device);
             a.ring_global = (uint4 *)ring_buf.p;
-            a.ring_cta_stride = (uint64_t)shape.blocks_per_cta * prog.ring;
+            a.ring_cta_stride = (uint64_t)sh.blocks_per_cta * prog.ring;
         }
-        gfs::LaunchShape s = shape;
-        s.grid = (int)std::min<uint64_t>((uint64_t)shape.grid, nslices);
+        if (sh.hits) {
+            // Regions per slice and occurrence: the expected hits plus a wide margin (an overflow is detected
+            // and the chunk redone with inline noise, so the margin only affects speed).
+            if (occs_blocks != sh.blocks_per_cta || !d_occs.p) {
+                std::vector<gfs::NoiseOcc> occs = prog.occs;
+                slice_cap = gfs::plan_hit_regions(occs, prog.occ_hits_per_block, (uint32_t)sh.blocks_per_cta,
+                                                  hit_capacity_override);
+                upload(d_occs, occs, device, stream);
+                occs_blocks = sh.blocks_per_cta;
+            }
+            hit_buf.ensure(std::max<uint64_t>(16, nslices * slice_cap * 8), device);
+            hit_count.ensure(std::max<uint64_t>(16, nslices * prog.occs.size() * 4), device);
+            a.hits = (uint64_t *)hit_buf.p;
+            a.hit_count = (uint32_t *)hit_count.p;
+            a.occs = (const gfs::NoiseOcc *)d_occs.p;
+            a.n_occ = (uint32_t)prog.occs.size();
+            a.slice_cap = slice_cap;
+            ck(cudaEventRecord(ev_noise[cur_slot + 1][0], stream), "event");
+            ck(gfs::launch_noise_kernel(a, sh.blocks_per_cta, stream), "noise kernel launch");
+            ck(cudaEventRecord(ev_noise[cur_slot + 1][1], stream), "event");
+            noise_pending[cur_slot + 1] = true;
+            n_noise++;
+        }
+        gfs::LaunchShape s = sh;
+        s.grid = (int)std::min<uint64_t>((uint64_t)sh.grid, nslices);
         ck(gfs::launch_frame_kernel(a, s, stream), "frame kernel launch");
         n_frame++;
     }
@@ -337,13 +421,22 @@ struct gfs_sampler {
         n_transpose++;
     }
 
-    void check_status() {
+    // Reads and clears the kernels' status word (after the stream has drained).  Bits 1 and 2 are errors;
+    // bit 4 (a hit list overflowed) is returned as true: the caller redoes the affected shots inline.
+    bool check_status() {
         uint32_t st = 0;
         ck(cudaMemcpy(&st, d_status.p, 4, cudaMemcpyDeviceToHost), "status read");
         if (st) {
-            cudaMemset(d_status.p, 0, 4);
+            ck(cudaMemset(d_status.p, 0, 4), "status clear");
+        }
+        if (st & 3u) {
             throw std::runtime_error("frame kernel reported error status " + std::to_string(st));
         }
+        if (st & 4u) {
+            n_hit_overflows++;
+            return true;
+        }
+        return false;
     }
 
     // Times the frame kernel on `trial_shots` shots for each candidate launch shape and keeps the fastest.
@@ -354,10 +447,10 @@ struct gfs_sampler {
         };
         const Cand cands[] = {{1, 256, 0}, {1, 256, 1}, {1, 128, 0}, {1, 128, 1}, {2, 256, 0},
                               {2, 256, 1}, {2, 128, 0}, {2, 128, 1}, {4, 256, 0}, {4, 256, 1}};
-        const gfs::LaunchShape before = shape;
+        const gfs::LaunchShape before = shape, before_inline = shape_inline;
         const uint64_t nblk = std::max<uint64_t>(1, (trial_shots + 127) / 128);
         double best = -1;
-        gfs::LaunchShape best_shape = shape;
+        gfs::LaunchShape best_shape = shape, best_inline = shape_inline;
         for (const Cand &c : cands) {
             try {
                 choose_shape(c.bpc, c.threads, 0, c.ring);
@@ -370,15 +463,18 @@ struct gfs_sampler {
                 run_frame(nblk, next_block);
                 ck(cudaEventRecord(ev[2], stream), "event");
                 ck(cudaStreamSynchronize(stream), "autotune");
-                total = (float)elapsed(1, 2);
+                total = (float)elapsed(1, 2);  // noise kernel + frame kernel
+                account_noise(-1);
             }
             check_status();
             if (best < 0 || total < best) {
                 best = total;
                 best_shape = shape;
+                best_inline = shape_inline;
             }
         }
         shape = best < 0 ? before : best_shape;
+        shape_inline = best < 0 ? before_inline : best_inline;
         return best;
     }
 
@@ -401,6 +497,7 @@ struct gfs_sampler {
     // memory may hold the calling thread until it completes.
     template <typename Produce, typename Copy>
     void host_pipeline(uint64_t shots, uint64_t slot_row_bytes, Produce produce, Copy copy) {
+        const uint64_t first_block = next_block;
         uint64_t nblk_total = (shots + 127) / 128;
         uint64_t cb = host_chunk_blocks(nblk_total, slot_row_bytes);
         uint64_t slot_bytes = cb * 128 * slot_row_bytes;
@@ -416,7 +513,7 @@ struct gfs_sampler {
             ck(cudaEventSynchronize(pev[slot][3]), "chunk copy");
             float ms = 0;
             ck(cudaEventElapsedTime(&ms, pev[slot][0], pev[slot][1]), "cudaEventElapsedTime");
-            t_frame += ms;
+            t_frame += ms - account_noise(slot);
             ck(cudaEventElapsedTime(&ms, pev[slot][1], pev[slot][2]), "cudaEventElapsedTime");
             t_transpose += ms;
             used[slot] = false;
@@ -437,7 +534,14 @@ struct gfs_sampler {
             uint64_t cs = std::min<uint64_t>(shots - done, cb * 128);
             uint64_t nblk = (cs + 127) / 128;
             ck(cudaEventRecord(pev[slot][0], stream), "event");
-            run_frame(nblk, next_block);
+            cur_slot = slot;
+            try {
+                run_frame(nblk, next_block);
+            } catch (...) {
+                cur_slot = -1;
+                throw;
+            }
+            cur_slot = -1;
             ck(cudaEventRecord(pev[slot][1], stream), "event");
             produce(done, cs, slots[slot]);
             ck(cudaEventRecord(pev[slot][2], stream), "event");
@@ -463,8 +567,19 @@ struct gfs_sampler {
         ck(cudaStreamSynchronize(stream), "sample");
         ck(cudaEventSynchronize(ev[1]), "sample");
         t_total = elapsed(0, 1);
-        t_copy = std::max(0.0, t_total - t_frame - t_transpose);
-        check_status();
+        t_copy = std::max(0.0, t_total - t_frame - t_noise - t_transpose);
+        if (check_status()) {
+            // A hit list overflowed somewhere: redo the whole request with inline noise (same results).
+            next_block = first_block;
+            force_inline = true;
+            try {
+                host_pipeline(shots, slot_row_bytes, produce, copy);
+            } catch (...) {
+                force_inline = false;
+                throw;
+            }
+            force_inline = false;
+        }
     }
 
     // Enqueues the transposes of one chunk's detection events (and observables) into dd / od.
@@ -540,16 +655,31 @@ struct gfs_sampler {
                                  obs ? obs + done * ostride : nullptr, ostride, dets != nullptr, obs != nullptr);
             ck(cudaEventRecord(ev[3], stream), "event");
             ck(cudaStreamSynchronize(stream), "sample");
-            t_frame += elapsed(1, 2);
+            t_frame += elapsed(1, 2) - account_noise(-1);
             t_transpose += elapsed(2, 3);
-            check_status();
+            if (check_status()) {
+                // The chunk's hit list overflowed: redo it with inline noise (same results).
+                force_inline = true;
+                try {
+                    run_frame(nblk, next_block);
+                    transpose_detections(flags, cs, dets ? dets + done * dstride : nullptr, dstride,
+                                         obs ? obs + done * ostride : nullptr, ostride, dets != nullptr,
+                                         obs != nullptr);
+                    ck(cudaStreamSynchronize(stream), "sample");
+                } catch (...) {
+                    force_inline = false;
+                    throw;
+                }
+                force_inline = false;
+                check_status();
+            }
             next_block += nblk;
             done += cs;
         }
         ck(cudaEventRecord(ev[1], stream), "event");
         ck(cudaStreamSynchronize(stream), "sample");
         t_total = elapsed(0, 1);
-        t_copy = std::max(0.0, t_total - t_frame - t_transpose);
+        t_copy = std::max(0.0, t_total - t_frame - t_noise - t_transpose);
     }
 
     void measurements(uint64_t shots, uint32_t flags, const uint8_t *ref, uint8_t *out, uint64_t stride) {

@@ -125,3 +125,36 @@ def batched_workload(num_circuits: int = 256, seed: int = 2024, d_choices=tuple(
         out.append({"text": code_circuit("surface_code:rotated_memory_z", d, d, p), "distance": d, "p": p,
                     "shots": shots, "seed": rng.randrange(1 << 62)})
     return out
+
+
+SERVING_FAMILIES = (
+    ("repetition_code:memory", tuple(range(3, 53, 2))),
+    ("surface_code:rotated_memory_x", tuple(range(3, 23, 2))),
+    ("surface_code:rotated_memory_z", tuple(range(3, 23, 2))),
+    ("color_code:memory_xyz", tuple(range(3, 17, 2))),
+)
+
+
+def serving_workload(rate: float = 2000.0, seconds: float = 60.0, seed: int = 7, p_lo: float = 1e-4,
+                     p_hi: float = 1e-2, p_per_decade: int = 16, shots_lo: int = 1 << 10, shots_hi: int = 1 << 22):
+    """The request-serving workload: Poisson arrivals at `rate` requests per second for `seconds`; each
+    request picks a family uniformly, then d uniformly from the family's range (rounds = d), p log-uniform
+    in [p_lo, p_hi] rounded to one of `p_per_decade` log-spaced values per decade (so that repeated
+    circuits can hit the device-side circuit cache), shots log-uniform in [shots_lo, shots_hi], and its
+    own seed.  Returns a list of dicts with keys t (arrival, seconds), family, distance, p, shots, seed."""
+    rng = random.Random(seed)
+    out = []
+    t = 0.0
+    lo, hi = math.log10(p_lo), math.log10(p_hi)
+    steps = max(1, int(round((hi - lo) * p_per_decade)))
+    while True:
+        t += rng.expovariate(rate)
+        if t >= seconds:
+            break
+        fam, ds = SERVING_FAMILIES[rng.randrange(len(SERVING_FAMILIES))]
+        d = ds[rng.randrange(len(ds))]
+        k = rng.randint(0, steps)
+        p = float(f"{10 ** (lo + (hi - lo) * k / steps):.4g}")
+        shots = int(round(math.exp(rng.uniform(math.log(shots_lo), math.log(shots_hi)))))
+        out.append({"t": t, "family": fam, "distance": d, "p": p, "shots": shots, "seed": rng.randrange(1 << 62)})
+    return out

@@ -16,7 +16,8 @@ GOLDEN_DIR = os.path.join(ROOT, "tests", "golden")
 
 
 def golden_names():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz"))
+    """Sampling fixtures (refsample_random.npz holds reference samples only)."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz") and not f.startswith("refsample_"))
 
 
 @pytest.fixture(scope="session")

@@ -9,6 +9,8 @@ Run in a container where the reference tree exists (it is never copied into this
 It writes
   * tests/golden/circuits/*.stim  circuits made by the reference's generator (`stim gen`) with all four
                                   noise knobs at 0.001 (stim_gb300.workloads substitutes other p);
+  * tests/golden/refsample_random.npz  reference samples (the reference's TableauSimulator) of 300 random
+                                  small circuits mixing every sign-sensitive gate family;
   * tests/golden/<case>.npz       for each case: the circuit text, seed, shot count, and the
                                   detection events, observable flips and measurement flips that the
                                   reference's FrameSimulator produced when fed the injected random
@@ -108,13 +110,90 @@ def cases():
     ]
 
 
+def random_small_circuit(rng, n=4, depth=25):
+    """A random small circuit over the gate families whose signs matter for the reference sample: Pauli
+    and Clifford gates, measurements and resets in three bases with inverted targets, MPP / SPP / SPP_DAG
+    products, pair measurements, classically controlled Paulis, MPAD, heralded erasure, noisy gates."""
+    g1 = ["H", "S", "S_DAG", "SQRT_X", "SQRT_Y_DAG", "C_XYZ", "H_YZ", "X", "Y", "Z"]
+    g2 = ["CX", "CZ", "CY", "ISWAP", "SQRT_ZZ_DAG", "XCY", "YCZ", "SWAP", "CXSWAP"]
+    lines = []
+    nmeas = 0
+
+    def term(q):
+        return f"{'!' if rng.random() < 0.3 else ''}{rng.choice('XYZ')}{q}"
+
+    for _ in range(depth):
+        k = rng.randrange(12)
+        qs = list(range(n))
+        rng.shuffle(qs)
+        if k == 0:
+            lines.append(f"{rng.choice(g1)} {qs[0]} {qs[1]}")
+        elif k == 1:
+            lines.append(f"{rng.choice(g2)} {qs[0]} {qs[1]}")
+        elif k == 2:
+            lines.append(f"{rng.choice(['M', 'MX', 'MY', 'MR', 'MRX', 'MRY'])} {'!' if rng.random() < 0.3 else ''}{qs[0]}")
+            nmeas += 1
+        elif k == 3:
+            lines.append(f"{rng.choice(['R', 'RX', 'RY'])} {qs[0]}")
+        elif k == 4:
+            lines.append("MPP " + "*".join(term(q) for q in qs[:rng.randint(1, 3)]))
+            nmeas += 1
+        elif k == 5:
+            lines.append(f"{rng.choice(['SPP', 'SPP_DAG'])} " + "*".join(term(q) for q in qs[:rng.randint(1, 3)]))
+        elif k == 6:
+            lines.append(f"{rng.choice(['MXX', 'MYY', 'MZZ'])} {'!' if rng.random() < 0.3 else ''}{qs[0]} {qs[1]}")
+            nmeas += 1
+        elif k == 7 and nmeas:
+            g = rng.choice(["CX", "CZ", "CY"])
+            lines.append(f"{g} rec[-{rng.randint(1, nmeas)}] {qs[0]}")
+        elif k == 8 and nmeas:
+            lines.append(f"{rng.choice(['XCZ', 'YCZ'])} {qs[0]} rec[-{rng.randint(1, nmeas)}]")
+        elif k == 9:
+            lines.append(f"MPAD {rng.randint(0, 1)}")
+            nmeas += 1
+        elif k == 10:
+            lines.append(f"HERALDED_ERASE(0.1) {qs[0]}")
+            nmeas += 1
+        elif k == 11:
+            lines.append(f"X_ERROR(0.2) {qs[0]}\nM(0.1) {qs[1]}")
+            nmeas += 1
+    return "\n".join(lines) + "\n"
+
+
+def refsample_fixtures(count=300, seed=3):
+    """Reference samples (the reference's TableauSimulator) of random small circuits."""
+    import random
+
+    rng = random.Random(seed)
+    texts, samples = [], []
+    while len(texts) < count:
+        text = random_small_circuit(rng)
+        try:
+            out = run_ref(text, 1, 128)
+        except subprocess.CalledProcessError:
+            continue  # a combination the reference rejects
+        texts.append(text)
+        samples.append(out["ref_sample"])
+    width = max(len(s) for s in samples)
+    packed = np.zeros((len(samples), width), dtype=np.uint8)
+    lengths = np.array([len(s) for s in samples], dtype=np.int64)
+    for k, s in enumerate(samples):
+        packed[k, :len(s)] = s
+    np.savez_compressed(os.path.join(HERE, "refsample_random.npz"), circuits=np.array(texts), samples=packed,
+                        lengths=lengths, seed=np.uint64(seed))
+
+
 def main():
+    if "--refsample-only" in sys.argv:
+        refsample_fixtures()
+        return
     gen_templates()
     for name, text, seed, shots in cases():
         out = run_ref(text, seed, shots)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), circuit=np.array(text), seed=np.uint64(seed),
                             shots=np.uint64(shots), **out)
         print(name, out["num_detectors"], out["num_measurements"], shots)
+    refsample_fixtures()
 
 
 if __name__ == "__main__":

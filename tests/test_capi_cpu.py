@@ -103,3 +103,35 @@ def test_lowering_keeps_repeat_as_loops():
     assert info["rows"] == 1249
     assert info["ops"] < 200  # the 24-round body is emitted once, not unrolled
     assert 3 * info["smem_bytes_per_block"] <= 227 * 1024  # three CTAs per SM
+
+
+def test_noise_occurrence_accounting():
+    # Occurrences with loops unrolled: the d=3 memory experiment has its noise in a 2-round REPEAT body.
+    from stim_gb300 import _native
+
+    c = stim_gb300.Circuit(workloads.code_circuit("surface_code:rotated_memory_z", 5, 5, 0.001))
+    info = c.program_info()
+    assert info["noise_occurrences"] > 0
+    # Expected hits per 128-shot block ~ p x (noisy units) x 128 shots.
+    assert 0 < info["hits_per_block"] < 10000
+    c0 = stim_gb300.Circuit(workloads.code_circuit("surface_code:rotated_memory_z", 5, 5, 0.0))
+    assert c0.program_info()["noise_occurrences"] == 0
+    assert _native.lib() is not None
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_reference_sample_matches_reference_tableau(name):
+    # The reference's own TableauSimulator::reference_sample_circuit output, stored with each fixture.
+    g = dict(np.load(os.path.join(GOLDEN_DIR, name + ".npz")))
+    c = stim_gb300.Circuit(str(g["circuit"]))
+    np.testing.assert_array_equal(c.reference_sample(bit_packed=True), g["ref_sample"])
+    bits = c.reference_sample()
+    assert bits.dtype == np.bool_ and bits.shape == (c.num_measurements,)
+    np.testing.assert_array_equal(np.packbits(bits, bitorder="little"), g["ref_sample"])
+
+
+def test_reference_sample_random_small_circuits():
+    d = np.load(os.path.join(GOLDEN_DIR, "refsample_random.npz"))
+    for text, row, n in zip(d["circuits"], d["samples"], d["lengths"]):
+        got = stim_gb300.Circuit(str(text)).reference_sample(bit_packed=True)
+        np.testing.assert_array_equal(got, row[:n], err_msg=str(text))

@@ -43,6 +43,10 @@ def test_measurements_match_reference_golden(name):
     s2 = c.compile_sampler(reference_sample=g["ref_sample"], seed=int(g["seed"]))
     m2 = s2.sample(int(g["shots"]), bit_packed=True)
     np.testing.assert_array_equal(m2, g["meas"] ^ g["ref_sample"][None, :])
+    # Default: the host computes the reference sample itself.
+    s3 = c.compile_sampler(seed=int(g["seed"]))
+    m3 = s3.sample(int(g["shots"]), bit_packed=True)
+    np.testing.assert_array_equal(m3, g["meas"] ^ g["ref_sample"][None, :])
 
 
 def _unpack(a, n):
@@ -161,3 +165,44 @@ def test_lookback_errors_match_reference():
         stim_gb300.Circuit("M 0\nDETECTOR rec[-2]").compile_detector_sampler()
     with pytest.raises(ValueError):
         stim_gb300.Circuit("M 0\nCX 0 rec[-1]").compile_detector_sampler()
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_inline_noise_mode_matches_golden(name):
+    # The default draws noise into hit lists with a separate kernel; mode 0 draws it inside the frame
+    # kernel.  Both must reproduce the reference's goldens.
+    g = load(name)
+    c = stim_gb300.Circuit(str(g["circuit"]))
+    s = c.compile_detector_sampler(seed=int(g["seed"]))
+    s.set_noise_mode(0)
+    d, o = s.sample(int(g["shots"]), separate_observables=True, bit_packed=True)
+    np.testing.assert_array_equal(d, g["dets"])
+    np.testing.assert_array_equal(o, g["obs"])
+    assert s.last_timings()["noise_launches"] == 0
+
+
+@pytest.mark.parametrize("device_out", [False, True])
+def test_hit_list_overflow_falls_back_to_inline_noise(device_out):
+    from stim_gb300 import _native
+
+    text = workloads.code_circuit("surface_code:rotated_memory_x", 5, 5, 0.02)
+    c = stim_gb300.Circuit(text)
+    want = c.compile_detector_sampler(seed=9)
+    want.set_noise_mode(0)
+    d0, o0 = want.sample(5000, bit_packed=True, separate_observables=True)
+    s = c.compile_detector_sampler(seed=9)
+    _native.check(_native.lib().gfs_sampler_set_hit_capacity(s._h, 100))  # far below the expected hits
+    if device_out:
+        torch = pytest.importorskip("torch")
+        d = torch.zeros((5000, d0.shape[1]), dtype=torch.uint8, device="cuda")
+        o = torch.zeros((5000, 1), dtype=torch.uint8, device="cuda")
+        _native.check(_native.lib().gfs_sample_detections_device(s._h, 5000, _native.BIT_PACKED, d.data_ptr(),
+                                                                 d.shape[1], o.data_ptr(), 1))
+        d, o = d.cpu().numpy(), o.cpu().numpy()
+    else:
+        d, o = s.sample(5000, bit_packed=True, separate_observables=True)
+    np.testing.assert_array_equal(d, d0)
+    np.testing.assert_array_equal(o, o0)
+    assert s.last_timings()["hit_overflows"] >= 1
+    # The stream continues exactly where it would have.
+    np.testing.assert_array_equal(s.sample(300, bit_packed=True), want.sample(300, bit_packed=True))
