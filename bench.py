@@ -228,6 +228,7 @@ def run_gpu(args):
     D, O = circ.num_detectors, circ.num_observables
     shots = args.shots
     sampler = circ.compile_detector_sampler(seed=args.seed + rank, device=local)
+    sampler.set_noise_mode(args.noise_mode)
     if args.shape:
         b, t = [int(x) for x in args.shape.split(",")]
         sampler.set_launch_shape(b, t)
@@ -528,6 +529,7 @@ def main():
     ap.add_argument("--ref-shots", type=int, default=1 << 20)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--shape", default="")
+    ap.add_argument("--noise-mode", type=int, default=-1, help="-1 automatic, 0 inline, 1 hit lists")
     ap.add_argument("--batched", type=int, default=1)
     ap.add_argument("--batch-circuits", type=int, default=256)
     ap.add_argument("--serve-seconds", type=float, default=2.0)

@@ -515,18 +515,59 @@ __global__ void __launch_bounds__(256) noise_kernel(const KernelArgs p) {
 // Applies the records of occurrence `occ` of this slice: Pauli flips into the frames, measurement flips
 // into the ring, heralds into the ring and frames; correlated-error hits are OR-ed into MSK (the caller
 // clears it first and derives the mask afterwards).
+// Shared-memory layout of a CTA holding B blocks of 128 shots: X and Z frames [row][block], the
+// measurement ring [ring row][block] (unless it is in global memory), observable accumulators, the
+// correlated-error flags and mask, then the gap tables, the op stream, and the occurrence cache when they
+// are cached.
+struct FrameState {
+    uint4 *X, *Z, *R, *O, *OCC, *MSK;
+    const uint32_t *tables;
+    const DevOp *ops;
+    uint32_t *occ_off, *occ_cnt;  // hit-list mode with cached occurrences: region offsets, slice's counts
+};
+
+// First record of occurrence `occ` in this slice, and its count.
+__device__ __forceinline__ const uint64_t *occ_records(const KernelArgs &p, const uint32_t *occ_off,
+                                                        const uint32_t *occ_cnt, uint32_t slice, uint32_t occ,
+                                                        uint32_t *count) {
+    *count = occ_cnt ? occ_cnt[occ] : p.hit_count[(uint64_t)slice * p.n_occ + occ];
+    return p.hits + (uint64_t)slice * p.slice_cap + (occ_off ? occ_off[occ] : p.occs[occ].off);
+}
+
+// Starts pulling occurrence `occ`'s records into L2 (one bulk prefetch; regions start on 16 bytes and
+// hold an even number of records, so rounding the size up stays inside the region).
+__device__ __forceinline__ void prefetch_occurrence(const KernelArgs &p, const uint32_t *occ_off,
+                                                    const uint32_t *occ_cnt, uint32_t slice, uint32_t occ) {
+    if (occ >= p.n_occ || !occ_cnt) {
+        return;
+    }
+    uint32_t count;
+    const uint64_t *h = occ_records(p, occ_off, occ_cnt, slice, occ, &count);
+    const uint32_t bytes = ((count + 1) & ~1u) * 8u;
+    if (bytes) {
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(h), "r"(bytes) : "memory");
+    }
+}
+
+// Applies the records of occurrence `occ` of this slice: Pauli flips into the frames, measurement flips
+// into the ring, heralds into the ring and frames; correlated-error hits are OR-ed into MSK (the caller
+// clears it first and derives the mask afterwards).  Thread 0 then prefetches the records two
+// occurrences ahead.
 template <int B>
-__device__ __forceinline__ void apply_hits(const KernelArgs &p, uint32_t slice, uint32_t occ, uint32_t kind,
-                                           uint4 *X, uint4 *Z, uint4 *R, uint4 *MSK, uint32_t rec, uint32_t L,
-                                           uint32_t n, uint32_t tid, uint32_t nt) {
+__device__ __forceinline__ void apply_hits(const KernelArgs &p, const FrameState &st, uint32_t slice, uint32_t occ,
+                                           uint32_t kind, uint4 *X, uint4 *Z, uint4 *R, uint4 *MSK, uint32_t rec,
+                                           uint32_t L, uint32_t n, uint32_t tid, uint32_t nt) {
     if (occ >= p.n_occ) {  // the host counted fewer occurrences than the program has
         if (tid == 0) {
             atomicOr(p.status, 2u);
         }
         return;
     }
-    const uint32_t count = p.hit_count[(uint64_t)slice * p.n_occ + occ];
-    const uint64_t *h = p.hits + (uint64_t)slice * p.slice_cap + p.occs[occ].off;
+    if (tid == 0) {
+        prefetch_occurrence(p, st.occ_off, st.occ_cnt, slice, occ + 2);
+    }
+    uint32_t count;
+    const uint64_t *h = occ_records(p, st.occ_off, st.occ_cnt, slice, occ, &count);
     for (uint32_t i = tid; i < count; i += nt) {
         const uint64_t r = __ldg(reinterpret_cast<const unsigned long long *>(h + i));
         const uint32_t ra = (uint32_t)r & kRowMask, rb = (uint32_t)(r >> 24) & kRowMask;
@@ -549,15 +590,6 @@ __device__ __forceinline__ void apply_hits(const KernelArgs &p, uint32_t slice, 
         }
     }
 }
-
-// Shared-memory layout of a CTA holding B blocks of 128 shots: X and Z frames [row][block], the
-// measurement ring [ring row][block] (unless it is in global memory), observable accumulators, the
-// correlated-error flags and mask, then the gap tables and the op stream when they are cached.
-struct FrameState {
-    uint4 *X, *Z, *R, *O, *OCC, *MSK;
-    const uint32_t *tables;
-    const DevOp *ops;
-};
 
 // Lays out shared memory for circuit `p` and copies its gap tables and op stream in; the copies are
 // visible after the next __syncthreads() (the first one in frame_slice).
@@ -594,6 +626,16 @@ __device__ __forceinline__ FrameState frame_state(const KernelArgs &p, uint4 *sm
         }
         st.ops = so;
     }
+    st.occ_off = st.occ_cnt = nullptr;
+    if (p.smem_occ) {
+        uint32_t *oo = reinterpret_cast<uint32_t *>(st_tables + ((p.smem_table_words + 3) & ~3u)) +
+                       (size_t)p.smem_ops * (sizeof(DevOp) / sizeof(uint32_t));
+        for (uint32_t i = tid; i < p.smem_occ; i += nt) {
+            oo[i] = __ldg(&p.occs[i].off);
+        }
+        st.occ_off = oo;
+        st.occ_cnt = oo + p.smem_occ;
+    }
     return st;
 }
 
@@ -622,7 +664,17 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
     for (uint32_t i = tid; i < B; i += nt) {
         OCC[i] = zero4();
     }
+    if (HITS && st.occ_cnt) {
+        const uint32_t *cnt = p.hit_count + (uint64_t)slice * p.n_occ;
+        for (uint32_t i = tid; i < p.smem_occ; i += nt) {
+            st.occ_cnt[i] = __ldg(cnt + i);
+        }
+    }
     __syncthreads();
+    if (HITS && tid == 0) {
+        prefetch_occurrence(p, st.occ_off, st.occ_cnt, slice, 0);
+        prefetch_occurrence(p, st.occ_off, st.occ_cnt, slice, 1);
+    }
 
     uint32_t rec = 0, occ = 0;
     uint64_t det_base = 0, meas_base = 0, inst_base = 0;
@@ -679,7 +731,7 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
             continue;
         }
         if (HITS && gate && (op.d & kFusedChanMask)) {  // noise before the gate
-            apply_hits<B>(p, slice, occ++, OCC_PAULI, X, Z, R, MSK, rec, L, n, tid, nt);
+            apply_hits<B>(p, st, slice, occ++, OCC_PAULI, X, Z, R, MSK, rec, L, n, tid, nt);
             __syncthreads();
         }
 
@@ -839,7 +891,7 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
             case OP_NOISE:
             case OP_MNOISE: {
                 if (HITS) {
-                    apply_hits<B>(p, slice, occ++, code == OP_MNOISE ? OCC_FLIP : OCC_PAULI, X, Z, R, MSK, rec, L, n,
+                    apply_hits<B>(p, st, slice, occ++, code == OP_MNOISE ? OCC_FLIP : OCC_PAULI, X, Z, R, MSK, rec, L, n,
                                   tid, nt);
                     break;
                 }
@@ -872,7 +924,7 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
 
             case OP_HERALD: {
                 if (HITS) {
-                    apply_hits<B>(p, slice, occ++, OCC_HERALD, X, Z, R, MSK, rec, L, n, tid, nt);
+                    apply_hits<B>(p, st, slice, occ++, OCC_HERALD, X, Z, R, MSK, rec, L, n, tid, nt);
                     break;
                 }
                 const DevChan &ch = p.chans[op.b];
@@ -901,7 +953,7 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
                         MSK[blk] = zero4();
                     }
                     __syncthreads();
-                    apply_hits<B>(p, slice, occ++, OCC_CORR, X, Z, R, MSK, rec, L, n, tid, nt);
+                    apply_hits<B>(p, st, slice, occ++, OCC_CORR, X, Z, R, MSK, rec, L, n, tid, nt);
                     __syncthreads();
                     for (uint32_t blk = tid; blk < (uint32_t)B; blk += nt) {
                         const uint4 hits = MSK[blk];
@@ -996,7 +1048,7 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
         }
         if (HITS && gate && (op.c & kFusedChanMask)) {  // noise after the gate
             __syncthreads();
-            apply_hits<B>(p, slice, occ++, OCC_PAULI, X, Z, R, MSK, rec, L, n, tid, nt);
+            apply_hits<B>(p, st, slice, occ++, OCC_PAULI, X, Z, R, MSK, rec, L, n, tid, nt);
         }
         __syncthreads();
         pc++;
@@ -1065,10 +1117,11 @@ __global__ void __launch_bounds__(256, 3) batch_frame_kernel(const BatchArgs b) 
 }
 
 size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words,
-                        uint32_t smem_ops) {
+                        uint32_t smem_ops, uint32_t smem_occ) {
     // `ring` = measurement-ring rows held in shared memory (0 when the ring is in global memory).
     return ((size_t)2 * nrows + ring + nobs + 2) * (size_t)blocks_per_cta * sizeof(uint4) +
-           (size_t)((table_words + 3) & ~3u) * sizeof(uint32_t) + (size_t)smem_ops * sizeof(DevOp);
+           (size_t)((table_words + 3) & ~3u) * sizeof(uint32_t) + (size_t)smem_ops * sizeof(DevOp) +
+           (size_t)2 * smem_occ * sizeof(uint32_t);
 }
 
 template <int B, bool H>

@@ -38,6 +38,8 @@ struct KernelArgs {
     const NoiseOcc *occs;    // the program's noise occurrences in order
     uint32_t n_occ;
     uint64_t slice_cap;      // records per slice region
+    uint32_t smem_occ;       // n_occ when the occurrence offsets and the slice's counts are cached in shared
+                             // memory, else 0
 };
 
 // Several circuits in one launch (batch_frame_kernel): circuit j owns work items
@@ -60,7 +62,7 @@ struct LaunchShape {
 };
 
 size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words,
-                        uint32_t smem_ops);
+                        uint32_t smem_ops, uint32_t smem_occ = 0);
 // Frame kernel; in hit-list mode (args.hits != null) noise_kernel must have run on the same arguments.
 cudaError_t launch_frame_kernel(const KernelArgs &args, const LaunchShape &shape, cudaStream_t stream);
 // Draws every noise hit of every slice into args.hits / args.hit_count: one warp per (slice, occurrence).

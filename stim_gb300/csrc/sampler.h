@@ -181,15 +181,19 @@ struct gfs_sampler {
         return prog.ops.size() <= 256 ? (uint32_t)prog.ops.size() : 0;
     }
 
-    size_t smem_for(int bpc, bool ring_global) const {
-        return gfs::frame_smem_bytes(prog.num_rows, ring_global ? 0 : prog.ring, (uint32_t)prog.num_observables,
-                                     bpc, smem_table_words(), smem_ops());
-    }
-
-    // Hit-list mode needs at least one noise occurrence and a bounded number of them per pass (the index
-    // holds one entry per slice and occurrence).
+    // Hit-list mode needs the program's noise occurrences listed (at least one, not too many).
     bool hits_possible() const {
         return hits_pref != 0 && !prog.occs.empty();
+    }
+
+    // Occurrence offsets and per-slice counts cached in shared memory in hit-list mode (small lists only).
+    uint32_t smem_occ(bool hits) const {
+        return (hits && prog.occs.size() <= 1024) ? (uint32_t)prog.occs.size() : 0;
+    }
+
+    size_t smem_for(int bpc, bool ring_global, bool hits = false) const {
+        return gfs::frame_smem_bytes(prog.num_rows, ring_global ? 0 : prog.ring, (uint32_t)prog.num_observables,
+                                     bpc, smem_table_words(), smem_ops(), smem_occ(hits));
     }
 
     // ring: 0 = shared memory, 1 = global memory, -1 = whichever keeps more 128-shot blocks resident per SM.
@@ -199,7 +203,7 @@ struct gfs_sampler {
         num_sms = prop.multiProcessorCount;
         if (ring < 0) {
             auto resident = [&](bool g) {
-                gfs::LaunchShape t{bpc, threads, 1, smem_for(bpc, g), g};
+                gfs::LaunchShape t{bpc, threads, 1, smem_for(bpc, g, hits_possible()), g};
                 t.hits = hits_possible();
                 if (t.smem > (size_t)prop.sharedMemPerBlockOptin) {
                     return 0;
@@ -227,6 +231,11 @@ struct gfs_sampler {
         gfs::LaunchShape s{bpc, threads, 1, smem, ring_global};
         gfs::LaunchShape si = s;
         s.hits = hits_possible();
+        s.smem = smem_for(bpc, ring_global, s.hits);
+        if (s.smem > (size_t)prop.sharedMemPerBlockOptin) {
+            s.hits = false;  // no room for the occurrence cache: draw noise inline
+            s.smem = smem;
+        }
         int per_sm = 0, per_sm_inline = 0;
         ck(gfs::frame_kernel_max_ctas_per_sm(s, &per_sm), "occupancy");
         ck(gfs::frame_kernel_max_ctas_per_sm(si, &per_sm_inline), "occupancy");
@@ -391,6 +400,7 @@ struct gfs_sampler {
             a.occs = (const gfs::NoiseOcc *)d_occs.p;
             a.n_occ = (uint32_t)prog.occs.size();
             a.slice_cap = slice_cap;
+            a.smem_occ = smem_occ(true);
             ck(cudaEventRecord(ev_noise[cur_slot + 1][0], stream), "event");
             ck(gfs::launch_noise_kernel(a, sh.blocks_per_cta, stream), "noise kernel launch");
             ck(cudaEventRecord(ev_noise[cur_slot + 1][1], stream), "event");

@@ -191,7 +191,7 @@ def test_hit_list_overflow_falls_back_to_inline_noise(device_out):
     want.set_noise_mode(0)
     d0, o0 = want.sample(5000, bit_packed=True, separate_observables=True)
     s = c.compile_detector_sampler(seed=9)
-    _native.check(_native.lib().gfs_sampler_set_hit_capacity(s._h, 100))  # far below the expected hits
+    _native.check(_native.lib().gfs_sampler_set_hit_capacity(s._h, 4))  # far below the expected hits
     if device_out:
         torch = pytest.importorskip("torch")
         d = torch.zeros((5000, d0.shape[1]), dtype=torch.uint8, device="cuda")
