@@ -232,6 +232,8 @@ def run_gpu(args):
     if args.shape:
         b, t = [int(x) for x in args.shape.split(",")]
         sampler.set_launch_shape(b, t)
+    elif args.autotune:
+        sampler.autotune(1 << 18)  # launch shape by measurement (results never depend on it)
     drow, orow = (D + 7) // 8, (O + 7) // 8
     dets = torch.empty((shots, drow), dtype=torch.uint8, device=f"cuda:{local}")
     obs = torch.empty((shots, orow), dtype=torch.uint8, device=f"cuda:{local}")
@@ -530,6 +532,7 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--shape", default="")
     ap.add_argument("--noise-mode", type=int, default=-1, help="-1 automatic, 0 inline, 1 hit lists")
+    ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--batched", type=int, default=1)
     ap.add_argument("--batch-circuits", type=int, default=256)
     ap.add_argument("--serve-seconds", type=float, default=2.0)

@@ -19,7 +19,7 @@ struct gfs_batch {
     cudaGraphExec_t exec = nullptr;
     std::vector<uint64_t> graph_key;
     double t_frame = 0, t_transpose = 0, t_copy = 0, t_total = 0;
-    uint64_t n_frame = 0, n_transpose = 0, n_graph_launches = 0, n_graph_builds = 0;
+    uint64_t n_frame = 0, n_transpose = 0, n_graph_launches = 0, n_graph_builds = 0, n_hit_overflows = 0;
 
     ~gfs_batch() {
         drop_graph();
@@ -174,7 +174,24 @@ struct gfs_batch {
             cudaGetLastError();
             t_frame = t_total;
         }
-        eng.check_status();
+        if (eng.check_status()) {
+            // A hit list overflowed: redo the batch with inline noise (identical results), outside the graph.
+            n_hit_overflows++;
+            eng.force_inline = true;
+            try {
+                eng.prepare(es, order);
+                eng.enqueue_frame();
+                eng.enqueue_transposes(es, flags);
+                ck(cudaStreamSynchronize(eng.stream), "batch sample");
+                eng.check_status();
+            } catch (...) {
+                eng.force_inline = false;
+                drop_graph();
+                throw;
+            }
+            eng.force_inline = false;
+            drop_graph();  // its descriptors were overwritten
+        }
         for (const auto &e : es) {
             gfs_sampler *s = const_cast<gfs_sampler *>(e.prog);
             s->next_block = std::max(s->next_block, e.block0 + (e.shots + 127) / 128);

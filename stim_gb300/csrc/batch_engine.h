@@ -4,6 +4,8 @@
 // batch_frame_kernel launch, and turned shot-major by one transpose per entry and output.
 #pragma once
 
+#include <unordered_map>
+
 #include "sampler.h"
 
 namespace gfs_rt {
@@ -34,8 +36,19 @@ struct BatchEngine {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // start, frame done, end
     DevBuf d_desc, d_prefix, d_counter, d_status, det_arena, obs_arena, ring_buf;
+    DevBuf hit_arena, count_arena, d_wprefix;
     gfs::LaunchShape shape{};
     uint64_t ring_stride_cur = 0;
+    bool force_inline = false;  // set while a batch is redone after a hit list overflowed
+    // Occurrence tables planned for this engine's blocks per CTA, per program.
+    struct OccPlan {
+        std::unique_ptr<DevBuf> occs;
+        uint64_t slice_cap = 0;
+        int blocks = 0;
+    };
+    std::unordered_map<const gfs_sampler *, OccPlan> occ_plans;
+    std::vector<uint64_t> wprefix;
+    uint64_t noise_warps = 0;
 
     // Current plan (set by prepare()).
     std::vector<gfs::KernelArgs> desc;
@@ -79,15 +92,28 @@ struct BatchEngine {
 
     // Shape for a set of programs: dynamic shared memory and ring stride of the largest; grid = one wave.
     // Returns false when it does not fit.
+    // Hit-list mode for a batch: every program either lists its noise occurrences or has none, and no
+    // sampler asked for inline noise.
+    static bool hits_for(const std::vector<const gfs_sampler *> &progs) {
+        for (auto *p : progs) {
+            if (p->hits_pref == 0 || (p->prog.occs.empty() && p->prog.noise_occurrences > 0)) {
+                return false;
+            }
+        }
+        return true;
+    }
+
     bool fit(const std::vector<const gfs_sampler *> &progs, int bpc, int threads, bool ring_global,
              gfs::LaunchShape *out, uint64_t *ring_stride) const {
+        const bool hits = hits_for(progs);
         size_t smem = 0;
         uint64_t rs = 0;
         for (auto *p : progs) {
-            smem = std::max(smem, p->smem_for(bpc, ring_global));
+            smem = std::max(smem, p->smem_for(bpc, ring_global, hits));
             rs = std::max<uint64_t>(rs, (uint64_t)bpc * p->prog.ring);
         }
         gfs::LaunchShape t{bpc, threads, 1, smem, ring_global};
+        t.hits = hits;
         if (t.smem > smem_optin) {
             return false;
         }
@@ -122,7 +148,7 @@ struct BatchEngine {
     }
 
     // Default shape without timing: four blocks per CTA when at least two such CTAs fit per SM (small
-    // and medium circuits), else one block per CTA; ring placement by residency.
+    // and medium circuits), else one block per CTA of 128 threads; ring placement by residency.
     void default_shape(const std::vector<const gfs_sampler *> &progs) {
         gfs::LaunchShape t{};
         uint64_t rs = 0;
@@ -132,7 +158,7 @@ struct BatchEngine {
                 return;
             }
         }
-        set_shape(progs, 1, 256, -1);
+        set_shape(progs, 1, 128, -1);
     }
 
     // Plans the entries (launch order = `order`, or input order when empty), allocates the arenas and
@@ -144,7 +170,10 @@ struct BatchEngine {
         prefix.assign(1, 0);
         det_off.assign(n, 0);
         obs_off.assign(n, 0);
-        uint64_t det_total = 0, obs_total = 0, total = 0;
+        uint64_t det_total = 0, obs_total = 0, total = 0, hit_total = 0, count_total = 0;
+        const bool hits = shape.hits && !force_inline;
+        std::vector<uint64_t> hit_off(n, 0), count_off(n, 0);
+        wprefix.assign(1, 0);
         for (size_t k = 0; k < n; k++) {
             const size_t j = order.empty() ? k : order[k];
             const BatchEntry &e = entries[j];
@@ -175,6 +204,18 @@ struct BatchEngine {
             a.smem_table_words = s->smem_table_words();
             a.smem_ops = s->smem_ops();
             a.ring_cta_stride = ring_stride_cur;
+            if (hits) {
+                const OccPlan &pl = occ_plan(s);
+                a.n_occ = (uint32_t)s->prog.occs.size();
+                a.slice_cap = pl.slice_cap;
+                a.occs = a.n_occ ? (const gfs::NoiseOcc *)pl.occs->p : nullptr;
+                a.smem_occ = s->smem_occ(true);
+                hit_off[j] = hit_total;
+                count_off[j] = count_total;
+                hit_total += nslices * pl.slice_cap;
+                count_total += nslices * a.n_occ;
+                wprefix.push_back(wprefix.back() + nslices * a.n_occ);
+            }
             desc.push_back(a);
             total += nslices;
             if (total > 0xFFFFFFFFull) {
@@ -184,6 +225,16 @@ struct BatchEngine {
         }
         det_arena.ensure(std::max<uint64_t>(16, det_total * 16), device);
         obs_arena.ensure(std::max<uint64_t>(16, obs_total * 16), device);
+        noise_warps = 0;
+        if (hits) {
+            hit_arena.ensure(std::max<uint64_t>(16, hit_total * 8), device);
+            count_arena.ensure(std::max<uint64_t>(16, count_total * 4), device);
+            noise_warps = wprefix.back();
+            d_wprefix.ensure(wprefix.size() * sizeof(uint64_t), device);
+            ck(cudaMemcpyAsync(d_wprefix.p, wprefix.data(), wprefix.size() * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                               stream),
+               "descriptor upload");
+        }
         if (shape.ring_global) {
             ring_buf.ensure(std::max<uint64_t>(16, (uint64_t)shape.grid * ring_stride_cur * 16), device);
         }
@@ -197,6 +248,10 @@ struct BatchEngine {
             a.det_out = (uint4 *)det_arena.p + det_off[j];
             a.obs_out = (uint4 *)obs_arena.p + obs_off[j];
             a.ring_global = shape.ring_global ? (uint4 *)ring_buf.p : nullptr;
+            if (hits) {
+                a.hits = (uint64_t *)hit_arena.p + hit_off[j];
+                a.hit_count = (uint32_t *)count_arena.p + count_off[j];
+            }
         }
         if (!desc.empty()) {
             d_desc.ensure(desc.size() * sizeof(gfs::KernelArgs), device);
@@ -220,9 +275,42 @@ struct BatchEngine {
         b.ncircuits = (uint32_t)desc.size();
         b.total_slices = items;
         b.counter = (uint32_t *)d_counter.p;
+        b.warp_prefix = (const uint64_t *)d_wprefix.p;
+        b.total_noise_warps = noise_warps;
         gfs::LaunchShape s = shape;
-        s.grid = (int)std::min<uint64_t>((uint64_t)shape.grid, items);
+        s.hits = shape.hits && !force_inline;
+        if (shape.hits && force_inline) {
+            s = inline_shape();
+        }
+        s.grid = (int)std::min<uint64_t>((uint64_t)s.grid, items);
         ck(gfs::launch_batch_frame_kernel(b, s, stream), "batch frame kernel launch");
+    }
+
+    // The current shape for the inline-noise batch kernel (same blocks, threads and ring placement).
+    gfs::LaunchShape inline_shape() const {
+        gfs::LaunchShape t = shape;
+        t.hits = false;
+        int per = 0;
+        if (gfs::batch_frame_kernel_max_ctas_per_sm(t, &per) != cudaSuccess || per < 1) {
+            cudaGetLastError();
+            per = 1;
+        }
+        t.grid = per * num_sms;
+        return t;
+    }
+
+    // Occurrence regions of program s planned for this engine's blocks per CTA (uploaded once).
+    const OccPlan &occ_plan(const gfs_sampler *s) {
+        OccPlan &pl = occ_plans[s];
+        if (!pl.occs || pl.blocks != shape.blocks_per_cta) {
+            std::vector<gfs::NoiseOcc> occs = s->prog.occs;
+            pl.slice_cap = gfs::plan_hit_regions(occs, s->prog.occ_hits_per_block, (uint32_t)shape.blocks_per_cta,
+                                                 s->hit_capacity_override);
+            pl.occs = std::make_unique<DevBuf>();
+            upload(*pl.occs, occs, device, stream);
+            pl.blocks = shape.blocks_per_cta;
+        }
+        return pl;
     }
 
     // One transpose per entry and output.  Returns the number of transpose calls enqueued.
@@ -271,14 +359,18 @@ struct BatchEngine {
         return calls;
     }
 
-    // Reads and clears the kernels' error word (call after the stream has drained).
-    void check_status() {
+    // Reads and clears the kernels' status word (after the stream has drained).  Bits 1 and 2 are errors;
+    // bit 4 (a hit list overflowed) is returned as true: the caller redoes the batch with inline noise.
+    bool check_status() {
         uint32_t st = 0;
         ck(cudaMemcpy(&st, d_status.p, 4, cudaMemcpyDeviceToHost), "status read");
         if (st) {
-            cudaMemset(d_status.p, 0, 4);
+            ck(cudaMemset(d_status.p, 0, 4), "status clear");
+        }
+        if (st & 3u) {
             throw std::runtime_error("batch frame kernel reported error status " + std::to_string(st));
         }
+        return (st & 4u) != 0;
     }
 };
 

@@ -163,16 +163,12 @@ GFS_HD uint32_t gfs_gap_fixup(uint32_t u, const uint32_t *table, int32_t est, in
  * further hits.  `always` marks p >= 1 (every trial hits, no draws); `inv_c` = 1 / -log2(1-p) only
  * seeds the lookup, so host and device may compute it with different log2 approximations.
  */
-GFS_HD int32_t gfs_next_hit(gfs_stream *s, const uint32_t *table, float inv_c, int32_t pos, int32_t trials,
-                            int always) {
-    if (always) {
-        return pos + 1 < trials ? pos + 1 : -1;
-    }
-    int32_t room = trials - pos - 1; /* a gap >= room leaves the segment */
-    if (room <= 0) {
-        return -1;
-    }
-    uint32_t u = gfs_stream_next(s);
+/*
+ * The hit that draw `u` selects after position `pos` with `room` = trials - pos - 1 > 0 trials left, or -1
+ * when u leaves the segment.  (Split out of gfs_next_hit so that a caller holding an already drawn value can
+ * continue a walk exactly.)
+ */
+GFS_HD int32_t gfs_hit_after_draw(uint32_t u, const uint32_t *table, float inv_c, int32_t pos, int32_t room) {
     if (u < table[room]) {
         return -1;
     }
@@ -190,6 +186,23 @@ GFS_HD int32_t gfs_next_hit(gfs_stream *s, const uint32_t *table, float inv_c, i
     }
     uint32_t g = gfs_gap_fixup(u, table, (int32_t)e, room - 1);
     return pos + 1 + (int32_t)g;
+}
+
+/*
+ * Next hit of a segment after position `pos` (start with pos = -1), or -1 when the segment has no
+ * further hits.  `always` marks p >= 1 (every trial hits, no draws); `inv_c` = 1 / -log2(1-p) only
+ * seeds the lookup, so host and device may compute it with different log2 approximations.
+ */
+GFS_HD int32_t gfs_next_hit(gfs_stream *s, const uint32_t *table, float inv_c, int32_t pos, int32_t trials,
+                            int always) {
+    if (always) {
+        return pos + 1 < trials ? pos + 1 : -1;
+    }
+    int32_t room = trials - pos - 1; /* a gap >= room leaves the segment */
+    if (room <= 0) {
+        return -1;
+    }
+    return gfs_hit_after_draw(gfs_stream_next(s), table, inv_c, pos, room);
 }
 
 /* Choice helpers. */

@@ -1,15 +1,20 @@
 // Frame-sampling kernels for sm_103a.
 //
-// frame_kernel: one CTA owns a slice of B x 128 shots at a time (persistent, grid-stride over slices).
-// Its X/Z Pauli frames ([row][block] uint4, 128 shots per uint4), the measurement ring, the observable
-// accumulators and the correlated-error flags live in shared memory for the whole circuit.  The CTA
-// walks the device program (program.h): every op spreads its independent units over the threads,
-// updates 128 shots per unit with 128-bit shared-memory loads/stores and bitwise logic, and ends with
-// one __syncthreads().  Noise is sampled from the counter-based stream of gfs_contract.h: a thread owns
-// a segment of 4 units x 128 shots and skips geometrically to its hits.  Noise next to a gate on the
-// same targets is fused into the gate op (the thread's segment is the four units it updates, so the hits
-// go straight into its own rows); other noise ops apply their hits with shared atomics.  Detection events
-// stream to global memory as [block][detector] uint4 rows.
+// frame_kernel<B, HITS>: one CTA owns a slice of B x 128 shots at a time (persistent, grid-stride over
+// slices).  Its X/Z Pauli frames ([row][block] uint4, 128 shots per uint4), the measurement ring, the
+// observable accumulators and the correlated-error flags live in shared memory for the whole circuit.  The
+// CTA walks the device program (program.h): every op spreads its independent units over the threads,
+// updates 128 shots per unit with 128-bit shared-memory loads/stores and bitwise logic, and ends with one
+// __syncthreads().  The lowering orders each gate op's units so that a quarter-warp's eight 16-byte
+// accesses fall in distinct bank groups.  Noise follows the counter-based stream of gfs_contract.h: with
+// HITS, noise_kernel has already drawn every hit into per-occurrence record lists and the frame kernel only
+// XORs them in; without, a thread owns a segment of 4 units x 128 shots and skips geometrically to its hits
+// (noise next to a gate on the same targets is fused into the gate op).  Detection events stream to
+// global memory as [block][detector] uint4 rows.
+//
+// noise_kernel<B>: one warp per (slice, noise occurrence), writing the hit records.
+//
+// batch_frame_kernel<B>: the frame kernel over many circuits' (circuit, slice) work items.
 //
 // transpose_tile_kernel: turns [block][row] bit-rows into shot-major bytes with 32x32 shuffle-butterfly
 // bit transposes, replacing the reference's bit-by-bit numpy conversion (numpy.pybind.cc:20-63) and
@@ -416,91 +421,168 @@ __device__ __forceinline__ uint64_t hit_record(uint32_t a, uint32_t b, uint32_t 
 // Occurrence kinds (how the frame kernel applies a record).
 enum : uint32_t { OCC_PAULI = 0, OCC_FLIP, OCC_HERALD, OCC_CORR };
 
-// Calls f(record) for every hit of one noise occurrence of `op` in this slice's B blocks: which = 0 for a
-// noise op, 1 for the noise fused before a gate (op.d), 2 for the noise fused after it (op.c).
-template <int B, typename F>
-__device__ __forceinline__ void occurrence_hits(const KernelArgs &p, const uint32_t *tables, const DevOp &op,
-                                                uint32_t which, uint64_t inst, uint64_t gb0, uint32_t tid,
-                                                uint32_t nt, F f) {
-    const uint32_t code = op.code & 0xFFu, sub = op.code >> 8;
-    const uint32_t a = op.a;
+// One noise occurrence resolved: channel, Pauli kind, stream purpose, units and where their rows are.
+struct OccParams {
     const DevChan *ch;
-    uint32_t kind, purpose = GFS_P_NOISE, n = op.n;
-    bool pair = false;
-    uint64_t oinst = inst;
+    uint32_t code, sub, kind, purpose, n, a;
+    bool pair, fused;
+    uint64_t inst;
+};
+
+// which = 0 for a noise op, 1 for the noise fused before a gate (op.d), 2 for the noise fused after it (op.c).
+__device__ __forceinline__ OccParams occ_params(const KernelArgs &p, const DevOp &op, uint32_t which,
+                                                uint64_t inst) {
+    OccParams o;
+    o.code = op.code & 0xFFu;
+    o.sub = (op.code >> 8) & 0xFFu;
+    o.a = op.a;
+    o.n = op.n;
+    o.purpose = GFS_P_NOISE;
+    o.pair = false;
+    o.fused = which != 0;
+    o.inst = inst;
     if (which) {
         const uint32_t w = which == 1 ? op.d : op.c;
-        ch = &p.chans[(w & kFusedChanMask) - 1];
-        kind = (w >> 20) & 0xFu;
-        oinst = inst + (int64_t)(int8_t)(w >> 24);
-        pair = code == OP_2Q;
+        o.ch = &p.chans[(w & kFusedChanMask) - 1];
+        o.kind = (w >> 20) & 0xFu;
+        o.inst = inst + (int64_t)(int8_t)(w >> 24);
+        o.pair = o.code == OP_2Q;
     } else {
-        ch = &p.chans[op.b];
-        kind = sub;
-        if (code == OP_NOISE) {
-            pair = sub == KN_DEP2 || sub == KN_PC2;
-        } else if (code == OP_MNOISE) {
-            purpose = GFS_P_MNOISE;
-            kind = KN_FLIP;
-        } else if (code == OP_CORR_MASK) {
-            n = 1;
+        o.ch = &p.chans[op.b];
+        o.kind = o.sub;
+        if (o.code == OP_NOISE) {
+            o.pair = o.sub == KN_DEP2 || o.sub == KN_PC2;
+        } else if (o.code == OP_MNOISE) {
+            o.purpose = GFS_P_MNOISE;
+            o.kind = KN_FLIP;
+        } else if (o.code == OP_CORR_MASK) {
+            o.n = 1;
         }
     }
-    if (!ch->active) {
-        return;
-    }
-    const uint32_t *T = tables + ch->table;
-    const uint32_t nseg = (n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
-    for (uint32_t item = tid; item < nseg * B; item += nt) {
-        const uint32_t g = item / B, blk = item % B;
-        const uint32_t u0 = g * GFS_SEG_UNITS;
-        walk_segment(*ch, T, p.seed, purpose, oinst, g, (uint32_t)(gb0 + blk), min(GFS_SEG_UNITS, n - u0),
-                     [&](uint32_t k, uint32_t shot, gfs_stream *st) {
-                         const uint32_t u = u0 + k, s9 = blk * 128 + shot;
-                         if (!which && code == OP_MNOISE) {
-                             f(hit_record(u, 0, 1, s9));
-                         } else if (!which && code == OP_CORR_MASK) {
-                             f(hit_record(0, 0, 0, s9));
-                         } else if (!which && code == OP_HERALD) {
-                             const uint32_t c = gfs_stream_next(st);
-                             const uint32_t v = sub == 0 ? (c & 3u) : pauli_xz(gfs_choice_weighted(c, ch->cum, 4));
-                             f(hit_record(__ldg(p.pool + a + u), u, v, s9));
-                         } else {
-                             const uint32_t bits = hit_bits(kind, *ch, st);
-                             const uint32_t r1 = __ldg(p.pool + a + (pair ? 2 * u : u));
-                             const uint32_t r2 = pair ? __ldg(p.pool + a + 2 * u + 1) : r1;
-                             f(hit_record(r1, r2, bits, s9));
-                         }
-                     });
-    }
+    return o;
 }
 
-// One warp per (slice, occurrence): the lanes walk the occurrence's segments and write each hit into the
-// occurrence's region of the slice, counting with a shared-memory cursor.  No barriers: occurrences and
-// slices are independent streams.
-template <int B>
-__global__ void __launch_bounds__(256) noise_kernel(const KernelArgs p) {
-    __shared__ uint32_t cursor[8];
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint64_t w = (uint64_t)blockIdx.x * 8 + warp;
-    if (w >= (uint64_t)p.nslices * p.n_occ) {
-        return;
+// The record of a hit on unit u at (block blk, shot), drawing the Pauli choice from the segment's stream
+// as the contract orders it.
+__device__ __forceinline__ uint64_t occ_record(const KernelArgs &p, const OccParams &o, uint32_t u, uint32_t blk,
+                                               uint32_t shot, gfs_stream *st) {
+    const uint32_t s9 = blk * 128 + shot;
+    if (!o.fused && o.code == OP_MNOISE) {
+        return hit_record(u, 0, 1, s9);
     }
+    if (!o.fused && o.code == OP_CORR_MASK) {
+        return hit_record(0, 0, 0, s9);
+    }
+    if (!o.fused && o.code == OP_HERALD) {
+        const uint32_t c = gfs_stream_next(st);
+        const uint32_t v = o.sub == 0 ? (c & 3u) : pauli_xz(gfs_choice_weighted(c, o.ch->cum, 4));
+        return hit_record(__ldg(p.pool + o.a + u), u, v, s9);
+    }
+    const uint32_t bits = hit_bits(o.kind, *o.ch, st);
+    const uint32_t r1 = __ldg(p.pool + o.a + (o.pair ? 2 * u : u));
+    const uint32_t r2 = o.pair ? __ldg(p.pool + o.a + 2 * u + 1) : r1;
+    return hit_record(r1, r2, bits, s9);
+}
+
+// One warp per (slice, occurrence).  Phase 1 is dense: each lane draws the first Philox group of one
+// segment, and the ~60% of segments (at p = 1e-3) whose first draw leaves the segment are done.  Segments
+// with a hit are queued in shared memory with their three unused draws; every 32 queued segments (and
+// at the end) phase 2 gives one to each lane, which continues the walk exactly where gfs_next_hit would
+// (same draws, same order) and writes each hit's record into the occurrence's region of the slice
+// through a shared-memory cursor.  No barriers: occurrences and slices are independent streams.
+struct NoiseQueued {
+    uint32_t item, u, d1, d2, d3;
+};
+
+// Warp `warp` of its CTA draws occurrence w % n_occ of slice w / n_occ of circuit p.
+template <int B>
+__device__ __forceinline__ void noise_warp(const KernelArgs &p, uint64_t w, uint32_t warp, uint32_t lane,
+                                           uint32_t *cursor, NoiseQueued (*queue)[64]) {
     const uint32_t slice = (uint32_t)(w / p.n_occ), k = (uint32_t)(w % p.n_occ);
     const NoiseOcc oc = p.occs[k];
     const DevOp op = p.ops[oc.pc];
+    const OccParams o = occ_params(p, op, oc.which, oc.inst);
     const uint64_t gb0 = p.block0 + (uint64_t)slice * B;
     uint64_t *region = p.hits + (uint64_t)slice * p.slice_cap + oc.off;
     if (lane == 0) {
         cursor[warp] = 0;
     }
     __syncwarp();
-    occurrence_hits<B>(p, p.tables, op, oc.which, oc.inst, gb0, lane, 32u, [&](uint64_t r) {
-        const uint32_t pos = atomicAdd(&cursor[warp], 1u);
-        if (pos < oc.cap) {
-            region[pos] = r;
+    if (o.ch->active) {
+        const DevChan &ch = *o.ch;
+        const uint32_t *T = p.tables + ch.table;
+        const bool always = ch.always != 0;
+        const uint32_t nseg = (o.n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
+        const uint32_t items = nseg * B;
+        const uint32_t kseed0 = (uint32_t)p.seed, kseed1 = (uint32_t)(p.seed >> 32);
+        const uint32_t c3base = gfs_c3(o.purpose, o.inst, 0);
+        NoiseQueued *q = queue[warp];
+        uint32_t qn = 0;  // warp-uniform
+        auto drain = [&](uint32_t take) {
+            if (lane < take) {
+                const NoiseQueued e = q[qn - take + lane];
+                const uint32_t g = e.item / B, blk = e.item % B;
+                const uint32_t u0 = g * GFS_SEG_UNITS;
+                const int32_t trials = (int32_t)(min(GFS_SEG_UNITS, o.n - u0) * GFS_BLOCK_SHOTS);
+                gfs_stream st;
+                gfs_stream_init(&st, p.seed, o.purpose, o.inst, g, (uint32_t)(gb0 + blk));
+                int32_t pos;
+                if (always) {
+                    pos = 0;
+                } else {
+                    // Group 0 was drawn in phase 1: u decided the first hit; d1..d3 come next.
+                    st.group = 1;
+                    st.left = 3;
+                    st.b0 = e.d1;
+                    st.b1 = e.d2;
+                    st.b2 = e.d3;
+                    pos = gfs_hit_after_draw(e.u, T, ch.inv_c, -1, trials);
+                }
+                while (pos >= 0) {
+                    const uint64_t r = occ_record(p, o, u0 + ((uint32_t)pos >> 7), blk, (uint32_t)pos & 127u, &st);
+                    const uint32_t at = atomicAdd(&cursor[warp], 1u);
+                    if (at < oc.cap) {
+                        region[at] = r;
+                    }
+                    pos = gfs_next_hit(&st, T, ch.inv_c, pos, trials, always);
+                }
+            }
+            qn -= take;
+            __syncwarp();
+        };
+        for (uint32_t base = 0; base < items; base += 32) {
+            const uint32_t item = base + lane;
+            bool hit = false;
+            uint32_t u = 0, d1 = 0, d2 = 0, d3 = 0;
+            if (item < items) {
+                if (always) {
+                    hit = true;
+                } else {
+                    const uint32_t g = item / B, blk = item % B;
+                    const uint32_t u0 = g * GFS_SEG_UNITS;
+                    const uint32_t trials = min(GFS_SEG_UNITS, o.n - u0) * GFS_BLOCK_SHOTS;
+                    const gfs_u32x4 r = gfs_philox(kseed0, kseed1, (uint32_t)(gb0 + blk), g, (uint32_t)o.inst, c3base);
+                    u = r.v[0];
+                    d1 = r.v[1];
+                    d2 = r.v[2];
+                    d3 = r.v[3];
+                    hit = u >= __ldg(T + trials);
+                }
+            }
+            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, hit);
+            if (hit) {
+                q[qn + __popc(mask & ((1u << lane) - 1u))] = NoiseQueued{item, u, d1, d2, d3};
+            }
+            qn += __popc(mask);
+            __syncwarp();
+            if (qn >= 32) {
+                drain(32);
+            }
         }
-    });
+        if (qn) {
+            drain(qn);
+        }
+    }
     __syncwarp();
     if (lane == 0) {
         uint32_t c = cursor[warp];
@@ -512,9 +594,40 @@ __global__ void __launch_bounds__(256) noise_kernel(const KernelArgs p) {
     }
 }
 
-// Applies the records of occurrence `occ` of this slice: Pauli flips into the frames, measurement flips
-// into the ring, heralds into the ring and frames; correlated-error hits are OR-ed into MSK (the caller
-// clears it first and derives the mask afterwards).
+template <int B>
+__global__ void __launch_bounds__(256) noise_kernel(const KernelArgs p) {
+    __shared__ uint32_t cursor[8];
+    __shared__ NoiseQueued queue[8][64];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint64_t w = (uint64_t)blockIdx.x * 8 + warp;
+    if (w < (uint64_t)p.nslices * p.n_occ) {
+        noise_warp<B>(p, w, warp, lane, cursor, queue);
+    }
+}
+
+// The noise of a batch: warp w belongs to circuit j with warp_prefix[j] <= w < warp_prefix[j + 1].
+template <int B>
+__global__ void __launch_bounds__(256) batch_noise_kernel(const BatchArgs b) {
+    __shared__ uint32_t cursor[8];
+    __shared__ NoiseQueued queue[8][64];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint64_t w = (uint64_t)blockIdx.x * 8 + warp;
+    if (w >= b.total_noise_warps) {
+        return;
+    }
+    uint32_t lo = 0, hi = b.ncircuits;  // last j with warp_prefix[j] <= w
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (b.warp_prefix[mid] <= w) {
+            lo = mid;
+        } else {
+            hi = mid;
+        }
+    }
+    const KernelArgs &p = b.circuits[lo];
+    noise_warp<B>(p, w - b.warp_prefix[lo], warp, lane, cursor, queue);
+}
+
 // Shared-memory layout of a CTA holding B blocks of 128 shots: X and Z frames [row][block], the
 // measurement ring [ring row][block] (unless it is in global memory), observable accumulators, the
 // correlated-error flags and mask, then the gap tables, the op stream, and the occurrence cache when they
@@ -685,7 +798,7 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
 
     for (;;) {
         const DevOp op = ops[pc];
-        const uint32_t code = op.code & 0xFFu, sub = op.code >> 8;
+        const uint32_t code = op.code & 0xFFu, sub = (op.code >> 8) & 0xFFu;
         const uint64_t inst = inst_base + op.inst;
         const uint32_t n = op.n, a = op.a;
         if (code == OP_END) {
@@ -735,11 +848,13 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
             __syncthreads();
         }
 
+        // Gate units in bank-friendly order (a second list when the op carries fused noise).
+        const uint32_t ga = (op.code & kGateOrderInB) ? op.b : a;
         switch (code) {
             case OP_1Q:
                 for (uint32_t i = tid; i < n * B; i += nt) {
                     uint32_t u = i / B, blk = i % B;
-                    uint32_t idx = __ldg(pool + a + u) * B + blk;
+                    uint32_t idx = __ldg(pool + ga + u) * B + blk;
                     uint4 x = X[idx], z = Z[idx];
                     switch (sub) {
                         case K1_H_XZ:
@@ -770,8 +885,8 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
                         const bool two = i2b < items;
                         const uint32_t ua = i / B, ba = i % B;
                         const uint32_t ub = two ? i2b / B : ua, bb = two ? i2b % B : ba;
-                        const uint32_t a1 = __ldg(pool + a + 2 * ua) * B + ba, a2 = __ldg(pool + a + 2 * ua + 1) * B + ba;
-                        const uint32_t b1 = __ldg(pool + a + 2 * ub) * B + bb, b2 = __ldg(pool + a + 2 * ub + 1) * B + bb;
+                        const uint32_t a1 = __ldg(pool + ga + 2 * ua) * B + ba, a2 = __ldg(pool + ga + 2 * ua + 1) * B + ba;
+                        const uint32_t b1 = __ldg(pool + ga + 2 * ub) * B + bb, b2 = __ldg(pool + ga + 2 * ub + 1) * B + bb;
                         uint4 az1 = Z[a1], az2 = Z[a2], ax1 = X[a1], ax2 = X[a2];
                         uint4 bz1 = Z[b1], bz2 = Z[b2], bx1 = X[b1], bx2 = X[b2];
                         if (sub == K2_CX) {
@@ -794,8 +909,8 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
                 }
                 for (uint32_t i = tid; i < n * B; i += nt) {
                     uint32_t u = i / B, blk = i % B;
-                    uint32_t i1 = __ldg(pool + a + 2 * u) * B + blk;
-                    uint32_t i2 = __ldg(pool + a + 2 * u + 1) * B + blk;
+                    uint32_t i1 = __ldg(pool + ga + 2 * u) * B + blk;
+                    uint32_t i2 = __ldg(pool + ga + 2 * u + 1) * B + blk;
                     uint4 x1 = X[i1], z1 = Z[i1], x2 = X[i2], z2 = Z[i2];
                     rule2v(sub, x1, z1, x2, z2);
                     X[i1] = x1;
@@ -1076,8 +1191,8 @@ __global__ void __launch_bounds__(256, HITS ? 4 : 3) frame_kernel(const KernelAr
 // circuit (b.slice_prefix[j] = first item of circuit j); CTAs claim items from a global counter, so
 // expensive and cheap circuits balance across the SMs.  A CTA reloads the circuit's descriptor, gap tables
 // and op stream only when its next item belongs to another circuit.
-template <int B>
-__global__ void __launch_bounds__(256, 3) batch_frame_kernel(const BatchArgs b) {
+template <int B, bool HITS>
+__global__ void __launch_bounds__(256, HITS ? 4 : 3) batch_frame_kernel(const BatchArgs b) {
     extern __shared__ uint4 sm[];
     __shared__ KernelArgs cur;
     __shared__ uint32_t s_item, s_circ;
@@ -1112,7 +1227,7 @@ __global__ void __launch_bounds__(256, 3) batch_frame_kernel(const BatchArgs b) 
             st = frame_state<B>(cur, sm);
             have = j;
         }
-        frame_slice<B, false>(cur, st, item - b.slice_prefix[j]);
+        frame_slice<B, HITS>(cur, st, item - b.slice_prefix[j]);
     }
 }
 
@@ -1179,48 +1294,63 @@ cudaError_t launch_noise_kernel(const KernelArgs &args, int blocks_per_cta, cuda
     }
 }
 
-template <int B>
+template <int B, bool H>
 static cudaError_t launch_batch_b(const BatchArgs &args, const LaunchShape &s, cudaStream_t stream) {
-    cudaError_t e = cudaFuncSetAttribute(batch_frame_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(batch_frame_kernel<B, H>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)s.smem);
     if (e != cudaSuccess) {
         return e;
     }
-    batch_frame_kernel<B><<<s.grid, s.threads, s.smem, stream>>>(args);
+    if (H) {
+        const uint64_t blocks = (args.total_noise_warps + 7) / 8;
+        if (blocks > 0x7FFFFFFFull) {
+            return cudaErrorInvalidValue;
+        }
+        if (blocks) {
+            batch_noise_kernel<B><<<(unsigned)blocks, 256, 0, stream>>>(args);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) {
+                return e;
+            }
+        }
+    }
+    batch_frame_kernel<B, H><<<s.grid, s.threads, s.smem, stream>>>(args);
     return cudaGetLastError();
 }
 
 cudaError_t launch_batch_frame_kernel(const BatchArgs &args, const LaunchShape &shape, cudaStream_t stream) {
+    const bool h = shape.hits;
     switch (shape.blocks_per_cta) {
         case 1:
-            return launch_batch_b<1>(args, shape, stream);
+            return h ? launch_batch_b<1, true>(args, shape, stream) : launch_batch_b<1, false>(args, shape, stream);
         case 2:
-            return launch_batch_b<2>(args, shape, stream);
+            return h ? launch_batch_b<2, true>(args, shape, stream) : launch_batch_b<2, false>(args, shape, stream);
         case 4:
-            return launch_batch_b<4>(args, shape, stream);
+            return h ? launch_batch_b<4, true>(args, shape, stream) : launch_batch_b<4, false>(args, shape, stream);
         default:
             return cudaErrorInvalidValue;
     }
 }
 
-template <int B>
+template <int B, bool H>
 static cudaError_t occ_batch_b(const LaunchShape &s, int *out) {
-    cudaError_t e = cudaFuncSetAttribute(batch_frame_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(batch_frame_kernel<B, H>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)s.smem);
     if (e != cudaSuccess) {
         return e;
     }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, batch_frame_kernel<B>, s.threads, s.smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, batch_frame_kernel<B, H>, s.threads, s.smem);
 }
 
 cudaError_t batch_frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out) {
+    const bool h = shape.hits;
     switch (shape.blocks_per_cta) {
         case 1:
-            return occ_batch_b<1>(shape, out);
+            return h ? occ_batch_b<1, true>(shape, out) : occ_batch_b<1, false>(shape, out);
         case 2:
-            return occ_batch_b<2>(shape, out);
+            return h ? occ_batch_b<2, true>(shape, out) : occ_batch_b<2, false>(shape, out);
         case 4:
-            return occ_batch_b<4>(shape, out);
+            return h ? occ_batch_b<4, true>(shape, out) : occ_batch_b<4, false>(shape, out);
         default:
             return cudaErrorInvalidValue;
     }
@@ -1272,17 +1402,33 @@ __device__ __forceinline__ uint4 load_concat(const TransposeArgs &t, uint64_t bl
     return v;
 }
 
-// Lane r holds row r of a 32x32 bit matrix (bit c = column c); afterwards lane c holds column c.
-__device__ __forceinline__ uint32_t transpose32(uint32_t x, uint32_t lane) {
-    const uint32_t lo[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+// Lane r holds row r of a 32x32 bit matrix (bit c = column c); afterwards lane c holds column c.  Stage s
+// (16, 8, 4, 2, 1) swaps the off-diagonal s x s sub-blocks between lanes l and l^s: the partner's word is
+// rotated by s toward the bits this lane takes (left when lane bit s is clear, right when set) and merged
+// under this lane's mask.  keep[k] / rot[k] depend only on the lane, so a stage is a shuffle, a funnel
+// shift and one bitwise select.
+struct Transpose32 {
+    uint32_t keep[5], rot[5];
+    __device__ __forceinline__ explicit Transpose32(uint32_t lane) {
+        const uint32_t lo[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
 #pragma unroll
-    for (int k = 0; k < 5; k++) {
-        const uint32_t s = 16u >> k, m = lo[k];
-        const uint32_t y = __shfl_xor_sync(0xFFFFFFFFu, x, s);
-        x = (lane & s) ? ((x & ~m) | ((y >> s) & m)) : ((x & m) | ((y & m) << s));
+        for (int k = 0; k < 5; k++) {
+            const uint32_t s = 16u >> k;
+            const bool hi = (lane & s) != 0;
+            keep[k] = hi ? ~lo[k] : lo[k];
+            rot[k] = hi ? 32u - s : s;
+        }
     }
-    return x;
-}
+    __device__ __forceinline__ uint32_t operator()(uint32_t x) const {
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+            const uint32_t y = __shfl_xor_sync(0xFFFFFFFFu, x, 16u >> k);
+            const uint32_t r = __funnelshift_l(y, y, rot[k]);
+            x = (x & keep[k]) | (r & ~keep[k]);
+        }
+        return x;
+    }
+};
 
 constexpr uint32_t kTileRows = 1024, kTileWords = kTileRows / 32;
 
@@ -1303,14 +1449,18 @@ __global__ void __launch_bounds__(256) transpose_tile_kernel(const TransposeArgs
     const uint64_t blk = blockIdx.y;
     const uint64_t total = t.n0 + t.n1 + t.n2;
     const uint64_t r0 = (uint64_t)blockIdx.x * kTileRows;
+    const Transpose32 transpose32(lane);
+    uint4 v[4];
+#pragma unroll
+    for (uint32_t g = 0; g < 4; g++) {  // all four loads in flight before the shuffles
+        v[g] = load_concat(t, blk, r0 + 128 * warp + 32 * g + lane, total);
+    }
 #pragma unroll
     for (uint32_t g = 0; g < 4; g++) {
-        const uint64_t r = r0 + 128 * warp + 32 * g + lane;
-        const uint4 v = load_concat(t, blk, r, total);
-        const uint32_t words[4] = {v.x, v.y, v.z, v.w};
+        const uint32_t words[4] = {v[g].x, v[g].y, v[g].z, v[g].w};
 #pragma unroll
         for (uint32_t w = 0; w < 4; w++) {
-            tile[32 * w + lane][4 * warp + g] = transpose32(words[w], lane);
+            tile[32 * w + lane][4 * warp + g] = transpose32(words[w]);
         }
     }
     __syncthreads();

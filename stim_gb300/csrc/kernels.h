@@ -50,6 +50,10 @@ struct BatchArgs {
     uint32_t ncircuits;
     uint32_t total_slices;
     uint32_t *counter;             // next unclaimed work item; zero before the launch
+    // Hit-list mode (LaunchShape::hits): batch_noise_kernel runs first, one warp per (circuit, slice,
+    // occurrence); circuit j owns noise warps warp_prefix[j] .. warp_prefix[j+1]-1.
+    const uint64_t *warp_prefix;   // ncircuits + 1 entries
+    uint64_t total_noise_warps;
 };
 
 struct LaunchShape {
@@ -70,6 +74,7 @@ cudaError_t launch_frame_kernel(const KernelArgs &args, const LaunchShape &shape
 // with inline noise).
 cudaError_t launch_noise_kernel(const KernelArgs &args, int blocks_per_cta, cudaStream_t stream);
 cudaError_t frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out);
+// In hit-list mode (shape.hits) this launches batch_noise_kernel and then the frame kernel.
 cudaError_t launch_batch_frame_kernel(const BatchArgs &args, const LaunchShape &shape, cudaStream_t stream);
 cudaError_t batch_frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out);
 

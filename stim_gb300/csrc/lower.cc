@@ -1065,6 +1065,91 @@ struct Lowerer {
         }
     }
 
+    // Reorders the units of every one- and two-qubit gate op so that each aligned group of 8 consecutive
+    // units touches 8 distinct residues (row mod 8) on each side.  Threads take consecutive units, a
+    // quarter-warp issues 8 lanes' 16-byte accesses together, and a row's 16 bytes sit in bank group
+    // row mod 8, so such a group is free of shared-memory bank conflicts (for 2 and 4 blocks per CTA the
+    // halves / quarters of a group stay distinct mod 4 / mod 2).  Units of one op act on distinct rows
+    // and commute, so the order does not change any result.  Ops with fused noise keep their list (the
+    // noise unit order is part of the random-bit contract) and get a second, reordered list at pool[b].
+    void bank_order_gates() {
+        for (DevOp &op : prog.ops) {
+            const uint32_t code = op.code & 0xFFu;
+            if ((code != OP_1Q && code != OP_2Q) || op.n < 16) {
+                continue;
+            }
+            const uint32_t stride = code == OP_2Q ? 2 : 1;
+            const uint32_t n = op.n;
+            std::vector<uint32_t> units(prog.pool.begin() + op.a, prog.pool.begin() + op.a + (size_t)n * stride);
+            std::vector<uint32_t> order;
+            order.reserve(n);
+            // Buckets by (first row mod 8, second row mod 8); one-qubit ops use residue 0 for the second.
+            std::vector<std::vector<uint32_t>> bucket(64);
+            for (uint32_t u = n; u-- > 0;) {
+                const uint32_t c = units[(size_t)u * stride] & 7u;
+                const uint32_t t = stride == 2 ? units[(size_t)u * stride + 1] & 7u : 0u;
+                bucket[c * 8 + t].push_back(u);
+            }
+            // Greedy, group by group: each slot takes a unit from the bucket whose residues are least used so
+            // far in the group (mod 8), in the slot's half of the group (mod 4: two blocks per CTA) and in its
+            // pair (mod 2: four blocks per CTA); ties go to the fullest bucket, keeping later groups balanced.
+            for (uint32_t left = n; left > 0;) {
+                uint32_t l8c[8] = {0}, l8t[8] = {0}, l4c[4] = {0}, l4t[4] = {0}, l2c[2] = {0}, l2t[2] = {0};
+                for (uint32_t slot = 0; slot < 8 && left > 0; slot++) {
+                    if (slot % 4 == 0) {
+                        std::fill(l4c, l4c + 4, 0u);
+                        std::fill(l4t, l4t + 4, 0u);
+                    }
+                    if (slot % 2 == 0) {
+                        l2c[0] = l2c[1] = l2t[0] = l2t[1] = 0;
+                    }
+                    int best = -1;
+                    uint32_t best_cost = ~0u;
+                    size_t best_size = 0;
+                    for (uint32_t bk = 0; bk < 64; bk++) {
+                        if (bucket[bk].empty()) {
+                            continue;
+                        }
+                        const uint32_t c = bk / 8, t = bk % 8;
+                        uint32_t cost = 4 * l8c[c] + 2 * l4c[c % 4] + l2c[c % 2];
+                        if (stride == 2) {
+                            cost += 4 * l8t[t] + 2 * l4t[t % 4] + l2t[t % 2];
+                        }
+                        if (cost < best_cost || (cost == best_cost && bucket[bk].size() > best_size)) {
+                            best = (int)bk;
+                            best_cost = cost;
+                            best_size = bucket[bk].size();
+                        }
+                    }
+                    order.push_back(bucket[best].back());
+                    bucket[best].pop_back();
+                    const uint32_t c = (uint32_t)best / 8, t = (uint32_t)best % 8;
+                    l8c[c]++;
+                    l8t[t]++;
+                    l4c[c % 4]++;
+                    l4t[t % 4]++;
+                    l2c[c % 2]++;
+                    l2t[t % 2]++;
+                    left--;
+                }
+            }
+            std::vector<uint32_t> out;
+            out.reserve(units.size());
+            for (uint32_t u : order) {
+                for (uint32_t j = 0; j < stride; j++) {
+                    out.push_back(units[(size_t)u * stride + j]);
+                }
+            }
+            if (op.c | op.d) {
+                op.b = (uint32_t)prog.pool.size();
+                op.code |= kGateOrderInB;
+                prog.pool.insert(prog.pool.end(), out.begin(), out.end());
+            } else {
+                std::copy(out.begin(), out.end(), prog.pool.begin() + op.a);
+            }
+        }
+    }
+
     void run() {
         prog.stats = root.stats();
         std::vector<uint8_t> used(prog.stats.num_qubits + 1, 0);
@@ -1072,9 +1157,21 @@ struct Lowerer {
         row_of.assign(used.size(), -1);
         for (size_t q = 0; q < used.size(); q++) {
             if (used[q]) {
-                row_of[q] = (int32_t)prog.qubit_orig.size();
                 prog.qubit_orig.push_back((uint32_t)q);
             }
+        }
+        // Rows are the used qubits in a fixed pseudo-random order (Fisher-Yates with a 64-bit LCG), so
+        // that the row residues mod 8 of any gate layer are spread out and bank_order_gates can form
+        // conflict-free groups; generated codes otherwise put a layer's rows on few residues.  Which row
+        // holds which qubit never affects results: the random streams are keyed by qubit and unit.
+        uint64_t lcg = 0x9E3779B97F4A7C15ull;
+        for (size_t k = prog.qubit_orig.size(); k > 1; k--) {
+            lcg = lcg * 6364136223846793005ull + 1442695040888963407ull;
+            const size_t j = (size_t)((lcg >> 33) % k);
+            std::swap(prog.qubit_orig[k - 1], prog.qubit_orig[j]);
+        }
+        for (size_t r = 0; r < prog.qubit_orig.size(); r++) {
+            row_of[prog.qubit_orig[r]] = (int32_t)r;
         }
         prog.num_rows = (uint32_t)prog.qubit_orig.size();
         if (prog.num_rows > kRowMask) {
@@ -1083,6 +1180,7 @@ struct Lowerer {
         lower_block(root, 0);
         flush_detectors();
         emit(OP_END, 0, 0, 0);
+        bank_order_gates();
         count_noise();
         prog.num_detectors = prog.stats.num_detectors;
         prog.num_observables = prog.stats.num_observables;

@@ -61,8 +61,12 @@ enum : uint32_t { KR_R = 0, KR_RX, KR_RY };
 enum : uint32_t { KN_X = 0, KN_Y, KN_Z, KN_DEP1, KN_PC1, KN_DEP2, KN_PC2, KN_FLIP };
 constexpr uint32_t kFusedChanMask = (1u << 20) - 1;
 
+// DevOp.code bit: the op's gate units are also listed, in bank-friendly order, at pool[b] (OP_1Q / OP_2Q
+// ops with fused noise, whose pool[a] list keeps the noise instruction's unit order).
+constexpr uint32_t kGateOrderInB = 1u << 24;
+
 struct alignas(16) DevOp {
-    uint32_t code;  // OpCode | sub << 8
+    uint32_t code;  // OpCode | sub << 8 | kGateOrderInB
     uint32_t n;
     uint32_t a, b, c, d;
     uint64_t inst;  // instance offset of the source instruction within the enclosing loop iteration

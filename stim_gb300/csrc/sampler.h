@@ -248,6 +248,20 @@ struct gfs_sampler {
         shape_inline = si;
     }
 
+    // Shape without timing: four 128-shot blocks per CTA when two such CTAs fit per SM (small and medium
+    // circuits), else one block per CTA of 128 threads, the ring wherever more blocks stay resident.
+    // (gfs_sampler_autotune picks by measurement instead.)
+    void default_shape() {
+        try {
+            choose_shape(4, 256, 0, ring_pref);
+            if (shape.grid >= 2 * num_sms) {
+                return;
+            }
+        } catch (const std::invalid_argument &) {
+        }
+        choose_shape(1, 128, 0, ring_pref);
+    }
+
     void init(const gfs_circuit *c, uint32_t m, uint64_t sd, int dev) {
         device = dev;
         mode = m;
@@ -282,8 +296,7 @@ struct gfs_sampler {
         upload(d_orig, prog.qubit_orig, device, stream);
         d_status.ensure(16, device);
         ck(cudaMemsetAsync(d_status.p, 0, 16, stream), "memset");
-        int bpc = 1;
-        choose_shape(bpc, 256, 0, ring_pref);
+        default_shape();
         ck(cudaStreamSynchronize(stream), "upload sync");
     }
 

@@ -360,7 +360,19 @@ struct gfs_server {
             err = std::string("batch failed: ") + cudaGetErrorString(e);
         } else {
             try {
-                slot.eng.check_status();
+                if (slot.eng.check_status()) {
+                    // A hit list overflowed: redo the batch with inline noise (identical results).
+                    slot.eng.force_inline = true;
+                    try {
+                        launch(slot);
+                        ck(cudaEventSynchronize(slot.eng.ev[2]), "batch redo");
+                        slot.eng.check_status();
+                    } catch (...) {
+                        slot.eng.force_inline = false;
+                        throw;
+                    }
+                    slot.eng.force_inline = false;
+                }
             } catch (const std::exception &x) {
                 err = x.what();
             }

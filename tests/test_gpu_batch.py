@@ -126,3 +126,20 @@ def test_sampler_autotune_keeps_results():
     d, o = s.sample(int(g["shots"]), bit_packed=True, separate_observables=True)
     np.testing.assert_array_equal(d, g["dets"])
     np.testing.assert_array_equal(o, g["obs"])
+
+
+def test_batch_hit_list_overflow_falls_back_to_inline_noise():
+    from stim_gb300 import _native
+
+    items = make(MIX)
+    samplers = [c.compile_detector_sampler(seed=seed) for c, seed, _, _ in items]
+    for s in samplers:
+        _native.check(_native.lib().gfs_sampler_set_hit_capacity(s._h, 2))  # far below the expected hits
+    batch = stim_gb300.BatchSampler(samplers)
+    shots = [s for _, _, s, _ in items]
+    got = [batch.sample(shots, bit_packed=True, separate_observables=True) for _ in range(2)]
+    want = singles(items, 2)
+    for call in range(2):
+        for j in range(len(items)):
+            np.testing.assert_array_equal(got[call][j][0], want[call][j][0])
+            np.testing.assert_array_equal(got[call][j][1], want[call][j][1])
