@@ -73,6 +73,20 @@ void gfs_circuit_free(gfs_circuit *c);
  */
 gfs_status gfs_program_info(const gfs_circuit *c, uint32_t mode, uint64_t *info8);
 /*
+ * sample_write: samples `shots` shots and writes them to `path` in a result format ("01", "b8", "r8",
+ * "hits", "dets", "ptb64"; null = "01").  Detections: flags may prepend or append observables, or
+ * obs_path (with obs_format) writes them to a file of their own; at most one of the three.  dets names
+ * detectors D<k>, observables L<k>, measurements M<k>.  ptb64 needs a multiple of 64 shots.
+ * Replaces CompiledDetectorSampler.sample_write (src/stim/py/compiled_detector_sampler.pybind.cc:88-141,
+ * 357-415) and CompiledMeasurementSampler.sample_write (src/stim/py/compiled_measurement_sampler.pybind.cc:
+ * 37-45, 245-290); the byte layouts are src/stim/io/measure_record_writer.cc:61-211.
+ */
+gfs_status gfs_sample_write_detections(gfs_sampler *s, uint64_t shots, const char *path, const char *format,
+                                       uint32_t flags, const char *obs_path, const char *obs_format);
+gfs_status gfs_sample_write_measurements(gfs_sampler *s, uint64_t shots, const char *path, const char *format,
+                                         const uint8_t *ref_sample);
+
+/*
  * The circuit's reference sample: its noiseless version run once on a host stabilizer tableau with every
  * random measurement outcome forced to 0, bit-packed little-endian into out[0 .. (measurements+7)/8).
  * Replaces TableauSimulator<W>::reference_sample_circuit (src/stim/simulators/tableau_simulator.inl:

@@ -221,6 +221,14 @@ class CompiledDetectorSampler(_SamplerBase):
         return dets
 
 
+def _path(p):
+    if isinstance(p, os.PathLike):
+        p = os.fspath(p)
+    if not isinstance(p, str):
+        raise ValueError(f"Don't know how to write to {p!r}")
+    return p.encode()
+
+
 class CompiledMeasurementSampler(_SamplerBase):
     """Samples measurement results = reference sample XOR frame flips (replaces CompiledMeasurementSampler)."""
 
@@ -248,6 +256,12 @@ class CompiledMeasurementSampler(_SamplerBase):
             self._ref = None
         else:
             self._ref = self._circuit.reference_sample(bit_packed=True)
+
+    def sample_write(self, shots: int, *, filepath, format: str = "01") -> None:
+        """Samples measurements and writes them to a file in a result format ("01", "b8", "r8", "hits",
+        "dets", "ptb64"), as the reference's CompiledMeasurementSampler.sample_write does."""
+        check(lib().gfs_sample_write_measurements(self._h, int(shots), _path(filepath), str(format).encode(),
+                                                  _ptr(self._ref) if self._ref is not None else None))
 
     def sample(self, shots: int, *, bit_packed: bool = False):
         shots = int(shots)

@@ -40,6 +40,9 @@ def _declare(L):
         "gfs_circuit_stats": [_vp, ctypes.POINTER(_u64)],
         "gfs_program_info": [_vp, ctypes.c_uint32, ctypes.POINTER(_u64)],
         "gfs_circuit_reference_sample": [_vp, _vp, _u64],
+        "gfs_sample_write_detections": [_vp, _u64, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint32,
+                                        ctypes.c_char_p, ctypes.c_char_p],
+        "gfs_sample_write_measurements": [_vp, _u64, ctypes.c_char_p, ctypes.c_char_p, _vp],
         "gfs_program_noise": [_vp, ctypes.c_uint32, ctypes.POINTER(_u64), ctypes.POINTER(ctypes.c_double)],
         "gfs_sampler_create": [_vp, ctypes.c_uint32, _u64, ctypes.c_int, ctypes.POINTER(_vp)],
         "gfs_sample_detections": [_vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64],

@@ -4,6 +4,7 @@
 
 #include <mutex>
 
+#include "formats.h"
 #include "noalloc.h"
 #include "tableau.h"
 
@@ -124,9 +125,110 @@ void detections_noalloc(gfs_sampler *s, uint64_t shots, uint32_t flags, uint8_t 
     s->t_copy = 0;
 }
 
+struct File {
+    FILE *f = nullptr;
+    File(const char *path) {
+        if (path) {
+            f = fopen(path, "wb");
+            if (!f) {
+                throw std::invalid_argument("Failed to open '" + std::string(path) + "' to write.");
+            }
+        }
+    }
+    ~File() {
+        if (f) {
+            fclose(f);
+        }
+    }
+};
+
+// Shots per sampled chunk when writing files: rows of `row_bytes` bytes in about 256 MiB of host memory,
+// a multiple of 128 shots (so of 64, as ptb64 needs).
+uint64_t write_chunk(uint64_t row_bytes) {
+    const uint64_t c = ((uint64_t)256 << 20) / std::max<uint64_t>(1, row_bytes);
+    return std::max<uint64_t>(128, c & ~(uint64_t)127);
+}
+
+// CompiledDetectorSampler.sample_write (compiled_detector_sampler.pybind.cc:88-141 and
+// frame_simulator_util.inl:120-200): detection events (observables prepended, appended, or to a file of
+// their own) in one of the result formats.
+void write_detections(gfs_sampler *s, uint64_t shots, const char *path, const char *format, uint32_t flags,
+                      const char *obs_path, const char *obs_format) {
+    if (s->mode != GFS_MODE_DETECTIONS) {
+        throw std::invalid_argument("sampler was not created in detection mode");
+    }
+    const bool prepend = flags & GFS_PREPEND_OBSERVABLES, append = flags & GFS_APPEND_OBSERVABLES;
+    if ((int)prepend + (int)append + (obs_path != nullptr) > 1) {
+        throw std::out_of_range("Can't combine --prepend_observables, --append_observables, or --obs_out");
+    }
+    const gfs::Format f = gfs::parse_format(format ? format : "01");
+    const gfs::Format of = gfs::parse_format(obs_format ? obs_format : "01");
+    const uint64_t D = s->prog.num_detectors, O = s->prog.num_observables;
+    if ((f == gfs::Format::PTB64 || (obs_path && of == gfs::Format::PTB64)) && shots % 64 != 0) {
+        throw std::invalid_argument("shots must be a multiple of 64 to use ptb64 format.");
+    }
+    File out(path), obs_out(obs_path);
+    const uint64_t nd = D + (prepend || append ? O : 0);
+    const uint64_t drow = (nd + 7) / 8, orow = (O + 7) / 8;
+    const uint64_t chunk = write_chunk(drow + orow);
+    std::vector<uint8_t> dbuf, obuf;
+    for (uint64_t done = 0; done < shots;) {
+        const uint64_t cs = std::min<uint64_t>(shots - done, chunk);
+        dbuf.resize(std::max<uint64_t>(1, cs * drow));
+        if (obs_path) {
+            obuf.resize(std::max<uint64_t>(1, cs * orow));
+        }
+        s->detections(cs, (flags & (GFS_PREPEND_OBSERVABLES | GFS_APPEND_OBSERVABLES)) | GFS_BIT_PACKED, dbuf.data(),
+                      std::max<uint64_t>(1, drow), obs_path ? obuf.data() : nullptr, std::max<uint64_t>(1, orow), false);
+        // Prefixes as the reference names them: D then L when appended, L then D when prepended.
+        if (append) {
+            gfs::write_rows(out.f, f, dbuf.data(), std::max<uint64_t>(1, drow), cs, nd, 'D', 'L', D);
+        } else if (prepend) {
+            gfs::write_rows(out.f, f, dbuf.data(), std::max<uint64_t>(1, drow), cs, nd, 'L', 'D', O);
+        } else {
+            gfs::write_rows(out.f, f, dbuf.data(), std::max<uint64_t>(1, drow), cs, nd, 'D', 'L', D);
+        }
+        if (obs_path) {
+            gfs::write_rows(obs_out.f, of, obuf.data(), std::max<uint64_t>(1, orow), cs, O, 'L', 'L', O);
+        }
+        done += cs;
+    }
+}
+
+// CompiledMeasurementSampler.sample_write (compiled_measurement_sampler.pybind.cc:37-45).
+void write_measurements(gfs_sampler *s, uint64_t shots, const char *path, const char *format, const uint8_t *ref) {
+    const gfs::Format f = gfs::parse_format(format ? format : "01");
+    if (f == gfs::Format::PTB64 && shots % 64 != 0) {
+        throw std::invalid_argument("shots must be a multiple of 64 to use ptb64 format.");
+    }
+    File out(path);
+    const uint64_t M = s->prog.num_measurements;
+    const uint64_t row = (M + 7) / 8;
+    const uint64_t chunk = write_chunk(row);
+    std::vector<uint8_t> buf;
+    for (uint64_t done = 0; done < shots;) {
+        const uint64_t cs = std::min<uint64_t>(shots - done, chunk);
+        buf.resize(std::max<uint64_t>(1, cs * row));
+        s->measurements(cs, GFS_BIT_PACKED, ref, buf.data(), std::max<uint64_t>(1, row));
+        gfs::write_rows(out.f, f, buf.data(), std::max<uint64_t>(1, row), cs, M, 'M', 'M', 0);
+        done += cs;
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+gfs_status gfs_sample_write_detections(gfs_sampler *s, uint64_t shots, const char *path, const char *format,
+                                       uint32_t flags, const char *obs_path, const char *obs_format) {
+    return guarded([&] { write_detections(s, shots, path, format, flags, obs_path, obs_format); });
+}
+
+gfs_status gfs_sample_write_measurements(gfs_sampler *s, uint64_t shots, const char *path, const char *format,
+                                         const uint8_t *ref_sample) {
+    return guarded([&] { write_measurements(s, shots, path, format, ref_sample); });
+}
+
 
 const char *gfs_last_error(void) {
     return g_err.c_str();

@@ -488,8 +488,8 @@ __device__ __forceinline__ uint64_t occ_record(const KernelArgs &p, const OccPar
 // segment, and the ~60% of segments (at p = 1e-3) whose first draw leaves the segment are done.  Segments
 // with a hit are queued in shared memory with their three unused draws; every 32 queued segments (and
 // at the end) phase 2 gives one to each lane, which continues the walk exactly where gfs_next_hit would
-// (same draws, same order) and writes each hit's record into the occurrence's region of the slice
-// through a shared-memory cursor.  No barriers: occurrences and slices are independent streams.
+// (same draws, same order) and writes each hit's record into the occurrence's region of the slice.  No
+// barriers: occurrences and slices are independent streams.
 struct NoiseQueued {
     uint32_t item, u, d1, d2, d3;
 };
@@ -497,17 +497,14 @@ struct NoiseQueued {
 // Warp `warp` of its CTA draws occurrence w % n_occ of slice w / n_occ of circuit p.
 template <int B>
 __device__ __forceinline__ void noise_warp(const KernelArgs &p, uint64_t w, uint32_t warp, uint32_t lane,
-                                           uint32_t *cursor, NoiseQueued (*queue)[64]) {
+                                           NoiseQueued (*queue)[64]) {
     const uint32_t slice = (uint32_t)(w / p.n_occ), k = (uint32_t)(w % p.n_occ);
     const NoiseOcc oc = p.occs[k];
     const DevOp op = p.ops[oc.pc];
     const OccParams o = occ_params(p, op, oc.which, oc.inst);
     const uint64_t gb0 = p.block0 + (uint64_t)slice * B;
     uint64_t *region = p.hits + (uint64_t)slice * p.slice_cap + oc.off;
-    if (lane == 0) {
-        cursor[warp] = 0;
-    }
-    __syncwarp();
+    uint32_t count = 0;  // records of this occurrence so far (warp-uniform)
     if (o.ch->active) {
         const DevChan &ch = *o.ch;
         const uint32_t *T = p.tables + ch.table;
@@ -518,15 +515,20 @@ __device__ __forceinline__ void noise_warp(const KernelArgs &p, uint64_t w, uint
         const uint32_t c3base = gfs_c3(o.purpose, o.inst, 0);
         NoiseQueued *q = queue[warp];
         uint32_t qn = 0;  // warp-uniform
+        // Phase 2 in lockstep: every round each lane with a pending hit writes one record; the records of a
+        // round get consecutive slots (ballot prefix), so the stores coalesce and no atomics are needed.
         auto drain = [&](uint32_t take) {
-            if (lane < take) {
+            const bool live = lane < take;
+            gfs_stream st;
+            int32_t pos = -1, trials = 0;
+            uint32_t u0 = 0, blk = 0;
+            if (live) {
                 const NoiseQueued e = q[qn - take + lane];
-                const uint32_t g = e.item / B, blk = e.item % B;
-                const uint32_t u0 = g * GFS_SEG_UNITS;
-                const int32_t trials = (int32_t)(min(GFS_SEG_UNITS, o.n - u0) * GFS_BLOCK_SHOTS);
-                gfs_stream st;
+                const uint32_t g = e.item / B;
+                blk = e.item % B;
+                u0 = g * GFS_SEG_UNITS;
+                trials = (int32_t)(min(GFS_SEG_UNITS, o.n - u0) * GFS_BLOCK_SHOTS);
                 gfs_stream_init(&st, p.seed, o.purpose, o.inst, g, (uint32_t)(gb0 + blk));
-                int32_t pos;
                 if (always) {
                     pos = 0;
                 } else {
@@ -538,14 +540,22 @@ __device__ __forceinline__ void noise_warp(const KernelArgs &p, uint64_t w, uint
                     st.b2 = e.d3;
                     pos = gfs_hit_after_draw(e.u, T, ch.inv_c, -1, trials);
                 }
-                while (pos >= 0) {
+            }
+            for (;;) {
+                const bool has = pos >= 0;
+                const uint32_t m = __ballot_sync(0xFFFFFFFFu, has);
+                if (!m) {
+                    break;
+                }
+                if (has) {
                     const uint64_t r = occ_record(p, o, u0 + ((uint32_t)pos >> 7), blk, (uint32_t)pos & 127u, &st);
-                    const uint32_t at = atomicAdd(&cursor[warp], 1u);
+                    const uint32_t at = count + __popc(m & ((1u << lane) - 1u));
                     if (at < oc.cap) {
                         region[at] = r;
                     }
                     pos = gfs_next_hit(&st, T, ch.inv_c, pos, trials, always);
                 }
+                count += __popc(m);
             }
             qn -= take;
             __syncwarp();
@@ -583,32 +593,28 @@ __device__ __forceinline__ void noise_warp(const KernelArgs &p, uint64_t w, uint
             drain(qn);
         }
     }
-    __syncwarp();
     if (lane == 0) {
-        uint32_t c = cursor[warp];
-        if (c > oc.cap) {
+        if (count > oc.cap) {
             atomicOr(p.status, 4u);
-            c = 0;
+            count = 0;
         }
-        p.hit_count[w] = c;
+        p.hit_count[w] = count;
     }
 }
 
 template <int B>
 __global__ void __launch_bounds__(256) noise_kernel(const KernelArgs p) {
-    __shared__ uint32_t cursor[8];
     __shared__ NoiseQueued queue[8][64];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint64_t w = (uint64_t)blockIdx.x * 8 + warp;
     if (w < (uint64_t)p.nslices * p.n_occ) {
-        noise_warp<B>(p, w, warp, lane, cursor, queue);
+        noise_warp<B>(p, w, warp, lane, queue);
     }
 }
 
 // The noise of a batch: warp w belongs to circuit j with warp_prefix[j] <= w < warp_prefix[j + 1].
 template <int B>
 __global__ void __launch_bounds__(256) batch_noise_kernel(const BatchArgs b) {
-    __shared__ uint32_t cursor[8];
     __shared__ NoiseQueued queue[8][64];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint64_t w = (uint64_t)blockIdx.x * 8 + warp;
@@ -625,7 +631,7 @@ __global__ void __launch_bounds__(256) batch_noise_kernel(const BatchArgs b) {
         }
     }
     const KernelArgs &p = b.circuits[lo];
-    noise_warp<B>(p, w - b.warp_prefix[lo], warp, lane, cursor, queue);
+    noise_warp<B>(p, w - b.warp_prefix[lo], warp, lane, queue);
 }
 
 // Shared-memory layout of a CTA holding B blocks of 128 shots: X and Z frames [row][block], the

@@ -501,16 +501,17 @@ struct gfs_sampler {
         return best;
     }
 
-    // Chunk size (in 128-shot blocks) for host destinations: at least four chunks for requests of four or
-    // more full waves, so that copies overlap kernels, within the device memory budget.
+    // Chunk size (in 128-shot blocks) for host destinations: about eight chunks for large requests, so that
+    // copies overlap kernels, each a whole number of resident waves (no extra tail), within the device
+    // memory budget.
     uint64_t host_chunk_blocks(uint64_t nblk_total, uint64_t slot_row_bytes) const {
         uint64_t cb = chunk_blocks(2 * slot_row_bytes);
         if (chunk_shots) {
             return cb;
         }
         uint64_t wave = (uint64_t)shape.grid * (uint64_t)shape.blocks_per_cta;
-        uint64_t quarter = (nblk_total + 3) / 4;
-        uint64_t target = std::max<uint64_t>(wave, ((quarter + wave - 1) / wave) * wave);
+        uint64_t eighth = (nblk_total + 7) / 8;
+        uint64_t target = std::max<uint64_t>(wave, ((eighth + wave - 1) / wave) * wave);
         return std::min<uint64_t>(cb, target);
     }
 
