@@ -30,6 +30,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "detection-event Gbit/s at d=25 r=25 (surface_code:rotated_memory_z, p=1e-3)"
+# DRAM bytes per shot of the frame kernel on this workload, dram__bytes_read.sum + dram__bytes_write.sum from
+# one ncu capture of 131,072 shots (hit-list mode, 1 block x 128 threads per CTA); traffic grows with shots.
+FRAME_DRAM_BYTES_PER_SHOT = 2898.0
 UNIT = "Gbit/s"
 WORKLOAD = dict(family="surface_code:rotated_memory_z", distance=25, rounds=25, p=0.001)
 
@@ -253,7 +256,7 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    frame_ms, noise_ms, step_ms, launches = [], [], [], 0
+    frame_ms, noise_ms, step_ms, launches, frame_launches = [], [], [], 0, 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
         flush.zero_()  # outputs exceed L2 anyway; also evict them between steps
@@ -262,6 +265,7 @@ def run_gpu(args):
         noise_ms.append(t["noise_ms"])
         step_ms.append(t["frame_ms"] + t["noise_ms"] + t["transpose_ms"])
         launches += t["frame_launches"] + t["noise_launches"] + t["transpose_launches"]
+        frame_launches += t["frame_launches"]
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     if world > 1:
@@ -292,6 +296,7 @@ def run_gpu(args):
     acc_bits, rbits, hits = algorithmic_work(text)
     frame_avg_s = statistics.mean(frame_ms) / 1e3
     achieved_gbs = acc_bits / 8 * shots / frame_avg_s / 1e9
+    shots_per_frame_launch = shots * args.steps / max(1, frame_launches)
     smem_peak = _native.measure_smem_peak(local) / 1e9
     # Transpose: reads the detector-major rows (16 bytes per row per 128 shots) and writes the shot-major rows.
     tr_ms = statistics.mean(t - f - z for t, f, z in zip(step_ms, frame_ms, noise_ms))
@@ -329,7 +334,10 @@ def run_gpu(args):
                     if e2e_parts else None},
             "gpu_launches": launches,
             "roofline": {"bound": "smem", "achieved": achieved_gbs, "peak": smem_peak, "unit": "GB/s",
-                         "frac": achieved_gbs / smem_peak, "traffic": None,
+                         "frac": achieved_gbs / smem_peak,
+                         "traffic": FRAME_DRAM_BYTES_PER_SHOT * shots_per_frame_launch,
+                         "traffic_note": "DRAM bytes per frame-kernel launch (ncu per-shot figure x shots per "
+                                         "launch); shared memory, not DRAM, bounds this kernel",
                          "basis": f"{acc_bits:.0f} frame-bit accesses/shot x {shots} shots per frame-kernel launch; "
                                   "peak = project shared-memory probe (gfs_measure_smem_peak)"},
             "roofline_transpose": {"bound": "hbm", "achieved": tr_bytes / (tr_ms / 1e3) / 1e9, "peak": hbm_peak,
