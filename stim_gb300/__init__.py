@@ -220,6 +220,18 @@ class CompiledDetectorSampler(_SamplerBase):
             return dets, obs
         return dets
 
+    def sample_write(self, shots: int, *, filepath, format: str = "01", obs_out_filepath=None,
+                     obs_out_format: str = "01", prepend_observables: bool = False,
+                     append_observables: bool = False) -> None:
+        """Samples detection events and writes them to a file in a result format ("01", "b8", "r8", "hits",
+        "dets", "ptb64"), observables prepended, appended or written to ``obs_out_filepath``, as the
+        reference's CompiledDetectorSampler.sample_write does (compiled_detector_sampler.pybind.cc:357-415)."""
+        flags = ((_native.PREPEND_OBSERVABLES if prepend_observables else 0)
+                 | (_native.APPEND_OBSERVABLES if append_observables else 0))
+        check(lib().gfs_sample_write_detections(
+            self._h, int(shots), _path(filepath), str(format).encode(), flags,
+            _path(obs_out_filepath) if obs_out_filepath is not None else None, str(obs_out_format).encode()))
+
 
 def _path(p):
     if isinstance(p, os.PathLike):
