@@ -192,6 +192,7 @@ struct BatchEngine {
             a.tables = (const uint32_t *)s->d_tables.p;
             a.chans = (const gfs::DevChan *)s->d_chans.p;
             a.qubit_orig = (const uint32_t *)s->d_orig.p;
+            a.reset_zero = s->prog.reset_norand ? 1u : 0u;
             a.nrows = s->prog.num_rows;
             a.ring = s->prog.ring;
             a.nobs = (uint32_t)s->prog.num_observables;

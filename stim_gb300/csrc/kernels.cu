@@ -22,6 +22,7 @@
 #include <cstdio>
 
 #include "gfs_contract.h"
+#include "frame_rules.h"
 #include "kernels.h"
 
 namespace gfs {
@@ -43,111 +44,6 @@ __device__ __forceinline__ void atomic_xor_bit(uint4 *base, uint32_t idx, uint32
 }
 __device__ __forceinline__ void atomic_or_bit(uint4 *base, uint32_t idx, uint32_t shot) {
     atomicOr(reinterpret_cast<uint32_t *>(base + idx) + (shot >> 5), 1u << (shot & 31));
-}
-
-// Two-qubit frame rules (frame_simulator.inl:386-630), one 32-bit word at a time.
-__device__ __forceinline__ void rule2(uint32_t sub, uint32_t &x1, uint32_t &z1, uint32_t &x2, uint32_t &z2) {
-    switch (sub) {
-        case K2_CX:
-            z1 ^= z2;
-            x2 ^= x1;
-            break;
-        case K2_CY:
-            z1 ^= x2 ^ z2;
-            z2 ^= x1;
-            x2 ^= x1;
-            break;
-        case K2_CZ:
-            z1 ^= x2;
-            z2 ^= x1;
-            break;
-        case K2_XCX:
-            x1 ^= z2;
-            x2 ^= z1;
-            break;
-        case K2_XCY:
-            x1 ^= x2 ^ z2;
-            x2 ^= z1;
-            z2 ^= z1;
-            break;
-        case K2_YCX:
-            x2 ^= x1 ^ z1;
-            x1 ^= z2;
-            z1 ^= z2;
-            break;
-        case K2_YCY: {
-            uint32_t y1 = x1 ^ z1, y2 = x2 ^ z2;
-            x1 ^= y2;
-            z1 ^= y2;
-            x2 ^= y1;
-            z2 ^= y1;
-            break;
-        }
-        case K2_SWAP: {
-            uint32_t t = x1;
-            x1 = x2;
-            x2 = t;
-            t = z1;
-            z1 = z2;
-            z2 = t;
-            break;
-        }
-        case K2_ISWAP: {
-            uint32_t dx = x1 ^ x2;
-            uint32_t t1 = z1 ^ dx, t2 = z2 ^ dx;
-            z1 = t2;
-            z2 = t1;
-            uint32_t t = x1;
-            x1 = x2;
-            x2 = t;
-            break;
-        }
-        case K2_CXSWAP:
-            z2 ^= z1;
-            z1 ^= z2;
-            x1 ^= x2;
-            x2 ^= x1;
-            break;
-        case K2_CZSWAP: {
-            uint32_t t = x1;
-            x1 = x2;
-            x2 = t;
-            t = z1;
-            z1 = z2;
-            z2 = t;
-            z1 ^= x2;
-            z2 ^= x1;
-            break;
-        }
-        case K2_SWAPCX:
-            z1 ^= z2;
-            z2 ^= z1;
-            x2 ^= x1;
-            x1 ^= x2;
-            break;
-        case K2_SQRT_XX: {
-            uint32_t dz = z1 ^ z2;
-            x1 ^= dz;
-            x2 ^= dz;
-            break;
-        }
-        case K2_SQRT_YY: {
-            uint32_t d = x1 ^ z1 ^ x2 ^ z2;
-            x1 ^= d;
-            z1 ^= d;
-            x2 ^= d;
-            z2 ^= d;
-            break;
-        }
-        case K2_SQRT_ZZ: {
-            uint32_t dx = x1 ^ x2;
-            z1 ^= dx;
-            z2 ^= dx;
-            break;
-        }
-        default:
-            break;
-    }
 }
 
 __device__ __forceinline__ void rule2v(uint32_t sub, uint4 &x1, uint4 &z1, uint4 &x2, uint4 &z2) {
@@ -244,29 +140,71 @@ __device__ __forceinline__ Fused decode_fused(const KernelArgs &p, uint32_t v, u
     return f;
 }
 
-// Applies the one-qubit frame rule of a K1_* gate.
+// Applies the one-qubit frame rule of a K1_* gate to 128 shots.
 __device__ __forceinline__ void rule1(uint32_t sub, uint4 &x, uint4 &z) {
+    rule1w(sub, x.x, z.x);
+    rule1w(sub, x.y, z.y);
+    rule1w(sub, x.z, z.z);
+    rule1w(sub, x.w, z.w);
+}
+
+// The randomized row of unit u of a measurement / reset instance (zero when the lowering proved the row
+// never reaches an output of this sampling mode).
+__device__ __forceinline__ uint4 rand_row(const KernelArgs &p, bool norand, uint64_t inst, uint32_t unit,
+                                          uint32_t block) {
+    return norand ? zero4() : u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, unit, block));
+}
+
+// Measurement-ring accesses.  When the ring is in global memory (rg) they go through L2 only: the ring is
+// private to its CTA, and keeping it out of L1 leaves L1 to the op lists that every CTA on the SM reads.
+__device__ __forceinline__ uint4 ring_ld(const uint4 *R, uint32_t i, bool rg) {
+    return rg ? __ldcg(R + i) : R[i];
+}
+__device__ __forceinline__ void ring_st(uint4 *R, uint32_t i, uint4 v, bool rg) {
+    if (rg) {
+        __stcg(R + i, v);
+    } else {
+        R[i] = v;
+    }
+}
+
+// Measurement of one row: the result goes to ring slot `slot`, the measured basis is re-randomized.
+__device__ __forceinline__ void measure_row(uint32_t sub, uint4 *X, uint4 *Z, uint4 *R, uint32_t idx, uint32_t slot,
+                                            uint4 r, bool rg) {
+    const uint4 x = X[idx];
     switch (sub) {
-        case K1_H_XZ: {
-            uint4 t = x;
-            x = z;
-            z = t;
+        case KM_M:
+            ring_st(R, slot, x, rg);
+            Z[idx] = r;
+            break;
+        case KM_MX:
+            ring_st(R, slot, Z[idx], rg);
+            X[idx] = r;
+            break;
+        case KM_MY: {
+            const uint4 y = x4(x, Z[idx]);
+            ring_st(R, slot, y, rg);
+            X[idx] = x4(y, r);
+            Z[idx] = r;
             break;
         }
-        case K1_H_XY:
-            z = x4(z, x);
+        case KM_MR:
+            ring_st(R, slot, x, rg);
+            X[idx] = zero4();
+            Z[idx] = r;
             break;
-        case K1_H_YZ:
-            x = x4(x, z);
+        case KM_MRX:
+            ring_st(R, slot, Z[idx], rg);
+            Z[idx] = zero4();
+            X[idx] = r;
             break;
-        case K1_C_XYZ:
-            x = x4(x, z);
-            z = x4(z, x);
+        default: {  // KM_MRY
+            const uint4 y = x4(x, Z[idx]);
+            ring_st(R, slot, y, rg);
+            Z[idx] = r;
+            X[idx] = r;
             break;
-        default:  // K1_C_ZYX
-            z = x4(z, x);
-            x = x4(x, z);
-            break;
+        }
     }
 }
 
@@ -280,7 +218,7 @@ __device__ __forceinline__ void rule1(uint32_t sub, uint4 &x, uint4 &z) {
 template <int B>
 __device__ __forceinline__ void gate_unit(const KernelArgs &p, uint32_t code, uint32_t sub, uint32_t a, uint32_t rb,
                                           uint64_t inst, uint32_t u, uint32_t blk, uint32_t block, uint4 *X, uint4 *Z,
-                                          uint4 *R, uint32_t rec, uint32_t L) {
+                                          uint4 *R, uint32_t rec, uint32_t L, bool norand) {
     const bool pair = code == OP_2Q;
     const uint32_t i1 = __ldg(p.pool + a + (pair ? 2 * u : u)) * B + blk;
     if (pair) {
@@ -297,41 +235,10 @@ __device__ __forceinline__ void gate_unit(const KernelArgs &p, uint32_t code, ui
         X[i1] = x;
         Z[i1] = z;
     } else if (code == OP_MEASURE) {
-        const uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, rb + u, block));
-        const uint32_t slot = wrap(rec + u, L) * B + blk;
-        const uint4 x = X[i1], z = Z[i1];
-        switch (sub) {
-            case KM_M:
-                R[slot] = x;
-                Z[i1] = r;
-                break;
-            case KM_MX:
-                R[slot] = z;
-                X[i1] = r;
-                break;
-            case KM_MY:
-                R[slot] = x4(x, z);
-                X[i1] = x4(x4(x, z), r);
-                Z[i1] = r;
-                break;
-            case KM_MR:
-                R[slot] = x;
-                X[i1] = zero4();
-                Z[i1] = r;
-                break;
-            case KM_MRX:
-                R[slot] = z;
-                Z[i1] = zero4();
-                X[i1] = r;
-                break;
-            default:  // KM_MRY
-                R[slot] = x4(x, z);
-                Z[i1] = r;
-                X[i1] = r;
-                break;
-        }
+        measure_row(sub, X, Z, R, i1, wrap(rec + u, L) * B + blk, rand_row(p, norand, inst, rb + u, block),
+                    p.ring_global != nullptr);
     } else {  // OP_RESET
-        const uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, rb + u, block));
+        const uint4 r = rand_row(p, norand, inst, rb + u, block);
         X[i1] = sub == KR_R ? zero4() : r;
         Z[i1] = sub == KR_RX ? zero4() : r;
     }
@@ -381,7 +288,8 @@ __device__ __forceinline__ void fused_gate(const KernelArgs &p, const DevOp &op,
             const uint32_t j = m * 32 + lane;  // (unit, block) gate item of this warp, blocks fastest
             const uint32_t u = ubase + j / B, gb = j % B;
             if (u < n && (item0 + (j / B) / GFS_SEG_UNITS * B + gb) < items) {
-                gate_unit<B>(p, code, sub, a, op.b, inst, u, gb, (uint32_t)(gb0 + gb), X, Z, R, rec, L);
+                gate_unit<B>(p, code, sub, a, op.b, inst, u, gb, (uint32_t)(gb0 + gb), X, Z, R, rec, L,
+                             (op.code & kNoRandomize) != 0);
             }
         }
         if (post.ch) {
@@ -653,6 +561,28 @@ __device__ __forceinline__ const uint64_t *occ_records(const KernelArgs &p, cons
     return p.hits + (uint64_t)slice * p.slice_cap + (occ_off ? occ_off[occ] : p.occs[occ].off);
 }
 
+// The records this thread applies first from the next occurrence (indices tid and tid + nt), loaded one
+// hit phase ahead so that their latency overlaps the gate phases in between.
+struct HitPre {
+    uint64_t r0, r1;
+};
+
+__device__ __forceinline__ void hit_prefetch(const KernelArgs &p, const uint32_t *occ_off, const uint32_t *occ_cnt,
+                                             uint32_t slice, uint32_t occ, uint32_t tid, uint32_t nt, HitPre &h) {
+    h.r0 = h.r1 = 0;
+    if (occ < p.n_occ) {
+        uint32_t count;
+        const uint64_t *r = occ_records(p, occ_off, occ_cnt, slice, occ, &count);
+        const unsigned long long *rr = reinterpret_cast<const unsigned long long *>(r);
+        if (tid < count) {
+            h.r0 = __ldg(rr + tid);
+        }
+        if (tid + nt < count) {
+            h.r1 = __ldg(rr + tid + nt);
+        }
+    }
+}
+
 // Starts pulling occurrence `occ`'s records into L2 (one bulk prefetch; regions start on 16 bytes and
 // hold an even number of records, so rounding the size up stays inside the region).
 __device__ __forceinline__ void prefetch_occurrence(const KernelArgs &p, const uint32_t *occ_off,
@@ -670,12 +600,13 @@ __device__ __forceinline__ void prefetch_occurrence(const KernelArgs &p, const u
 
 // Applies the records of occurrence `occ` of this slice: Pauli flips into the frames, measurement flips
 // into the ring, heralds into the ring and frames; correlated-error hits are OR-ed into MSK (the caller
-// clears it first and derives the mask afterwards).  Thread 0 then prefetches the records two
-// occurrences ahead.
+// clears it first and derives the mask afterwards).  The thread's first two records come from `pre`
+// (loaded a phase earlier); it then loads its first two records of the next occurrence into `pre`, and
+// thread 0 prefetches the records two occurrences ahead into L2.
 template <int B>
 __device__ __forceinline__ void apply_hits(const KernelArgs &p, const FrameState &st, uint32_t slice, uint32_t occ,
                                            uint32_t kind, uint4 *X, uint4 *Z, uint4 *R, uint4 *MSK, uint32_t rec,
-                                           uint32_t L, uint32_t n, uint32_t tid, uint32_t nt) {
+                                           uint32_t L, uint32_t n, uint32_t tid, uint32_t nt, HitPre &pre) {
     if (occ >= p.n_occ) {  // the host counted fewer occurrences than the program has
         if (tid == 0) {
             atomicOr(p.status, 2u);
@@ -687,8 +618,12 @@ __device__ __forceinline__ void apply_hits(const KernelArgs &p, const FrameState
     }
     uint32_t count;
     const uint64_t *h = occ_records(p, st.occ_off, st.occ_cnt, slice, occ, &count);
+    const HitPre cur = pre;
+    hit_prefetch(p, st.occ_off, st.occ_cnt, slice, occ + 1, tid, nt, pre);
     for (uint32_t i = tid; i < count; i += nt) {
-        const uint64_t r = __ldg(reinterpret_cast<const unsigned long long *>(h + i));
+        const uint64_t r = i == tid ? cur.r0
+                           : i == tid + nt ? cur.r1
+                                           : __ldg(reinterpret_cast<const unsigned long long *>(h + i));
         const uint32_t ra = (uint32_t)r & kRowMask, rb = (uint32_t)(r >> 24) & kRowMask;
         const uint32_t bits = (uint32_t)(r >> 48) & 15u, s9 = (uint32_t)(r >> 52) & 511u;
         const uint32_t blk = s9 >> 7, shot = s9 & 127u;
@@ -758,6 +693,115 @@ __device__ __forceinline__ FrameState frame_state(const KernelArgs &p, uint4 *sm
     return st;
 }
 
+// ------------------------------------------------------------------------------------------------
+// Compact unit lists (DevOp.g).  A thread owns the items i = tid + j * nt (item = unit * B + block) and
+// first loads the list entries of up to J of them together, so an op costs one load latency per thread
+// instead of one (or three, for detectors) per unit.
+// ------------------------------------------------------------------------------------------------
+template <int B, int J, bool HALF>
+__device__ __forceinline__ void load_entries(const uint32_t *list, uint32_t items, uint32_t i0, uint32_t nt,
+                                             uint32_t (&w)[J]) {
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+        const uint32_t i = i0 + (uint32_t)j * nt;
+        if (HALF) {
+            w[j] = i < items ? (uint32_t)__ldg(reinterpret_cast<const unsigned short *>(list) + i / B) : 0u;
+        } else {
+            w[j] = i < items ? __ldg(list + i / B) : 0u;
+        }
+    }
+}
+
+// f(unit, block, entry) for every item of this thread.
+template <int B, int J, bool HALF, typename F>
+__device__ __forceinline__ void for_items(const uint32_t *list, uint32_t items, uint32_t tid, uint32_t nt, F f) {
+    for (uint32_t i0 = tid; i0 < items; i0 += (uint32_t)J * nt) {
+        uint32_t w[J];
+        load_entries<B, J, HALF>(list, items, i0, nt, w);
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const uint32_t i = i0 + (uint32_t)j * nt;
+            if (i < items) {
+                f(i / B, i % B, w[j]);
+            }
+        }
+    }
+}
+
+// CX / CZ over a compact pair list, two pairs at a time so that both pairs' loads are in flight together
+// (the pairs of one op touch distinct rows, which the compiler cannot know).
+template <int B>
+__device__ __forceinline__ void cx_cz_compact(const uint32_t *list, bool cz, uint32_t items, uint4 *X, uint4 *Z,
+                                              uint32_t tid, uint32_t nt) {
+    constexpr int J = 8;
+    for (uint32_t i0 = tid; i0 < items; i0 += (uint32_t)J * nt) {
+        uint32_t w[J];
+        load_entries<B, J, false>(list, items, i0, nt, w);
+#pragma unroll
+        for (int j = 0; j < J; j += 2) {
+            const uint32_t ia = i0 + (uint32_t)j * nt, ib = ia + nt;
+            if (ia < items) {
+                const bool two = ib < items;
+                const uint32_t ba = ia % B, bb = ib % B;
+                const uint32_t a1 = (w[j] & 0xFFFFu) * B + ba, a2 = (w[j] >> 16) * B + ba;
+                const uint32_t b1 = (w[j + 1] & 0xFFFFu) * B + bb, b2 = (w[j + 1] >> 16) * B + bb;
+                if (!cz) {
+                    const uint4 az1 = Z[a1], az2 = Z[a2], ax1 = X[a1], ax2 = X[a2];
+                    const uint4 bz1 = Z[b1], bz2 = Z[b2], bx1 = X[b1], bx2 = X[b2];
+                    Z[a1] = x4(az1, az2);
+                    X[a2] = x4(ax2, ax1);
+                    if (two) {
+                        Z[b1] = x4(bz1, bz2);
+                        X[b2] = x4(bx2, bx1);
+                    }
+                } else {
+                    const uint4 az1 = Z[a1], az2 = Z[a2], ax1 = X[a1], ax2 = X[a2];
+                    const uint4 bz1 = Z[b1], bz2 = Z[b2], bx1 = X[b1], bx2 = X[b2];
+                    Z[a1] = x4(az1, ax2);
+                    Z[a2] = x4(az2, ax1);
+                    if (two) {
+                        Z[b1] = x4(bz1, bx2);
+                        Z[b2] = x4(bz2, bx1);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Detectors over a compact lookback list: each reads at most two records; the records of four detectors are
+// loaded before any result is stored.
+template <int B>
+__device__ __forceinline__ void detectors_compact(const uint32_t *list, uint32_t items, const uint4 *R, uint32_t rec,
+                                                  uint32_t L, bool rg, uint4 *out, uint64_t ndet, uint64_t lb0,
+                                                  uint64_t det_base, uint32_t tid, uint32_t nt) {
+    constexpr int J = 4;
+    for (uint32_t i0 = tid; i0 < items; i0 += (uint32_t)J * nt) {
+        uint32_t w[J];
+        load_entries<B, J, false>(list, items, i0, nt, w);
+        uint4 acc[J];
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const uint32_t i = i0 + (uint32_t)j * nt;
+            const uint32_t blk = i % B, k1 = w[j] & 0xFFFFu, k2 = w[j] >> 16;
+            acc[j] = zero4();
+            if (i < items && k1) {
+                acc[j] = ring_ld(R, wrap(rec + L - k1, L) * B + blk, rg);
+            }
+            if (i < items && k2) {
+                acc[j] = x4(acc[j], ring_ld(R, wrap(rec + L - k2, L) * B + blk, rg));
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const uint32_t i = i0 + (uint32_t)j * nt;
+            if (i < items) {
+                out[(lb0 + i % B) * ndet + det_base + i / B] = acc[j];
+            }
+        }
+    }
+}
+
 // Samples slice `slice` (blocks slice*B .. slice*B+B-1 of this launch) of circuit `p` from the start of
 // the circuit to its end, leaving detection events, observables and measurements in global memory.
 template <int B, bool HITS>
@@ -775,7 +819,8 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
     for (uint32_t i = tid; i < nr * B; i += nt) {
         uint32_t r = i / B, blk = i % B;
         X[i] = zero4();
-        Z[i] = u4(gfs_row_bits(p.seed, GFS_P_RESET, 0, __ldg(p.qubit_orig + r), (uint32_t)(gb0 + blk)));
+        Z[i] = p.reset_zero ? zero4()
+                            : u4(gfs_row_bits(p.seed, GFS_P_RESET, 0, __ldg(p.qubit_orig + r), (uint32_t)(gb0 + blk)));
     }
     for (uint32_t i = tid; i < NO * B; i += nt) {
         O[i] = zero4();
@@ -793,6 +838,11 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
     if (HITS && tid == 0) {
         prefetch_occurrence(p, st.occ_off, st.occ_cnt, slice, 0);
         prefetch_occurrence(p, st.occ_off, st.occ_cnt, slice, 1);
+    }
+    HitPre pre;
+    pre.r0 = pre.r1 = 0;
+    if (HITS) {
+        hit_prefetch(p, st.occ_off, st.occ_cnt, slice, 0, tid, nt, pre);
     }
 
     uint32_t rec = 0, occ = 0;
@@ -850,14 +900,28 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
             continue;
         }
         if (HITS && gate && (op.d & kFusedChanMask)) {  // noise before the gate
-            apply_hits<B>(p, st, slice, occ++, OCC_PAULI, X, Z, R, MSK, rec, L, n, tid, nt);
+            apply_hits<B>(p, st, slice, occ++, OCC_PAULI, X, Z, R, MSK, rec, L, n, tid, nt, pre);
             __syncthreads();
         }
 
         // Gate units in bank-friendly order (a second list when the op carries fused noise).
         const uint32_t ga = (op.code & kGateOrderInB) ? op.b : a;
+        const bool compact = (op.code & kCompact) != 0;
+        const bool norand = (op.code & kNoRandomize) != 0;
+        const bool rg = p.ring_global != nullptr;
+        const uint32_t *const glist = pool + op.g;
         switch (code) {
             case OP_1Q:
+                if (compact) {
+                    for_items<B, 4, true>(glist, n * B, tid, nt, [&](uint32_t, uint32_t blk, uint32_t row) {
+                        const uint32_t idx = row * B + blk;
+                        uint4 x = X[idx], z = Z[idx];
+                        rule1(sub, x, z);
+                        X[idx] = x;
+                        Z[idx] = z;
+                    });
+                    break;
+                }
                 for (uint32_t i = tid; i < n * B; i += nt) {
                     uint32_t u = i / B, blk = i % B;
                     uint32_t idx = __ldg(pool + ga + u) * B + blk;
@@ -883,6 +947,22 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
                 break;
 
             case OP_2Q:
+                if (compact) {
+                    if (sub == K2_CX || sub == K2_CZ) {
+                        cx_cz_compact<B>(glist, sub == K2_CZ, n * B, X, Z, tid, nt);
+                        break;
+                    }
+                    for_items<B, 4, false>(glist, n * B, tid, nt, [&](uint32_t, uint32_t blk, uint32_t w) {
+                        const uint32_t i1 = (w & 0xFFFFu) * B + blk, i2 = (w >> 16) * B + blk;
+                        uint4 x1 = X[i1], z1 = Z[i1], x2 = X[i2], z2 = Z[i2];
+                        rule2v(sub, x1, z1, x2, z2);
+                        X[i1] = x1;
+                        Z[i1] = z1;
+                        X[i2] = x2;
+                        Z[i2] = z2;
+                    });
+                    break;
+                }
                 if (sub == K2_CX || sub == K2_CZ) {
                     // Two independent pairs per iteration: both pairs' loads are in flight together.
                     const uint32_t items = n * B;
@@ -932,7 +1012,7 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
                     uint32_t k = __ldg(pool + a + 2 * u);
                     uint32_t rm = __ldg(pool + a + 2 * u + 1);
                     uint32_t idx = (rm & kRowMask) * B + blk;
-                    uint4 v = R[wrap(rec + L - k, L) * B + blk];
+                    uint4 v = ring_ld(R, wrap(rec + L - k, L) * B + blk, rg);
                     if ((rm >> 24) & kFeedbackX) {
                         X[idx] = x4(X[idx], v);
                     }
@@ -943,68 +1023,42 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
                 break;
 
             case OP_MEASURE:
-                for (uint32_t i = tid; i < n * B; i += nt) {
-                    uint32_t u = i / B, blk = i % B;
-                    uint32_t idx = __ldg(pool + a + u) * B + blk;
-                    uint32_t slot = wrap(rec + u, L) * B + blk;
-                    uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, op.b + u, (uint32_t)(gb0 + blk)));
-                    uint4 x = X[idx], z = Z[idx];
-                    switch (sub) {
-                        case KM_M:
-                            R[slot] = x;
-                            Z[idx] = r;
-                            break;
-                        case KM_MX:
-                            R[slot] = z;
-                            X[idx] = r;
-                            break;
-                        case KM_MY:
-                            R[slot] = x4(x, z);
-                            X[idx] = x4(x4(x, z), r);
-                            Z[idx] = r;
-                            break;
-                        case KM_MR:
-                            R[slot] = x;
-                            X[idx] = zero4();
-                            Z[idx] = r;
-                            break;
-                        case KM_MRX:
-                            R[slot] = z;
-                            Z[idx] = zero4();
-                            X[idx] = r;
-                            break;
-                        default:  // KM_MRY
-                            R[slot] = x4(x, z);
-                            Z[idx] = r;
-                            X[idx] = r;
-                            break;
+                if (compact) {
+                    for_items<B, 4, true>(glist, n * B, tid, nt, [&](uint32_t u, uint32_t blk, uint32_t row) {
+                        measure_row(sub, X, Z, R, row * B + blk, wrap(rec + u, L) * B + blk,
+                                    rand_row(p, norand, inst, op.b + u, (uint32_t)(gb0 + blk)), rg);
+                    });
+                } else {
+                    for (uint32_t i = tid; i < n * B; i += nt) {
+                        const uint32_t u = i / B, blk = i % B;
+                        measure_row(sub, X, Z, R, __ldg(pool + a + u) * B + blk, wrap(rec + u, L) * B + blk,
+                                    rand_row(p, norand, inst, op.b + u, (uint32_t)(gb0 + blk)), rg);
                     }
                 }
                 rec = wrap(rec + n, L);
                 break;
 
-            case OP_RESET:
-                for (uint32_t i = tid; i < n * B; i += nt) {
-                    uint32_t u = i / B, blk = i % B;
-                    uint32_t idx = __ldg(pool + a + u) * B + blk;
-                    uint4 r = u4(gfs_row_bits(p.seed, GFS_P_RAND, inst, op.b + u, (uint32_t)(gb0 + blk)));
-                    if (sub == KR_R) {
-                        X[idx] = zero4();
-                        Z[idx] = r;
-                    } else if (sub == KR_RX) {
-                        X[idx] = r;
-                        Z[idx] = zero4();
-                    } else {
-                        X[idx] = r;
-                        Z[idx] = r;
+            case OP_RESET: {
+                auto reset_row = [&](uint32_t u, uint32_t blk, uint32_t row) {
+                    const uint32_t idx = row * B + blk;
+                    const uint4 r = rand_row(p, norand, inst, op.b + u, (uint32_t)(gb0 + blk));
+                    X[idx] = sub == KR_R ? zero4() : r;
+                    Z[idx] = sub == KR_RX ? zero4() : r;
+                };
+                if (compact) {
+                    for_items<B, 4, true>(glist, n * B, tid, nt, reset_row);
+                } else {
+                    for (uint32_t i = tid; i < n * B; i += nt) {
+                        reset_row(i / B, i % B, __ldg(pool + a + i / B));
                     }
                 }
                 break;
+            }
 
             case OP_RECORD_ZERO:
                 for (uint32_t i = tid; i < n * B; i += nt) {
                     uint32_t u = i / B, blk = i % B;
-                    R[wrap(rec + u, L) * B + blk] = zero4();
+                    ring_st(R, wrap(rec + u, L) * B + blk, zero4(), rg);
                 }
                 rec = wrap(rec + n, L);
                 break;
@@ -1013,7 +1067,7 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
             case OP_MNOISE: {
                 if (HITS) {
                     apply_hits<B>(p, st, slice, occ++, code == OP_MNOISE ? OCC_FLIP : OCC_PAULI, X, Z, R, MSK, rec, L, n,
-                                  tid, nt);
+                                  tid, nt, pre);
                     break;
                 }
                 // Standalone noise: one segment per lane; rows may repeat within an instruction, so hits
@@ -1045,7 +1099,7 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
 
             case OP_HERALD: {
                 if (HITS) {
-                    apply_hits<B>(p, st, slice, occ++, OCC_HERALD, X, Z, R, MSK, rec, L, n, tid, nt);
+                    apply_hits<B>(p, st, slice, occ++, OCC_HERALD, X, Z, R, MSK, rec, L, n, tid, nt, pre);
                     break;
                 }
                 const DevChan &ch = p.chans[op.b];
@@ -1074,7 +1128,7 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
                         MSK[blk] = zero4();
                     }
                     __syncthreads();
-                    apply_hits<B>(p, st, slice, occ++, OCC_CORR, X, Z, R, MSK, rec, L, n, tid, nt);
+                    apply_hits<B>(p, st, slice, occ++, OCC_CORR, X, Z, R, MSK, rec, L, n, tid, nt, pre);
                     __syncthreads();
                     for (uint32_t blk = tid; blk < (uint32_t)B; blk += nt) {
                         const uint4 hits = MSK[blk];
@@ -1119,13 +1173,18 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
                 break;
 
             case OP_DETECTORS:
+                if (compact) {
+                    detectors_compact<B>(glist, n * B, R, rec, L, rg, p.det_out, p.ndet, lb0, det_base, tid, nt);
+                    det_base += n;
+                    break;
+                }
                 for (uint32_t i = tid; i < n * B; i += nt) {
                     uint32_t u = i / B, blk = i % B;
                     uint32_t s = __ldg(pool + a + u), e = __ldg(pool + a + u + 1);
                     uint4 acc = zero4();
                     for (uint32_t j = s; j < e; j++) {
                         uint32_t k = __ldg(pool + j);
-                        acc = x4(acc, R[wrap(rec + L - k, L) * B + blk]);
+                        acc = x4(acc, ring_ld(R, wrap(rec + L - k, L) * B + blk, rg));
                     }
                     p.det_out[(lb0 + blk) * p.ndet + det_base + u] = acc;
                 }
@@ -1138,7 +1197,7 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
                     uint32_t t = __ldg(pool + a + u);
                     uint4 v;
                     if (t & kTermRecord) {
-                        v = R[wrap(rec + L - (t & kRowMask), L) * B + blk];
+                        v = ring_ld(R, wrap(rec + L - (t & kRowMask), L) * B + blk, rg);
                     } else {
                         uint32_t idx = (t & kRowMask) * B + blk;
                         v = zero4();
@@ -1156,7 +1215,7 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
             case OP_EMIT:
                 for (uint32_t i = tid; i < n * B; i += nt) {
                     uint32_t u = i / B, blk = i % B;
-                    p.meas_out[(lb0 + blk) * p.nmeas + meas_base + u] = R[wrap(rec + L - n + u, L) * B + blk];
+                    p.meas_out[(lb0 + blk) * p.nmeas + meas_base + u] = ring_ld(R, wrap(rec + L - n + u, L) * B + blk, rg);
                 }
                 meas_base += n;
                 break;
@@ -1169,7 +1228,7 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
         }
         if (HITS && gate && (op.c & kFusedChanMask)) {  // noise after the gate
             __syncthreads();
-            apply_hits<B>(p, st, slice, occ++, OCC_PAULI, X, Z, R, MSK, rec, L, n, tid, nt);
+            apply_hits<B>(p, st, slice, occ++, OCC_PAULI, X, Z, R, MSK, rec, L, n, tid, nt, pre);
         }
         __syncthreads();
         pc++;
@@ -1182,10 +1241,10 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
     __syncthreads();
 }
 
-// Hit-list mode draws no noise in the frame kernel, which leaves room for a fourth resident CTA per SM
-// (64 registers a thread) when shared memory allows it.
+// Register budget: 96 a thread keeps five 128-thread CTAs resident per SM (the usual shared-memory limit
+// at large circuits) without spilling to local memory.
 template <int B, bool HITS>
-__global__ void __launch_bounds__(256, HITS ? 4 : 3) frame_kernel(const KernelArgs p) {
+__global__ void __maxnreg__(96) frame_kernel(const KernelArgs p) {
     extern __shared__ uint4 sm[];
     const FrameState st = frame_state<B>(p, sm);
     for (uint32_t slice = blockIdx.x; slice < p.nslices; slice += gridDim.x) {
@@ -1198,7 +1257,7 @@ __global__ void __launch_bounds__(256, HITS ? 4 : 3) frame_kernel(const KernelAr
 // expensive and cheap circuits balance across the SMs.  A CTA reloads the circuit's descriptor, gap tables
 // and op stream only when its next item belongs to another circuit.
 template <int B, bool HITS>
-__global__ void __launch_bounds__(256, HITS ? 4 : 3) batch_frame_kernel(const BatchArgs b) {
+__global__ void __maxnreg__(96) batch_frame_kernel(const BatchArgs b) {
     extern __shared__ uint4 sm[];
     __shared__ KernelArgs cur;
     __shared__ uint32_t s_item, s_circ;

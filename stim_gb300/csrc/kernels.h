@@ -40,6 +40,7 @@ struct KernelArgs {
     uint64_t slice_cap;      // records per slice region
     uint32_t smem_occ;       // n_occ when the occurrence offsets and the slice's counts are cached in shared
                              // memory, else 0
+    uint32_t reset_zero;     // 1: start every shot's Z frame at zero instead of random (Program::reset_norand)
 };
 
 // Several circuits in one launch (batch_frame_kernel): circuit j owns work items

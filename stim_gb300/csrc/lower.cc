@@ -10,11 +10,14 @@
 
 #include <algorithm>
 #include <cmath>
+#include <functional>
+#include <iterator>
 #include <map>
 #include <stdexcept>
 #include <unordered_map>
 #include <unordered_set>
 
+#include "frame_rules.h"
 #include "gfs_contract.h"
 
 namespace gfs {
@@ -1150,6 +1153,286 @@ struct Lowerer {
         }
     }
 
+    // Appends the compact unit lists (DevOp.g) of the gate, measurement, reset and detector ops: one load per
+    // unit instead of two (pairs) or three dependent ones (detectors), and half the bytes, so a thread can
+    // fetch all of its units' entries at once and a loop body's lists stay in L1.  Only when every row and
+    // lookback fits 16 bits; detectors only when none reads more than two records.
+    void build_compact_lists() {
+        if (prog.num_rows > 0xFFFFu) {
+            return;
+        }
+        for (DevOp &op : prog.ops) {
+            const uint32_t code = op.code & 0xFFu;
+            const uint32_t n = op.n;
+            const uint32_t list = (op.code & kGateOrderInB) ? op.b : op.a;
+            std::vector<uint32_t> words;
+            if (code == OP_2Q) {
+                for (uint32_t u = 0; u < n; u++) {
+                    words.push_back(prog.pool[list + 2 * u] | (prog.pool[list + 2 * u + 1] << 16));
+                }
+            } else if (code == OP_1Q || code == OP_MEASURE || code == OP_RESET) {
+                words.assign((n + 1) / 2, 0u);
+                for (uint32_t u = 0; u < n; u++) {
+                    words[u / 2] |= prog.pool[list + u] << (16 * (u % 2));
+                }
+            } else if (code == OP_DETECTORS) {
+                bool ok = true;
+                for (uint32_t u = 0; u < n && ok; u++) {
+                    const uint32_t s = prog.pool[op.a + u], e = prog.pool[op.a + u + 1];
+                    if (e - s > 2) {
+                        ok = false;
+                        break;
+                    }
+                    uint32_t w = 0;
+                    for (uint32_t j = s; j < e; j++) {
+                        const uint32_t k = prog.pool[j];
+                        if (k == 0 || k > 0xFFFFu) {
+                            ok = false;
+                            break;
+                        }
+                        w |= k << (16 * (j - s));
+                    }
+                    words.push_back(w);
+                }
+                if (!ok) {
+                    continue;
+                }
+            } else {
+                continue;
+            }
+            op.g = (uint32_t)prog.pool.size();
+            op.code |= kCompact;
+            prog.pool.insert(prog.pool.end(), words.begin(), words.end());
+        }
+    }
+
+    // Detection sampling: finds the measurement / reset ops whose randomized rows cannot change any detector
+    // or observable, and marks them kNoRandomize (and the start-of-shot Z randomization, reset_norand).
+    //
+    // Every output is a GF(2)-linear function of the noise bits and of the randomization bits, because the
+    // frame updates are XORs, copies and overwrites.  The pass walks the program backwards (loops unrolled)
+    // keeping, for every row, the sorted sets of outputs that an X or a Z frame bit at that point flips
+    // (the transpose of the forward map), and for every pending measurement result the outputs that read
+    // it.  A randomized row whose set is empty has coefficient zero in every output, so writing zeros
+    // instead of random bits leaves every detection event and observable unchanged for every noise
+    // realisation.  The pass gives up (marks nothing) past a work limit.
+    void analyze_randomization() {
+        using Set = std::vector<uint32_t>;
+        const uint32_t rows = prog.num_rows;
+        std::vector<Set> xs(rows), zs(rows);
+        const uint64_t R = (uint64_t)prog.ring + 1;
+        std::vector<Set> pend(R);
+        std::vector<uint8_t> ok(prog.ops.size(), 1);
+        uint64_t meas = prog.stats.num_measurements, det = prog.stats.num_detectors;
+        const uint32_t D = (uint32_t)prog.stats.num_detectors;
+        uint64_t work = 0;
+        const uint64_t kWorkLimit = 400000000ull;
+        Set tmp;
+        auto sdiff = [&](Set &a, const Set &b) {  // a ^= b
+            if (b.empty()) {
+                return;
+            }
+            tmp.clear();
+            std::set_symmetric_difference(a.begin(), a.end(), b.begin(), b.end(), std::back_inserter(tmp));
+            a.swap(tmp);
+            work += a.size() + b.size();
+        };
+        auto toggle = [&](Set &a, uint32_t id) {
+            auto it = std::lower_bound(a.begin(), a.end(), id);
+            if (it != a.end() && *it == id) {
+                a.erase(it);
+            } else {
+                a.insert(it, id);
+            }
+            work += 1 + a.size() / 8;
+        };
+        // S_before[k] = XOR of S_after[i] over the outputs i of the forward map that input k reaches.
+        auto transpose = [&](uint32_t nv, uint32_t image[4], Set *after[4]) {
+            Set before[4];
+            for (uint32_t k = 0; k < nv; k++) {
+                for (uint32_t i = 0; i < nv; i++) {
+                    if ((image[k] >> i) & 1u) {
+                        sdiff(before[k], *after[i]);
+                    }
+                }
+            }
+            for (uint32_t k = 0; k < nv; k++) {
+                after[k]->swap(before[k]);
+            }
+        };
+        bool failed = false;
+        std::function<void(uint32_t, uint32_t)> walk = [&](uint32_t lo, uint32_t hi) {
+            for (int64_t pc = (int64_t)hi - 1; pc >= (int64_t)lo && !failed; pc--) {
+                if (work > kWorkLimit) {
+                    failed = true;
+                    return;
+                }
+                const DevOp &op = prog.ops[(size_t)pc];
+                const uint32_t code = op.code & 0xFFu, sub = (op.code >> 8) & 0xFFu, n = op.n;
+                const uint32_t list = (op.code & kGateOrderInB) ? op.b : op.a;
+                switch (code) {
+                    case OP_LOOP_END: {
+                        const int64_t lb = pc - (int64_t)n - 1;
+                        const DevOp &b = prog.ops[(size_t)lb];
+                        const uint64_t reps = (uint64_t)b.a | ((uint64_t)b.b << 32);
+                        for (uint64_t r = 0; r < reps && !failed; r++) {
+                            walk((uint32_t)lb + 1, (uint32_t)pc);
+                        }
+                        pc = lb;
+                        break;
+                    }
+                    case OP_1Q:
+                        for (uint32_t u = 0; u < n; u++) {
+                            const uint32_t r = prog.pool[list + u];
+                            uint32_t image[4];
+                            for (uint32_t k = 0; k < 2; k++) {
+                                uint32_t x = k == 0, z = k == 1;
+                                rule1w(sub, x, z);
+                                image[k] = (x & 1u) | ((z & 1u) << 1);
+                            }
+                            Set *after[4] = {&xs[r], &zs[r], nullptr, nullptr};
+                            transpose(2, image, after);
+                        }
+                        break;
+                    case OP_2Q:
+                        for (uint32_t u = 0; u < n; u++) {
+                            const uint32_t r1 = prog.pool[list + 2 * u], r2 = prog.pool[list + 2 * u + 1];
+                            uint32_t image[4];
+                            for (uint32_t k = 0; k < 4; k++) {
+                                uint32_t v[4] = {k == 0, k == 1, k == 2, k == 3};
+                                rule2(sub, v[0], v[1], v[2], v[3]);
+                                image[k] = (v[0] & 1u) | ((v[1] & 1u) << 1) | ((v[2] & 1u) << 2) | ((v[3] & 1u) << 3);
+                            }
+                            Set *after[4] = {&xs[r1], &zs[r1], &xs[r2], &zs[r2]};
+                            transpose(4, image, after);
+                        }
+                        break;
+                    case OP_MEASURE:
+                        for (uint32_t u = 0; u < n; u++) {
+                            const uint32_t r = prog.pool[op.a + u];
+                            Set &P = pend[(meas - n + u) % R];
+                            Set &X = xs[r], &Z = zs[r];
+                            const bool ybasis = sub == KM_MY || sub == KM_MRY;
+                            const bool xbasis = sub == KM_MX || sub == KM_MRX;
+                            if (ybasis) {
+                                Set y = X;
+                                sdiff(y, Z);
+                                ok[(size_t)pc] &= y.empty();
+                            } else {
+                                ok[(size_t)pc] &= (xbasis ? X : Z).empty();
+                            }
+                            switch (sub) {
+                                case KM_M:
+                                    sdiff(X, P);
+                                    Z.clear();
+                                    break;
+                                case KM_MX:
+                                    sdiff(Z, P);
+                                    X.clear();
+                                    break;
+                                case KM_MY:
+                                    sdiff(X, P);
+                                    Z = X;
+                                    break;
+                                case KM_MR:
+                                    X = P;
+                                    Z.clear();
+                                    break;
+                                case KM_MRX:
+                                    Z = P;
+                                    X.clear();
+                                    break;
+                                default:  // KM_MRY
+                                    X = P;
+                                    Z = P;
+                                    break;
+                            }
+                            P.clear();
+                        }
+                        meas -= n;
+                        break;
+                    case OP_RESET:
+                        for (uint32_t u = 0; u < n; u++) {
+                            const uint32_t r = prog.pool[op.a + u];
+                            Set &X = xs[r], &Z = zs[r];
+                            if (sub == KR_RY) {
+                                Set y = X;
+                                sdiff(y, Z);
+                                ok[(size_t)pc] &= y.empty();
+                            } else {
+                                ok[(size_t)pc] &= (sub == KR_RX ? X : Z).empty();
+                            }
+                            X.clear();
+                            Z.clear();
+                        }
+                        break;
+                    case OP_FEEDBACK:
+                        for (uint32_t u = 0; u < n; u++) {
+                            const uint32_t k = prog.pool[op.a + 2 * u], rm = prog.pool[op.a + 2 * u + 1];
+                            const uint32_t r = rm & kRowMask;
+                            Set &P = pend[(meas - k) % R];
+                            if ((rm >> 24) & kFeedbackX) {
+                                sdiff(P, xs[r]);
+                            }
+                            if ((rm >> 24) & kFeedbackZ) {
+                                sdiff(P, zs[r]);
+                            }
+                        }
+                        break;
+                    case OP_RECORD_ZERO:
+                        for (uint32_t u = 0; u < n; u++) {
+                            pend[(meas - n + u) % R].clear();
+                        }
+                        meas -= n;
+                        break;
+                    case OP_DETECTORS:
+                        for (uint32_t u = 0; u < n; u++) {
+                            const uint32_t id = (uint32_t)(det - n + u);
+                            for (uint32_t j = prog.pool[op.a + u]; j < prog.pool[op.a + u + 1]; j++) {
+                                toggle(pend[(meas - prog.pool[j]) % R], id);
+                            }
+                        }
+                        det -= n;
+                        break;
+                    case OP_OBS:
+                        for (uint32_t u = 0; u < n; u++) {
+                            const uint32_t t = prog.pool[op.a + u], id = D + op.b;
+                            if (t & kTermRecord) {
+                                toggle(pend[(meas - (t & kRowMask)) % R], id);
+                            } else {
+                                if (t & kTermX) {
+                                    toggle(zs[t & kRowMask], id);
+                                }
+                                if (t & kTermZ) {
+                                    toggle(xs[t & kRowMask], id);
+                                }
+                            }
+                        }
+                        break;
+                    case OP_EMIT:
+                        failed = true;
+                        break;
+                    default:  // noise, heralds, correlated errors, loop starts, end: no effect on the map
+                        break;
+                }
+            }
+        };
+        walk(0, (uint32_t)prog.ops.size());
+        if (failed || meas != 0 || det != 0) {
+            return;
+        }
+        prog.reset_norand = true;
+        for (uint32_t r = 0; r < rows; r++) {
+            prog.reset_norand &= zs[r].empty();
+        }
+        for (size_t pc = 0; pc < prog.ops.size(); pc++) {
+            const uint32_t code = prog.ops[pc].code & 0xFFu;
+            if ((code == OP_MEASURE || code == OP_RESET) && ok[pc]) {
+                prog.ops[pc].code |= kNoRandomize;
+            }
+        }
+    }
+
     void run() {
         prog.stats = root.stats();
         std::vector<uint8_t> used(prog.stats.num_qubits + 1, 0);
@@ -1181,6 +1464,7 @@ struct Lowerer {
         flush_detectors();
         emit(OP_END, 0, 0, 0);
         bank_order_gates();
+        build_compact_lists();
         count_noise();
         prog.num_detectors = prog.stats.num_detectors;
         prog.num_observables = prog.stats.num_observables;
@@ -1192,6 +1476,9 @@ struct Lowerer {
         prog.ring = (uint32_t)ring;
         if (dets_unrolled != prog.stats.num_detectors) {
             throw std::logic_error("detector count mismatch in lowering");
+        }
+        if (mode == SampleMode::DETECTIONS) {
+            analyze_randomization();
         }
     }
 };

@@ -24,6 +24,9 @@ struct Program {
     uint64_t num_measurements = 0;
     uint32_t max_loop_depth = 0;
     double work = 0;  // estimated cost of one 128-shot block (orders circuits in a batched launch)
+    // Detection sampling: the start-of-shot Z randomization never reaches an output (the kernel may start
+    // every frame at zero); ops with the same property carry kNoRandomize.
+    bool reset_norand = false;
     std::vector<double> chan_p;  // hit probability of each channel
 
     // Noise occurrences (a noise instruction instance, or the noise fused before/after a gate) met by one

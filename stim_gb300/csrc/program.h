@@ -65,13 +65,25 @@ constexpr uint32_t kFusedChanMask = (1u << 20) - 1;
 // ops with fused noise, whose pool[a] list keeps the noise instruction's unit order).
 constexpr uint32_t kGateOrderInB = 1u << 24;
 
+// DevOp.code bit: the op also has a compact unit list at pool[g] (see DevOp.g).
+constexpr uint32_t kCompact = 1u << 25;
+// DevOp.code bit (OP_MEASURE / OP_RESET): the rows this op randomizes never reach a detector or observable,
+// so in detection sampling the kernel may write zeros instead of drawing them (results are unchanged).
+constexpr uint32_t kNoRandomize = 1u << 26;
+
 struct alignas(16) DevOp {
-    uint32_t code;  // OpCode | sub << 8 | kGateOrderInB
+    uint32_t code;  // OpCode | sub << 8 | kGateOrderInB | kCompact | kNoRandomize
     uint32_t n;
     uint32_t a, b, c, d;
     uint64_t inst;  // instance offset of the source instruction within the enclosing loop iteration
+    // Compact unit list (code & kCompact), in the order the gate is applied: OP_2Q one word per pair
+    // (row1 | row2 << 16); OP_1Q / OP_MEASURE / OP_RESET one 16-bit row per unit (halfword 2 * g + u);
+    // OP_DETECTORS one word per detector (lookback1 | lookback2 << 16, 0 = no record).  Used when every row
+    // and lookback fits 16 bits and no detector reads more than two records.
+    uint32_t g;
+    uint32_t pad[3];
 };
-static_assert(sizeof(DevOp) == 32, "DevOp layout");
+static_assert(sizeof(DevOp) == 48, "DevOp layout");
 
 // A noise channel: hit probability p (gap table) plus the Pauli choice thresholds.
 struct alignas(16) DevChan {

@@ -376,6 +376,7 @@ struct gfs_sampler {
         a.tables = (const uint32_t *)d_tables.p;
         a.chans = (const gfs::DevChan *)d_chans.p;
         a.qubit_orig = (const uint32_t *)d_orig.p;
+        a.reset_zero = prog.reset_norand ? 1u : 0u;
         a.nrows = prog.num_rows;
         a.ring = prog.ring;
         a.nobs = (uint32_t)prog.num_observables;
