@@ -562,7 +562,8 @@ __device__ __forceinline__ const uint64_t *occ_records(const KernelArgs &p, cons
 }
 
 // The records this thread applies first from the next occurrence (indices tid and tid + nt), loaded one
-// hit phase ahead so that their latency overlaps the gate phases in between.
+// hit phase ahead so that their latency overlaps the gate phases in between.  Records are read through L2
+// only, so that they do not evict the op lists from L1.
 struct HitPre {
     uint64_t r0, r1;
 };
@@ -575,10 +576,10 @@ __device__ __forceinline__ void hit_prefetch(const KernelArgs &p, const uint32_t
         const uint64_t *r = occ_records(p, occ_off, occ_cnt, slice, occ, &count);
         const unsigned long long *rr = reinterpret_cast<const unsigned long long *>(r);
         if (tid < count) {
-            h.r0 = __ldg(rr + tid);
+            h.r0 = __ldcg(rr + tid);
         }
         if (tid + nt < count) {
-            h.r1 = __ldg(rr + tid + nt);
+            h.r1 = __ldcg(rr + tid + nt);
         }
     }
 }
@@ -620,10 +621,13 @@ __device__ __forceinline__ void apply_hits(const KernelArgs &p, const FrameState
     const uint64_t *h = occ_records(p, st.occ_off, st.occ_cnt, slice, occ, &count);
     const HitPre cur = pre;
     hit_prefetch(p, st.occ_off, st.occ_cnt, slice, occ + 1, tid, nt, pre);
+    if ((tid & ~31u) >= count) {  // no record for this warp (warp-uniform)
+        return;
+    }
     for (uint32_t i = tid; i < count; i += nt) {
         const uint64_t r = i == tid ? cur.r0
                            : i == tid + nt ? cur.r1
-                                           : __ldg(reinterpret_cast<const unsigned long long *>(h + i));
+                                           : __ldcg(reinterpret_cast<const unsigned long long *>(h + i));
         const uint32_t ra = (uint32_t)r & kRowMask, rb = (uint32_t)(r >> 24) & kRowMask;
         const uint32_t bits = (uint32_t)(r >> 48) & 15u, s9 = (uint32_t)(r >> 52) & 511u;
         const uint32_t blk = s9 >> 7, shot = s9 & 127u;
@@ -733,7 +737,7 @@ __device__ __forceinline__ void for_items(const uint32_t *list, uint32_t items, 
 template <int B>
 __device__ __forceinline__ void cx_cz_compact(const uint32_t *list, bool cz, uint32_t items, uint4 *X, uint4 *Z,
                                               uint32_t tid, uint32_t nt) {
-    constexpr int J = 8;
+    constexpr int J = 4;
     for (uint32_t i0 = tid; i0 < items; i0 += (uint32_t)J * nt) {
         uint32_t w[J];
         load_entries<B, J, false>(list, items, i0, nt, w);
@@ -848,6 +852,9 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
     uint32_t rec = 0, occ = 0;
     uint64_t det_base = 0, meas_base = 0, inst_base = 0;
     int depth = 0;
+    // The two outermost REPEAT levels keep their state in registers; deeper ones in local arrays.
+    uint32_t lpc0 = 0, lpc1 = 0;
+    uint64_t left0 = 0, left1 = 0, base0 = 0, base1 = 0, stride0 = 0, stride1 = 0;
     uint32_t loop_pc[kMaxLoopDepth + 1];
     uint64_t loop_left[kMaxLoopDepth + 1], loop_base[kMaxLoopDepth + 1], loop_stride[kMaxLoopDepth + 1];
     uint32_t pc = 0;
@@ -867,22 +874,54 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
                 }
                 break;
             }
-            loop_pc[depth] = pc;
-            loop_left[depth] = (uint64_t)op.a | ((uint64_t)op.b << 32);
-            loop_base[depth] = inst_base;
-            loop_stride[depth] = (uint64_t)op.c | ((uint64_t)op.d << 32);
+            const uint64_t reps = (uint64_t)op.a | ((uint64_t)op.b << 32);
+            const uint64_t stride = (uint64_t)op.c | ((uint64_t)op.d << 32);
+            if (depth == 0) {
+                lpc0 = pc;
+                left0 = reps;
+                base0 = inst_base;
+                stride0 = stride;
+            } else if (depth == 1) {
+                lpc1 = pc;
+                left1 = reps;
+                base1 = inst_base;
+                stride1 = stride;
+            } else {
+                loop_pc[depth] = pc;
+                loop_left[depth] = reps;
+                loop_base[depth] = inst_base;
+                loop_stride[depth] = stride;
+            }
             depth++;
             inst_base = inst;
             pc++;
             continue;
         }
         if (code == OP_LOOP_END) {
-            int d = depth - 1;
-            if (--loop_left[d] > 0) {
-                inst_base += loop_stride[d];
-                pc = loop_pc[d] + 1;
+            const int d = depth - 1;
+            uint64_t left, stride, base;
+            uint32_t lpc;
+            if (d == 0) {
+                left = --left0;
+                stride = stride0;
+                base = base0;
+                lpc = lpc0;
+            } else if (d == 1) {
+                left = --left1;
+                stride = stride1;
+                base = base1;
+                lpc = lpc1;
             } else {
-                inst_base = loop_base[d];
+                left = --loop_left[d];
+                stride = loop_stride[d];
+                base = loop_base[d];
+                lpc = loop_pc[d];
+            }
+            if (left > 0) {
+                inst_base += stride;
+                pc = lpc + 1;
+            } else {
+                inst_base = base;
                 depth = d;
                 pc++;
             }
@@ -1533,6 +1572,9 @@ __global__ void __launch_bounds__(256) transpose_tile_kernel(const TransposeArgs
     const int packed = t.bit_packed;
     const int32_t nbytes = (int32_t)(packed ? (rows + 7) / 8 : rows);
     const uint64_t col = packed ? r0 / 8 : r0;
+    // One warp per shot row.  Destinations 4-byte aligned get one 4-byte word per lane; others (any row
+    // stride, e.g. ceil(detectors / 8) bytes) get bytes, lane q writing byte 32k + q so that every store
+    // instruction covers 32 consecutive bytes: no funnel shifts, no divergent edge handling.
     for (uint32_t s = warp; s < 128; s += 8) {
         const uint64_t shot = blk * 128 + s;
         if (shot >= t.nshots) {
@@ -1540,27 +1582,24 @@ __global__ void __launch_bounds__(256) transpose_tile_kernel(const TransposeArgs
         }
         const uint32_t *row = tile[s];
         uint8_t *dst = t.out + shot * t.out_stride + col;
-        const int32_t m = (int32_t)((uintptr_t)dst & 3);
-        uint32_t *base = reinterpret_cast<uint32_t *>(dst - m);
-        const int32_t nq = (m + nbytes + 3) / 4;
-        for (int32_t q = (int32_t)lane; q < nq; q += 32) {
-            const int32_t b0 = 4 * q - m;  // chunk byte held by byte 0 of aligned word q
-            if (b0 >= 0 && b0 + 4 <= nbytes) {
-                uint32_t val;
-                if (m == 0) {
-                    val = chunk_word(row, q, packed);
-                } else {
-                    val = __funnelshift_r(chunk_word(row, q - 1, packed), chunk_word(row, q, packed), 8 * (4 - m));
-                }
-                base[q] = val;
-            } else {
-                uint8_t *bytes = reinterpret_cast<uint8_t *>(base + q);
-                for (int32_t i = 0; i < 4; i++) {
-                    const int32_t b = b0 + i;
-                    if (b >= 0 && b < nbytes) {
-                        bytes[i] = (uint8_t)(chunk_word(row, b >> 2, packed) >> (8 * (b & 3)));
-                    }
-                }
+        if (((uintptr_t)dst & 3) == 0) {
+            uint32_t *d32 = reinterpret_cast<uint32_t *>(dst);
+            const int32_t full = nbytes / 4;
+            for (int32_t q = (int32_t)lane; q < full; q += 32) {
+                d32[q] = chunk_word(row, q, packed);
+            }
+            if ((int32_t)lane < nbytes - 4 * full) {
+                const int32_t b = 4 * full + (int32_t)lane;
+                dst[b] = (uint8_t)(chunk_word(row, b >> 2, packed) >> (8 * (b & 3)));
+            }
+        } else if (packed) {
+            const uint8_t *rb = reinterpret_cast<const uint8_t *>(row);
+            for (int32_t b = (int32_t)lane; b < nbytes; b += 32) {
+                dst[b] = rb[b];
+            }
+        } else {
+            for (int32_t b = (int32_t)lane; b < nbytes; b += 32) {
+                dst[b] = (uint8_t)((row[b >> 5] >> (b & 31)) & 1u);
             }
         }
     }
