@@ -516,6 +516,17 @@ struct gfs_sampler {
         return std::min<uint64_t>(cb, target);
     }
 
+    // Device->host copy of `rows` rows of `width` bytes on copy_stream: one linear copy when both sides are
+    // contiguous (a strided copy of narrow rows moves them one by one).
+    void copy_rows(uint8_t *dst, uint64_t dpitch, const uint8_t *src, uint64_t spitch, uint64_t width, uint64_t rows,
+                   const char *what) {
+        if (dpitch == width && spitch == width) {
+            ck(cudaMemcpyAsync(dst, src, width * rows, cudaMemcpyDeviceToHost, copy_stream), what);
+        } else {
+            ck(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, rows, cudaMemcpyDeviceToHost, copy_stream), what);
+        }
+    }
+
     // Host destinations.  Chunk k is sampled and transposed on `stream` into slot k % 2 of a device
     // staging buffer; its device->host copy runs on `copy_stream` while chunk k + 1's kernels run.  The
     // copy of chunk k is issued only after chunk k + 1's kernels are queued, because a copy into pageable
@@ -646,8 +657,9 @@ struct gfs_sampler {
         ck(cudaSetDevice(device), "cudaSetDevice");
         reset_timings();
         if (!device_out) {
-            // Staging rows are padded to 32 bytes so the transpose writes whole sectors.
-            const uint64_t ds = pad32(drow), os = pad32(orow);
+            // Staging rows use the caller's stride when its rows are contiguous, so that each chunk leaves in
+            // one linear copy; otherwise they are padded to 32 bytes and copied row by row.
+            const uint64_t ds = dstride == drow ? drow : pad32(drow), os = ostride == orow ? orow : pad32(orow);
             host_pipeline(
                 shots, ds + os,
                 [&](uint64_t, uint64_t cs, uint8_t *buf) {
@@ -655,14 +667,10 @@ struct gfs_sampler {
                 },
                 [&](uint64_t done, uint64_t cs, uint8_t *buf) {
                     if (dets && drow) {
-                        ck(cudaMemcpy2DAsync(dets + done * dstride, dstride, buf, ds, drow, cs,
-                                             cudaMemcpyDeviceToHost, copy_stream),
-                           "copy dets");
+                        copy_rows(dets + done * dstride, dstride, buf, ds, drow, cs, "copy dets");
                     }
                     if (obs && orow) {
-                        ck(cudaMemcpy2DAsync(obs + done * ostride, ostride, buf + cs * ds, os, orow, cs,
-                                             cudaMemcpyDeviceToHost, copy_stream),
-                           "copy obs");
+                        copy_rows(obs + done * ostride, ostride, buf + cs * ds, os, orow, cs, "copy obs");
                     }
                 });
             return;
@@ -725,7 +733,7 @@ struct gfs_sampler {
             ck(cudaMemcpyAsync(ref_bits.p, ref, (M + 7) / 8, cudaMemcpyHostToDevice, stream), "ref upload");
             dref = (const uint8_t *)ref_bits.p;
         }
-        const uint64_t rs = pad32(row);
+        const uint64_t rs = stride == row ? row : pad32(row);
         host_pipeline(
             shots, rs,
             [&](uint64_t, uint64_t cs, uint8_t *buf) {
@@ -733,9 +741,7 @@ struct gfs_sampler {
             },
             [&](uint64_t done, uint64_t cs, uint8_t *buf) {
                 if (row) {
-                    ck(cudaMemcpy2DAsync(out + done * stride, stride, buf, rs, row, cs, cudaMemcpyDeviceToHost,
-                                         copy_stream),
-                       "copy meas");
+                    copy_rows(out + done * stride, stride, buf, rs, row, cs, "copy meas");
                 }
             });
     }
