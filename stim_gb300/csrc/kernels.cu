@@ -392,46 +392,54 @@ __device__ __forceinline__ uint64_t occ_record(const KernelArgs &p, const OccPar
     return hit_record(r1, r2, bits, s9);
 }
 
-// One warp per (slice, occurrence).  Phase 1 is dense: each lane draws the first Philox group of one
-// segment, and the ~60% of segments (at p = 1e-3) whose first draw leaves the segment are done.  Segments
-// with a hit are queued in shared memory with their three unused draws; every 32 queued segments (and
-// at the end) phase 2 gives one to each lane, which continues the walk exactly where gfs_next_hit would
-// (same draws, same order) and writes each hit's record into the occurrence's region of the slice.  No
-// barriers: occurrences and slices are independent streams.
+// One warp draws the hit records of one (slice, occurrence).  Screening rounds are dense: each lane draws
+// the first Philox group of one segment, and the ~60% of segments (at p = 1e-3) whose first draw leaves the
+// segment are done.  Segments with a hit are queued in shared memory with their three unused draws.  Lanes
+// then walk queued segments hit by hit, exactly as gfs_next_hit would (same draws, same order); a lane whose
+// segment ends takes the next queued one at once, and a new screening round runs whenever the queue can no
+// longer refill the warp.  Every step each lane with a pending hit writes one record; the records of a step
+// get consecutive slots (ballot prefix), so the stores coalesce and no atomics are needed.  No barriers:
+// occurrences and slices are independent streams.
 struct NoiseQueued {
     uint32_t item, u, d1, d2, d3;
 };
 
-// Warp `warp` of its CTA draws occurrence w % n_occ of slice w / n_occ of circuit p.
+// One warp draws occurrence k of slice `slice` of circuit p into region[0 .. cap) and returns the number
+// of records (records past `cap` are counted but not written).  `q` is the warp's queue (64 entries).
 template <int B>
-__device__ __forceinline__ void noise_warp(const KernelArgs &p, uint64_t w, uint32_t warp, uint32_t lane,
-                                           NoiseQueued (*queue)[64]) {
-    const uint32_t slice = (uint32_t)(w / p.n_occ), k = (uint32_t)(w % p.n_occ);
+__device__ __forceinline__ uint32_t noise_records(const KernelArgs &p, uint32_t slice, uint32_t k, uint64_t *region,
+                                                  uint32_t cap, uint32_t lane, NoiseQueued *q) {
     const NoiseOcc oc = p.occs[k];
     const DevOp op = p.ops[oc.pc];
     const OccParams o = occ_params(p, op, oc.which, oc.inst);
     const uint64_t gb0 = p.block0 + (uint64_t)slice * B;
-    uint64_t *region = p.hits + (uint64_t)slice * p.slice_cap + oc.off;
     uint32_t count = 0;  // records of this occurrence so far (warp-uniform)
-    if (o.ch->active) {
-        const DevChan &ch = *o.ch;
-        const uint32_t *T = p.tables + ch.table;
-        const bool always = ch.always != 0;
-        const uint32_t nseg = (o.n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
-        const uint32_t items = nseg * B;
-        const uint32_t kseed0 = (uint32_t)p.seed, kseed1 = (uint32_t)(p.seed >> 32);
-        const uint32_t c3base = gfs_c3(o.purpose, o.inst, 0);
-        NoiseQueued *q = queue[warp];
-        uint32_t qn = 0;  // warp-uniform
-        // Phase 2 in lockstep: every round each lane with a pending hit writes one record; the records of a
-        // round get consecutive slots (ballot prefix), so the stores coalesce and no atomics are needed.
-        auto drain = [&](uint32_t take) {
-            const bool live = lane < take;
-            gfs_stream st;
-            int32_t pos = -1, trials = 0;
-            uint32_t u0 = 0, blk = 0;
-            if (live) {
-                const NoiseQueued e = q[qn - take + lane];
+    if (!o.ch->active) {
+        return 0;
+    }
+    const DevChan &ch = *o.ch;
+    const uint32_t *T = p.tables + ch.table;
+    const bool always = ch.always != 0;
+    const uint32_t nseg = (o.n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
+    const uint32_t items = nseg * B;
+    const uint32_t kseed0 = (uint32_t)p.seed, kseed1 = (uint32_t)(p.seed >> 32);
+    const uint32_t c3base = gfs_c3(o.purpose, o.inst, 0);
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t qn = 0;        // queued segments (warp-uniform)
+    uint32_t screened = 0;  // items screened so far (warp-uniform)
+    // This lane's segment walk.
+    bool active = false;
+    gfs_stream st;
+    int32_t pos = -1, trials = 0;
+    uint32_t u0 = 0, blk = 0;
+    for (;;) {
+        // Idle lanes take queued segments (the most recently queued first).
+        const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !active);
+        if (idle && qn) {
+            const uint32_t take = min((uint32_t)__popc(idle), qn);
+            const uint32_t rank = __popc(idle & lt);
+            if (!active && rank < take) {
+                const NoiseQueued e = q[qn - 1 - rank];
                 const uint32_t g = e.item / B;
                 blk = e.item % B;
                 u0 = g * GFS_SEG_UNITS;
@@ -440,7 +448,7 @@ __device__ __forceinline__ void noise_warp(const KernelArgs &p, uint64_t w, uint
                 if (always) {
                     pos = 0;
                 } else {
-                    // Group 0 was drawn in phase 1: u decided the first hit; d1..d3 come next.
+                    // Group 0 was drawn when screening: u decided the first hit; d1..d3 come next.
                     st.group = 1;
                     st.left = 3;
                     st.b0 = e.d1;
@@ -448,59 +456,69 @@ __device__ __forceinline__ void noise_warp(const KernelArgs &p, uint64_t w, uint
                     st.b2 = e.d3;
                     pos = gfs_hit_after_draw(e.u, T, ch.inv_c, -1, trials);
                 }
-            }
-            for (;;) {
-                const bool has = pos >= 0;
-                const uint32_t m = __ballot_sync(0xFFFFFFFFu, has);
-                if (!m) {
-                    break;
-                }
-                if (has) {
-                    const uint64_t r = occ_record(p, o, u0 + ((uint32_t)pos >> 7), blk, (uint32_t)pos & 127u, &st);
-                    const uint32_t at = count + __popc(m & ((1u << lane) - 1u));
-                    if (at < oc.cap) {
-                        region[at] = r;
-                    }
-                    pos = gfs_next_hit(&st, T, ch.inv_c, pos, trials, always);
-                }
-                count += __popc(m);
+                active = pos >= 0;
             }
             qn -= take;
             __syncwarp();
-        };
-        for (uint32_t base = 0; base < items; base += 32) {
-            const uint32_t item = base + lane;
+        }
+        // Screen the next 32 segments when the queue could not refill the whole warp.
+        if (qn < 32 && screened < items) {
+            const uint32_t item = screened + lane;
             bool hit = false;
             uint32_t u = 0, d1 = 0, d2 = 0, d3 = 0;
             if (item < items) {
                 if (always) {
                     hit = true;
                 } else {
-                    const uint32_t g = item / B, blk = item % B;
-                    const uint32_t u0 = g * GFS_SEG_UNITS;
-                    const uint32_t trials = min(GFS_SEG_UNITS, o.n - u0) * GFS_BLOCK_SHOTS;
-                    const gfs_u32x4 r = gfs_philox(kseed0, kseed1, (uint32_t)(gb0 + blk), g, (uint32_t)o.inst, c3base);
+                    const uint32_t g = item / B, b = item % B;
+                    const uint32_t units = min(GFS_SEG_UNITS, o.n - g * GFS_SEG_UNITS);
+                    const gfs_u32x4 r = gfs_philox(kseed0, kseed1, (uint32_t)(gb0 + b), g, (uint32_t)o.inst, c3base);
                     u = r.v[0];
                     d1 = r.v[1];
                     d2 = r.v[2];
                     d3 = r.v[3];
-                    hit = u >= __ldg(T + trials);
+                    hit = u >= __ldg(T + units * GFS_BLOCK_SHOTS);
                 }
             }
             const uint32_t mask = __ballot_sync(0xFFFFFFFFu, hit);
             if (hit) {
-                q[qn + __popc(mask & ((1u << lane) - 1u))] = NoiseQueued{item, u, d1, d2, d3};
+                q[qn + __popc(mask & lt)] = NoiseQueued{item, u, d1, d2, d3};
             }
             qn += __popc(mask);
+            screened += 32;
             __syncwarp();
-            if (qn >= 32) {
-                drain(32);
+            continue;
+        }
+        const uint32_t act = __ballot_sync(0xFFFFFFFFu, active);
+        if (!act) {
+            if (qn == 0 && screened >= items) {
+                break;
             }
+            continue;
         }
-        if (qn) {
-            drain(qn);
+        // One hit per active lane.
+        if (active) {
+            const uint64_t r = occ_record(p, o, u0 + ((uint32_t)pos >> 7), blk, (uint32_t)pos & 127u, &st);
+            const uint32_t at = count + __popc(act & lt);
+            if (at < cap) {
+                region[at] = r;
+            }
+            pos = gfs_next_hit(&st, T, ch.inv_c, pos, trials, always);
+            active = pos >= 0;
         }
+        count += __popc(act);
     }
+    return count;
+}
+
+// Warp `warp` of its CTA draws occurrence w % n_occ of slice w / n_occ of circuit p into the slice's region.
+template <int B>
+__device__ __forceinline__ void noise_warp(const KernelArgs &p, uint64_t w, uint32_t warp, uint32_t lane,
+                                           NoiseQueued (*queue)[64]) {
+    const uint32_t slice = (uint32_t)(w / p.n_occ), k = (uint32_t)(w % p.n_occ);
+    const NoiseOcc oc = p.occs[k];
+    uint32_t count = noise_records<B>(p, slice, k, p.hits + (uint64_t)slice * p.slice_cap + oc.off, oc.cap, lane,
+                                      queue[warp]);
     if (lane == 0) {
         if (count > oc.cap) {
             atomicOr(p.status, 4u);

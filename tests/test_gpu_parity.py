@@ -167,18 +167,20 @@ def test_lookback_errors_match_reference():
         stim_gb300.Circuit("M 0\nCX 0 rec[-1]").compile_detector_sampler()
 
 
+@pytest.mark.parametrize("mode", [0, 1])
 @pytest.mark.parametrize("name", golden_names())
-def test_inline_noise_mode_matches_golden(name):
-    # The default draws noise into hit lists with a separate kernel; mode 0 draws it inside the frame
-    # kernel.  Both must reproduce the reference's goldens.
+def test_every_noise_mode_matches_golden(name, mode):
+    # Mode 1 (the default) draws the hit lists with a separate kernel; mode 0 draws noise inside the frame
+    # program.  Both must reproduce the reference's goldens.
     g = load(name)
     c = stim_gb300.Circuit(str(g["circuit"]))
     s = c.compile_detector_sampler(seed=int(g["seed"]))
-    s.set_noise_mode(0)
+    s.set_noise_mode(mode)
     d, o = s.sample(int(g["shots"]), separate_observables=True, bit_packed=True)
     np.testing.assert_array_equal(d, g["dets"])
     np.testing.assert_array_equal(o, g["obs"])
-    assert s.last_timings()["noise_launches"] == 0
+    if mode == 0:
+        assert s.last_timings()["noise_launches"] == 0
 
 
 @pytest.mark.parametrize("device_out", [False, True])
