@@ -272,6 +272,28 @@ gfs_status gfs_server_wait(gfs_server *s, uint64_t ticket, double timeout_s, int
  * cache misses, longest queue, bits completed, seconds spanned. */
 gfs_status gfs_server_stats(gfs_server *s, double *out12);
 
+/*
+ * Measurements to detection events (replaces CompiledMeasurementsToDetectionEventsConverter,
+ * src/stim/simulators/measurements_to_detection_events.pybind.cc:80-150, behind
+ * Circuit.compile_m2d_converter(*, skip_reference_sample), and measurements_to_detection_events_helper,
+ * measurements_to_detection_events.inl:29-131).  ref_sample = the circuit's reference sample bit-packed
+ * (gfs_circuit_reference_sample), or null for all zeros (skip_reference_sample = True).
+ * stats4 = measurements, detectors, observables, sweep bits.
+ * gfs_m2d_convert: meas = `shots` host rows of ceil(measurements / 8) bit-packed bytes, meas_stride bytes
+ * apart; flags = GFS_BIT_PACKED and at most one of GFS_PREPEND_OBSERVABLES / GFS_APPEND_OBSERVABLES; dets and
+ * obs (either may be null) as in gfs_sample_detections.  Detector k fires when the parity of its measurements
+ * differs from their parity in the reference sample; observables likewise.  sweep (may be null) = host rows
+ * of ceil(sweep bits / 8) bytes: accepted when every bit is zero or the circuit has no sweep-controlled
+ * operation (then they change nothing); otherwise the call fails with GFS_ERR_INVALID_ARGUMENT.
+ */
+typedef struct gfs_m2d gfs_m2d;
+gfs_status gfs_m2d_create(const gfs_circuit *c, const uint8_t *ref_sample, int device, gfs_m2d **out);
+void gfs_m2d_free(gfs_m2d *m);
+gfs_status gfs_m2d_stats(const gfs_m2d *m, uint64_t *stats4);
+gfs_status gfs_m2d_convert(gfs_m2d *m, uint64_t shots, const uint8_t *meas, uint64_t meas_stride,
+                           const uint8_t *sweep, uint64_t sweep_stride, uint32_t flags, uint8_t *dets,
+                           uint64_t dets_stride, uint8_t *obs, uint64_t obs_stride);
+
 #ifdef __cplusplus
 }
 #endif

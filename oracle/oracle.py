@@ -36,6 +36,9 @@ def lib():
             ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t,
         ]
+        L.oracle_m2d.restype = ctypes.c_int
+        L.oracle_m2d.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
+                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
         _lib = L
     return _lib
 
@@ -80,3 +83,20 @@ class OracleCircuit:
         if rc != 0:
             raise ValueError(err.value.decode())
         return d, o, m
+
+    def m2d(self, meas_packed, ref_sample_packed=None):
+        """Detection events and observable flips (bit-packed) of bit-packed measurement rows."""
+        meas = np.ascontiguousarray(meas_packed, dtype=np.uint8)
+        shots = meas.shape[0]
+        d = np.zeros((shots, (self.num_detectors + 7) // 8), dtype=np.uint8)
+        o = np.zeros((shots, (self.num_observables + 7) // 8), dtype=np.uint8)
+        ref = None if ref_sample_packed is None else np.ascontiguousarray(ref_sample_packed, dtype=np.uint8)
+        err = ctypes.create_string_buffer(512)
+
+        def ptr(a):
+            return None if a is None or a.size == 0 else a.ctypes.data_as(ctypes.c_void_p)
+
+        rc = lib().oracle_m2d(self._h, shots, ptr(meas), ptr(ref), ptr(d), ptr(o), err, 512)
+        if rc != 0:
+            raise ValueError(err.value.decode())
+        return d, o

@@ -1913,3 +1913,83 @@ int oracle_sample(const oracle_circuit *c, uint64_t seed, uint64_t first_shot, u
     free(th);
     return rc;
 }
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Measurements to detection events                                                                 */
+/* ------------------------------------------------------------------------------------------------ */
+
+/*
+ * Restates measurements_to_detection_events_helper (src/stim/simulators/measurements_to_detection_events.inl
+ * :29-131) for circuits whose sweep bits are all zero: walking the circuit with REPEAT unrolled, detector d
+ * of a shot is the XOR of the measurement bits its rec targets name, inverted when the same bits of the
+ * reference sample have odd parity; observable k likewise over all of its OBSERVABLE_INCLUDE rec targets
+ * (Pauli targets only read the frame, which stays zero without sweep data).  Bit by bit, one shot at a time.
+ */
+typedef struct om2d {
+    const uint8_t *meas; /* this shot's measurement bits */
+    const uint8_t *ref;  /* reference sample bits, or NULL for zeros */
+    uint8_t *dets, *obs;
+    uint64_t nmeas, ndet;
+    int failed;
+} om2d;
+
+static int obit(const uint8_t *row, uint64_t i) {
+    return (row[i >> 3] >> (i & 7)) & 1;
+}
+
+static void om2d_block(const oracle_circuit *circ, size_t b, om2d *s) {
+    const oblock *blk = &circ->blocks[b];
+    for (size_t i = 0; i < blk->n && !s->failed; i++) {
+        const oinst *op = &blk->ops[i];
+        if (op->gate == GFS_REPEAT) {
+            for (uint64_t r = 0; r < op->reps && !s->failed; r++) {
+                om2d_block(circ, op->block, s);
+            }
+            continue;
+        }
+        if (op->gate == GFS_DETECTOR || op->gate == GFS_OBSERVABLE_INCLUDE) {
+            int v = 0;
+            for (size_t k = 0; k < op->nt; k++) {
+                uint32_t t = op->t[k];
+                if (!(t & GFS_T_RECORD)) {
+                    continue;
+                }
+                uint64_t lb = t & GFS_T_VALUE_MASK;
+                if (lb == 0 || lb > s->nmeas) {
+                    s->failed = 1;
+                    return;
+                }
+                uint64_t m = s->nmeas - lb;
+                v ^= obit(s->meas, m) ^ (s->ref ? obit(s->ref, m) : 0);
+            }
+            if (op->gate == GFS_DETECTOR) {
+                if (v) {
+                    s->dets[s->ndet >> 3] |= (uint8_t)(1u << (s->ndet & 7));
+                }
+                s->ndet++;
+            } else if (v) {
+                uint64_t k = (uint64_t)op->a[0];
+                s->obs[k >> 3] ^= (uint8_t)(1u << (k & 7));
+            }
+            continue;
+        }
+        s->nmeas += count_results(op);
+    }
+}
+
+int oracle_m2d(const oracle_circuit *c, uint64_t shots, const uint8_t *meas, const uint8_t *ref, uint8_t *dets,
+               uint8_t *obs, char *err, size_t err_len) {
+    oerr e = {err, err_len, 0};
+    uint64_t mrow = (c->num_meas + 7) / 8, drow = (c->num_dets + 7) / 8, orow = (c->num_obs + 7) / 8;
+    memset(dets, 0, shots * drow);
+    memset(obs, 0, shots * orow);
+    for (uint64_t s = 0; s < shots; s++) {
+        om2d st = {meas + s * mrow, ref, dets + s * drow, obs + s * orow, 0, 0, 0};
+        om2d_block(c, 0, &st);
+        if (st.failed) {
+            seterr(&e, "lookback before the beginning of time");
+            return -1;
+        }
+    }
+    return 0;
+}

@@ -39,6 +39,14 @@ void oracle_stats(const oracle_circuit *c, uint64_t *out);
 int oracle_sample(const oracle_circuit *c, uint64_t seed, uint64_t first_shot, uint64_t num_shots, int num_threads,
                   uint8_t *dets, uint8_t *obs, uint8_t *meas, char *err, size_t err_len);
 
+/*
+ * Measurements to detection events for circuits without sweep data: meas = `shots` rows of
+ * ceil(measurements / 8) bit-packed bytes, ref = the reference sample (NULL = zeros); dets / obs receive
+ * ceil(n / 8)-byte rows.  Returns 0, or -1 with err filled.
+ */
+int oracle_m2d(const oracle_circuit *c, uint64_t shots, const uint8_t *meas, const uint8_t *ref, uint8_t *dets,
+               uint8_t *obs, char *err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,7 +23,8 @@ import numpy as np
 from . import _native
 from ._native import check, lib
 
-__all__ = ["Circuit", "CompiledDetectorSampler", "CompiledMeasurementSampler", "BatchSampler", "Server", "device_count"]
+__all__ = ["Circuit", "CompiledDetectorSampler", "CompiledMeasurementSampler",
+           "CompiledMeasurementsToDetectionEventsConverter", "BatchSampler", "Server", "device_count"]
 
 
 def device_count() -> int:
@@ -96,6 +97,11 @@ class Circuit:
                         device: int = 0) -> "CompiledMeasurementSampler":
         return CompiledMeasurementSampler(self, skip_reference_sample=skip_reference_sample, seed=seed,
                                           reference_sample=reference_sample, device=device)
+
+    def compile_m2d_converter(self, *, skip_reference_sample: bool = False,
+                              device: int = 0) -> "CompiledMeasurementsToDetectionEventsConverter":
+        return CompiledMeasurementsToDetectionEventsConverter(self, skip_reference_sample=skip_reference_sample,
+                                                              device=device)
 
 
 class _SamplerBase:
@@ -285,6 +291,80 @@ class CompiledMeasurementSampler(_SamplerBase):
                 _ptr(self._ref) if self._ref is not None else None, _ptr(out),
                 out.strides[0] if out.size else max(1, out.shape[1])))
         return out
+
+
+class CompiledMeasurementsToDetectionEventsConverter:
+    """Converts measurement records into detection events and observable flips on the GPU (replaces the
+    reference's CompiledMeasurementsToDetectionEventsConverter, measurements_to_detection_events.pybind.cc).
+    A detector fires when the parity of its measurements differs from their parity in the circuit's
+    reference sample (all zeros with skip_reference_sample=True)."""
+
+    def __init__(self, circuit, *, skip_reference_sample: bool = False, device: int = 0):
+        if not isinstance(circuit, Circuit):
+            circuit = Circuit(str(circuit))
+        self._circuit = circuit
+        ref = None if skip_reference_sample else circuit.reference_sample(bit_packed=True)
+        h = ctypes.c_void_p()
+        check(lib().gfs_m2d_create(circuit._h, _ptr(ref) if ref is not None and ref.size else None, int(device),
+                                   ctypes.byref(h)))
+        self._h = h
+        self._ref = ref
+        s = (ctypes.c_uint64 * 4)()
+        check(lib().gfs_m2d_stats(self._h, s))
+        self.num_measurements, self.num_detectors, self.num_observables, self.num_sweep_bits = [int(v) for v in s]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().gfs_m2d_free(h)
+            self._h = None
+
+    @staticmethod
+    def _packed(a, nbits, what):
+        """Bit-packed uint8 rows (shots, ceil(nbits / 8)) from a bool (shots, nbits) or packed uint8 array."""
+        a = np.asarray(a)
+        if a.ndim != 2:
+            raise ValueError(f"{what} must be a 2d numpy array")
+        if a.dtype == np.bool_:
+            if a.shape[1] != nbits:
+                raise ValueError(f"Expected {what}.shape[1] == {nbits} but got {a.shape[1]}")
+            return np.ascontiguousarray(np.packbits(a, axis=1, bitorder="little"))
+        if a.dtype == np.uint8:
+            if a.shape[1] != (nbits + 7) // 8:
+                raise ValueError(f"Expected bit packed {what}.shape[1] == {(nbits + 7) // 8} but got {a.shape[1]}")
+            return np.ascontiguousarray(a)
+        raise ValueError(f"{what} must be a numpy array of bool or of bit packed uint8")
+
+    def convert(self, *, measurements, sweep_bits=None, separate_observables=None, append_observables=None,
+                bit_packed: bool = False):
+        if separate_observables is None and append_observables is None:
+            raise ValueError("To ignore observable flip data, you must explicitly specify either "
+                             "separate_observables=False or append_observables=False.")
+        separate = bool(separate_observables)
+        append = bool(append_observables)
+        m = self._packed(measurements, self.num_measurements, "measurements")
+        shots = m.shape[0]
+        sw = None
+        if sweep_bits is not None:
+            sw = self._packed(sweep_bits, self.num_sweep_bits, "sweep_bits")
+            if sw.shape[0] != shots:
+                raise ValueError("Need sweep_bits.shape[0] == measurements.shape[0]")
+        D, O = self.num_detectors, self.num_observables
+        nd = D + (O if append else 0)
+        width = (lambda n: (n + 7) // 8) if bit_packed else (lambda n: n)
+        dtype = np.uint8 if bit_packed else np.bool_
+        dets = np.empty((shots, width(nd)), dtype=dtype)
+        obs = np.empty((shots, width(O)), dtype=dtype) if separate else None
+        flags = (_native.APPEND_OBSERVABLES if append else 0) | (_native.BIT_PACKED if bit_packed else 0)
+        if shots:
+            check(lib().gfs_m2d_convert(
+                self._h, shots, _ptr(m) if m.size else None, max(1, m.shape[1]),
+                _ptr(sw) if sw is not None and sw.size else None, max(1, sw.shape[1]) if sw is not None else 0,
+                flags, _ptr(dets) if dets.size else None, max(1, dets.shape[1]),
+                _ptr(obs) if obs is not None and obs.size else None, max(1, obs.shape[1]) if obs is not None else 0))
+        if separate:
+            return dets, obs
+        return dets
 
 
 class BatchSampler:

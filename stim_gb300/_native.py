@@ -76,12 +76,15 @@ def _declare(L):
                               _vp, _u64, _vp, _u64, ctypes.POINTER(_u64)],
         "gfs_server_wait": [_vp, _u64, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)],
         "gfs_server_stats": [_vp, ctypes.POINTER(ctypes.c_double)],
+        "gfs_m2d_create": [_vp, _vp, ctypes.c_int, ctypes.POINTER(_vp)],
+        "gfs_m2d_stats": [_vp, ctypes.POINTER(_u64)],
+        "gfs_m2d_convert": [_vp, _u64, _vp, _u64, _vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64],
     }
     for name, args in sigs.items():
         f = getattr(L, name)
         f.restype = ctypes.c_int
         f.argtypes = args
-    for name in ("gfs_circuit_free", "gfs_sampler_free", "gfs_batch_free", "gfs_server_free"):
+    for name in ("gfs_circuit_free", "gfs_sampler_free", "gfs_batch_free", "gfs_server_free", "gfs_m2d_free"):
         f = getattr(L, name)
         f.restype = None
         f.argtypes = [_vp]

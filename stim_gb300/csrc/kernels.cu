@@ -19,6 +19,7 @@
 // transpose_tile_kernel: turns [block][row] bit-rows into shot-major bytes with 32x32 shuffle-butterfly
 // bit transposes, replacing the reference's bit-by-bit numpy conversion (numpy.pybind.cc:20-63) and
 // simd_bit_table::transpose_into (simd_bit_table.inl:192-208).
+#include <algorithm>
 #include <cstdio>
 
 #include "gfs_contract.h"
@@ -1649,6 +1650,87 @@ cudaError_t launch_transpose(const TransposeArgs &args, cudaStream_t stream) {
         }
     }
     return cudaSuccess;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Measurements to detection events.  rows_from_shots_kernel is the inverse of transpose_tile_kernel: a CTA
+// of 256 threads owns (one 128-shot block, 1024 measurement rows).  Phase 1 stages the 128 shots' 128-byte
+// pieces of their rows in shared memory (lane q reading byte 32k + q, so any row stride and alignment
+// works); phase 2 turns each 32 x 32 bit block around with the shuffle butterfly (lane = shot in, lane =
+// measurement out); phase 3 writes [block][row] uint4 rows with coalesced 16-byte stores.
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) rows_from_shots_kernel(const RowsInArgs a) {
+    __shared__ uint32_t tin[128][kTileWords + 1];  // [shot][word of the 1024-bit piece], padded
+    __shared__ uint32_t tout[kTileRows][5];        // [row][32-shot group], stride 5 words: conflict-free
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint64_t blk = blockIdx.y;
+    const uint64_t r0 = (uint64_t)blockIdx.x * kTileRows;
+    const uint64_t rows = a.nbits - r0 < kTileRows ? a.nbits - r0 : kTileRows;
+    const uint32_t nbytes = (uint32_t)((rows + 7) / 8);
+    for (uint32_t s = warp; s < 128; s += 8) {
+        const uint64_t shot = blk * 128 + s;
+        const uint8_t *src = a.in + shot * a.in_stride + r0 / 8;
+        uint8_t *dst = reinterpret_cast<uint8_t *>(tin[s]);
+        for (uint32_t b = lane; b < 4 * kTileWords; b += 32) {
+            dst[b] = (shot < a.nshots && b < nbytes) ? src[b] : (uint8_t)0;
+        }
+    }
+    __syncthreads();
+    const Transpose32 transpose32(lane);
+    for (uint32_t t = warp; t < 4 * kTileWords; t += 8) {
+        const uint32_t g = t / kTileWords, w = t % kTileWords;
+        tout[32 * w + lane][g] = transpose32(tin[32 * g + lane][w]);
+    }
+    __syncthreads();
+    for (uint32_t r = tid; r < rows; r += 256) {
+        a.out[blk * a.nbits + r0 + r] = make_uint4(tout[r][0], tout[r][1], tout[r][2], tout[r][3]);
+    }
+}
+
+cudaError_t launch_rows_from_shots(const RowsInArgs &args, cudaStream_t stream) {
+    if (args.nbits == 0 || args.nshots == 0) {
+        return cudaSuccess;
+    }
+    const uint64_t tiles = (args.nbits + kTileRows - 1) / kTileRows;
+    const uint64_t nblk = (args.nshots + 127) / 128;
+    if (tiles > 0x7FFFFFFFull || nblk > 65535) {
+        return cudaErrorInvalidValue;
+    }
+    rows_from_shots_kernel<<<dim3((unsigned)tiles, (unsigned)nblk), 256, 0, stream>>>(args);
+    return cudaGetLastError();
+}
+
+// One thread per (block, output row), outputs of a block consecutive so that the block's measurement rows
+// stay in L2 while its outputs are folded.
+__global__ void __launch_bounds__(256) m2d_fold_kernel(const FoldArgs a) {
+    const uint64_t total = a.D + a.O;
+    const uint64_t n = a.nblk * total;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t blk = i / total, o = i % total;
+        const uint4 *rows = a.rows + blk * a.nrows;
+        uint4 acc = zero4();
+        for (uint32_t j = __ldg(a.off + o), e = __ldg(a.off + o + 1); j < e; j++) {
+            acc = x4(acc, rows[__ldg(a.idx + j)]);
+        }
+        if ((__ldg(a.expect + (o >> 3)) >> (o & 7)) & 1u) {
+            acc = make_uint4(~acc.x, ~acc.y, ~acc.z, ~acc.w);
+        }
+        if (o < a.D) {
+            a.dets[blk * a.D + o] = acc;
+        } else {
+            a.obs[blk * a.O + (o - a.D)] = acc;
+        }
+    }
+}
+
+cudaError_t launch_fold(const FoldArgs &args, cudaStream_t stream) {
+    const uint64_t n = args.nblk * (args.D + args.O);
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    const uint64_t grid = std::min<uint64_t>((n + 255) / 256, (uint64_t)1 << 20);
+    m2d_fold_kernel<<<(unsigned)grid, 256, 0, stream>>>(args);
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------------------------------------

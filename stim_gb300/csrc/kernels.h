@@ -97,6 +97,33 @@ struct TransposeArgs {
 };
 cudaError_t launch_transpose(const TransposeArgs &args, cudaStream_t stream);
 
+// Measurements to detection events (CompiledMeasurementsToDetectionEventsConverter).
+// Shot-major bit-packed rows (in_stride bytes apart, nbits bits each) into [local block][nbits] uint4 rows
+// (128 shots per uint4); bits of shots past nshots are zero.
+struct RowsInArgs {
+    const uint8_t *in;
+    uint64_t in_stride;
+    uint64_t nshots;
+    uint64_t nbits;
+    uint4 *out;
+};
+cudaError_t launch_rows_from_shots(const RowsInArgs &args, cudaStream_t stream);
+
+// out row o of block b = XOR of rows[b][idx[j]] for j in [off[o], off[o+1]), inverted when bit o of `expect`
+// is set; outputs [0, D) go to dets[b][.], [D, D + O) to obs[b][.].
+struct FoldArgs {
+    const uint4 *rows;
+    uint64_t nrows;
+    const uint32_t *off;
+    const uint32_t *idx;
+    const uint8_t *expect;
+    uint64_t D, O;
+    uint64_t nblk;
+    uint4 *dets;
+    uint4 *obs;
+};
+cudaError_t launch_fold(const FoldArgs &args, cudaStream_t stream);
+
 // Shared-memory load+store throughput of the current device (bytes per second over all SMs).
 cudaError_t measure_smem_peak(double *bytes_per_s);
 

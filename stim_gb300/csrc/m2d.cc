@@ -1,0 +1,280 @@
+// Measurements to detection events on the GPU: the host side of gfs_m2d_* (include/stim_gb300.h).
+//
+// Replaces CompiledMeasurementsToDetectionEventsConverter (src/stim/simulators/measurements_to_detection_events
+// .pybind.cc:80-150) and its helper (measurements_to_detection_events.inl:29-131).  The reference walks the
+// noiseless circuit once per batch with a frame simulator and XORs each detector's (and observable's)
+// referenced measurement rows, inverting a row when the reference sample's parity of those measurements is
+// 1.  Here the walk happens once, at creation: every output becomes a list of absolute measurement indices
+// plus an expectation bit (the reference sample's parity), uploaded to the device.  A conversion then runs
+// three kernels per chunk of shots: shot-major input bits into 128-shot measurement rows, the XOR fold, and
+// the usual shot-major output transpose.
+//
+// Sweep bits: the reference's frame simulator turns sweep-controlled Paulis into extra flips.  Without sweep
+// data every sweep bit is zero and those flips vanish, which is the case handled here; a circuit with
+// sweep-controlled operations rejects explicit sweep data (gfs_m2d_convert documents this).
+#include "sampler.h"
+
+using namespace gfs_rt;
+
+struct gfs_m2d {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t M = 0, D = 0, O = 0;
+    uint64_t num_sweep_bits = 0;
+    bool sweep_controlled = false;  // the circuit has sweep-controlled operations
+    std::vector<uint32_t> off, idx;
+    std::vector<uint8_t> expect;
+    DevBuf d_off, d_idx, d_expect, in_buf, rows_buf, det_buf, obs_buf, out_buf;
+
+    ~gfs_m2d() {
+        if (stream) {
+            cudaStreamSynchronize(stream);
+            cudaStreamDestroy(stream);
+        }
+    }
+};
+
+namespace {
+
+// Walks `c` with REPEAT blocks unrolled (the reference's for_each_operation, circuit.h:180-193): each
+// DETECTOR and each OBSERVABLE_INCLUDE record target becomes absolute measurement indices.
+struct Lists {
+    std::vector<std::vector<uint32_t>> det;  // per detector
+    std::vector<std::vector<uint32_t>> obs;  // per observable (all its OBSERVABLE_INCLUDE record targets)
+    uint64_t meas = 0;
+    uint64_t sweep_bits = 0;
+    bool sweep_controlled = false;
+};
+
+void walk(const gfs::Circuit &c, Lists &l) {
+    for (const gfs::Instruction &op : c.ops) {
+        if (op.gate == GFS_REPEAT) {
+            for (uint64_t r = 0; r < op.reps; r++) {
+                walk(c.blocks[op.block], l);
+            }
+            continue;
+        }
+        auto absolute = [&](uint32_t t) -> uint32_t {
+            const uint64_t k = t & GFS_T_VALUE_MASK;
+            if (k == 0) {
+                throw std::out_of_range("Lookback must be non-zero.");
+            }
+            if (k > l.meas) {
+                throw std::out_of_range("Referred to a measurement record before the beginning of time.");
+            }
+            return (uint32_t)(l.meas - k);
+        };
+        if (op.gate == GFS_DETECTOR) {
+            std::vector<uint32_t> refs;
+            for (uint32_t t : op.targets) {
+                if (t & GFS_T_RECORD) {
+                    refs.push_back(absolute(t));
+                }
+            }
+            l.det.push_back(std::move(refs));
+            continue;
+        }
+        if (op.gate == GFS_OBSERVABLE_INCLUDE) {
+            const size_t k = (size_t)op.args[0];
+            if (l.obs.size() <= k) {
+                l.obs.resize(k + 1);
+            }
+            for (uint32_t t : op.targets) {
+                if (t & GFS_T_RECORD) {
+                    l.obs[k].push_back(absolute(t));
+                }
+                // Pauli targets read the frame, which without sweep data stays zero in the reference.
+            }
+            continue;
+        }
+        for (uint32_t t : op.targets) {
+            if (t & GFS_T_SWEEP) {
+                l.sweep_controlled = true;
+                l.sweep_bits = std::max<uint64_t>(l.sweep_bits, (uint64_t)(t & GFS_T_VALUE_MASK) + 1);
+            }
+        }
+        l.meas += op.count_results();
+        if (l.meas > 0xFFFFFFFFull) {
+            throw std::invalid_argument("too many measurements for the GPU converter");
+        }
+    }
+}
+
+void create(gfs_m2d *m, const gfs_circuit *c, const uint8_t *ref, int device) {
+    int count = 0;
+    ck(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
+    if (device < 0 || device >= count) {
+        throw std::invalid_argument("no CUDA device " + std::to_string(device));
+    }
+    Lists l;
+    walk(c->circuit, l);
+    m->device = device;
+    m->M = l.meas;
+    m->D = l.det.size();
+    m->O = std::max<uint64_t>(l.obs.size(), c->stats.num_observables);
+    l.obs.resize(m->O);
+    m->num_sweep_bits = l.sweep_bits;
+    m->sweep_controlled = l.sweep_controlled;
+    const uint64_t n = m->D + m->O;
+    m->off.assign(1, 0);
+    m->expect.assign((n + 7) / 8, 0);
+    uint64_t o = 0;
+    for (auto *group : {&l.det, &l.obs}) {
+        for (const std::vector<uint32_t> &refs : *group) {
+            bool parity = false;
+            for (uint32_t i : refs) {
+                m->idx.push_back(i);
+                if (ref) {
+                    parity ^= (ref[i >> 3] >> (i & 7)) & 1;
+                }
+            }
+            if (m->idx.size() > 0xFFFFFFFFull) {
+                throw std::invalid_argument("too many record references for the GPU converter");
+            }
+            m->off.push_back((uint32_t)m->idx.size());
+            if (parity) {
+                m->expect[o >> 3] |= (uint8_t)(1u << (o & 7));
+            }
+            o++;
+        }
+    }
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    ck(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    upload(m->d_off, m->off, device, m->stream);
+    upload(m->d_idx, m->idx, device, m->stream);
+    upload(m->d_expect, m->expect, device, m->stream);
+    ck(cudaStreamSynchronize(m->stream), "upload");
+}
+
+void copy2d(void *dst, uint64_t dpitch, const void *src, uint64_t spitch, uint64_t width, uint64_t rows,
+            cudaMemcpyKind kind, cudaStream_t s, const char *what) {
+    if (!width || !rows) {
+        return;
+    }
+    if (dpitch == width && spitch == width) {
+        ck(cudaMemcpyAsync(dst, src, width * rows, kind, s), what);
+    } else {
+        ck(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, rows, kind, s), what);
+    }
+}
+
+void convert(gfs_m2d *m, uint64_t shots, const uint8_t *meas, uint64_t meas_stride, const uint8_t *sweep,
+             uint64_t sweep_stride, uint32_t flags, uint8_t *dets, uint64_t dstride, uint8_t *obs, uint64_t ostride) {
+    const uint64_t M = m->M, D = m->D, O = m->O;
+    const uint64_t mrow = (M + 7) / 8;
+    if (meas_stride < mrow) {
+        throw std::invalid_argument("measurement row stride too small");
+    }
+    if (sweep && m->sweep_controlled) {
+        bool any = false;
+        const uint64_t srow = (m->num_sweep_bits + 7) / 8;
+        for (uint64_t s = 0; s < shots && !any; s++) {
+            for (uint64_t b = 0; b < srow && !any; b++) {
+                any = sweep[s * sweep_stride + b] != 0;
+            }
+        }
+        if (any) {
+            throw std::invalid_argument(
+                "the GPU converter does not support nonzero sweep bits on circuits with sweep-controlled operations");
+        }
+    }
+    const bool packed = flags & GFS_BIT_PACKED;
+    const uint64_t nd = D + ((flags & GFS_PREPEND_OBSERVABLES) ? O : 0) + ((flags & GFS_APPEND_OBSERVABLES) ? O : 0);
+    const uint64_t drow = packed ? (nd + 7) / 8 : nd;
+    const uint64_t orow = packed ? (O + 7) / 8 : O;
+    if (dets && dstride < drow) {
+        throw std::invalid_argument("dets row stride too small");
+    }
+    if (obs && ostride < orow) {
+        throw std::invalid_argument("obs row stride too small");
+    }
+    ck(cudaSetDevice(m->device), "cudaSetDevice");
+    // Chunks of up to 2^16 shots, fewer when a circuit's rows are large (about 1 GiB of device buffers).
+    const uint64_t per_block = (M + D + O) * 16 + 128 * (mrow + drow + orow);
+    uint64_t cb = std::max<uint64_t>(1, std::min<uint64_t>(512, ((uint64_t)1 << 30) / std::max<uint64_t>(1, per_block)));
+    const uint64_t chunk = cb * 128;
+    m->in_buf.ensure(std::max<uint64_t>(16, chunk * mrow), m->device);
+    m->rows_buf.ensure(std::max<uint64_t>(16, cb * M * 16), m->device);
+    m->det_buf.ensure(std::max<uint64_t>(16, cb * D * 16), m->device);
+    m->obs_buf.ensure(std::max<uint64_t>(16, cb * O * 16), m->device);
+    m->out_buf.ensure(std::max<uint64_t>(16, chunk * (drow + orow)), m->device);
+    uint8_t *dout = (uint8_t *)m->out_buf.p, *oout = dout + chunk * drow;
+    const uint4 *dt = (const uint4 *)m->det_buf.p, *ot = (const uint4 *)m->obs_buf.p;
+    for (uint64_t done = 0; done < shots;) {
+        const uint64_t cs = std::min<uint64_t>(shots - done, chunk);
+        const uint64_t nblk = (cs + 127) / 128;
+        copy2d(m->in_buf.p, mrow, meas + done * meas_stride, meas_stride, mrow, cs, cudaMemcpyHostToDevice, m->stream,
+               "copy measurements");
+        gfs::RowsInArgs ra{(const uint8_t *)m->in_buf.p, mrow, cs, M, (uint4 *)m->rows_buf.p};
+        ck(gfs::launch_rows_from_shots(ra, m->stream), "rows kernel launch");
+        gfs::FoldArgs fa{(const uint4 *)m->rows_buf.p, M, (const uint32_t *)m->d_off.p, (const uint32_t *)m->d_idx.p,
+                         (const uint8_t *)m->d_expect.p, D, O, nblk, (uint4 *)m->det_buf.p, (uint4 *)m->obs_buf.p};
+        if (M == 0) {
+            ck(cudaMemsetAsync(m->rows_buf.p, 0, 16, m->stream), "memset");
+        }
+        ck(gfs::launch_fold(fa, m->stream), "fold kernel launch");
+        auto tr = [&](const uint4 *s0, uint64_t n0, const uint4 *s1, uint64_t n1, uint8_t *out, uint64_t stride) {
+            gfs::TransposeArgs t{};
+            t.src0 = s0;
+            t.n0 = n0;
+            t.src1 = s1;
+            t.n1 = n1;
+            t.nshots = cs;
+            t.out = out;
+            t.out_stride = stride;
+            t.bit_packed = packed ? 1 : 0;
+            ck(gfs::launch_transpose(t, m->stream), "transpose launch");
+        };
+        if (dets && drow) {
+            if ((flags & GFS_PREPEND_OBSERVABLES) && (flags & GFS_APPEND_OBSERVABLES)) {
+                throw std::invalid_argument("prepend and append observables together are not supported");
+            } else if (flags & GFS_PREPEND_OBSERVABLES) {
+                tr(ot, O, dt, D, dout, drow);
+            } else if (flags & GFS_APPEND_OBSERVABLES) {
+                tr(dt, D, ot, O, dout, drow);
+            } else {
+                tr(dt, D, nullptr, 0, dout, drow);
+            }
+            copy2d(dets + done * dstride, dstride, dout, drow, drow, cs, cudaMemcpyDeviceToHost, m->stream, "copy dets");
+        }
+        if (obs && orow) {
+            tr(ot, O, nullptr, 0, oout, orow);
+            copy2d(obs + done * ostride, ostride, oout, orow, orow, cs, cudaMemcpyDeviceToHost, m->stream, "copy obs");
+        }
+        ck(cudaStreamSynchronize(m->stream), "convert");
+        done += cs;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+gfs_status gfs_m2d_create(const gfs_circuit *c, const uint8_t *ref_sample, int device, gfs_m2d **out) {
+    return guarded([&] {
+        auto m = std::make_unique<gfs_m2d>();
+        create(m.get(), c, ref_sample, device);
+        *out = m.release();
+    });
+}
+
+void gfs_m2d_free(gfs_m2d *m) {
+    delete m;
+}
+
+gfs_status gfs_m2d_stats(const gfs_m2d *m, uint64_t *stats4) {
+    return guarded([&] {
+        stats4[0] = m->M;
+        stats4[1] = m->D;
+        stats4[2] = m->O;
+        stats4[3] = m->num_sweep_bits;
+    });
+}
+
+gfs_status gfs_m2d_convert(gfs_m2d *m, uint64_t shots, const uint8_t *meas, uint64_t meas_stride,
+                           const uint8_t *sweep, uint64_t sweep_stride, uint32_t flags, uint8_t *dets,
+                           uint64_t dets_stride, uint8_t *obs, uint64_t obs_stride) {
+    return guarded([&] { convert(m, shots, meas, meas_stride, sweep, sweep_stride, flags, dets, dets_stride, obs, obs_stride); });
+}
+
+}  // extern "C"
