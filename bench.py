@@ -305,6 +305,7 @@ def run_gpu(args):
 
     batched = run_batched(args, local) if args.batched else None
     serving = run_serving(args, local) if args.serve_seconds > 0 else None
+    m2d = run_m2d(args, local, text) if args.m2d_steps > 0 else None
 
     if rank == 0:
         cb_value, cb_s, cb_shots = cpu_baseline(text, D, O, args.cpu_chunk, os.cpu_count() or 1, args.cpu_seconds,
@@ -350,10 +351,43 @@ def run_gpu(args):
             "clocks": clk,
             "batched": batched,
             "serving": serving,
+            "m2d": m2d,
         }
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_m2d(args, local, text):
+    """Measurements to detection events (compile_m2d_converter().convert) on the main workload: the
+    measurement sampler's records of `--shots` shots, converted from host numpy arrays into host numpy
+    arrays (host->device and device->host copies inside the timed region).  Reports detection-event Gbit/s
+    out and measurement Gbit/s in, and checks the result against the detection sampler with the same seed."""
+    import numpy as np
+
+    import stim_gb300
+
+    shots = args.shots
+    c = stim_gb300.Circuit(text)
+    meas = c.compile_sampler(seed=args.seed, device=local).sample(shots, bit_packed=True)
+    conv = c.compile_m2d_converter(device=local)
+    times = []
+    d = o = None
+    for k in range(args.m2d_steps + 1):
+        t0 = time.perf_counter()
+        d, o = conv.convert(measurements=meas, separate_observables=True, append_observables=False,
+                            bit_packed=True)
+        if k:
+            times.append(time.perf_counter() - t0)
+    want_d, want_o = c.compile_detector_sampler(seed=args.seed, device=local).sample(
+        shots, separate_observables=True, bit_packed=True)
+    D, O, M = c.num_detectors, c.num_observables, c.num_measurements
+    ms = 1e3 * statistics.median(times)
+    return {"workload": f"{shots} shots of {M} measurement bits (the measurement sampler's records) -> {D} "
+                        f"detectors + {O} observables, host arrays in and out",
+            "gbits": shots * (D + O) / (ms / 1e3) / 1e9, "meas_gbits_in": shots * M / (ms / 1e3) / 1e9,
+            "ms": ms, "h2d_bytes": int(meas.nbytes), "d2h_bytes": int(d.nbytes + o.nbytes),
+            "equals_detection_sampler": bool(np.array_equal(d, want_d) and np.array_equal(o, want_o))}
 
 
 def run_batched(args, local):
@@ -542,6 +576,7 @@ def main():
     ap.add_argument("--noise-mode", type=int, default=-1, help="-1 automatic, 0 inline, 1 hit lists")
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--batched", type=int, default=1)
+    ap.add_argument("--m2d-steps", type=int, default=2)
     ap.add_argument("--batch-circuits", type=int, default=256)
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
