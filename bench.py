@@ -361,7 +361,7 @@ def run_gpu(args):
 def run_m2d(args, local, text):
     """Measurements to detection events (compile_m2d_converter().convert) on the main workload: the
     measurement sampler's records of `--shots` shots, converted from host numpy arrays into host numpy
-    arrays (host->device and device->host copies inside the timed region).  Reports detection-event Gbit/s
+    arrays reused across calls (host->device and device->host copies inside the timed region).  Reports detection-event Gbit/s
     out and measurement Gbit/s in, and checks the result against the detection sampler with the same seed."""
     import numpy as np
 
@@ -372,11 +372,12 @@ def run_m2d(args, local, text):
     meas = c.compile_sampler(seed=args.seed, device=local).sample(shots, bit_packed=True)
     conv = c.compile_m2d_converter(device=local)
     times = []
-    d = o = None
-    for k in range(args.m2d_steps + 1):
+    d = np.empty((shots, (c.num_detectors + 7) // 8), dtype=np.uint8)
+    o = np.empty((shots, (c.num_observables + 7) // 8), dtype=np.uint8)
+    for k in range(args.m2d_steps + 1):  # the first call touches the reused output arrays' pages
         t0 = time.perf_counter()
         d, o = conv.convert(measurements=meas, separate_observables=True, append_observables=False,
-                            bit_packed=True)
+                            bit_packed=True, dets_out=d, obs_out=o)
         if k:
             times.append(time.perf_counter() - t0)
     want_d, want_o = c.compile_detector_sampler(seed=args.seed, device=local).sample(

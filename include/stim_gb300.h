@@ -294,6 +294,26 @@ gfs_status gfs_m2d_convert(gfs_m2d *m, uint64_t shots, const uint8_t *meas, uint
                            const uint8_t *sweep, uint64_t sweep_stride, uint32_t flags, uint8_t *dets,
                            uint64_t dets_stride, uint8_t *obs, uint64_t obs_stride);
 
+/*
+ * Detector-error-model sampling (replaces DemSampler<W>, src/stim/simulators/dem_sampler.inl:27-77, behind
+ * DetectorErrorModel.compile_sampler(seed=...).sample(shots, bit_packed, return_errors,
+ * recorded_errors_to_replay), src/stim/simulators/dem_sampler.pybind.cc:40-80; the text format is
+ * src/stim/dem/detector_error_model.cc:195-360).
+ * gfs_dem_parse_stats: host only; stats3 = detectors, observables, error mechanisms.
+ * gfs_dem_sample: `shots` rows of detector / observable / error bits (GFS_BIT_PACKED or one byte per bit;
+ * each pointer may be null).  replay = null samples the next shots of the sampler's stream (the position
+ * moves on, as after gfs_sample_detections); otherwise replay holds `shots` bit-packed rows of recorded
+ * errors (ceil(errors / 8) bytes, replay_stride apart) whose symptoms are XORed instead, the stream does not
+ * move, and errs receives the replayed errors.
+ */
+typedef struct gfs_dem gfs_dem;
+gfs_status gfs_dem_parse_stats(const char *text, size_t len, uint64_t *stats3);
+gfs_status gfs_dem_create(const char *text, size_t len, uint64_t seed, int device, gfs_dem **out);
+void gfs_dem_free(gfs_dem *d);
+gfs_status gfs_dem_sample(gfs_dem *d, uint64_t shots, uint32_t flags, uint8_t *dets, uint64_t dets_stride,
+                          uint8_t *obs, uint64_t obs_stride, uint8_t *errs, uint64_t errs_stride,
+                          const uint8_t *replay, uint64_t replay_stride);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,6 +39,13 @@ def lib():
         L.oracle_m2d.restype = ctypes.c_int
         L.oracle_m2d.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
+        L.oracle_dem_parse.restype = ctypes.c_void_p
+        L.oracle_dem_parse.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]
+        L.oracle_dem_free.argtypes = [ctypes.c_void_p]
+        L.oracle_dem_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
+        L.oracle_dem_sample.restype = ctypes.c_int
+        L.oracle_dem_sample.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -100,3 +107,34 @@ class OracleCircuit:
         if rc != 0:
             raise ValueError(err.value.decode())
         return d, o
+
+
+class OracleDem:
+    """A detector error model parsed by the oracle."""
+
+    def __init__(self, text: str):
+        err = ctypes.create_string_buffer(512)
+        self._h = lib().oracle_dem_parse(text.encode(), err, 512)
+        if not self._h:
+            raise ValueError(err.value.decode())
+        s = (ctypes.c_uint64 * 3)()
+        lib().oracle_dem_stats(self._h, s)
+        self.num_detectors, self.num_observables, self.num_errors = [int(v) for v in s]
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().oracle_dem_free(self._h)
+            self._h = None
+
+    def sample(self, shots: int, seed: int = 0, *, first_shot: int = 0, errors: bool = False, replay=None):
+        """(dets, obs, errs) bit-packed; replay = bit-packed recorded errors (then seed is unused)."""
+        d = np.zeros((shots, (self.num_detectors + 7) // 8), dtype=np.uint8)
+        o = np.zeros((shots, (self.num_observables + 7) // 8), dtype=np.uint8)
+        e = np.zeros((shots, (self.num_errors + 7) // 8), dtype=np.uint8) if errors else None
+        r = None if replay is None else np.ascontiguousarray(replay, dtype=np.uint8)
+
+        def ptr(a):
+            return None if a is None or a.size == 0 else a.ctypes.data_as(ctypes.c_void_p)
+
+        lib().oracle_dem_sample(self._h, seed & (2**64 - 1), first_shot, shots, ptr(d), ptr(o), ptr(e), ptr(r))
+        return d, o, e

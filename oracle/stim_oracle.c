@@ -1993,3 +1993,365 @@ int oracle_m2d(const oracle_circuit *c, uint64_t shots, const uint8_t *meas, con
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Detector error models                                                                            */
+/* ------------------------------------------------------------------------------------------------ */
+
+/*
+ * Restates the reference's detector-error-model text format (src/stim/dem/detector_error_model.cc:195-360,
+ * dem_instruction.cc validate) and DemSampler::resample (src/stim/simulators/dem_sampler.inl:51-77): the
+ * error mechanisms are the `error` instructions with repeat blocks unrolled and shift_detectors applied; a
+ * sampled or replayed error XORs its detector and observable targets.  Sampling follows the DEM purpose of
+ * gfs_contract.h (mechanisms grouped by probability in order of first appearance, each group walked like a
+ * noise instruction whose units are its mechanisms).
+ */
+struct oracle_dem {
+    uint64_t nd, no;
+    size_t ne, ecap;
+    double *p;
+    size_t *soff; /* ne + 1 */
+    uint32_t *sym;
+    size_t ns, scap;
+};
+
+typedef struct odp {
+    const char *s;
+    size_t n, k;
+    oerr *e;
+} odp;
+
+static int odp_peek(odp *p) {
+    return p->k < p->n ? (unsigned char)p->s[p->k] : -1;
+}
+
+static void odp_spaces(odp *p) {
+    while (odp_peek(p) == ' ' || odp_peek(p) == '\t' || odp_peek(p) == '\r') {
+        p->k++;
+    }
+}
+
+static uint64_t odp_uint(odp *p) {
+    int c = odp_peek(p);
+    if (c < '0' || c > '9') {
+        seterr(p->e, "Expected a digit");
+        return 0;
+    }
+    uint64_t v = 0;
+    while (odp_peek(p) >= '0' && odp_peek(p) <= '9') {
+        v = v * 10 + (uint64_t)(p->s[p->k++] - '0');
+    }
+    return v;
+}
+
+static void odem_push_sym(oracle_dem *d, uint32_t v) {
+    if (d->ns == d->scap) {
+        d->scap = d->scap ? 2 * d->scap : 64;
+        d->sym = (uint32_t *)realloc(d->sym, d->scap * sizeof(uint32_t));
+    }
+    d->sym[d->ns++] = v;
+}
+
+/* Reads one block's text range [p->k, end of block) once, applying it `reps` times: the text is re-read
+ * for every repetition (a repeat body is short and the models in the tests are small). */
+static void odem_block(odp *p, oracle_dem *d, uint64_t *off, int top);
+
+static void odem_line(odp *p, oracle_dem *d, uint64_t *off) {
+    char name[32];
+    size_t nl = 0;
+    while (1) {
+        int c = odp_peek(p);
+        if ((c >= 'a' && c <= 'z') || (c >= 'A' && c <= 'Z') || (c >= '0' && c <= '9') || c == '_') {
+            if (nl < sizeof(name) - 1) {
+                name[nl++] = (char)(c >= 'A' && c <= 'Z' ? c - 'A' + 'a' : c);
+            }
+            p->k++;
+        } else {
+            break;
+        }
+    }
+    name[nl] = 0;
+    if (odp_peek(p) == '[') { /* tag: ignored */
+        while (odp_peek(p) != -1 && odp_peek(p) != ']') {
+            if (odp_peek(p) == '\\') {
+                p->k++;
+            }
+            p->k++;
+        }
+        p->k++;
+    }
+    double args[16];
+    size_t na = 0;
+    odp_spaces(p);
+    if (odp_peek(p) == '(') {
+        p->k++;
+        while (1) {
+            odp_spaces(p);
+            if (odp_peek(p) == ')') {
+                p->k++;
+                break;
+            }
+            char *end;
+            double v = strtod(p->s + p->k, &end);
+            if (end == p->s + p->k) {
+                seterr(p->e, "bad number");
+                return;
+            }
+            if (na < 16) {
+                args[na++] = v;
+            }
+            p->k = (size_t)(end - p->s);
+            odp_spaces(p);
+            if (odp_peek(p) == ',') {
+                p->k++;
+            }
+        }
+    }
+    if (!strcmp(name, "repeat")) {
+        odp_spaces(p);
+        uint64_t reps = odp_uint(p);
+        odp_spaces(p);
+        if (odp_peek(p) != '{') {
+            seterr(p->e, "Missing '{' at start of repeat block.");
+            return;
+        }
+        p->k++;
+        size_t start = p->k;
+        if (reps == 0) {
+            uint64_t scratch_off = 0;
+            oracle_dem scratch = {0};
+            odem_block(p, &scratch, &scratch_off, 0);
+            free(scratch.p);
+            free(scratch.soff);
+            free(scratch.sym);
+            return;
+        }
+        for (uint64_t r = 0; r < reps && !p->e->failed; r++) {
+            p->k = start;
+            odem_block(p, d, off, 0);
+        }
+        return;
+    }
+    int is_error = !strcmp(name, "error"), is_shift = !strcmp(name, "shift_detectors");
+    int is_det = !strcmp(name, "detector"), is_obs = !strcmp(name, "logical_observable");
+    if (!is_error && !is_shift && !is_det && !is_obs) {
+        seterr(p->e, "Unrecognized instruction name: %s", name);
+        return;
+    }
+    if (is_error) {
+        if (na != 1 || args[0] < 0 || args[0] > 1) {
+            seterr(p->e, "'error' instruction takes one probability");
+            return;
+        }
+        if (d->ne + 1 >= d->ecap) {
+            d->ecap = d->ecap ? 2 * d->ecap : 64;
+            d->p = (double *)realloc(d->p, d->ecap * sizeof(double));
+            d->soff = (size_t *)realloc(d->soff, (d->ecap + 1) * sizeof(size_t));
+        }
+        if (d->ne == 0) {
+            d->soff[0] = 0;
+        }
+        d->p[d->ne] = args[0];
+    }
+    while (!p->e->failed) {
+        odp_spaces(p);
+        int c = odp_peek(p);
+        if (c == -1 || c == '\n' || c == '#' || c == '}') {
+            break;
+        }
+        if (c == '^') {
+            p->k++;
+            continue;
+        }
+        if (c == 'D' || c == 'd' || c == 'L' || c == 'l') {
+            p->k++;
+            uint64_t v = odp_uint(p);
+            if (c == 'D' || c == 'd') {
+                uint64_t id = *off + v;
+                if (id + 1 > d->nd) {
+                    d->nd = id + 1;
+                }
+                if (is_error) {
+                    odem_push_sym(d, (uint32_t)id);
+                }
+            } else {
+                if (v + 1 > d->no) {
+                    d->no = v + 1;
+                }
+                if (is_error) {
+                    odem_push_sym(d, (uint32_t)v | 0x80000000u); /* observables marked; resolved at the end */
+                }
+            }
+            continue;
+        }
+        uint64_t v = odp_uint(p);
+        if (is_shift) {
+            *off += v;
+        }
+    }
+    if (is_error) {
+        d->ne++;
+        d->soff[d->ne] = d->ns;
+    }
+}
+
+static void odem_block(odp *p, oracle_dem *d, uint64_t *off, int top) {
+    while (!p->e->failed) {
+        odp_spaces(p);
+        int c = odp_peek(p);
+        if (c == '#') {
+            while (odp_peek(p) != -1 && odp_peek(p) != '\n') {
+                p->k++;
+            }
+            continue;
+        }
+        if (c == -1) {
+            if (!top) {
+                seterr(p->e, "Unterminated block.");
+            }
+            return;
+        }
+        if (c == '\n') {
+            p->k++;
+            continue;
+        }
+        if (c == '}') {
+            p->k++;
+            if (top) {
+                seterr(p->e, "Uninitiated block.");
+            }
+            return;
+        }
+        odem_line(p, d, off);
+    }
+}
+
+oracle_dem *oracle_dem_parse(const char *text, char *err, size_t err_len) {
+    oerr e = {err, err_len, 0};
+    oracle_dem *d = (oracle_dem *)calloc(1, sizeof(oracle_dem));
+    d->soff = (size_t *)calloc(1, sizeof(size_t));
+    odp p = {text, strlen(text), 0, &e};
+    uint64_t off = 0;
+    odem_block(&p, d, &off, 1);
+    if (e.failed) {
+        oracle_dem_free(d);
+        return NULL;
+    }
+    for (size_t j = 0; j < d->ns; j++) {
+        if (d->sym[j] & 0x80000000u) {
+            d->sym[j] = (uint32_t)(d->nd + (d->sym[j] & 0x7FFFFFFFu));
+        }
+    }
+    return d;
+}
+
+void oracle_dem_free(oracle_dem *d) {
+    if (d) {
+        free(d->p);
+        free(d->soff);
+        free(d->sym);
+        free(d);
+    }
+}
+
+void oracle_dem_stats(const oracle_dem *d, uint64_t *out3) {
+    out3[0] = d->nd;
+    out3[1] = d->no;
+    out3[2] = d->ne;
+}
+
+static void odem_flip(const oracle_dem *d, size_t m, uint64_t s, uint8_t *dets, uint8_t *obs) {
+    uint64_t drow = (d->nd + 7) / 8, orow = (d->no + 7) / 8;
+    for (size_t j = d->soff[m]; j < d->soff[m + 1]; j++) {
+        uint64_t o = d->sym[j];
+        if (o < d->nd) {
+            dets[s * drow + (o >> 3)] ^= (uint8_t)(1u << (o & 7));
+        } else {
+            o -= d->nd;
+            obs[s * orow + (o >> 3)] ^= (uint8_t)(1u << (o & 7));
+        }
+    }
+}
+
+int oracle_dem_sample(const oracle_dem *d, uint64_t seed, uint64_t first_shot, uint64_t shots, uint8_t *dets,
+                      uint8_t *obs, uint8_t *errs, const uint8_t *replay) {
+    uint64_t drow = (d->nd + 7) / 8, orow = (d->no + 7) / 8, erow = (d->ne + 7) / 8;
+    memset(dets, 0, shots * drow);
+    memset(obs, 0, shots * orow);
+    if (errs) {
+        memset(errs, 0, shots * erow);
+    }
+    if (replay) {
+        for (uint64_t s = 0; s < shots; s++) {
+            for (size_t m = 0; m < d->ne; m++) {
+                if ((replay[s * erow + (m >> 3)] >> (m & 7)) & 1) {
+                    odem_flip(d, m, s, dets, obs);
+                }
+            }
+        }
+        if (errs) {
+            memcpy(errs, replay, shots * erow);
+        }
+        return 0;
+    }
+    /* Groups by probability, in order of first appearance. */
+    size_t *group = (size_t *)malloc((d->ne + 1) * sizeof(size_t));
+    double *gp = (double *)malloc((d->ne + 1) * sizeof(double));
+    size_t ng = 0;
+    for (size_t m = 0; m < d->ne; m++) {
+        size_t g = 0;
+        while (g < ng && gp[g] != d->p[m]) {
+            g++;
+        }
+        if (g == ng) {
+            gp[ng++] = d->p[m];
+        }
+        group[m] = g;
+    }
+    uint32_t *table = (uint32_t *)malloc(GFS_TABLE_LEN * sizeof(uint32_t));
+    size_t *members = (size_t *)malloc((d->ne + 1) * sizeof(size_t));
+    for (size_t g = 0; g < ng; g++) {
+        size_t n = 0;
+        for (size_t m = 0; m < d->ne; m++) {
+            if (group[m] == g) {
+                members[n++] = m;
+            }
+        }
+        double p = gp[g];
+        if (!(p > 0)) {
+            continue;
+        }
+        int always = p >= 1;
+        float inv_c = 0;
+        if (!always) {
+            gfs_build_gap_table(p, table);
+            inv_c = gfs_inv_c(p);
+        }
+        uint64_t nblk = (shots + 127) / 128;
+        for (uint64_t b = 0; b < nblk; b++) {
+            uint64_t block = first_shot / 128 + b;
+            for (size_t seg = 0; 4 * seg < n; seg++) {
+                size_t units = n - 4 * seg < 4 ? n - 4 * seg : 4;
+                gfs_stream st;
+                gfs_stream_init(&st, seed, GFS_P_DEM, g, (uint32_t)seg, (uint32_t)block);
+                int32_t pos = -1;
+                while ((pos = gfs_next_hit(&st, table, inv_c, pos, (int32_t)(units * 128), always)) >= 0) {
+                    uint64_t s = b * 128 + ((uint32_t)pos & 127u);
+                    if (s >= shots) {
+                        continue;
+                    }
+                    size_t m = members[4 * seg + ((uint32_t)pos >> 7)];
+                    odem_flip(d, m, s, dets, obs);
+                    if (errs) {
+                        errs[s * erow + (m >> 3)] |= (uint8_t)(1u << (m & 7));
+                    }
+                }
+            }
+        }
+    }
+    free(group);
+    free(gp);
+    free(table);
+    free(members);
+    return 0;
+}

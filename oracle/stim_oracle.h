@@ -47,6 +47,17 @@ int oracle_sample(const oracle_circuit *c, uint64_t seed, uint64_t first_shot, u
 int oracle_m2d(const oracle_circuit *c, uint64_t shots, const uint8_t *meas, const uint8_t *ref, uint8_t *dets,
                uint8_t *obs, char *err, size_t err_len);
 
+/* Detector error models: parse (NULL + err on failure), stats (detectors, observables, errors), and sample
+ * shots [first_shot, first_shot + shots) (first_shot a multiple of 128) under the DEM purpose of the
+ * contract, or replay recorded errors (replay != NULL: ceil(errors / 8)-byte rows).  Outputs are bit-packed
+ * shot-major rows; errs may be NULL. */
+typedef struct oracle_dem oracle_dem;
+oracle_dem *oracle_dem_parse(const char *text, char *err, size_t err_len);
+void oracle_dem_free(oracle_dem *d);
+void oracle_dem_stats(const oracle_dem *d, uint64_t *out3);
+int oracle_dem_sample(const oracle_dem *d, uint64_t seed, uint64_t first_shot, uint64_t shots, uint8_t *dets,
+                      uint8_t *obs, uint8_t *errs, const uint8_t *replay);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,7 +24,8 @@ from . import _native
 from ._native import check, lib
 
 __all__ = ["Circuit", "CompiledDetectorSampler", "CompiledMeasurementSampler",
-           "CompiledMeasurementsToDetectionEventsConverter", "BatchSampler", "Server", "device_count"]
+           "CompiledMeasurementsToDetectionEventsConverter", "DetectorErrorModel", "CompiledDemSampler",
+           "BatchSampler", "Server", "device_count"]
 
 
 def device_count() -> int:
@@ -336,7 +337,10 @@ class CompiledMeasurementsToDetectionEventsConverter:
         raise ValueError(f"{what} must be a numpy array of bool or of bit packed uint8")
 
     def convert(self, *, measurements, sweep_bits=None, separate_observables=None, append_observables=None,
-                bit_packed: bool = False):
+                bit_packed: bool = False, dets_out=None, obs_out=None):
+        """As the reference's convert; dets_out / obs_out (optional, no counterpart in the reference) are
+        caller-owned arrays of the result's shape and dtype, reused across calls to avoid touching fresh
+        pages on every call."""
         if separate_observables is None and append_observables is None:
             raise ValueError("To ignore observable flip data, you must explicitly specify either "
                              "separate_observables=False or append_observables=False.")
@@ -352,9 +356,10 @@ class CompiledMeasurementsToDetectionEventsConverter:
         D, O = self.num_detectors, self.num_observables
         nd = D + (O if append else 0)
         width = (lambda n: (n + 7) // 8) if bit_packed else (lambda n: n)
-        dtype = np.uint8 if bit_packed else np.bool_
-        dets = np.empty((shots, width(nd)), dtype=dtype)
-        obs = np.empty((shots, width(O)), dtype=dtype) if separate else None
+        dets, dets_user = _out_array(dets_out, (shots, width(nd)), bit_packed)
+        obs = obs_user = None
+        if separate:
+            obs, obs_user = _out_array(obs_out, (shots, width(O)), bit_packed)
         flags = (_native.APPEND_OBSERVABLES if append else 0) | (_native.BIT_PACKED if bit_packed else 0)
         if shots:
             check(lib().gfs_m2d_convert(
@@ -362,9 +367,99 @@ class CompiledMeasurementsToDetectionEventsConverter:
                 _ptr(sw) if sw is not None and sw.size else None, max(1, sw.shape[1]) if sw is not None else 0,
                 flags, _ptr(dets) if dets.size else None, max(1, dets.shape[1]),
                 _ptr(obs) if obs is not None and obs.size else None, max(1, obs.shape[1]) if obs is not None else 0))
+        if dets_user is not None:
+            dets_user[...] = dets
+            dets = dets_user
+        if obs_user is not None:
+            obs_user[...] = obs
+            obs = obs_user
         if separate:
             return dets, obs
         return dets
+
+
+class DetectorErrorModel:
+    """A detector error model in the reference's text format (parsed and validated by the library's C++ host
+    code; src/stim/dem/detector_error_model.cc:195-360)."""
+
+    def __init__(self, text: str = ""):
+        if not isinstance(text, str):
+            text = str(text)
+        self._text = text
+        s = (ctypes.c_uint64 * 3)()
+        data = text.encode()
+        check(lib().gfs_dem_parse_stats(data, len(data), s))
+        self.num_detectors, self.num_observables, self.num_errors = [int(v) for v in s]
+
+    def __str__(self):
+        return self._text
+
+    def __repr__(self):
+        return f"stim_gb300.DetectorErrorModel({self._text!r})"
+
+    def compile_sampler(self, *, seed=None, device: int = 0) -> "CompiledDemSampler":
+        return CompiledDemSampler(self, seed=seed, device=device)
+
+
+class CompiledDemSampler:
+    """Samples detection events, observable flips and (optionally) the errors themselves from a detector error
+    model on the GPU (replaces the reference's DemSampler, src/stim/simulators/dem_sampler.pybind.cc:40-80).
+    Draws follow the counter-based contract of csrc/gfs_contract.h (purpose DEM), not the reference's
+    mt19937_64 stream; replayed errors give exactly the reference's symptoms."""
+
+    def __init__(self, dem, *, seed=None, device: int = 0):
+        if not isinstance(dem, DetectorErrorModel):
+            dem = DetectorErrorModel(str(dem))
+        self._dem = dem
+        data = dem._text.encode()
+        h = ctypes.c_void_p()
+        check(lib().gfs_dem_create(data, len(data), _seed_value(seed), int(device), ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().gfs_dem_free(h)
+            self._h = None
+
+    @property
+    def num_detectors(self):
+        return self._dem.num_detectors
+
+    @property
+    def num_observables(self):
+        return self._dem.num_observables
+
+    @property
+    def num_errors(self):
+        return self._dem.num_errors
+
+    def sample(self, shots: int, *, bit_packed: bool = False, return_errors: bool = False,
+               recorded_errors_to_replay=None):
+        shots = int(shots)
+        if shots < 0:
+            raise ValueError("shots must be non-negative")
+        D, O, E = self.num_detectors, self.num_observables, self.num_errors
+        width = (lambda n: (n + 7) // 8) if bit_packed else (lambda n: n)
+        dtype = np.uint8 if bit_packed else np.bool_
+        dets = np.empty((shots, width(D)), dtype=dtype)
+        obs = np.empty((shots, width(O)), dtype=dtype)
+        errs = np.empty((shots, width(E)), dtype=dtype) if return_errors else None
+        replay = None
+        if recorded_errors_to_replay is not None:
+            replay = CompiledMeasurementsToDetectionEventsConverter._packed(recorded_errors_to_replay, E,
+                                                                             "recorded_errors_to_replay")
+            if replay.shape[0] != shots:
+                raise ValueError("recorded_errors_to_replay.shape[0] != shots")
+        if shots:
+            check(lib().gfs_dem_sample(
+                self._h, shots, _native.BIT_PACKED if bit_packed else 0,
+                _ptr(dets) if dets.size else None, max(1, dets.shape[1]),
+                _ptr(obs) if obs.size else None, max(1, obs.shape[1]),
+                _ptr(errs) if errs is not None and errs.size else None, max(1, errs.shape[1]) if errs is not None else 0,
+                _ptr(replay) if replay is not None and replay.size else None,
+                max(1, replay.shape[1]) if replay is not None else 0))
+        return dets, obs, errs
 
 
 class BatchSampler:

@@ -79,12 +79,16 @@ def _declare(L):
         "gfs_m2d_create": [_vp, _vp, ctypes.c_int, ctypes.POINTER(_vp)],
         "gfs_m2d_stats": [_vp, ctypes.POINTER(_u64)],
         "gfs_m2d_convert": [_vp, _u64, _vp, _u64, _vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64],
+        "gfs_dem_parse_stats": [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(_u64)],
+        "gfs_dem_create": [ctypes.c_char_p, ctypes.c_size_t, _u64, ctypes.c_int, ctypes.POINTER(_vp)],
+        "gfs_dem_sample": [_vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64, _vp, _u64, _vp, _u64],
     }
     for name, args in sigs.items():
         f = getattr(L, name)
         f.restype = ctypes.c_int
         f.argtypes = args
-    for name in ("gfs_circuit_free", "gfs_sampler_free", "gfs_batch_free", "gfs_server_free", "gfs_m2d_free"):
+    for name in ("gfs_circuit_free", "gfs_sampler_free", "gfs_batch_free", "gfs_server_free", "gfs_m2d_free",
+                 "gfs_dem_free"):
         f = getattr(L, name)
         f.restype = None
         f.argtypes = [_vp]

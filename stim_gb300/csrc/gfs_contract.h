@@ -30,6 +30,10 @@
  *   RAND    purpose 2: the randomized row of result/target r of instance i = Philox(b, r, i, 2<<28)
  *   NOISE   purpose 3: a sequential stream of 32-bit draws per segment, 4 per Philox call (group 0, 1, ...)
  *   MNOISE  purpose 4: the same for measurement-result flips (M(p), MR(p), MPP(p), ...)
+ *   DEM     purpose 5: detector-error-model sampling.  The error mechanisms (error instructions with REPEAT
+ *           unrolled) are grouped by probability, groups numbered by first appearance and each group's
+ *           mechanisms kept in model order; group j is sampled like a noise instruction of instance j whose
+ *           units are its mechanisms (same segments, same draws).
  *
  *   A segment's hits: pos = -1; repeat { pos += 1 + G(next draw); if pos >= trials: stop; hit(pos);
  *   if the channel picks a Pauli: choice = next draw }.  G(u) = max{k : u < T[k]} with
@@ -61,6 +65,7 @@
 #define GFS_P_RAND 2u
 #define GFS_P_NOISE 3u
 #define GFS_P_MNOISE 4u
+#define GFS_P_DEM 5u
 
 typedef struct gfs_u32x4 {
     uint32_t v[4];

@@ -1734,6 +1734,132 @@ cudaError_t launch_fold(const FoldArgs &args, cudaStream_t stream) {
 }
 
 // ------------------------------------------------------------------------------------------------
+// Detector-error-model sampling.  The same walk as noise_records (screening rounds of 32 segments, queued
+// segments walked by lanes that refill as soon as their walk ends), over a chunk of one probability group's
+// mechanisms; a hit on mechanism m at `shot` XORs the shot's bit into every symptom row of m (global
+// atomics, the rows are per launch and L2-resident) and sets it in m's error row when errors are wanted.
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ void dem_apply(const DemArgs &a, uint64_t blk, uint32_t m, uint32_t shot) {
+    const uint32_t bit = 1u << (shot & 31);
+    for (uint32_t j = __ldg(a.sym_off + m), e = __ldg(a.sym_off + m + 1); j < e; j++) {
+        const uint32_t o = __ldg(a.sym + j);
+        uint4 *row = o < a.D ? a.dets + blk * a.D + o : a.obs + blk * a.O + (o - a.D);
+        atomicXor(reinterpret_cast<uint32_t *>(row) + (shot >> 5), bit);
+    }
+    if (a.errs) {
+        atomicOr(reinterpret_cast<uint32_t *>(a.errs + blk * a.E + m) + (shot >> 5), bit);
+    }
+}
+
+__global__ void __launch_bounds__(256) dem_sample_kernel(const DemArgs a) {
+    __shared__ NoiseQueued queue[8][64];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint64_t w = (uint64_t)blockIdx.x * 8 + warp;
+    if (w >= a.nblk * a.nchunks) {
+        return;
+    }
+    NoiseQueued *q = queue[warp];
+    const uint64_t blk = w / a.nchunks;
+    const uint32_t chunk = (uint32_t)(w % a.nchunks);
+    const uint32_t g = __ldg(a.chunk_group + chunk), cu0 = __ldg(a.chunk_unit0 + chunk);
+    const uint32_t cn = __ldg(a.chunk_units + chunk);
+    const DemGroup G = a.groups[g];
+    const uint32_t *T = a.tables + G.table;
+    const bool always = (G.flags & 2u) != 0;
+    const uint32_t block = (uint32_t)(a.block0 + blk);
+    const uint32_t seg0 = cu0 / GFS_SEG_UNITS;  // chunks start on segment boundaries
+    const uint32_t items = (cn + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
+    const uint32_t kseed0 = (uint32_t)a.seed, kseed1 = (uint32_t)(a.seed >> 32);
+    const uint32_t c3base = gfs_c3(GFS_P_DEM, g, 0);
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t qn = 0, screened = 0;
+    bool active = false;
+    gfs_stream st;
+    int32_t pos = -1, trials = 0;
+    uint32_t ubase = 0;
+    for (;;) {
+        const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !active);
+        if (idle && qn) {
+            const uint32_t take = min((uint32_t)__popc(idle), qn);
+            const uint32_t rank = __popc(idle & lt);
+            if (!active && rank < take) {
+                const NoiseQueued e = q[qn - 1 - rank];
+                const uint32_t sg = seg0 + e.item;
+                ubase = sg * GFS_SEG_UNITS;
+                trials = (int32_t)(min(GFS_SEG_UNITS, G.n - ubase) * GFS_BLOCK_SHOTS);
+                gfs_stream_init(&st, a.seed, GFS_P_DEM, g, sg, block);
+                if (always) {
+                    pos = 0;
+                } else {
+                    st.group = 1;
+                    st.left = 3;
+                    st.b0 = e.d1;
+                    st.b1 = e.d2;
+                    st.b2 = e.d3;
+                    pos = gfs_hit_after_draw(e.u, T, G.inv_c, -1, trials);
+                }
+                active = pos >= 0;
+            }
+            qn -= take;
+            __syncwarp();
+        }
+        if (qn < 32 && screened < items) {
+            const uint32_t item = screened + lane;
+            bool hit = false;
+            uint32_t u = 0, d1 = 0, d2 = 0, d3 = 0;
+            if (item < items) {
+                if (always) {
+                    hit = true;
+                } else {
+                    const uint32_t sg = seg0 + item;
+                    const uint32_t units = min(GFS_SEG_UNITS, G.n - sg * GFS_SEG_UNITS);
+                    const gfs_u32x4 r = gfs_philox(kseed0, kseed1, block, sg, g, c3base);
+                    u = r.v[0];
+                    d1 = r.v[1];
+                    d2 = r.v[2];
+                    d3 = r.v[3];
+                    hit = u >= __ldg(T + units * GFS_BLOCK_SHOTS);
+                }
+            }
+            const uint32_t mask = __ballot_sync(0xFFFFFFFFu, hit);
+            if (hit) {
+                q[qn + __popc(mask & lt)] = NoiseQueued{item, u, d1, d2, d3};
+            }
+            qn += __popc(mask);
+            screened += 32;
+            __syncwarp();
+            continue;
+        }
+        const uint32_t act = __ballot_sync(0xFFFFFFFFu, active);
+        if (!act) {
+            if (qn == 0 && screened >= items) {
+                break;
+            }
+            continue;
+        }
+        if (active) {
+            const uint32_t m = __ldg(a.units + G.first + ubase + ((uint32_t)pos >> 7));
+            dem_apply(a, blk, m, (uint32_t)pos & 127u);
+            pos = gfs_next_hit(&st, T, G.inv_c, pos, trials, always);
+            active = pos >= 0;
+        }
+    }
+}
+
+cudaError_t launch_dem_sample(const DemArgs &args, cudaStream_t stream) {
+    const uint64_t warps = args.nblk * args.nchunks;
+    if (warps == 0) {
+        return cudaSuccess;
+    }
+    const uint64_t blocks = (warps + 7) / 8;
+    if (blocks > 0x7FFFFFFFull) {
+        return cudaErrorInvalidValue;
+    }
+    dem_sample_kernel<<<(unsigned)blocks, 256, 0, stream>>>(args);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------------------
 // Shared-memory throughput probe: every thread streams 128-bit load/XOR/store passes over a 64 KiB
 // shared buffer with conflict-free addressing (consecutive lanes touch consecutive 16-byte words).
 // Reports the bytes moved (loads + stores) per second over all SMs: the denominator of the frame

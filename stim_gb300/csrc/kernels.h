@@ -124,6 +124,39 @@ struct FoldArgs {
 };
 cudaError_t launch_fold(const FoldArgs &args, cudaStream_t stream);
 
+// Detector-error-model sampling (gfs_dem_*).  A probability group of error mechanisms: its mechanisms are
+// units[first .. first + n); gap table at tables[table] (when 0 < p < 1).
+struct DemGroup {
+    uint32_t first;
+    uint32_t n;
+    uint32_t table;
+    uint32_t flags;  // bit 0: p > 0, bit 1: p >= 1
+    float inv_c;
+    uint32_t pad[3];
+};
+
+// One warp per (128-shot block, chunk of up to 1024 mechanisms of one group): the chunk's segments are walked
+// under the contract (purpose GFS_P_DEM, instance = group, segment index within the group) and each error
+// XORs its symptoms into dets[block][.] / obs[block][.] (which the caller zeroes) and, when errs != null,
+// sets its bit in errs[block][mechanism].
+struct DemArgs {
+    const DemGroup *groups;
+    const uint32_t *units;
+    const uint32_t *sym_off;
+    const uint32_t *sym;
+    const uint32_t *tables;
+    const uint32_t *chunk_group;
+    const uint32_t *chunk_unit0;
+    const uint32_t *chunk_units;
+    uint32_t nchunks;
+    uint64_t seed;
+    uint64_t block0;  // stream position of local block 0
+    uint64_t nblk;
+    uint64_t D, O, E;
+    uint4 *dets, *obs, *errs;
+};
+cudaError_t launch_dem_sample(const DemArgs &args, cudaStream_t stream);
+
 // Shared-memory load+store throughput of the current device (bytes per second over all SMs).
 cudaError_t measure_smem_peak(double *bytes_per_s);
 
