@@ -435,15 +435,17 @@ class CompiledDemSampler:
         return self._dem.num_errors
 
     def sample(self, shots: int, *, bit_packed: bool = False, return_errors: bool = False,
-               recorded_errors_to_replay=None):
+               recorded_errors_to_replay=None, dets_out=None, obs_out=None):
+        """As the reference's sample; dets_out / obs_out (optional, no counterpart in the reference) are
+        caller-owned arrays of the result's shape and dtype, reused across calls."""
         shots = int(shots)
         if shots < 0:
             raise ValueError("shots must be non-negative")
         D, O, E = self.num_detectors, self.num_observables, self.num_errors
         width = (lambda n: (n + 7) // 8) if bit_packed else (lambda n: n)
         dtype = np.uint8 if bit_packed else np.bool_
-        dets = np.empty((shots, width(D)), dtype=dtype)
-        obs = np.empty((shots, width(O)), dtype=dtype)
+        dets, dets_user = _out_array(dets_out, (shots, width(D)), bit_packed)
+        obs, obs_user = _out_array(obs_out, (shots, width(O)), bit_packed)
         errs = np.empty((shots, width(E)), dtype=dtype) if return_errors else None
         replay = None
         if recorded_errors_to_replay is not None:
@@ -459,6 +461,12 @@ class CompiledDemSampler:
                 _ptr(errs) if errs is not None and errs.size else None, max(1, errs.shape[1]) if errs is not None else 0,
                 _ptr(replay) if replay is not None and replay.size else None,
                 max(1, replay.shape[1]) if replay is not None else 0))
+        if dets_user is not None:
+            dets_user[...] = dets
+            dets = dets_user
+        if obs_user is not None:
+            obs_user[...] = obs
+            obs = obs_user
         return dets, obs, errs
 
 

@@ -50,6 +50,15 @@ def code_circuit(family: str, distance: int, rounds: int, p: float) -> str:
     return text.replace("(" + TEMPLATE_P + ")", "(" + format_p(p) + ")")
 
 
+def dem_d25_text() -> str:
+    """The reference's `stim analyze_errors` of the d=25, 25-round rotated memory-Z circuit at p = 1e-3
+    (15,600 detectors, 1 observable, 326,897 error mechanisms), written by tests/golden/make_dem.py."""
+    import lzma
+
+    with lzma.open(os.path.join(_ROOT, "tests", "golden", "dem", "surface_rz_d25_r25_p0.001.dem.xz"), "rt") as f:
+        return f.read()
+
+
 def random_clifford_circuit(num_qubits: int, depth: int, seed: int, p_lo: float = 1e-4,
                             p_hi: float = 1e-2) -> str:
     rng = random.Random(seed)

@@ -10,9 +10,12 @@ reference's `stim analyze_errors` of a generated circuit), the model's detector 
 as the reference's `stim sample_dem` reports them (row lengths of its 01 output), recorded errors (seeded
 random bits) with the detection events and observable flips the reference's `stim sample_dem
 --replay_err_in` gives for them, and the per-detector / per-observable counts of 2^18 shots of the
-reference's own sampler (its native RNG) for the statistical agreement tests.
+reference's own sampler (its native RNG) for the statistical agreement tests.  It also writes
+tests/golden/dem/surface_rz_d25_r25_p0.001.dem.xz, the reference's `stim analyze_errors` of the d=25,
+25-round rotated memory-Z circuit at p = 1e-3 (the benchmark's model).
 """
 
+import lzma
 import os
 import subprocess
 import sys
@@ -63,6 +66,9 @@ def read_b8(path, shots, n):
 
 def main():
     os.makedirs(OUT, exist_ok=True)
+    big = analyze(workloads.code_circuit("surface_code:rotated_memory_z", 25, 25, 0.001))
+    with lzma.open(os.path.join(OUT, "surface_rz_d25_r25_p0.001.dem.xz"), "wt", preset=9) as f:
+        f.write(big)
     rng = np.random.default_rng(77)
     for name, text, shots in cases():
         with tempfile.TemporaryDirectory() as td:
