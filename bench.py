@@ -230,7 +230,11 @@ def run_gpu(args):
     circ = stim_gb300.Circuit(text)
     D, O = circ.num_detectors, circ.num_observables
     shots = args.shots
-    sampler = circ.compile_detector_sampler(seed=args.seed + rank, device=local)
+    # One stream sharded by shot range: every rank uses the same seed and samples its own blocks of it
+    # (step k of rank r = global shots [(k * world + r) * shots, ...)); no collective touches the data.
+    sampler = circ.compile_detector_sampler(seed=args.seed, device=local)
+    shots_al = (args.shots + 127) // 128 * 128
+    step_no = [0]
     sampler.set_noise_mode(args.noise_mode)
     if args.shape:
         b, t = [int(x) for x in args.shape.split(",")]
@@ -245,6 +249,8 @@ def run_gpu(args):
     flags = _native.BIT_PACKED
 
     def device_step():
+        sampler.set_stream_position((step_no[0] * world + rank) * shots_al)
+        step_no[0] += 1
         _native.check(L.gfs_sample_detections_device(sampler._h, shots, flags, dets.data_ptr(), drow,
                                                      obs.data_ptr(), orow))
         return sampler.last_timings()

@@ -188,6 +188,13 @@ gfs_status gfs_measure_smem_peak(int device, double *bytes_per_s);
 
 /* Maximum shots per device chunk (bounds HBM use); 0 restores the default. */
 gfs_status gfs_sampler_set_chunk_shots(gfs_sampler *s, uint64_t shots);
+/*
+ * Stream position (the global index of the next shot; a multiple of 128).  Every shot's bits depend only on
+ * (circuit, seed, global shot index), so ranks that set disjoint positions sample disjoint parts of one stream
+ * (sharding by shot range).  No counterpart in the reference, whose sampler always continues one mt19937_64.
+ */
+gfs_status gfs_sampler_set_stream_position(gfs_sampler *s, uint64_t shot);
+gfs_status gfs_sampler_get_stream_position(const gfs_sampler *s, uint64_t *shot);
 
 /*
  * Noise generation: 1 (default, -1 = automatic) draws every noise hit of a chunk in a separate kernel

@@ -23,13 +23,26 @@ import numpy as np
 from . import _native
 from ._native import check, lib
 
-__all__ = ["Circuit", "CompiledDetectorSampler", "CompiledMeasurementSampler",
+__all__ = ["shard_range", "Circuit", "CompiledDetectorSampler", "CompiledMeasurementSampler",
            "CompiledMeasurementsToDetectionEventsConverter", "DetectorErrorModel", "CompiledDemSampler",
            "BatchSampler", "Server", "device_count"]
 
 
 def device_count() -> int:
     return _native.device_count()
+
+
+def shard_range(total_shots: int, rank: int, world: int):
+    """(first_shot, shots) of `rank`'s share when `world` ranks sample `total_shots` shots of one stream: whole
+    128-shot blocks, as even as possible, in rank order.  No collective is needed: every shot's bits depend
+    only on (circuit, seed, global shot index)."""
+    if world < 1 or not 0 <= rank < world or total_shots < 0:
+        raise ValueError("need 0 <= rank < world and total_shots >= 0")
+    blocks = (total_shots + 127) // 128
+    lo = blocks * rank // world
+    hi = blocks * (rank + 1) // world
+    first = lo * 128
+    return first, max(0, min(total_shots, hi * 128) - first)
 
 
 def _seed_value(seed):
@@ -139,6 +152,16 @@ class _SamplerBase:
 
     def set_chunk_shots(self, shots: int):
         check(lib().gfs_sampler_set_chunk_shots(self._h, int(shots)))
+
+    def set_stream_position(self, shot: int):
+        """Global index of the next shot (a multiple of 128): ranks sampling one stream by shot range set
+        disjoint positions (see shard_range)."""
+        check(lib().gfs_sampler_set_stream_position(self._h, int(shot)))
+
+    def stream_position(self) -> int:
+        v = ctypes.c_uint64()
+        check(lib().gfs_sampler_get_stream_position(self._h, ctypes.byref(v)))
+        return v.value
 
     def autotune(self, trial_shots: int = 0) -> float:
         """Times the frame kernel for each candidate launch shape and keeps the fastest (results never

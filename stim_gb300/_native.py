@@ -54,6 +54,8 @@ def _declare(L):
         "gfs_sampler_get_shape": [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                   ctypes.POINTER(ctypes.c_int), ctypes.POINTER(_u64)],
         "gfs_sampler_set_chunk_shots": [_vp, _u64],
+        "gfs_sampler_set_stream_position": [_vp, _u64],
+        "gfs_sampler_get_stream_position": [_vp, ctypes.POINTER(_u64)],
         "gfs_sampler_set_ring_placement": [_vp, ctypes.c_int],
         "gfs_measure_smem_peak": [ctypes.c_int, ctypes.POINTER(ctypes.c_double)],
         "gfs_sampler_autotune": [_vp, _u64, ctypes.POINTER(ctypes.c_double)],

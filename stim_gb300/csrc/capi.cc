@@ -431,6 +431,19 @@ gfs_status gfs_measure_smem_peak(int device, double *bytes_per_s) {
     });
 }
 
+gfs_status gfs_sampler_set_stream_position(gfs_sampler *s, uint64_t shot) {
+    return guarded([&] {
+        if (shot % 128) {
+            throw std::invalid_argument("the stream position must be a multiple of 128 shots");
+        }
+        s->next_block = shot / 128;
+    });
+}
+
+gfs_status gfs_sampler_get_stream_position(const gfs_sampler *s, uint64_t *shot) {
+    return guarded([&] { *shot = s->next_block * 128; });
+}
+
 gfs_status gfs_sampler_set_chunk_shots(gfs_sampler *s, uint64_t shots) {
     return guarded([&] { s->chunk_shots = shots; });
 }
