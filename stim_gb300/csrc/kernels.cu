@@ -405,24 +405,30 @@ struct NoiseQueued {
     uint32_t item, u, d1, d2, d3;
 };
 
-// One warp draws occurrence k of slice `slice` of circuit p into region[0 .. cap) and returns the number
-// of records (records past `cap` are counted but not written).  `q` is the warp's queue (64 entries).
-template <int B>
-__device__ __forceinline__ uint32_t noise_records(const KernelArgs &p, uint32_t slice, uint32_t k, uint64_t *region,
-                                                  uint32_t cap, uint32_t lane, NoiseQueued *q) {
+// One warp draws occurrence k of the SB slices slice0 .. slice0 + nsub - 1 (B blocks each) into their regions
+// of the hit list; count[s] receives the records of slice slice0 + s (records past the region's capacity are
+// counted but not written).  Items are (segment, slice, block), blocks fastest, so a warp screens the same
+// segment of several blocks together; records of one step go to consecutive slots of their own slice's
+// region (per-slice ballot prefixes).  `q` is the warp's queue (64 entries).
+template <int B, int SB>
+__device__ __forceinline__ void noise_records(const KernelArgs &p, uint32_t slice0, uint32_t nsub, uint32_t k,
+                                              uint32_t lane, NoiseQueued *q, uint32_t (&count)[SB]) {
     const NoiseOcc oc = p.occs[k];
     const DevOp op = p.ops[oc.pc];
     const OccParams o = occ_params(p, op, oc.which, oc.inst);
-    const uint64_t gb0 = p.block0 + (uint64_t)slice * B;
-    uint32_t count = 0;  // records of this occurrence so far (warp-uniform)
+#pragma unroll
+    for (int s = 0; s < SB; s++) {
+        count[s] = 0;  // warp-uniform
+    }
     if (!o.ch->active) {
-        return 0;
+        return;
     }
     const DevChan &ch = *o.ch;
     const uint32_t *T = p.tables + ch.table;
     const bool always = ch.always != 0;
     const uint32_t nseg = (o.n + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
-    const uint32_t items = nseg * B;
+    constexpr uint32_t per_seg = (uint32_t)(B * SB);
+    const uint32_t items = nseg * per_seg;
     const uint32_t kseed0 = (uint32_t)p.seed, kseed1 = (uint32_t)(p.seed >> 32);
     const uint32_t c3base = gfs_c3(o.purpose, o.inst, 0);
     const uint32_t lt = (1u << lane) - 1u;
@@ -432,7 +438,7 @@ __device__ __forceinline__ uint32_t noise_records(const KernelArgs &p, uint32_t 
     bool active = false;
     gfs_stream st;
     int32_t pos = -1, trials = 0;
-    uint32_t u0 = 0, blk = 0;
+    uint32_t u0 = 0, blk = 0, sub = 0;
     for (;;) {
         // Idle lanes take queued segments (the most recently queued first).
         const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !active);
@@ -441,11 +447,13 @@ __device__ __forceinline__ uint32_t noise_records(const KernelArgs &p, uint32_t 
             const uint32_t rank = __popc(idle & lt);
             if (!active && rank < take) {
                 const NoiseQueued e = q[qn - 1 - rank];
-                const uint32_t g = e.item / B;
-                blk = e.item % B;
+                const uint32_t g = e.item / per_seg, r = e.item % per_seg;
+                sub = r / B;
+                blk = r % B;
                 u0 = g * GFS_SEG_UNITS;
                 trials = (int32_t)(min(GFS_SEG_UNITS, o.n - u0) * GFS_BLOCK_SHOTS);
-                gfs_stream_init(&st, p.seed, o.purpose, o.inst, g, (uint32_t)(gb0 + blk));
+                gfs_stream_init(&st, p.seed, o.purpose, o.inst, g,
+                                (uint32_t)(p.block0 + (uint64_t)(slice0 + sub) * B + blk));
                 if (always) {
                     pos = 0;
                 } else {
@@ -462,22 +470,23 @@ __device__ __forceinline__ uint32_t noise_records(const KernelArgs &p, uint32_t 
             qn -= take;
             __syncwarp();
         }
-        // Screen the next 32 segments when the queue could not refill the whole warp.
+        // Screen the next 32 items when the queue could not refill the whole warp.
         if (qn < 32 && screened < items) {
             const uint32_t item = screened + lane;
             bool hit = false;
             uint32_t u = 0, d1 = 0, d2 = 0, d3 = 0;
-            if (item < items) {
+            const uint32_t g = item / per_seg, r = item % per_seg;
+            if (item < items && r / B < nsub) {
                 if (always) {
                     hit = true;
                 } else {
-                    const uint32_t g = item / B, b = item % B;
                     const uint32_t units = min(GFS_SEG_UNITS, o.n - g * GFS_SEG_UNITS);
-                    const gfs_u32x4 r = gfs_philox(kseed0, kseed1, (uint32_t)(gb0 + b), g, (uint32_t)o.inst, c3base);
-                    u = r.v[0];
-                    d1 = r.v[1];
-                    d2 = r.v[2];
-                    d3 = r.v[3];
+                    const uint32_t block = (uint32_t)(p.block0 + (uint64_t)(slice0 + r / B) * B + r % B);
+                    const gfs_u32x4 rr = gfs_philox(kseed0, kseed1, block, g, (uint32_t)o.inst, c3base);
+                    u = rr.v[0];
+                    d1 = rr.v[1];
+                    d2 = rr.v[2];
+                    d3 = rr.v[3];
                     hit = u >= __ldg(T + units * GFS_BLOCK_SHOTS);
                 }
             }
@@ -497,45 +506,65 @@ __device__ __forceinline__ uint32_t noise_records(const KernelArgs &p, uint32_t 
             }
             continue;
         }
-        // One hit per active lane.
+        // One hit per active lane, each into its own slice's region.
+        uint32_t at = 0;
+#pragma unroll
+        for (int s = 0; s < SB; s++) {
+            const uint32_t ms = SB == 1 ? act : __ballot_sync(0xFFFFFFFFu, active && sub == (uint32_t)s);
+            if (active && sub == (uint32_t)s) {
+                at = count[s] + __popc(ms & lt);
+            }
+            count[s] += __popc(ms);
+        }
         if (active) {
             const uint64_t r = occ_record(p, o, u0 + ((uint32_t)pos >> 7), blk, (uint32_t)pos & 127u, &st);
-            const uint32_t at = count + __popc(act & lt);
-            if (at < cap) {
-                region[at] = r;
+            if (at < oc.cap) {
+                p.hits[(uint64_t)(slice0 + sub) * p.slice_cap + oc.off + at] = r;
             }
             pos = gfs_next_hit(&st, T, ch.inv_c, pos, trials, always);
             active = pos >= 0;
         }
-        count += __popc(act);
     }
-    return count;
 }
 
-// Warp `warp` of its CTA draws occurrence w % n_occ of slice w / n_occ of circuit p into the slice's region.
-template <int B>
+// Warp w draws occurrence w % n_occ of the SB slices from (w / n_occ) * SB on into their regions.
+template <int B, int SB>
 __device__ __forceinline__ void noise_warp(const KernelArgs &p, uint64_t w, uint32_t warp, uint32_t lane,
                                            NoiseQueued (*queue)[64]) {
-    const uint32_t slice = (uint32_t)(w / p.n_occ), k = (uint32_t)(w % p.n_occ);
-    const NoiseOcc oc = p.occs[k];
-    uint32_t count = noise_records<B>(p, slice, k, p.hits + (uint64_t)slice * p.slice_cap + oc.off, oc.cap, lane,
-                                      queue[warp]);
+    const uint32_t slice0 = (uint32_t)(w / p.n_occ) * SB, k = (uint32_t)(w % p.n_occ);
+    const uint32_t nsub = min((uint32_t)SB, p.nslices - slice0);
+    uint32_t count[SB];
+    noise_records<B, SB>(p, slice0, nsub, k, lane, queue[warp], count);
     if (lane == 0) {
-        if (count > oc.cap) {
-            atomicOr(p.status, 4u);
-            count = 0;
+        const uint32_t cap = p.occs[k].cap;
+#pragma unroll
+        for (int s = 0; s < SB; s++) {
+            if ((uint32_t)s < nsub) {
+                uint32_t c = count[s];
+                if (c > cap) {
+                    atomicOr(p.status, 4u);
+                    c = 0;
+                }
+                p.hit_count[(uint64_t)(slice0 + s) * p.n_occ + k] = c;
+            }
         }
-        p.hit_count[w] = count;
     }
+}
+
+// One-block slices are drawn four per warp (fuller screening rounds, one setup per four slices).
+template <int B>
+__host__ __device__ constexpr int noise_slices_per_warp() {
+    return B == 1 ? 4 : 1;
 }
 
 template <int B>
 __global__ void __launch_bounds__(256) noise_kernel(const KernelArgs p) {
     __shared__ NoiseQueued queue[8][64];
+    constexpr int SB = noise_slices_per_warp<B>();
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint64_t w = (uint64_t)blockIdx.x * 8 + warp;
-    if (w < (uint64_t)p.nslices * p.n_occ) {
-        noise_warp<B>(p, w, warp, lane, queue);
+    if (w < (uint64_t)((p.nslices + SB - 1) / SB) * p.n_occ) {
+        noise_warp<B, SB>(p, w, warp, lane, queue);
     }
 }
 
@@ -558,7 +587,7 @@ __global__ void __launch_bounds__(256) batch_noise_kernel(const BatchArgs b) {
         }
     }
     const KernelArgs &p = b.circuits[lo];
-    noise_warp<B>(p, w - b.warp_prefix[lo], warp, lane, queue);
+    noise_warp<B, 1>(p, w - b.warp_prefix[lo], warp, lane, queue);
 }
 
 // Shared-memory layout of a CTA holding B blocks of 128 shots: X and Z frames [row][block], the
@@ -1392,7 +1421,8 @@ cudaError_t launch_frame_kernel(const KernelArgs &args, const LaunchShape &shape
 
 template <int B>
 static cudaError_t launch_noise_b(const KernelArgs &args, cudaStream_t stream) {
-    const uint64_t warps = (uint64_t)args.nslices * args.n_occ;
+    constexpr int SB = noise_slices_per_warp<B>();
+    const uint64_t warps = (uint64_t)((args.nslices + SB - 1) / SB) * args.n_occ;
     const uint64_t blocks = (warps + 7) / 8;
     if (blocks > 0x7FFFFFFFull) {
         return cudaErrorInvalidValue;
