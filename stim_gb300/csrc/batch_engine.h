@@ -109,7 +109,7 @@ struct BatchEngine {
         size_t smem = 0;
         uint64_t rs = 0;
         for (auto *p : progs) {
-            smem = std::max(smem, p->smem_for(bpc, ring_global, hits));
+            smem = std::max(smem, p->smem_for(bpc, ring_global, hits, false));
             rs = std::max<uint64_t>(rs, (uint64_t)bpc * p->prog.ring);
         }
         gfs::LaunchShape t{bpc, threads, 1, smem, ring_global};
@@ -202,7 +202,7 @@ struct BatchEngine {
             a.seed = e.seed;
             a.block0 = e.block0;
             a.status = (uint32_t *)d_status.p;
-            a.smem_table_words = s->smem_table_words();
+            a.smem_table_words = 0;  // the same shared-memory layout in hit-list mode and its inline fallback
             a.smem_ops = s->smem_ops();
             a.ring_cta_stride = ring_stride_cur;
             if (hits) {

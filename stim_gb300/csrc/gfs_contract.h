@@ -20,7 +20,7 @@
  *                   (adjacent fusable instructions fused exactly as the reference parser does)
  *   unit        a target (1-qubit channels), a target pair (2-qubit channels), a measurement
  *               result (noisy measurements, heralds), or the single unit of E/ELSE_CORRELATED_ERROR
- *   segment     units [4g, 4g+4) x the 128 shots of a block; trial tau = (u - 4g) * 128 + shot
+ *   segment     units [16g, 16g+16) x the 128 shots of a block; trial tau = (u - 16g) * 128 + shot
  *
  *   Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",
  *   SC'11) with key (lo32(seed), hi32(seed)) and counter
@@ -39,8 +39,9 @@
  *   if the channel picks a Pauli: choice = next draw }.  G(u) = max{k : u < T[k]} with
  *   T[k] = floor((1-p)^k * 2^32) computed in 64-bit fixed point, so P(G >= k) = (1-p)^k.
  *   p == 0 draws nothing and hits nothing; p >= 1 hits every trial without gap draws.
- *   A segment is exactly the four units one GPU lane updates, so at small p one Philox call per lane
- *   and segment usually decides everything.
+ *   A segment is the sixteen units one GPU lane walks: at small p one Philox call per lane and segment
+ *   usually decides everything, and sixteen units (2,048 trials) keep the screening calls few while a
+ *   segment rarely holds more than a few hits.
  */
 #ifndef GFS_CONTRACT_H
 #define GFS_CONTRACT_H
@@ -57,7 +58,7 @@
 #endif
 
 #define GFS_BLOCK_SHOTS 128u
-#define GFS_SEG_UNITS 4u
+#define GFS_SEG_UNITS 16u
 #define GFS_SEG_TRIALS (GFS_BLOCK_SHOTS * GFS_SEG_UNITS)
 #define GFS_TABLE_LEN (GFS_SEG_TRIALS + 1u) /* T[0..512] */
 

@@ -8,7 +8,7 @@
 // __syncthreads().  The lowering orders each gate op's units so that a quarter-warp's eight 16-byte
 // accesses fall in distinct bank groups.  Noise follows the counter-based stream of gfs_contract.h: with
 // HITS, noise_kernel has already drawn every hit into per-occurrence record lists and the frame kernel only
-// XORs them in; without, a thread owns a segment of 4 units x 128 shots and skips geometrically to its hits
+// XORs them in; without, a thread owns a segment of 16 units x 128 shots and skips geometrically to its hits
 // (noise next to a gate on the same targets is fused into the gate op).  Detection events stream to
 // global memory as [block][detector] uint4 rows.
 //
@@ -84,7 +84,7 @@ __device__ __forceinline__ uint32_t hit_bits(uint32_t kind, const DevChan &ch, g
     }
 }
 
-// The hits of one segment (units [4g, 4g+4) x the 128 shots of a block), following gfs_contract.h:
+// The hits of one segment (units [16g, 16g+16) x the 128 shots of a block), following gfs_contract.h:
 // f(k, shot, stream) is called for each hit, on unit 4g + k at `shot`.  At small p the first Philox
 // call of the segment usually shows there is no hit at all.
 template <typename F>
@@ -212,8 +212,8 @@ __device__ __forceinline__ void measure_row(uint32_t sub, uint4 *X, uint4 *Z, ui
 // Gate op with noise fused before and/or after it.  The op's units are its instruction's units (the
 // lowering fuses only single-run instructions whose noise targets are the same list), so the noise of
 // unit u is keyed exactly as the standalone noise instruction would be.  Each lane takes one noise
-// segment (four units x 128 shots): it walks the pre-noise hits into those units' shared-memory rows,
-// applies the gate to the four units, then walks the post-noise hits.  The rows are the lane's own, so
+// segment (sixteen units x 128 shots): it walks the pre-noise hits into those units' shared-memory rows,
+// applies the gate to the sixteen units, then walks the post-noise hits.  The rows are the lane's own, so
 // there are no atomics and no extra phase.
 // The gate of one unit of a fused op (noise is applied separately, in place, by the segment owner).
 template <int B>
@@ -248,7 +248,7 @@ __device__ __forceinline__ void gate_unit(const KernelArgs &p, uint32_t code, ui
 // Gate op with noise fused before and/or after it.  The op's units are its instruction's units (the
 // lowering fuses only single-run instructions whose noise targets are the same list), so the noise of
 // unit u is keyed exactly as the standalone noise instruction would be.  A warp takes 32 noise segments
-// (four units x 128 shots each): every lane walks its segment's pre-noise hits into those units'
+// (sixteen units x 128 shots each): every lane walks its segment's pre-noise hits into those units'
 // shared-memory rows; after a __syncwarp the warp applies the gate to the 128 units with consecutive lanes
 // on consecutive units (so quarter-warps touch distinct banks); after another __syncwarp each lane walks
 // its post-noise hits.  All rows stay within the warp: no atomics, no extra CTA phase.

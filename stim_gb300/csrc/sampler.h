@@ -171,9 +171,10 @@ struct gfs_sampler {
         }
     }
 
-    // Gap tables go to shared memory when they are small (up to 32 distinct probabilities).
-    uint32_t smem_table_words() const {
-        return prog.tables.size() <= 32 * GFS_TABLE_LEN ? (uint32_t)prog.tables.size() : 0;
+    // Gap tables go to shared memory for the inline-noise kernel when they are small (up to 16 KiB, two
+    // distinct probabilities); hit-list mode draws no noise in the frame kernel and keeps none.
+    uint32_t smem_table_words(bool hits = false) const {
+        return (!hits && prog.tables.size() * sizeof(uint32_t) <= 16384) ? (uint32_t)prog.tables.size() : 0;
     }
 
     // Small op streams go to shared memory too (every thread reads every op).
@@ -191,9 +192,11 @@ struct gfs_sampler {
         return (hits && prog.occs.size() <= 1024) ? (uint32_t)prog.occs.size() : 0;
     }
 
-    size_t smem_for(int bpc, bool ring_global, bool hits = false) const {
+    // tables = false: no gap tables in shared memory whatever the mode (the batched engine, whose inline
+    // fallback runs with the hit-list shape's shared-memory size).
+    size_t smem_for(int bpc, bool ring_global, bool hits = false, bool tables = true) const {
         return gfs::frame_smem_bytes(prog.num_rows, ring_global ? 0 : prog.ring, (uint32_t)prog.num_observables,
-                                     bpc, smem_table_words(), smem_ops(), smem_occ(hits));
+                                     bpc, tables ? smem_table_words(hits) : 0, smem_ops(), smem_occ(hits));
     }
 
     // ring: 0 = shared memory, 1 = global memory, -1 = whichever keeps more 128-shot blocks resident per SM.
@@ -389,7 +392,7 @@ struct gfs_sampler {
         a.obs_out = (uint4 *)obs_tmp.p;
         a.meas_out = (uint4 *)meas_tmp.p;
         a.status = (uint32_t *)d_status.p;
-        a.smem_table_words = smem_table_words();
+        a.smem_table_words = smem_table_words(sh.hits);
         a.smem_ops = smem_ops();
         a.ring_global = nullptr;
         if (sh.ring_global) {
