@@ -2330,8 +2330,8 @@ int oracle_dem_sample(const oracle_dem *d, uint64_t seed, uint64_t first_shot, u
         uint64_t nblk = (shots + 127) / 128;
         for (uint64_t b = 0; b < nblk; b++) {
             uint64_t block = first_shot / 128 + b;
-            for (size_t seg = 0; GFS_SEG_UNITS * seg < n; seg++) {
-                size_t units = n - GFS_SEG_UNITS * seg < GFS_SEG_UNITS ? n - GFS_SEG_UNITS * seg : GFS_SEG_UNITS;
+            for (size_t seg = 0; GFS_DEM_SEG_UNITS * seg < n; seg++) {
+                size_t units = n - GFS_DEM_SEG_UNITS * seg < GFS_DEM_SEG_UNITS ? n - GFS_DEM_SEG_UNITS * seg : GFS_DEM_SEG_UNITS;
                 gfs_stream st;
                 gfs_stream_init(&st, seed, GFS_P_DEM, g, (uint32_t)seg, (uint32_t)block);
                 int32_t pos = -1;
@@ -2340,7 +2340,7 @@ int oracle_dem_sample(const oracle_dem *d, uint64_t seed, uint64_t first_shot, u
                     if (s >= shots) {
                         continue;
                     }
-                    size_t m = members[GFS_SEG_UNITS * seg + ((uint32_t)pos >> 7)];
+                    size_t m = members[GFS_DEM_SEG_UNITS * seg + ((uint32_t)pos >> 7)];
                     odem_flip(d, m, s, dets, obs);
                     if (errs) {
                         errs[s * erow + (m >> 3)] |= (uint8_t)(1u << (m & 7));

@@ -33,7 +33,7 @@
  *   DEM     purpose 5: detector-error-model sampling.  The error mechanisms (error instructions with REPEAT
  *           unrolled) are grouped by probability, groups numbered by first appearance and each group's
  *           mechanisms kept in model order; group j is sampled like a noise instruction of instance j whose
- *           units are its mechanisms (same segments, same draws).
+ *           units are its mechanisms, with segments of GFS_DEM_SEG_UNITS units (same draws otherwise).
  *
  *   A segment's hits: pos = -1; repeat { pos += 1 + G(next draw); if pos >= trials: stop; hit(pos);
  *   if the channel picks a Pauli: choice = next draw }.  G(u) = max{k : u < T[k]} with
@@ -67,6 +67,9 @@
 #define GFS_P_NOISE 3u
 #define GFS_P_MNOISE 4u
 #define GFS_P_DEM 5u
+/* DEM segments stay at 4 mechanisms: a sampled error does several dependent global updates, and shorter
+ * walks keep more lanes busy per step. */
+#define GFS_DEM_SEG_UNITS 4u
 
 typedef struct gfs_u32x4 {
     uint32_t v[4];

@@ -1797,8 +1797,8 @@ __global__ void __launch_bounds__(256) dem_sample_kernel(const DemArgs a) {
     const uint32_t *T = a.tables + G.table;
     const bool always = (G.flags & 2u) != 0;
     const uint32_t block = (uint32_t)(a.block0 + blk);
-    const uint32_t seg0 = cu0 / GFS_SEG_UNITS;  // chunks start on segment boundaries
-    const uint32_t items = (cn + GFS_SEG_UNITS - 1) / GFS_SEG_UNITS;
+    const uint32_t seg0 = cu0 / GFS_DEM_SEG_UNITS;  // chunks start on segment boundaries
+    const uint32_t items = (cn + GFS_DEM_SEG_UNITS - 1) / GFS_DEM_SEG_UNITS;
     const uint32_t kseed0 = (uint32_t)a.seed, kseed1 = (uint32_t)(a.seed >> 32);
     const uint32_t c3base = gfs_c3(GFS_P_DEM, g, 0);
     const uint32_t lt = (1u << lane) - 1u;
@@ -1815,8 +1815,8 @@ __global__ void __launch_bounds__(256) dem_sample_kernel(const DemArgs a) {
             if (!active && rank < take) {
                 const NoiseQueued e = q[qn - 1 - rank];
                 const uint32_t sg = seg0 + e.item;
-                ubase = sg * GFS_SEG_UNITS;
-                trials = (int32_t)(min(GFS_SEG_UNITS, G.n - ubase) * GFS_BLOCK_SHOTS);
+                ubase = sg * GFS_DEM_SEG_UNITS;
+                trials = (int32_t)(min(GFS_DEM_SEG_UNITS, G.n - ubase) * GFS_BLOCK_SHOTS);
                 gfs_stream_init(&st, a.seed, GFS_P_DEM, g, sg, block);
                 if (always) {
                     pos = 0;
@@ -1842,7 +1842,7 @@ __global__ void __launch_bounds__(256) dem_sample_kernel(const DemArgs a) {
                     hit = true;
                 } else {
                     const uint32_t sg = seg0 + item;
-                    const uint32_t units = min(GFS_SEG_UNITS, G.n - sg * GFS_SEG_UNITS);
+                    const uint32_t units = min(GFS_DEM_SEG_UNITS, G.n - sg * GFS_DEM_SEG_UNITS);
                     const gfs_u32x4 r = gfs_philox(kseed0, kseed1, block, sg, g, c3base);
                     u = r.v[0];
                     d1 = r.v[1];
