@@ -157,6 +157,19 @@ gfs_status gfs_sample_detections_device_noalloc(gfs_sampler *s, uint64_t shots, 
                                                 uint64_t dets_stride, void *obs, uint64_t obs_stride);
 
 /*
+ * Sampling for a decoder, as sinter's StimThenDecodeSampler does it
+ * (glue/sample/src/sinter/_decoding/_stim_then_decode_sampler.py:170-190): `shots` shots of detection
+ * events, bit-packed, observables separate.  Shots whose detector row has a set bit under
+ * `postselection_mask` (ceil(D / 8) bytes, little-endian bits like the rows; NULL keeps every shot) are
+ * dropped on the device, and the kept shots' rows go, in shot order, to the first rows of the host buffers
+ * `dets` / `obs` (room for `shots` rows each; either may be NULL).  out3[0] = shots kept, out3[1] = shots
+ * dropped, out3[2] = detection events (set detector bits) over all `shots` shots before dropping, sinter's
+ * 'detection_events' count.  The stream position advances by `shots` as in gfs_sample_detections.
+ */
+gfs_status gfs_sample_for_decoder(gfs_sampler *s, uint64_t shots, const uint8_t *postselection_mask, uint8_t *dets,
+                                  uint64_t dets_stride, uint8_t *obs, uint64_t obs_stride, uint64_t *out3);
+
+/*
  * Device timings (milliseconds, CUDA events on the sampler's stream) of the last sample call:
  * out[0] = frame kernel, out[1] = transpose kernel(s), out[2] = device->host copies, out[3] = whole call.
  * counts[0] = frame-kernel launches, counts[1] = transpose launches.

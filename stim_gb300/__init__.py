@@ -250,6 +250,35 @@ class CompiledDetectorSampler(_SamplerBase):
             return dets, obs
         return dets
 
+    def sample_for_decoder(self, shots: int, *, postselection_mask=None):
+        """Samples ``shots`` shots for a decoder, as sinter's StimThenDecodeSampler does
+        (glue/sample/src/sinter/_decoding/_stim_then_decode_sampler.py:170-190), with the counting and the
+        postselection done on the device.
+
+        Returns ``(dets, obs, num_discards, num_detection_events)``: the kept shots' bit-packed detector and
+        observable rows in shot order, the number of shots dropped because a detection event fell under
+        ``postselection_mask`` (uint8, ``ceil(num_detectors / 8)`` bytes, or None), and the number of
+        detection events over all sampled shots before dropping."""
+        shots = int(shots)
+        if shots < 0:
+            raise ValueError("shots must be non-negative")
+        c = self._circuit
+        drow, orow = (c.num_detectors + 7) // 8, (c.num_observables + 7) // 8
+        mask = None
+        if postselection_mask is not None:
+            mask = np.ascontiguousarray(np.asarray(postselection_mask), dtype=np.uint8).reshape(-1)
+            if mask.shape[0] != drow:
+                raise ValueError(f"postselection_mask must have {drow} bytes, got {mask.shape[0]}")
+        dets = np.empty((shots, drow), dtype=np.uint8)
+        obs = np.empty((shots, orow), dtype=np.uint8)
+        out = (ctypes.c_uint64 * 3)()
+        if shots:
+            check(lib().gfs_sample_for_decoder(
+                self._h, shots, _ptr(mask) if mask is not None else None, _ptr(dets), max(1, drow), _ptr(obs),
+                max(1, orow), out))
+        kept = int(out[0])
+        return dets[:kept], obs[:kept], int(out[1]), int(out[2])
+
     def sample_write(self, shots: int, *, filepath, format: str = "01", obs_out_filepath=None,
                      obs_out_format: str = "01", prepend_observables: bool = False,
                      append_observables: bool = False) -> None:

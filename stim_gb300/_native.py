@@ -48,6 +48,7 @@ def _declare(L):
         "gfs_sample_detections": [_vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64],
         "gfs_sample_detections_device": [_vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64],
         "gfs_sample_detections_device_noalloc": [_vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64],
+        "gfs_sample_for_decoder": [_vp, _u64, _vp, _vp, _u64, _vp, _u64, ctypes.POINTER(_u64)],
         "gfs_sample_measurements": [_vp, _u64, ctypes.c_uint32, _vp, _vp, _u64],
         "gfs_sampler_last_timings": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_u64)],
         "gfs_sampler_set_shape": [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int],

@@ -1594,6 +1594,18 @@ __device__ __forceinline__ uint32_t chunk_word(const uint32_t *row, int32_t j, i
     return (v & 1u) | ((v >> 1) & 1u) << 8 | ((v >> 2) & 1u) << 16 | ((v >> 3) & 1u) << 24;
 }
 
+// Half-word j of a shot's output chunk (2-byte aligned destinations): packed bits, or two 0/1 bytes.
+__device__ __forceinline__ uint32_t chunk_half(const uint32_t *row, int32_t j, int packed) {
+    if (packed) {
+        return reinterpret_cast<const uint16_t *>(row)[j];
+    }
+    const uint32_t v = (row[j >> 4] >> (2 * (j & 15))) & 3u;
+    return (v & 1u) | (v >> 1) << 8;
+}
+
+// kSingle: one source, no row inversion (the detector, observable and measurement outputs of the samplers),
+// so a row load is one bounds test and one 16-byte load from a per-block base pointer.
+template <bool kSingle>
 __global__ void __launch_bounds__(256) transpose_tile_kernel(const TransposeArgs t) {
     __shared__ uint32_t tile[128][kTileWords + 1];  // [shot][32-row word], padded against bank conflicts
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1604,9 +1616,19 @@ __global__ void __launch_bounds__(256) transpose_tile_kernel(const TransposeArgs
     const uint64_t r0 = (uint64_t)blockIdx.x * kTileRows;
     const Transpose32 transpose32(lane);
     uint4 v[4];
+    if (kSingle) {
+        const uint4 *src = t.src0 + blk * t.n0 + r0;
+        const uint32_t avail = total - r0 < kTileRows ? (uint32_t)(total - r0) : kTileRows;
 #pragma unroll
-    for (uint32_t g = 0; g < 4; g++) {  // all four loads in flight before the shuffles
-        v[g] = load_concat(t, blk, r0 + 128 * warp + 32 * g + lane, total);
+        for (uint32_t g = 0; g < 4; g++) {  // all four loads in flight before the shuffles
+            const uint32_t r = 128 * warp + 32 * g + lane;
+            v[g] = r < avail ? src[r] : zero4();
+        }
+    } else {
+#pragma unroll
+        for (uint32_t g = 0; g < 4; g++) {
+            v[g] = load_concat(t, blk, r0 + 128 * warp + 32 * g + lane, total);
+        }
     }
 #pragma unroll
     for (uint32_t g = 0; g < 4; g++) {
@@ -1620,18 +1642,18 @@ __global__ void __launch_bounds__(256) transpose_tile_kernel(const TransposeArgs
     const uint64_t rows = total - r0 < kTileRows ? total - r0 : kTileRows;
     const int packed = t.bit_packed;
     const int32_t nbytes = (int32_t)(packed ? (rows + 7) / 8 : rows);
-    const uint64_t col = packed ? r0 / 8 : r0;
-    // One warp per shot row.  Destinations 4-byte aligned get one 4-byte word per lane; others (any row
-    // stride, e.g. ceil(detectors / 8) bytes) get bytes, lane q writing byte 32k + q so that every store
-    // instruction covers 32 consecutive bytes: no funnel shifts, no divergent edge handling.
-    for (uint32_t s = warp; s < 128; s += 8) {
-        const uint64_t shot = blk * 128 + s;
-        if (shot >= t.nshots) {
-            break;
-        }
+    const uint64_t left = t.nshots - blk * 128;
+    const uint32_t nvalid = left < 128 ? (uint32_t)left : 128u;
+    uint8_t *const base = t.out + blk * 128 * t.out_stride + (packed ? r0 / 8 : r0);
+    // One warp per shot row.  Destinations 4-byte aligned get one 4-byte word per lane, 2-byte aligned ones
+    // (even row strides, e.g. ceil(detectors / 8) = 1950 bytes) one half-word per lane, others bytes, lane q
+    // writing unit 32k + q so that every store instruction covers 32 consecutive units: no funnel shifts,
+    // no divergent edge handling.
+    for (uint32_t s = warp; s < nvalid; s += 8) {
         const uint32_t *row = tile[s];
-        uint8_t *dst = t.out + shot * t.out_stride + col;
-        if (((uintptr_t)dst & 3) == 0) {
+        uint8_t *dst = base + s * t.out_stride;
+        const uint32_t mis = (uint32_t)(uintptr_t)dst & 3u;
+        if (mis == 0) {
             uint32_t *d32 = reinterpret_cast<uint32_t *>(dst);
             const int32_t full = nbytes / 4;
             for (int32_t q = (int32_t)lane; q < full; q += 32) {
@@ -1640,6 +1662,15 @@ __global__ void __launch_bounds__(256) transpose_tile_kernel(const TransposeArgs
             if ((int32_t)lane < nbytes - 4 * full) {
                 const int32_t b = 4 * full + (int32_t)lane;
                 dst[b] = (uint8_t)(chunk_word(row, b >> 2, packed) >> (8 * (b & 3)));
+            }
+        } else if (mis == 2) {
+            uint16_t *d16 = reinterpret_cast<uint16_t *>(dst);
+            const int32_t full = nbytes / 2;
+            for (int32_t q = (int32_t)lane; q < full; q += 32) {
+                d16[q] = (uint16_t)chunk_half(row, q, packed);
+            }
+            if (lane == 0 && (nbytes & 1)) {
+                dst[nbytes - 1] = (uint8_t)chunk_half(row, full, packed);
             }
         } else if (packed) {
             const uint8_t *rb = reinterpret_cast<const uint8_t *>(row);
@@ -1664,6 +1695,7 @@ cudaError_t launch_transpose(const TransposeArgs &args, cudaStream_t stream) {
         return cudaErrorInvalidValue;
     }
     const uint64_t nblk = (args.nshots + 127) / 128;
+    const bool single = args.n1 == 0 && args.n2 == 0 && args.xor_rows == nullptr;
     const uint64_t per_launch = 65535;  // grid.y limit; larger requests are split by 128-shot block
     for (uint64_t b0 = 0; b0 < nblk; b0 += per_launch) {
         TransposeArgs t = args;
@@ -1673,7 +1705,11 @@ cudaError_t launch_transpose(const TransposeArgs &args, cudaStream_t stream) {
         t.out = args.out + b0 * 128 * args.out_stride;
         t.nshots = args.nshots - b0 * 128;
         const uint64_t nb = nblk - b0 < per_launch ? nblk - b0 : per_launch;
-        transpose_tile_kernel<<<dim3((unsigned)tiles, (unsigned)nb), 256, 0, stream>>>(t);
+        if (single) {
+            transpose_tile_kernel<true><<<dim3((unsigned)tiles, (unsigned)nb), 256, 0, stream>>>(t);
+        } else {
+            transpose_tile_kernel<false><<<dim3((unsigned)tiles, (unsigned)nb), 256, 0, stream>>>(t);
+        }
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {
             return e;
@@ -1886,6 +1922,235 @@ cudaError_t launch_dem_sample(const DemArgs &args, cudaStream_t stream) {
         return cudaErrorInvalidValue;
     }
     dem_sample_kernel<<<(unsigned)blocks, 256, 0, stream>>>(args);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------------------
+// Decoder feed.  The reference's sinter sampler (glue/sample/src/sinter/_decoding/_stim_then_decode_sampler.py:
+// 170-190) counts detection events with eight numpy passes over the shot-major bytes and drops postselected
+// shots with a numpy mask; here both run over the device rows before anything crosses the link, and only the
+// kept rows are copied out.
+// ------------------------------------------------------------------------------------------------
+
+// Set bits over the flat detector bytes (16-byte aligned base): one 16-byte load per thread and step.
+__global__ void __launch_bounds__(256) feed_popcount_kernel(const uint8_t *p, uint64_t n, unsigned long long *count) {
+    const uint64_t n16 = n / 16;
+    const uint4 *q = reinterpret_cast<const uint4 *>(p);
+    unsigned long long c = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * 256 + threadIdx.x; i < n16; i += (uint64_t)gridDim.x * 256) {
+        const uint4 v = q[i];
+        c += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (n & 15)) {
+        c += __popc(p[16 * n16 + threadIdx.x]);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
+    }
+    if ((threadIdx.x & 31) == 0 && c) {
+        atomicAdd(count, c);
+    }
+}
+
+// One warp per shot: lanes test the mask's bytes; the group's kept count goes to group_kept.
+__global__ void __launch_bounds__(256) feed_flags_kernel(const FeedArgs a) {
+    __shared__ uint32_t kept_warp[8];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t s0 = (uint64_t)blockIdx.x * kFeedGroup;
+    uint32_t kept = 0;
+    for (uint32_t i = warp; i < kFeedGroup; i += 8) {
+        const uint64_t s = s0 + i;
+        if (s >= a.nshots) {
+            break;
+        }
+        const uint8_t *row = a.dets + s * a.drow;
+        uint32_t hit = 0;
+        for (uint32_t k = lane; k < a.nmask; k += 32) {
+            hit |= row[a.mask_idx[k]] & a.mask_bits[k];
+        }
+        const uint32_t keep = __any_sync(0xFFFFFFFFu, hit != 0) ? 0u : 1u;
+        if (lane == 0) {
+            a.keep[s] = (uint8_t)keep;
+        }
+        kept += keep;
+    }
+    if (lane == 0) {
+        kept_warp[warp] = kept;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < 8; w++) {
+            t += kept_warp[w];
+        }
+        a.group_kept[blockIdx.x] = t;
+        const uint64_t left = a.nshots - s0;
+        const uint32_t n = left < kFeedGroup ? (uint32_t)left : kFeedGroup;
+        if (n > t) {
+            atomicAdd(&a.counts[1], (unsigned long long)(n - t));
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t warp_inclusive_sum(uint32_t x, uint32_t lane) {
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) {
+            x += y;
+        }
+    }
+    return x;
+}
+
+// Exclusive prefix sum of the groups' kept counts, in place: one CTA walks tiles of 1024 with a carry.
+__global__ void __launch_bounds__(1024) feed_scan_kernel(uint32_t *v, uint32_t n) {
+    __shared__ uint32_t wsum[32];
+    __shared__ uint32_t carry_s;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        carry_s = 0;
+    }
+    __syncthreads();
+    for (uint32_t base = 0; base < n; base += 1024) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t x = i < n ? v[i] : 0u;
+        const uint32_t inc = warp_inclusive_sum(x, lane);
+        if (lane == 31) {
+            wsum[warp] = inc;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t w = wsum[lane];
+            wsum[lane] = warp_inclusive_sum(w, lane) - w;
+        }
+        __syncthreads();
+        const uint32_t carry = carry_s;
+        if (i < n) {
+            v[i] = carry + wsum[warp] + inc - x;
+        }
+        __syncthreads();
+        if (threadIdx.x == 1023) {
+            carry_s = carry + wsum[31] + inc;
+        }
+        __syncthreads();
+    }
+}
+
+// Copies n bytes with the widest unit dividing n (both rows start at multiples of n from 256-byte aligned
+// bases, so that unit is aligned on both sides).
+__device__ __forceinline__ void feed_copy_row(uint8_t *dst, const uint8_t *src, uint64_t n, uint32_t lane) {
+    if ((n & 15) == 0) {
+        for (uint64_t j = lane; j < n / 16; j += 32) {
+            reinterpret_cast<uint4 *>(dst)[j] = reinterpret_cast<const uint4 *>(src)[j];
+        }
+    } else if ((n & 7) == 0) {
+        for (uint64_t j = lane; j < n / 8; j += 32) {
+            reinterpret_cast<uint2 *>(dst)[j] = reinterpret_cast<const uint2 *>(src)[j];
+        }
+    } else if ((n & 3) == 0) {
+        for (uint64_t j = lane; j < n / 4; j += 32) {
+            reinterpret_cast<uint32_t *>(dst)[j] = reinterpret_cast<const uint32_t *>(src)[j];
+        }
+    } else if ((n & 1) == 0) {
+        for (uint64_t j = lane; j < n / 2; j += 32) {
+            reinterpret_cast<uint16_t *>(dst)[j] = reinterpret_cast<const uint16_t *>(src)[j];
+        }
+    } else {
+        for (uint64_t j = lane; j < n; j += 32) {
+            dst[j] = src[j];
+        }
+    }
+}
+
+// Kept shots of a group get consecutive output rows from the group's scanned start: thread t ranks shots
+// 4t .. 4t + 3, then one warp per kept shot copies its detector and observable rows.
+__global__ void __launch_bounds__(256) feed_compact_kernel(const FeedArgs a) {
+    __shared__ uint32_t dst[kFeedGroup];
+    __shared__ uint32_t wsum[8];
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint64_t s0 = (uint64_t)blockIdx.x * kFeedGroup;
+    uint32_t k[4], c = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < 4; j++) {
+        const uint64_t s = s0 + 4 * tid + j;
+        k[j] = s < a.nshots ? (uint32_t)a.keep[s] : 0u;
+        c += k[j];
+    }
+    const uint32_t inc = warp_inclusive_sum(c, lane);
+    if (lane == 31) {
+        wsum[warp] = inc;
+    }
+    __syncthreads();
+    uint32_t before = 0;
+    for (uint32_t w = 0; w < warp; w++) {
+        before += wsum[w];
+    }
+    uint32_t pos = a.group_kept[blockIdx.x] + before + inc - c;
+#pragma unroll
+    for (uint32_t j = 0; j < 4; j++) {
+        dst[4 * tid + j] = k[j] ? pos : 0xFFFFFFFFu;
+        pos += k[j];
+    }
+    __syncthreads();
+    for (uint32_t i = warp; i < kFeedGroup; i += 8) {
+        const uint32_t r = dst[i];
+        if (r == 0xFFFFFFFFu) {
+            continue;
+        }
+        const uint64_t s = s0 + i;
+        feed_copy_row(a.cdets + (uint64_t)r * a.drow, a.dets + s * a.drow, a.drow, lane);
+        if (a.orow) {
+            feed_copy_row(a.cobs + (uint64_t)r * a.orow, a.obs + s * a.orow, a.orow, lane);
+        }
+    }
+}
+
+cudaError_t launch_feed_popcount(const FeedArgs &args, cudaStream_t stream) {
+    const uint64_t n = args.nshots * args.drow;
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    const uint64_t want = (n / 16 + 255) / 256;
+    const unsigned grid = (unsigned)(want < 1 ? 1 : (want > 4096 ? 4096 : want));
+    feed_popcount_kernel<<<grid, 256, 0, stream>>>(args.dets, n, args.counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_feed_flags(const FeedArgs &args, cudaStream_t stream) {
+    const uint64_t groups = (args.nshots + kFeedGroup - 1) / kFeedGroup;
+    if (groups == 0) {
+        return cudaSuccess;
+    }
+    if (groups > 0x7FFFFFFFull) {
+        return cudaErrorInvalidValue;
+    }
+    feed_flags_kernel<<<(unsigned)groups, 256, 0, stream>>>(args);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_feed_scan(const FeedArgs &args, cudaStream_t stream) {
+    const uint64_t groups = (args.nshots + kFeedGroup - 1) / kFeedGroup;
+    if (groups == 0) {
+        return cudaSuccess;
+    }
+    if (groups > 0xFFFFFFFFull) {
+        return cudaErrorInvalidValue;
+    }
+    feed_scan_kernel<<<1, 1024, 0, stream>>>(args.group_kept, (uint32_t)groups);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_feed_compact(const FeedArgs &args, cudaStream_t stream) {
+    const uint64_t groups = (args.nshots + kFeedGroup - 1) / kFeedGroup;
+    if (groups == 0) {
+        return cudaSuccess;
+    }
+    if (groups > 0x7FFFFFFFull) {
+        return cudaErrorInvalidValue;
+    }
+    feed_compact_kernel<<<(unsigned)groups, 256, 0, stream>>>(args);
     return cudaGetLastError();
 }
 

@@ -157,6 +157,29 @@ struct DemArgs {
 };
 cudaError_t launch_dem_sample(const DemArgs &args, cudaStream_t stream);
 
+// Decoder feed (gfs_sample_for_decoder): dense shot-major bit-packed detector rows (drow bytes each) and
+// observable rows (orow bytes each) on the device.  A shot is dropped when its detector row has a set bit
+// under the postselection mask, given as nmask (byte index, byte bits) pairs.  Shots are handled in groups
+// of kFeedGroup: group_kept[g] first counts group g's kept shots, then (after launch_feed_scan) holds the
+// output row of its first kept shot.
+constexpr uint32_t kFeedGroup = 1024;
+struct FeedArgs {
+    const uint8_t *dets;
+    const uint8_t *obs;
+    uint64_t drow, orow, nshots;
+    const uint32_t *mask_idx;
+    const uint8_t *mask_bits;
+    uint32_t nmask;
+    uint32_t *group_kept;
+    uint8_t *keep;                // per shot: 1 kept, 0 dropped
+    unsigned long long *counts;   // [0] += set bits over the detector rows, [1] += dropped shots
+    uint8_t *cdets, *cobs;        // kept rows, in shot order
+};
+cudaError_t launch_feed_popcount(const FeedArgs &args, cudaStream_t stream);
+cudaError_t launch_feed_flags(const FeedArgs &args, cudaStream_t stream);
+cudaError_t launch_feed_scan(const FeedArgs &args, cudaStream_t stream);
+cudaError_t launch_feed_compact(const FeedArgs &args, cudaStream_t stream);
+
 // Shared-memory load+store throughput of the current device (bytes per second over all SMs).
 cudaError_t measure_smem_peak(double *bytes_per_s);
 

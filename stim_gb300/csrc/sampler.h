@@ -117,6 +117,7 @@ struct gfs_sampler {
     gfs::Program prog;
     DevBuf d_ops, d_pool, d_tables, d_chans, d_orig, d_status;
     DevBuf det_tmp, obs_tmp, meas_tmp, out_tmp, ref_bits, ring_buf;
+    DevBuf feed_rows, feed_compact, feed_aux;  // gfs_sample_for_decoder (feed.cc)
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;  // device->host copies of host-destination chunks
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
