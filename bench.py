@@ -34,6 +34,10 @@ METRIC = "detection-event Gbit/s at d=25 r=25 (surface_code:rotated_memory_z, p=
 # one ncu capture of 131,072 shots (hit-list mode, 1 block x 128 threads per CTA); traffic grows with shots.
 FRAME_DRAM_BYTES_PER_SHOT = 2860.0
 UNIT = "Gbit/s"
+E2E_WARMUP = 3
+# Device-to-host rate of the GB300 machine's host link, measured with page-locked copies of 2 GiB on 1, 2, 4 and 8
+# concurrent streams (192.5-192.9 GB/s in every case): the floor of the e2e step time.
+LINK_GBS = 192.9
 WORKLOAD = dict(family="surface_code:rotated_memory_z", distance=25, rounds=25, p=0.001)
 
 
@@ -285,19 +289,29 @@ def run_gpu(args):
     value = world * args.steps * shots * (D + O) / dev_s / 1e9
 
     # End to end through the public API into host numpy arrays that the caller reuses between requests
-    # (dets_out= / obs_out=, as a streaming caller does); the first call touches their pages.
-    host_dets = np.empty((shots, drow), dtype=np.uint8)
-    host_obs = np.empty((shots, orow), dtype=np.uint8)
-    e2e_times = []
-    e2e_parts = []
-    for k in range(args.e2e_steps + 1):
-        t1 = time.perf_counter()
-        sampler.sample(shots, bit_packed=True, separate_observables=True, dets_out=host_dets, obs_out=host_obs)
-        if k:
-            e2e_times.append(time.perf_counter() - t1)
-            e2e_parts.append(sampler.last_timings())
+    # (dets_out= / obs_out=, as a streaming caller does).  The headline uses page-locked arrays (numpy views of
+    # torch pin_memory tensors), so the device->host copies run as DMA at the link's rate; the same call into
+    # ordinary pageable numpy arrays is reported beside it.  E2E_WARMUP untimed calls touch the pages first.
+    def e2e_leg(dets_arr, obs_arr):
+        times, parts = [], []
+        if args.e2e_steps <= 0:
+            return times, parts
+        for k in range(E2E_WARMUP + args.e2e_steps):
+            t1 = time.perf_counter()
+            sampler.sample(shots, bit_packed=True, separate_observables=True, dets_out=dets_arr, obs_out=obs_arr)
+            if k >= E2E_WARMUP:
+                times.append(time.perf_counter() - t1)
+                parts.append(sampler.last_timings())
+        return times, parts
+
+    pin_rows = shots if args.e2e_steps > 0 else 0
+    pinned_dets = torch.empty((pin_rows, drow), dtype=torch.uint8, pin_memory=True).numpy()
+    pinned_obs = torch.empty((pin_rows, orow), dtype=torch.uint8, pin_memory=True).numpy()
+    e2e_times, e2e_parts = e2e_leg(pinned_dets, pinned_obs)
     e2e_s = sum(e2e_times)
     e2e_value = world * len(e2e_times) * shots * (D + O) / e2e_s / 1e9 if e2e_times else None
+    page_times, _ = e2e_leg(np.empty((pin_rows, drow), dtype=np.uint8), np.empty((pin_rows, orow), dtype=np.uint8))
+    page_value = world * len(page_times) * shots * (D + O) / sum(page_times) / 1e9 if page_times else None
 
     acc_bits, rbits, hits = algorithmic_work(text)
     frame_avg_s = statistics.mean(frame_ms) / 1e3
@@ -336,7 +350,12 @@ def run_gpu(args):
                     "p50_ms": 1e3 * statistics.median(e2e_times) if e2e_times else None,
                     "p99_ms": 1e3 * max(e2e_times) if e2e_times else None,
                     "api": "CompiledDetectorSampler.sample(shots, bit_packed=True, separate_observables=True, "
-                           "dets_out=, obs_out=) into reused host numpy arrays",
+                           "dets_out=, obs_out=) into reused page-locked host numpy arrays",
+                    "pageable": {"value": page_value, "unit": UNIT,
+                                 "p50_ms": 1e3 * statistics.median(page_times) if page_times else None,
+                                 "p99_ms": 1e3 * max(page_times) if page_times else None,
+                                 "api": "the same call into reused pageable numpy arrays"},
+                    "link_bound_ms": 1e3 * shots * (drow + orow) / LINK_GBS / 1e9,
                     "device_ms": {k: statistics.mean(p[k] for p in e2e_parts) for k in
                                   ("frame_ms", "noise_ms", "transpose_ms", "copy_ms", "total_ms")}
                     if e2e_parts else None},
@@ -382,11 +401,11 @@ def run_m2d(args, local, text):
     times = []
     d = np.empty((shots, (c.num_detectors + 7) // 8), dtype=np.uint8)
     o = np.empty((shots, (c.num_observables + 7) // 8), dtype=np.uint8)
-    for k in range(args.m2d_steps + 1):  # the first call touches the reused output arrays' pages
+    for k in range(E2E_WARMUP + args.m2d_steps):  # the untimed calls touch the reused output arrays' pages
         t0 = time.perf_counter()
         d, o = conv.convert(measurements=meas, separate_observables=True, append_observables=False,
                             bit_packed=True, dets_out=d, obs_out=o)
-        if k:
+        if k >= E2E_WARMUP:
             times.append(time.perf_counter() - t0)
     want_d, want_o = c.compile_detector_sampler(seed=args.seed, device=local).sample(
         shots, separate_observables=True, bit_packed=True)
@@ -415,10 +434,10 @@ def run_dem(args, local):
     d = np.empty((shots, (D + 7) // 8), dtype=np.uint8)
     o = np.empty((shots, (O + 7) // 8), dtype=np.uint8)
     times = []
-    for k in range(args.dem_steps + 1):  # the first call touches the reused output arrays' pages
+    for k in range(E2E_WARMUP + args.dem_steps):  # the untimed calls touch the reused output arrays' pages
         t0 = time.perf_counter()
         s.sample(shots, bit_packed=True, dets_out=d, obs_out=o)
-        if k:
+        if k >= E2E_WARMUP:
             times.append(time.perf_counter() - t0)
     ms = 1e3 * statistics.median(times)
     return {"workload": f"{shots} shots of the d=25 r=25 p=1e-3 detector error model ({dem.num_errors} error "
@@ -604,7 +623,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--shots", type=int, default=1 << 20)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-chunk", type=int, default=1 << 16)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-shots", type=int, default=1 << 20)
@@ -613,8 +632,8 @@ def main():
     ap.add_argument("--noise-mode", type=int, default=-1, help="-1 automatic, 0 inline, 1 hit lists")
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--batched", type=int, default=1)
-    ap.add_argument("--m2d-steps", type=int, default=2)
-    ap.add_argument("--dem-steps", type=int, default=2)
+    ap.add_argument("--m2d-steps", type=int, default=5)
+    ap.add_argument("--dem-steps", type=int, default=5)
     ap.add_argument("--batch-circuits", type=int, default=256)
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
