@@ -303,8 +303,10 @@ gfs_status gfs_server_stats(gfs_server *s, double *out12);
  * apart; flags = GFS_BIT_PACKED and at most one of GFS_PREPEND_OBSERVABLES / GFS_APPEND_OBSERVABLES; dets and
  * obs (either may be null) as in gfs_sample_detections.  Detector k fires when the parity of its measurements
  * differs from their parity in the reference sample; observables likewise.  sweep (may be null) = host rows
- * of ceil(sweep bits / 8) bytes: accepted when every bit is zero or the circuit has no sweep-controlled
- * operation (then they change nothing); otherwise the call fails with GFS_ERR_INVALID_ARGUMENT.
+ * of ceil(sweep bits / 8) bit-packed bytes, sweep_stride bytes apart: the sweep-controlled Paulis they switch
+ * on flip measurement results (and observables' Pauli terms) as in the reference, through a noiseless,
+ * randomization-free run of the frame kernel over the sweep table (skipped when every bit is zero or no
+ * operation is sweep-controlled).
  */
 typedef struct gfs_m2d gfs_m2d;
 gfs_status gfs_m2d_create(const gfs_circuit *c, const uint8_t *ref_sample, int device, gfs_m2d **out);

@@ -169,42 +169,82 @@ __device__ __forceinline__ void ring_st(uint4 *R, uint32_t i, uint4 v, bool rg) 
     }
 }
 
-// Measurement of one row: the result goes to ring slot `slot`, the measured basis is re-randomized.
+// Measurement of one row: the result goes to ring slot `slot`, the measured basis is re-randomized.  With
+// norand the frame keeps what the reference's frame simulator keeps when it does not randomize
+// (guarantee_anticommutation_via_frame_randomization = false, frame_simulator.inl:172-317): the randomized
+// component is left as it was.  Where the lowering set norand to skip randomization, the randomized
+// combination provably reaches no output, so keeping it gives the same outputs as a fresh draw.
 __device__ __forceinline__ void measure_row(uint32_t sub, uint4 *X, uint4 *Z, uint4 *R, uint32_t idx, uint32_t slot,
-                                            uint4 r, bool rg) {
+                                            uint4 r, bool rg, bool norand) {
     const uint4 x = X[idx];
     switch (sub) {
         case KM_M:
             ring_st(R, slot, x, rg);
-            Z[idx] = r;
+            if (!norand) {
+                Z[idx] = r;
+            }
             break;
         case KM_MX:
             ring_st(R, slot, Z[idx], rg);
-            X[idx] = r;
+            if (!norand) {
+                X[idx] = r;
+            }
             break;
         case KM_MY: {
             const uint4 y = x4(x, Z[idx]);
             ring_st(R, slot, y, rg);
-            X[idx] = x4(y, r);
-            Z[idx] = r;
+            if (!norand) {
+                X[idx] = x4(y, r);
+                Z[idx] = r;
+            }
             break;
         }
         case KM_MR:
             ring_st(R, slot, x, rg);
             X[idx] = zero4();
-            Z[idx] = r;
+            if (!norand) {
+                Z[idx] = r;
+            }
             break;
         case KM_MRX:
             ring_st(R, slot, Z[idx], rg);
             Z[idx] = zero4();
-            X[idx] = r;
+            if (!norand) {
+                X[idx] = r;
+            }
             break;
         default: {  // KM_MRY
-            const uint4 y = x4(x, Z[idx]);
-            ring_st(R, slot, y, rg);
-            Z[idx] = r;
-            X[idx] = r;
+            const uint4 z = Z[idx];
+            ring_st(R, slot, x4(x, z), rg);
+            if (!norand) {
+                Z[idx] = r;
+                X[idx] = r;
+            } else {
+                X[idx] = z;
+            }
             break;
+        }
+    }
+}
+
+// Reset of one row (same norand rule as measure_row).
+__device__ __forceinline__ void reset_row(uint32_t sub, uint4 *X, uint4 *Z, uint32_t idx, uint4 r, bool norand) {
+    if (sub == KR_R) {
+        X[idx] = zero4();
+        if (!norand) {
+            Z[idx] = r;
+        }
+    } else if (sub == KR_RX) {
+        Z[idx] = zero4();
+        if (!norand) {
+            X[idx] = r;
+        }
+    } else {  // KR_RY
+        if (!norand) {
+            X[idx] = r;
+            Z[idx] = r;
+        } else {
+            X[idx] = Z[idx];
         }
     }
 }
@@ -237,11 +277,9 @@ __device__ __forceinline__ void gate_unit(const KernelArgs &p, uint32_t code, ui
         Z[i1] = z;
     } else if (code == OP_MEASURE) {
         measure_row(sub, X, Z, R, i1, wrap(rec + u, L) * B + blk, rand_row(p, norand, inst, rb + u, block),
-                    p.ring_global != nullptr);
+                    p.ring_global != nullptr, norand);
     } else {  // OP_RESET
-        const uint4 r = rand_row(p, norand, inst, rb + u, block);
-        X[i1] = sub == KR_R ? zero4() : r;
-        Z[i1] = sub == KR_RX ? zero4() : r;
+        reset_row(sub, X, Z, i1, rand_row(p, norand, inst, rb + u, block), norand);
     }
 }
 
@@ -1099,7 +1137,12 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
                     uint32_t k = __ldg(pool + a + 2 * u);
                     uint32_t rm = __ldg(pool + a + 2 * u + 1);
                     uint32_t idx = (rm & kRowMask) * B + blk;
-                    uint4 v = ring_ld(R, wrap(rec + L - k, L) * B + blk, rg);
+                    uint4 v;
+                    if (k & kFeedbackSweep) {  // sweep bit (k & ~kFeedbackSweep) < nsweep, checked by the host
+                        v = p.sweep ? p.sweep[(lb0 + blk) * p.nsweep + (k & ~kFeedbackSweep)] : zero4();
+                    } else {
+                        v = ring_ld(R, wrap(rec + L - k, L) * B + blk, rg);
+                    }
                     if ((rm >> 24) & kFeedbackX) {
                         X[idx] = x4(X[idx], v);
                     }
@@ -1113,30 +1156,28 @@ __device__ __forceinline__ void frame_slice(const KernelArgs &p, const FrameStat
                 if (compact) {
                     for_items<B, 4, true>(glist, n * B, tid, nt, [&](uint32_t u, uint32_t blk, uint32_t row) {
                         measure_row(sub, X, Z, R, row * B + blk, wrap(rec + u, L) * B + blk,
-                                    rand_row(p, norand, inst, op.b + u, (uint32_t)(gb0 + blk)), rg);
+                                    rand_row(p, norand, inst, op.b + u, (uint32_t)(gb0 + blk)), rg, norand);
                     });
                 } else {
                     for (uint32_t i = tid; i < n * B; i += nt) {
                         const uint32_t u = i / B, blk = i % B;
                         measure_row(sub, X, Z, R, __ldg(pool + a + u) * B + blk, wrap(rec + u, L) * B + blk,
-                                    rand_row(p, norand, inst, op.b + u, (uint32_t)(gb0 + blk)), rg);
+                                    rand_row(p, norand, inst, op.b + u, (uint32_t)(gb0 + blk)), rg, norand);
                     }
                 }
                 rec = wrap(rec + n, L);
                 break;
 
             case OP_RESET: {
-                auto reset_row = [&](uint32_t u, uint32_t blk, uint32_t row) {
-                    const uint32_t idx = row * B + blk;
-                    const uint4 r = rand_row(p, norand, inst, op.b + u, (uint32_t)(gb0 + blk));
-                    X[idx] = sub == KR_R ? zero4() : r;
-                    Z[idx] = sub == KR_RX ? zero4() : r;
+                auto reset_unit = [&](uint32_t u, uint32_t blk, uint32_t row) {
+                    reset_row(sub, X, Z, row * B + blk, rand_row(p, norand, inst, op.b + u, (uint32_t)(gb0 + blk)),
+                              norand);
                 };
                 if (compact) {
-                    for_items<B, 4, true>(glist, n * B, tid, nt, reset_row);
+                    for_items<B, 4, true>(glist, n * B, tid, nt, reset_unit);
                 } else {
                     for (uint32_t i = tid; i < n * B; i += nt) {
-                        reset_row(i / B, i % B, __ldg(pool + a + i / B));
+                        reset_unit(i / B, i % B, __ldg(pool + a + i / B));
                     }
                 }
                 break;
@@ -1782,8 +1823,14 @@ __global__ void __launch_bounds__(256) m2d_fold_kernel(const FoldArgs a) {
             acc = make_uint4(~acc.x, ~acc.y, ~acc.z, ~acc.w);
         }
         if (o < a.D) {
+            if (a.base_dets) {
+                acc = x4(acc, a.base_dets[blk * a.D + o]);
+            }
             a.dets[blk * a.D + o] = acc;
         } else {
+            if (a.base_obs) {
+                acc = x4(acc, a.base_obs[blk * a.O + (o - a.D)]);
+            }
             a.obs[blk * a.O + (o - a.D)] = acc;
         }
     }

@@ -41,6 +41,8 @@ struct KernelArgs {
     uint32_t smem_occ;       // n_occ when the occurrence offsets and the slice's counts are cached in shared
                              // memory, else 0
     uint32_t reset_zero;     // 1: start every shot's Z frame at zero instead of random (Program::reset_norand)
+    const uint4 *sweep;      // [local block][nsweep] sweep bits read by sweep feedback; null: all zero
+    uint32_t nsweep;
 };
 
 // Several circuits in one launch (batch_frame_kernel): circuit j owns work items
@@ -110,7 +112,7 @@ struct RowsInArgs {
 cudaError_t launch_rows_from_shots(const RowsInArgs &args, cudaStream_t stream);
 
 // out row o of block b = XOR of rows[b][idx[j]] for j in [off[o], off[o+1]), inverted when bit o of `expect`
-// is set; outputs [0, D) go to dets[b][.], [D, D + O) to obs[b][.].
+// is set, XORed with the base rows when given; outputs [0, D) go to dets[b][.], [D, D + O) to obs[b][.].
 struct FoldArgs {
     const uint4 *rows;
     uint64_t nrows;
@@ -121,6 +123,8 @@ struct FoldArgs {
     uint64_t nblk;
     uint4 *dets;
     uint4 *obs;
+    const uint4 *base_dets;  // non-null: XORed into the outputs ([block][D] and [block][O], e.g. the frame
+    const uint4 *base_obs;   // kernel's detectors and observables of the sweep-driven flips)
 };
 cudaError_t launch_fold(const FoldArgs &args, cudaStream_t stream);
 

@@ -38,11 +38,23 @@ struct Lowerer {
     std::vector<std::vector<uint32_t>> pending_dets;
     uint64_t pending_inst = 0;
 
-    Lowerer(const Circuit &c, SampleMode m) : root(c), mode(m) {
+    LowerOptions opts;
+
+    Lowerer(const Circuit &c, SampleMode m, const LowerOptions &o) : root(c), mode(m), opts(o) {
     }
 
     uint32_t row(uint32_t t) const {
         return (uint32_t)row_of[t & GFS_T_VALUE_MASK];
+    }
+
+    // OP_FEEDBACK source word of sweep target `t` (LowerOptions::sweep).
+    uint32_t sweep_source(uint32_t t) {
+        const uint32_t k = t & GFS_T_VALUE_MASK;
+        if (k >= kFeedbackSweep) {
+            throw std::invalid_argument("sweep bit index too large for the GPU frame sampler");
+        }
+        prog.num_sweep_bits = std::max<uint64_t>(prog.num_sweep_bits, (uint64_t)k + 1);
+        return kFeedbackSweep | k;
     }
 
     void collect_qubits(const Circuit &c, std::vector<uint8_t> &used) {
@@ -268,17 +280,22 @@ struct Lowerer {
                 q = t;
                 mask = sub == K2_CX ? kFeedbackX : (kFeedbackX | kFeedbackZ);
             }
+            uint32_t src;
             if (bit & GFS_T_SWEEP) {
-                continue;  // sweep bits read as zero in the samplers
+                if (!opts.sweep) {
+                    continue;  // sweep bits read as zero in the samplers
+                }
+                src = sweep_source(bit);
+            } else {
+                src = bit & GFS_T_VALUE_MASK;
+                check_lookback(src);
             }
-            uint32_t k_back = bit & GFS_T_VALUE_MASK;
-            check_lookback(k_back);
             uint32_t r = row(q);
             if (!qrows.empty() || seen.count(r)) {
                 flush();
             }
             seen.insert(r);
-            fb.push_back(k_back);
+            fb.push_back(src);
             fb.push_back(r | (mask << 24));
         }
         flush();
@@ -440,12 +457,18 @@ struct Lowerer {
                     prog.pool.push_back(focus);
                 }
                 for (auto b : p.bits) {
+                    uint32_t src;
                     if (b & GFS_T_SWEEP) {
-                        continue;
+                        if (!opts.sweep) {
+                            continue;
+                        }
+                        src = sweep_source(b);
+                    } else {
+                        src = b & GFS_T_VALUE_MASK;
+                        check_lookback(src);
                     }
-                    check_lookback(b & GFS_T_VALUE_MASK);
                     emit(OP_FEEDBACK, 0, 1, inst);
-                    prog.pool.push_back(b & GFS_T_VALUE_MASK);
+                    prog.pool.push_back(src);
                     prog.pool.push_back(focus | (kFeedbackX << 24));
                 }
             };
@@ -1369,6 +1392,9 @@ struct Lowerer {
                     case OP_FEEDBACK:
                         for (uint32_t u = 0; u < n; u++) {
                             const uint32_t k = prog.pool[op.a + 2 * u], rm = prog.pool[op.a + 2 * u + 1];
+                            if (k & kFeedbackSweep) {
+                                continue;  // sweep data is an input, not randomness
+                            }
                             const uint32_t r = rm & kRowMask;
                             Set &P = pend[(meas - k) % R];
                             if ((rm >> 24) & kFeedbackX) {
@@ -1477,7 +1503,15 @@ struct Lowerer {
         if (dets_unrolled != prog.stats.num_detectors) {
             throw std::logic_error("detector count mismatch in lowering");
         }
-        if (mode == SampleMode::DETECTIONS) {
+        if (opts.no_randomization) {
+            prog.reset_norand = true;
+            for (DevOp &op : prog.ops) {
+                const uint32_t code = op.code & 0xFFu;
+                if (code == OP_MEASURE || code == OP_RESET) {
+                    op.code |= kNoRandomize;
+                }
+            }
+        } else if (mode == SampleMode::DETECTIONS) {
             analyze_randomization();
         }
     }
@@ -1507,10 +1541,33 @@ uint64_t plan_hit_regions(std::vector<NoiseOcc> &occs, const std::vector<double>
     return off;
 }
 
-Program lower(const Circuit &circuit, SampleMode mode) {
-    Lowerer l(circuit, mode);
+Program lower(const Circuit &circuit, SampleMode mode, const LowerOptions &opts) {
+    Lowerer l(circuit, mode, opts);
     l.run();
     return std::move(l.prog);
+}
+
+Circuit noiseless_copy(const Circuit &c) {
+    Circuit out;
+    for (const Instruction &op : c.ops) {
+        const uint32_t flags = gate_info(op.gate).flags;
+        if (op.gate == GFS_HERALDED_ERASE || op.gate == GFS_HERALDED_PAULI_CHANNEL_1) {
+            Instruction pad;
+            pad.gate = GFS_MPAD;
+            pad.targets.assign(op.targets.size(), 0u);
+            out.ops.push_back(pad);
+        } else if (flags & GFS_F_RESULTS) {
+            Instruction m = op;
+            m.args.clear();
+            out.ops.push_back(m);
+        } else if (!(flags & GFS_F_NOISY)) {
+            out.ops.push_back(op);
+        }
+    }
+    for (const Circuit &b : c.blocks) {
+        out.blocks.push_back(noiseless_copy(b));
+    }
+    return out;
 }
 
 }  // namespace gfs

@@ -22,6 +22,7 @@ struct Program {
     uint64_t num_detectors = 0;
     uint64_t num_observables = 0;
     uint64_t num_measurements = 0;
+    uint64_t num_sweep_bits = 0;  // columns of the sweep table read by sweep feedback (LowerOptions::sweep)
     uint32_t max_loop_depth = 0;
     double work = 0;  // estimated cost of one 128-shot block (orders circuits in a batched launch)
     // Detection sampling: the start-of-shot Z randomization never reaches an output (the kernel may start
@@ -40,9 +41,22 @@ struct Program {
     CircuitStats stats;
 };
 
+struct LowerOptions {
+    // Frames start at zero and measurements / resets draw no randomization (the reference's
+    // guarantee_anticommutation_via_frame_randomization = false, frame_simulator.h:65).
+    bool no_randomization = false;
+    // Sweep-controlled Paulis become OP_FEEDBACK entries reading KernelArgs.sweep (the samplers leave them out:
+    // their sweep bits are all zero).
+    bool sweep = false;
+};
+
 // Throws std::invalid_argument (bad circuit) or std::out_of_range (lookback before the beginning of
 // time), mirroring the reference's errors for the same circuits.
-Program lower(const Circuit &circuit, SampleMode mode);
+Program lower(const Circuit &circuit, SampleMode mode, const LowerOptions &opts = LowerOptions());
+
+// The reference's Circuit::aliased_noiseless_circuit (src/stim/circuit/circuit.cc:775-807): noise instructions
+// dropped, heralded errors replaced by MPAD of zeros (same number of results), result-flip probabilities removed.
+Circuit noiseless_copy(const Circuit &c);
 
 constexpr uint64_t kMaxNoiseOccurrences = 1u << 16;
 

@@ -9,9 +9,12 @@
 // three kernels per chunk of shots: shot-major input bits into 128-shot measurement rows, the XOR fold, and
 // the usual shot-major output transpose.
 //
-// Sweep bits: the reference's frame simulator turns sweep-controlled Paulis into extra flips.  Without sweep
-// data every sweep bit is zero and those flips vanish, which is the case handled here; a circuit with
-// sweep-controlled operations rejects explicit sweep data (gfs_m2d_convert documents this).
+// Sweep bits: the reference's frame simulator turns sweep-controlled Paulis into extra flips of measurement
+// results (and of observables' Pauli terms).  Without sweep data, or with all-zero sweep bits, those flips
+// vanish and the fold is the whole answer.  Otherwise the frame kernel runs the circuit's noiseless copy with
+// no randomization (the reference's aliased_noiseless_circuit and
+// guarantee_anticommutation_via_frame_randomization = false) over the chunk's sweep table, and the fold XORs
+// its detector and observable rows into the outputs.
 #include "sampler.h"
 
 using namespace gfs_rt;
@@ -24,7 +27,8 @@ struct gfs_m2d {
     bool sweep_controlled = false;  // the circuit has sweep-controlled operations
     std::vector<uint32_t> off, idx;
     std::vector<uint8_t> expect;
-    DevBuf d_off, d_idx, d_expect, in_buf, rows_buf, det_buf, obs_buf, out_buf;
+    DevBuf d_off, d_idx, d_expect, in_buf, rows_buf, det_buf, obs_buf, out_buf, sweep_in, sweep_rows;
+    std::unique_ptr<gfs_sampler> sweep_sim;  // sweep-controlled circuits: the noiseless frame program
 
     ~gfs_m2d() {
         if (stream) {
@@ -115,6 +119,17 @@ void create(gfs_m2d *m, const gfs_circuit *c, const uint8_t *ref, int device) {
     l.obs.resize(m->O);
     m->num_sweep_bits = l.sweep_bits;
     m->sweep_controlled = l.sweep_controlled;
+    if (l.sweep_controlled) {
+        gfs::LowerOptions opts;
+        opts.no_randomization = true;
+        opts.sweep = true;
+        m->sweep_sim = std::make_unique<gfs_sampler>();
+        m->sweep_sim->init_program(gfs::lower(gfs::noiseless_copy(c->circuit), gfs::SampleMode::DETECTIONS, opts),
+                                   GFS_MODE_DETECTIONS, 0, device);
+        if (m->sweep_sim->prog.num_sweep_bits > m->num_sweep_bits) {
+            throw std::logic_error("sweep bit count mismatch in the converter");
+        }
+    }
     const uint64_t n = m->D + m->O;
     m->off.assign(1, 0);
     m->expect.assign((n + 7) / 8, 0);
@@ -165,17 +180,16 @@ void convert(gfs_m2d *m, uint64_t shots, const uint8_t *meas, uint64_t meas_stri
     if (meas_stride < mrow) {
         throw std::invalid_argument("measurement row stride too small");
     }
+    const uint64_t srow = (m->num_sweep_bits + 7) / 8;
+    bool use_sweep = false;  // some sweep bit is set and some operation reads one
     if (sweep && m->sweep_controlled) {
-        bool any = false;
-        const uint64_t srow = (m->num_sweep_bits + 7) / 8;
-        for (uint64_t s = 0; s < shots && !any; s++) {
-            for (uint64_t b = 0; b < srow && !any; b++) {
-                any = sweep[s * sweep_stride + b] != 0;
-            }
+        if (sweep_stride < srow) {
+            throw std::invalid_argument("sweep row stride too small");
         }
-        if (any) {
-            throw std::invalid_argument(
-                "the GPU converter does not support nonzero sweep bits on circuits with sweep-controlled operations");
+        for (uint64_t s = 0; s < shots && !use_sweep; s++) {
+            for (uint64_t b = 0; b < srow && !use_sweep; b++) {
+                use_sweep = sweep[s * sweep_stride + b] != 0;
+            }
         }
     }
     const bool packed = flags & GFS_BIT_PACKED;
@@ -198,6 +212,11 @@ void convert(gfs_m2d *m, uint64_t shots, const uint8_t *meas, uint64_t meas_stri
     m->det_buf.ensure(std::max<uint64_t>(16, cb * D * 16), m->device);
     m->obs_buf.ensure(std::max<uint64_t>(16, cb * O * 16), m->device);
     m->out_buf.ensure(std::max<uint64_t>(16, chunk * (drow + orow)), m->device);
+    if (use_sweep) {
+        m->sweep_in.ensure(std::max<uint64_t>(16, chunk * srow), m->device);
+        // Room for the frame kernel's padding blocks (up to four 128-shot blocks per CTA slice).
+        m->sweep_rows.ensure(std::max<uint64_t>(16, (cb + 4) * m->num_sweep_bits * 16), m->device);
+    }
     uint8_t *dout = (uint8_t *)m->out_buf.p, *oout = dout + chunk * drow;
     const uint4 *dt = (const uint4 *)m->det_buf.p, *ot = (const uint4 *)m->obs_buf.p;
     for (uint64_t done = 0; done < shots;) {
@@ -211,6 +230,25 @@ void convert(gfs_m2d *m, uint64_t shots, const uint8_t *meas, uint64_t meas_stri
                          (const uint8_t *)m->d_expect.p, D, O, nblk, (uint4 *)m->det_buf.p, (uint4 *)m->obs_buf.p};
         if (M == 0) {
             ck(cudaMemsetAsync(m->rows_buf.p, 0, 16, m->stream), "memset");
+        }
+        if (use_sweep) {
+            // Sweep rows [block][sweep bit], then the noiseless frame program over them on the sampler's stream.
+            copy2d(m->sweep_in.p, srow, sweep + done * sweep_stride, sweep_stride, srow, cs, cudaMemcpyHostToDevice,
+                   m->stream, "copy sweep bits");
+            gfs::RowsInArgs sa{(const uint8_t *)m->sweep_in.p, srow, cs, m->num_sweep_bits, (uint4 *)m->sweep_rows.p};
+            ck(gfs::launch_rows_from_shots(sa, m->stream), "rows kernel launch");
+            ck(cudaStreamSynchronize(m->stream), "sweep rows");
+            gfs_sampler &sim = *m->sweep_sim;
+            sim.sweep_rows = (const uint4 *)m->sweep_rows.p;
+            sim.nsweep = (uint32_t)m->num_sweep_bits;
+            sim.run_frame(nblk, 0);
+            ck(cudaStreamSynchronize(sim.stream), "sweep frames");
+            sim.sweep_rows = nullptr;
+            if (sim.check_status()) {
+                throw std::logic_error("noiseless frame program reported a hit-list overflow");
+            }
+            fa.base_dets = (const uint4 *)sim.det_tmp.p;
+            fa.base_obs = (const uint4 *)sim.obs_tmp.p;
         }
         ck(gfs::launch_fold(fa, m->stream), "fold kernel launch");
         auto tr = [&](const uint4 *s0, uint64_t n0, const uint4 *s1, uint64_t n1, uint8_t *out, uint64_t stride) {

@@ -17,7 +17,8 @@ enum OpCode : uint32_t {
     OP_LOOP_END,     // n = body length in ops
     OP_1Q,           // sub = K1_*; pool[a+i] = row
     OP_2Q,           // sub = K2_*; pool[a+2i], pool[a+2i+1] = rows
-    OP_FEEDBACK,     // pool[a+2i] = lookback, pool[a+2i+1] = row | mask<<24 (1 = x, 2 = z)
+    OP_FEEDBACK,     // pool[a+2i] = lookback (or kFeedbackSweep | sweep bit), pool[a+2i+1] = row | mask<<24
+                     // (1 = x, 2 = z)
     OP_MEASURE,      // sub = KM_*; pool[a+i] = row; b = first randomization unit
     OP_RESET,        // sub = KR_*; pool[a+i] = row; b = first randomization unit
     OP_RECORD_ZERO,  // append n zero results (MPAD, herald slots)
@@ -108,6 +109,7 @@ struct alignas(16) NoiseOcc {
 static_assert(sizeof(NoiseOcc) == 32, "NoiseOcc layout");
 
 constexpr uint32_t kFeedbackX = 1, kFeedbackZ = 2;
+constexpr uint32_t kFeedbackSweep = 1u << 31;  // OP_FEEDBACK source: column of the sweep table, not a lookback
 constexpr uint32_t kTermRecord = 1u << 31, kTermX = 1u << 30, kTermZ = 1u << 29;
 constexpr uint32_t kRowMask = (1u << 24) - 1;
 constexpr int kMaxLoopDepth = 16;

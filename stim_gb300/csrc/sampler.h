@@ -118,6 +118,8 @@ struct gfs_sampler {
     DevBuf d_ops, d_pool, d_tables, d_chans, d_orig, d_status;
     DevBuf det_tmp, obs_tmp, meas_tmp, out_tmp, ref_bits, ring_buf;
     DevBuf feed_rows, feed_compact, feed_aux;  // gfs_sample_for_decoder (feed.cc)
+    const uint4 *sweep_rows = nullptr;  // [local block][nsweep] sweep bits for the next run_frame (m2d.cc)
+    uint32_t nsweep = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;  // device->host copies of host-destination chunks
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -267,11 +269,17 @@ struct gfs_sampler {
     }
 
     void init(const gfs_circuit *c, uint32_t m, uint64_t sd, int dev) {
+        init_program(gfs::lower(c->circuit, m == GFS_MODE_MEASUREMENTS ? gfs::SampleMode::MEASUREMENTS
+                                                                     : gfs::SampleMode::DETECTIONS),
+                     m, sd, dev);
+    }
+
+    // A sampler over an already lowered program (e.g. the converter's noiseless, sweep-reading one).
+    void init_program(gfs::Program &&p, uint32_t m, uint64_t sd, int dev) {
         device = dev;
         mode = m;
         seed = sd;
-        prog = gfs::lower(c->circuit, m == GFS_MODE_MEASUREMENTS ? gfs::SampleMode::MEASUREMENTS
-                                                               : gfs::SampleMode::DETECTIONS);
+        prog = std::move(p);
         int count = 0;
         ck(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
         if (dev < 0 || dev >= count) {
@@ -381,6 +389,8 @@ struct gfs_sampler {
         a.chans = (const gfs::DevChan *)d_chans.p;
         a.qubit_orig = (const uint32_t *)d_orig.p;
         a.reset_zero = prog.reset_norand ? 1u : 0u;
+        a.sweep = sweep_rows;
+        a.nsweep = nsweep;
         a.nrows = prog.num_rows;
         a.ring = prog.ring;
         a.nobs = (uint32_t)prog.num_observables;

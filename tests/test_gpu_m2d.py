@@ -54,15 +54,16 @@ def test_m2d_argument_errors_match_reference():
     assert conv.convert(measurements=np.zeros((0, 2), dtype=np.bool_), append_observables=True).shape == (0, 2)
 
 
-def test_m2d_ignores_zero_sweep_bits_and_rejects_others_on_swept_circuits():
+def test_m2d_sweep_bit_flips_the_results_it_controls():
     c = stim_gb300.Circuit("CX sweep[0] 0\nM 0\nDETECTOR rec[-1]")
     conv = c.compile_m2d_converter()
     meas = np.array([[0], [1]], dtype=np.uint8)
     zero = np.zeros((2, 1), dtype=np.uint8)
     d = conv.convert(measurements=meas, sweep_bits=zero, append_observables=False, bit_packed=True)
     np.testing.assert_array_equal(d, meas)
-    with pytest.raises(ValueError, match="sweep"):
-        conv.convert(measurements=meas, sweep_bits=np.ones((2, 1), dtype=np.uint8), append_observables=False)
+    d = conv.convert(measurements=meas, sweep_bits=np.ones((2, 1), dtype=np.uint8), append_observables=False,
+                     bit_packed=True)
+    np.testing.assert_array_equal(d, meas ^ 1)
 
 
 @pytest.mark.parametrize("family,d,p,shots", [
@@ -80,3 +81,59 @@ def test_m2d_of_sampled_measurements_equals_detection_sampler(family, d, p, shot
     np.testing.assert_array_equal(got_d, want_d)
     np.testing.assert_array_equal(got_o, want_o)
     assert got_d.any()
+
+
+from test_m2d_oracle import load_m2d_sweep, m2d_sweep_cases  # noqa: E402
+
+
+@pytest.mark.parametrize("name", m2d_sweep_cases())
+def test_m2d_sweep_bits_match_reference_cli(name):
+    g = load_m2d_sweep(name)
+    D, O, S = int(g["num_detectors"]), int(g["num_observables"]), int(g["num_sweep_bits"])
+    c = stim_gb300.Circuit(str(g["circuit"]))
+    conv = c.compile_m2d_converter()
+    assert conv.num_sweep_bits == S
+    out = conv.convert(measurements=g["meas"], sweep_bits=g["sweep"], append_observables=True, bit_packed=True)
+    np.testing.assert_array_equal(out, g["out"])
+    # Bool sweep input, separate observables.
+    want_d, want_o = split_appended(g["out"], D, O)
+    d, o = conv.convert(measurements=g["meas"], sweep_bits=unpack(g["sweep"], S), separate_observables=True,
+                        append_observables=False)
+    np.testing.assert_array_equal(d, want_d)
+    np.testing.assert_array_equal(o, want_o)
+
+
+def _swept_circuit():
+    text = workloads.code_circuit("surface_code:rotated_memory_x", 7, 7, 0.005)
+    lines = text.splitlines()
+    out = []
+    for k, line in enumerate(lines):
+        out.append(line)
+        if line.strip().startswith(("CX ", "H ")) and k % 2 == 0:
+            out.append(f"CX sweep[{k % 11}] {k % 97}")
+            out.append(f"CZ sweep[{(k + 3) % 11}] {(k * 7) % 97}")
+    return "\n".join(out) + "\n"
+
+
+def test_m2d_sweep_is_affine_at_scale():
+    # Over GF(2) the conversion is affine in (measurements, sweep bits):
+    # out(m, s) = out(m, 0) ^ out(0, s) ^ out(0, 0).  150,000 shots take three converter chunks.
+    c = stim_gb300.Circuit(_swept_circuit())
+    conv = c.compile_m2d_converter()
+    S = conv.num_sweep_bits
+    assert S == 11
+    shots = 150_000
+    rng = np.random.default_rng(8)
+    m = rng.integers(0, 256, (shots, (c.num_measurements + 7) // 8), dtype=np.uint8)
+    s = rng.integers(0, 256, (shots, (S + 7) // 8), dtype=np.uint8)
+    s[:, -1] &= (1 << (S % 8)) - 1
+    zm, zs = np.zeros_like(m), np.zeros_like(s)
+
+    def conv_(mm, ss):
+        return conv.convert(measurements=mm, sweep_bits=ss, append_observables=True, bit_packed=True)
+
+    ms, m0, s0, z = conv_(m, s), conv_(m, zs), conv_(zm, s), conv_(zm, zs)
+    np.testing.assert_array_equal(ms, m0 ^ s0 ^ z)
+    assert (s0 != z).any()   # the sweep bits flip something
+    # Zero sweep data is the same as none.
+    np.testing.assert_array_equal(m0, conv.convert(measurements=m, append_observables=True, bit_packed=True))

@@ -51,3 +51,32 @@ def test_m2d_fixtures_cover_sampled_and_random_rows():
     half = d.shape[0] // 2
     assert d[:half].mean() < 0.1  # sampled rows: few detection events
     assert 0.3 < d[half:].mean() < 0.7  # random rows: about half
+
+
+M2D_SWEEP_DIR = os.path.join(GOLDEN_DIR, "m2d_sweep")
+
+
+def m2d_sweep_cases():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(M2D_SWEEP_DIR, "*.npz")))
+
+
+def load_m2d_sweep(name):
+    return np.load(os.path.join(M2D_SWEEP_DIR, name + ".npz"))
+
+
+@pytest.mark.parametrize("name", m2d_sweep_cases())
+def test_sweep_fixtures_agree_with_oracle_where_sweep_bits_are_zero(name):
+    # The oracle's converter has no sweep data; on the shots whose sweep rows are all zero the reference's
+    # sweep-aware output must equal it (pins the fixtures' measurement / reference-sample side).
+    g = load_m2d_sweep(name)
+    D, O = int(g["num_detectors"]), int(g["num_observables"])
+    zero = ~g["sweep"].any(axis=1)
+    assert zero.sum() >= 7
+    d, o = OracleCircuit(str(g["circuit"])).m2d(g["meas"][zero], g["ref_sample"])
+    want_d, want_o = split_appended(g["out"][zero], D, O)
+    np.testing.assert_array_equal(unpack(d, D), want_d)
+    np.testing.assert_array_equal(unpack(o, O), want_o)
+    # And the sweep data matters on the other shots (the fixtures exercise it).
+    dd, oo = OracleCircuit(str(g["circuit"])).m2d(g["meas"][~zero], g["ref_sample"])
+    got = np.concatenate([unpack(dd, D), unpack(oo, O)], axis=1)
+    assert (got != np.concatenate(split_appended(g["out"][~zero], D, O), axis=1)).any()
