@@ -315,6 +315,25 @@ gfs_status gfs_m2d_stats(const gfs_m2d *m, uint64_t *stats4);
 gfs_status gfs_m2d_convert(gfs_m2d *m, uint64_t shots, const uint8_t *meas, uint64_t meas_stride,
                            const uint8_t *sweep, uint64_t sweep_stride, uint32_t flags, uint8_t *dets,
                            uint64_t dets_stride, uint8_t *obs, uint64_t obs_stride);
+/*
+ * File to file (replaces CompiledMeasurementsToDetectionEventsConverter.convert_file,
+ * measurements_to_detection_events.pybind.cc:45-77, and the CLI's `stim m2d`): measurement records (and, when
+ * sweep_path is non-null, as many sweep records) in one of the result formats "01", "b8", "r8", "hits", "dets",
+ * "ptb64" (null format = "01"); detection events written to dets_path (observables appended when
+ * append_observables != 0) and observables to obs_path when non-null.  The reference's reader and writer error
+ * messages.
+ */
+/*
+ * Host only (replaces stim.read_shot_data_file, src/stim/io/read_write.pybind.cc:97-145): the records of a result
+ * file, each num_measurements + num_detectors + num_observables bits (dets tokens M / D / L in that order),
+ * bit-packed into `out` (ceil(bits / 8) bytes per record, room for capacity_shots records); *shots = records read.
+ */
+gfs_status gfs_read_shot_data_file(const char *path, const char *format, uint64_t num_measurements,
+                                   uint64_t num_detectors, uint64_t num_observables, uint8_t *out,
+                                   uint64_t capacity_shots, uint64_t *shots);
+gfs_status gfs_m2d_convert_file(gfs_m2d *m, const char *meas_path, const char *meas_format, const char *sweep_path,
+                                const char *sweep_format, const char *dets_path, const char *dets_format,
+                                int append_observables, const char *obs_path, const char *obs_format);
 
 /*
  * Detector-error-model sampling (replaces DemSampler<W>, src/stim/simulators/dem_sampler.inl:27-77, behind

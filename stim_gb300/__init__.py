@@ -25,7 +25,7 @@ from ._native import check, lib
 
 __all__ = ["shard_range", "Circuit", "CompiledDetectorSampler", "CompiledMeasurementSampler",
            "CompiledMeasurementsToDetectionEventsConverter", "DetectorErrorModel", "CompiledDemSampler",
-           "BatchSampler", "Server", "device_count"]
+           "BatchSampler", "Server", "device_count", "read_shot_data_file"]
 
 
 def device_count() -> int:
@@ -51,6 +51,36 @@ def _seed_value(seed):
     if isinstance(seed, bool) or not isinstance(seed, (int, np.integer)) or not (0 <= int(seed) < 2**64):
         raise ValueError("Expected seed to be None or a 64 bit unsigned integer.")
     return int(seed)
+
+
+def read_shot_data_file(*, path, format: str = "01", num_measurements=None, num_detectors=None,
+                        num_observables=None, separate_observables: bool = False, bit_packed: bool = False):
+    """Reads a result file (formats "01", "b8", "r8", "ptb64", "hits", "dets") as the reference's
+    stim.read_shot_data_file does (src/stim/io/read_write.pybind.cc:97-145): records of num_measurements +
+    num_detectors + num_observables bits; bool arrays, or bit-packed uint8 rows; observables split off with
+    separate_observables."""
+    if num_measurements is None and num_detectors is None and num_observables is None:
+        raise ValueError("Must specify num_measurements, num_detectors, num_observables.")
+    nm, nd, no = (int(v or 0) for v in (num_measurements, num_detectors, num_observables))
+    n = nm + nd + no
+    nb = (n + 7) // 8
+    p = _path(path)
+    size = os.path.getsize(p.decode()) if os.path.exists(p.decode()) else 0
+    # An upper bound on the records a file of this size can hold in this format.
+    cap = {"b8": size // nb if nb else 0, "01": size // (n + 1), "ptb64": (size // (8 * n)) * 64 if n else 0,
+           "dets": size // 5}.get(str(format), size) + 1
+    buf = np.zeros((cap, max(1, nb)), dtype=np.uint8)
+    shots = ctypes.c_uint64()
+    check(lib().gfs_read_shot_data_file(p, str(format).encode(), nm, nd, no, _ptr(buf), cap, ctypes.byref(shots)))
+    rows = buf[:shots.value, :nb]
+
+    def part(lo, count):
+        bits = np.unpackbits(rows, axis=1, bitorder="little")[:, lo:lo + count].astype(bool)
+        return np.packbits(bits, axis=1, bitorder="little") if bit_packed else bits
+
+    if separate_observables:
+        return part(0, n - no), part(n - no, no)
+    return part(0, n)
 
 
 class Circuit:
@@ -428,6 +458,20 @@ class CompiledMeasurementsToDetectionEventsConverter:
         if separate:
             return dets, obs
         return dets
+
+
+    def convert_file(self, *, measurements_filepath, measurements_format: str = "01", sweep_bits_filepath=None,
+                     sweep_bits_format: str = "01", detection_events_filepath, detection_events_format: str = "01",
+                     append_observables: bool = False, obs_out_filepath=None, obs_out_format: str = "01") -> None:
+        """Reads measurement data from a file and writes detection events to another file, as the reference's
+        convert_file does (measurements_to_detection_events.pybind.cc:45-77, 211-222); formats "01", "b8", "r8",
+        "ptb64", "hits", "dets"."""
+        check(lib().gfs_m2d_convert_file(
+            self._h, _path(measurements_filepath), str(measurements_format).encode(),
+            _path(sweep_bits_filepath) if sweep_bits_filepath is not None else None,
+            str(sweep_bits_format).encode(), _path(detection_events_filepath),
+            str(detection_events_format).encode(), 1 if append_observables else 0,
+            _path(obs_out_filepath) if obs_out_filepath is not None else None, str(obs_out_format).encode()))
 
 
 class DetectorErrorModel:

@@ -8,6 +8,7 @@
 // 64-bit word per bit position.
 #include "formats.h"
 
+#include <algorithm>
 #include <cinttypes>
 #include <stdexcept>
 #include <string>
@@ -131,6 +132,247 @@ void write_rows(FILE *out, Format f, const uint8_t *rows, uint64_t stride, uint6
         }
         fwrite(s.data(), 1, s.size(), out);
     }
+}
+
+
+// ---- Readers (convert_file) ----
+
+namespace {
+
+// Decimal digits starting at the next character; `next` receives the first character after them.
+bool read_uint(FILE *in, uint64_t &value, int &next) {
+    next = getc(in);
+    if (next < '0' || next > '9') {
+        return false;
+    }
+    value = 0;
+    while (next >= '0' && next <= '9') {
+        value = value * 10 + (uint64_t)(next - '0');
+        next = getc(in);
+    }
+    return true;
+}
+
+inline void set_bit(uint8_t *row, uint64_t k) {
+    row[k >> 3] |= (uint8_t)(1u << (k & 7));
+}
+
+}  // namespace
+
+RowReader::RowReader(FILE *in_, Format f_, uint64_t nm_, uint64_t nd_, uint64_t nl_)
+    : in(in_), f(f_), nm(nm_), nd(nd_), nl(nl_), n(nm_ + nd_ + nl_) {
+}
+
+bool RowReader::empty_records() const {
+    return (f == Format::B8 || f == Format::PTB64) && n == 0;
+}
+
+bool RowReader::read(uint8_t *row) {
+    switch (f) {
+        case Format::F01:
+            return read_01(row);
+        case Format::B8:
+            return read_b8(row);
+        case Format::HITS:
+            return read_hits(row);
+        case Format::R8:
+            return read_r8(row);
+        case Format::DETS:
+            return read_dets(row);
+        default:
+            return read_ptb64(row);
+    }
+}
+
+bool RowReader::read_01(uint8_t *row) {
+    std::fill(row, row + (n + 7) / 8, 0);
+    for (uint64_t k = 0; k < n; k++) {
+        const int b = getc(in);
+        if (b == '1') {
+            set_bit(row, k);
+        } else if (b == '0') {
+        } else if (b == EOF && k == 0) {
+            return false;
+        } else if (b == EOF || b == '\r' || b == '\n') {
+            throw std::invalid_argument("01 data ended in middle of record at byte position " + std::to_string(k) +
+                                        ".\nExpected bits per record was " + std::to_string(n) + ".");
+        } else {
+            throw std::invalid_argument("Unexpected character in 01 format data: '" + std::to_string(b) + "'.");
+        }
+    }
+    int last = getc(in);
+    if (n == 0 && last == EOF) {
+        return false;
+    }
+    if (last == '\r') {
+        last = getc(in);
+    }
+    if (last != '\n') {
+        throw std::invalid_argument("01 data didn't end with a newline after the expected data length of '" +
+                                    std::to_string(n) + "'.");
+    }
+    return true;
+}
+
+bool RowReader::read_b8(uint8_t *row) {
+    const uint64_t nb = (n + 7) / 8;
+    const size_t nr = fread(row, 1, nb, in);
+    if (nr == 0) {
+        return false;
+    }
+    if (nr != nb) {
+        throw std::invalid_argument("b8 data ended in middle of record at byte position " + std::to_string(nr) +
+                                    ".\nExpected bytes per record was " + std::to_string(nb) + " (" +
+                                    std::to_string(n) + " bits padded).");
+    }
+    return true;
+}
+
+bool RowReader::read_hits(uint8_t *row) {
+    std::fill(row, row + (n + 7) / 8, 0);
+    const char *bad = "HITS data wasn't comma-separated integers terminated by a newline.";
+    bool first = true;
+    for (;;) {
+        uint64_t v = 0;
+        int next = 0;
+        if (!read_uint(in, v, next)) {
+            if (first && next == EOF) {
+                return false;
+            }
+            if (first && next == '\r') {
+                next = getc(in);
+            }
+            if (first && next == '\n') {
+                return true;
+            }
+            throw std::invalid_argument(bad);
+        }
+        if (v >= n) {
+            throw std::invalid_argument("hit index is too large.");
+        }
+        row[v >> 3] ^= (uint8_t)(1u << (v & 7));
+        first = false;
+        if (next == '\r') {
+            next = getc(in);
+            if (next == '\n') {
+                return true;
+            }
+        } else if (next == '\n') {
+            return true;
+        }
+        if (next != ',') {
+            throw std::invalid_argument(bad);
+        }
+    }
+}
+
+bool RowReader::read_r8(uint8_t *row) {
+    int c = getc(in);
+    if (c == EOF) {
+        return false;
+    }
+    std::fill(row, row + (n + 7) / 8, 0);
+    uint64_t pos = 0;
+    for (;;) {
+        pos += (uint64_t)c;
+        if (c != 255) {
+            if (pos < n) {
+                set_bit(row, pos);
+                pos++;
+            } else if (pos == n) {
+                return true;
+            } else {
+                throw std::invalid_argument("r8 data jumped past expected end of encoded data. Expected to decode " +
+                                            std::to_string(n) + " bits.");
+            }
+        }
+        c = getc(in);
+        if (c == EOF) {
+            throw std::invalid_argument("End of file before end of r8 data. Expected to decode " + std::to_string(n) +
+                                        " bits.");
+        }
+    }
+}
+
+bool RowReader::read_dets(uint8_t *row) {
+    for (;;) {
+        const int c = getc(in);
+        if (c == ' ' || c == '\n' || c == '\r' || c == '\t') {
+            continue;
+        }
+        if (c == EOF) {
+            return false;
+        }
+        if (c != 's' || getc(in) != 'h' || getc(in) != 'o' || getc(in) != 't') {
+            throw std::invalid_argument("DETS data didn't start with 'shot'");
+        }
+        break;
+    }
+    std::fill(row, row + (n + 7) / 8, 0);
+    int c = getc(in);
+    for (;;) {
+        if (c == '\r') {
+            c = getc(in);
+        }
+        if (c == '\n' || c == EOF) {
+            return true;
+        }
+        if (c != ' ') {
+            throw std::invalid_argument("DETS data wasn't single-space-separated with no trailing spaces.");
+        }
+        c = getc(in);
+        uint64_t offset, length;
+        if (c == 'M') {
+            offset = 0;
+            length = nm;
+        } else if (c == 'D') {
+            offset = nm;
+            length = nd;
+        } else if (c == 'L') {
+            offset = nm + nd;
+            length = nl;
+        } else {
+            throw std::invalid_argument("Unrecognized DETS prefix. Expected M or D or L not '" + std::to_string(c) +
+                                        "'");
+        }
+        const char prefix = (char)c;
+        uint64_t v = 0;
+        if (!read_uint(in, v, c)) {
+            throw std::invalid_argument("DETS data had a value prefix (M or D or L) not followed by an integer.");
+        }
+        if (v >= length) {
+            throw std::invalid_argument("DETS data had a value larger than expected. Got " + std::string(1, prefix) +
+                                        std::to_string(v) + " but expected length of " + std::string(1, prefix) +
+                                        " space to be " + std::to_string(length) + ".");
+        }
+        set_bit(row, offset + v);
+    }
+}
+
+bool RowReader::read_ptb64(uint8_t *row) {
+    if (group_left == 0) {
+        const uint64_t nb = n * 8;
+        group.resize(nb);
+        const size_t nr = nb ? fread(group.data(), 1, nb, in) : 0;
+        if (nr == 0) {
+            return false;
+        }
+        if (nr != nb) {
+            throw std::invalid_argument("ptb64 data ended in middle of 64 record group at byte position " +
+                                        std::to_string(nr) + ".\nExpected bytes per 64 records was " +
+                                        std::to_string(nb) + " (" + std::to_string(n) + " bits padded).");
+        }
+        group_left = 64;
+    }
+    const uint32_t s = 64 - group_left;  // record within the group
+    std::fill(row, row + (n + 7) / 8, 0);
+    for (uint64_t k = 0; k < n; k++) {
+        if ((group[8 * k + (s >> 3)] >> (s & 7)) & 1) {
+            set_bit(row, k);
+        }
+    }
+    group_left--;
+    return true;
 }
 
 }  // namespace gfs

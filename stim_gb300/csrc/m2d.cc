@@ -15,6 +15,7 @@
 // no randomization (the reference's aliased_noiseless_circuit and
 // guarantee_anticommutation_via_frame_randomization = false) over the chunk's sweep table, and the fold XORs
 // its detector and observable rows into the outputs.
+#include "formats.h"
 #include "sampler.h"
 
 using namespace gfs_rt;
@@ -284,9 +285,136 @@ void convert(gfs_m2d *m, uint64_t shots, const uint8_t *meas, uint64_t meas_stri
     }
 }
 
+// Files opened like the reference's RaiiFile (src/stim/io/raii_file.cc:44-66): no path, no file.
+struct PathFile {
+    FILE *f = nullptr;
+    PathFile(const char *path, const char *mode) {
+        if (path && *path) {
+            f = fopen(path, mode);
+            if (!f) {
+                throw std::invalid_argument("Failed to open '" + std::string(path) + "' for " +
+                                            (*mode == 'r' ? "reading." : "writing."));
+            }
+        }
+    }
+    ~PathFile() {
+        if (f) {
+            fclose(f);
+        }
+    }
+};
+
+// CompiledMeasurementsToDetectionEventsConverter.convert_file (measurements_to_detection_events.pybind.cc:45-77)
+// through stream_measurements_to_detection_events_helper (measurements_to_detection_events.inl:190-294): records
+// are read in chunks of 65,536 shots (measurements and, when given, as many sweep records), converted on the
+// device by convert() and written in the requested formats, detection events with D / L prefixes and
+// observables (obs_path) with L prefixes.
+void convert_file(gfs_m2d *m, const char *meas_path, const char *meas_format, const char *sweep_path,
+                  const char *sweep_format, const char *dets_path, const char *dets_format, bool append,
+                  const char *obs_path, const char *obs_format) {
+    const gfs::Format fin = gfs::parse_format(meas_format ? meas_format : "01");
+    const gfs::Format fsweep = gfs::parse_format(sweep_format ? sweep_format : "01");
+    const gfs::Format fout = gfs::parse_format(dets_format ? dets_format : "01");
+    PathFile in(meas_path, "rb"), obs_out(obs_path, "wb"), sweep_in(sweep_path, "rb"), dets_out(dets_path, "wb");
+    const gfs::Format fobs = gfs::parse_format(obs_format ? obs_format : "01");
+    if (!in.f) {
+        throw std::invalid_argument("measurements_filepath is required");
+    }
+    if (!dets_out.f) {
+        throw std::invalid_argument("detection_events_filepath is required");
+    }
+    const uint64_t M = m->M, D = m->D, O = m->O, S = m->num_sweep_bits;
+    gfs::RowReader meas_reader(in.f, fin, M);
+    // The reference's record writers cannot write ptb64 one record at a time (measure_record_writer.cc:33-34).
+    if ((obs_out.f && fobs == gfs::Format::PTB64) || fout == gfs::Format::PTB64) {
+        throw std::invalid_argument("SAMPLE_FORMAT_PTB64 incompatible with SingleMeasurementRecord");
+    }
+    std::unique_ptr<gfs::RowReader> sweep_reader;
+    if (sweep_in.f) {
+        sweep_reader = std::make_unique<gfs::RowReader>(sweep_in.f, fsweep, S);
+    }
+    if (meas_reader.empty_records()) {
+        throw std::invalid_argument(
+            "Can't tell how many shots are in the measurement data.\n"
+            "The circuit has no measurements and the measurement format encodes empty shots into no bytes.");
+    }
+    const uint64_t chunk = 1 << 16;
+    const uint64_t mrow = (M + 7) / 8, srow = (S + 7) / 8, drow = (D + (append ? O : 0) + 7) / 8, orow = (O + 7) / 8;
+    std::vector<uint8_t> meas(chunk * mrow + 1), sweep(chunk * srow + 1), dets(chunk * drow + 1), obs(chunk * orow + 1);
+    const bool sweep_rows = sweep_reader && !sweep_reader->empty_records();
+    uint64_t total = 0;
+    for (;;) {
+        uint64_t n = 0;
+        while (n < chunk && meas_reader.read(meas.data() + n * mrow)) {
+            n++;
+        }
+        if (sweep_reader) {
+            uint64_t ns = 0;
+            while (ns < chunk && sweep_reader->read(sweep.data() + ns * srow)) {
+                ns++;
+            }
+            if (ns != n && sweep_rows) {
+                std::string msg = "The sweep data contained a different number of shots than the measurement data.\n";
+                msg += "There was " + std::to_string(n + total) + " shot records total.\n";
+                if (ns < n) {
+                    msg += "But there was " + std::to_string(n + ns) + " sweep records total.";
+                } else {
+                    msg += "But there was at least " + std::to_string(n + ns) + " sweep records.";
+                }
+                throw std::invalid_argument(msg);
+            }
+        }
+        if (n == 0) {
+            break;
+        }
+        total += n;
+        convert(m, n, meas.data(), std::max<uint64_t>(1, mrow), sweep_rows ? sweep.data() : nullptr,
+                std::max<uint64_t>(1, srow), GFS_BIT_PACKED | (append ? GFS_APPEND_OBSERVABLES : 0), dets.data(),
+                std::max<uint64_t>(1, drow), obs_out.f ? obs.data() : nullptr, std::max<uint64_t>(1, orow));
+        gfs::write_rows(dets_out.f, fout, dets.data(), std::max<uint64_t>(1, drow), n, D + (append ? O : 0), 'D', 'L',
+                        D);
+        if (obs_out.f) {
+            gfs::write_rows(obs_out.f, fobs, obs.data(), std::max<uint64_t>(1, orow), n, O, 'L', 'L', 0);
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+gfs_status gfs_read_shot_data_file(const char *path, const char *format, uint64_t num_measurements,
+                                   uint64_t num_detectors, uint64_t num_observables, uint8_t *out,
+                                   uint64_t capacity_shots, uint64_t *shots) {
+    return guarded([&] {
+        const gfs::Format f = gfs::parse_format(format ? format : "01");
+        PathFile in(path, "rb");
+        if (!in.f) {
+            throw std::invalid_argument("path is required");
+        }
+        gfs::RowReader reader(in.f, f, num_measurements, num_detectors, num_observables);
+        const uint64_t nb = (num_measurements + num_detectors + num_observables + 7) / 8;
+        std::vector<uint8_t> row(nb + 1);
+        uint64_t k = 0;
+        while (reader.read(row.data())) {
+            if (k >= capacity_shots) {
+                throw std::invalid_argument("the file holds more records than the output buffer");
+            }
+            std::copy(row.begin(), row.begin() + nb, out + k * nb);
+            k++;
+        }
+        *shots = k;
+    });
+}
+
+gfs_status gfs_m2d_convert_file(gfs_m2d *m, const char *meas_path, const char *meas_format, const char *sweep_path,
+                                const char *sweep_format, const char *dets_path, const char *dets_format,
+                                int append_observables, const char *obs_path, const char *obs_format) {
+    return guarded([&] {
+        convert_file(m, meas_path, meas_format, sweep_path, sweep_format, dets_path, dets_format,
+                     append_observables != 0, obs_path, obs_format);
+    });
+}
 
 gfs_status gfs_m2d_create(const gfs_circuit *c, const uint8_t *ref_sample, int device, gfs_m2d **out) {
     return guarded([&] {

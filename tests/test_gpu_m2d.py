@@ -137,3 +137,51 @@ def test_m2d_sweep_is_affine_at_scale():
     assert (s0 != z).any()   # the sweep bits flip something
     # Zero sweep data is the same as none.
     np.testing.assert_array_equal(m0, conv.convert(measurements=m, append_observables=True, bit_packed=True))
+
+
+from test_m2d_files import FORMATS, OUT_FORMATS, file_cases, load_files  # noqa: E402
+
+
+@pytest.mark.parametrize("name", file_cases())
+def test_convert_file_matches_reference_cli_in_every_format(name, tmp_path):
+    g = load_files(name)
+    conv = stim_gb300.Circuit(str(g["circuit"])).compile_m2d_converter()
+    swept = bool(g["has_sweep"])
+    for fin in FORMATS:
+        meas = tmp_path / f"m.{fin}"
+        g[f"meas_{fin}"].tofile(meas)
+        sweep = None
+        if swept:
+            sweep = tmp_path / f"s.{fin}"
+            g[f"sweep_{fin}"].tofile(sweep)
+        for fout in OUT_FORMATS:
+            out, det, obs = tmp_path / "o", tmp_path / "d", tmp_path / "l"
+            conv.convert_file(measurements_filepath=meas, measurements_format=fin, sweep_bits_filepath=sweep,
+                              sweep_bits_format=fin, detection_events_filepath=out, detection_events_format=fout,
+                              append_observables=True)
+            assert out.read_bytes() == g[f"out_{fout}"].tobytes(), (fin, fout)
+            conv.convert_file(measurements_filepath=meas, measurements_format=fin, sweep_bits_filepath=sweep,
+                              sweep_bits_format=fin, detection_events_filepath=det, detection_events_format=fout,
+                              obs_out_filepath=obs, obs_out_format=fout)
+            assert det.read_bytes() == g[f"det_{fout}"].tobytes(), (fin, fout)
+            assert obs.read_bytes() == g[f"obs_{fout}"].tobytes(), (fin, fout)
+    with pytest.raises(ValueError, match="SAMPLE_FORMAT_PTB64 incompatible"):
+        conv.convert_file(measurements_filepath=tmp_path / "m.b8", measurements_format="b8",
+                          detection_events_filepath=tmp_path / "x", detection_events_format="ptb64")
+    with pytest.raises(ValueError, match="Failed to open"):
+        conv.convert_file(measurements_filepath=tmp_path / "missing.b8", measurements_format="b8",
+                          detection_events_filepath=tmp_path / "x")
+
+
+def test_convert_file_sweep_record_count_must_match(tmp_path):
+    c = stim_gb300.Circuit("CX sweep[0] 0\nM 0\nDETECTOR rec[-1]")
+    conv = c.compile_m2d_converter()
+    (tmp_path / "m.01").write_text("0\n1\n1\n")
+    (tmp_path / "s.01").write_text("1\n1\n")
+    with pytest.raises(ValueError, match="different number of shots"):
+        conv.convert_file(measurements_filepath=tmp_path / "m.01", sweep_bits_filepath=tmp_path / "s.01",
+                          detection_events_filepath=tmp_path / "o.01")
+    (tmp_path / "s.01").write_text("1\n0\n1\n")
+    conv.convert_file(measurements_filepath=tmp_path / "m.01", sweep_bits_filepath=tmp_path / "s.01",
+                      detection_events_filepath=tmp_path / "o.01")
+    assert (tmp_path / "o.01").read_text() == "1\n1\n0\n"
