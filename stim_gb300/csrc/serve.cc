@@ -55,10 +55,19 @@ struct Chunk {
     uint64_t first = 0, shots = 0;  // shot offset within the request (a multiple of 128)
 };
 
+// A batch is split by launch-shape class: circuits whose own sampler takes several 128-shot blocks per CTA
+// (small and medium circuits: wide CTAs, many items per phase) and circuits that take one block per CTA (the
+// largest: shared memory allows few blocks per SM).  Each class runs as its own persistent launch on its own
+// engine and stream, so a batch's shape no longer follows its largest circuit (one shared shape ran a mixed
+// 160-request batch at 513 Gbit/s, the two classes back to back at 765).
+constexpr int kClasses = 2;
+
 struct Slot {
-    gfs_rt::BatchEngine eng;
+    gfs_rt::BatchEngine eng[kClasses];
     gfs_rt::DevBuf staging;  // shot-major rows for host destinations
     std::vector<Chunk> chunks;
+    std::vector<size_t> members[kClasses];  // indices into chunks, per class
+    std::vector<uint64_t> soff;             // staging offset of each chunk (host destinations)
     bool busy = false;
     uint64_t bits = 0;
 };
@@ -107,7 +116,9 @@ struct gfs_server {
         slot_budget = std::max<uint64_t>(hbm_budget / 2, (uint64_t)64 << 20);
         max_chunk = std::max<uint64_t>(128, (chunk_shots ? chunk_shots : (uint64_t)1 << 18) & ~(uint64_t)127);
         for (auto &s : slots) {
-            s.eng.init(device);
+            for (auto &e : s.eng) {
+                e.init(device);
+            }
         }
         worker = std::thread([this] { run(); });
     }
@@ -267,27 +278,48 @@ struct gfs_server {
         return !slot.chunks.empty();
     }
 
+    static int shape_class(const Request &r) {
+        return r.prog->s->shape.blocks_per_cta > 1 ? 0 : 1;
+    }
+
     void launch(Slot &slot) {
         ck(cudaSetDevice(device), "cudaSetDevice");
-        std::vector<const gfs_sampler *> progs;
-        std::vector<gfs_rt::BatchEntry> es(slot.chunks.size());
+        for (int g = 0; g < kClasses; g++) {
+            slot.members[g].clear();
+        }
         uint64_t staging = 0;
         std::vector<uint64_t> soff(slot.chunks.size(), 0);
-        for (size_t k = 0; k < slot.chunks.size(); k++) {
-            const Chunk &c = slot.chunks[k];
-            const Request &r = *c.req;
-            progs.push_back(r.prog->s.get());
-            if (!r.device_out) {
-                soff[k] = staging;
-                staging += c.shots * (pad32(r.drow) * (r.dets ? 1 : 0) + pad32(r.orow) * (r.obs ? 1 : 0));
-            }
-        }
-        slot.staging.ensure(std::max<uint64_t>(16, staging), device);
         slot.bits = 0;
         for (size_t k = 0; k < slot.chunks.size(); k++) {
             const Chunk &c = slot.chunks[k];
             const Request &r = *c.req;
-            gfs_rt::BatchEntry &e = es[k];
+            slot.members[shape_class(r)].push_back(k);
+            if (!r.device_out) {
+                soff[k] = staging;
+                staging += c.shots * (pad32(r.drow) * (r.dets ? 1 : 0) + pad32(r.orow) * (r.obs ? 1 : 0));
+            }
+            slot.bits += c.shots * (r.prog->s->prog.num_detectors + r.prog->s->prog.num_observables);
+        }
+        slot.staging.ensure(std::max<uint64_t>(16, staging), device);
+        slot.soff = std::move(soff);
+        for (int g = 0; g < kClasses; g++) {
+            if (!slot.members[g].empty()) {
+                launch_class(slot, g);
+            }
+        }
+    }
+
+    // One class of the slot's chunks as one persistent launch on the class's engine and stream.
+    void launch_class(Slot &slot, int g) {
+        gfs_rt::BatchEngine &eng = slot.eng[g];
+        const std::vector<size_t> &mem = slot.members[g];
+        std::vector<const gfs_sampler *> progs;
+        std::vector<gfs_rt::BatchEntry> es(mem.size());
+        for (size_t i = 0; i < mem.size(); i++) {
+            const Chunk &c = slot.chunks[mem[i]];
+            const Request &r = *c.req;
+            progs.push_back(r.prog->s.get());
+            gfs_rt::BatchEntry &e = es[i];
             e.prog = r.prog->s.get();
             e.seed = r.seed;
             e.block0 = c.first / 128;
@@ -298,80 +330,107 @@ struct gfs_server {
                 e.obs = r.obs ? r.obs + c.first * r.ostride : nullptr;
                 e.ostride = r.ostride;
             } else {
-                uint8_t *base = (uint8_t *)slot.staging.p + soff[k];
+                uint8_t *base = (uint8_t *)slot.staging.p + slot.soff[mem[i]];
                 e.dets = r.dets ? base : nullptr;
                 e.dstride = pad32(r.drow);
                 e.obs = r.obs ? base + (r.dets ? c.shots * pad32(r.drow) : 0) : nullptr;
                 e.ostride = pad32(r.orow);
             }
-            slot.bits += c.shots * (e.prog->prog.num_detectors + e.prog->prog.num_observables);
         }
-        slot.eng.default_shape(progs);
-        if (slot.eng.prepare(es, {}) == 0) {
+        eng.default_shape(progs);
+        if (eng.prepare(es, {}) == 0) {
+            ck(cudaEventRecord(eng.ev[2], eng.stream), "event");
             return;
         }
-        slot.eng.enqueue_frame();
-        enqueue_transposes(slot, es);
-        for (size_t k = 0; k < slot.chunks.size(); k++) {
-            const Chunk &c = slot.chunks[k];
+        eng.enqueue_frame();
+        enqueue_transposes(slot, g, es);
+        for (size_t i = 0; i < mem.size(); i++) {
+            const Chunk &c = slot.chunks[mem[i]];
             const Request &r = *c.req;
             if (r.device_out) {
                 continue;
             }
             if (r.dets && r.drow) {
-                ck(cudaMemcpy2DAsync(r.dets + c.first * r.dstride, r.dstride, es[k].dets, es[k].dstride, r.drow,
-                                     c.shots, cudaMemcpyDeviceToHost, slot.eng.stream),
+                ck(cudaMemcpy2DAsync(r.dets + c.first * r.dstride, r.dstride, es[i].dets, es[i].dstride, r.drow,
+                                     c.shots, cudaMemcpyDeviceToHost, eng.stream),
                    "copy dets");
             }
             if (r.obs && r.orow) {
-                ck(cudaMemcpy2DAsync(r.obs + c.first * r.ostride, r.ostride, es[k].obs, es[k].ostride, r.orow,
-                                     c.shots, cudaMemcpyDeviceToHost, slot.eng.stream),
+                ck(cudaMemcpy2DAsync(r.obs + c.first * r.ostride, r.ostride, es[i].obs, es[i].ostride, r.orow,
+                                     c.shots, cudaMemcpyDeviceToHost, eng.stream),
                    "copy obs");
             }
         }
-        ck(cudaEventRecord(slot.eng.ev[2], slot.eng.stream), "event");
+        ck(cudaEventRecord(eng.ev[2], eng.stream), "event");
     }
 
-    // Transposes with each entry's own layout flags.
-    void enqueue_transposes(Slot &slot, const std::vector<gfs_rt::BatchEntry> &es) {
-        // Group entries by flags so each group goes through the engine's transpose path.
+    // Transposes with each entry's own layout flags (entries `es` are class g's members in order).
+    void enqueue_transposes(Slot &slot, int g, const std::vector<gfs_rt::BatchEntry> &es) {
+        const std::vector<size_t> &mem = slot.members[g];
         std::vector<gfs_rt::BatchEntry> group(es.size());
         std::vector<uint32_t> flags_seen;
-        for (const Chunk &c : slot.chunks) {
-            if (std::find(flags_seen.begin(), flags_seen.end(), c.req->flags) == flags_seen.end()) {
-                flags_seen.push_back(c.req->flags);
+        for (size_t k : mem) {
+            const uint32_t f = slot.chunks[k].req->flags;
+            if (std::find(flags_seen.begin(), flags_seen.end(), f) == flags_seen.end()) {
+                flags_seen.push_back(f);
             }
         }
         for (uint32_t f : flags_seen) {
-            for (size_t k = 0; k < es.size(); k++) {
-                group[k] = slot.chunks[k].req->flags == f ? es[k] : gfs_rt::BatchEntry{};
-                if (slot.chunks[k].req->flags != f) {
-                    group[k].shots = 0;
+            for (size_t i = 0; i < es.size(); i++) {
+                const bool same = slot.chunks[mem[i]].req->flags == f;
+                group[i] = same ? es[i] : gfs_rt::BatchEntry{};
+                if (!same) {
+                    group[i].shots = 0;
                 }
             }
-            slot.eng.enqueue_transposes(group, f);
+            slot.eng[g].enqueue_transposes(group, f);
+        }
+    }
+
+    // True when every class launched for the slot has finished on the device.
+    bool slot_ready(Slot &slot) {
+        for (int g = 0; g < kClasses; g++) {
+            if (!slot.members[g].empty() && cudaEventQuery(slot.eng[g].ev[2]) == cudaErrorNotReady) {
+                return false;
+            }
+        }
+        return true;
+    }
+
+    void sync_slot(Slot &slot) {
+        for (auto &e : slot.eng) {
+            cudaStreamSynchronize(e.stream);
         }
     }
 
     void complete(Slot &slot) {
-        cudaError_t e = cudaEventSynchronize(slot.eng.ev[2]);
         std::string err;
-        if (e != cudaSuccess) {
-            err = std::string("batch failed: ") + cudaGetErrorString(e);
-        } else {
+        for (int g = 0; g < kClasses; g++) {  // every class's launch has ended before the slot is released
+            if (!slot.members[g].empty()) {
+                cudaError_t e = cudaEventSynchronize(slot.eng[g].ev[2]);
+                if (e != cudaSuccess && err.empty()) {
+                    err = std::string("batch failed: ") + cudaGetErrorString(e);
+                }
+            }
+        }
+        for (int g = 0; g < kClasses && err.empty(); g++) {
+            if (slot.members[g].empty()) {
+                continue;
+            }
+            gfs_rt::BatchEngine &eng = slot.eng[g];
             try {
-                if (slot.eng.check_status()) {
-                    // A hit list overflowed: redo the batch with inline noise (identical results).
-                    slot.eng.force_inline = true;
+                if (eng.check_status()) {
+                    // A hit list overflowed: redo this class with inline noise (identical results).
+                    eng.force_inline = true;
                     try {
-                        launch(slot);
-                        ck(cudaEventSynchronize(slot.eng.ev[2]), "batch redo");
-                        slot.eng.check_status();
+                        launch_class(slot, g);
+                        ck(cudaEventSynchronize(eng.ev[2]), "batch redo");
+                        eng.check_status();
                     } catch (...) {
-                        slot.eng.force_inline = false;
+                        eng.force_inline = false;
                         throw;
                     }
-                    slot.eng.force_inline = false;
+                    eng.force_inline = false;
                 }
             } catch (const std::exception &x) {
                 err = x.what();
@@ -418,7 +477,7 @@ struct gfs_server {
                 try {
                     launch(*to_launch);
                 } catch (const std::exception &x) {
-                    cudaStreamSynchronize(to_launch->eng.stream);
+                    sync_slot(*to_launch);
                     std::lock_guard<std::mutex> lk(mu);
                     for (const Chunk &c : to_launch->chunks) {
                         Request &r = *c.req;
@@ -443,7 +502,7 @@ struct gfs_server {
                 continue;
             }
             const bool both_busy = slots[0].busy && slots[1].busy;
-            if (both_busy || cudaEventQuery(old.eng.ev[2]) != cudaErrorNotReady) {
+            if (both_busy || slot_ready(old)) {
                 complete(old);
             } else {
                 std::unique_lock<std::mutex> lk(mu);
