@@ -1690,6 +1690,31 @@ __global__ void __launch_bounds__(256) transpose_tile_kernel(const TransposeArgs
     // (even row strides, e.g. ceil(detectors / 8) = 1950 bytes) one half-word per lane, others bytes, lane q
     // writing unit 32k + q so that every store instruction covers 32 consecutive units: no funnel shifts,
     // no divergent edge handling.
+    if (packed && nbytes == 4 * (int32_t)kTileWords) {
+        // A full bit-packed tile: 128 bytes per shot row, one store per lane per row (two or four below 4-byte
+        // alignment), no inner loops.
+#pragma unroll 4
+        for (uint32_t s = warp; s < nvalid; s += 8) {
+            const uint32_t *row = tile[s];
+            uint8_t *dst = base + s * t.out_stride;
+            const uint32_t mis = (uint32_t)(uintptr_t)dst & 3u;
+            if (mis == 0) {
+                reinterpret_cast<uint32_t *>(dst)[lane] = row[lane];
+            } else if (mis == 2) {
+                const uint16_t *r16 = reinterpret_cast<const uint16_t *>(row);
+                uint16_t *d16 = reinterpret_cast<uint16_t *>(dst);
+                d16[lane] = r16[lane];
+                d16[lane + 32] = r16[lane + 32];
+            } else {
+                const uint8_t *rb = reinterpret_cast<const uint8_t *>(row);
+#pragma unroll
+                for (uint32_t k = 0; k < 4; k++) {
+                    dst[lane + 32 * k] = rb[lane + 32 * k];
+                }
+            }
+        }
+        return;
+    }
     for (uint32_t s = warp; s < nvalid; s += 8) {
         const uint32_t *row = tile[s];
         uint8_t *dst = base + s * t.out_stride;
