@@ -385,43 +385,66 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def _pinned(shape):
+    import torch
+
+    return torch.empty(shape, dtype=torch.uint8, pin_memory=True).numpy()
+
+
+def _median_ms(fn, steps):
+    """Median wall time of `steps` calls of fn after E2E_WARMUP untimed calls (which touch the arrays' pages)."""
+    times = []
+    for k in range(E2E_WARMUP + steps):
+        t0 = time.perf_counter()
+        fn()
+        if k >= E2E_WARMUP:
+            times.append(time.perf_counter() - t0)
+    return 1e3 * statistics.median(times)
+
+
 def run_m2d(args, local, text):
     """Measurements to detection events (compile_m2d_converter().convert) on the main workload: the
-    measurement sampler's records of `--shots` shots, converted from host numpy arrays into host numpy
-    arrays reused across calls (host->device and device->host copies inside the timed region).  Reports detection-event Gbit/s
-    out and measurement Gbit/s in, and checks the result against the detection sampler with the same seed."""
+    measurement sampler's records of `--shots` shots, converted from host arrays into host arrays reused across
+    calls (host->device and device->host copies inside the timed region; chunks pipelined so that one chunk's
+    copies overlap the next one's).  Headline with page-locked arrays, the same call on pageable numpy arrays
+    beside it.  Reports detection-event Gbit/s out and measurement Gbit/s in, and checks the result against the
+    detection sampler with the same seed."""
     import numpy as np
 
     import stim_gb300
 
     shots = args.shots
     c = stim_gb300.Circuit(text)
-    meas = c.compile_sampler(seed=args.seed, device=local).sample(shots, bit_packed=True)
+    D, O, M = c.num_detectors, c.num_observables, c.num_measurements
+    meas_page = c.compile_sampler(seed=args.seed, device=local).sample(shots, bit_packed=True)
     conv = c.compile_m2d_converter(device=local)
-    times = []
-    d = np.empty((shots, (c.num_detectors + 7) // 8), dtype=np.uint8)
-    o = np.empty((shots, (c.num_observables + 7) // 8), dtype=np.uint8)
-    for k in range(E2E_WARMUP + args.m2d_steps):  # the untimed calls touch the reused output arrays' pages
-        t0 = time.perf_counter()
-        d, o = conv.convert(measurements=meas, separate_observables=True, append_observables=False,
-                            bit_packed=True, dets_out=d, obs_out=o)
-        if k >= E2E_WARMUP:
-            times.append(time.perf_counter() - t0)
+    meas = _pinned(meas_page.shape)
+    meas[...] = meas_page
+    d, o = _pinned((shots, (D + 7) // 8)), _pinned((shots, (O + 7) // 8))
+
+    def call(mm, dd, oo):
+        conv.convert(measurements=mm, separate_observables=True, append_observables=False, bit_packed=True,
+                     dets_out=dd, obs_out=oo)
+
+    ms = _median_ms(lambda: call(meas, d, o), args.m2d_steps)
+    dp, op = np.empty_like(d), np.empty_like(o)
+    ms_page = _median_ms(lambda: call(meas_page, dp, op), args.m2d_steps)
     want_d, want_o = c.compile_detector_sampler(seed=args.seed, device=local).sample(
         shots, separate_observables=True, bit_packed=True)
-    D, O, M = c.num_detectors, c.num_observables, c.num_measurements
-    ms = 1e3 * statistics.median(times)
     return {"workload": f"{shots} shots of {M} measurement bits (the measurement sampler's records) -> {D} "
-                        f"detectors + {O} observables, host arrays in and out",
+                        f"detectors + {O} observables, page-locked host arrays in and out",
             "gbits": shots * (D + O) / (ms / 1e3) / 1e9, "meas_gbits_in": shots * M / (ms / 1e3) / 1e9,
             "ms": ms, "h2d_bytes": int(meas.nbytes), "d2h_bytes": int(d.nbytes + o.nbytes),
-            "equals_detection_sampler": bool(np.array_equal(d, want_d) and np.array_equal(o, want_o))}
+            "pageable": {"gbits": shots * (D + O) / (ms_page / 1e3) / 1e9, "ms": ms_page},
+            "equals_detection_sampler": bool(np.array_equal(d, want_d) and np.array_equal(o, want_o)
+                                             and np.array_equal(dp, want_d) and np.array_equal(op, want_o))}
 
 
 def run_dem(args, local):
     """Detector-error-model sampling (DetectorErrorModel.compile_sampler().sample) of the main workload's
     model (the reference's analyze_errors of the same circuit: 326,897 error mechanisms), `--shots` shots
-    into reused host arrays, device->host copies inside the timed region."""
+    into reused host arrays, device->host copies inside the timed region (pipelined with the next chunk's
+    kernels); page-locked arrays, pageable beside them."""
     import numpy as np
 
     import stim_gb300
@@ -431,18 +454,14 @@ def run_dem(args, local):
     dem = stim_gb300.DetectorErrorModel(workloads.dem_d25_text())
     s = dem.compile_sampler(seed=args.seed, device=local)
     D, O = dem.num_detectors, dem.num_observables
-    d = np.empty((shots, (D + 7) // 8), dtype=np.uint8)
-    o = np.empty((shots, (O + 7) // 8), dtype=np.uint8)
-    times = []
-    for k in range(E2E_WARMUP + args.dem_steps):  # the untimed calls touch the reused output arrays' pages
-        t0 = time.perf_counter()
-        s.sample(shots, bit_packed=True, dets_out=d, obs_out=o)
-        if k >= E2E_WARMUP:
-            times.append(time.perf_counter() - t0)
-    ms = 1e3 * statistics.median(times)
+    d, o = _pinned((shots, (D + 7) // 8)), _pinned((shots, (O + 7) // 8))
+    ms = _median_ms(lambda: s.sample(shots, bit_packed=True, dets_out=d, obs_out=o), args.dem_steps)
+    dp, op = np.empty_like(d), np.empty_like(o)
+    ms_page = _median_ms(lambda: s.sample(shots, bit_packed=True, dets_out=dp, obs_out=op), args.dem_steps)
     return {"workload": f"{shots} shots of the d=25 r=25 p=1e-3 detector error model ({dem.num_errors} error "
-                        f"mechanisms, {D} detectors, {O} observables), host arrays out",
+                        f"mechanisms, {D} detectors, {O} observables), page-locked host arrays out",
             "gbits": shots * (D + O) / (ms / 1e3) / 1e9, "ms": ms, "d2h_bytes": int(d.nbytes + o.nbytes),
+            "pageable": {"gbits": shots * (D + O) / (ms_page / 1e3) / 1e9, "ms": ms_page},
             "mean_detection_events_per_shot": float(np.unpackbits(d[:4096], axis=1).sum() / 4096)}
 
 

@@ -15,18 +15,22 @@ using namespace gfs_rt;
 
 struct gfs_dem {
     int device = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;  // streams[0]
     uint64_t seed = 0;
     uint64_t next_block = 0;  // stream position, in 128-shot blocks
     gfs::DemModel model;
     gfs::DemLayout lay;
     DevBuf d_groups, d_units, d_sym_off, d_sym, d_tables, d_cg, d_cu0, d_cn, d_out_off, d_out_mech, d_expect;
-    DevBuf det_buf, obs_buf, err_buf, in_buf, out_buf;
+    // Two pipeline slots: chunk k runs on slot k % 2, so its device->host copies overlap chunk k + 1's kernels.
+    cudaStream_t streams[2] = {nullptr, nullptr};
+    DevBuf det_buf[2], obs_buf[2], err_buf[2], in_buf[2], out_buf[2];
 
     ~gfs_dem() {
-        if (stream) {
-            cudaStreamSynchronize(stream);
-            cudaStreamDestroy(stream);
+        for (cudaStream_t st : streams) {
+            if (st) {
+                cudaStreamSynchronize(st);
+                cudaStreamDestroy(st);
+            }
         }
     }
 };
@@ -44,7 +48,10 @@ void create(gfs_dem *d, const char *text, size_t len, uint64_t seed, int device)
     d->device = device;
     d->seed = seed;
     ck(cudaSetDevice(device), "cudaSetDevice");
-    ck(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (cudaStream_t &st : d->streams) {
+        ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    }
+    d->stream = d->streams[0];
     const gfs::DemLayout &L = d->lay;
     upload(d->d_groups, L.groups, device, d->stream);
     upload(d->d_units, L.units, device, d->stream);
@@ -91,34 +98,36 @@ void sample(gfs_dem *d, uint64_t shots, uint32_t flags, uint8_t *dets, uint64_t 
                                128 * (drow + orow + (want_errs ? erow : 0) + (replay ? rrow : 0));
     const uint64_t cb = std::max<uint64_t>(1, std::min<uint64_t>(512, ((uint64_t)1 << 30) / std::max<uint64_t>(1, per_block)));
     const uint64_t chunk = cb * 128;
-    d->det_buf.ensure(std::max<uint64_t>(16, cb * D * 16), d->device);
-    d->obs_buf.ensure(std::max<uint64_t>(16, cb * O * 16), d->device);
-    if (want_errs || replay) {
-        d->err_buf.ensure(std::max<uint64_t>(16, cb * E * 16), d->device);
+    for (int k = 0; k < 2; k++) {
+        d->det_buf[k].ensure(std::max<uint64_t>(16, cb * D * 16), d->device);
+        d->obs_buf[k].ensure(std::max<uint64_t>(16, cb * O * 16), d->device);
+        if (want_errs || replay) {
+            d->err_buf[k].ensure(std::max<uint64_t>(16, cb * E * 16), d->device);
+        }
+        if (replay) {
+            d->in_buf[k].ensure(std::max<uint64_t>(16, chunk * rrow), d->device);
+        }
+        d->out_buf[k].ensure(std::max<uint64_t>(16, chunk * (drow + orow + (want_errs ? erow : 0))), d->device);
     }
-    if (replay) {
-        d->in_buf.ensure(std::max<uint64_t>(16, chunk * rrow), d->device);
-    }
-    d->out_buf.ensure(std::max<uint64_t>(16, chunk * (drow + orow + (want_errs ? erow : 0))), d->device);
-    uint8_t *dout = (uint8_t *)d->out_buf.p, *oout = dout + chunk * drow, *eout = oout + chunk * orow;
     const gfs::DemLayout &L = d->lay;
-    for (uint64_t done = 0; done < shots;) {
-        const uint64_t cs = std::min<uint64_t>(shots - done, chunk);
+    // Kernels of the chunk at `done` in slot k, sampling from stream block `block0`.
+    auto compute = [&](int k, uint64_t done, uint64_t cs, uint64_t block0) {
+        cudaStream_t st = d->streams[k];
         const uint64_t nblk = (cs + 127) / 128;
         if (replay) {
-            copy2d(d->in_buf.p, rrow, replay + done * rstride, rstride, rrow, cs, cudaMemcpyHostToDevice, d->stream,
+            copy2d(d->in_buf[k].p, rrow, replay + done * rstride, rstride, rrow, cs, cudaMemcpyHostToDevice, st,
                    "copy recorded errors");
-            gfs::RowsInArgs ra{(const uint8_t *)d->in_buf.p, rrow, cs, E, (uint4 *)d->err_buf.p};
-            ck(gfs::launch_rows_from_shots(ra, d->stream), "rows kernel launch");
-            gfs::FoldArgs fa{(const uint4 *)d->err_buf.p, E, (const uint32_t *)d->d_out_off.p,
+            gfs::RowsInArgs ra{(const uint8_t *)d->in_buf[k].p, rrow, cs, E, (uint4 *)d->err_buf[k].p};
+            ck(gfs::launch_rows_from_shots(ra, st), "rows kernel launch");
+            gfs::FoldArgs fa{(const uint4 *)d->err_buf[k].p, E, (const uint32_t *)d->d_out_off.p,
                              (const uint32_t *)d->d_out_mech.p, (const uint8_t *)d->d_expect.p, D, O, nblk,
-                             (uint4 *)d->det_buf.p, (uint4 *)d->obs_buf.p};
-            ck(gfs::launch_fold(fa, d->stream), "fold kernel launch");
+                             (uint4 *)d->det_buf[k].p, (uint4 *)d->obs_buf[k].p};
+            ck(gfs::launch_fold(fa, st), "fold kernel launch");
         } else {
-            ck(cudaMemsetAsync(d->det_buf.p, 0, nblk * D * 16, d->stream), "memset");
-            ck(cudaMemsetAsync(d->obs_buf.p, 0, nblk * O * 16, d->stream), "memset");
+            ck(cudaMemsetAsync(d->det_buf[k].p, 0, nblk * D * 16, st), "memset");
+            ck(cudaMemsetAsync(d->obs_buf[k].p, 0, nblk * O * 16, st), "memset");
             if (want_errs) {
-                ck(cudaMemsetAsync(d->err_buf.p, 0, nblk * E * 16, d->stream), "memset");
+                ck(cudaMemsetAsync(d->err_buf[k].p, 0, nblk * E * 16, st), "memset");
             }
             gfs::DemArgs a{};
             a.groups = (const gfs::DemGroup *)d->d_groups.p;
@@ -131,16 +140,17 @@ void sample(gfs_dem *d, uint64_t shots, uint32_t flags, uint8_t *dets, uint64_t 
             a.chunk_units = (const uint32_t *)d->d_cn.p;
             a.nchunks = (uint32_t)L.chunk_group.size();
             a.seed = d->seed;
-            a.block0 = d->next_block;
+            a.block0 = block0;
             a.nblk = nblk;
             a.D = D;
             a.O = O;
             a.E = E;
-            a.dets = (uint4 *)d->det_buf.p;
-            a.obs = (uint4 *)d->obs_buf.p;
-            a.errs = want_errs ? (uint4 *)d->err_buf.p : nullptr;
-            ck(gfs::launch_dem_sample(a, d->stream), "dem kernel launch");
+            a.dets = (uint4 *)d->det_buf[k].p;
+            a.obs = (uint4 *)d->obs_buf[k].p;
+            a.errs = want_errs ? (uint4 *)d->err_buf[k].p : nullptr;
+            ck(gfs::launch_dem_sample(a, st), "dem kernel launch");
         }
+        uint8_t *dout = (uint8_t *)d->out_buf[k].p, *oout = dout + chunk * drow, *eout = oout + chunk * orow;
         auto tr = [&](const uint4 *src, uint64_t n, uint8_t *out, uint64_t stride) {
             gfs::TransposeArgs t{};
             t.src0 = src;
@@ -149,25 +159,63 @@ void sample(gfs_dem *d, uint64_t shots, uint32_t flags, uint8_t *dets, uint64_t 
             t.out = out;
             t.out_stride = stride;
             t.bit_packed = packed ? 1 : 0;
-            ck(gfs::launch_transpose(t, d->stream), "transpose launch");
+            ck(gfs::launch_transpose(t, st), "transpose launch");
         };
         if (dets && drow) {
-            tr((const uint4 *)d->det_buf.p, D, dout, drow);
-            copy2d(dets + done * dstride, dstride, dout, drow, drow, cs, cudaMemcpyDeviceToHost, d->stream, "copy dets");
+            tr((const uint4 *)d->det_buf[k].p, D, dout, drow);
         }
         if (obs && orow) {
-            tr((const uint4 *)d->obs_buf.p, O, oout, orow);
-            copy2d(obs + done * ostride, ostride, oout, orow, orow, cs, cudaMemcpyDeviceToHost, d->stream, "copy obs");
+            tr((const uint4 *)d->obs_buf[k].p, O, oout, orow);
         }
         if (want_errs && erow) {
-            tr((const uint4 *)d->err_buf.p, E, eout, erow);
-            copy2d(errs + done * estride, estride, eout, erow, erow, cs, cudaMemcpyDeviceToHost, d->stream, "copy errs");
+            tr((const uint4 *)d->err_buf[k].p, E, eout, erow);
         }
-        ck(cudaStreamSynchronize(d->stream), "dem sample");
+    };
+    auto copy_out = [&](int k, uint64_t done, uint64_t cs) {
+        cudaStream_t st = d->streams[k];
+        uint8_t *dout = (uint8_t *)d->out_buf[k].p, *oout = dout + chunk * drow, *eout = oout + chunk * orow;
+        if (dets && drow) {
+            copy2d(dets + done * dstride, dstride, dout, drow, drow, cs, cudaMemcpyDeviceToHost, st, "copy dets");
+        }
+        if (obs && orow) {
+            copy2d(obs + done * ostride, ostride, oout, orow, orow, cs, cudaMemcpyDeviceToHost, st, "copy obs");
+        }
+        if (want_errs && erow) {
+            copy2d(errs + done * estride, estride, eout, erow, erow, cs, cudaMemcpyDeviceToHost, st, "copy errs");
+        }
+    };
+    // Chunk k's copies are issued after chunk k + 1's kernels are queued (a copy into pageable memory may hold
+    // the calling thread until it completes); a slot is reused once its previous chunk has left.
+    struct Pending {
+        uint64_t done, cs;
+    };
+    Pending pend[2] = {};
+    bool used[2] = {false, false};
+    int prev = -1;
+    uint64_t n = 0;
+    for (uint64_t done = 0; done < shots; n++) {
+        const int k = (int)(n & 1);
+        const uint64_t cs = std::min<uint64_t>(shots - done, chunk);
+        if (used[k]) {
+            ck(cudaStreamSynchronize(d->streams[k]), "dem sample");
+        }
+        compute(k, done, cs, d->next_block);
         if (!replay) {
-            d->next_block += nblk;
+            d->next_block += (cs + 127) / 128;
         }
+        pend[k] = Pending{done, cs};
+        used[k] = true;
+        if (prev >= 0) {
+            copy_out(prev, pend[prev].done, pend[prev].cs);
+        }
+        prev = k;
         done += cs;
+    }
+    if (prev >= 0) {
+        copy_out(prev, pend[prev].done, pend[prev].cs);
+    }
+    for (cudaStream_t st : d->streams) {
+        ck(cudaStreamSynchronize(st), "dem sample");
     }
     if (errs && replay && erow) {
         // Replayed errors are returned as given (as the reference returns its replayed error table).

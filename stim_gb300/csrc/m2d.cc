@@ -28,13 +28,19 @@ struct gfs_m2d {
     bool sweep_controlled = false;  // the circuit has sweep-controlled operations
     std::vector<uint32_t> off, idx;
     std::vector<uint8_t> expect;
-    DevBuf d_off, d_idx, d_expect, in_buf, rows_buf, det_buf, obs_buf, out_buf, sweep_in, sweep_rows;
+    DevBuf d_off, d_idx, d_expect, sweep_in, sweep_rows;
+    // Two pipeline slots: chunk k runs on slot k % 2 (its own stream and buffers), so chunk k's device->host
+    // copy overlaps chunk k + 1's host->device copy and kernels.
+    cudaStream_t streams[2] = {nullptr, nullptr};
+    DevBuf in_buf[2], rows_buf[2], det_buf[2], obs_buf[2], out_buf[2];
     std::unique_ptr<gfs_sampler> sweep_sim;  // sweep-controlled circuits: the noiseless frame program
 
     ~gfs_m2d() {
-        if (stream) {
-            cudaStreamSynchronize(stream);
-            cudaStreamDestroy(stream);
+        for (cudaStream_t s : streams) {
+            if (s) {
+                cudaStreamSynchronize(s);
+                cudaStreamDestroy(s);
+            }
         }
     }
 };
@@ -155,7 +161,10 @@ void create(gfs_m2d *m, const gfs_circuit *c, const uint8_t *ref, int device) {
         }
     }
     ck(cudaSetDevice(device), "cudaSetDevice");
-    ck(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (cudaStream_t &st : m->streams) {
+        ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    }
+    m->stream = m->streams[0];
     upload(m->d_off, m->off, device, m->stream);
     upload(m->d_idx, m->idx, device, m->stream);
     upload(m->d_expect, m->expect, device, m->stream);
@@ -208,50 +217,40 @@ void convert(gfs_m2d *m, uint64_t shots, const uint8_t *meas, uint64_t meas_stri
     const uint64_t per_block = (M + D + O) * 16 + 128 * (mrow + drow + orow);
     uint64_t cb = std::max<uint64_t>(1, std::min<uint64_t>(512, ((uint64_t)1 << 30) / std::max<uint64_t>(1, per_block)));
     const uint64_t chunk = cb * 128;
-    m->in_buf.ensure(std::max<uint64_t>(16, chunk * mrow), m->device);
-    m->rows_buf.ensure(std::max<uint64_t>(16, cb * M * 16), m->device);
-    m->det_buf.ensure(std::max<uint64_t>(16, cb * D * 16), m->device);
-    m->obs_buf.ensure(std::max<uint64_t>(16, cb * O * 16), m->device);
-    m->out_buf.ensure(std::max<uint64_t>(16, chunk * (drow + orow)), m->device);
+    for (int k = 0; k < 2; k++) {
+        m->in_buf[k].ensure(std::max<uint64_t>(16, chunk * mrow), m->device);
+        m->rows_buf[k].ensure(std::max<uint64_t>(16, cb * M * 16), m->device);
+        m->det_buf[k].ensure(std::max<uint64_t>(16, cb * D * 16), m->device);
+        m->obs_buf[k].ensure(std::max<uint64_t>(16, cb * O * 16), m->device);
+        m->out_buf[k].ensure(std::max<uint64_t>(16, chunk * (drow + orow)), m->device);
+    }
     if (use_sweep) {
         m->sweep_in.ensure(std::max<uint64_t>(16, chunk * srow), m->device);
         // Room for the frame kernel's padding blocks (up to four 128-shot blocks per CTA slice).
         m->sweep_rows.ensure(std::max<uint64_t>(16, (cb + 4) * m->num_sweep_bits * 16), m->device);
     }
-    uint8_t *dout = (uint8_t *)m->out_buf.p, *oout = dout + chunk * drow;
-    const uint4 *dt = (const uint4 *)m->det_buf.p, *ot = (const uint4 *)m->obs_buf.p;
-    for (uint64_t done = 0; done < shots;) {
-        const uint64_t cs = std::min<uint64_t>(shots - done, chunk);
+    if ((flags & GFS_PREPEND_OBSERVABLES) && (flags & GFS_APPEND_OBSERVABLES)) {
+        throw std::invalid_argument("prepend and append observables together are not supported");
+    }
+    // Host->device copy and kernels of the chunk at `done` in slot k (sweep rows, when used, are XORed in).
+    auto compute = [&](int k, uint64_t done, uint64_t cs, const uint4 *base_dets, const uint4 *base_obs) {
+        cudaStream_t st = m->streams[k];
         const uint64_t nblk = (cs + 127) / 128;
-        copy2d(m->in_buf.p, mrow, meas + done * meas_stride, meas_stride, mrow, cs, cudaMemcpyHostToDevice, m->stream,
+        copy2d(m->in_buf[k].p, mrow, meas + done * meas_stride, meas_stride, mrow, cs, cudaMemcpyHostToDevice, st,
                "copy measurements");
-        gfs::RowsInArgs ra{(const uint8_t *)m->in_buf.p, mrow, cs, M, (uint4 *)m->rows_buf.p};
-        ck(gfs::launch_rows_from_shots(ra, m->stream), "rows kernel launch");
-        gfs::FoldArgs fa{(const uint4 *)m->rows_buf.p, M, (const uint32_t *)m->d_off.p, (const uint32_t *)m->d_idx.p,
-                         (const uint8_t *)m->d_expect.p, D, O, nblk, (uint4 *)m->det_buf.p, (uint4 *)m->obs_buf.p};
         if (M == 0) {
-            ck(cudaMemsetAsync(m->rows_buf.p, 0, 16, m->stream), "memset");
+            ck(cudaMemsetAsync(m->rows_buf[k].p, 0, 16, st), "memset");
         }
-        if (use_sweep) {
-            // Sweep rows [block][sweep bit], then the noiseless frame program over them on the sampler's stream.
-            copy2d(m->sweep_in.p, srow, sweep + done * sweep_stride, sweep_stride, srow, cs, cudaMemcpyHostToDevice,
-                   m->stream, "copy sweep bits");
-            gfs::RowsInArgs sa{(const uint8_t *)m->sweep_in.p, srow, cs, m->num_sweep_bits, (uint4 *)m->sweep_rows.p};
-            ck(gfs::launch_rows_from_shots(sa, m->stream), "rows kernel launch");
-            ck(cudaStreamSynchronize(m->stream), "sweep rows");
-            gfs_sampler &sim = *m->sweep_sim;
-            sim.sweep_rows = (const uint4 *)m->sweep_rows.p;
-            sim.nsweep = (uint32_t)m->num_sweep_bits;
-            sim.run_frame(nblk, 0);
-            ck(cudaStreamSynchronize(sim.stream), "sweep frames");
-            sim.sweep_rows = nullptr;
-            if (sim.check_status()) {
-                throw std::logic_error("noiseless frame program reported a hit-list overflow");
-            }
-            fa.base_dets = (const uint4 *)sim.det_tmp.p;
-            fa.base_obs = (const uint4 *)sim.obs_tmp.p;
-        }
-        ck(gfs::launch_fold(fa, m->stream), "fold kernel launch");
+        gfs::RowsInArgs ra{(const uint8_t *)m->in_buf[k].p, mrow, cs, M, (uint4 *)m->rows_buf[k].p};
+        ck(gfs::launch_rows_from_shots(ra, st), "rows kernel launch");
+        gfs::FoldArgs fa{(const uint4 *)m->rows_buf[k].p, M, (const uint32_t *)m->d_off.p, (const uint32_t *)m->d_idx.p,
+                         (const uint8_t *)m->d_expect.p, D, O, nblk, (uint4 *)m->det_buf[k].p,
+                         (uint4 *)m->obs_buf[k].p};
+        fa.base_dets = base_dets;
+        fa.base_obs = base_obs;
+        ck(gfs::launch_fold(fa, st), "fold kernel launch");
+        const uint4 *dt = (const uint4 *)m->det_buf[k].p, *ot = (const uint4 *)m->obs_buf[k].p;
+        uint8_t *dout = (uint8_t *)m->out_buf[k].p, *oout = dout + chunk * drow;
         auto tr = [&](const uint4 *s0, uint64_t n0, const uint4 *s1, uint64_t n1, uint8_t *out, uint64_t stride) {
             gfs::TransposeArgs t{};
             t.src0 = s0;
@@ -262,26 +261,87 @@ void convert(gfs_m2d *m, uint64_t shots, const uint8_t *meas, uint64_t meas_stri
             t.out = out;
             t.out_stride = stride;
             t.bit_packed = packed ? 1 : 0;
-            ck(gfs::launch_transpose(t, m->stream), "transpose launch");
+            ck(gfs::launch_transpose(t, st), "transpose launch");
         };
         if (dets && drow) {
-            if ((flags & GFS_PREPEND_OBSERVABLES) && (flags & GFS_APPEND_OBSERVABLES)) {
-                throw std::invalid_argument("prepend and append observables together are not supported");
-            } else if (flags & GFS_PREPEND_OBSERVABLES) {
+            if (flags & GFS_PREPEND_OBSERVABLES) {
                 tr(ot, O, dt, D, dout, drow);
             } else if (flags & GFS_APPEND_OBSERVABLES) {
                 tr(dt, D, ot, O, dout, drow);
             } else {
                 tr(dt, D, nullptr, 0, dout, drow);
             }
-            copy2d(dets + done * dstride, dstride, dout, drow, drow, cs, cudaMemcpyDeviceToHost, m->stream, "copy dets");
         }
         if (obs && orow) {
             tr(ot, O, nullptr, 0, oout, orow);
-            copy2d(obs + done * ostride, ostride, oout, orow, orow, cs, cudaMemcpyDeviceToHost, m->stream, "copy obs");
         }
-        ck(cudaStreamSynchronize(m->stream), "convert");
+    };
+    auto copy_out = [&](int k, uint64_t done, uint64_t cs) {
+        cudaStream_t st = m->streams[k];
+        uint8_t *dout = (uint8_t *)m->out_buf[k].p, *oout = dout + chunk * drow;
+        if (dets && drow) {
+            copy2d(dets + done * dstride, dstride, dout, drow, drow, cs, cudaMemcpyDeviceToHost, st, "copy dets");
+        }
+        if (obs && orow) {
+            copy2d(obs + done * ostride, ostride, oout, orow, orow, cs, cudaMemcpyDeviceToHost, st, "copy obs");
+        }
+    };
+    if (use_sweep) {
+        // Sweep data: one chunk at a time on slot 0 (the frame program runs on its sampler's stream).
+        for (uint64_t done = 0; done < shots;) {
+            const uint64_t cs = std::min<uint64_t>(shots - done, chunk);
+            const uint64_t nblk = (cs + 127) / 128;
+            copy2d(m->sweep_in.p, srow, sweep + done * sweep_stride, sweep_stride, srow, cs, cudaMemcpyHostToDevice,
+                   m->streams[0], "copy sweep bits");
+            gfs::RowsInArgs sa{(const uint8_t *)m->sweep_in.p, srow, cs, m->num_sweep_bits, (uint4 *)m->sweep_rows.p};
+            ck(gfs::launch_rows_from_shots(sa, m->streams[0]), "rows kernel launch");
+            ck(cudaStreamSynchronize(m->streams[0]), "sweep rows");
+            gfs_sampler &sim = *m->sweep_sim;
+            sim.sweep_rows = (const uint4 *)m->sweep_rows.p;
+            sim.nsweep = (uint32_t)m->num_sweep_bits;
+            sim.run_frame(nblk, 0);
+            ck(cudaStreamSynchronize(sim.stream), "sweep frames");
+            sim.sweep_rows = nullptr;
+            if (sim.check_status()) {
+                throw std::logic_error("noiseless frame program reported a hit-list overflow");
+            }
+            compute(0, done, cs, (const uint4 *)sim.det_tmp.p, (const uint4 *)sim.obs_tmp.p);
+            copy_out(0, done, cs);
+            ck(cudaStreamSynchronize(m->streams[0]), "convert");
+            done += cs;
+        }
+        return;
+    }
+    // Chunk k's copy out is issued after chunk k + 1's copy in and kernels are queued (a copy to or from
+    // pageable memory may hold the calling thread until it completes); a slot is reused once its previous
+    // chunk has left.
+    struct Pending {
+        uint64_t done, cs;
+    };
+    Pending pend[2] = {};
+    bool used[2] = {false, false};
+    int prev = -1;
+    uint64_t n = 0;
+    for (uint64_t done = 0; done < shots; n++) {
+        const int k = (int)(n & 1);
+        const uint64_t cs = std::min<uint64_t>(shots - done, chunk);
+        if (used[k]) {
+            ck(cudaStreamSynchronize(m->streams[k]), "convert");
+        }
+        compute(k, done, cs, nullptr, nullptr);
+        pend[k] = Pending{done, cs};
+        used[k] = true;
+        if (prev >= 0) {
+            copy_out(prev, pend[prev].done, pend[prev].cs);
+        }
+        prev = k;
         done += cs;
+    }
+    if (prev >= 0) {
+        copy_out(prev, pend[prev].done, pend[prev].cs);
+    }
+    for (cudaStream_t st : m->streams) {
+        ck(cudaStreamSynchronize(st), "convert");
     }
 }
 
