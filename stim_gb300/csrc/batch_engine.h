@@ -215,7 +215,8 @@ struct BatchEngine {
                 count_off[j] = count_total;
                 hit_total += nslices * pl.slice_cap;
                 count_total += nslices * a.n_occ;
-                wprefix.push_back(wprefix.back() + nslices * a.n_occ);
+                const uint64_t sb = (uint64_t)gfs::noise_slices_per_warp_for((int)B);
+                wprefix.push_back(wprefix.back() + (nslices + sb - 1) / sb * a.n_occ);
             }
             desc.push_back(a);
             total += nslices;

@@ -450,14 +450,14 @@ struct NoiseQueued {
 // region (per-slice ballot prefixes).  `q` is the warp's queue (64 entries).
 template <int B, int SB>
 __device__ __forceinline__ void noise_records(const KernelArgs &p, uint32_t slice0, uint32_t nsub, uint32_t k,
-                                              uint32_t lane, NoiseQueued *q, uint32_t (&count)[SB]) {
+                                              uint32_t lane, NoiseQueued *q, uint32_t *count) {
     const NoiseOcc oc = p.occs[k];
     const DevOp op = p.ops[oc.pc];
     const OccParams o = occ_params(p, op, oc.which, oc.inst);
-#pragma unroll
-    for (int s = 0; s < SB; s++) {
-        count[s] = 0;  // warp-uniform
+    if (lane < (uint32_t)SB) {
+        count[lane] = 0;  // this warp's records per slice (shared memory)
     }
+    __syncwarp();
     if (!o.ch->active) {
         return;
     }
@@ -544,17 +544,26 @@ __device__ __forceinline__ void noise_records(const KernelArgs &p, uint32_t slic
             }
             continue;
         }
-        // One hit per active lane, each into its own slice's region.
-        uint32_t at = 0;
-#pragma unroll
-        for (int s = 0; s < SB; s++) {
-            const uint32_t ms = SB == 1 ? act : __ballot_sync(0xFFFFFFFFu, active && sub == (uint32_t)s);
-            if (active && sub == (uint32_t)s) {
-                at = count[s] + __popc(ms & lt);
-            }
-            count[s] += __popc(ms);
-        }
+        // One hit per active lane, each into its own slice's region: the lanes of one slice take consecutive
+        // places after the slice's count, which their first lane advances once.
         if (active) {
+            uint32_t at;
+            if (SB == 1) {
+                at = count[0] + __popc(act & lt);
+                __syncwarp(act);
+                if (lane == (uint32_t)(__ffs(act) - 1)) {
+                    count[0] += __popc(act);
+                }
+            } else {
+                const uint32_t peers = __match_any_sync(act, sub);
+                const uint32_t leader = (uint32_t)__ffs(peers) - 1u;
+                uint32_t base = 0;
+                if (lane == leader) {
+                    base = count[sub];
+                    count[sub] = base + __popc(peers);
+                }
+                at = __shfl_sync(act, base, leader) + __popc(peers & lt);
+            }
             const uint64_t r = occ_record(p, o, u0 + ((uint32_t)pos >> 7), blk, (uint32_t)pos & 127u, &st);
             if (at < oc.cap) {
                 p.hits[(uint64_t)(slice0 + sub) * p.slice_cap + oc.off + at] = r;
@@ -562,17 +571,19 @@ __device__ __forceinline__ void noise_records(const KernelArgs &p, uint32_t slic
             pos = gfs_next_hit(&st, T, ch.inv_c, pos, trials, always);
             active = pos >= 0;
         }
+        __syncwarp();
     }
 }
 
 // Warp w draws occurrence w % n_occ of the SB slices from (w / n_occ) * SB on into their regions.
 template <int B, int SB>
 __device__ __forceinline__ void noise_warp(const KernelArgs &p, uint64_t w, uint32_t warp, uint32_t lane,
-                                           NoiseQueued (*queue)[64]) {
+                                           NoiseQueued (*queue)[64], uint32_t *counts) {
     const uint32_t slice0 = (uint32_t)(w / p.n_occ) * SB, k = (uint32_t)(w % p.n_occ);
     const uint32_t nsub = min((uint32_t)SB, p.nslices - slice0);
-    uint32_t count[SB];
+    uint32_t *count = counts + warp * SB;
     noise_records<B, SB>(p, slice0, nsub, k, lane, queue[warp], count);
+    __syncwarp();
     if (lane == 0) {
         const uint32_t cap = p.occs[k].cap;
 #pragma unroll
@@ -589,27 +600,29 @@ __device__ __forceinline__ void noise_warp(const KernelArgs &p, uint64_t w, uint
     }
 }
 
-// One-block slices are drawn four per warp (fuller screening rounds, one setup per four slices).
 template <int B>
 __host__ __device__ constexpr int noise_slices_per_warp() {
-    return B == 1 ? 4 : 1;
+    return noise_slices_per_warp_for(B);
 }
 
 template <int B>
 __global__ void __launch_bounds__(256) noise_kernel(const KernelArgs p) {
-    __shared__ NoiseQueued queue[8][64];
     constexpr int SB = noise_slices_per_warp<B>();
+    __shared__ NoiseQueued queue[8][64];
+    __shared__ uint32_t counts[8 * SB];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint64_t w = (uint64_t)blockIdx.x * 8 + warp;
     if (w < (uint64_t)((p.nslices + SB - 1) / SB) * p.n_occ) {
-        noise_warp<B, SB>(p, w, warp, lane, queue);
+        noise_warp<B, SB>(p, w, warp, lane, queue, counts);
     }
 }
 
 // The noise of a batch: warp w belongs to circuit j with warp_prefix[j] <= w < warp_prefix[j + 1].
 template <int B>
 __global__ void __launch_bounds__(256) batch_noise_kernel(const BatchArgs b) {
+    constexpr int SB = noise_slices_per_warp<B>();
     __shared__ NoiseQueued queue[8][64];
+    __shared__ uint32_t counts[8 * SB];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint64_t w = (uint64_t)blockIdx.x * 8 + warp;
     if (w >= b.total_noise_warps) {
@@ -625,7 +638,7 @@ __global__ void __launch_bounds__(256) batch_noise_kernel(const BatchArgs b) {
         }
     }
     const KernelArgs &p = b.circuits[lo];
-    noise_warp<B, 1>(p, w - b.warp_prefix[lo], warp, lane, queue);
+    noise_warp<B, SB>(p, w - b.warp_prefix[lo], warp, lane, queue, counts);
 }
 
 // Shared-memory layout of a CTA holding B blocks of 128 shots: X and Z frames [row][block], the
