@@ -29,10 +29,11 @@ struct gfs_m2d {
     std::vector<uint32_t> off, idx;
     std::vector<uint8_t> expect;
     DevBuf d_off, d_idx, d_expect, sweep_in, sweep_rows;
-    // Two pipeline slots: chunk k runs on slot k % 2 (its own stream and buffers), so chunk k's device->host
-    // copy overlaps chunk k + 1's host->device copy and kernels.
-    cudaStream_t streams[2] = {nullptr, nullptr};
-    DevBuf in_buf[2], rows_buf[2], det_buf[2], obs_buf[2], out_buf[2];
+    // Three pipeline slots: chunk k runs on slot k % 3 (its own stream and buffers), so chunk k's device->host
+    // copy overlaps chunk k + 1's host->device copy and kernels, and chunk k + 2's copy in need not wait for it.
+    static constexpr int kSlots = 3;
+    cudaStream_t streams[kSlots] = {};
+    DevBuf in_buf[kSlots], rows_buf[kSlots], det_buf[kSlots], obs_buf[kSlots], out_buf[kSlots];
     std::unique_ptr<gfs_sampler> sweep_sim;  // sweep-controlled circuits: the noiseless frame program
 
     ~gfs_m2d() {
@@ -217,7 +218,7 @@ void convert(gfs_m2d *m, uint64_t shots, const uint8_t *meas, uint64_t meas_stri
     const uint64_t per_block = (M + D + O) * 16 + 128 * (mrow + drow + orow);
     uint64_t cb = std::max<uint64_t>(1, std::min<uint64_t>(512, ((uint64_t)1 << 30) / std::max<uint64_t>(1, per_block)));
     const uint64_t chunk = cb * 128;
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < gfs_m2d::kSlots; k++) {
         m->in_buf[k].ensure(std::max<uint64_t>(16, chunk * mrow), m->device);
         m->rows_buf[k].ensure(std::max<uint64_t>(16, cb * M * 16), m->device);
         m->det_buf[k].ensure(std::max<uint64_t>(16, cb * D * 16), m->device);
@@ -318,12 +319,12 @@ void convert(gfs_m2d *m, uint64_t shots, const uint8_t *meas, uint64_t meas_stri
     struct Pending {
         uint64_t done, cs;
     };
-    Pending pend[2] = {};
-    bool used[2] = {false, false};
+    Pending pend[gfs_m2d::kSlots] = {};
+    bool used[gfs_m2d::kSlots] = {};
     int prev = -1;
     uint64_t n = 0;
     for (uint64_t done = 0; done < shots; n++) {
-        const int k = (int)(n & 1);
+        const int k = (int)(n % gfs_m2d::kSlots);
         const uint64_t cs = std::min<uint64_t>(shots - done, chunk);
         if (used[k]) {
             ck(cudaStreamSynchronize(m->streams[k]), "convert");
