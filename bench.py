@@ -331,6 +331,9 @@ def run_gpu(args):
     if rank == 0:
         cb_value, cb_s, cb_shots = cpu_baseline(text, D, O, args.cpu_chunk, os.cpu_count() or 1, args.cpu_seconds,
                                                 3 * args.cpu_seconds)
+        # The same port on one core (the reference CLI's `stim detect` is single-threaded).
+        cb1_value, cb1_s, cb1_shots = cpu_baseline(text, D, O, 4096, 1, min(args.cpu_seconds, 3.0),
+                                                   3 * min(args.cpu_seconds, 3.0))
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
@@ -373,7 +376,9 @@ def run_gpu(args):
                                             "peak = measured HBM copy bandwidth"},
             "cpu_baseline": {"value": cb_value, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                              "sample": f"{cb_shots} shots of the same workload in {args.cpu_chunk}-shot calls "
-                                       f"({cb_s:.1f} s), oracle port (64-bit words, pthreads)"},
+                                       f"({cb_s:.1f} s), oracle port (64-bit words, pthreads)",
+                             "one_core": {"value": cb1_value, "unit": UNIT, "cores": 1,
+                                          "sample": f"{cb1_shots} shots in 4096-shot calls ({cb1_s:.1f} s)"}},
             "clocks": clk,
             "batched": batched,
             "serving": serving,
