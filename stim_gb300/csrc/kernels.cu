@@ -444,10 +444,11 @@ struct NoiseQueued {
 };
 
 // One warp draws occurrence k of the SB slices slice0 .. slice0 + nsub - 1 (B blocks each) into their regions
-// of the hit list; count[s] receives the records of slice slice0 + s (records past the region's capacity are
-// counted but not written).  Items are (segment, slice, block), blocks fastest, so a warp screens the same
-// segment of several blocks together; records of one step go to consecutive slots of their own slice's
-// region (per-slice ballot prefixes).  `q` is the warp's queue (64 entries).
+// of the hit list; count[s] (the warp's counters in shared memory) receives the records of slice slice0 + s
+// (records past the region's capacity are counted but not written).  Items are (segment, slice, block), blocks
+// fastest, so a warp screens the same segment of several blocks together; records of one step go to
+// consecutive slots of their own slice's region (lanes of one slice grouped by __match_any_sync).  `q` is the
+// warp's queue (64 entries).
 template <int B, int SB>
 __device__ __forceinline__ void noise_records(const KernelArgs &p, uint32_t slice0, uint32_t nsub, uint32_t k,
                                               uint32_t lane, NoiseQueued *q, uint32_t *count) {
