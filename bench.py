@@ -327,6 +327,7 @@ def run_gpu(args):
     serving = run_serving(args, local) if args.serve_seconds > 0 else None
     m2d = run_m2d(args, local, text) if args.m2d_steps > 0 else None
     dem = run_dem(args, local) if args.dem_steps > 0 else None
+    feed = run_feed(args, local, text) if args.feed_steps > 0 else None
 
     if rank == 0:
         cb_value, cb_s, cb_shots = cpu_baseline(text, D, O, args.cpu_chunk, os.cpu_count() or 1, args.cpu_seconds,
@@ -384,6 +385,7 @@ def run_gpu(args):
             "serving": serving,
             "m2d": m2d,
             "dem": dem,
+            "feed": feed,
         }
         print(json.dumps(line))
     if world > 1:
@@ -468,6 +470,33 @@ def run_dem(args, local):
             "gbits": shots * (D + O) / (ms / 1e3) / 1e9, "ms": ms, "d2h_bytes": int(d.nbytes + o.nbytes),
             "pageable": {"gbits": shots * (D + O) / (ms_page / 1e3) / 1e9, "ms": ms_page},
             "mean_detection_events_per_shot": float(np.unpackbits(d[:4096], axis=1).sum() / 4096)}
+
+
+def run_feed(args, local, text):
+    """The decoder feed (CompiledDetectorSampler.sample_for_decoder, the sampling half of sinter's
+    StimThenDecodeSampler) on the main workload: `--shots` shots with the first 40 detectors postselected, kept
+    rows into reused page-locked host arrays; detection events counted and discarded shots dropped on the device."""
+    import numpy as np
+
+    import stim_gb300
+
+    shots = args.shots
+    c = stim_gb300.Circuit(text)
+    D, O = c.num_detectors, c.num_observables
+    s = c.compile_detector_sampler(seed=args.seed, device=local)
+    mask = np.zeros((D + 7) // 8, dtype=np.uint8)
+    mask[:5] = 0xFF
+    d, o = _pinned((shots, (D + 7) // 8)), _pinned((shots, (O + 7) // 8))
+    last = {}
+
+    def call():
+        kd, ko, disc, ev = s.sample_for_decoder(shots, postselection_mask=mask, dets_out=d, obs_out=o)
+        last.update(kept=kd.shape[0], discards=disc, events=ev)
+
+    ms = _median_ms(call, args.feed_steps)
+    return {"workload": f"{shots} shots, detectors 0-39 postselected, kept rows into page-locked host arrays",
+            "gbits_sampled": shots * (D + O) / (ms / 1e3) / 1e9, "ms": ms, "kept": last["kept"],
+            "discards": last["discards"], "detection_events_per_shot": last["events"] / shots}
 
 
 def run_batched(args, local):
@@ -658,6 +687,7 @@ def main():
     ap.add_argument("--batched", type=int, default=1)
     ap.add_argument("--m2d-steps", type=int, default=5)
     ap.add_argument("--dem-steps", type=int, default=5)
+    ap.add_argument("--feed-steps", type=int, default=3)
     ap.add_argument("--batch-circuits", type=int, default=256)
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0)

@@ -280,7 +280,7 @@ class CompiledDetectorSampler(_SamplerBase):
             return dets, obs
         return dets
 
-    def sample_for_decoder(self, shots: int, *, postselection_mask=None):
+    def sample_for_decoder(self, shots: int, *, postselection_mask=None, dets_out=None, obs_out=None):
         """Samples ``shots`` shots for a decoder, as sinter's StimThenDecodeSampler does
         (glue/sample/src/sinter/_decoding/_stim_then_decode_sampler.py:170-190), with the counting and the
         postselection done on the device.
@@ -288,7 +288,8 @@ class CompiledDetectorSampler(_SamplerBase):
         Returns ``(dets, obs, num_discards, num_detection_events)``: the kept shots' bit-packed detector and
         observable rows in shot order, the number of shots dropped because a detection event fell under
         ``postselection_mask`` (uint8, ``ceil(num_detectors / 8)`` bytes, or None), and the number of
-        detection events over all sampled shots before dropping."""
+        detection events over all sampled shots before dropping.  dets_out / obs_out (optional) are caller-owned
+        uint8 arrays of shape (shots, row bytes) reused across calls; the kept rows are views of their first rows."""
         shots = int(shots)
         if shots < 0:
             raise ValueError("shots must be non-negative")
@@ -299,8 +300,8 @@ class CompiledDetectorSampler(_SamplerBase):
             mask = np.ascontiguousarray(np.asarray(postselection_mask), dtype=np.uint8).reshape(-1)
             if mask.shape[0] != drow:
                 raise ValueError(f"postselection_mask must have {drow} bytes, got {mask.shape[0]}")
-        dets = np.empty((shots, drow), dtype=np.uint8)
-        obs = np.empty((shots, orow), dtype=np.uint8)
+        dets, _ = _out_array(dets_out, (shots, drow), True)
+        obs, _ = _out_array(obs_out, (shots, orow), True)
         out = (ctypes.c_uint64 * 3)()
         if shots:
             check(lib().gfs_sample_for_decoder(
