@@ -121,3 +121,21 @@ def test_sinter_adapter_matches_reference_rules_on_oracle_shots():
     assert st.custom_counts["detectors_checked"] == c.num_detectors * 20_000
     for k, v in combos.items():
         assert st.custom_counts[k] == v
+
+
+def test_feed_reuses_caller_arrays():
+    text = workloads.code_circuit("surface_code:rotated_memory_z", 5, 5, 0.02)
+    c = stim_gb300.Circuit(text)
+    mask = _mask(c.num_detectors, 4, 9)
+    shots = 3000
+    d = np.full((shots, (c.num_detectors + 7) // 8), 0xAB, dtype=np.uint8)
+    o = np.full((shots, (c.num_observables + 7) // 8), 0xCD, dtype=np.uint8)
+    kd, ko, disc, ev = c.compile_detector_sampler(seed=4).sample_for_decoder(shots, postselection_mask=mask,
+                                                                             dets_out=d, obs_out=o)
+    assert kd.base is d or np.shares_memory(kd, d)
+    wd, wo, wdisc, wev = c.compile_detector_sampler(seed=4).sample_for_decoder(shots, postselection_mask=mask)
+    np.testing.assert_array_equal(kd, wd)
+    np.testing.assert_array_equal(ko, wo)
+    assert (disc, ev) == (wdisc, wev)
+    with pytest.raises(ValueError):
+        c.compile_detector_sampler(seed=4).sample_for_decoder(shots, dets_out=np.zeros((shots, 1), np.uint8))
