@@ -80,6 +80,10 @@ void detections_noalloc(gfs_sampler *s, uint64_t shots, uint32_t flags, uint8_t 
         a.smem_ops = s->smem_ops();
         a.ring_global = nullptr;  // this path allocates nothing: the ring stays in shared memory
         gfs::LaunchShape shape = s->shape_inline;  // no hit lists: they would need allocations
+        if (shape.frames_global) {
+            throw std::invalid_argument("the circuit's frames do not fit in shared memory, which the allocation-free "
+                                        "entry point requires");
+        }
         if (shape.ring_global) {
             shape.ring_global = false;
             shape.smem = s->smem_for(shape.blocks_per_cta, false);

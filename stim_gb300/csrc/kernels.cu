@@ -752,16 +752,20 @@ __device__ __forceinline__ void apply_hits(const KernelArgs &p, const FrameState
 // Lays out shared memory for circuit `p` and copies its gap tables and op stream in; the copies are
 // visible after the next __syncthreads() (the first one in frame_slice).
 template <int B>
-__device__ __forceinline__ FrameState frame_state(const KernelArgs &p, uint4 *sm) {
+__device__ __forceinline__ FrameState frame_state(const KernelArgs &p, uint4 *sm, bool frames_global = false) {
     FrameState st;
     const uint32_t nr = p.nrows, L = p.ring, NO = p.nobs;
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    st.X = sm;
+    // Frames in shared memory, or (circuits too large for it; a compile-time choice of the kernel) in this CTA's
+    // region of a global buffer.
+    uint4 *const fr = frames_global ? p.frames_global + (size_t)blockIdx.x * p.frames_cta_stride : sm;
+    uint4 *const after = frames_global ? sm : sm + (size_t)2 * nr * B;  // next free shared-memory entry
+    st.X = fr;
     st.Z = st.X + (size_t)nr * B;
     // The measurement ring lives in shared memory, or (for large rings, to fit more CTAs per SM) in this
     // CTA's own region of a global scratch buffer, which stays L2-resident.
-    st.R = p.ring_global ? p.ring_global + (size_t)blockIdx.x * p.ring_cta_stride : st.Z + (size_t)nr * B;
-    st.O = p.ring_global ? st.Z + (size_t)nr * B : st.R + (size_t)L * B;
+    st.R = p.ring_global ? p.ring_global + (size_t)blockIdx.x * p.ring_cta_stride : after;
+    st.O = p.ring_global ? after : st.R + (size_t)L * B;
     st.OCC = st.O + (size_t)NO * B;
     st.MSK = st.OCC + B;
     // Gap tables are read on every noise draw; keep them in shared memory when the launch reserved room.
@@ -1394,6 +1398,17 @@ __global__ void __maxnreg__(96) frame_kernel(const KernelArgs p) {
     }
 }
 
+// The same with the X / Z frames in a per-CTA global region (one block per CTA): circuits whose frames do not
+// fit in shared memory.  Frame accesses go through L1 / L2; everything else is as in frame_kernel.
+template <bool HITS>
+__global__ void __maxnreg__(96) frame_kernel_global(const KernelArgs p) {
+    extern __shared__ uint4 sm[];
+    const FrameState st = frame_state<1>(p, sm, true);
+    for (uint32_t slice = blockIdx.x; slice < p.nslices; slice += gridDim.x) {
+        frame_slice<1, HITS>(p, st, slice);
+    }
+}
+
 // Many circuits in one persistent launch: work items are (circuit, slice) pairs numbered circuit by
 // circuit (b.slice_prefix[j] = first item of circuit j); CTAs claim items from a global counter, so
 // expensive and cheap circuits balance across the SMs.  A CTA reloads the circuit's descriptor, gap tables
@@ -1457,10 +1472,27 @@ static cudaError_t launch_b(const KernelArgs &args, const LaunchShape &s, cudaSt
     return cudaGetLastError();
 }
 
+template <bool H>
+static cudaError_t launch_global_frames(const KernelArgs &args, const LaunchShape &s, cudaStream_t stream) {
+    cudaError_t e =
+        cudaFuncSetAttribute(frame_kernel_global<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    frame_kernel_global<H><<<s.grid, s.threads, s.smem, stream>>>(args);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_frame_kernel(const KernelArgs &args, const LaunchShape &shape, cudaStream_t stream) {
     const bool h = args.hits != nullptr;
     if (h != shape.hits) {
         return cudaErrorInvalidValue;
+    }
+    if (shape.frames_global) {
+        if (shape.blocks_per_cta != 1 || !args.frames_global) {
+            return cudaErrorInvalidValue;
+        }
+        return h ? launch_global_frames<true>(args, shape, stream) : launch_global_frames<false>(args, shape, stream);
     }
     switch (shape.blocks_per_cta) {
         case 1:
@@ -1574,8 +1606,24 @@ static cudaError_t occ_b(const LaunchShape &s, int *out) {
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, frame_kernel<B, H>, s.threads, s.smem);
 }
 
+template <bool H>
+static cudaError_t occ_global_frames(const LaunchShape &s, int *out) {
+    cudaError_t e =
+        cudaFuncSetAttribute(frame_kernel_global<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, frame_kernel_global<H>, s.threads, s.smem);
+}
+
 cudaError_t frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out) {
     const bool h = shape.hits;
+    if (shape.frames_global) {
+        if (shape.blocks_per_cta != 1) {
+            return cudaErrorInvalidValue;
+        }
+        return h ? occ_global_frames<true>(shape, out) : occ_global_frames<false>(shape, out);
+    }
     switch (shape.blocks_per_cta) {
         case 1:
             return h ? occ_b<1, true>(shape, out) : occ_b<1, false>(shape, out);

@@ -43,6 +43,10 @@ struct KernelArgs {
     uint32_t reset_zero;     // 1: start every shot's Z frame at zero instead of random (Program::reset_norand)
     const uint4 *sweep;      // [local block][nsweep] sweep bits read by sweep feedback; null: all zero
     uint32_t nsweep;
+    // Non-null (LaunchShape::frames_global): the X and Z frames live in this CTA's region of a global buffer
+    // (frames_cta_stride uint4 entries per CTA) instead of shared memory, for circuits whose frames do not fit.
+    uint4 *frames_global;
+    uint64_t frames_cta_stride;
 };
 
 // Several circuits in one launch (batch_frame_kernel): circuit j owns work items
@@ -66,8 +70,10 @@ struct LaunchShape {
     size_t smem;         // dynamic shared memory bytes
     bool ring_global;    // measurement ring in global memory (per-CTA region) instead of shared memory
     bool hits = false;   // hit-list mode (noise precomputed by noise_kernel)
+    bool frames_global = false;  // X / Z frames in global memory (one block per CTA only)
 };
 
+// `nrows` = frame rows held in shared memory (0 when the frames are in global memory).
 size_t frame_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t table_words,
                         uint32_t smem_ops, uint32_t smem_occ = 0);
 // Frame kernel; in hit-list mode (args.hits != null) noise_kernel must have run on the same arguments.

@@ -116,7 +116,7 @@ struct gfs_sampler {
     uint64_t next_block = 0;
     gfs::Program prog;
     DevBuf d_ops, d_pool, d_tables, d_chans, d_orig, d_status;
-    DevBuf det_tmp, obs_tmp, meas_tmp, out_tmp, ref_bits, ring_buf;
+    DevBuf det_tmp, obs_tmp, meas_tmp, out_tmp, ref_bits, ring_buf, frames_buf;
     DevBuf feed_rows, feed_compact, feed_aux;  // gfs_sample_for_decoder (feed.cc)
     const uint4 *sweep_rows = nullptr;  // [local block][nsweep] sweep bits for the next run_frame (m2d.cc)
     uint32_t nsweep = 0;
@@ -197,9 +197,11 @@ struct gfs_sampler {
 
     // tables = false: no gap tables in shared memory whatever the mode (the batched engine, whose inline
     // fallback runs with the hit-list shape's shared-memory size).
-    size_t smem_for(int bpc, bool ring_global, bool hits = false, bool tables = true) const {
-        return gfs::frame_smem_bytes(prog.num_rows, ring_global ? 0 : prog.ring, (uint32_t)prog.num_observables,
-                                     bpc, tables ? smem_table_words(hits) : 0, smem_ops(), smem_occ(hits));
+    // frames_global: the X / Z frames are in global memory (not counted).
+    size_t smem_for(int bpc, bool ring_global, bool hits = false, bool tables = true, bool frames_global = false) const {
+        return gfs::frame_smem_bytes(frames_global ? 0 : prog.num_rows, ring_global ? 0 : prog.ring,
+                                     (uint32_t)prog.num_observables, bpc, tables ? smem_table_words(hits) : 0,
+                                     smem_ops(), smem_occ(hits));
     }
 
     // ring: 0 = shared memory, 1 = global memory, -1 = whichever keeps more 128-shot blocks resident per SM.
@@ -224,8 +226,16 @@ struct gfs_sampler {
             int in_smem = resident(false), in_global = resident(true);
             ring = (in_smem == 0 || in_global * 2 >= in_smem * 3) ? 1 : 0;
         }
-        const bool ring_global = ring == 1;
+        bool ring_global = ring == 1;
         size_t smem = smem_for(bpc, ring_global);
+        // Frames too large for shared memory even with the ring in global memory: one block per CTA with the
+        // frames in a per-CTA global region (slower, but no size limit short of device memory).
+        const bool frames_global = smem > (size_t)prop.sharedMemPerBlockOptin && bpc == 1 &&
+                                   smem_for(1, true, false, true, true) <= (size_t)prop.sharedMemPerBlockOptin;
+        if (frames_global) {
+            ring_global = true;
+            smem = smem_for(1, true, false, true, true);
+        }
         if (smem > (size_t)prop.sharedMemPerBlockOptin) {
             throw std::invalid_argument("circuit state (" + std::to_string(smem) +
                                         " bytes) does not fit in shared memory with " + std::to_string(bpc) +
@@ -235,9 +245,10 @@ struct gfs_sampler {
             throw std::invalid_argument("threads per CTA must be a multiple of 32 in [32, 256]");
         }
         gfs::LaunchShape s{bpc, threads, 1, smem, ring_global};
+        s.frames_global = frames_global;
         gfs::LaunchShape si = s;
         s.hits = hits_possible();
-        s.smem = smem_for(bpc, ring_global, s.hits);
+        s.smem = smem_for(bpc, ring_global, s.hits, true, frames_global);
         if (s.smem > (size_t)prop.sharedMemPerBlockOptin) {
             s.hits = false;  // no room for the occurrence cache: draw noise inline
             s.smem = smem;
@@ -247,6 +258,10 @@ struct gfs_sampler {
         ck(gfs::frame_kernel_max_ctas_per_sm(si, &per_sm_inline), "occupancy");
         if (per_sm < 1 || per_sm_inline < 1) {
             throw std::invalid_argument("frame kernel cannot be resident with this launch shape");
+        }
+        if (frames_global) {  // bound the global frame buffer: at most eight CTAs per SM
+            per_sm = std::min(per_sm, 8);
+            per_sm_inline = std::min(per_sm_inline, 8);
         }
         s.grid = grid > 0 ? grid : per_sm * num_sms;
         si.grid = grid > 0 ? grid : per_sm_inline * num_sms;
@@ -406,6 +421,12 @@ struct gfs_sampler {
         a.smem_table_words = smem_table_words(sh.hits);
         a.smem_ops = smem_ops();
         a.ring_global = nullptr;
+        if (sh.frames_global) {
+            const uint64_t stride = (uint64_t)2 * prog.num_rows;  // X then Z rows of one block
+            frames_buf.ensure((uint64_t)sh.grid * stride * sizeof(uint4), device);
+            a.frames_global = (uint4 *)frames_buf.p;
+            a.frames_cta_stride = stride;
+        }
         if (sh.ring_global) {
             ring_buf.ensure((uint64_t)sh.grid * (uint64_t)sh.blocks_per_cta * prog.ring * sizeof(uint4), device);
             a.ring_global = (uint4 *)ring_buf.p;

@@ -208,3 +208,34 @@ def test_hit_list_overflow_falls_back_to_inline_noise(device_out):
     assert s.last_timings()["hit_overflows"] >= 1
     # The stream continues exactly where it would have.
     np.testing.assert_array_equal(s.sample(300, bit_packed=True), want.sample(300, bit_packed=True))
+
+
+def _wide_circuit(n=9000, rounds=3):
+    """A circuit whose frames (2 x 9000 rows x 16 B per 128 shots) exceed shared memory."""
+    q = " ".join(map(str, range(n)))
+    lines = ["R " + q, "X_ERROR(0.01) " + q]
+    for _ in range(rounds):
+        lines.append("CX " + " ".join(f"{2 * i} {2 * i + 1}" for i in range(n // 2)))
+        lines.append("DEPOLARIZE1(0.001) " + q)
+        lines.append("MR " + " ".join(str(2 * i + 1) for i in range(n // 2)))
+        lines += ["DETECTOR rec[-%d]" % (k + 1) for k in range(0, n // 2, 97)]
+    lines.append("M " + " ".join(str(2 * i) for i in range(n // 2)))
+    lines += ["DETECTOR rec[-%d] rec[-%d]" % (k + 1, k + 1 + n // 2) for k in range(0, n // 2, 101)]
+    lines.append("OBSERVABLE_INCLUDE(0) rec[-1] rec[-2]")
+    return "\n".join(lines) + "\n"
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_circuit_too_large_for_shared_memory_matches_oracle(mode):
+    # Frames in a per-CTA global region (one block per CTA); bit-exact against the oracle in both noise modes.
+    text = _wide_circuit()
+    c = stim_gb300.Circuit(text)
+    assert c.program_info()["smem_bytes_per_block"] > 227 * 1024
+    s = c.compile_detector_sampler(seed=17)
+    s.set_noise_mode(mode)
+    shots = 1500
+    gd, go = s.sample(shots, separate_observables=True, bit_packed=True)
+    od, oo, _ = OracleCircuit(text).sample(shots, 17, threads=8)
+    np.testing.assert_array_equal(gd, od)
+    np.testing.assert_array_equal(go, oo)
+    assert gd.any()
