@@ -155,6 +155,11 @@ struct gfs_server {
             p->text = key;
             p->s = std::make_unique<gfs_sampler>();
             p->s->init(&gc, GFS_MODE_DETECTIONS, 0, device);
+            if (p->s->shape.frames_global) {
+                // Rejected here, alone, rather than failing the batch it would join.
+                throw std::invalid_argument("circuit too large for the server: its frames do not fit in shared "
+                                            "memory (sample it with a CompiledDetectorSampler instead)");
+            }
             std::lock_guard<std::mutex> lk(mu);
             auto it = cache.find(key);
             if (it != cache.end()) {

@@ -98,3 +98,18 @@ def test_server_device_destinations_and_errors():
     d0, o0 = _alone(text, shots, 11, bit_packed=True, separate_observables=True)
     np.testing.assert_array_equal(d.cpu().numpy(), d0)
     np.testing.assert_array_equal(o.cpu().numpy(), o0)
+
+
+def test_oversized_circuit_is_rejected_alone():
+    # A circuit whose frames exceed shared memory fails at submission; the requests around it are served.
+    from test_gpu_parity import _wide_circuit
+
+    small = workloads.code_circuit("surface_code:rotated_memory_z", 5, 5, 0.01)
+    with stim_gb300.Server(device=0) as server:
+        a = server.submit(small, 5000, seed=1, bit_packed=True)
+        with pytest.raises(ValueError, match="too large for the server"):
+            server.submit(_wide_circuit(), 1000, seed=2, bit_packed=True).result()
+        b = server.submit(small, 5000, seed=3, bit_packed=True)
+        want_a = stim_gb300.Circuit(small).compile_detector_sampler(seed=1).sample(5000, bit_packed=True)
+        np.testing.assert_array_equal(a.result(), want_a)
+        assert b.result().shape == want_a.shape
