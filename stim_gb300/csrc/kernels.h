@@ -85,12 +85,12 @@ cudaError_t launch_noise_kernel(const KernelArgs &args, int blocks_per_cta, cuda
 
 // Slices (of blocks_per_cta 128-shot blocks) that one noise-kernel warp draws for an occurrence: several per warp
 // keep its screening rounds full and spread one setup over them (d=25, one block per CTA: 4 slices 2.43 ms,
-// 8: 2.31, 16: 2.13, 32: 2.18 per 2^20 shots).
+// 8: 2.31, 16: 2.13, 32: 2.18 per 2^20 shots; four-block slices, d=11: 4 slices 0.225 ms, 8: 0.206).
 #if defined(__CUDACC__)
 __host__ __device__
 #endif
 constexpr int noise_slices_per_warp_for(int blocks_per_cta) {
-    return blocks_per_cta == 1 ? 16 : blocks_per_cta == 2 ? 8 : 4;
+    return blocks_per_cta == 1 ? 16 : blocks_per_cta == 2 ? 16 : 8;
 }
 cudaError_t frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out);
 // In hit-list mode (shape.hits) this launches batch_noise_kernel and then the frame kernel.
