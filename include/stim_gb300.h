@@ -102,6 +102,9 @@ gfs_status gfs_program_noise(const gfs_circuit *c, uint32_t mode, uint64_t *occu
  * Lowers the circuit for `mode` and uploads it to CUDA device `device`; the random stream starts at
  * shot 0 of `seed` (replaces the sampler constructors, compiled_detector_sampler.pybind.cc:28-32,151-154
  * and compiled_measurement_sampler.pybind.cc:63-83).  Successive sample calls continue the stream.
+ * Circuits whose frames do not fit in shared memory (about 7,000 qubits and up) are sampled with the frames
+ * in device memory (slower, same bits); the batched engine, the server and
+ * gfs_sample_detections_device_noalloc reject them.
  */
 gfs_status gfs_sampler_create(const gfs_circuit *c, uint32_t mode, uint64_t seed, int device, gfs_sampler **out);
 void gfs_sampler_free(gfs_sampler *s);
