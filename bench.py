@@ -32,7 +32,7 @@ sys.path.insert(0, ROOT)
 METRIC = "detection-event Gbit/s at d=25 r=25 (surface_code:rotated_memory_z, p=1e-3)"
 # DRAM bytes per shot of the frame kernel on this workload, dram__bytes_read.sum + dram__bytes_write.sum from
 # one ncu capture of 131,072 shots (hit-list mode, 1 block x 128 threads per CTA); traffic grows with shots.
-FRAME_DRAM_BYTES_PER_SHOT = 2860.0
+FRAME_DRAM_BYTES_PER_SHOT = 2855.0
 UNIT = "Gbit/s"
 E2E_WARMUP = 3
 # Device-to-host rate of the GB300 machine's host link, measured with page-locked copies of 2 GiB on 1, 2, 4 and 8
