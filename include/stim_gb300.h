@@ -334,6 +334,14 @@ gfs_status gfs_m2d_convert(gfs_m2d *m, uint64_t shots, const uint8_t *meas, uint
 gfs_status gfs_read_shot_data_file(const char *path, const char *format, uint64_t num_measurements,
                                    uint64_t num_detectors, uint64_t num_observables, uint8_t *out,
                                    uint64_t capacity_shots, uint64_t *shots);
+/*
+ * Host only (replaces stim.write_shot_data_file, src/stim/io/read_write.pybind.cc:147-183): `shots` bit-packed
+ * records (`stride` bytes apart) of num_measurements, or num_detectors + num_observables, bits written to `path`
+ * in a result format (dets tokens M<k>, or D<k> then L<k>).
+ */
+gfs_status gfs_write_shot_data_file(const uint8_t *rows, uint64_t stride, uint64_t shots, const char *path,
+                                    const char *format, uint64_t num_measurements, uint64_t num_detectors,
+                                    uint64_t num_observables);
 gfs_status gfs_m2d_convert_file(gfs_m2d *m, const char *meas_path, const char *meas_format, const char *sweep_path,
                                 const char *sweep_format, const char *dets_path, const char *dets_format,
                                 int append_observables, const char *obs_path, const char *obs_format);

@@ -25,7 +25,7 @@ from ._native import check, lib
 
 __all__ = ["shard_range", "Circuit", "CompiledDetectorSampler", "CompiledMeasurementSampler",
            "CompiledMeasurementsToDetectionEventsConverter", "DetectorErrorModel", "CompiledDemSampler",
-           "BatchSampler", "Server", "device_count", "read_shot_data_file"]
+           "BatchSampler", "Server", "device_count", "read_shot_data_file", "write_shot_data_file"]
 
 
 def device_count() -> int:
@@ -81,6 +81,35 @@ def read_shot_data_file(*, path, format: str = "01", num_measurements=None, num_
     if separate_observables:
         return part(0, n - no), part(n - no, no)
     return part(0, n)
+
+
+def write_shot_data_file(*, data, path, format: str = "01", num_measurements=None, num_detectors=None,
+                         num_observables=None) -> None:
+    """Writes shot records to a result file as the reference's stim.write_shot_data_file does
+    (src/stim/io/read_write.pybind.cc:147-183): `data` is a bool array (shots, bits) or bit-packed uint8 rows
+    (shots, ceil(bits / 8)); bits = num_measurements, or num_detectors + num_observables."""
+    if num_measurements is None and num_detectors is None and num_observables is None:
+        raise ValueError("Must specify num_measurements, num_detectors, num_observables.")
+    nm, nd, no = (int(v or 0) for v in (num_measurements, num_detectors, num_observables))
+    n = nm + nd + no
+    a = np.asarray(data)
+    if a.ndim != 2:
+        raise ValueError("data must be two dimensional")
+    if a.dtype == np.bool_:
+        if a.shape[1] != n:
+            raise ValueError(f"Expected data.shape[1] == {n} but got {a.shape[1]}")
+        rows = np.packbits(a, axis=1, bitorder="little")
+    elif a.dtype == np.uint8:
+        if a.shape[1] != (n + 7) // 8:
+            raise ValueError(f"Expected bit-packed data.shape[1] == {(n + 7) // 8} but got {a.shape[1]}")
+        rows = a
+    else:
+        raise ValueError("data must be a numpy array of bool or bit-packed uint8")
+    rows = np.ascontiguousarray(rows, dtype=np.uint8)
+    if rows.shape[1] == 0:
+        rows = np.zeros((rows.shape[0], 1), dtype=np.uint8)
+    check(lib().gfs_write_shot_data_file(_ptr(rows), rows.shape[1], rows.shape[0], _path(path),
+                                         str(format).encode(), nm, nd, no))
 
 
 class Circuit:

@@ -84,6 +84,7 @@ def _declare(L):
         "gfs_m2d_convert": [_vp, _u64, _vp, _u64, _vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64],
         "gfs_read_shot_data_file": [ctypes.c_char_p, ctypes.c_char_p, _u64, _u64, _u64, _vp, _u64,
                                     ctypes.POINTER(_u64)],
+        "gfs_write_shot_data_file": [_vp, _u64, _u64, ctypes.c_char_p, ctypes.c_char_p, _u64, _u64, _u64],
         "gfs_m2d_convert_file": [_vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
                                  ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p],
         "gfs_dem_parse_stats": [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(_u64)],

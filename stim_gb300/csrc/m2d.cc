@@ -468,6 +468,25 @@ gfs_status gfs_read_shot_data_file(const char *path, const char *format, uint64_
     });
 }
 
+gfs_status gfs_write_shot_data_file(const uint8_t *rows, uint64_t stride, uint64_t shots, const char *path,
+                                    const char *format, uint64_t num_measurements, uint64_t num_detectors,
+                                    uint64_t num_observables) {
+    return guarded([&] {
+        if (num_measurements && (num_detectors || num_observables)) {
+            throw std::invalid_argument("num_measurements and (num_detectors or num_observables)");
+        }
+        const gfs::Format f = gfs::parse_format(format ? format : "01");
+        PathFile out(path, "wb");
+        if (!out.f) {
+            throw std::invalid_argument("path is required");
+        }
+        const uint64_t n = num_measurements + num_detectors + num_observables;
+        const char c1 = num_measurements ? 'M' : 'D', c2 = num_measurements ? 'M' : 'L';
+        gfs::write_rows(out.f, f, rows, std::max<uint64_t>(1, stride), shots, n, c1, c2,
+                        num_measurements + num_detectors);
+    });
+}
+
 gfs_status gfs_m2d_convert_file(gfs_m2d *m, const char *meas_path, const char *meas_format, const char *sweep_path,
                                 const char *sweep_format, const char *dets_path, const char *dets_format,
                                 int append_observables, const char *obs_path, const char *obs_format) {
