@@ -2241,6 +2241,17 @@ __global__ void __launch_bounds__(256) feed_compact_kernel(const FeedArgs a) {
     }
 }
 
+__global__ void publish_words_kernel(const uint32_t *src, uint32_t *dst, uint32_t n) {
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        dst[i] = src[i];
+    }
+}
+
+cudaError_t launch_publish_words(const uint32_t *src, uint32_t *dst, uint32_t n, cudaStream_t stream) {
+    publish_words_kernel<<<1, 32, 0, stream>>>(src, dst, n);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_feed_popcount(const FeedArgs &args, cudaStream_t stream) {
     const uint64_t n = args.nshots * args.drow;
     if (n == 0) {

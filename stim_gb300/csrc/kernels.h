@@ -195,6 +195,9 @@ struct FeedArgs {
     unsigned long long *counts;   // [0] += set bits over the detector rows, [1] += dropped shots
     uint8_t *cdets, *cobs;        // kept rows, in shot order
 };
+// Copies n words of device memory to `dst`, a mapped page-locked host buffer, with a kernel: small results reach
+// the host without a device-to-host copy, which could queue behind a large copy on the copy engine.
+cudaError_t launch_publish_words(const uint32_t *src, uint32_t *dst, uint32_t n, cudaStream_t stream);
 cudaError_t launch_feed_popcount(const FeedArgs &args, cudaStream_t stream);
 cudaError_t launch_feed_flags(const FeedArgs &args, cudaStream_t stream);
 cudaError_t launch_feed_scan(const FeedArgs &args, cudaStream_t stream);

@@ -117,8 +117,11 @@ struct gfs_sampler {
     gfs::Program prog;
     DevBuf d_ops, d_pool, d_tables, d_chans, d_orig, d_status;
     DevBuf det_tmp, obs_tmp, meas_tmp, out_tmp, ref_bits, ring_buf, frames_buf;
-    DevBuf feed_rows, feed_compact, feed_aux;  // gfs_sample_for_decoder (feed.cc)
+    DevBuf feed_rows[2], feed_compact[2], feed_aux[2];  // gfs_sample_for_decoder (feed.cc), per pipeline slot
     const uint4 *sweep_rows = nullptr;  // [local block][nsweep] sweep bits for the next run_frame (m2d.cc)
+    // 16 words of mapped page-locked host memory: the status word (word 0) and the decoder feed's counts
+    // (words 4-7) are published here by a kernel instead of copied (launch_publish_words).
+    uint32_t *h_words = nullptr, *h_words_dev = nullptr;
     uint32_t nsweep = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;  // device->host copies of host-destination chunks
@@ -171,6 +174,9 @@ struct gfs_sampler {
                 }
             }
             cudaStreamDestroy(stream);
+        }
+        if (h_words) {
+            cudaFreeHost(h_words);
         }
     }
 
@@ -322,6 +328,8 @@ struct gfs_sampler {
         upload(d_chans, prog.chans, device, stream);
         upload(d_orig, prog.qubit_orig, device, stream);
         d_status.ensure(16, device);
+        ck(cudaHostAlloc((void **)&h_words, 64, cudaHostAllocMapped), "cudaHostAlloc");
+        ck(cudaHostGetDevicePointer((void **)&h_words_dev, h_words, 0), "cudaHostGetDevicePointer");
         ck(cudaMemsetAsync(d_status.p, 0, 16, stream), "memset");
         default_shape();
         ck(cudaStreamSynchronize(stream), "upload sync");
@@ -483,10 +491,12 @@ struct gfs_sampler {
     // Reads and clears the kernels' status word (after the stream has drained).  Bits 1 and 2 are errors;
     // bit 4 (a hit list overflowed) is returned as true: the caller redoes the affected shots inline.
     bool check_status() {
-        uint32_t st = 0;
-        ck(cudaMemcpy(&st, d_status.p, 4, cudaMemcpyDeviceToHost), "status read");
+        ck(gfs::launch_publish_words((const uint32_t *)d_status.p, h_words_dev, 1, stream), "status publish");
+        ck(cudaStreamSynchronize(stream), "status read");
+        const uint32_t st = *(volatile uint32_t *)h_words;
         if (st) {
-            ck(cudaMemset(d_status.p, 0, 4), "status clear");
+            ck(cudaMemsetAsync(d_status.p, 0, 4, stream), "status clear");
+            ck(cudaStreamSynchronize(stream), "status clear");
         }
         if (st & 3u) {
             throw std::runtime_error("frame kernel reported error status " + std::to_string(st));
