@@ -5,10 +5,14 @@ Workload (one step): 2^20 shots of the rotated surface code memory-Z experiment,
 knobs, generated by the reference's generator (tests/golden/circuits/surface_rz_d25_r25.stim).  This is
 one 2^20-shot chunk of the 2^24-shot streamed configuration.
 
-  value : device-resident Gbit/s = shots x (detectors + observables) / time of the frame kernel plus the
-          shot-major transpose, output left in HBM (CUDA events on the library's stream).
+  value : device-resident Gbit/s = shots x (detectors + observables) / time of the noise kernel, the frame
+          kernel and the shot-major transpose, output left in HBM (CUDA events on the library's stream).
   e2e   : the same metric through the public API (CompiledDetectorSampler.sample(..., bit_packed=True,
-          separate_observables=True)) into host numpy arrays, device->host copy included.
+          separate_observables=True, dets_out=, obs_out=)) into reused page-locked host arrays, device->host
+          copies included (the same call into pageable arrays is reported beside it).
+  other legs (same JSON line): batched (256 circuits in one launch), serving (Poisson arrivals), m2d (the
+          measurements-to-detection-events converter), dem (detector-error-model sampling), feed (the decoder
+          feed with postselection), cpu_baseline (the oracle port on all host cores and on one).
 
 `--impl reference` times the CPU reference implementation of the path on the host cores: the oracle port
 (oracle/stim_oracle.c, a 64-bit-word restatement of the reference's FrameSimulator) with all host threads,
