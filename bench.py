@@ -39,9 +39,6 @@ METRIC = "detection-event Gbit/s at d=25 r=25 (surface_code:rotated_memory_z, p=
 FRAME_DRAM_BYTES_PER_SHOT = 2855.0
 UNIT = "Gbit/s"
 E2E_WARMUP = 3
-# Device-to-host rate of the GB300 machine's host link, measured with page-locked copies of 2 GiB on 1, 2, 4 and 8
-# concurrent streams (192.5-192.9 GB/s in every case): the floor of the e2e step time.
-LINK_GBS = 192.9
 WORKLOAD = dict(family="surface_code:rotated_memory_z", distance=25, rounds=25, p=0.001)
 
 
@@ -100,6 +97,103 @@ def algorithmic_work(text):
             hits += k * (n // 2) * float(args)
             acc += k * (n // 2) * float(args) * 8
     return acc, rbits, hits
+
+
+class quiet_gc:
+    """Python's cyclic garbage collector off inside a timed loop (as the standard library's timeit does), so
+    that a collection of the interpreter's objects does not land inside one timed call."""
+
+    def __enter__(self):
+        import gc
+
+        gc.collect()
+        self.was = gc.isenabled()
+        gc.disable()
+
+    def __exit__(self, *exc):
+        import gc
+
+        if self.was:
+            gc.enable()
+
+
+def measure_link(local, nbytes=1 << 31, reps=5):
+    """Device-to-host and host-to-device rates of this GPU's host link: cudaMemcpyAsync of `nbytes` between
+    HBM and page-locked host memory, best of `reps` (CUDA events on a side stream).  The device-to-host figure
+    is the floor of the end-to-end step (every output byte crosses it once)."""
+    import torch
+
+    dev = torch.empty(nbytes, dtype=torch.uint8, device=f"cuda:{local}")
+    dev.fill_(1)
+    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    host.fill_(0)
+    st = torch.cuda.Stream(device=f"cuda:{local}")
+    out = {}
+    for name, (dst, src) in (("d2h", (host, dev)), ("h2d", (dev, host))):
+        best = None
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            with torch.cuda.stream(st):
+                a.record(st)
+                dst.copy_(src, non_blocking=True)
+                b.record(st)
+            b.synchronize()
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        out[name + "_gbs"] = nbytes / (best / 1e3) / 1e9
+    del dev, host
+    torch.cuda.empty_cache()
+    return out
+
+
+def noise_philox_calls(text):
+    """Expected Philox4x32-10 calls per shot of the hit-list noise kernel under the random-bit contract: each
+    noise instruction instance is cut into segments of 16 units x 128 shots; a segment draws one 32-bit value
+    for the first gap, then per hit one more for the Pauli choice (DEPOLARIZE1/2) and one for the next gap,
+    four draws per Philox call.  E[ceil(draws / 4)] under the binomial number of hits, per 128 shots, / 128."""
+    from math import comb
+
+    def calls_per_segment(trials, p, choice):
+        if p <= 0:
+            return 0.0
+        if p >= 1:
+            return math.ceil(trials * (1 + choice) / 4)
+        acc, cum, h = 0.0, 0.0, 0
+        while cum < 1 - 1e-12 and h <= trials:
+            pr = comb(trials, h) * p ** h * (1 - p) ** (trials - h)
+            acc += pr * math.ceil((1 + h * (1 + choice)) / 4)
+            cum += pr
+            h += 1
+        return acc
+
+    total = 0.0
+    mult = [1]
+    for line in text.splitlines():
+        line = line.split("#")[0].strip()
+        if not line:
+            continue
+        if line.startswith("REPEAT"):
+            mult.append(mult[-1] * int(line.split()[1]))
+            continue
+        if line == "}":
+            mult.pop()
+            continue
+        m = re.match(r"([A-Z_0-9]+)(?:\(([^)]*)\))?\s*(.*)", line)
+        g, args, targets = m.group(1), m.group(2), m.group(3).split()
+        if g in ("X_ERROR", "Y_ERROR", "Z_ERROR", "DEPOLARIZE1"):
+            units, choice = len(targets), 1 if g == "DEPOLARIZE1" else 0
+        elif g == "DEPOLARIZE2":
+            units, choice = len(targets) // 2, 1
+        elif g in ("M", "MX", "MY", "MR", "MRX", "MRY") and args:
+            units, choice = len(targets), 0
+        else:
+            continue
+        p = float(args)
+        full, rest = divmod(units, 16)
+        seg = full * calls_per_segment(16 * 128, p, choice) + (calls_per_segment(rest * 128, p, choice) if rest else 0)
+        total += mult[-1] * seg / 128.0
+    return total
 
 
 class ClockSampler:
@@ -182,36 +276,147 @@ def _measured_hbm_peak():
     return 6800.0
 
 
+def reference_stim():
+    """The reference's own `stim` binary, built from the reference's sources with the reference's release flags
+    (oracle/Makefile `ref-bench`: g++ -O3 -fno-strict-aliasing; on aarch64 the reference sets no SIMD flag, so it
+    runs on 64-bit words) on first use.  The sources come from $STIM_REFERENCE_TREE or the copy staged under
+    baseline/_ref.  Returns None where neither exists."""
+    arch = os.uname().machine
+    exe = os.path.join(ROOT, "oracle", "_ref", f"bench-{arch}", "stim")
+
+    def runs():
+        try:
+            return subprocess.run([exe, "help"], capture_output=True, timeout=30).returncode == 0
+        except (OSError, subprocess.TimeoutExpired):
+            return False
+
+    if os.path.isfile(exe) and runs():
+        return exe
+    staged = os.path.join(ROOT, "baseline", "_ref", "stim", "file_lists", "source_files_no_main")
+    if not (os.environ.get("STIM_REFERENCE_TREE") or os.path.isfile(staged)):
+        return None
+    jobs = str(max(1, os.cpu_count() or 1))
+    r = subprocess.run(["make", "-s", "-j" + jobs, "-C", os.path.join(ROOT, "oracle"), "ref-bench"],
+                       capture_output=True, text=True)
+    if r.returncode != 0 or not runs():
+        sys.stderr.write("reference build failed:\n" + r.stderr[-2000:] + "\n")
+        return None
+    return exe
+
+
+def reference_compiler():
+    try:
+        return subprocess.run(["g++", "--version"], capture_output=True, text=True).stdout.splitlines()[0]
+    except (OSError, IndexError):
+        return "g++"
+
+
+def time_reference_detect(exe, circuit_path, shots, procs, seed0):
+    """Wall time of `stim detect --shots N --seed s --out_format b8 --append_observables --out /dev/null` as
+    `procs` concurrent processes with distinct seeds, `shots` shots in total (sinter-style sharding of one
+    job over the host cores; procs = 1 is the single-core CLI)."""
+    per = [shots // procs + (1 if i < shots % procs else 0) for i in range(procs)]
+    t0 = time.perf_counter()
+    ps = [subprocess.Popen([exe, "detect", "--shots", str(n), "--seed", str(seed0 + i), "--out_format", "b8",
+                            "--append_observables", "--out", "/dev/null", "--in", circuit_path],
+                           stdout=subprocess.DEVNULL, stderr=subprocess.PIPE) for i, n in enumerate(per) if n]
+    errs = [p.communicate()[1] for p in ps]
+    dt = time.perf_counter() - t0
+    for p, e in zip(ps, errs):
+        if p.returncode != 0:
+            raise RuntimeError("reference stim failed: " + e.decode(errors="replace")[-500:])
+    return dt
+
+
+def _circuit_file(text):
+    import tempfile
+
+    fd, path = tempfile.mkstemp(suffix=".stim")
+    with os.fdopen(fd, "w") as f:
+        f.write(text)
+    return path
+
+
+def reference_cpu_figures(text, D, O, shots_all, shots_one, reps):
+    """The reference's CLI sampler on this host: all cores (one process per core) and one core.  Returns a
+    dict, or None when the reference cannot be built here."""
+    exe = reference_stim()
+    if exe is None:
+        return None
+    path = _circuit_file(text)
+    try:
+        cores = os.cpu_count() or 1
+        time_reference_detect(exe, path, min(shots_all, 4096 * cores), cores, 1000)  # warm page cache
+        all_s = [time_reference_detect(exe, path, shots_all, cores, 100 * k) for k in range(reps)]
+        one_s = [time_reference_detect(exe, path, shots_one, 1, 7)]
+    finally:
+        os.unlink(path)
+    med = statistics.median(all_s)
+    return {"value": shots_all * (D + O) / med / 1e9, "unit": UNIT, "cores": cores, "kind": "reference",
+            "sample": f"stim detect --out_format b8 --append_observables --out /dev/null: {shots_all} shots as "
+                      f"{cores} processes (distinct seeds), median of {reps}; reference built from its own sources "
+                      f"with -O3 -fno-strict-aliasing ({reference_compiler()}), "
+                      f"{'64-bit words (no SIMD flag on aarch64)' if os.uname().machine == 'aarch64' else 'SSE2 128-bit words'}",
+            "one_core": {"value": shots_one * (D + O) / one_s[0] / 1e9, "unit": UNIT, "cores": 1,
+                         "sample": f"{shots_one} shots, one process"},
+            "p50_ms": 1e3 * med, "p99_ms": 1e3 * max(all_s)}
+
+
 def run_reference(args):
+    """The reference arm: the reference's own CPU sampler (its `stim detect` CLI, built from its sources) on the
+    host cores, one process per core, over --ref-shots shots of the main workload per step.  Falls back to the
+    oracle port (oracle/stim_oracle.c) only where the reference's sources are not on this machine."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from oracle.oracle import OracleCircuit
 
     text = circuit_text()
-    c = OracleCircuit(text)
-    D, O = c.num_detectors, c.num_observables
-    threads = os.cpu_count() or 1
-    sample_shots = args.ref_shots
-    for _ in range(args.warmup):
-        c.sample(sample_shots, 0, threads=threads)
+    exe = reference_stim()
+    cores = os.cpu_count() or 1
     times = []
-    for k in range(args.steps):
-        t0 = time.perf_counter()
-        c.sample(sample_shots, 1 + k, threads=threads)
-        times.append(time.perf_counter() - t0)
+    oc = OracleCircuit(text)  # detector and observable counts (nothing of the GPU library runs in this arm)
+    D, O = oc.num_detectors, oc.num_observables
+    if exe is not None:
+        path = _circuit_file(text)
+        try:
+            for k in range(args.warmup):
+                time_reference_detect(exe, path, args.ref_shots, cores, 10_000 + k * cores)
+            for k in range(args.steps):
+                times.append(time_reference_detect(exe, path, args.ref_shots, cores, 20_000 + k * cores))
+            one = time_reference_detect(exe, path, args.ref_shots // 16, 1, 7)
+        finally:
+            os.unlink(path)
+        kind = "reference"
+        simd = "64-bit words (no SIMD flag on aarch64)" if os.uname().machine == "aarch64" else "SSE2 128-bit words"
+        note = (f"the reference's `stim detect --out_format b8 --append_observables --out /dev/null`, built from "
+                f"its own sources with its release flags (-O3 -fno-strict-aliasing, {reference_compiler()}), "
+                f"{simd}; one process per host core with distinct seeds, shots split evenly")
+        extra = {"one_core": {"value": (args.ref_shots // 16) * (D + O) / one / 1e9, "unit": UNIT, "cores": 1,
+                              "sample": f"{args.ref_shots // 16} shots, one process"}}
+    else:
+        c = oc
+        for _ in range(args.warmup):
+            c.sample(args.ref_shots, 0, threads=cores)
+        for k in range(args.steps):
+            t0 = time.perf_counter()
+            c.sample(args.ref_shots, 1 + k, threads=cores)
+            times.append(time.perf_counter() - t0)
+        kind = "port"
+        note = ("oracle port (oracle/stim_oracle.c, pthreads over 1024-shot batches, 64-bit words): the reference's "
+                "sources are not on this machine")
+        extra = {}
     total = sum(times)
-    value = args.steps * sample_shots * (D + O) / total / 1e9
+    value = args.steps * args.ref_shots * (D + O) / total / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 bitwise",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 bitwise",
         "data": "synthetic (reference-generated circuit, seeded shots)",
-        "config": {"workload": "surface_code:rotated_memory_z d=25 r=25 p=1e-3", "shots_per_step": sample_shots,
-                   "note": "oracle port (oracle/stim_oracle.c, pthreads over 1024-shot batches, 64-bit words) on "
-                           "the host cores; the reference's own sources are not available on this machine"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{sample_shots} shots per step x {args.steps} steps, 64-bit words"},
+        "config": {"workload": "surface_code:rotated_memory_z d=25 r=25 p=1e-3", "shots_per_step": args.ref_shots,
+                   "note": note},
+        "cpu_baseline": dict({"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                              "sample": f"{args.ref_shots} shots per step x {args.steps} steps"}, **extra),
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "p50_ms": 1e3 * statistics.median(times),
         "p99_ms": 1e3 * sorted(times)[min(len(times) - 1, int(math.ceil(0.99 * len(times))) - 1)],
@@ -270,7 +475,7 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    frame_ms, noise_ms, step_ms, launches, frame_launches = [], [], [], 0, 0
+    frame_ms, noise_ms, step_ms, launches, frame_launches, noise_launches = [], [], [], 0, 0, 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
         flush.zero_()  # outputs exceed L2 anyway; also evict them between steps
@@ -280,6 +485,7 @@ def run_gpu(args):
         step_ms.append(t["frame_ms"] + t["noise_ms"] + t["transpose_ms"])
         launches += t["frame_launches"] + t["noise_launches"] + t["transpose_launches"]
         frame_launches += t["frame_launches"]
+        noise_launches += t["noise_launches"]
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     if world > 1:
@@ -300,12 +506,14 @@ def run_gpu(args):
         times, parts = [], []
         if args.e2e_steps <= 0:
             return times, parts
-        for k in range(E2E_WARMUP + args.e2e_steps):
-            t1 = time.perf_counter()
-            sampler.sample(shots, bit_packed=True, separate_observables=True, dets_out=dets_arr, obs_out=obs_arr)
-            if k >= E2E_WARMUP:
-                times.append(time.perf_counter() - t1)
-                parts.append(sampler.last_timings())
+        with quiet_gc():
+            for k in range(E2E_WARMUP + args.e2e_steps):
+                t1 = time.perf_counter()
+                sampler.sample(shots, bit_packed=True, separate_observables=True, dets_out=dets_arr,
+                               obs_out=obs_arr)
+                if k >= E2E_WARMUP:
+                    times.append(time.perf_counter() - t1)
+                    parts.append(sampler.last_timings())
         return times, parts
 
     pin_rows = shots if args.e2e_steps > 0 else 0
@@ -322,11 +530,20 @@ def run_gpu(args):
     achieved_gbs = acc_bits / 8 * shots / frame_avg_s / 1e9
     shots_per_frame_launch = shots * args.steps / max(1, frame_launches)
     smem_peak = _native.measure_smem_peak(local) / 1e9
+    int_peaks = _native.measure_int_peaks(local)
+    # Noise kernel: Philox calls per launch (the contract's expected count) / its CUDA-event time, against the
+    # Philox probe's calls/s on the same GPU.
+    philox_per_shot = noise_philox_calls(text)
+    noise_avg_s = statistics.mean(noise_ms) / 1e3 * args.steps / max(1, noise_launches)
+    shots_per_noise_launch = shots * args.steps / max(1, noise_launches)
+    noise_achieved = philox_per_shot * shots_per_noise_launch / noise_avg_s if noise_launches else None
+    link = measure_link(local)
     # Transpose: reads the detector-major rows (16 bytes per row per 128 shots) and writes the shot-major rows.
     tr_ms = statistics.mean(t - f - z for t, f, z in zip(step_ms, frame_ms, noise_ms))
     tr_bytes = shots * ((D + O) / 8 + drow + orow)
     hbm_peak = _measured_hbm_peak()
 
+    configs = run_configs(args, local) if args.config_steps > 0 else None
     batched = run_batched(args, local) if args.batched else None
     serving = run_serving(args, local) if args.serve_seconds > 0 else None
     m2d = run_m2d(args, local, text) if args.m2d_steps > 0 else None
@@ -363,7 +580,9 @@ def run_gpu(args):
                                  "p50_ms": 1e3 * statistics.median(page_times) if page_times else None,
                                  "p99_ms": 1e3 * max(page_times) if page_times else None,
                                  "api": "the same call into reused pageable numpy arrays"},
-                    "link_bound_ms": 1e3 * shots * (drow + orow) / LINK_GBS / 1e9,
+                    "link": dict(link, note="cudaMemcpyAsync of 2 GiB between HBM and page-locked host memory, "
+                                                   "best of 5, measured in this run"),
+                    "link_bound_ms": 1e3 * shots * (drow + orow) / (link["d2h_gbs"] * 1e9),
                     "device_ms": {k: statistics.mean(p[k] for p in e2e_parts) for k in
                                   ("frame_ms", "noise_ms", "transpose_ms", "copy_ms", "total_ms")}
                     if e2e_parts else None},
@@ -375,6 +594,17 @@ def run_gpu(args):
                                          "launch); shared memory, not DRAM, bounds this kernel",
                          "basis": f"{acc_bits:.0f} frame-bit accesses/shot x {shots} shots per frame-kernel launch; "
                                   "peak = project shared-memory probe (gfs_measure_smem_peak)"},
+            "roofline_noise": {"bound": "integer issue (Philox4x32-10)", "achieved": noise_achieved,
+                               "peak": int_peaks["philox_per_s"], "unit": "Philox calls/s",
+                               "frac": noise_achieved / int_peaks["philox_per_s"] if noise_achieved else None,
+                               "philox_calls_per_shot": philox_per_shot, "ms_per_launch": 1e3 * noise_avg_s,
+                               "shots_per_launch": shots_per_noise_launch,
+                               "basis": "expected Philox calls of the random-bit contract per shot (segments of "
+                                        "16 units x 128 shots: first gap draw, then per hit a choice draw for "
+                                        "DEPOLARIZE1/2 and a gap draw, 4 draws per call) x shots per noise-kernel "
+                                        "launch / its CUDA-event time; peak = project Philox probe "
+                                        "(gfs_measure_int_peaks)"},
+            "lop3_peak_ops_per_s": int_peaks["lop3_per_s"],
             "roofline_transpose": {"bound": "hbm", "achieved": tr_bytes / (tr_ms / 1e3) / 1e9, "peak": hbm_peak,
                                    "unit": "GB/s", "frac": tr_bytes / (tr_ms / 1e3) / 1e9 / hbm_peak,
                                    "basis": "detector-major rows read + shot-major rows written per step; "
@@ -385,6 +615,7 @@ def run_gpu(args):
                              "one_core": {"value": cb1_value, "unit": UNIT, "cores": 1,
                                           "sample": f"{cb1_shots} shots in 4096-shot calls ({cb1_s:.1f} s)"}},
             "clocks": clk,
+            "configs": configs,
             "batched": batched,
             "serving": serving,
             "m2d": m2d,
@@ -405,11 +636,12 @@ def _pinned(shape):
 def _median_ms(fn, steps):
     """Median wall time of `steps` calls of fn after E2E_WARMUP untimed calls (which touch the arrays' pages)."""
     times = []
-    for k in range(E2E_WARMUP + steps):
-        t0 = time.perf_counter()
-        fn()
-        if k >= E2E_WARMUP:
-            times.append(time.perf_counter() - t0)
+    with quiet_gc():
+        for k in range(E2E_WARMUP + steps):
+            t0 = time.perf_counter()
+            fn()
+            if k >= E2E_WARMUP:
+                times.append(time.perf_counter() - t0)
     return 1e3 * statistics.median(times)
 
 
@@ -503,6 +735,83 @@ def run_feed(args, local, text):
             "discards": last["discards"], "detection_events_per_shot": last["events"] / shots}
 
 
+def run_configs(args, local):
+    """The two smaller configurations of the metric, each through the device entry point (kernels only, CUDA
+    events) and the public API into page-locked host arrays (device->host copies included), beside the
+    reference's own CLI sampler and the oracle port on the host cores:
+      plain CPU-runnable: surface_code:rotated_memory_z d=3 r=3 p=1e-3, 65,536 shots, seed 0;
+      plain GPU: surface_code:rotated_memory_x d=11 r=11, p in {1e-3, 5e-3, 0}, 2^20 shots, seeds 0..3
+      (p = 0 must give no detection events)."""
+    import numpy as np
+    import torch
+
+    import stim_gb300
+    from oracle.oracle import OracleCircuit
+    from stim_gb300 import _native, workloads
+
+    L = _native.lib()
+    dev = f"cuda:{local}"
+    exe = reference_stim()
+    cases = [("surface_code:rotated_memory_z", 3, 0.001, 1 << 16, [0])]
+    cases += [("surface_code:rotated_memory_x", 11, p, 1 << 20, [0, 1, 2, 3]) for p in (0.001, 0.005, 0.0)]
+    out = []
+    for family, d, p, shots, seeds in cases:
+        text = workloads.code_circuit(family, d, d, p)
+        c = stim_gb300.Circuit(text)
+        D, O = c.num_detectors, c.num_observables
+        drow, orow = (D + 7) // 8, (O + 7) // 8
+        bits = shots * (D + O)
+        dd = torch.empty((shots, drow), dtype=torch.uint8, device=dev)
+        od = torch.empty((shots, orow), dtype=torch.uint8, device=dev)
+        hd, ho = _pinned((shots, drow)), _pinned((shots, orow))
+        dev_ms, e2e_ms, events = [], [], 0
+        with quiet_gc():
+            for seed in seeds:
+                s = c.compile_detector_sampler(seed=seed, device=local)
+                for k in range(E2E_WARMUP + max(3, args.config_steps)):
+                    _native.check(L.gfs_sample_detections_device(s._h, shots, _native.BIT_PACKED, dd.data_ptr(), drow,
+                                                                 od.data_ptr(), orow))
+                    t = s.last_timings()
+                    if k >= E2E_WARMUP:
+                        dev_ms.append(t["frame_ms"] + t["noise_ms"] + t["transpose_ms"])
+                s = c.compile_detector_sampler(seed=seed, device=local)
+                for k in range(E2E_WARMUP + max(3, args.config_steps)):
+                    t0 = time.perf_counter()
+                    s.sample(shots, bit_packed=True, separate_observables=True, dets_out=hd, obs_out=ho)
+                    if k >= E2E_WARMUP:
+                        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+                if p == 0:
+                    events += int(np.count_nonzero(hd)) + int(np.count_nonzero(ho))
+        row = {"workload": f"{family} d={d} r={d} p={p:g}, {shots} shots, seeds {seeds}",
+               "detectors": D, "observables": O,
+               "value": bits / (statistics.median(dev_ms) / 1e3) / 1e9,
+               "e2e": {"value": bits / (statistics.median(e2e_ms) / 1e3) / 1e9,
+                       "p50_ms": statistics.median(e2e_ms), "p99_ms": max(e2e_ms),
+                       "d2h_bytes_per_call": shots * (drow + orow)},
+               "device_ms_p50": statistics.median(dev_ms)}
+        if p == 0:
+            row["zero_detection_events"] = events == 0  # every seed's last end-to-end output, all bytes
+        if exe is not None:
+            path = _circuit_file(text)
+            try:
+                cores = os.cpu_count() or 1
+                all_s = statistics.median(time_reference_detect(exe, path, shots, cores, 50 + 10 * k)
+                                          for k in range(3))
+                one_s = time_reference_detect(exe, path, min(shots, 1 << 16), 1, 5)
+            finally:
+                os.unlink(path)
+            row["reference_cpu"] = {"value": bits / all_s / 1e9, "cores": cores,
+                                    "one_core": min(shots, 1 << 16) * (D + O) / one_s / 1e9,
+                                    "kind": "reference", "unit": UNIT}
+        oc = OracleCircuit(text)
+        t0 = time.perf_counter()
+        oc.sample(shots, 1, threads=os.cpu_count() or 1)
+        row["port_cpu"] = {"value": bits / (time.perf_counter() - t0) / 1e9, "cores": os.cpu_count() or 1,
+                           "kind": "port", "unit": UNIT}
+        out.append(row)
+    return out
+
+
 def run_batched(args, local):
     """The many-circuit workload: 256 rotated surface-code circuits (d in 3..17, rounds = d, p log-uniform in
     [1e-4, 1e-2], shots log-uniform in [2^12, 2^20], one seed each) sampled (a) in one batched persistent
@@ -529,9 +838,14 @@ def run_batched(args, local):
     for _ in range(args.warmup):
         batch.sample_device(shots, dptr, dstr, optr, ostr)
     torch.cuda.synchronize()
-    times, frame = [], []
+    # Both forms are timed the same way: host wall clock around a call that returns with its work complete
+    # (sample_device synchronizes; the sequential loop is followed by a synchronize).  The batched call's CUDA
+    # events (graph replay, and its frame-kernel part) are reported beside it.
+    wall, times, frame = [], [], []
     for _ in range(args.steps):
+        t0 = time.perf_counter()
         batch.sample_device(shots, dptr, dstr, optr, ostr)
+        wall.append(time.perf_counter() - t0)
         t = batch.last_timings()
         times.append(t["total_ms"])
         frame.append(t["frame_ms"])
@@ -554,15 +868,17 @@ def run_batched(args, local):
         torch.cuda.synchronize()
         seq.append(time.perf_counter() - t0)
     seq_s = statistics.median(seq)
-    bat_s = statistics.median(times) / 1e3
+    bat_s = statistics.median(wall)
     return {
         "workload": f"{len(wl)} rotated surface-code memory-Z circuits, d in 3..17 (rounds = d), p log-uniform "
                     "[1e-4, 1e-2], shots log-uniform [2^12, 2^20], generator seed 2024",
         "total_shots": sum(shots), "total_bits": bits,
-        "batched_gbits": bits / bat_s / 1e9, "batched_p50_ms": statistics.median(times),
-        "batched_p99_ms": max(times), "batched_frame_ms": statistics.median(frame),
+        "batched_gbits": bits / bat_s / 1e9, "batched_p50_ms": 1e3 * statistics.median(wall),
+        "batched_p99_ms": 1e3 * max(wall), "batched_graph_ms": statistics.median(times),
+        "batched_frame_ms": statistics.median(frame),
         "sequential_gbits": bits / seq_s / 1e9, "sequential_ms": 1e3 * seq_s,
-        "speedup": seq_s / bat_s, "launch_shape": batch.launch_shape(), "autotune_best_frame_ms": tune_ms,
+        "speedup": seq_s / bat_s, "timing": "host wall clock around a completed call, both forms (median)",
+        "launch_shape": batch.launch_shape(), "autotune_best_frame_ms": tune_ms,
         "graph_launches": t["graph_launches"], "graph_builds": t["graph_builds"],
         "note": "device-resident outputs; batched = one persistent frame-kernel launch + per-circuit transposes "
                 "in one CUDA graph; sequential = one gfs_sample_detections_device call per circuit",
@@ -680,7 +996,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--shots", type=int, default=1 << 20)
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--cpu-chunk", type=int, default=1 << 16)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-shots", type=int, default=1 << 20)
@@ -689,6 +1005,7 @@ def main():
     ap.add_argument("--noise-mode", type=int, default=-1, help="-1 automatic, 0 inline, 1 hit lists")
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--batched", type=int, default=1)
+    ap.add_argument("--config-steps", type=int, default=5, help="timed calls per seed of the d=3 and d=11 legs")
     ap.add_argument("--m2d-steps", type=int, default=5)
     ap.add_argument("--dem-steps", type=int, default=5)
     ap.add_argument("--feed-steps", type=int, default=3)

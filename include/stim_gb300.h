@@ -149,7 +149,10 @@ gfs_status gfs_sample_detections_device(gfs_sampler *s, uint64_t shots, uint32_t
  * program once, at set-up.
  *
  * The first call on a device looks up the array's device address (cudaGetSymbolAddress, with that
- * device current); make that first call before any stream capture.  Circuits needing more than 64 MiB
+ * device current); make that first call before any stream capture.  CUDA loads modules lazily by
+ * default, so that first call is also when the array is placed in the device's memory: make it before
+ * reserving the rest of HBM for your own pool.  Circuits whose measurement ring or frames need global
+ * memory (beyond the array) are rejected with GFS_ERR_INVALID_ARGUMENT.  Circuits needing more than 64 MiB
  * of scratch for one CTA's slice of shots are rejected with GFS_ERR_INVALID_ARGUMENT.  Larger shot
  * counts are processed in chunks that fit.  All calls share the array and it keeps the last call's
  * contents (nothing in it needs to start at zero: every scratch row is written before it is read).
@@ -201,6 +204,14 @@ gfs_status gfs_sampler_set_ring_placement(gfs_sampler *s, int placement);
  * the reference (it has no GPU code).
  */
 gfs_status gfs_measure_smem_peak(int device, double *bytes_per_s);
+
+/*
+ * Measures the integer-issue peaks of `device` with project-written probe kernels: 32-bit three-input logic
+ * operations per second (lop3, the frame kernel's arithmetic) and Philox4x32-10 generator calls per second
+ * (the noise kernel's random-draw work), each summed over all SMs.  Roofline denominators for the
+ * instruction-bound kernels.  No counterpart in the reference (it has no GPU code).
+ */
+gfs_status gfs_measure_int_peaks(int device, double *lop3_per_s, double *philox_per_s);
 
 /* Maximum shots per device chunk (bounds HBM use); 0 restores the default. */
 gfs_status gfs_sampler_set_chunk_shots(gfs_sampler *s, uint64_t shots);

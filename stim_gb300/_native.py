@@ -59,6 +59,7 @@ def _declare(L):
         "gfs_sampler_get_stream_position": [_vp, ctypes.POINTER(_u64)],
         "gfs_sampler_set_ring_placement": [_vp, ctypes.c_int],
         "gfs_measure_smem_peak": [ctypes.c_int, ctypes.POINTER(ctypes.c_double)],
+        "gfs_measure_int_peaks": [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
         "gfs_sampler_autotune": [_vp, _u64, ctypes.POINTER(ctypes.c_double)],
         "gfs_sampler_set_noise_mode": [_vp, ctypes.c_int],
         "gfs_sampler_set_hit_capacity": [_vp, _u64],
@@ -139,6 +140,14 @@ def measure_smem_peak(device: int = 0) -> float:
     v = ctypes.c_double(0)
     check(lib().gfs_measure_smem_peak(int(device), ctypes.byref(v)))
     return v.value
+
+
+def measure_int_peaks(device: int = 0) -> dict:
+    """Integer-issue peaks of the device from the library's probe kernels: 32-bit lop3 ops/s and Philox4x32-10
+    calls/s."""
+    a, b = ctypes.c_double(0), ctypes.c_double(0)
+    check(lib().gfs_measure_int_peaks(int(device), ctypes.byref(a), ctypes.byref(b)))
+    return {"lop3_per_s": a.value, "philox_per_s": b.value}
 
 
 def device_info(device: int = 0) -> dict:

@@ -137,7 +137,9 @@ struct gfs_batch {
             ck(cudaStreamBeginCapture(eng.stream, cudaStreamCaptureModeThreadLocal), "graph capture");
             try {
                 eng.enqueue_frame();
-                ck(cudaEventRecord(eng.ev[1], eng.stream), "event");
+                // An external event-record node: it records ev[1] on every replay, splitting the frame kernel
+                // from the transposes (a plain record made during capture would not be a timing point).
+                ck(cudaEventRecordWithFlags(eng.ev[1], eng.stream, cudaEventRecordExternal), "event");
                 calls = eng.enqueue_transposes(es, flags);
             } catch (...) {
                 cudaStreamEndCapture(eng.stream, &graph);

@@ -87,8 +87,14 @@ void detections_noalloc(gfs_sampler *s, uint64_t shots, uint32_t flags, uint8_t 
         if (shape.ring_global) {
             shape.ring_global = false;
             shape.smem = s->smem_for(shape.blocks_per_cta, false);
+            int optin = 0;
+            ck(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device), "device attribute");
             int per_sm = 0;
-            ck(gfs::frame_kernel_max_ctas_per_sm(shape, &per_sm), "occupancy");
+            if (shape.smem <= (size_t)optin &&
+                gfs::frame_kernel_max_ctas_per_sm(shape, &per_sm) != cudaSuccess) {
+                cudaGetLastError();  // a failed query must not surface as the error of a later launch
+                per_sm = 0;
+            }
             if (per_sm < 1) {
                 throw std::invalid_argument("the circuit's measurement ring does not fit in shared memory, which the "
                                             "allocation-free entry point requires");
@@ -432,6 +438,13 @@ gfs_status gfs_measure_smem_peak(int device, double *bytes_per_s) {
     return guarded([&] {
         ck(cudaSetDevice(device), "cudaSetDevice");
         ck(gfs::measure_smem_peak(bytes_per_s), "shared-memory probe");
+    });
+}
+
+gfs_status gfs_measure_int_peaks(int device, double *lop3_per_s, double *philox_per_s) {
+    return guarded([&] {
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        ck(gfs::measure_int_peaks(lop3_per_s, philox_per_s), "integer-issue probe");
     });
 }
 

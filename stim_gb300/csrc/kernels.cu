@@ -2365,4 +2365,105 @@ cudaError_t measure_smem_peak(double *bytes_per_s) {
     return cudaGetLastError();
 }
 
+
+// ------------------------------------------------------------------------------------------------
+// Integer-issue probes (the denominators of the instruction-bound rooflines):
+// * lop3_probe_kernel: eight independent chains of 3-input logic ops (lop3.b32 XOR3) per thread, the
+//   operation the frame kernel's gate updates are made of; reports 32-bit logic ops per second.
+// * philox_probe_kernel: back-to-back Philox4x32-10 calls (the contract's generator) on distinct counters,
+//   four independent streams per thread; reports generator calls per second, the peak of the noise kernel's
+//   random-draw work.
+// Both run one full wave of 1024-thread CTAs on every SM.
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) lop3_probe_kernel(uint32_t iters, uint32_t *sink) {
+    uint32_t a[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        a[j] = threadIdx.x * 2654435761u + (uint32_t)j * 40503u + blockIdx.x;
+    }
+    const uint32_t b = blockIdx.x * 97u + 1u, c = threadIdx.x ^ 0x5bd1e995u;
+    for (uint32_t it = 0; it < iters; it++) {
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                asm volatile("lop3.b32 %0, %0, %1, %2, 0x96;" : "+r"(a[j]) : "r"(b), "r"(c + (uint32_t)k));
+            }
+        }
+    }
+    uint32_t x = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        x ^= a[j];
+    }
+    if (x == 0x9E3779B9u) {
+        atomicAdd(sink, 1u);
+    }
+}
+
+__global__ void __launch_bounds__(1024) philox_probe_kernel(uint32_t iters, uint32_t *sink) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    // The key is a run-time value, as the seed is in the sampling kernels (so its schedule is not folded).
+    const uint32_t k0 = iters * 0x9E3779B9u + 17u, k1 = iters ^ 0x85EBCA6Bu;
+    uint32_t x = 0;
+    for (uint32_t it = 0; it < iters; it++) {
+#pragma unroll
+        for (uint32_t j = 0; j < 4; j++) {
+            const gfs_u32x4 r = gfs_philox(k0, k1, t, it, j, GFS_P_NOISE << 28);
+            x ^= r.v[0] ^ r.v[1] ^ r.v[2] ^ r.v[3];
+        }
+    }
+    if (x == 0x9E3779B9u) {
+        atomicAdd(sink, 1u);
+    }
+}
+
+// Runs `kernel` for one full wave (resident 1024-thread CTAs on every SM) and returns seconds.
+template <typename K>
+static cudaError_t time_probe(K kernel, uint32_t iters, double *seconds, double *threads) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, dev);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 1024, 0);
+    if (e != cudaSuccess) return e;
+    const int grid = prop.multiProcessorCount * (per_sm > 0 ? per_sm : 1);
+    uint32_t *sink = nullptr;
+    e = cudaMalloc(&sink, 4);
+    if (e != cudaSuccess) return e;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    kernel<<<grid, 1024>>>(iters / 16 + 1, sink);  // warm-up
+    cudaEventRecord(a);
+    kernel<<<grid, 1024>>>(iters, sink);
+    cudaEventRecord(b);
+    e = cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(sink);
+    if (e != cudaSuccess) return e;
+    *seconds = ms * 1e-3;
+    *threads = (double)grid * 1024.0;
+    return cudaGetLastError();
+}
+
+cudaError_t measure_int_peaks(double *lop3_per_s, double *philox_per_s) {
+    double s = 0, th = 0;
+    const uint32_t lop_iters = 4096;
+    cudaError_t e = time_probe(lop3_probe_kernel, lop_iters, &s, &th);
+    if (e != cudaSuccess) return e;
+    *lop3_per_s = th * lop_iters * 16.0 * 8.0 / s;
+    const uint32_t ph_iters = 256;
+    e = time_probe(philox_probe_kernel, ph_iters, &s, &th);
+    if (e != cudaSuccess) return e;
+    *philox_per_s = th * ph_iters * 4.0 / s;
+    return cudaSuccess;
+}
+
 }  // namespace gfs

@@ -205,5 +205,7 @@ cudaError_t launch_feed_compact(const FeedArgs &args, cudaStream_t stream);
 
 // Shared-memory load+store throughput of the current device (bytes per second over all SMs).
 cudaError_t measure_smem_peak(double *bytes_per_s);
+// 32-bit three-input logic ops per second and Philox4x32-10 calls per second over the whole GPU.
+cudaError_t measure_int_peaks(double *lop3_per_s, double *philox_per_s);
 
 }  // namespace gfs

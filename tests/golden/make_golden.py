@@ -4,7 +4,8 @@ Run in a container where the reference tree exists (it is never copied into this
 
     make -C oracle ref                 # builds oracle/_ref/stim and oracle/_ref/ref_inject from the
                                        # reference's own sources
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py                 # everything
+    python tests/golden/make_golden.py --only=NAME     # one sampling fixture (repeatable)
 
 It writes
   * tests/golden/circuits/*.stim  circuits made by the reference's generator (`stim gen`) with all four
@@ -107,6 +108,12 @@ def cases():
         ("random_clifford_n64_d200_s2", rc(64, 200, 2), 12, 512),
         ("random_clifford_n128_d200_s3", rc(128, 200, 3), 13, 256),
         ("random_clifford_n300_d60_s4", rc(300, 60, 4), 14, 256),
+        # The configured random-Clifford sizes (n = 256 and 512 qubits, depth 200).
+        ("random_clifford_n256_d200_s25", rc(256, 200, 25), 25, 256),
+        ("random_clifford_n512_d200_s26", rc(512, 200, 26), 26, 256),
+        # The benchmarked circuit itself: distance 25, 25 rounds, p = 1e-3 (one CTA block per 128 shots,
+        # measurement ring in global memory, every randomization removed by the lowering's analysis).
+        ("surface_rz_d25_r25_p0.001", cc("surface_code:rotated_memory_z", 25, 25, 0.001), 0, 1024),
     ]
 
 
@@ -187,13 +194,18 @@ def main():
     if "--refsample-only" in sys.argv:
         refsample_fixtures()
         return
-    gen_templates()
+    only = [a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")]
+    if not only:
+        gen_templates()
     for name, text, seed, shots in cases():
+        if only and name not in only:
+            continue
         out = run_ref(text, seed, shots)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), circuit=np.array(text), seed=np.uint64(seed),
                             shots=np.uint64(shots), **out)
         print(name, out["num_detectors"], out["num_measurements"], shots)
-    refsample_fixtures()
+    if not only:
+        refsample_fixtures()
 
 
 if __name__ == "__main__":

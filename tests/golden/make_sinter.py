@@ -2,7 +2,7 @@
 classify_discards_and_errors, read (as text, through `ast`) from the reference's own test file
 glue/sample/src/sinter/_decoding/_stim_then_decode_sampler_test.py.  Nothing of sinter is imported or run.
 
-    python tests/golden/make_sinter.py [path/to/reference/root]
+    python tests/golden/make_sinter.py path/to/reference/root     (or set STIM_REFERENCE_TREE)
 """
 
 import ast
@@ -10,7 +10,9 @@ import json
 import os
 import sys
 
-ROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("STIM_REFERENCE_TREE", "")
+if not ROOT:
+    sys.exit("usage: make_sinter.py path/to/reference/root (or set STIM_REFERENCE_TREE)")
 SRC = os.path.join(ROOT, "glue/sample/src/sinter/_decoding/_stim_then_decode_sampler_test.py")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "sinter", "classify_cases.json")
 

@@ -117,13 +117,39 @@ def test_separate_with_append_raises():
 @pytest.mark.parametrize("seed", [0, 1, 2, 3])
 @pytest.mark.parametrize("p", [0.001, 0.005])
 def test_surface_d11_matches_oracle(seed, p):
+    # The plain-GPU configuration: rotated memory-X, distance 11, 11 rounds, 2^20 shots, seeds 0..3.
     text = workloads.code_circuit("surface_code:rotated_memory_x", 11, 11, p)
-    shots = 8192
+    shots = 1 << 20
     gd, go = stim_gb300.Circuit(text).compile_detector_sampler(seed=seed).sample(
         shots, separate_observables=True, bit_packed=True)
-    od, oo, _ = OracleCircuit(text).sample(shots, seed, threads=8)
+    od, oo, _ = OracleCircuit(text).sample(shots, seed, threads=_THREADS)
     np.testing.assert_array_equal(gd, od)
     np.testing.assert_array_equal(go, oo)
+
+
+_THREADS = max(1, min(32, os.cpu_count() or 1))
+
+
+@pytest.mark.parametrize("mode,shots,autotune", [(1, 1 << 20, True), (1, 1 << 17, False), (0, 1 << 17, False)])
+def test_surface_d25_benchmark_chunk_matches_oracle(mode, shots, autotune):
+    # The benchmarked step: distance 25, 25 rounds, p = 1e-3, seed 0, hit-list noise with the launch shape the
+    # autotuner picks (as the benchmark does) over a whole 2^20-shot chunk, and both noise modes at the default
+    # shape.  The oracle is pinned to the reference's own FrameSimulator on this circuit by the
+    # surface_rz_d25_r25_p0.001 fixture.
+    text = workloads.code_circuit("surface_code:rotated_memory_z", 25, 25, 0.001)
+    s = stim_gb300.Circuit(text).compile_detector_sampler(seed=0)
+    s.set_noise_mode(mode)
+    if autotune:
+        s.autotune(1 << 18)
+    gd, go = s.sample(shots, separate_observables=True, bit_packed=True)
+    od, oo, _ = OracleCircuit(text).sample(shots, 0, threads=_THREADS)
+    np.testing.assert_array_equal(gd, od)
+    np.testing.assert_array_equal(go, oo)
+    assert gd.any()
+    t = s.last_timings()
+    assert t["frame_launches"] >= 1
+    if mode == 0:
+        assert t["noise_launches"] == 0
 
 
 def test_noiseless_surface_d11_gives_zero_detection_events():

@@ -11,6 +11,9 @@ This file is collected last so that, if it fails, a run that stops at the first 
 every other test.
 """
 
+import os
+
+import numpy as np
 import pytest
 
 import stim_gb300
@@ -68,3 +71,40 @@ def test_noalloc_rejects_circuits_beyond_its_fixed_scratch():
     dets, obs = _buffers(torch, shots, (circ.num_detectors + 7) // 8, 1)
     with pytest.raises(ValueError, match="allocation-free entry point holds"):
         _call(L.gfs_sample_detections_device_noalloc, s, shots, _native.BIT_PACKED, dets, obs)
+
+
+def test_noalloc_matches_reference_fixture_at_distance_25():
+    # The benchmarked circuit (distance 25, 25 rounds, p = 1e-3): the allocation-free entry point reproduces
+    # the detection events and observable flips that the reference's own FrameSimulator produced on the same
+    # injected random stream (tests/golden/surface_rz_d25_r25_p0.001.npz), on two calls in a row.
+    torch = pytest.importorskip("torch")
+    L = _native.lib()
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                  "surface_rz_d25_r25_p0.001.npz")))
+    circ = stim_gb300.Circuit(str(g["circuit"]))
+    s = circ.compile_detector_sampler(seed=int(g["seed"]))
+    total = int(g["shots"])
+    half = total // 2
+    for k, (lo, hi) in enumerate([(0, half), (half, total)]):
+        dets, obs = _buffers(torch, hi - lo, g["dets"].shape[1], g["obs"].shape[1])
+        _call(L.gfs_sample_detections_device_noalloc, s, hi - lo, _native.BIT_PACKED, dets, obs)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(dets.cpu().numpy(), g["dets"][lo:hi], err_msg=f"call {k}")
+        np.testing.assert_array_equal(obs.cpu().numpy(), g["obs"][lo:hi], err_msg=f"call {k}")
+
+
+def test_noalloc_rejects_a_ring_that_needs_global_memory_and_later_calls_still_work():
+    torch = pytest.importorskip("torch")
+    L = _native.lib()
+    # A lookback of 20,000 measurements: the ring (20,000 rows x 16 bytes per 128 shots) only fits in global
+    # memory, which the allocation-free entry point does not use.
+    text = "REPEAT 20000 {\n    X_ERROR(0.1) 0\n    M 0\n}\nDETECTOR rec[-1] rec[-20000]\n"
+    circ = stim_gb300.Circuit(text)
+    s = circ.compile_detector_sampler(seed=3)
+    dets, obs = _buffers(torch, 256, 1, 1)
+    with pytest.raises(ValueError, match="measurement ring does not fit in shared memory"):
+        _call(L.gfs_sample_detections_device_noalloc, s, 256, _native.BIT_PACKED, dets, obs)
+    # The rejected call leaves no CUDA error behind: the ordinary entry point still samples this circuit.
+    _call(L.gfs_sample_detections_device, s, 256, _native.BIT_PACKED, dets, obs)
+    torch.cuda.synchronize()
+    assert int(dets.sum()) > 0
