@@ -229,6 +229,14 @@ gfs_status gfs_sampler_get_stream_position(const gfs_sampler *s, uint64_t *shot)
  * identical either way.  No counterpart in the reference.
  */
 gfs_status gfs_sampler_set_noise_mode(gfs_sampler *s, int mode);
+/*
+ * Frame kernel for hit-list launches: 1 (default, -1 = automatic) the lean kernel when the program has a lean
+ * phase list (no correlated errors, heralds or sweep feedback; compact unit lists; at most two loop levels),
+ * 0 the generic kernel.  Results are identical either way.  gfs_sampler_get_frame_kernel reports which one the
+ * next hit-list launch uses (1 lean, 0 generic).  No counterpart in the reference.
+ */
+gfs_status gfs_sampler_set_frame_kernel(gfs_sampler *s, int kind);
+gfs_status gfs_sampler_get_frame_kernel(const gfs_sampler *s, int *kind);
 /* Noise-kernel time (ms) of the last sample call; gfs_sampler_last_timings' frame time excludes it. */
 gfs_status gfs_sampler_last_noise_ms(const gfs_sampler *s, double *ms);
 /* Hit-list region capacity in records per noise occurrence and slice (0 = automatic: expected hits plus a

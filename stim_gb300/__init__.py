@@ -203,7 +203,15 @@ class _SamplerBase:
         sm = ctypes.c_uint64()
         check(lib().gfs_sampler_get_shape(self._h, ctypes.byref(b), ctypes.byref(t), ctypes.byref(g),
                                           ctypes.byref(sm)))
-        return {"blocks_per_cta": b.value, "threads": t.value, "grid": g.value, "smem_bytes": sm.value}
+        k = ctypes.c_int()
+        check(lib().gfs_sampler_get_frame_kernel(self._h, ctypes.byref(k)))
+        return {"blocks_per_cta": b.value, "threads": t.value, "grid": g.value, "smem_bytes": sm.value,
+                "kernel": "lean" if k.value == 1 else "generic"}
+
+    def set_frame_kernel(self, kind: int):
+        """Frame kernel of hit-list launches: -1 automatic, 0 generic, 1 lean when the program has a lean phase
+        list.  Results are identical."""
+        check(lib().gfs_sampler_set_frame_kernel(self._h, int(kind)))
 
     def set_ring_placement(self, placement: int):
         """-1 automatic, 0 shared memory, 1 global memory (per-CTA, L2-resident)."""

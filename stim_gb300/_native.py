@@ -62,6 +62,8 @@ def _declare(L):
         "gfs_measure_int_peaks": [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
         "gfs_sampler_autotune": [_vp, _u64, ctypes.POINTER(ctypes.c_double)],
         "gfs_sampler_set_noise_mode": [_vp, ctypes.c_int],
+        "gfs_sampler_set_frame_kernel": [_vp, ctypes.c_int],
+        "gfs_sampler_get_frame_kernel": [_vp, ctypes.POINTER(ctypes.c_int)],
         "gfs_sampler_set_hit_capacity": [_vp, _u64],
         "gfs_sampler_last_noise_ms": [_vp, ctypes.POINTER(ctypes.c_double)],
         "gfs_sampler_last_counts": [_vp, ctypes.POINTER(_u64)],

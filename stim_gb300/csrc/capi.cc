@@ -427,11 +427,25 @@ gfs_status gfs_sampler_set_ring_placement(gfs_sampler *s, int placement) {
 gfs_status gfs_sampler_get_shape(const gfs_sampler *s, int *blocks_per_cta, int *threads, int *grid,
                                  uint64_t *smem_bytes) {
     return guarded([&] {
-        *blocks_per_cta = s->shape.blocks_per_cta;
-        *threads = s->shape.threads;
-        *grid = s->shape.grid;
-        *smem_bytes = s->shape.smem;
+        const gfs::LaunchShape &sh = s->lean_active() ? s->shape_lean : s->shape;
+        *blocks_per_cta = sh.blocks_per_cta;
+        *threads = sh.threads;
+        *grid = sh.grid;
+        *smem_bytes = sh.smem;
     });
+}
+
+gfs_status gfs_sampler_set_frame_kernel(gfs_sampler *s, int kind) {
+    return guarded([&] {
+        if (kind < -1 || kind > 1) {
+            throw std::invalid_argument("frame kernel must be -1 (automatic), 0 (generic) or 1 (lean when possible)");
+        }
+        s->lean_pref = kind;
+    });
+}
+
+gfs_status gfs_sampler_get_frame_kernel(const gfs_sampler *s, int *kind) {
+    return guarded([&] { *kind = s->lean_active() ? 1 : 0; });
 }
 
 gfs_status gfs_measure_smem_peak(int device, double *bytes_per_s) {

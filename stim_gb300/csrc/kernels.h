@@ -47,6 +47,10 @@ struct KernelArgs {
     // (frames_cta_stride uint4 entries per CTA) instead of shared memory, for circuits whose frames do not fit.
     uint4 *frames_global;
     uint64_t frames_cta_stride;
+    // Lean kernel (frame_lean.cu): the phase list and each phase's instance offset (Program::lean).
+    const LeanPhase *lean;
+    const uint64_t *lean_inst;
+    uint32_t n_lean;
 };
 
 // Several circuits in one launch (batch_frame_kernel): circuit j owns work items
@@ -93,6 +97,11 @@ constexpr int noise_slices_per_warp_for(int blocks_per_cta) {
     return blocks_per_cta == 1 ? 16 : blocks_per_cta == 2 ? 16 : 8;
 }
 cudaError_t frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out);
+// The lean frame kernel (hit-list mode, programs with Program::lean_ok): same results as launch_frame_kernel.
+size_t lean_smem_bytes(uint32_t nrows, uint32_t ring, uint32_t nobs, int blocks_per_cta, uint32_t n_lean,
+                       uint32_t n_occ, int threads);
+cudaError_t launch_frame_kernel_lean(const KernelArgs &args, const LaunchShape &shape, cudaStream_t stream);
+cudaError_t frame_kernel_lean_max_ctas_per_sm(const LaunchShape &shape, int *out);
 // In hit-list mode (shape.hits) this launches batch_noise_kernel and then the frame kernel.
 cudaError_t launch_batch_frame_kernel(const BatchArgs &args, const LaunchShape &shape, cudaStream_t stream);
 cudaError_t batch_frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out);

@@ -9,6 +9,7 @@
 #include "lower.h"
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <functional>
 #include <iterator>
@@ -1459,6 +1460,160 @@ struct Lowerer {
         }
     }
 
+    // The lean kernel's phase list (program.h LeanPhase): one phase per op, plus a hit phase for the noise fused
+    // before / after a gate, in the order the generic kernel meets the noise occurrences.  Gives up (lean_ok =
+    // false) on ops without a lean form.
+    void build_lean() {
+        prog.lean.clear();
+        prog.lean_inst.clear();
+        prog.lean_ok = false;
+        std::vector<uint32_t> open;  // phase indices of the open LK_LOOP_BEGINs
+        auto add = [&](uint32_t kind, uint32_t sub, uint32_t flags, uint32_t n, uint32_t a, uint32_t b, uint64_t inst) {
+            prog.lean.push_back(LeanPhase{kind | (sub << 8) | flags, n, a, b});
+            prog.lean_inst.push_back(inst);
+        };
+        for (const DevOp &op : prog.ops) {
+            const uint32_t code = op.code & 0xFFu, sub = (op.code >> 8) & 0xFFu;
+            const bool compact = (op.code & kCompact) != 0;
+            const uint32_t norand = (op.code & kNoRandomize) ? kLeanNoRandomize : 0u;
+            const bool gate = code == OP_1Q || code == OP_2Q || code == OP_MEASURE || code == OP_RESET;
+            if (gate && !compact) {
+                return;
+            }
+            if (gate && (op.d & kFusedChanMask)) {
+                add(LK_HITS, 0, 0, op.n, 0, 0, op.inst);
+            }
+            switch (code) {
+                case OP_END:
+                    add(LK_END, 0, 0, 0, 0, 0, 0);
+                    break;
+                case OP_LOOP_BEGIN: {
+                    const uint64_t reps = (uint64_t)op.a | ((uint64_t)op.b << 32);
+                    const uint64_t stride = (uint64_t)op.c | ((uint64_t)op.d << 32);
+                    if (reps == 0 || reps > 0xFFFFFFFFull || open.size() >= 2) {
+                        return;
+                    }
+                    open.push_back((uint32_t)prog.lean.size());
+                    add(LK_LOOP_BEGIN, 0, 0, (uint32_t)reps, (uint32_t)stride, (uint32_t)(stride >> 32), op.inst);
+                    break;
+                }
+                case OP_LOOP_END:
+                    if (open.empty()) {
+                        return;
+                    }
+                    add(LK_LOOP_END, 0, 0, 0, open.back(), 0, 0);
+                    open.pop_back();
+                    break;
+                case OP_1Q:
+                    add(LK_1Q, sub, 0, op.n, op.g, 0, op.inst);
+                    break;
+                case OP_2Q:
+                    add(sub == K2_CX ? LK_CX : sub == K2_CZ ? LK_CZ : LK_2Q, sub, 0, op.n, op.g, 0, op.inst);
+                    break;
+                case OP_MEASURE:
+                    add(LK_MEAS, sub, norand, op.n, op.g, op.b, op.inst);
+                    break;
+                case OP_RESET:
+                    add(LK_RESET, sub, norand, op.n, op.g, op.b, op.inst);
+                    break;
+                case OP_RECORD_ZERO:
+                    add(LK_ZERO, 0, 0, op.n, 0, 0, op.inst);
+                    break;
+                case OP_NOISE:
+                    add(LK_HITS, 0, 0, op.n, 0, 0, op.inst);
+                    break;
+                case OP_MNOISE:
+                    add(LK_FLIPS, 0, 0, op.n, 0, 0, op.inst);
+                    break;
+                case OP_DETECTORS:
+                    if (compact) {
+                        add(LK_DETS2, 0, 0, op.n, op.g, 0, op.inst);
+                    } else {
+                        add(LK_DETS, 0, 0, op.n, op.a, 0, op.inst);
+                    }
+                    break;
+                case OP_OBS:
+                    add(LK_OBS, 0, 0, op.n, op.a, op.b, op.inst);
+                    break;
+                case OP_EMIT:
+                    add(LK_EMIT, 0, 0, op.n, 0, 0, op.inst);
+                    break;
+                case OP_FEEDBACK:
+                    for (uint32_t u = 0; u < op.n; u++) {
+                        if (prog.pool[op.a + 2 * u] & kFeedbackSweep) {
+                            return;
+                        }
+                    }
+                    add(LK_FEEDBACK, 0, 0, op.n, op.a, 0, op.inst);
+                    break;
+                default:  // correlated errors, heralds
+                    return;
+            }
+            if (gate && (op.c & kFusedChanMask)) {
+                add(LK_HITS, 0, 0, op.n, 0, 0, op.inst);
+            }
+        }
+        if (!open.empty() || prog.num_detectors > 0xFFFFFFFFull || prog.num_measurements > 0xFFFFFFFFull) {
+            return;
+        }
+        mark_lean_barriers();
+        prog.lean_ok = true;
+    }
+
+    // Sets kLeanNoBarrier on the phases that every possible successor may follow without a barrier.
+    void mark_lean_barriers() {
+        std::vector<LeanPhase> &ph = prog.lean;
+        const size_t n = ph.size();
+        auto kind = [&](size_t i) { return ph[i].op & 0xFFu; };
+        // The work phases that can run right after phase i (loop markers followed; both outcomes of a loop end).
+        std::function<void(size_t, std::vector<size_t> &, int)> succ = [&](size_t j, std::vector<size_t> &out,
+                                                                            int guard) {
+            if (j >= n || guard > 8) {
+                out.push_back(n);  // unknown: treat as needing a barrier
+                return;
+            }
+            const uint32_t k = kind(j);
+            if (k == LK_LOOP_BEGIN) {
+                succ(j + 1, out, guard + 1);
+            } else if (k == LK_LOOP_END) {
+                succ(ph[j].a + 1, out, guard + 1);  // another iteration
+                succ(j + 1, out, guard + 1);        // loop done
+            } else {
+                out.push_back(j);
+            }
+        };
+        auto commutes = [&](uint32_t a, uint32_t b) {
+            const bool ha = a == LK_HITS || a == LK_FLIPS, hb = b == LK_HITS || b == LK_FLIPS;
+            const bool ra = a == LK_DETS2 || a == LK_DETS || a == LK_EMIT;
+            const bool rb = b == LK_DETS2 || b == LK_DETS || b == LK_EMIT;
+            if (ha && hb) {
+                return true;  // XORs into frames / ring commute
+            }
+            if ((a == LK_HITS && rb) || (ra && b == LK_HITS)) {
+                return true;  // frames vs ring reads and output rows: disjoint
+            }
+            return ra && rb;  // ring reads into distinct output rows
+        };
+        for (size_t i = 0; i < n; i++) {
+            const uint32_t k = kind(i);
+            if (k == LK_END || k == LK_LOOP_BEGIN || k == LK_LOOP_END) {
+                continue;
+            }
+            std::vector<size_t> next;
+            succ(i + 1, next, 0);
+            bool ok = !next.empty();
+            for (size_t j : next) {
+                if (j >= n || kind(j) == LK_END || !commutes(k, kind(j))) {
+                    ok = false;
+                    break;
+                }
+            }
+            if (ok) {
+                ph[i].op |= kLeanNoBarrier;
+            }
+        }
+    }
+
     void run() {
         prog.stats = root.stats();
         std::vector<uint8_t> used(prog.stats.num_qubits + 1, 0);
@@ -1514,6 +1669,7 @@ struct Lowerer {
         } else if (mode == SampleMode::DETECTIONS) {
             analyze_randomization();
         }
+        build_lean();
     }
 };
 

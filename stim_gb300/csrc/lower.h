@@ -39,6 +39,12 @@ struct Program {
     std::vector<NoiseOcc> occs;
     std::vector<double> occ_hits_per_block;
     CircuitStats stats;
+    // The lean kernel's phase list (program.h LeanPhase) and each phase's instance offset; lean_ok when
+    // every op has a lean form (no correlated errors or heralds, compact unit lists, at most two loop levels
+    // of fewer than 2^32 repetitions).
+    std::vector<LeanPhase> lean;
+    std::vector<uint64_t> lean_inst;
+    bool lean_ok = false;
 };
 
 struct LowerOptions {

@@ -108,6 +108,44 @@ struct alignas(16) NoiseOcc {
 };
 static_assert(sizeof(NoiseOcc) == 32, "NoiseOcc layout");
 
+// Phase list of the lean frame kernel (frame_lean.cu): the device program re-cut into the phases the kernel
+// executes, each one barrier-separated step with its fields pre-resolved, so that a phase costs one 16-byte
+// shared-memory read to decode.  Noise fused into a gate becomes its own hit phase before / after the gate
+// (hit-list mode only: noise_kernel has drawn the hit records).  Built by the lowering when every op has a
+// lean form (see Program::lean_ok).
+enum LeanKind : uint32_t {
+    LK_END = 0,
+    LK_LOOP_BEGIN,  // n = repetitions; a | b << 32 = instances per iteration; the body follows
+    LK_LOOP_END,    // a = phase index of the matching LK_LOOP_BEGIN
+    LK_HITS,        // Pauli hit records of the next noise occurrence (into X / Z rows)
+    LK_FLIPS,       // measurement-flip records of the next occurrence: n = results of the noisy instruction
+    LK_1Q,          // sub = K1_*; a = compact list (16-bit rows, halfword index 2a + u)
+    LK_CX,          // a = compact pair list (row1 | row2 << 16)
+    LK_CZ,
+    LK_2Q,          // sub = K2_*, other two-qubit gates; a = compact pair list
+    LK_MEAS,        // sub = KM_*; a = compact list (16-bit rows); b = first randomization unit
+    LK_RESET,       // sub = KR_*; a = compact list; b = first randomization unit
+    LK_ZERO,        // n zero results appended (MPAD)
+    LK_DETS2,       // n detectors; a = compact list (lookback1 | lookback2 << 16)
+    LK_DETS,        // n detectors; a = CSR range offsets into the pool (as OP_DETECTORS)
+    LK_OBS,         // b = observable index; a = pool offset of the n terms (as OP_OBS)
+    LK_EMIT,        // copy the last n results to the measurement output
+    LK_FEEDBACK,    // as OP_FEEDBACK (record-controlled Paulis only)
+};
+constexpr uint32_t kLeanNoRandomize = 1u << 16;  // LeanPhase.op flag: write zeros instead of randomization
+// LeanPhase.op flag: no barrier after this phase, because every phase that can follow it touches disjoint state
+// or only XORs into the same rows (hit phases commute with one another; detector phases read the ring and write
+// detection rows, disjoint from the frames that Pauli hits change).
+constexpr uint32_t kLeanNoBarrier = 1u << 17;
+
+struct alignas(16) LeanPhase {
+    uint32_t op;  // LeanKind | sub << 8 | flags
+    uint32_t n;
+    uint32_t a;
+    uint32_t b;
+};
+static_assert(sizeof(LeanPhase) == 16, "LeanPhase layout");
+
 constexpr uint32_t kFeedbackX = 1, kFeedbackZ = 2;
 constexpr uint32_t kFeedbackSweep = 1u << 31;  // OP_FEEDBACK source: column of the sweep table, not a lookback
 constexpr uint32_t kTermRecord = 1u << 31, kTermX = 1u << 30, kTermZ = 1u << 29;

@@ -138,6 +138,12 @@ struct gfs_sampler {
     bool force_inline = false;  // set while a chunk is redone after its hit list overflowed
     gfs::LaunchShape shape_inline{};  // the same shape for the inline-noise frame kernel
     DevBuf hit_buf, hit_count, d_occs;
+    // Lean frame kernel (frame_lean.cu): used for hit-list launches of programs with a phase list, unless
+    // lean_pref = 0.  shape_lean mirrors `shape` with the lean kernel's shared memory and occupancy.
+    DevBuf d_lean, d_lean_inst;
+    int lean_pref = -1;  // -1 automatic (lean when possible), 0 never, 1 when possible
+    bool lean_ready = false;
+    gfs::LaunchShape shape_lean{};
     int occs_blocks = 0;          // blocks per slice the uploaded occurrence regions were planned for
     uint64_t slice_cap = 0;       // records per slice region
     uint64_t n_hit_overflows = 0;
@@ -273,6 +279,29 @@ struct gfs_sampler {
         si.grid = grid > 0 ? grid : per_sm_inline * num_sms;
         shape = s;
         shape_inline = si;
+        // The lean kernel's shape: same blocks, threads and ring placement, its own shared memory and occupancy.
+        lean_ready = false;
+        if (prog.lean_ok && s.hits && !frames_global && !prog.occs.empty()) {
+            gfs::LaunchShape l = s;
+            l.smem = gfs::lean_smem_bytes(prog.num_rows, ring_global ? 0 : prog.ring, (uint32_t)prog.num_observables,
+                                          bpc, (uint32_t)prog.lean.size(), (uint32_t)prog.occs.size(), threads);
+            int per_sm_lean = 0;
+            if (l.smem <= (size_t)prop.sharedMemPerBlockOptin &&
+                gfs::frame_kernel_lean_max_ctas_per_sm(l, &per_sm_lean) != cudaSuccess) {
+                cudaGetLastError();
+                per_sm_lean = 0;
+            }
+            if (per_sm_lean >= 1) {
+                l.grid = grid > 0 ? grid : per_sm_lean * num_sms;
+                shape_lean = l;
+                lean_ready = true;
+            }
+        }
+    }
+
+    // Whether a hit-list launch of the current shape runs the lean kernel.
+    bool lean_active() const {
+        return lean_ready && lean_pref != 0 && shape.hits && !force_inline && sweep_rows == nullptr;
     }
 
     // Shape without timing: four 128-shot blocks per CTA when two such CTAs fit per SM (small and medium
@@ -327,6 +356,10 @@ struct gfs_sampler {
         upload(d_tables, prog.tables, device, stream);
         upload(d_chans, prog.chans, device, stream);
         upload(d_orig, prog.qubit_orig, device, stream);
+        if (prog.lean_ok) {
+            upload(d_lean, prog.lean, device, stream);
+            upload(d_lean_inst, prog.lean_inst, device, stream);
+        }
         d_status.ensure(16, device);
         ck(cudaHostAlloc((void **)&h_words, 64, cudaHostAllocMapped), "cudaHostAlloc");
         ck(cudaHostGetDevicePointer((void **)&h_words_dev, h_words, 0), "cudaHostGetDevicePointer");
@@ -396,7 +429,8 @@ struct gfs_sampler {
     // Runs the frame kernel for nblk blocks starting at stream block `block0`; results land in the tmp buffers.
     // In hit-list mode noise_kernel runs first and draws the chunk's noise into hit_buf.
     void run_frame(uint64_t nblk, uint64_t block0) {
-        const gfs::LaunchShape &sh = (shape.hits && !force_inline) ? shape : shape_inline;
+        const bool lean = lean_active();
+        const gfs::LaunchShape &sh = lean ? shape_lean : (shape.hits && !force_inline) ? shape : shape_inline;
         uint64_t bpc = (uint64_t)sh.blocks_per_cta;
         uint64_t nslices = (nblk + bpc - 1) / bpc;
         uint64_t alloc_blocks = nslices * bpc;
@@ -466,7 +500,14 @@ struct gfs_sampler {
         }
         gfs::LaunchShape s = sh;
         s.grid = (int)std::min<uint64_t>((uint64_t)sh.grid, nslices);
-        ck(gfs::launch_frame_kernel(a, s, stream), "frame kernel launch");
+        if (lean) {
+            a.lean = (const gfs::LeanPhase *)d_lean.p;
+            a.lean_inst = (const uint64_t *)d_lean_inst.p;
+            a.n_lean = (uint32_t)prog.lean.size();
+            ck(gfs::launch_frame_kernel_lean(a, s, stream), "lean frame kernel launch");
+        } else {
+            ck(gfs::launch_frame_kernel(a, s, stream), "frame kernel launch");
+        }
         n_frame++;
     }
 

@@ -265,3 +265,43 @@ def test_circuit_too_large_for_shared_memory_matches_oracle(mode):
     np.testing.assert_array_equal(gd, od)
     np.testing.assert_array_equal(go, oo)
     assert gd.any()
+
+
+@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("name", golden_names())
+def test_both_frame_kernels_match_golden(name, kernel):
+    # Hit-list noise through the generic frame kernel (0) and the lean one (1, used by default wherever the
+    # program has a lean phase list); both must reproduce the reference's goldens bit for bit.
+    g = load(name)
+    c = stim_gb300.Circuit(str(g["circuit"]))
+    s = c.compile_detector_sampler(seed=int(g["seed"]))
+    s.set_noise_mode(1)
+    s.set_frame_kernel(kernel)
+    d, o = s.sample(int(g["shots"]), separate_observables=True, bit_packed=True)
+    np.testing.assert_array_equal(d, g["dets"])
+    np.testing.assert_array_equal(o, g["obs"])
+    m = c.compile_sampler(skip_reference_sample=True, seed=int(g["seed"]))
+    m.set_noise_mode(1)
+    m.set_frame_kernel(kernel)
+    np.testing.assert_array_equal(m.sample(int(g["shots"]), bit_packed=True), g["meas"])
+    if kernel == 0:
+        assert s.launch_shape()["kernel"] == "generic"
+
+
+def test_lean_kernel_is_used_for_generated_codes():
+    for family, d in [("surface_code:rotated_memory_z", 25), ("repetition_code:memory", 9),
+                      ("color_code:memory_xyz", 5)]:
+        s = stim_gb300.Circuit(workloads.code_circuit(family, d, d, 0.001)).compile_detector_sampler(seed=1)
+        assert s.launch_shape()["kernel"] == "lean", family
+
+
+@pytest.mark.parametrize("shape", [(1, 128), (1, 256), (2, 128), (4, 256)])
+def test_lean_kernel_shapes_match_oracle(shape):
+    text = workloads.code_circuit("surface_code:rotated_memory_x", 11, 11, 0.005)
+    s = stim_gb300.Circuit(text).compile_detector_sampler(seed=4)
+    s.set_launch_shape(*shape)
+    assert s.launch_shape()["kernel"] == "lean"
+    gd, go = s.sample(20000, separate_observables=True, bit_packed=True)
+    od, oo, _ = OracleCircuit(text).sample(20000, 4, threads=_THREADS)
+    np.testing.assert_array_equal(gd, od)
+    np.testing.assert_array_equal(go, oo)
