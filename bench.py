@@ -545,7 +545,7 @@ def run_gpu(args):
 
     configs = run_configs(args, local) if args.config_steps > 0 else None
     batched = run_batched(args, local) if args.batched else None
-    serving = run_serving(args, local) if args.serve_seconds > 0 else None
+    serving = run_serving_legs(args, local) if args.serve_seconds > 0 else None
     m2d = run_m2d(args, local, text) if args.m2d_steps > 0 else None
     dem = run_dem(args, local) if args.dem_steps > 0 else None
     feed = run_feed(args, local, text) if args.feed_steps > 0 else None
@@ -885,7 +885,22 @@ def run_batched(args, local):
     }
 
 
-def run_serving(args, local):
+def run_serving_legs(args, local):
+    """The serving configuration (Poisson --serve-rate req/s for --serve-seconds s) and a sweep of lower arrival
+    rates (--serve-sweep, --serve-sweep-seconds each) showing latency below saturation."""
+    main = run_serving(args, local, args.serve_rate, args.serve_seconds)
+    sweep = []
+    for rate in [float(x) for x in args.serve_sweep.split(",") if x.strip()]:
+        if args.serve_sweep_seconds > 0:
+            sweep.append(run_serving(args, local, rate, args.serve_sweep_seconds))
+    main["sweep"] = [{k: r[k] for k in ("rate", "seconds", "requests", "gbits", "offered_gbits", "p50_ms", "p99_ms",
+                                        "wall_s", "counters")} for r in sweep]
+    bounded = [r["rate"] for r in sweep if r["p99_ms"] is not None and r["p99_ms"] < 1000.0]
+    main["highest_swept_rate_with_p99_under_1s"] = max(bounded) if bounded else None
+    return main
+
+
+def run_serving(args, local, rate, seconds):
     """Open-loop serving: Poisson arrivals at --serve-rate requests/s for --serve-seconds, each request a
     generated code circuit (repetition d 3..51, rotated surface X/Z d 3..21, color d 3..15; rounds = d;
     p log-uniform [1e-4, 1e-2] on a 16-per-decade grid; shots log-uniform [2^10, 2^22]; own seed),
@@ -899,7 +914,7 @@ def run_serving(args, local):
     import stim_gb300
     from stim_gb300 import workloads
 
-    wl = workloads.serving_workload(rate=args.serve_rate, seconds=args.serve_seconds, seed=7)
+    wl = workloads.serving_workload(rate=rate, seconds=seconds, seed=7)
     texts, dims = {}, {}
     for w in wl:
         key = (w["family"], w["distance"], w["p"])
@@ -972,13 +987,15 @@ def run_serving(args, local):
         retire(True)
     wall = time.perf_counter() - t0
     st = server.stats()
+    counters = server.counters()
     server.close()
     lat.sort()
-    offered = sum(w["shots"] * sum(dims[(w["family"], w["distance"], w["p"])]) for w in wl) / args.serve_seconds
+    offered = sum(w["shots"] * sum(dims[(w["family"], w["distance"], w["p"])]) for w in wl) / seconds
     return {
-        "workload": f"Poisson {args.serve_rate:g} req/s for {args.serve_seconds:g} s; repetition d3-51, surface "
+        "workload": f"Poisson {rate:g} req/s for {seconds:g} s; repetition d3-51, surface "
                     "X/Z d3-21, color d3-15, rounds = d, p log-uniform [1e-4, 1e-2] (16 per decade), shots "
                     "log-uniform [2^10, 2^22], per-request seed; bit-packed results in device memory",
+        "rate": rate, "seconds": seconds, "counters": counters,
         "requests": len(wl), "distinct_circuits": len(texts),
         "gbits": bits / wall / 1e9, "offered_gbits": offered / 1e9,
         "p50_ms": lat[len(lat) // 2] if lat else None,
@@ -1010,8 +1027,10 @@ def main():
     ap.add_argument("--dem-steps", type=int, default=5)
     ap.add_argument("--feed-steps", type=int, default=3)
     ap.add_argument("--batch-circuits", type=int, default=256)
-    ap.add_argument("--serve-seconds", type=float, default=2.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-sweep", default="250,500,1000", help="arrival rates (req/s) of the latency sweep")
+    ap.add_argument("--serve-sweep-seconds", type=float, default=8.0)
     ap.add_argument("--serve-arena-gb", type=int, default=48)
     ap.add_argument("--serve-hbm-gb", type=int, default=16)
     args = ap.parse_args()

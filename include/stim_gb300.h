@@ -313,6 +313,10 @@ gfs_status gfs_server_wait(gfs_server *s, uint64_t ticket, double timeout_s, int
  * of completed requests / first submit to last completion), batches, mean chunks per batch, cache hits,
  * cache misses, longest queue, bits completed, seconds spanned. */
 gfs_status gfs_server_stats(gfs_server *s, double *out12);
+/* Admission counters, out8: requests submitted (accepted into the queue), rejected at submission (invalid
+ * circuit or arguments, or a circuit too large for the server), completed, failed after admission, queued now
+ * (shots not yet handed to a batch), not yet finished, longest queue seen, chunks admitted into batches. */
+gfs_status gfs_server_counters(gfs_server *s, uint64_t *out8);
 
 /*
  * Measurements to detection events (replaces CompiledMeasurementsToDetectionEventsConverter,

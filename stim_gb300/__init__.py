@@ -831,3 +831,11 @@ class Server:
         keys = ["completed", "failed", "p50_ms", "p99_ms", "gbits", "batches", "chunks_per_batch", "cache_hits",
                 "cache_misses", "max_queue", "bits", "seconds"]
         return dict(zip(keys, list(o)))
+
+    def counters(self) -> dict:
+        """Admission counters: submitted, rejected (at submission), completed, failed, queued (now), pending (not
+        finished), max_queue, chunks_admitted."""
+        o = (ctypes.c_uint64 * 8)()
+        check(lib().gfs_server_counters(self._h, o))
+        keys = ["submitted", "rejected", "completed", "failed", "queued", "pending", "max_queue", "chunks_admitted"]
+        return dict(zip(keys, [int(v) for v in o]))

@@ -82,6 +82,7 @@ def _declare(L):
                               _vp, _u64, _vp, _u64, ctypes.POINTER(_u64)],
         "gfs_server_wait": [_vp, _u64, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)],
         "gfs_server_stats": [_vp, ctypes.POINTER(ctypes.c_double)],
+        "gfs_server_counters": [_vp, ctypes.POINTER(_u64)],
         "gfs_m2d_create": [_vp, _vp, ctypes.c_int, ctypes.POINTER(_vp)],
         "gfs_m2d_stats": [_vp, ctypes.POINTER(_u64)],
         "gfs_m2d_convert": [_vp, _u64, _vp, _u64, _vp, _u64, ctypes.c_uint32, _vp, _u64, _vp, _u64],

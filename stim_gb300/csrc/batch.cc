@@ -122,7 +122,8 @@ struct gfs_batch {
         std::vector<uint64_t> key = {(uint64_t)sh.blocks_per_cta, (uint64_t)sh.threads, (uint64_t)sh.grid, sh.smem,
                                      (uint64_t)sh.ring_global, flags, items, (uint64_t)(uintptr_t)eng.det_arena.p,
                                      (uint64_t)(uintptr_t)eng.obs_arena.p, (uint64_t)(uintptr_t)eng.d_desc.p,
-                                     (uint64_t)(uintptr_t)eng.d_prefix.p, (uint64_t)(uintptr_t)eng.ring_buf.p};
+                                     (uint64_t)(uintptr_t)eng.d_prefix.p, (uint64_t)(uintptr_t)eng.ring_buf.p,
+                                     (uint64_t)eng.lean, (uint64_t)eng.lean_shape.grid, eng.lean_shape.smem};
         for (const auto &e : es) {
             key.push_back(e.shots);
             key.push_back((uint64_t)(uintptr_t)e.dets);
@@ -296,6 +297,7 @@ struct gfs_batch {
         }
         eng.shape = best_shape;
         eng.ring_stride_cur = best_stride;
+        eng.set_lean_shape(progs);
         drop_graph();
         return best;
     }
@@ -342,11 +344,12 @@ gfs_status gfs_batch_set_shape(gfs_batch *b, int blocks_per_cta, int threads, in
 gfs_status gfs_batch_get_shape(const gfs_batch *b, int *blocks_per_cta, int *threads, int *grid, uint64_t *smem_bytes,
                                int *ring_global) {
     return guarded([&] {
-        *blocks_per_cta = b->eng.shape.blocks_per_cta;
-        *threads = b->eng.shape.threads;
-        *grid = b->eng.shape.grid;
-        *smem_bytes = b->eng.shape.smem;
-        *ring_global = b->eng.shape.ring_global ? 1 : 0;
+        const gfs::LaunchShape &sh = b->eng.lean ? b->eng.lean_shape : b->eng.shape;
+        *blocks_per_cta = sh.blocks_per_cta;
+        *threads = sh.threads;
+        *grid = sh.grid;
+        *smem_bytes = sh.smem;
+        *ring_global = sh.ring_global ? 1 : 0;
     });
 }
 

@@ -38,6 +38,10 @@ struct BatchEngine {
     DevBuf d_desc, d_prefix, d_counter, d_status, det_arena, obs_arena, ring_buf;
     DevBuf hit_arena, count_arena, d_wprefix;
     gfs::LaunchShape shape{};
+    // The lean batched kernel (frame_lean.cu) in hit-list mode when every program has a lean phase list:
+    // same blocks, threads and ring placement as `shape`, its own shared memory and grid.
+    bool lean = false;
+    gfs::LaunchShape lean_shape{};
     uint64_t ring_stride_cur = 0;
     bool force_inline = false;  // set while a batch is redone after a hit list overflowed
     // Occurrence tables planned for this engine's blocks per CTA, per program.
@@ -145,6 +149,37 @@ struct BatchEngine {
         const bool global = !fa || (fb && ring < 0 && res_b * 2 >= res_a * 3) || ring == 1;
         shape = global ? b : a;
         ring_stride_cur = global ? rb : ra;
+        set_lean_shape(progs);
+    }
+
+    void set_lean_shape(const std::vector<const gfs_sampler *> &progs) {
+        lean = false;
+        if (!shape.hits) {
+            return;
+        }
+        size_t smem = 0;
+        for (auto *p : progs) {
+            if (!p->prog.lean_ok || p->lean_pref == 0) {
+                return;
+            }
+            smem = std::max(smem, gfs::lean_smem_bytes(p->prog.num_rows, shape.ring_global ? 0 : p->prog.ring,
+                                                       (uint32_t)p->prog.num_observables, shape.blocks_per_cta,
+                                                       (uint32_t)p->prog.lean.size(), (uint32_t)p->prog.occs.size(),
+                                                       shape.threads));
+        }
+        gfs::LaunchShape l = shape;
+        l.smem = smem;
+        int per = 0;
+        if (smem > smem_optin || gfs::batch_frame_kernel_lean_max_ctas_per_sm(l, &per) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        if (per < 1) {
+            return;
+        }
+        l.grid = per * num_sms;
+        lean_shape = l;
+        lean = true;
     }
 
     // Default shape without timing: four blocks per CTA when at least two such CTAs fit per SM (small
@@ -205,6 +240,11 @@ struct BatchEngine {
             a.smem_table_words = 0;  // the same shared-memory layout in hit-list mode and its inline fallback
             a.smem_ops = s->smem_ops();
             a.ring_cta_stride = ring_stride_cur;
+            if (s->prog.lean_ok) {
+                a.lean = (const gfs::LeanPhase *)s->d_lean.p;
+                a.lean_inst = (const uint64_t *)s->d_lean_inst.p;
+                a.n_lean = (uint32_t)s->prog.lean.size();
+            }
             if (hits) {
                 const OccPlan &pl = occ_plan(s);
                 a.n_occ = (uint32_t)s->prog.occs.size();
@@ -238,7 +278,8 @@ struct BatchEngine {
                "descriptor upload");
         }
         if (shape.ring_global) {
-            ring_buf.ensure(std::max<uint64_t>(16, (uint64_t)shape.grid * ring_stride_cur * 16), device);
+            const uint64_t grid = std::max<uint64_t>((uint64_t)shape.grid, lean ? (uint64_t)lean_shape.grid : 0);
+            ring_buf.ensure(std::max<uint64_t>(16, grid * ring_stride_cur * 16), device);
         }
         size_t k = 0;
         for (size_t q = 0; q < n; q++) {
@@ -279,6 +320,12 @@ struct BatchEngine {
         b.counter = (uint32_t *)d_counter.p;
         b.warp_prefix = (const uint64_t *)d_wprefix.p;
         b.total_noise_warps = noise_warps;
+        if (lean && !force_inline) {
+            gfs::LaunchShape l = lean_shape;
+            l.grid = (int)std::min<uint64_t>((uint64_t)l.grid, items);
+            ck(gfs::launch_batch_frame_kernel_lean(b, l, stream), "lean batch frame kernel launch");
+            return;
+        }
         gfs::LaunchShape s = shape;
         s.hits = shape.hits && !force_inline;
         if (shape.hits && force_inline) {

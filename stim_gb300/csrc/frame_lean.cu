@@ -480,6 +480,73 @@ __global__ void __maxnreg__(96) frame_kernel_lean(const KernelArgs p) {
     }
 }
 
+// Many circuits in one persistent launch (as batch_frame_kernel): CTAs claim (circuit, slice) work items from a
+// global counter and reload a circuit's phase list and occurrence table only when the circuit changes.
+template <int B>
+__global__ void __maxnreg__(96) batch_frame_kernel_lean(const BatchArgs b) {
+    extern __shared__ uint4 sm[];
+    __shared__ KernelArgs cur;
+    __shared__ uint32_t s_item, s_circ;
+    uint32_t have = 0xFFFFFFFFu;
+    LeanState st{};
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const uint32_t item = atomicAdd(b.counter, 1u);
+            s_item = item;
+            if (item < b.total_slices) {
+                uint32_t lo = 0, hi = b.ncircuits;  // last j with slice_prefix[j] <= item
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) / 2;
+                    if (b.slice_prefix[mid] <= item) {
+                        lo = mid;
+                    } else {
+                        hi = mid;
+                    }
+                }
+                s_circ = lo;
+                if (lo != have) {
+                    cur = b.circuits[lo];
+                }
+            }
+        }
+        __syncthreads();
+        const uint32_t item = s_item, j = s_circ;
+        if (item >= b.total_slices) {
+            break;
+        }
+        if (j != have) {
+            st = lean_state<B>(cur, sm);
+            have = j;
+        }
+        lean_slice<B>(cur, st, item - b.slice_prefix[j]);
+    }
+}
+
+template <int B>
+cudaError_t lean_batch_launch_b(const BatchArgs &args, const LaunchShape &s, cudaStream_t stream) {
+    cudaError_t e =
+        cudaFuncSetAttribute(batch_frame_kernel_lean<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    e = launch_batch_noise_kernel(args, B, stream);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    batch_frame_kernel_lean<B><<<s.grid, s.threads, s.smem, stream>>>(args);
+    return cudaGetLastError();
+}
+
+template <int B>
+cudaError_t lean_batch_occ_b(const LaunchShape &s, int *out) {
+    cudaError_t e =
+        cudaFuncSetAttribute(batch_frame_kernel_lean<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, batch_frame_kernel_lean<B>, s.threads, s.smem);
+}
+
 template <int B>
 cudaError_t lean_launch_b(const KernelArgs &args, const LaunchShape &s, cudaStream_t stream) {
     cudaError_t e = cudaFuncSetAttribute(frame_kernel_lean<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
@@ -520,6 +587,35 @@ cudaError_t launch_frame_kernel_lean(const KernelArgs &args, const LaunchShape &
             return lean_launch_b<2>(args, shape, stream);
         case 4:
             return lean_launch_b<4>(args, shape, stream);
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_batch_frame_kernel_lean(const BatchArgs &args, const LaunchShape &shape, cudaStream_t stream) {
+    if (!shape.hits) {
+        return cudaErrorInvalidValue;
+    }
+    switch (shape.blocks_per_cta) {
+        case 1:
+            return lean_batch_launch_b<1>(args, shape, stream);
+        case 2:
+            return lean_batch_launch_b<2>(args, shape, stream);
+        case 4:
+            return lean_batch_launch_b<4>(args, shape, stream);
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t batch_frame_kernel_lean_max_ctas_per_sm(const LaunchShape &shape, int *out) {
+    switch (shape.blocks_per_cta) {
+        case 1:
+            return lean_batch_occ_b<1>(shape, out);
+        case 2:
+            return lean_batch_occ_b<2>(shape, out);
+        case 4:
+            return lean_batch_occ_b<4>(shape, out);
         default:
             return cudaErrorInvalidValue;
     }

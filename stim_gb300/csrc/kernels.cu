@@ -1296,6 +1296,32 @@ static cudaError_t launch_batch_b(const BatchArgs &args, const LaunchShape &s, c
     return cudaGetLastError();
 }
 
+template <int B>
+static cudaError_t launch_batch_noise_b(const BatchArgs &args, cudaStream_t stream) {
+    const uint64_t blocks = (args.total_noise_warps + 7) / 8;
+    if (blocks > 0x7FFFFFFFull) {
+        return cudaErrorInvalidValue;
+    }
+    if (blocks) {
+        batch_noise_kernel<B><<<(unsigned)blocks, 256, 0, stream>>>(args);
+        return cudaGetLastError();
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_batch_noise_kernel(const BatchArgs &args, int blocks_per_cta, cudaStream_t stream) {
+    switch (blocks_per_cta) {
+        case 1:
+            return launch_batch_noise_b<1>(args, stream);
+        case 2:
+            return launch_batch_noise_b<2>(args, stream);
+        case 4:
+            return launch_batch_noise_b<4>(args, stream);
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
 cudaError_t launch_batch_frame_kernel(const BatchArgs &args, const LaunchShape &shape, cudaStream_t stream) {
     const bool h = shape.hits;
     switch (shape.blocks_per_cta) {

@@ -105,6 +105,11 @@ cudaError_t frame_kernel_lean_max_ctas_per_sm(const LaunchShape &shape, int *out
 // In hit-list mode (shape.hits) this launches batch_noise_kernel and then the frame kernel.
 cudaError_t launch_batch_frame_kernel(const BatchArgs &args, const LaunchShape &shape, cudaStream_t stream);
 cudaError_t batch_frame_kernel_max_ctas_per_sm(const LaunchShape &shape, int *out);
+// The noise kernel of a batch alone (hit-list mode), and the lean batched frame kernel: batch_noise_kernel, then
+// the lean kernel over the work items (every circuit with a lean phase list; shape.smem covers the largest).
+cudaError_t launch_batch_noise_kernel(const BatchArgs &args, int blocks_per_cta, cudaStream_t stream);
+cudaError_t launch_batch_frame_kernel_lean(const BatchArgs &args, const LaunchShape &shape, cudaStream_t stream);
+cudaError_t batch_frame_kernel_lean_max_ctas_per_sm(const LaunchShape &shape, int *out);
 
 // Transposes [local block][rows] bit-rows (128 shots per entry) of up to three sources, concatenated
 // (src0 rows, then src1, then src2), into shot-major output rows.  `xor_rows` (optional) is a bit vector over the

@@ -549,8 +549,8 @@ struct gfs_sampler {
         return false;
     }
 
-    // Times the frame kernel on `trial_shots` shots for each candidate launch shape and keeps the fastest.
-    // The stream position does not move (the trial's results are discarded).
+    // Times the frame kernel for each candidate launch shape on whole waves of at least `trial_shots` shots and
+    // keeps the fastest per shot.  The stream position does not move (the trial's results are discarded).
     double autotune(uint64_t trial_shots) {
         struct Cand {
             int bpc, threads, ring;
@@ -558,15 +558,23 @@ struct gfs_sampler {
         const Cand cands[] = {{1, 256, 0}, {1, 256, 1}, {1, 128, 0}, {1, 128, 1}, {2, 256, 0},
                               {2, 256, 1}, {2, 128, 0}, {2, 128, 1}, {4, 256, 0}, {4, 256, 1}};
         const gfs::LaunchShape before = shape, before_inline = shape_inline;
-        const uint64_t nblk = std::max<uint64_t>(1, (trial_shots + 127) / 128);
-        double best = -1;
-        gfs::LaunchShape best_shape = shape, best_inline = shape_inline;
+        const uint64_t want_blk = std::max<uint64_t>(1, (trial_shots + 127) / 128);
+        double best = -1;  // ms per 128-shot block
+        gfs::LaunchShape best_shape = shape, best_inline = shape_inline, best_lean = shape_lean;
+        bool best_lean_ready = lean_ready;
+        const gfs::LaunchShape before_lean = shape_lean;
+        const bool before_lean_ready = lean_ready;
         for (const Cand &c : cands) {
             try {
                 choose_shape(c.bpc, c.threads, 0, c.ring);
             } catch (const std::invalid_argument &) {
                 continue;
             }
+            // Whole waves of the candidate's persistent grid (at least two), so that no candidate is timed on a
+            // partly filled last wave that a full-size chunk would not have.
+            const gfs::LaunchShape &run = lean_active() ? shape_lean : shape;
+            const uint64_t wave = (uint64_t)run.grid * (uint64_t)run.blocks_per_cta;
+            const uint64_t nblk = std::max<uint64_t>(2, (want_blk + wave - 1) / wave) * wave;
             float total = 0;
             for (int rep = 0; rep < 2; rep++) {
                 ck(cudaEventRecord(ev[1], stream), "event");
@@ -577,15 +585,20 @@ struct gfs_sampler {
                 account_noise(-1);
             }
             check_status();
-            if (best < 0 || total < best) {
-                best = total;
+            const double per_block = total / (double)nblk;
+            if (best < 0 || per_block < best) {
+                best = per_block;
                 best_shape = shape;
                 best_inline = shape_inline;
+                best_lean = shape_lean;
+                best_lean_ready = lean_ready;
             }
         }
         shape = best < 0 ? before : best_shape;
         shape_inline = best < 0 ? before_inline : best_inline;
-        return best;
+        shape_lean = best < 0 ? before_lean : best_lean;
+        lean_ready = best < 0 ? before_lean_ready : best_lean_ready;
+        return best < 0 ? best : best * (double)want_blk;  // ms for the requested trial size
     }
 
     // Chunk size (in 128-shot blocks) for host destinations: one resident wave of the frame kernel (every

@@ -94,6 +94,9 @@ struct gfs_server {
     std::vector<double> latencies_ms;
     uint64_t completed = 0, failed_count = 0, batches = 0, entries_total = 0, cache_hits = 0, cache_misses = 0;
     uint64_t bits_done = 0, max_queue = 0;
+    // Admission counters: requests accepted into the queue, rejected at submission (invalid circuit or
+    // arguments, circuit too large for the server), chunks admitted into batches.
+    uint64_t submitted = 0, rejected = 0, chunks_admitted = 0;
     Clock::time_point t_first_submit{}, t_last_done{};
     bool any_submit = false;
 
@@ -138,6 +141,17 @@ struct gfs_server {
 
     uint64_t submit(const char *text, size_t len, uint64_t shots, uint64_t seed, uint32_t flags, bool device_out,
                     uint8_t *dets, uint64_t dstride, uint8_t *obs, uint64_t ostride) {
+        try {
+            return submit_checked(text, len, shots, seed, flags, device_out, dets, dstride, obs, ostride);
+        } catch (...) {
+            std::lock_guard<std::mutex> lk(mu);
+            rejected++;
+            throw;
+        }
+    }
+
+    uint64_t submit_checked(const char *text, size_t len, uint64_t shots, uint64_t seed, uint32_t flags,
+                            bool device_out, uint8_t *dets, uint64_t dstride, uint8_t *obs, uint64_t ostride) {
         const Clock::time_point t0 = Clock::now();  // latency includes lowering on a cache miss
         std::string key(text, len);
         std::shared_ptr<CachedProgram> prog;
@@ -196,6 +210,7 @@ struct gfs_server {
         {
             std::lock_guard<std::mutex> lk(mu);
             id = r->id = next_id++;
+            submitted++;
             if (!any_submit) {
                 t_first_submit = r->t_submit;
                 any_submit = true;
@@ -270,6 +285,7 @@ struct gfs_server {
                     continue;
                 }
                 slot.chunks.push_back(Chunk{r, r->issued, take});
+                chunks_admitted++;
                 used += footprint(*r, take, 4);
                 r->issued += take;
                 progress = true;
@@ -566,6 +582,22 @@ struct gfs_server {
         out[10] = (double)bits_done;
         out[11] = span;
     }
+
+    void counters(uint64_t *out) {
+        std::lock_guard<std::mutex> lk(mu);
+        uint64_t pending = 0;
+        for (const auto &kv : live) {
+            pending += kv.second->finished ? 0 : 1;
+        }
+        out[0] = submitted;
+        out[1] = rejected;
+        out[2] = completed;
+        out[3] = failed_count;
+        out[4] = queue.size();
+        out[5] = pending;
+        out[6] = max_queue;
+        out[7] = chunks_admitted;
+    }
 };
 
 extern "C" {
@@ -603,6 +635,10 @@ gfs_status gfs_server_wait(gfs_server *s, uint64_t ticket, double timeout_s, int
 
 gfs_status gfs_server_stats(gfs_server *s, double *out12) {
     return guarded([&] { s->stats(out12); });
+}
+
+gfs_status gfs_server_counters(gfs_server *s, uint64_t *out8) {
+    return guarded([&] { s->counters(out8); });
 }
 
 }  // extern "C"

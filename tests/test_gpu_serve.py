@@ -113,3 +113,6 @@ def test_oversized_circuit_is_rejected_alone():
         want_a = stim_gb300.Circuit(small).compile_detector_sampler(seed=1).sample(5000, bit_packed=True)
         np.testing.assert_array_equal(a.result(), want_a)
         assert b.result().shape == want_a.shape
+        k = server.counters()
+        assert (k["submitted"], k["rejected"], k["completed"], k["failed"]) == (2, 1, 2, 0)
+        assert k["queued"] == 0 and k["pending"] == 0 and k["chunks_admitted"] >= 2
