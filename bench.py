@@ -544,6 +544,7 @@ def run_gpu(args):
     hbm_peak = _measured_hbm_peak()
 
     configs = run_configs(args, local) if args.config_steps > 0 else None
+    writes = run_sample_write(args, local, text) if args.write_steps > 0 else None
     batched = run_batched(args, local) if args.batched else None
     serving = run_serving_legs(args, local) if args.serve_seconds > 0 else None
     m2d = run_m2d(args, local, text) if args.m2d_steps > 0 else None
@@ -616,6 +617,7 @@ def run_gpu(args):
                                           "sample": f"{cb1_shots} shots in 4096-shot calls ({cb1_s:.1f} s)"}},
             "clocks": clk,
             "configs": configs,
+            "sample_write": writes,
             "batched": batched,
             "serving": serving,
             "m2d": m2d,
@@ -810,6 +812,25 @@ def run_configs(args, local):
                            "kind": "port", "unit": UNIT}
         out.append(row)
     return out
+
+
+def run_sample_write(args, local, text):
+    """sample_write (the result file formats, made on the device) of the main workload into /dev/null, so that the
+    figure is the library's own rate, not the disk's: detection events with the observables appended, per format,
+    median of --write-steps calls.  01 writes one byte per bit, so it samples a quarter of the shots."""
+    import stim_gb300
+
+    c = stim_gb300.Circuit(text)
+    D, O = c.num_detectors, c.num_observables
+    s = c.compile_detector_sampler(seed=args.seed, device=local)
+    out = {}
+    for fmt in ("b8", "r8", "hits", "dets", "ptb64", "01"):
+        shots = args.write_shots // 4 if fmt == "01" else args.write_shots
+        ms = _median_ms(lambda: s.sample_write(shots, filepath="/dev/null", format=fmt, append_observables=True),
+                        args.write_steps)
+        out[fmt] = {"shots": shots, "ms": ms, "gbits": shots * (D + O) / (ms / 1e3) / 1e9}
+    return {"workload": f"sample_write of d=25 r=25 p=1e-3 detection events + observable, to /dev/null",
+            "formats": out}
 
 
 def run_batched(args, local):
@@ -1022,6 +1043,8 @@ def main():
     ap.add_argument("--noise-mode", type=int, default=-1, help="-1 automatic, 0 inline, 1 hit lists")
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--batched", type=int, default=1)
+    ap.add_argument("--write-steps", type=int, default=3, help="timed sample_write calls per result format")
+    ap.add_argument("--write-shots", type=int, default=1 << 18)
     ap.add_argument("--config-steps", type=int, default=5, help="timed calls per seed of the d=3 and d=11 legs")
     ap.add_argument("--m2d-steps", type=int, default=5)
     ap.add_argument("--dem-steps", type=int, default=5)

@@ -17,9 +17,9 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["kernels.cu", "frame_lean.cu", "noalloc.cu"]
+CU_SOURCES = ["kernels.cu", "frame_lean.cu", "formats.cu", "noalloc.cu"]
 CC_SOURCES = ["circuit.cc", "lower.cc", "tableau.cc", "formats.cc", "capi.cc", "batch.cc", "serve.cc", "m2d.cc", "dem.cc", "dem_sampler.cc", "feed.cc"]
-HEADERS = ["gfs_contract.h", "gfs_gates.h", "frame_rules.h", "circuit.h", "lower.h", "program.h", "kernels.h", "frame_device.cuh", "noalloc.h", "sampler.h", "batch_engine.h", "tableau.h", "formats.h", "dem.h"]
+HEADERS = ["gfs_contract.h", "gfs_gates.h", "frame_rules.h", "circuit.h", "lower.h", "program.h", "kernels.h", "frame_device.cuh", "noalloc.h", "sampler.h", "batch_engine.h", "tableau.h", "formats.h", "formats_device.h", "dem.h"]
 
 
 def _newest_input():

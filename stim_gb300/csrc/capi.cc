@@ -5,6 +5,7 @@
 #include <mutex>
 
 #include "formats.h"
+#include "formats_device.h"
 #include "noalloc.h"
 #include "tableau.h"
 
@@ -153,11 +154,81 @@ struct File {
     }
 };
 
-// Shots per sampled chunk when writing files: rows of `row_bytes` bytes in about 256 MiB of host memory,
+// Shots per sampled chunk when writing files: about 256 MiB of rows or of file bytes (01 is eight times the rows),
 // a multiple of 128 shots (so of 64, as ptb64 needs).
-uint64_t write_chunk(uint64_t row_bytes) {
-    const uint64_t c = ((uint64_t)256 << 20) / std::max<uint64_t>(1, row_bytes);
+uint64_t write_chunk(uint64_t row_bytes, gfs::Format f, uint64_t nbits) {
+    const uint64_t per_shot = std::max<uint64_t>(1, f == gfs::Format::F01 ? std::max(row_bytes, nbits + 1) : row_bytes);
+    const uint64_t c = ((uint64_t)256 << 20) / per_shot;
     return std::max<uint64_t>(128, c & ~(uint64_t)127);
+}
+
+// Writes `shots` device rows (bit-packed, `stride` bytes apart, `nbits` bits) to `out` in format f: the file's
+// bytes are made on the device (formats.cu), copied to a page-locked buffer and written.  The prefix rules for
+// dets follow the host writer (formats.cc write_rows).
+void write_device_rows(gfs_sampler *s, FILE *out, gfs::Format f, const uint8_t *rows, uint64_t stride,
+                       uint64_t shots, uint64_t nbits, char c1, char c2, uint64_t transition) {
+    if (!out || shots == 0) {
+        return;
+    }
+    if (transition == 0) {
+        transition = nbits;
+        c1 = c2;
+    } else if (c1 == c2 || transition >= nbits) {
+        transition = nbits;
+    }
+    gfs::FormatArgs a{};
+    a.rows = rows;
+    a.stride = stride;
+    a.shots = shots;
+    a.nbits = nbits;
+    a.fmt = (uint32_t)f;
+    a.c1 = (uint8_t)c1;
+    a.c2 = (uint8_t)c2;
+    a.transition = transition;
+    const uint8_t *src = nullptr;
+    uint64_t bytes = 0;
+    if (f == gfs::Format::B8 && stride == (nbits + 7) / 8) {
+        src = rows;
+        bytes = shots * stride;
+    } else if (f == gfs::Format::B8 || f == gfs::Format::F01 || f == gfs::Format::PTB64) {
+        if (f == gfs::Format::B8) {
+            throw std::logic_error("b8 rows must be contiguous");
+        }
+        bytes = gfs::fixed_format_bytes(f, shots, nbits);
+        s->fmt_out.ensure(std::max<uint64_t>(16, bytes), s->device);
+        a.out = (uint8_t *)s->fmt_out.p;
+        ck(gfs::launch_format_write(a, s->stream), "format kernel");
+        src = a.out;
+    } else {
+        s->fmt_lens.ensure(std::max<uint64_t>(16, shots * 4), s->device);
+        s->fmt_offs.ensure((shots + 1) * 8, s->device);
+        s->fmt_sums.ensure(((shots + 1024) / 1024) * 8, s->device);
+        s->fmt_total.ensure(16, s->device);
+        a.lens = (uint32_t *)s->fmt_lens.p;
+        a.offs = (uint64_t *)s->fmt_offs.p;
+        ck(gfs::launch_format_lengths(a, (uint64_t *)s->fmt_sums.p, (uint64_t *)s->fmt_total.p, s->stream),
+           "format lengths");
+        ck(cudaMemcpyAsync(&bytes, s->fmt_total.p, 8, cudaMemcpyDeviceToHost, s->stream), "format size");
+        ck(cudaStreamSynchronize(s->stream), "format size");
+        s->fmt_out.ensure(std::max<uint64_t>(16, bytes), s->device);
+        a.out = (uint8_t *)s->fmt_out.p;
+        ck(gfs::launch_format_write(a, s->stream), "format kernel");
+        src = a.out;
+    }
+    if (bytes > s->h_fmt_cap) {
+        if (s->h_fmt) {
+            cudaFreeHost(s->h_fmt);
+            s->h_fmt = nullptr;
+            s->h_fmt_cap = 0;
+        }
+        ck(cudaHostAlloc((void **)&s->h_fmt, bytes, cudaHostAllocDefault), "cudaHostAlloc");
+        s->h_fmt_cap = bytes;
+    }
+    ck(cudaMemcpyAsync(s->h_fmt, src, bytes, cudaMemcpyDeviceToHost, s->stream), "copy file bytes");
+    ck(cudaStreamSynchronize(s->stream), "copy file bytes");
+    if (fwrite(s->h_fmt, 1, bytes, out) != bytes) {
+        throw std::runtime_error("failed to write the result file");
+    }
 }
 
 // CompiledDetectorSampler.sample_write (compiled_detector_sampler.pybind.cc:88-141 and
@@ -180,27 +251,25 @@ void write_detections(gfs_sampler *s, uint64_t shots, const char *path, const ch
     }
     File out(path), obs_out(obs_path);
     const uint64_t nd = D + (prepend || append ? O : 0);
-    const uint64_t drow = (nd + 7) / 8, orow = (O + 7) / 8;
-    const uint64_t chunk = write_chunk(drow + orow);
-    std::vector<uint8_t> dbuf, obuf;
+    const uint64_t drow = std::max<uint64_t>(1, (nd + 7) / 8), orow = std::max<uint64_t>(1, (O + 7) / 8);
+    const uint64_t chunk = std::min(write_chunk(drow + orow, f, nd), write_chunk(drow + orow, of, O));
     for (uint64_t done = 0; done < shots;) {
         const uint64_t cs = std::min<uint64_t>(shots - done, chunk);
-        dbuf.resize(std::max<uint64_t>(1, cs * drow));
+        s->fmt_rows.ensure(cs * drow, s->device);
         if (obs_path) {
-            obuf.resize(std::max<uint64_t>(1, cs * orow));
+            s->fmt_obs.ensure(cs * orow, s->device);
         }
-        s->detections(cs, (flags & (GFS_PREPEND_OBSERVABLES | GFS_APPEND_OBSERVABLES)) | GFS_BIT_PACKED, dbuf.data(),
-                      std::max<uint64_t>(1, drow), obs_path ? obuf.data() : nullptr, std::max<uint64_t>(1, orow), false);
+        s->detections(cs, (flags & (GFS_PREPEND_OBSERVABLES | GFS_APPEND_OBSERVABLES)) | GFS_BIT_PACKED,
+                      (uint8_t *)s->fmt_rows.p, drow, obs_path ? (uint8_t *)s->fmt_obs.p : nullptr, orow, true);
         // Prefixes as the reference names them: D then L when appended, L then D when prepended.
-        if (append) {
-            gfs::write_rows(out.f, f, dbuf.data(), std::max<uint64_t>(1, drow), cs, nd, 'D', 'L', D);
-        } else if (prepend) {
-            gfs::write_rows(out.f, f, dbuf.data(), std::max<uint64_t>(1, drow), cs, nd, 'L', 'D', O);
+        const uint8_t *rows = (const uint8_t *)s->fmt_rows.p;
+        if (prepend) {
+            write_device_rows(s, out.f, f, rows, drow, cs, nd, 'L', 'D', O);
         } else {
-            gfs::write_rows(out.f, f, dbuf.data(), std::max<uint64_t>(1, drow), cs, nd, 'D', 'L', D);
+            write_device_rows(s, out.f, f, rows, drow, cs, nd, 'D', 'L', D);
         }
         if (obs_path) {
-            gfs::write_rows(obs_out.f, of, obuf.data(), std::max<uint64_t>(1, orow), cs, O, 'L', 'L', O);
+            write_device_rows(s, obs_out.f, of, (const uint8_t *)s->fmt_obs.p, orow, cs, O, 'L', 'L', O);
         }
         done += cs;
     }
@@ -214,14 +283,13 @@ void write_measurements(gfs_sampler *s, uint64_t shots, const char *path, const 
     }
     File out(path);
     const uint64_t M = s->prog.num_measurements;
-    const uint64_t row = (M + 7) / 8;
-    const uint64_t chunk = write_chunk(row);
-    std::vector<uint8_t> buf;
+    const uint64_t row = std::max<uint64_t>(1, (M + 7) / 8);
+    const uint64_t chunk = write_chunk(row, f, M);
     for (uint64_t done = 0; done < shots;) {
         const uint64_t cs = std::min<uint64_t>(shots - done, chunk);
-        buf.resize(std::max<uint64_t>(1, cs * row));
-        s->measurements(cs, GFS_BIT_PACKED, ref, buf.data(), std::max<uint64_t>(1, row));
-        gfs::write_rows(out.f, f, buf.data(), std::max<uint64_t>(1, row), cs, M, 'M', 'M', 0);
+        s->fmt_rows.ensure(cs * row, s->device);
+        s->measurements_device(cs, GFS_BIT_PACKED, ref, (uint8_t *)s->fmt_rows.p, row);
+        write_device_rows(s, out.f, f, (const uint8_t *)s->fmt_rows.p, row, cs, M, 'M', 'M', 0);
         done += cs;
     }
 }

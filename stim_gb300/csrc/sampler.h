@@ -118,6 +118,11 @@ struct gfs_sampler {
     DevBuf d_ops, d_pool, d_tables, d_chans, d_orig, d_status;
     DevBuf det_tmp, obs_tmp, meas_tmp, out_tmp, ref_bits, ring_buf, frames_buf;
     DevBuf feed_rows[2], feed_compact[2], feed_aux[2];  // gfs_sample_for_decoder (feed.cc), per pipeline slot
+    // sample_write (capi.cc): device rows of a chunk, the device formatter's scratch and output, and a page-locked
+    // host buffer the file's bytes are copied into.
+    DevBuf fmt_rows, fmt_obs, fmt_lens, fmt_offs, fmt_sums, fmt_total, fmt_out;
+    uint8_t *h_fmt = nullptr;
+    size_t h_fmt_cap = 0;
     const uint4 *sweep_rows = nullptr;  // [local block][nsweep] sweep bits for the next run_frame (m2d.cc)
     // 16 words of mapped page-locked host memory: the status word (word 0) and the decoder feed's counts
     // (words 4-7) are published here by a kernel instead of copied (launch_publish_words).
@@ -183,6 +188,9 @@ struct gfs_sampler {
         }
         if (h_words) {
             cudaFreeHost(h_words);
+        }
+        if (h_fmt) {
+            cudaFreeHost(h_fmt);
         }
     }
 
@@ -812,6 +820,51 @@ struct gfs_sampler {
         ck(cudaStreamSynchronize(stream), "sample");
         t_total = elapsed(0, 1);
         t_copy = std::max(0.0, t_total - t_frame - t_noise - t_transpose);
+    }
+
+    // Measurement records into device memory (shot-major, `stride` bytes apart), the reference sample XORed in.
+    void measurements_device(uint64_t shots, uint32_t flags, const uint8_t *ref, uint8_t *out, uint64_t stride) {
+        if (mode != GFS_MODE_MEASUREMENTS) {
+            throw std::invalid_argument("sampler was not created in measurement mode");
+        }
+        const bool packed = flags & GFS_BIT_PACKED;
+        const uint64_t M = prog.num_measurements;
+        const uint64_t row = packed ? (M + 7) / 8 : M;
+        if (stride < row) {
+            throw std::invalid_argument("output row stride too small");
+        }
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        reset_timings();
+        const uint8_t *dref = nullptr;
+        if (ref && M) {
+            ref_bits.ensure((M + 7) / 8, device);
+            ck(cudaMemcpyAsync(ref_bits.p, ref, (M + 7) / 8, cudaMemcpyHostToDevice, stream), "ref upload");
+            dref = (const uint8_t *)ref_bits.p;
+        }
+        ck(cudaEventRecord(ev[0], stream), "event");
+        const uint64_t cb = chunk_blocks(row);
+        for (uint64_t done = 0; done < shots;) {
+            const uint64_t cs = std::min<uint64_t>(shots - done, cb * 128);
+            const uint64_t nblk = (cs + 127) / 128;
+            for (int attempt = 0; attempt < 2; attempt++) {
+                run_frame(nblk, next_block);
+                transpose((const uint4 *)meas_tmp.p, M, nullptr, 0, nullptr, 0, dref, cs, out + done * stride, stride,
+                          packed);
+                ck(cudaStreamSynchronize(stream), "sample");
+                account_noise(-1);
+                const bool overflow = check_status();
+                force_inline = false;
+                if (!overflow) {
+                    break;
+                }
+                force_inline = true;  // redo the chunk with inline noise (same results)
+            }
+            next_block += nblk;
+            done += cs;
+        }
+        ck(cudaEventRecord(ev[1], stream), "event");
+        ck(cudaStreamSynchronize(stream), "sample");
+        t_total = elapsed(0, 1);
     }
 
     void measurements(uint64_t shots, uint32_t flags, const uint8_t *ref, uint8_t *out, uint64_t stride) {

@@ -112,3 +112,27 @@ def test_sample_write_errors(tmp_path):
     with pytest.raises(IndexError, match="Can't combine"):
         s.sample_write(64, filepath=str(tmp_path / "x"), append_observables=True,
                        obs_out_filepath=str(tmp_path / "y"))
+
+
+@pytest.mark.parametrize("fmt", ["01", "b8", "r8", "hits", "dets", "ptb64"])
+@pytest.mark.parametrize("family,d,p,shots", [("surface_code:rotated_memory_z", 25, 0.001, 4096),
+                                              ("surface_code:rotated_memory_x", 11, 0.02, 8192)])
+def test_device_formatted_files_equal_host_writer_at_scale(fmt, family, d, p, shots, tmp_path):
+    # sample_write formats on the device; the same bits written by the host writer (write_shot_data_file, whose
+    # files are pinned to the reference CLI's) must give the same bytes.
+    from stim_gb300 import workloads
+
+    c = stim_gb300.Circuit(workloads.code_circuit(family, d, d, p))
+    D, O, M = c.num_detectors, c.num_observables, c.num_measurements
+    out = tmp_path / "dev"
+    c.compile_detector_sampler(seed=5).sample_write(shots, filepath=str(out), format=fmt, append_observables=True)
+    bits = c.compile_detector_sampler(seed=5).sample(shots, bit_packed=True, append_observables=True)
+    ref = tmp_path / "host"
+    stim_gb300.write_shot_data_file(data=bits, path=str(ref), format=fmt, num_detectors=D, num_observables=O)
+    assert open(out, "rb").read() == open(ref, "rb").read()
+    mout = tmp_path / "mdev"
+    c.compile_sampler(seed=6).sample_write(shots, filepath=str(mout), format=fmt)
+    m = c.compile_sampler(seed=6).sample(shots, bit_packed=True)
+    mref = tmp_path / "mhost"
+    stim_gb300.write_shot_data_file(data=m, path=str(mref), format=fmt, num_measurements=M)
+    assert open(mout, "rb").read() == open(mref, "rb").read()
