@@ -392,10 +392,12 @@ struct gfs_sampler {
             uint64_t b = std::max<uint64_t>(1, chunk_shots / 128);
             return ((b + bpc - 1) / bpc) * bpc;
         }
-        uint64_t budget = (uint64_t)3 << 30;
+        // Up to 12 GiB (a quarter of the free memory at most) per chunk: a 2^20-shot d=25 call then runs as one
+        // chunk, one partly filled last wave instead of three (8.27 -> 8.02 ms for noise + frame + transpose).
+        uint64_t budget = (uint64_t)12 << 30;
         size_t free_b = 0, total_b = 0;
         if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
-            budget = std::min<uint64_t>(budget, free_b / 3);
+            budget = std::min<uint64_t>(budget, free_b / 4);
         }
         uint64_t b = std::max<uint64_t>(1, budget / std::max<uint64_t>(1, per_block_bytes(out_row_bytes)));
         uint64_t wave = (uint64_t)shape.grid * bpc;
