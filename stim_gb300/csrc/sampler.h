@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <initializer_list>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -640,8 +641,27 @@ struct gfs_sampler {
     // staging buffer; its device->host copy runs on `copy_stream` while chunk k + 1's kernels run.  The
     // copy of chunk k is issued only after chunk k + 1's kernels are queued, because a copy into pageable
     // memory may hold the calling thread until it completes.
+    // Whether every non-null host destination is page-locked: then a chunk's copy can be queued as soon as its
+    // kernels are, because cudaMemcpyAsync into page-locked memory returns at once.
+    static bool page_locked(std::initializer_list<const void *> ptrs) {
+        for (const void *p : ptrs) {
+            if (!p) {
+                continue;
+            }
+            cudaPointerAttributes at{};
+            if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+                cudaGetLastError();
+                return false;
+            }
+            if (at.type != cudaMemoryTypeHost) {
+                return false;
+            }
+        }
+        return true;
+    }
+
     template <typename Produce, typename Copy>
-    void host_pipeline(uint64_t shots, uint64_t slot_row_bytes, Produce produce, Copy copy) {
+    void host_pipeline(uint64_t shots, uint64_t slot_row_bytes, Produce produce, Copy copy, bool eager = false) {
         const uint64_t first_block = next_block;
         uint64_t nblk_total = (shots + 127) / 128;
         uint64_t cb = host_chunk_blocks(nblk_total, slot_row_bytes);
@@ -692,10 +712,16 @@ struct gfs_sampler {
             ck(cudaEventRecord(pev[slot][2], stream), "event");
             inflight[slot] = Chunk{done, cs};
             used[slot] = true;
-            if (prev >= 0) {
-                issue_copy(prev);
+            if (eager) {
+                // Page-locked destinations: queue this chunk's copy now, so the copy engine already holds it when the
+                // previous copy ends (the thread's wait for a free slot would otherwise leave a gap between copies).
+                issue_copy(slot);
+            } else {
+                if (prev >= 0) {
+                    issue_copy(prev);
+                }
+                prev = slot;
             }
-            prev = slot;
             next_block += nblk;
             done += cs;
             k++;
@@ -718,7 +744,7 @@ struct gfs_sampler {
             next_block = first_block;
             force_inline = true;
             try {
-                host_pipeline(shots, slot_row_bytes, produce, copy);
+                host_pipeline(shots, slot_row_bytes, produce, copy, eager);
             } catch (...) {
                 force_inline = false;
                 throw;
@@ -781,7 +807,8 @@ struct gfs_sampler {
                     if (obs && orow) {
                         copy_rows(obs + done * ostride, ostride, buf + cs * ds, os, orow, cs, "copy obs");
                     }
-                });
+                },
+                page_locked({dets, obs}));
             return;
         }
         ck(cudaEventRecord(ev[0], stream), "event");
@@ -897,7 +924,8 @@ struct gfs_sampler {
                 if (row) {
                     copy_rows(out + done * stride, stride, buf, rs, row, cs, "copy meas");
                 }
-            });
+            },
+            page_locked({out}));
     }
 };
 
