@@ -250,6 +250,7 @@ struct BatchEngine {
                 a.n_occ = (uint32_t)s->prog.occs.size();
                 a.slice_cap = pl.slice_cap;
                 a.occs = a.n_occ ? (const gfs::NoiseOcc *)pl.occs->p : nullptr;
+                a.occ_xform = lean ? s->occ_xform() : nullptr;  // records for the lean plan's moved hit phases
                 a.smem_occ = s->smem_occ(true);
                 hit_off[j] = hit_total;
                 count_off[j] = count_total;

@@ -143,7 +143,25 @@ struct OccParams {
     uint32_t code, sub, kind, purpose, n, a;
     bool pair, fused;
     uint64_t inst;
+    const OccXform *xf;  // the lean plan moved this occurrence: transform its Paulis (program.h OccXform)
 };
+
+// The Pauli bits of a hit on rows (r1, r2) as they must be applied where the lean plan moved the occurrence.
+__device__ __forceinline__ uint32_t xform_bits(const OccXform &x, const uint32_t *pool, uint32_t bits, uint32_t r1,
+                                               uint32_t r2, bool pair) {
+    bits = ((bits < 8 ? x.own_lo >> (4 * bits) : x.own_hi >> (4 * (bits - 8)))) & 15u;
+    for (uint32_t f = 0; f < x.nf; f++) {
+        const uint32_t tab = x.ftab[f];
+        const uint32_t *mem = pool + x.fmem[f];
+        if ((__ldg(mem + (r1 >> 5)) >> (r1 & 31)) & 1u) {
+            bits = (bits & ~3u) | ((tab >> (2 * (bits & 3u))) & 3u);
+        }
+        if (pair && ((__ldg(mem + (r2 >> 5)) >> (r2 & 31)) & 1u)) {
+            bits = (bits & 3u) | (((tab >> (2 * ((bits >> 2) & 3u))) & 3u) << 2);
+        }
+    }
+    return bits;
+}
 
 // which = 0 for a noise op, 1 for the noise fused before a gate (op.d), 2 for the noise fused after it (op.c).
 __device__ __forceinline__ OccParams occ_params(const KernelArgs &p, const DevOp &op, uint32_t which,
@@ -157,6 +175,7 @@ __device__ __forceinline__ OccParams occ_params(const KernelArgs &p, const DevOp
     o.pair = false;
     o.fused = which != 0;
     o.inst = inst;
+    o.xf = nullptr;
     if (which) {
         const uint32_t w = which == 1 ? op.d : op.c;
         o.ch = &p.chans[(w & kFusedChanMask) - 1];
@@ -194,9 +213,12 @@ __device__ __forceinline__ uint64_t occ_record(const KernelArgs &p, const OccPar
         const uint32_t v = o.sub == 0 ? (c & 3u) : pauli_xz(gfs_choice_weighted(c, o.ch->cum, 4));
         return hit_record(__ldg(p.pool + o.a + u), u, v, s9);
     }
-    const uint32_t bits = hit_bits(o.kind, *o.ch, st);
+    uint32_t bits = hit_bits(o.kind, *o.ch, st);
     const uint32_t r1 = __ldg(p.pool + o.a + (o.pair ? 2 * u : u));
     const uint32_t r2 = o.pair ? __ldg(p.pool + o.a + 2 * u + 1) : r1;
+    if (o.xf) {
+        bits = xform_bits(*o.xf, p.pool, bits, r1, r2, o.pair);
+    }
     return hit_record(r1, r2, bits, s9);
 }
 
@@ -223,7 +245,10 @@ __device__ __forceinline__ void noise_records(const KernelArgs &p, uint32_t slic
                                               uint32_t lane, NoiseQueued *q, uint32_t *count) {
     const NoiseOcc oc = p.occs[k];
     const DevOp op = p.ops[oc.pc];
-    const OccParams o = occ_params(p, op, oc.which, oc.inst);
+    OccParams o = occ_params(p, op, oc.which, oc.inst);
+    if (p.occ_xform && oc.xform) {
+        o.xf = p.occ_xform + (oc.xform - 1);
+    }
     if (lane < (uint32_t)SB) {
         count[lane] = 0;  // this warp's records per slice (shared memory)
     }

@@ -51,6 +51,9 @@ struct KernelArgs {
     const LeanPhase *lean;
     const uint64_t *lean_inst;
     uint32_t n_lean;
+    // Non-null when the lean kernel consumes the hit records: noise_kernel transforms the Paulis of the occurrences
+    // the lean plan moved (NoiseOcc.xform, program.h OccXform).
+    const OccXform *occ_xform;
 };
 
 // Several circuits in one launch (batch_frame_kernel): circuit j owns work items

@@ -9,7 +9,6 @@
 #include "lower.h"
 
 #include <algorithm>
-#include <functional>
 #include <cmath>
 #include <functional>
 #include <iterator>
@@ -40,6 +39,9 @@ struct Lowerer {
     uint64_t pending_inst = 0;
 
     LowerOptions opts;
+
+    // The op and the noise slot (0 noise op, 1 fused before the gate, 2 after it) of each lean phase.
+    std::vector<uint32_t> lean_pc, lean_which;
 
     Lowerer(const Circuit &c, SampleMode m, const LowerOptions &o) : root(c), mode(m), opts(o) {
     }
@@ -1466,13 +1468,20 @@ struct Lowerer {
     void build_lean() {
         prog.lean.clear();
         prog.lean_inst.clear();
+        prog.occ_xform.clear();
         prog.lean_ok = false;
+        lean_pc.clear();
+        lean_which.clear();
         std::vector<uint32_t> open;  // phase indices of the open LK_LOOP_BEGINs
+        uint32_t pc = 0, which = 0;
         auto add = [&](uint32_t kind, uint32_t sub, uint32_t flags, uint32_t n, uint32_t a, uint32_t b, uint64_t inst) {
             prog.lean.push_back(LeanPhase{kind | (sub << 8) | flags, n, a, b});
             prog.lean_inst.push_back(inst);
+            lean_pc.push_back(pc);
+            lean_which.push_back(which);
         };
-        for (const DevOp &op : prog.ops) {
+        for (pc = 0; pc < prog.ops.size(); pc++) {
+            const DevOp &op = prog.ops[pc];
             const uint32_t code = op.code & 0xFFu, sub = (op.code >> 8) & 0xFFu;
             const bool compact = (op.code & kCompact) != 0;
             const uint32_t norand = (op.code & kNoRandomize) ? kLeanNoRandomize : 0u;
@@ -1481,8 +1490,10 @@ struct Lowerer {
                 return;
             }
             if (gate && (op.d & kFusedChanMask)) {
+                which = 1;
                 add(LK_HITS, 0, 0, op.n, 0, 0, op.inst);
             }
+            which = 0;
             switch (code) {
                 case OP_END:
                     add(LK_END, 0, 0, 0, 0, 0, 0);
@@ -1550,14 +1561,182 @@ struct Lowerer {
                     return;
             }
             if (gate && (op.c & kFusedChanMask)) {
+                which = 2;
                 add(LK_HITS, 0, 0, op.n, 0, 0, op.inst);
             }
         }
         if (!open.empty() || prog.num_detectors > 0xFFFFFFFFull || prog.num_measurements > 0xFFFFFFFFull) {
             return;
         }
+        move_lean_hits();
         mark_lean_barriers();
         prog.lean_ok = true;
+    }
+
+    // Rows touched by the units of op pc (gate rows, or the rows of a noise op); `pair` when units are pairs.
+    void op_rows(uint32_t pc, std::vector<uint32_t> &rows, bool &pair) const {
+        const DevOp &op = prog.ops[pc];
+        const uint32_t code = op.code & 0xFFu, sub = (op.code >> 8) & 0xFFu;
+        pair = code == OP_2Q || (code == OP_NOISE && (sub == KN_DEP2 || sub == KN_PC2));
+        const uint32_t k = pair ? 2u : 1u;
+        rows.assign(prog.pool.begin() + op.a, prog.pool.begin() + op.a + (size_t)k * op.n);
+    }
+
+    // Moves hit phases earlier across the gates right before them when that lands them next to another phase they
+    // commute with (a hit, flip or detector phase), so that the two run with no barrier between.  A Pauli P
+    // applied after a gate with frame map M equals M^-1(P) applied before it (the maps are linear over GF(2)), so
+    // a moved occurrence gets a transform of its records (program.h OccXform) that noise_kernel applies.  A hit
+    // phase crosses: its own gate (the noise fused after a one- or two-qubit gate: the gate's inverse map on the
+    // unit's 2 or 4 Pauli bits), up to two other one-qubit gates (their inverse map on the rows they act on), and
+    // gates, measurements and resets on rows disjoint from its own (no change).  It never crosses another hit
+    // phase, so the kernel still consumes the occurrences in order.
+    void move_lean_hits() {
+        if (prog.occs.empty()) {
+            return;  // no hit lists, so no records to transform
+        }
+        std::vector<LeanPhase> &ph = prog.lean;
+        const size_t n = ph.size();
+        auto kind = [&](size_t i) { return ph[i].op & 0xFFu; };
+        auto lands = [&](uint32_t k) {
+            return k == LK_HITS || k == LK_FLIPS || k == LK_DETS2 || k == LK_DETS || k == LK_EMIT;
+        };
+        // Inverse one-qubit map of K1_* gate `sub` on (x, z) = bits 0, 1: entry v (2 bits each) = M^-1(v).
+        auto inv1 = [](uint32_t sub) {
+            uint32_t t = 0;
+            for (uint32_t w = 0; w < 4; w++) {
+                uint32_t x = w & 1u, z = (w >> 1) & 1u;
+                rule1w(sub, x, z);
+                t |= w << (2 * ((x & 1u) | (z & 1u) << 1));
+            }
+            return t;
+        };
+        // Inverse two-qubit map of K2_* gate `sub` on (x1, z1, x2, z2) = bits 0..3 (4 bits per entry).
+        auto inv2 = [](uint32_t sub, uint32_t &lo, uint32_t &hi) {
+            uint64_t t = 0;
+            for (uint32_t w = 0; w < 16; w++) {
+                uint32_t x1 = w & 1u, z1 = (w >> 1) & 1u, x2 = (w >> 2) & 1u, z2 = (w >> 3) & 1u;
+                rule2(sub, x1, z1, x2, z2);
+                const uint32_t v = (x1 & 1u) | (z1 & 1u) << 1 | (x2 & 1u) << 2 | (z2 & 1u) << 3;
+                t |= (uint64_t)w << (4 * v);
+            }
+            lo = (uint32_t)t;
+            hi = (uint32_t)(t >> 32);
+        };
+        const uint64_t kIdLo = 0x76543210u, kIdHi = 0xFEDCBA98u;
+        std::map<uint32_t, uint32_t> member_at;  // gate op -> pool offset of its row bitmap
+        auto member_bitmap = [&](uint32_t gpc) {
+            auto it = member_at.find(gpc);
+            if (it != member_at.end()) {
+                return it->second;
+            }
+            std::vector<uint32_t> rows;
+            bool pr = false;
+            op_rows(gpc, rows, pr);
+            const uint32_t off = (uint32_t)prog.pool.size();
+            prog.pool.resize(prog.pool.size() + (prog.num_rows + 31) / 32, 0u);
+            for (uint32_t r : rows) {
+                prog.pool[off + (r >> 5)] |= 1u << (r & 31);
+            }
+            member_at[gpc] = off;
+            return off;
+        };
+        std::vector<uint32_t> xf_of(n, 0);  // 1 + index into prog.occ_xform of each phase
+        std::vector<uint8_t> in_hit(prog.num_rows, 0);
+        std::vector<uint32_t> hit_rows, gate_rows;
+        for (size_t i = 0; i < n; i++) {
+            if (kind(i) != LK_HITS) {
+                continue;
+            }
+            const uint32_t hpc = lean_pc[i], hwhich = lean_which[i];
+            const uint32_t hcode = prog.ops[hpc].code & 0xFFu;
+            if (hwhich == 0 && hcode != OP_NOISE) {
+                continue;
+            }
+            bool hpair = false;
+            op_rows(hpc, hit_rows, hpair);
+            for (uint32_t r : hit_rows) {
+                in_hit[r] = 1;
+            }
+            OccXform x{};
+            x.own_lo = (uint32_t)kIdLo;
+            x.own_hi = (uint32_t)kIdHi;
+            uint32_t fgate[2] = {0, 0};
+            size_t j = i;
+            while (j > 0) {
+                const size_t g = j - 1;
+                const uint32_t k = kind(g);
+                if (k != LK_1Q && k != LK_CX && k != LK_CZ && k != LK_2Q && k != LK_MEAS && k != LK_RESET) {
+                    break;
+                }
+                const uint32_t gpc = lean_pc[g];
+                bool gpair = false;
+                op_rows(gpc, gate_rows, gpair);
+                bool disjoint = true;
+                for (uint32_t r : gate_rows) {
+                    disjoint &= in_hit[r] == 0;
+                }
+                if (disjoint) {
+                    j = g;
+                    continue;
+                }
+                const uint32_t gsub = (prog.ops[gpc].code >> 8) & 0xFFu;
+                if (gpc == hpc && hwhich == 2 && g + 1 == i && (k == LK_1Q || k == LK_CX || k == LK_CZ || k == LK_2Q)) {
+                    if (k == LK_1Q) {
+                        const uint32_t t = inv1(gsub);
+                        x.own_lo = (uint32_t)kIdLo;
+                        for (uint32_t v = 0; v < 4; v++) {
+                            x.own_lo = (x.own_lo & ~(15u << (4 * v))) | (((t >> (2 * v)) & 3u) << (4 * v));
+                        }
+                    } else {
+                        inv2(gsub, x.own_lo, x.own_hi);
+                    }
+                    j = g;
+                    continue;
+                }
+                if (k == LK_1Q && x.nf < 2) {
+                    fgate[x.nf] = gpc;
+                    x.ftab[x.nf] = inv1(gsub);
+                    x.nf++;
+                    j = g;
+                    continue;
+                }
+                break;
+            }
+            for (uint32_t r : hit_rows) {
+                in_hit[r] = 0;
+            }
+            if (j == i || j == 0 || !lands(kind(j - 1))) {
+                continue;
+            }
+            for (uint32_t f = 0; f < x.nf; f++) {
+                x.fmem[f] = member_bitmap(fgate[f]);
+            }
+            const bool identity = x.nf == 0 && x.own_lo == (uint32_t)kIdLo && x.own_hi == (uint32_t)kIdHi;
+            if (!identity) {
+                prog.occ_xform.push_back(x);
+                xf_of[i] = (uint32_t)prog.occ_xform.size();
+            }
+            // Rotate phase i down to position j (every parallel list alike).
+            auto rot = [&](auto &v) { std::rotate(v.begin() + j, v.begin() + i, v.begin() + i + 1); };
+            rot(ph);
+            rot(prog.lean_inst);
+            rot(lean_pc);
+            rot(lean_which);
+            rot(xf_of);
+        }
+        if (prog.occ_xform.empty()) {
+            return;
+        }
+        std::map<std::pair<uint32_t, uint32_t>, uint32_t> xf_at;
+        for (size_t i = 0; i < n; i++) {
+            if (xf_of[i]) {
+                xf_at[{lean_pc[i], lean_which[i]}] = xf_of[i];
+            }
+        }
+        for (NoiseOcc &o : prog.occs) {
+            auto it = xf_at.find({o.pc, o.which});
+            o.xform = it == xf_at.end() ? 0u : it->second;
+        }
     }
 
     // Sets kLeanNoBarrier on the phases that every possible successor may follow without a barrier.

@@ -44,6 +44,7 @@ struct Program {
     // of fewer than 2^32 repetitions).
     std::vector<LeanPhase> lean;
     std::vector<uint64_t> lean_inst;
+    std::vector<OccXform> occ_xform;  // transforms of the hit occurrences the lean plan moved (NoiseOcc.xform)
     bool lean_ok = false;
 };
 

@@ -104,8 +104,25 @@ struct alignas(16) NoiseOcc {
     uint64_t inst;   // instance of the op (loop iteration applied)
     uint32_t off;    // first record within the slice region (even, so regions start on 16 bytes)
     uint32_t cap;    // records reserved
-    uint32_t pad[2];
+    uint32_t xform;  // 1 + index into the lean plan's OccXform table (0: the records' Paulis as drawn)
+    uint32_t pad;
 };
+
+// The lean phase list moves some hit phases earlier, across the gates they follow, so that they run next to other
+// hit phases without a barrier between (lower.cc move_lean_hits).  A Pauli P applied after a gate G whose frame
+// update is the linear map M equals M^-1(P) applied before G, so when the lean kernel consumes the records,
+// noise_kernel writes each moved occurrence's Pauli bits transformed: first by `own` (the inverse map of the gate
+// the noise is fused to, a 16-entry table of 4-bit patterns: X, Z on the first row, X, Z on the second), then for
+// each of `nf` one-qubit gates crossed by the row-local inverse map ftab (four 2-bit entries) on the rows of the
+// crossed gate (bitmap of rows at pool word fmem).
+struct OccXform {
+    uint32_t own_lo, own_hi;  // entries 0-7 and 8-15, four bits each
+    uint32_t nf;
+    uint32_t ftab[2];
+    uint32_t fmem[2];
+    uint32_t pad;
+};
+static_assert(sizeof(OccXform) == 32, "OccXform layout");
 static_assert(sizeof(NoiseOcc) == 32, "NoiseOcc layout");
 
 // Phase list of the lean frame kernel (frame_lean.cu): the device program re-cut into the phases the kernel

@@ -146,7 +146,7 @@ struct gfs_sampler {
     DevBuf hit_buf, hit_count, d_occs;
     // Lean frame kernel (frame_lean.cu): used for hit-list launches of programs with a phase list, unless
     // lean_pref = 0.  shape_lean mirrors `shape` with the lean kernel's shared memory and occupancy.
-    DevBuf d_lean, d_lean_inst;
+    DevBuf d_lean, d_lean_inst, d_occ_xform;
     int lean_pref = -1;  // -1 automatic (lean when possible), 0 never, 1 when possible
     bool lean_ready = false;
     gfs::LaunchShape shape_lean{};
@@ -308,6 +308,11 @@ struct gfs_sampler {
         }
     }
 
+    // Transforms of the occurrences the lean phase list moved (null when it moved none).
+    const gfs::OccXform *occ_xform() const {
+        return prog.occ_xform.empty() ? nullptr : (const gfs::OccXform *)d_occ_xform.p;
+    }
+
     // Whether a hit-list launch of the current shape runs the lean kernel.
     bool lean_active() const {
         return lean_ready && lean_pref != 0 && shape.hits && !force_inline && sweep_rows == nullptr;
@@ -368,6 +373,9 @@ struct gfs_sampler {
         if (prog.lean_ok) {
             upload(d_lean, prog.lean, device, stream);
             upload(d_lean_inst, prog.lean_inst, device, stream);
+            if (!prog.occ_xform.empty()) {
+                upload(d_occ_xform, prog.occ_xform, device, stream);
+            }
         }
         d_status.ensure(16, device);
         ck(cudaHostAlloc((void **)&h_words, 64, cudaHostAllocMapped), "cudaHostAlloc");
@@ -503,6 +511,7 @@ struct gfs_sampler {
             a.n_occ = (uint32_t)prog.occs.size();
             a.slice_cap = slice_cap;
             a.smem_occ = smem_occ(true);
+            a.occ_xform = lean ? occ_xform() : nullptr;  // records for the lean plan's moved hit phases
             ck(cudaEventRecord(ev_noise[cur_slot + 1][0], stream), "event");
             ck(gfs::launch_noise_kernel(a, sh.blocks_per_cta, stream), "noise kernel launch");
             ck(cudaEventRecord(ev_noise[cur_slot + 1][1], stream), "event");
