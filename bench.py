@@ -1053,7 +1053,7 @@ def main():
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--batched", type=int, default=1)
     ap.add_argument("--write-steps", type=int, default=3, help="timed sample_write calls per result format")
-    ap.add_argument("--write-shots", type=int, default=1 << 18)
+    ap.add_argument("--write-shots", type=int, default=1 << 20)
     ap.add_argument("--config-steps", type=int, default=5, help="timed calls per seed of the d=3 and d=11 legs")
     ap.add_argument("--m2d-steps", type=int, default=5)
     ap.add_argument("--dem-steps", type=int, default=5)

@@ -155,21 +155,22 @@ struct File {
 };
 
 // Shots per sampled chunk when writing files: about 256 MiB of rows or of file bytes (01 is eight times the rows),
-// a multiple of 128 shots (so of 64, as ptb64 needs).
-uint64_t write_chunk(uint64_t row_bytes, gfs::Format f, uint64_t nbits) {
+// and at most one resident wave of the frame kernel, so that consecutive chunks overlap well; a multiple of 128
+// shots (so of 64, as ptb64 needs).
+uint64_t write_chunk(const gfs_sampler *s, uint64_t row_bytes, gfs::Format f, uint64_t nbits) {
     const uint64_t per_shot = std::max<uint64_t>(1, f == gfs::Format::F01 ? std::max(row_bytes, nbits + 1) : row_bytes);
-    const uint64_t c = ((uint64_t)256 << 20) / per_shot;
+    uint64_t c = ((uint64_t)256 << 20) / per_shot;
+    const gfs::LaunchShape &sh = s->lean_active() ? s->shape_lean : s->shape;
+    c = std::min<uint64_t>(c, (uint64_t)std::max(1, sh.grid) * (uint64_t)std::max(1, sh.blocks_per_cta) * 128);
     return std::max<uint64_t>(128, c & ~(uint64_t)127);
 }
 
-// Writes `shots` device rows (bit-packed, `stride` bytes apart, `nbits` bits) to `out` in format f: the file's
-// bytes are made on the device (formats.cu), copied to a page-locked buffer and written.  The prefix rules for
-// dets follow the host writer (formats.cc write_rows).
-void write_device_rows(gfs_sampler *s, FILE *out, gfs::Format f, const uint8_t *rows, uint64_t stride,
-                       uint64_t shots, uint64_t nbits, char c1, char c2, uint64_t transition) {
-    if (!out || shots == 0) {
-        return;
-    }
+// Makes the file bytes of `shots` device rows (bit-packed, `stride` bytes apart, `nbits` bits) in format f on
+// s->stream (formats.cu), into `out` unless the rows already are the file (contiguous b8).  Returns where the
+// bytes are and how many.  The prefix rules for dets follow the host writer (formats.cc write_rows).
+std::pair<const uint8_t *, uint64_t> format_rows(gfs_sampler *s, DevBuf &out, gfs::Format f, const uint8_t *rows,
+                                                 uint64_t stride, uint64_t shots, uint64_t nbits, char c1, char c2,
+                                                 uint64_t transition) {
     if (transition == 0) {
         transition = nbits;
         c1 = c2;
@@ -185,20 +186,15 @@ void write_device_rows(gfs_sampler *s, FILE *out, gfs::Format f, const uint8_t *
     a.c1 = (uint8_t)c1;
     a.c2 = (uint8_t)c2;
     a.transition = transition;
-    const uint8_t *src = nullptr;
-    uint64_t bytes = 0;
-    if (f == gfs::Format::B8 && stride == (nbits + 7) / 8) {
-        src = rows;
-        bytes = shots * stride;
-    } else if (f == gfs::Format::B8 || f == gfs::Format::F01 || f == gfs::Format::PTB64) {
-        if (f == gfs::Format::B8) {
+    if (f == gfs::Format::B8) {
+        if (stride != (nbits + 7) / 8) {
             throw std::logic_error("b8 rows must be contiguous");
         }
+        return {rows, shots * stride};
+    }
+    uint64_t bytes = 0;
+    if (f == gfs::Format::F01 || f == gfs::Format::PTB64) {
         bytes = gfs::fixed_format_bytes(f, shots, nbits);
-        s->fmt_out.ensure(std::max<uint64_t>(16, bytes), s->device);
-        a.out = (uint8_t *)s->fmt_out.p;
-        ck(gfs::launch_format_write(a, s->stream), "format kernel");
-        src = a.out;
     } else {
         s->fmt_lens.ensure(std::max<uint64_t>(16, shots * 4), s->device);
         s->fmt_offs.ensure((shots + 1) * 8, s->device);
@@ -210,26 +206,86 @@ void write_device_rows(gfs_sampler *s, FILE *out, gfs::Format f, const uint8_t *
            "format lengths");
         ck(cudaMemcpyAsync(&bytes, s->fmt_total.p, 8, cudaMemcpyDeviceToHost, s->stream), "format size");
         ck(cudaStreamSynchronize(s->stream), "format size");
-        s->fmt_out.ensure(std::max<uint64_t>(16, bytes), s->device);
-        a.out = (uint8_t *)s->fmt_out.p;
-        ck(gfs::launch_format_write(a, s->stream), "format kernel");
-        src = a.out;
     }
-    if (bytes > s->h_fmt_cap) {
-        if (s->h_fmt) {
-            cudaFreeHost(s->h_fmt);
-            s->h_fmt = nullptr;
-            s->h_fmt_cap = 0;
-        }
-        ck(cudaHostAlloc((void **)&s->h_fmt, bytes, cudaHostAllocDefault), "cudaHostAlloc");
-        s->h_fmt_cap = bytes;
-    }
-    ck(cudaMemcpyAsync(s->h_fmt, src, bytes, cudaMemcpyDeviceToHost, s->stream), "copy file bytes");
-    ck(cudaStreamSynchronize(s->stream), "copy file bytes");
-    if (fwrite(s->h_fmt, 1, bytes, out) != bytes) {
-        throw std::runtime_error("failed to write the result file");
-    }
+    out.ensure(std::max<uint64_t>(16, bytes), s->device);
+    a.out = (uint8_t *)out.p;
+    ck(gfs::launch_format_write(a, s->stream), "format kernel");
+    return {a.out, bytes};
 }
+
+// File output of sample_write as a two-slot pipeline: chunk k is sampled and formatted on the sampler's stream
+// into slot k % 2, its bytes are copied to that slot's page-locked buffers on copy_stream, and written to the files
+// once chunk k + 1 has been sampled, so a chunk's copy overlaps the next chunk's kernels and its fwrite the next
+// chunk's copy.  Files receive the chunks in order.
+class FileWriter {
+   public:
+    explicit FileWriter(gfs_sampler *s) : s_(s) {
+        for (gfs_sampler::WriteSlot &w : s_->wslot) {
+            if (!w.formatted) {
+                ck(cudaEventCreateWithFlags(&w.formatted, cudaEventDisableTiming), "cudaEventCreate");
+            }
+            if (!w.copied) {
+                ck(cudaEventCreateWithFlags(&w.copied, cudaEventDisableTiming), "cudaEventCreate");
+            }
+            w.pending = false;
+        }
+    }
+    ~FileWriter() {
+        // Normal exit has flushed every slot; after an error, no copy may still be writing into a slot's buffer.
+        cudaStreamSynchronize(s_->copy_stream);
+        for (gfs_sampler::WriteSlot &w : s_->wslot) {
+            w.pending = false;
+        }
+    }
+
+    // The slot for chunk k (written out two chunks ago, so free).
+    gfs_sampler::WriteSlot &slot(uint64_t k) {
+        return s_->wslot[k & 1];
+    }
+
+    // Queues the copies of the slot's formatted bytes (part 0: the main file, part 1: the observables' file).
+    void queue(gfs_sampler::WriteSlot &w, const std::pair<const uint8_t *, uint64_t> part[2], FILE *files[2]) {
+        ck(cudaEventRecord(w.formatted, s_->stream), "event");
+        ck(cudaStreamWaitEvent(s_->copy_stream, w.formatted, 0), "cudaStreamWaitEvent");
+        for (int j = 0; j < 2; j++) {
+            w.file[j] = files[j];
+            w.bytes[j] = files[j] ? part[j].second : 0;
+            if (!w.bytes[j]) {
+                continue;
+            }
+            if (w.bytes[j] > w.host_cap[j]) {
+                if (w.host[j]) {
+                    cudaFreeHost(w.host[j]);
+                    w.host[j] = nullptr;
+                    w.host_cap[j] = 0;
+                }
+                ck(cudaHostAlloc((void **)&w.host[j], w.bytes[j], cudaHostAllocDefault), "cudaHostAlloc");
+                w.host_cap[j] = w.bytes[j];
+            }
+            ck(cudaMemcpyAsync(w.host[j], part[j].first, w.bytes[j], cudaMemcpyDeviceToHost, s_->copy_stream),
+               "copy file bytes");
+        }
+        ck(cudaEventRecord(w.copied, s_->copy_stream), "event");
+        w.pending = true;
+    }
+
+    // Writes the slot's bytes once their copies are done.
+    void flush(gfs_sampler::WriteSlot &w) {
+        if (!w.pending) {
+            return;
+        }
+        ck(cudaEventSynchronize(w.copied), "copy file bytes");
+        w.pending = false;
+        for (int j = 0; j < 2; j++) {
+            if (w.bytes[j] && fwrite(w.host[j], 1, w.bytes[j], w.file[j]) != w.bytes[j]) {
+                throw std::runtime_error("failed to write the result file");
+            }
+        }
+    }
+
+   private:
+    gfs_sampler *s_;
+};
 
 // CompiledDetectorSampler.sample_write (compiled_detector_sampler.pybind.cc:88-141 and
 // frame_simulator_util.inl:120-200): detection events (observables prepended, appended, or to a file of
@@ -252,27 +308,33 @@ void write_detections(gfs_sampler *s, uint64_t shots, const char *path, const ch
     File out(path), obs_out(obs_path);
     const uint64_t nd = D + (prepend || append ? O : 0);
     const uint64_t drow = std::max<uint64_t>(1, (nd + 7) / 8), orow = std::max<uint64_t>(1, (O + 7) / 8);
-    const uint64_t chunk = std::min(write_chunk(drow + orow, f, nd), write_chunk(drow + orow, of, O));
-    for (uint64_t done = 0; done < shots;) {
+    const uint64_t chunk = std::min(write_chunk(s, drow + orow, f, nd), write_chunk(s, drow + orow, of, O));
+    FileWriter fw(s);
+    uint64_t k = 0;
+    for (uint64_t done = 0; done < shots; k++) {
         const uint64_t cs = std::min<uint64_t>(shots - done, chunk);
-        s->fmt_rows.ensure(cs * drow, s->device);
+        gfs_sampler::WriteSlot &w = fw.slot(k);
+        w.rows.ensure(cs * drow, s->device);
         if (obs_path) {
-            s->fmt_obs.ensure(cs * orow, s->device);
+            w.obs.ensure(cs * orow, s->device);
         }
         s->detections(cs, (flags & (GFS_PREPEND_OBSERVABLES | GFS_APPEND_OBSERVABLES)) | GFS_BIT_PACKED,
-                      (uint8_t *)s->fmt_rows.p, drow, obs_path ? (uint8_t *)s->fmt_obs.p : nullptr, orow, true);
+                      (uint8_t *)w.rows.p, drow, obs_path ? (uint8_t *)w.obs.p : nullptr, orow, true);
         // Prefixes as the reference names them: D then L when appended, L then D when prepended.
-        const uint8_t *rows = (const uint8_t *)s->fmt_rows.p;
-        if (prepend) {
-            write_device_rows(s, out.f, f, rows, drow, cs, nd, 'L', 'D', O);
-        } else {
-            write_device_rows(s, out.f, f, rows, drow, cs, nd, 'D', 'L', D);
-        }
+        std::pair<const uint8_t *, uint64_t> part[2] = {
+            prepend ? format_rows(s, w.out[0], f, (const uint8_t *)w.rows.p, drow, cs, nd, 'L', 'D', O)
+                    : format_rows(s, w.out[0], f, (const uint8_t *)w.rows.p, drow, cs, nd, 'D', 'L', D),
+            {nullptr, 0}};
         if (obs_path) {
-            write_device_rows(s, obs_out.f, of, (const uint8_t *)s->fmt_obs.p, orow, cs, O, 'L', 'L', O);
+            part[1] = format_rows(s, w.out[1], of, (const uint8_t *)w.obs.p, orow, cs, O, 'L', 'L', O);
         }
+        FILE *files[2] = {out.f, obs_out.f};
+        fw.queue(w, part, files);
+        fw.flush(fw.slot(k + 1));  // the previous chunk, whose copy ran beside this chunk's kernels
         done += cs;
     }
+    fw.flush(fw.slot(k + 1));
+    fw.flush(fw.slot(k));
 }
 
 // CompiledMeasurementSampler.sample_write (compiled_measurement_sampler.pybind.cc:37-45).
@@ -284,14 +346,23 @@ void write_measurements(gfs_sampler *s, uint64_t shots, const char *path, const 
     File out(path);
     const uint64_t M = s->prog.num_measurements;
     const uint64_t row = std::max<uint64_t>(1, (M + 7) / 8);
-    const uint64_t chunk = write_chunk(row, f, M);
-    for (uint64_t done = 0; done < shots;) {
+    const uint64_t chunk = write_chunk(s, row, f, M);
+    FileWriter fw(s);
+    uint64_t k = 0;
+    for (uint64_t done = 0; done < shots; k++) {
         const uint64_t cs = std::min<uint64_t>(shots - done, chunk);
-        s->fmt_rows.ensure(cs * row, s->device);
-        s->measurements_device(cs, GFS_BIT_PACKED, ref, (uint8_t *)s->fmt_rows.p, row);
-        write_device_rows(s, out.f, f, (const uint8_t *)s->fmt_rows.p, row, cs, M, 'M', 'M', 0);
+        gfs_sampler::WriteSlot &w = fw.slot(k);
+        w.rows.ensure(cs * row, s->device);
+        s->measurements_device(cs, GFS_BIT_PACKED, ref, (uint8_t *)w.rows.p, row);
+        std::pair<const uint8_t *, uint64_t> part[2] = {
+            format_rows(s, w.out[0], f, (const uint8_t *)w.rows.p, row, cs, M, 'M', 'M', 0), {nullptr, 0}};
+        FILE *files[2] = {out.f, nullptr};
+        fw.queue(w, part, files);
+        fw.flush(fw.slot(k + 1));
         done += cs;
     }
+    fw.flush(fw.slot(k + 1));
+    fw.flush(fw.slot(k));
 }
 
 }  // namespace

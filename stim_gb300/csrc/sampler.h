@@ -5,8 +5,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <initializer_list>
+#include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <memory>
 #include <new>
 #include <stdexcept>
@@ -119,11 +120,20 @@ struct gfs_sampler {
     DevBuf d_ops, d_pool, d_tables, d_chans, d_orig, d_status;
     DevBuf det_tmp, obs_tmp, meas_tmp, out_tmp, ref_bits, ring_buf, frames_buf;
     DevBuf feed_rows[2], feed_compact[2], feed_aux[2];  // gfs_sample_for_decoder (feed.cc), per pipeline slot
-    // sample_write (capi.cc): device rows of a chunk, the device formatter's scratch and output, and a page-locked
-    // host buffer the file's bytes are copied into.
-    DevBuf fmt_rows, fmt_obs, fmt_lens, fmt_offs, fmt_sums, fmt_total, fmt_out;
-    uint8_t *h_fmt = nullptr;
-    size_t h_fmt_cap = 0;
+    // sample_write (capi.cc), two pipeline slots: a chunk's device rows (detectors or measurements, and observables
+    // for their own file), the file bytes the device formatter makes of them (one buffer per output file), page-locked
+    // host copies of those bytes, and events for the formatter's end and the copies' end.
+    struct WriteSlot {
+        DevBuf rows, obs, out[2];
+        uint8_t *host[2] = {nullptr, nullptr};
+        size_t host_cap[2] = {0, 0};
+        uint64_t bytes[2] = {0, 0};
+        FILE *file[2] = {nullptr, nullptr};
+        cudaEvent_t formatted = nullptr, copied = nullptr;
+        bool pending = false;  // copies queued whose bytes are not written yet
+    };
+    WriteSlot wslot[2];
+    DevBuf fmt_lens, fmt_offs, fmt_sums, fmt_total;  // the variable-length formatter's scratch (shared by the slots)
     const uint4 *sweep_rows = nullptr;  // [local block][nsweep] sweep bits for the next run_frame (m2d.cc)
     // 16 words of mapped page-locked host memory: the status word (word 0) and the decoder feed's counts
     // (words 4-7) are published here by a kernel instead of copied (launch_publish_words).
@@ -190,8 +200,18 @@ struct gfs_sampler {
         if (h_words) {
             cudaFreeHost(h_words);
         }
-        if (h_fmt) {
-            cudaFreeHost(h_fmt);
+        for (WriteSlot &w : wslot) {
+            for (uint8_t *h : w.host) {
+                if (h) {
+                    cudaFreeHost(h);
+                }
+            }
+            if (w.formatted) {
+                cudaEventDestroy(w.formatted);
+            }
+            if (w.copied) {
+                cudaEventDestroy(w.copied);
+            }
         }
     }
 
