@@ -155,13 +155,14 @@ struct File {
 };
 
 // Shots per sampled chunk when writing files: about 256 MiB of rows or of file bytes (01 is eight times the rows),
-// and at most one resident wave of the frame kernel, so that consecutive chunks overlap well; a multiple of 128
-// shots (so of 64, as ptb64 needs).
+// and at most one resident wave of the frame kernel (or the sampler's chunk size, when one is set), so that
+// consecutive chunks overlap well; a multiple of 128 shots (so of 64, as ptb64 needs).
 uint64_t write_chunk(const gfs_sampler *s, uint64_t row_bytes, gfs::Format f, uint64_t nbits) {
     const uint64_t per_shot = std::max<uint64_t>(1, f == gfs::Format::F01 ? std::max(row_bytes, nbits + 1) : row_bytes);
     uint64_t c = ((uint64_t)256 << 20) / per_shot;
     const gfs::LaunchShape &sh = s->lean_active() ? s->shape_lean : s->shape;
-    c = std::min<uint64_t>(c, (uint64_t)std::max(1, sh.grid) * (uint64_t)std::max(1, sh.blocks_per_cta) * 128);
+    c = std::min<uint64_t>(c, s->chunk_shots ? s->chunk_shots
+                                             : (uint64_t)std::max(1, sh.grid) * (uint64_t)std::max(1, sh.blocks_per_cta) * 128);
     return std::max<uint64_t>(128, c & ~(uint64_t)127);
 }
 
@@ -314,19 +315,37 @@ void write_detections(gfs_sampler *s, uint64_t shots, const char *path, const ch
     for (uint64_t done = 0; done < shots; k++) {
         const uint64_t cs = std::min<uint64_t>(shots - done, chunk);
         gfs_sampler::WriteSlot &w = fw.slot(k);
-        w.rows.ensure(cs * drow, s->device);
-        if (obs_path) {
-            w.obs.ensure(cs * orow, s->device);
-        }
-        s->detections(cs, (flags & (GFS_PREPEND_OBSERVABLES | GFS_APPEND_OBSERVABLES)) | GFS_BIT_PACKED,
-                      (uint8_t *)w.rows.p, drow, obs_path ? (uint8_t *)w.obs.p : nullptr, orow, true);
-        // Prefixes as the reference names them: D then L when appended, L then D when prepended.
-        std::pair<const uint8_t *, uint64_t> part[2] = {
-            prepend ? format_rows(s, w.out[0], f, (const uint8_t *)w.rows.p, drow, cs, nd, 'L', 'D', O)
-                    : format_rows(s, w.out[0], f, (const uint8_t *)w.rows.p, drow, cs, nd, 'D', 'L', D),
-            {nullptr, 0}};
-        if (obs_path) {
-            part[1] = format_rows(s, w.out[1], of, (const uint8_t *)w.obs.p, orow, cs, O, 'L', 'L', O);
+        std::pair<const uint8_t *, uint64_t> part[2] = {{nullptr, 0}, {nullptr, 0}};
+        if (f == gfs::Format::PTB64 && (!obs_path || of == gfs::Format::PTB64)) {
+            // ptb64's words are halves of the frame kernel's detector-major rows: no shot-major rows needed.
+            s->detections_detmajor(cs);
+            const uint4 *dt = (const uint4 *)s->det_tmp.p, *ot = (const uint4 *)s->obs_tmp.p;
+            const uint64_t bytes = gfs::fixed_format_bytes(gfs::Format::PTB64, cs, nd);
+            w.out[0].ensure(std::max<uint64_t>(16, bytes), s->device);
+            ck(prepend  ? gfs::launch_ptb64_detmajor(ot, O, dt, D, cs, (uint8_t *)w.out[0].p, s->stream)
+               : append ? gfs::launch_ptb64_detmajor(dt, D, ot, O, cs, (uint8_t *)w.out[0].p, s->stream)
+                        : gfs::launch_ptb64_detmajor(dt, D, nullptr, 0, cs, (uint8_t *)w.out[0].p, s->stream),
+               "ptb64 kernel");
+            part[0] = {(const uint8_t *)w.out[0].p, bytes};
+            if (obs_path) {
+                const uint64_t obytes = gfs::fixed_format_bytes(gfs::Format::PTB64, cs, O);
+                w.out[1].ensure(std::max<uint64_t>(16, obytes), s->device);
+                ck(gfs::launch_ptb64_detmajor(ot, O, nullptr, 0, cs, (uint8_t *)w.out[1].p, s->stream), "ptb64 kernel");
+                part[1] = {(const uint8_t *)w.out[1].p, obytes};
+            }
+        } else {
+            w.rows.ensure(cs * drow, s->device);
+            if (obs_path) {
+                w.obs.ensure(cs * orow, s->device);
+            }
+            s->detections(cs, (flags & (GFS_PREPEND_OBSERVABLES | GFS_APPEND_OBSERVABLES)) | GFS_BIT_PACKED,
+                          (uint8_t *)w.rows.p, drow, obs_path ? (uint8_t *)w.obs.p : nullptr, orow, true);
+            // Prefixes as the reference names them: D then L when appended, L then D when prepended.
+            part[0] = prepend ? format_rows(s, w.out[0], f, (const uint8_t *)w.rows.p, drow, cs, nd, 'L', 'D', O)
+                              : format_rows(s, w.out[0], f, (const uint8_t *)w.rows.p, drow, cs, nd, 'D', 'L', D);
+            if (obs_path) {
+                part[1] = format_rows(s, w.out[1], of, (const uint8_t *)w.obs.p, orow, cs, O, 'L', 'L', O);
+            }
         }
         FILE *files[2] = {out.f, obs_out.f};
         fw.queue(w, part, files);

@@ -6,9 +6,10 @@
 // * 01: one thread per (shot, row byte) writes its eight characters; the last one of a row adds the newline.
 // * ptb64: one warp per (64-shot group, 32 bit positions); lane b gathers bit (32c + b) of the group's 64 rows
 //   into one little-endian 64-bit word.
-// * hits, dets, r8 (variable length): one warp per shot measures its record (lanes take contiguous ranges of the
-//   row so that the record's order is the lanes' order), an exclusive scan over shots places the records, and
-//   the same warp then writes its record, each lane at the offset its predecessors leave it.
+// * hits, dets, r8 (variable length): one warp per shot measures its record, walking the row in 128-byte windows
+//   (lane i on bytes 4i..4i+3, so the record's order is the lanes' order within a window), an exclusive scan over
+//   shots places the records, and the same warp then writes its record, each lane at the offset its predecessors
+//   leave it.
 #include <cstdint>
 
 #include "formats_device.h"
@@ -18,12 +19,16 @@ namespace gfs {
 namespace {
 
 __device__ __forceinline__ uint32_t ndigits(uint32_t v) {
-    uint32_t n = 1;
-    while (v >= 10) {
-        v /= 10;
-        n++;
-    }
-    return n;
+    return v < 10u ? 1u
+           : v < 100u ? 2u
+           : v < 1000u ? 3u
+           : v < 10000u ? 4u
+           : v < 100000u ? 5u
+           : v < 1000000u ? 6u
+           : v < 10000000u ? 7u
+           : v < 100000000u ? 8u
+           : v < 1000000000u ? 9u
+                             : 10u;
 }
 
 // Writes v in decimal at p (exactly ndigits(v) characters).
@@ -46,104 +51,54 @@ __device__ __forceinline__ uint32_t warp_excl_sum(uint32_t x, uint32_t lane) {
     return incl - x;
 }
 
-// Lane `lane`'s contiguous range of row bytes [b0, b1).
-__device__ __forceinline__ void lane_range(uint64_t nbytes, uint32_t lane, uint64_t *b0, uint64_t *b1) {
-    const uint64_t per = (nbytes + 31) / 32;
-    *b0 = min(nbytes, per * lane);
-    *b1 = min(nbytes, *b0 + per);
-}
-
-// Bytes this lane's part of the record takes (WRITE = false) or writes them at `out` (WRITE = true).  `prev` is
-// the row's last set bit before this lane's range (-1 for none), `mine` this lane's last set bit (-1 for none),
-// `hits_after` whether later lanes hold set bits, `row_empty` whether the row has none at all.
+// The record bytes of the set bits of `word` (bit t = row bit base + t), given the row's last set bit before it
+// (`prev`, -1 for none); WRITE also writes them at `o`.  hits: "k," per bit (the record's last ',' becomes its
+// newline afterwards); dets: " D<k>" / " L<k - transition>"; r8: the zeros since the previous set bit, a 255 for
+// each full run of 255.
 template <bool WRITE>
-__device__ __forceinline__ uint32_t lane_record(const FormatArgs &a, const uint8_t *row, uint64_t b0, uint64_t b1,
-                                                int64_t prev, int64_t mine, bool hits_after, bool row_empty,
-                                                bool first_lane, bool last_lane, uint8_t *out) {
+__device__ __forceinline__ uint32_t word_record(const FormatArgs &a, uint32_t word, uint32_t base, int32_t prev,
+                                                uint8_t *o) {
     uint32_t n = 0;
-    auto emit = [&](uint8_t c) {
-        if (WRITE) {
-            out[n] = c;
-        }
-        n++;
-    };
-    const uint32_t fmt = a.fmt;
-    if (fmt == (uint32_t)Format::DETS && first_lane) {
-        emit('s');
-        emit('h');
-        emit('o');
-        emit('t');
-    }
-    for (uint64_t j = b0; j < b1; j++) {
-        uint32_t byte = row[j];
-        if (8 * j + 8 > a.nbits) {
-            byte &= (1u << (a.nbits - 8 * j)) - 1u;
-        }
-        while (byte) {
-            const uint32_t t = __ffs(byte) - 1;
-            byte &= byte - 1;
-            const uint64_t k = 8 * j + t;
-            if (k >= a.nbits) {
-                break;
+    while (word) {
+        const uint32_t k = base + (uint32_t)(__ffs(word) - 1);
+        word &= word - 1;
+        if (a.fmt == (uint32_t)Format::HITS) {
+            const uint32_t nd = ndigits(k);
+            if (WRITE) {
+                put_dec(o + n, k, nd);
+                o[n + nd] = ',';
             }
-            if (fmt == (uint32_t)Format::HITS) {
-                const uint32_t nd = ndigits((uint32_t)k);
-                if (WRITE) {
-                    put_dec(out + n, (uint32_t)k, nd);
-                }
-                n += nd;
-                emit(((int64_t)k != mine || hits_after) ? ',' : '\n');  // ',' unless it is the row's last hit
-            } else if (fmt == (uint32_t)Format::DETS) {
-                const bool second = k >= a.transition;
-                const uint32_t idx = (uint32_t)(second ? k - a.transition : k);
-                emit(' ');
-                emit(second ? a.c2 : a.c1);
-                const uint32_t nd = ndigits(idx);
-                if (WRITE) {
-                    put_dec(out + n, idx, nd);
-                }
-                n += nd;
-            } else {  // R8: the zeros since the previous set bit, a 255 for each full run of 255
-                uint64_t z = (uint64_t)((int64_t)k - prev - 1);
-                while (z >= 255) {
-                    emit(255);
-                    z -= 255;
-                }
-                emit((uint8_t)z);
-                prev = (int64_t)k;
+            n += nd + 1;
+        } else if (a.fmt == (uint32_t)Format::DETS) {
+            const bool second = k >= a.transition;
+            const uint32_t idx = second ? k - (uint32_t)a.transition : k;
+            const uint32_t nd = ndigits(idx);
+            if (WRITE) {
+                o[n] = ' ';
+                o[n + 1] = second ? a.c2 : a.c1;
+                put_dec(o + n + 2, idx, nd);
             }
-        }
-    }
-    if (last_lane) {
-        if (fmt == (uint32_t)Format::R8) {
-            uint64_t z = (uint64_t)((int64_t)a.nbits - 1 - prev);
-            while (z >= 255) {
-                emit(255);
-                z -= 255;
+            n += nd + 2;
+        } else {
+            uint32_t z = k - (uint32_t)(prev + 1);
+            prev = (int32_t)k;
+            if (WRITE) {
+                for (; z >= 255; z -= 255) {
+                    o[n++] = 255;
+                }
+                o[n++] = (uint8_t)z;
+            } else {
+                n += z / 255 + 1;
             }
-            emit((uint8_t)z);
-        } else if (fmt == (uint32_t)Format::DETS || (fmt == (uint32_t)Format::HITS && row_empty)) {
-            emit('\n');
         }
     }
     return n;
 }
 
-// The last set bit of the row in bytes [b0, b1), or -1.
-__device__ __forceinline__ int64_t lane_last_bit(const FormatArgs &a, const uint8_t *row, uint64_t b0, uint64_t b1) {
-    for (uint64_t j = b1; j-- > b0;) {
-        uint32_t byte = row[j];
-        if (8 * j + 8 > a.nbits) {
-            byte &= (1u << (a.nbits - 8 * j)) - 1u;  // padding bits past the row's last bit
-        }
-        if (byte) {
-            return (int64_t)(8 * j + (31 - __clz(byte)));
-        }
-    }
-    return -1;
-}
-
-// One warp per shot: WRITE = false stores the record length, WRITE = true writes the record at offs[shot].
+// One warp per shot: WRITE = false stores the record length, WRITE = true writes the record at offs[shot].  The
+// warp walks the row in windows of 128 bytes, lane i on bytes [4i, 4i + 4) of each (coalesced loads); a lane's
+// part of the record goes where the lanes before it, and the earlier windows, leave off (warp prefix sums), and
+// the row's last set bit before each lane comes from a warp max-scan carried across windows (r8's run lengths).
 template <bool WRITE>
 __global__ void __launch_bounds__(256) fmt_record_kernel(const FormatArgs a) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -152,41 +107,80 @@ __global__ void __launch_bounds__(256) fmt_record_kernel(const FormatArgs a) {
         return;
     }
     const uint8_t *row = a.rows + shot * a.stride;
-    const uint64_t nbytes = (a.nbits + 7) / 8;
-    uint64_t b0, b1;
-    lane_range(nbytes, lane, &b0, &b1);
-    // The previous set bit before this lane's range (r8) and whether later lanes hold hits (hits).
-    const int64_t mine = lane_last_bit(a, row, b0, b1);
-    int64_t prev = -1;
-    {
-        int64_t incl = mine;
+    const uint32_t nbits = (uint32_t)a.nbits, nbytes = (nbits + 7) / 8;
+    uint8_t *const out = WRITE ? a.out + a.offs[shot] : nullptr;
+    uint32_t pos = 0;   // record bytes so far
+    int32_t carry = -1;  // the row's last set bit before the current window
+    if (a.fmt == (uint32_t)Format::DETS) {
+        if (WRITE && lane < 4) {
+            out[lane] = (uint8_t)"shot"[lane];
+        }
+        pos = 4;
+    }
+    for (uint32_t w0 = 0; w0 < nbytes; w0 += 128) {
+        const uint32_t b = w0 + 4 * lane, base = 8 * b;
+        uint32_t word = 0;
+#pragma unroll
+        for (uint32_t t = 0; t < 4; t++) {
+            if (b + t < nbytes) {
+                word |= (uint32_t)row[b + t] << (8 * t);
+            }
+        }
+        if (base >= nbits) {
+            word = 0;
+        } else if (nbits - base < 32) {
+            word &= (1u << (nbits - base)) - 1u;  // padding bits past the row's last bit
+        }
+        const int32_t mine = word ? (int32_t)(base + 31 - __clz(word)) : -1;
+        int32_t incl = mine;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            const int64_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            const int32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
             if (lane >= (uint32_t)d && y > incl) {
                 incl = y;
             }
         }
-        prev = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
-        if (lane == 0) {
-            prev = -1;
+        int32_t before = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
+        if (lane == 0 || before < carry) {
+            before = carry;
+        }
+        const uint32_t n = word_record<false>(a, word, base, before, nullptr);
+        const uint32_t at = warp_excl_sum(n, lane);
+        if (WRITE && n) {
+            word_record<true>(a, word, base, before, out + pos + at);
+        }
+        pos += __shfl_sync(0xFFFFFFFFu, at + n, 31);
+        const int32_t last = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        if (last > carry) {
+            carry = last;
         }
     }
-    const uint32_t any_mask = __ballot_sync(0xFFFFFFFFu, mine >= 0);
-    const bool hits_after = lane < 31 && (any_mask >> (lane + 1)) != 0;
-    const bool row_empty = any_mask == 0;
-    const uint32_t n = lane_record<false>(a, row, b0, b1, prev, mine, hits_after, row_empty, lane == 0, lane == 31,
-                                          nullptr);
-    if (!WRITE) {
-        const uint32_t total = __reduce_add_sync(0xFFFFFFFFu, n);
-        if (lane == 0) {
-            a.lens[shot] = total;
+    // The record's end: r8's final run, dets' newline, hits' newline (in place of the last ',').
+    uint32_t tail = 0;
+    if (a.fmt == (uint32_t)Format::R8) {
+        uint32_t z = nbits - 1 - (uint32_t)carry;  // carry = -1 gives nbits zeros
+        tail = z / 255 + 1;
+        if (WRITE && lane == 0) {
+            uint8_t *o = out + pos;
+            for (; z >= 255; z -= 255) {
+                *o++ = 255;
+            }
+            *o = (uint8_t)z;
         }
-        return;
+    } else if (a.fmt == (uint32_t)Format::DETS || carry < 0) {
+        tail = 1;
+        if (WRITE && lane == 0) {
+            out[pos] = '\n';
+        }
+    } else {
+        __syncwarp();  // the ',' written by whichever lane held the row's last hit
+        if (WRITE && lane == 0) {
+            out[pos - 1] = '\n';
+        }
     }
-    const uint32_t at = warp_excl_sum(n, lane);
-    lane_record<true>(a, row, b0, b1, prev, mine, hits_after, row_empty, lane == 0, lane == 31,
-                      a.out + a.offs[shot] + at);
+    if (!WRITE && lane == 0) {
+        a.lens[shot] = pos + tail;
+    }
 }
 
 __global__ void __launch_bounds__(256) fmt_01_kernel(const FormatArgs a) {
@@ -224,6 +218,26 @@ __global__ void __launch_bounds__(256) fmt_ptb64_kernel(const FormatArgs a) {
     }
     if (m < a.nbits) {
         reinterpret_cast<unsigned long long *>(a.out)[g * a.nbits + m] = word;
+    }
+}
+
+// ptb64 straight from detector-major rows ([128-shot block][row] uint4, bit j of 32-bit word q = shot 32q + j): a
+// 64-shot group's word for a bit is half of that bit's 16-byte row, so one thread per (block, bit) writes the
+// words of the block's two groups; bits [0, n1) come from `first`, [n1, n1 + n2) from `second`.
+__global__ void __launch_bounds__(256) fmt_ptb64_detmajor_kernel(const uint4 *first, uint64_t n1, const uint4 *second,
+                                                                 uint64_t n2, uint64_t shots, uint8_t *out) {
+    const uint64_t nbits = n1 + n2;
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t blocks = (shots + 127) / 128;
+    if (i >= blocks * nbits) {
+        return;
+    }
+    const uint64_t b = i / nbits, m = i % nbits;
+    const uint4 v = m < n1 ? first[b * n1 + m] : second[b * n2 + (m - n1)];
+    unsigned long long *o = reinterpret_cast<unsigned long long *>(out);
+    o[(2 * b) * nbits + m] = (unsigned long long)v.x | ((unsigned long long)v.y << 32);
+    if ((2 * b + 1) * 64 < shots) {
+        o[(2 * b + 1) * nbits + m] = (unsigned long long)v.z | ((unsigned long long)v.w << 32);
     }
 }
 
@@ -345,9 +359,25 @@ uint64_t fixed_format_bytes(Format f, uint64_t shots, uint64_t nbits) {
     }
 }
 
+cudaError_t launch_ptb64_detmajor(const uint4 *first, uint64_t n1, const uint4 *second, uint64_t n2, uint64_t shots,
+                                  uint8_t *out, cudaStream_t stream) {
+    const uint64_t n = (shots + 127) / 128 * (n1 + n2);
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    if (shots % 64 != 0 || (n + 255) / 256 > 0x7FFFFFFFull) {
+        return cudaErrorInvalidValue;
+    }
+    fmt_ptb64_detmajor_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(first, n1, second, n2, shots, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_format_lengths(const FormatArgs &a, uint64_t *block_sums, uint64_t *total, cudaStream_t stream) {
     if (a.shots == 0) {
         return cudaSuccess;
+    }
+    if (a.nbits >= (1ull << 31)) {  // bit indices are 32-bit in the record kernel
+        return cudaErrorInvalidValue;
     }
     const uint64_t warps_blocks = (a.shots + 7) / 8;
     if (warps_blocks > 0x7FFFFFFFull) {

@@ -28,6 +28,10 @@ uint64_t fixed_format_bytes(Format f, uint64_t shots, uint64_t nbits);
 // hits / dets / r8: record lengths and offsets; *total (device) receives the bytes of all records.
 // block_sums needs (shots + 1024) / 1024 entries.
 cudaError_t launch_format_lengths(const FormatArgs &a, uint64_t *block_sums, uint64_t *total, cudaStream_t stream);
+// ptb64 file bytes of `shots` shots (a multiple of 64) from detector-major rows: `first` holds n1 rows and
+// `second` n2 rows per 128-shot block ([block][row] uint4); the file's bits are first's rows, then second's.
+cudaError_t launch_ptb64_detmajor(const uint4 *first, uint64_t n1, const uint4 *second, uint64_t n2, uint64_t shots,
+                                  uint8_t *out, cudaStream_t stream);
 // Writes the file bytes (01, ptb64, or hits / dets / r8 after launch_format_lengths).
 cudaError_t launch_format_write(const FormatArgs &a, cudaStream_t stream);
 

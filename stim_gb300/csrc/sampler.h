@@ -804,6 +804,37 @@ struct gfs_sampler {
         }
     }
 
+    // Samples `shots` detection-event shots (at most one chunk) and leaves them detector-major in det_tmp / obs_tmp
+    // ([128-shot block][detector] and [block][observable] uint4 rows), without the shot-major transpose, for
+    // consumers that read that layout (ptb64 files).  An overflowed hit list redoes the chunk with inline noise.
+    void detections_detmajor(uint64_t shots) {
+        if (mode != GFS_MODE_DETECTIONS) {
+            throw std::invalid_argument("sampler was not created in detection mode");
+        }
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        reset_timings();
+        const uint64_t nblk = (shots + 127) / 128;
+        ck(cudaEventRecord(ev[0], stream), "event");
+        run_frame(nblk, next_block);
+        ck(cudaEventRecord(ev[1], stream), "event");
+        ck(cudaStreamSynchronize(stream), "sample");
+        t_frame = elapsed(0, 1) - account_noise(-1);
+        if (check_status()) {
+            force_inline = true;
+            try {
+                run_frame(nblk, next_block);
+                ck(cudaStreamSynchronize(stream), "sample");
+            } catch (...) {
+                force_inline = false;
+                throw;
+            }
+            force_inline = false;
+            check_status();
+        }
+        next_block += nblk;
+        t_total = t_frame + t_noise;
+    }
+
     // Shared driver for detections (host or device destinations).
     void detections(uint64_t shots, uint32_t flags, uint8_t *dets, uint64_t dstride, uint8_t *obs, uint64_t ostride,
                     bool device_out) {

@@ -136,3 +136,36 @@ def test_device_formatted_files_equal_host_writer_at_scale(fmt, family, d, p, sh
     mref = tmp_path / "mhost"
     stim_gb300.write_shot_data_file(data=m, path=str(mref), format=fmt, num_measurements=M)
     assert open(mout, "rb").read() == open(mref, "rb").read()
+
+
+@pytest.mark.parametrize("fmt", ["01", "b8", "r8", "hits", "dets", "ptb64"])
+@pytest.mark.parametrize("layout", ["append", "prepend", "obs"])
+def test_pipelined_chunks_equal_host_writer(fmt, layout, tmp_path):
+    # Many small chunks through the two-slot file pipeline (and, for ptb64, the detector-major path), with every
+    # observable layout, against the host writer on the same bits.
+    from stim_gb300 import workloads
+
+    if layout == "prepend" and fmt == "dets":
+        pytest.skip("dets names prepended observables L0.. first; the host writer names row bits D then L")
+    c = stim_gb300.Circuit(workloads.code_circuit("surface_code:rotated_memory_z", 7, 7, 0.01))
+    D, O = c.num_detectors, c.num_observables
+    shots = 9 * 1024 + 64
+    s = c.compile_detector_sampler(seed=11)
+    s.set_chunk_shots(1024)
+    out = tmp_path / "dev"
+    if layout == "obs":
+        obs = tmp_path / "obs"
+        s.sample_write(shots, filepath=str(out), format=fmt, obs_out_filepath=str(obs), obs_out_format=fmt)
+        d, o = c.compile_detector_sampler(seed=11).sample(shots, bit_packed=True, separate_observables=True)
+        stim_gb300.write_shot_data_file(data=d, path=str(tmp_path / "h"), format=fmt, num_detectors=D)
+        stim_gb300.write_shot_data_file(data=o, path=str(tmp_path / "ho"), format=fmt, num_observables=O)
+        assert open(obs, "rb").read() == open(tmp_path / "ho", "rb").read()
+    else:
+        s.sample_write(shots, filepath=str(out), format=fmt, append_observables=layout == "append",
+                       prepend_observables=layout == "prepend")
+        bits = c.compile_detector_sampler(seed=11).sample(shots, bit_packed=True,
+                                                          append_observables=layout == "append",
+                                                          prepend_observables=layout == "prepend")
+        stim_gb300.write_shot_data_file(data=bits, path=str(tmp_path / "h"), format=fmt, num_detectors=D,
+                                        num_observables=O)
+    assert open(out, "rb").read() == open(tmp_path / "h", "rb").read()
