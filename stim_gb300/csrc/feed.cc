@@ -56,7 +56,7 @@ void sample_for_decoder(gfs_sampler *s, uint64_t shots, const uint8_t *mask, uin
     const uint64_t dbytes = up256(chunk * drow), obytes = up256(chunk * orow);
     const uint64_t aux_counts = 0, aux_groups = 256, aux_keep = aux_groups + up256(4 * groups),
                    aux_idx = aux_keep + up256(chunk), aux_bits = aux_idx + up256(4 * (uint64_t)nmask),
-                   aux_total = aux_bits + up256(nmask);
+                   aux_dst = aux_bits + up256(nmask), aux_total = aux_dst + up256(4 * chunk);
     gfs::FeedArgs args[2];
     for (int k = 0; k < 2; k++) {
         s->feed_rows[k].ensure(std::max<uint64_t>(256, dbytes + obytes), s->device);
@@ -86,6 +86,7 @@ void sample_for_decoder(gfs_sampler *s, uint64_t shots, const uint8_t *mask, uin
         a.counts = (unsigned long long *)(aux + aux_counts);
         a.cdets = crows;
         a.cobs = crows ? crows + dbytes : nullptr;
+        a.dst = (uint32_t *)(aux + aux_dst);
     }
     ck(cudaStreamSynchronize(s->stream), "mask upload");
     // Two slots: chunk n samples into slot n % 2 while the kept rows of chunk n - 1 leave on the copy stream (with

@@ -1876,30 +1876,26 @@ __global__ void __launch_bounds__(256) feed_popcount_kernel(const uint8_t *p, ui
     }
 }
 
-// One warp per shot: lanes test the mask's bytes; the group's kept count goes to group_kept.
+// One warp per shot, eight shots (of one group) per CTA: lanes test the mask's bytes; the CTA adds its kept shots
+// to its group's count in group_kept (zeroed by the launcher).  feed_scan_kernel derives the dropped count.
 __global__ void __launch_bounds__(256) feed_flags_kernel(const FeedArgs a) {
     __shared__ uint32_t kept_warp[8];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint64_t s0 = (uint64_t)blockIdx.x * kFeedGroup;
-    uint32_t kept = 0;
-    for (uint32_t i = warp; i < kFeedGroup; i += 8) {
-        const uint64_t s = s0 + i;
-        if (s >= a.nshots) {
-            break;
-        }
+    const uint64_t s0 = (uint64_t)blockIdx.x * 8, s = s0 + warp;
+    uint32_t keep = 0;
+    if (s < a.nshots) {
         const uint8_t *row = a.dets + s * a.drow;
         uint32_t hit = 0;
         for (uint32_t k = lane; k < a.nmask; k += 32) {
             hit |= row[a.mask_idx[k]] & a.mask_bits[k];
         }
-        const uint32_t keep = __any_sync(0xFFFFFFFFu, hit != 0) ? 0u : 1u;
+        keep = __any_sync(0xFFFFFFFFu, hit != 0) ? 0u : 1u;
         if (lane == 0) {
             a.keep[s] = (uint8_t)keep;
         }
-        kept += keep;
     }
     if (lane == 0) {
-        kept_warp[warp] = kept;
+        kept_warp[warp] = keep;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1907,11 +1903,8 @@ __global__ void __launch_bounds__(256) feed_flags_kernel(const FeedArgs a) {
         for (int w = 0; w < 8; w++) {
             t += kept_warp[w];
         }
-        a.group_kept[blockIdx.x] = t;
-        const uint64_t left = a.nshots - s0;
-        const uint32_t n = left < kFeedGroup ? (uint32_t)left : kFeedGroup;
-        if (n > t) {
-            atomicAdd(&a.counts[1], (unsigned long long)(n - t));
+        if (t) {
+            atomicAdd(&a.group_kept[s0 / kFeedGroup], t);
         }
     }
 }
@@ -1928,7 +1921,10 @@ __device__ __forceinline__ uint32_t warp_inclusive_sum(uint32_t x, uint32_t lane
 }
 
 // Exclusive prefix sum of the groups' kept counts, in place: one CTA walks tiles of 1024 with a carry.
-__global__ void __launch_bounds__(1024) feed_scan_kernel(uint32_t *v, uint32_t n) {
+// Exclusive scan of the groups' kept counts in place; the shots the scan does not cover were dropped, and their
+// number goes to dropped[0].
+__global__ void __launch_bounds__(1024) feed_scan_kernel(uint32_t *v, uint32_t n, uint64_t nshots,
+                                                         unsigned long long *dropped) {
     __shared__ uint32_t wsum[32];
     __shared__ uint32_t carry_s;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1959,6 +1955,9 @@ __global__ void __launch_bounds__(1024) feed_scan_kernel(uint32_t *v, uint32_t n
         }
         __syncthreads();
     }
+    if (threadIdx.x == 0) {
+        dropped[0] = (unsigned long long)(nshots - carry_s);
+    }
 }
 
 // Copies n bytes with the widest unit dividing n (both rows start at multiples of n from 256-byte aligned
@@ -1988,9 +1987,8 @@ __device__ __forceinline__ void feed_copy_row(uint8_t *dst, const uint8_t *src, 
 }
 
 // Kept shots of a group get consecutive output rows from the group's scanned start: thread t ranks shots
-// 4t .. 4t + 3, then one warp per kept shot copies its detector and observable rows.
-__global__ void __launch_bounds__(256) feed_compact_kernel(const FeedArgs a) {
-    __shared__ uint32_t dst[kFeedGroup];
+// 4t .. 4t + 3 and writes each shot's output row (or 0xFFFFFFFF) to dst.
+__global__ void __launch_bounds__(256) feed_rank_kernel(const FeedArgs a) {
     __shared__ uint32_t wsum[8];
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint64_t s0 = (uint64_t)blockIdx.x * kFeedGroup;
@@ -2013,20 +2011,29 @@ __global__ void __launch_bounds__(256) feed_compact_kernel(const FeedArgs a) {
     uint32_t pos = a.group_kept[blockIdx.x] + before + inc - c;
 #pragma unroll
     for (uint32_t j = 0; j < 4; j++) {
-        dst[4 * tid + j] = k[j] ? pos : 0xFFFFFFFFu;
+        const uint64_t s = s0 + 4 * tid + j;
+        if (s < a.nshots) {
+            a.dst[s] = k[j] ? pos : 0xFFFFFFFFu;
+        }
         pos += k[j];
     }
-    __syncthreads();
-    for (uint32_t i = warp; i < kFeedGroup; i += 8) {
-        const uint32_t r = dst[i];
-        if (r == 0xFFFFFFFFu) {
-            continue;
-        }
-        const uint64_t s = s0 + i;
-        feed_copy_row(a.cdets + (uint64_t)r * a.drow, a.dets + s * a.drow, a.drow, lane);
-        if (a.orow) {
-            feed_copy_row(a.cobs + (uint64_t)r * a.orow, a.obs + s * a.orow, a.orow, lane);
-        }
+}
+
+// One warp per shot copies a kept shot's detector and observable rows to its output row; eight shots per CTA,
+// so the copy runs with the whole GPU's warps in flight.
+__global__ void __launch_bounds__(256) feed_gather_kernel(const FeedArgs a) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t s = (uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (s >= a.nshots) {
+        return;
+    }
+    const uint32_t r = a.dst[s];
+    if (r == 0xFFFFFFFFu) {
+        return;
+    }
+    feed_copy_row(a.cdets + (uint64_t)r * a.drow, a.dets + s * a.drow, a.drow, lane);
+    if (a.orow) {
+        feed_copy_row(a.cobs + (uint64_t)r * a.orow, a.obs + s * a.orow, a.orow, lane);
     }
 }
 
@@ -2060,7 +2067,15 @@ cudaError_t launch_feed_flags(const FeedArgs &args, cudaStream_t stream) {
     if (groups > 0x7FFFFFFFull) {
         return cudaErrorInvalidValue;
     }
-    feed_flags_kernel<<<(unsigned)groups, 256, 0, stream>>>(args);
+    const uint64_t blocks = (args.nshots + 7) / 8;
+    if (blocks > 0x7FFFFFFFull) {
+        return cudaErrorInvalidValue;
+    }
+    cudaError_t e = cudaMemsetAsync(args.group_kept, 0, groups * sizeof(uint32_t), stream);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    feed_flags_kernel<<<(unsigned)blocks, 256, 0, stream>>>(args);
     return cudaGetLastError();
 }
 
@@ -2072,7 +2087,7 @@ cudaError_t launch_feed_scan(const FeedArgs &args, cudaStream_t stream) {
     if (groups > 0xFFFFFFFFull) {
         return cudaErrorInvalidValue;
     }
-    feed_scan_kernel<<<1, 1024, 0, stream>>>(args.group_kept, (uint32_t)groups);
+    feed_scan_kernel<<<1, 1024, 0, stream>>>(args.group_kept, (uint32_t)groups, args.nshots, args.counts + 1);
     return cudaGetLastError();
 }
 
@@ -2084,7 +2099,12 @@ cudaError_t launch_feed_compact(const FeedArgs &args, cudaStream_t stream) {
     if (groups > 0x7FFFFFFFull) {
         return cudaErrorInvalidValue;
     }
-    feed_compact_kernel<<<(unsigned)groups, 256, 0, stream>>>(args);
+    feed_rank_kernel<<<(unsigned)groups, 256, 0, stream>>>(args);
+    const uint64_t blocks = (args.nshots + 7) / 8;
+    if (blocks > 0x7FFFFFFFull) {
+        return cudaErrorInvalidValue;
+    }
+    feed_gather_kernel<<<(unsigned)blocks, 256, 0, stream>>>(args);
     return cudaGetLastError();
 }
 

@@ -211,6 +211,7 @@ struct FeedArgs {
     uint8_t *keep;                // per shot: 1 kept, 0 dropped
     unsigned long long *counts;   // [0] += set bits over the detector rows, [1] += dropped shots
     uint8_t *cdets, *cobs;        // kept rows, in shot order
+    uint32_t *dst;                // per shot: its kept row's index, or 0xFFFFFFFF when dropped
 };
 // Copies n words of device memory to `dst`, a mapped page-locked host buffer, with a kernel: small results reach
 // the host without a device-to-host copy, which could queue behind a large copy on the copy engine.
