@@ -99,6 +99,25 @@ def algorithmic_work(text):
     return acc, rbits, hits
 
 
+def e2e_tail(times, parts):
+    """Where the slow end-to-end calls (over 1.15x the median) spend their time: the sampler's own CUDA-event split
+    of each call into kernels and the rest (device->host copies and the gaps between them)."""
+    if not times:
+        return None
+    med = statistics.median(times)
+    slow = [k for k, t in enumerate(times) if t > 1.15 * med]
+    fast = [k for k in range(len(times)) if k not in set(slow)]
+
+    def split(ks):
+        if not ks:
+            return None
+        kern = statistics.mean(parts[k]["frame_ms"] + parts[k]["noise_ms"] + parts[k]["transpose_ms"] for k in ks)
+        return {"kernels_ms": kern, "copy_ms": statistics.mean(parts[k]["copy_ms"] for k in ks),
+                "wall_ms": 1e3 * statistics.mean(times[k] for k in ks)}
+
+    return {"slow_calls": len(slow), "slow_call_indices": slow[:16], "slow": split(slow), "typical": split(fast)}
+
+
 def _nearest_rank(values, q):
     """The q-quantile of `values` by the nearest-rank rule (the ceil(q * n)-th smallest)."""
     xs = sorted(values)
@@ -595,7 +614,8 @@ def run_gpu(args):
                     "link_bound_ms": 1e3 * shots * (drow + orow) / (link["d2h_gbs"] * 1e9),
                     "device_ms": {k: statistics.mean(p[k] for p in e2e_parts) for k in
                                   ("frame_ms", "noise_ms", "transpose_ms", "copy_ms", "total_ms")}
-                    if e2e_parts else None},
+                    if e2e_parts else None,
+                    "tail": e2e_tail(e2e_times, e2e_parts)},
             "gpu_launches": launches,
             "roofline": {"bound": "smem", "achieved": achieved_gbs, "peak": smem_peak, "unit": "GB/s",
                          "frac": achieved_gbs / smem_peak,
