@@ -223,11 +223,11 @@ __device__ __forceinline__ uint64_t occ_record(const KernelArgs &p, const OccPar
 }
 
 // One warp draws the hit records of one (slice, occurrence).  Screening rounds are dense: each lane draws
-// the first Philox group of one segment, and the ~60% of segments (at p = 1e-3) whose first draw leaves the
-// segment are done.  Segments with a hit are queued in shared memory with their three unused draws.  Lanes
+// the first Philox group of one segment, and the segments whose first draw leaves the segment (13% of them at
+// p = 1e-3 with 2,048 trials) are done.  Segments with a hit are queued in shared memory with their three unused draws.  Lanes
 // then walk queued segments hit by hit, exactly as gfs_next_hit would (same draws, same order); a lane whose
 // segment ends takes the next queued one at once, and a new screening round runs whenever the queue can no
-// longer refill the warp.  Every step each lane with a pending hit writes one record; the records of a step
+// longer refill the warp.  Every step each lane with a pending hit writes up to two records; the records of a step
 // get consecutive slots (ballot prefix), so the stores coalesce and no atomics are needed.  No barriers:
 // occurrences and slices are independent streams.
 struct NoiseQueued {
@@ -339,15 +339,26 @@ __device__ __forceinline__ void noise_records(const KernelArgs &p, uint32_t slic
             }
             continue;
         }
-        // One hit per active lane, each into its own slice's region: the lanes of one slice take consecutive
-        // places after the slice's count, which their first lane advances once.
+        // Up to two hits per active lane (the walk's next two), each lane's records into its own slice's region: the
+        // lanes of one slice take consecutive places after the slice's count, which their first lane advances once.
+        // Two per step halve the warp-level bookkeeping per hit (ballots, queue and screening checks, routing);
+        // three or four per step cost more in code size and registers than they save.
         if (active) {
+            const uint64_t r1 = occ_record(p, o, u0 + ((uint32_t)pos >> 7), blk, (uint32_t)pos & 127u, &st);
+            pos = gfs_next_hit(&st, T, ch.inv_c, pos, trials, always);
+            const bool two = pos >= 0;
+            uint64_t r2 = 0;
+            if (two) {
+                r2 = occ_record(p, o, u0 + ((uint32_t)pos >> 7), blk, (uint32_t)pos & 127u, &st);
+                pos = gfs_next_hit(&st, T, ch.inv_c, pos, trials, always);
+            }
+            const uint32_t sec = __ballot_sync(act, two);  // lanes with a second record
             uint32_t at;
             if (SB == 1) {
-                at = count[0] + __popc(act & lt);
+                at = count[0] + __popc(act & lt) + __popc(sec & lt);
                 __syncwarp(act);
                 if (lane == (uint32_t)(__ffs(act) - 1)) {
-                    count[0] += __popc(act);
+                    count[0] += __popc(act) + __popc(sec);
                 }
             } else {
                 const uint32_t peers = __match_any_sync(act, sub);
@@ -355,15 +366,17 @@ __device__ __forceinline__ void noise_records(const KernelArgs &p, uint32_t slic
                 uint32_t base = 0;
                 if (lane == leader) {
                     base = count[sub];
-                    count[sub] = base + __popc(peers);
+                    count[sub] = base + __popc(peers) + __popc(peers & sec);
                 }
-                at = __shfl_sync(act, base, leader) + __popc(peers & lt);
+                at = __shfl_sync(act, base, leader) + __popc(peers & lt) + __popc(peers & sec & lt);
             }
-            const uint64_t r = occ_record(p, o, u0 + ((uint32_t)pos >> 7), blk, (uint32_t)pos & 127u, &st);
+            uint64_t *const region = p.hits + (uint64_t)(slice0 + sub) * p.slice_cap + oc.off;
             if (at < oc.cap) {
-                p.hits[(uint64_t)(slice0 + sub) * p.slice_cap + oc.off + at] = r;
+                region[at] = r1;
             }
-            pos = gfs_next_hit(&st, T, ch.inv_c, pos, trials, always);
+            if (two && at + 1 < oc.cap) {
+                region[at + 1] = r2;
+            }
             active = pos >= 0;
         }
         __syncwarp();
