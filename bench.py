@@ -35,8 +35,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "detection-event Gbit/s at d=25 r=25 (surface_code:rotated_memory_z, p=1e-3)"
 # DRAM bytes per shot of the frame kernel on this workload, dram__bytes_read.sum + dram__bytes_write.sum from
-# one ncu capture of 131,072 shots (hit-list mode, 1 block x 128 threads per CTA); traffic grows with shots.
-FRAME_DRAM_BYTES_PER_SHOT = 2855.0
+# one ncu capture of 131,072 shots (lean frame kernel, hit-list mode, 1 block x 128 threads per CTA: 155.93 +
+# 218.82 MB); traffic grows with shots.
+FRAME_DRAM_BYTES_PER_SHOT = 2859.1
 UNIT = "Gbit/s"
 E2E_WARMUP = 3
 WORKLOAD = dict(family="surface_code:rotated_memory_z", distance=25, rounds=25, p=0.001)
