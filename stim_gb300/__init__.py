@@ -177,6 +177,13 @@ class Circuit:
                                                               device=device)
 
 
+def _circuit_repr(c) -> str:
+    """The circuit as a Python expression: its lines, stripped and indented by four spaces, in a triple-quoted
+    literal (the layout of the reference's circuit_repr)."""
+    body = "".join(f"    {ln.strip()}\n" for ln in str(c).splitlines() if ln.strip())
+    return "stim_gb300.Circuit('''\n" + body + "''')"
+
+
 class _SamplerBase:
     _mode = None
 
@@ -282,6 +289,15 @@ class CompiledDetectorSampler(_SamplerBase):
     def __init__(self, circuit, *, seed=None, device: int = 0):
         super().__init__(circuit, seed, device)
 
+    def __repr__(self):
+        # As the reference's CompiledDetectorSampler.repr (compiled_detector_sampler.pybind.cc:143-149).
+        return f"stim_gb300.CompiledDetectorSampler({_circuit_repr(self._circuit)})"
+
+    def sample_bit_packed(self, shots: int, *, prepend_observables: bool = False, append_observables: bool = False):
+        """Deprecated in the reference: sample(shots, bit_packed=True, ...) (compiled_detector_sampler.pybind.cc:324-356)."""
+        return self.sample(shots, prepend_observables=prepend_observables, append_observables=append_observables,
+                           bit_packed=True)
+
     def sample(self, shots: int, *, prepend_observables: bool = False, append_observables: bool = False,
                separate_observables: bool = False, bit_packed: bool = False, dets_out=None, obs_out=None):
         if separate_observables and (append_observables or prepend_observables):
@@ -377,6 +393,7 @@ class CompiledMeasurementSampler(_SamplerBase):
                  device: int = 0):
         super().__init__(circuit, seed, device)
         M = self._circuit.num_measurements
+        self._skip = bool(skip_reference_sample)
         if reference_sample is not None:
             if skip_reference_sample:
                 raise ValueError("skip_reference_sample = True but reference_sample is not None.")
@@ -395,6 +412,15 @@ class CompiledMeasurementSampler(_SamplerBase):
             self._ref = None
         else:
             self._ref = self._circuit.reference_sample(bit_packed=True)
+
+    def __repr__(self):
+        # As the reference's CompiledMeasurementSampler.repr (compiled_measurement_sampler.pybind.cc:47-56).
+        skip = ", skip_reference_sample=True" if self._skip else ""
+        return f"stim_gb300.CompiledMeasurementSampler({_circuit_repr(self._circuit)}{skip})"
+
+    def sample_bit_packed(self, shots: int):
+        """Deprecated in the reference: sample(shots, bit_packed=True) (compiled_measurement_sampler.pybind.cc:210-241)."""
+        return self.sample(shots, bit_packed=True)
 
     def sample_write(self, shots: int, *, filepath, format: str = "01") -> None:
         """Samples measurements and writes them to a file in a result format ("01", "b8", "r8", "hits",
