@@ -17,6 +17,8 @@ unstable across versions and machines).
 
 import ctypes
 import os
+import shutil
+import tempfile
 
 import numpy as np
 
@@ -628,6 +630,45 @@ class CompiledDemSampler:
             obs_user[...] = obs
             obs = obs_user
         return dets, obs, errs
+
+    def sample_write(self, shots: int, *, det_out_file, det_out_format: str = "01", obs_out_file,
+                     obs_out_format: str = "01", err_out_file=None, err_out_format: str = "01",
+                     replay_err_in_file=None, replay_err_in_format: str = "01") -> None:
+        """As the reference's DemSampler.sample_write (dem_sampler.pybind.cc:274-380, dem_sampler.inl:75-130):
+        detection events (D<k>), observable flips (L<k>) and the sampled errors (M<k>) to files (None: not
+        written), optionally replaying errors read from a file.  Works in chunks of shots, each written after the
+        previous one, so memory stays bounded whatever the shot count."""
+        shots = int(shots)
+        if shots < 0:
+            raise ValueError("shots must be non-negative")
+        D, O, E = self.num_detectors, self.num_observables, self.num_errors
+        replay = None
+        if replay_err_in_file is not None:
+            replay = read_shot_data_file(path=replay_err_in_file, format=replay_err_in_format, num_measurements=E,
+                                         bit_packed=True)
+            if replay.shape[0] < shots:
+                raise ValueError("Expected more error data for the requested number of shots.")
+        outs = [(det_out_file, det_out_format, dict(num_detectors=D)),
+                (obs_out_file, obs_out_format, dict(num_observables=O)),
+                (err_out_file, err_out_format, dict(num_measurements=E))]
+        if any(f is not None and str(fmt) == "ptb64" for f, fmt, _ in outs) and shots % 64:
+            raise ValueError("shots must be a multiple of 64 to use ptb64 format.")
+        for f, _, _ in outs:
+            if f is not None:
+                open(os.fspath(f), "wb").close()
+        chunk = max(64, min(1 << 20, ((256 << 23) // max(1, D + O + E)) // 64 * 64))
+        with tempfile.TemporaryDirectory() as tmp:
+            part = os.path.join(tmp, "part")
+            for done in range(0, shots, chunk):
+                cs = min(chunk, shots - done)
+                d, o, e = self.sample(cs, bit_packed=True, return_errors=err_out_file is not None,
+                                      recorded_errors_to_replay=None if replay is None else replay[done:done + cs])
+                for (f, fmt, counts), data in zip(outs, (d, o, e)):
+                    if f is None:
+                        continue
+                    write_shot_data_file(data=data, path=part, format=fmt, **counts)
+                    with open(part, "rb") as src, open(os.fspath(f), "ab") as dst:
+                        shutil.copyfileobj(src, dst)
 
 
 class BatchSampler:
