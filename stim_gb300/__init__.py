@@ -485,10 +485,12 @@ class CompiledMeasurementsToDetectionEventsConverter:
         raise ValueError(f"{what} must be a numpy array of bool or of bit packed uint8")
 
     def convert(self, *, measurements, sweep_bits=None, separate_observables=None, append_observables=None,
-                bit_packed: bool = False, dets_out=None, obs_out=None):
-        """As the reference's convert; dets_out / obs_out (optional, no counterpart in the reference) are
-        caller-owned arrays of the result's shape and dtype, reused across calls to avoid touching fresh
-        pages on every call."""
+                bit_packed: bool = False, bit_pack_result: bool = False, dets_out=None, obs_out=None):
+        """As the reference's convert (bit_pack_result is its legacy name for bit_packed,
+        measurements_to_detection_events.pybind.cc:84-86); dets_out / obs_out (optional, no counterpart in the
+        reference) are caller-owned arrays of the result's shape and dtype, reused across calls to avoid touching
+        fresh pages on every call."""
+        bit_packed = bool(bit_packed) or bool(bit_pack_result)
         if separate_observables is None and append_observables is None:
             raise ValueError("To ignore observable flip data, you must explicitly specify either "
                              "separate_observables=False or append_observables=False.")
