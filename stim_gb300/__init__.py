@@ -56,11 +56,13 @@ def _seed_value(seed):
 
 
 def read_shot_data_file(*, path, format: str = "01", num_measurements=None, num_detectors=None,
-                        num_observables=None, separate_observables: bool = False, bit_packed: bool = False):
+                        num_observables=None, separate_observables: bool = False, bit_packed: bool = False,
+                        bit_pack: bool = False):
     """Reads a result file (formats "01", "b8", "r8", "ptb64", "hits", "dets") as the reference's
     stim.read_shot_data_file does (src/stim/io/read_write.pybind.cc:97-145): records of num_measurements +
-    num_detectors + num_observables bits; bool arrays, or bit-packed uint8 rows; observables split off with
-    separate_observables."""
+    num_detectors + num_observables bits; bool arrays, or bit-packed uint8 rows (bit_pack is the reference's
+    legacy name for bit_packed); observables split off with separate_observables."""
+    bit_packed = bool(bit_packed) or bool(bit_pack)
     if num_measurements is None and num_detectors is None and num_observables is None:
         raise ValueError("Must specify num_measurements, num_detectors, num_observables.")
     nm, nd, no = (int(v or 0) for v in (num_measurements, num_detectors, num_observables))
@@ -93,20 +95,23 @@ def write_shot_data_file(*, data, path, format: str = "01", num_measurements=Non
     if num_measurements is None and num_detectors is None and num_observables is None:
         raise ValueError("Must specify num_measurements, num_detectors, num_observables.")
     nm, nd, no = (int(v or 0) for v in (num_measurements, num_detectors, num_observables))
+    if nm and (nd or no):
+        raise ValueError("num_measurements and (num_detectors or num_observables)")
     n = nm + nd + no
     a = np.asarray(data)
-    if a.ndim != 2:
-        raise ValueError("data must be two dimensional")
+    if a.ndim != 2 or a.dtype not in (np.bool_, np.uint8):
+        raise ValueError("data must be a 2-dimensional numpy array with dtype=np.uint8 or dtype=np.bool_")
+    # The reference's messages for a wrong row width (src/stim/py/numpy.pybind.cc:256-263, 290-296).
     if a.dtype == np.bool_:
         if a.shape[1] != n:
-            raise ValueError(f"Expected data.shape[1] == {n} but got {a.shape[1]}")
+            raise ValueError(f"Expected {n} bits per shot. Got unpacked boolean data (dtype=np.bool_) but "
+                             f"data.shape[1]={a.shape[1]}")
         rows = np.packbits(a, axis=1, bitorder="little")
-    elif a.dtype == np.uint8:
-        if a.shape[1] != (n + 7) // 8:
-            raise ValueError(f"Expected bit-packed data.shape[1] == {(n + 7) // 8} but got {a.shape[1]}")
-        rows = a
     else:
-        raise ValueError("data must be a numpy array of bool or bit-packed uint8")
+        if a.shape[1] != (n + 7) // 8:
+            raise ValueError(f"Expected {n} bits per shot. Got bit packed data (dtype=np.uint8) but "
+                             f"data.shape[1]={a.shape[1]} != math.ceil({n} / 8)={(n + 7) // 8}")
+        rows = a
     rows = np.ascontiguousarray(rows, dtype=np.uint8)
     if rows.shape[1] == 0:
         rows = np.zeros((rows.shape[0], 1), dtype=np.uint8)
