@@ -188,6 +188,8 @@ def _circuit_repr(c) -> str:
     """The circuit as a Python expression: its lines, stripped and indented by four spaces, in a triple-quoted
     literal (the layout of the reference's circuit_repr)."""
     body = "".join(f"    {ln.strip()}\n" for ln in str(c).splitlines() if ln.strip())
+    if not body:
+        return "stim_gb300.Circuit()"
     return "stim_gb300.Circuit('''\n" + body + "''')"
 
 

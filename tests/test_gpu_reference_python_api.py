@@ -152,3 +152,43 @@ def test_repr():
     assert repr(c.compile_sampler(skip_reference_sample=True)) == (
         f"stim_gb300.CompiledMeasurementSampler({want}, skip_reference_sample=True)")
     assert repr(c.compile_detector_sampler()) == f"stim_gb300.CompiledDetectorSampler({want})"
+
+
+# From src/stim/circuit/circuit_pybind_test.py:216-260, 520-570, 2079-2090.
+def test_compiled_sampler_reprs_evaluate():
+    empty = stim_gb300.Circuit()
+    assert repr(empty.compile_sampler()) == "stim_gb300.CompiledMeasurementSampler(stim_gb300.Circuit())"
+    assert repr(empty.compile_detector_sampler()) == "stim_gb300.CompiledDetectorSampler(stim_gb300.Circuit())"
+    c = stim_gb300.Circuit("M 0\nH 0 1 2 3 4\nM 0 1 2 3 4")
+    r = repr(c.compile_sampler())
+    assert r == ("stim_gb300.CompiledMeasurementSampler(stim_gb300.Circuit('''\n    M 0\n    H 0 1 2 3 4\n"
+                 "    M 0 1 2 3 4\n'''))")
+    assert repr(eval(r, {"stim_gb300": stim_gb300})) == r
+    d = stim_gb300.Circuit("M 0\nDETECTOR rec[-1]")
+    r = repr(d.compile_detector_sampler())
+    assert repr(eval(r, {"stim_gb300": stim_gb300})) == r
+
+
+@pytest.mark.parametrize("compile_name,text", [
+    ("compile_sampler", "H 0\nM 0"),
+    ("compile_detector_sampler", "X_ERROR(0.5) 0\nM 0\nDETECTOR rec[-1]"),
+])
+def test_sampling_seeded(compile_name, text):
+    c = stim_gb300.Circuit(text)
+    compile_ = getattr(c, compile_name)
+    with pytest.raises(ValueError, match="seed"):
+        compile_(seed=-1)
+    with pytest.raises(ValueError, match="seed"):
+        compile_(seed=object())
+    assert not np.array_equal(compile_().sample(256), compile_().sample(256))
+    assert not np.array_equal(compile_(seed=None).sample(256), compile_(seed=None).sample(256))
+    s1, s2, s3 = compile_(seed=5).sample(256), compile_(seed=5).sample(256), compile_(seed=6).sample(256)
+    assert np.array_equal(s1, s2)
+    assert not np.array_equal(s1, s3)
+
+
+def test_tagged_instructions_sample():
+    c = stim_gb300.Circuit("R[test1] 0\nX_ERROR[test2](0.25) 0\nM[test3](0.25) 0\nDETECTOR[test4](1, 2) rec[-1]")
+    assert 200 < np.sum(c.compile_detector_sampler().sample(shots=1000)) < 600
+    assert 200 < np.sum(c.compile_sampler().sample(shots=1000)) < 600
+    c.compile_m2d_converter()
