@@ -1,7 +1,8 @@
 """Noisy measurements, measure-resets, Pauli-product measurements and Pauli observable terms as the reference's own
 tests state them (src/stim/simulators/frame_simulator.test.cc:1177-1457 noisy_measurement_{x,y,z} and
 noisy_measurement_reset_{x,y,z}, measure_pauli_product_4body, non_deterministic_pauli_product_detectors;
-:1685-1744 observable_include_paulis_r{z,y,x}).  Raw measurement flips (reference sample all zeros) as the
+:1685-1744 observable_include_paulis_r{z,y,x}; frame_simulator_util.test.cc:223-426, the same noisy measurements
+as detection events, one detector per measurement).  Raw measurement flips (reference sample all zeros) as the
 reference tests sample them; the oracle on the CPU, the GPU samplers in both noise modes."""
 
 import numpy as np
@@ -37,6 +38,23 @@ def meas_gpu(text, shots, seed, noise_mode):
     return s.sample(shots).astype(np.uint8)
 
 
+def with_detectors(text):
+    """The circuit with one detector per measurement, in order (the detection-event form of the tests)."""
+    n = stim_gb300.Circuit(text).num_measurements
+    return text + "".join(f"\nDETECTOR rec[-{n - k}]" for k in range(n))
+
+
+def dets_oracle(text, shots, seed):
+    d, _, _ = OracleCircuit(with_detectors(text)).sample(shots, seed, obs=False, threads=4)
+    return np.unpackbits(d, axis=1, bitorder="little")[:, :stim_gb300.Circuit(text).num_measurements]
+
+
+def dets_gpu(text, shots, seed, noise_mode):
+    s = stim_gb300.Circuit(with_detectors(text)).compile_detector_sampler(seed=seed)
+    s.set_noise_mode(noise_mode)
+    return s.sample(shots).astype(np.uint8)
+
+
 def check_noisy(sample, basis, m, err, resets):
     r = sample(f"R{basis} 0\n{m}(0.05) 0\n{m} 0", 10000)
     assert not r[:, 1].any()
@@ -65,6 +83,11 @@ def test_oracle_noisy_measurements(basis, m, err, resets):
     check_noisy(lambda text, shots: meas_oracle(text, shots, 3), basis, m, err, resets)
 
 
+@pytest.mark.parametrize("basis,m,err,resets", NOISY, ids=[n[1] for n in NOISY])
+def test_oracle_noisy_measurement_detectors(basis, m, err, resets):
+    check_noisy(lambda text, shots: dets_oracle(text, shots, 4), basis, m, err, resets)
+
+
 def test_oracle_pauli_products():
     check_mpp4(meas_oracle(MPP4, 10, 5))
     for text in RANDOM_PRODUCTS:
@@ -83,6 +106,13 @@ def test_oracle_observable_paulis(basis):
 @pytest.mark.parametrize("basis,m,err,resets", NOISY, ids=[n[1] for n in NOISY])
 def test_gpu_noisy_measurements(basis, m, err, resets, noise_mode):
     check_noisy(lambda text, shots: meas_gpu(text, shots, 3, noise_mode), basis, m, err, resets)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("noise_mode", [0, 1], ids=["inline", "hit_lists"])
+@pytest.mark.parametrize("basis,m,err,resets", NOISY, ids=[n[1] for n in NOISY])
+def test_gpu_noisy_measurement_detectors(basis, m, err, resets, noise_mode):
+    check_noisy(lambda text, shots: dets_gpu(text, shots, 4, noise_mode), basis, m, err, resets)
 
 
 @pytest.mark.gpu
