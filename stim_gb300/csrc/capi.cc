@@ -188,6 +188,9 @@ std::pair<const uint8_t *, uint64_t> format_rows(gfs_sampler *s, DevBuf &out, gf
     a.c2 = (uint8_t)c2;
     a.transition = transition;
     if (f == gfs::Format::B8) {
+        if (nbits == 0) {  // empty records take no bytes
+            return {rows, 0};
+        }
         if (stride != (nbits + 7) / 8) {
             throw std::logic_error("b8 rows must be contiguous");
         }

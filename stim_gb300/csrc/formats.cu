@@ -397,10 +397,10 @@ cudaError_t launch_format_write(const FormatArgs &a, cudaStream_t stream) {
     }
     const Format f = (Format)a.fmt;
     if (f == Format::F01) {
-        const uint64_t n = a.shots * ((a.nbits + 7) / 8);
-        if (n == 0) {
-            return cudaSuccess;
+        if (a.nbits == 0) {  // every record is its newline alone
+            return cudaMemsetAsync(a.out, '\n', a.shots, stream);
         }
+        const uint64_t n = a.shots * ((a.nbits + 7) / 8);
         fmt_01_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(a);
     } else if (f == Format::PTB64) {
         const uint64_t w = (a.shots / 64) * ((a.nbits + 31) / 32);

@@ -107,3 +107,26 @@ def test_gpu_writer_dets_detectors_and_observables(tmp_path):
     stim_gb300.Circuit(text).compile_detector_sampler().sample_write(3, filepath=str(path), format="dets",
                                                                       append_observables=True)
     assert path.read_text() == "shot D3 D4 D5 D6 D7 D12 D13 D14 D15 D16 L1\n" * 3
+
+
+# FormatDets_EmptyRecords in every format: records of no bits (a circuit without measurements, a detection sampler
+# without detectors or observables).
+EMPTY_RECORD = {"01": b"\n", "b8": b"", "r8": b"\x00", "hits": b"\n", "dets": b"shot\n", "ptb64": b""}
+
+
+@pytest.mark.parametrize("fmt", sorted(EMPTY_RECORD))
+def test_host_writer_empty_records(tmp_path, fmt):
+    path = tmp_path / "out"
+    stim_gb300.write_shot_data_file(data=np.zeros((64, 0), dtype=np.bool_), path=str(path), format=fmt,
+                                    num_measurements=0)
+    assert path.read_bytes() == EMPTY_RECORD[fmt] * 64
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fmt", sorted(EMPTY_RECORD))
+def test_gpu_writer_empty_records(tmp_path, fmt):
+    path = tmp_path / "out"
+    stim_gb300.Circuit("H 0").compile_sampler().sample_write(64, filepath=str(path), format=fmt)
+    assert path.read_bytes() == EMPTY_RECORD[fmt] * 64
+    stim_gb300.Circuit("M 0").compile_detector_sampler().sample_write(128, filepath=str(path), format=fmt)
+    assert path.read_bytes() == EMPTY_RECORD[fmt] * 128
