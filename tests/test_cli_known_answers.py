@@ -1,7 +1,9 @@
-"""The reference's command-line tests of `stim detect` and `stim sample`, restated against this package's samplers
-(src/stim/cmd/command_detect.test.cc:21-196, command_sample.test.cc:73-420): the CLI's 01 output is what
-sample_write(format="01") writes, and `--prepend_observables` / `--append_observables` / `--skip_reference_sample`
-are the samplers' arguments of the same names.
+"""The reference's command-line tests of `stim detect`, `stim sample`, `stim m2d` and `stim sample_dem`, restated
+against this package (src/stim/cmd/command_detect.test.cc:21-233, command_sample.test.cc:73-420,
+command_m2d.test.cc:22-176, command_sample_dem.test.cc:22-51): the CLI's output is what sample_write / convert_file
+write, and `--prepend_observables` / `--append_observables` / `--skip_reference_sample` / `--obs_out` are the
+arguments of the same meaning.  (`m2d --ran_without_feedback` has no counterpart in the reference's Python
+converter, which this package mirrors, and is left out.)
 
 Exact outputs for deterministic circuits; for random ones the reference's `deviation` check
 (command_sample.test.cc:37-71): every sampled line must be an expected one, and each expected line's rate must lie
@@ -206,3 +208,135 @@ def test_gpu_seeded_sampling(tmp_path, compile_name, text):
     assert run(5) == run(5)
     assert run(5) != run(6)
     assert run(None) != run(None)
+
+
+# command_m2d.test.cc:22-62: X 0, M 0 1, D0 = rec[-2], D1 = rec[-1], L2 = rec[-1]; inputs 00, 01, 10, 11.
+M2D = "X 0\nM 0 1\nDETECTOR rec[-2]\nDETECTOR rec[-1]\nOBSERVABLE_INCLUDE(2) rec[-1]"
+M2D_IN = "00\n01\n10\n11\n"
+M2D_CASES = [
+    (False, True, "shot D0\nshot D0 D1 L2\nshot\nshot D1 L2\n"),
+    (False, False, "shot D0\nshot D0 D1\nshot\nshot D1\n"),
+    (True, False, "shot\nshot D1\nshot D0\nshot D0 D1\n"),
+]
+# command_m2d.test.cc:64-120: records controlling Paulis change the reference sample, not the conversion.
+FEEDBACK = """
+CX 0 2 1 2
+M 2
+CX rec[-1] 2
+DETECTOR rec[-1]
+TICK
+CX 0 2 1 2
+M 2
+CX rec[-1] 2
+DETECTOR rec[-1] rec[-2]
+TICK
+CX 0 2 1 2
+M 2
+CX rec[-1] 2
+DETECTOR rec[-1] rec[-2]
+TICK
+M 0 1
+DETECTOR rec[-1] rec[-2] rec[-3]
+OBSERVABLE_INCLUDE(0) rec[-1]
+"""
+FEEDBACK_IN = "00000\n10000\n01000\n00100\n00010\n00001\n"
+FEEDBACK_OUT = "shot\nshot D0 D1\nshot D1 D2\nshot D2 D3\nshot D3\nshot D3 L0\n"
+# command_m2d.test.cc:158-176: observables of Pauli terms only; the conversion ignores the terms.
+UNPHYSICAL = """
+QUBIT_COORDS(0, 0) 0
+QUBIT_COORDS(1, 0) 1
+QUBIT_COORDS(0, 1) 2
+QUBIT_COORDS(1, 1) 3
+OBSERVABLE_INCLUDE(0) X0 X1
+OBSERVABLE_INCLUDE(1) Z0 Z2
+MPP X0*X1*X2*X3 Z0*Z1 Z2*Z3
+DEPOLARIZE1(0.001) 0 1 2 3
+MPP X0*X1*X2*X3 Z0*Z1 Z2*Z3
+DETECTOR rec[-1] rec[-4]
+DETECTOR rec[-2] rec[-5]
+DETECTOR rec[-3] rec[-6]
+OBSERVABLE_INCLUDE(0) X0 X1
+OBSERVABLE_INCLUDE(1) Z0 Z2
+"""
+
+
+def parse01(text):
+    return np.array([[ch == "1" for ch in line] for line in text.splitlines()], dtype=np.bool_)
+
+
+def dets_lines(d, o, append):
+    out = []
+    for dr, orow in zip(d, o):
+        line = "shot" + "".join(f" D{k}" for k in np.nonzero(dr)[0])
+        if append:
+            line += "".join(f" L{k}" for k in np.nonzero(orow)[0])
+        out.append(line + "\n")
+    return "".join(out)
+
+
+def oracle_m2d_dets(text, data01, skip, append):
+    c, o = stim_gb300.Circuit(text), OracleCircuit(text)
+    ref = None if skip else c.reference_sample(bit_packed=True)
+    d, ob = o.m2d(np.packbits(parse01(data01), axis=1, bitorder="little"), ref if ref is not None and ref.size else None)
+    d = np.unpackbits(d, axis=1, bitorder="little")[:, :o.num_detectors]
+    ob = np.unpackbits(ob, axis=1, bitorder="little")[:, :o.num_observables]
+    return d, ob
+
+
+@pytest.mark.parametrize("skip,append,want", M2D_CASES)
+def test_oracle_m2d_command(skip, append, want):
+    assert dets_lines(*oracle_m2d_dets(M2D, M2D_IN, skip, append), append) == want
+
+
+def test_oracle_m2d_feedback_and_unphysical_observables():
+    assert dets_lines(*oracle_m2d_dets(FEEDBACK, FEEDBACK_IN, False, True), True) == FEEDBACK_OUT
+    d, ob = oracle_m2d_dets(UNPHYSICAL, "000000\n100100\n000110\n", False, False)
+    assert lines_of(d) == ["000", "000", "011"] and lines_of(ob) == ["00", "00", "00"]
+
+
+def m2d_file(tmp_path, text, data01, out_format, skip=False, append=False, obs=False):
+    src, out, obs_path = tmp_path / "in", tmp_path / "out", tmp_path / "obs"
+    src.write_text(data01)
+    conv = stim_gb300.Circuit(text).compile_m2d_converter(skip_reference_sample=skip)
+    conv.convert_file(measurements_filepath=str(src), measurements_format="01", detection_events_filepath=str(out),
+                      detection_events_format=out_format, append_observables=append,
+                      obs_out_filepath=str(obs_path) if obs else None, obs_out_format="01")
+    return out.read_text(), (obs_path.read_text() if obs else None)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("skip,append,want", M2D_CASES)
+def test_gpu_m2d_command(tmp_path, skip, append, want):
+    assert m2d_file(tmp_path, M2D, M2D_IN, "dets", skip=skip, append=append)[0] == want
+
+
+@pytest.mark.gpu
+def test_gpu_m2d_feedback(tmp_path):
+    assert m2d_file(tmp_path, FEEDBACK, FEEDBACK_IN, "dets", append=True)[0] == FEEDBACK_OUT
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("index,obs_line", [(0, "0\n"), (10, "00000000000\n")])
+def test_gpu_m2d_obs_file_sizes(tmp_path, index, obs_line):
+    # command_m2d.test.cc:122-156: 1,024 detectors and an observables file of 1 or 11 observables.
+    text = f"M 0\nREPEAT 1024 {{\n    DETECTOR rec[-1]\n}}\nOBSERVABLE_INCLUDE({index}) rec[-1]"
+    assert m2d_file(tmp_path, text, "0\n", "01", obs=True) == ("0" * 1024 + "\n", obs_line)
+
+
+@pytest.mark.gpu
+def test_gpu_m2d_unphysical_observables(tmp_path):
+    assert m2d_file(tmp_path, UNPHYSICAL, "000000\n100100\n000110\n", "01", obs=True) == (
+        "000\n000\n011\n", "00\n00\n00\n")
+
+
+@pytest.mark.gpu
+def test_gpu_sample_dem_command(tmp_path):
+    # command_sample_dem.test.cc:22-51: an empty model gives one empty line; error(0) D0, error(1) D1 L2 at seed 0.
+    det, obs = tmp_path / "det", tmp_path / "obs"
+    stim_gb300.DetectorErrorModel("").compile_sampler(seed=0).sample_write(
+        1, det_out_file=str(det), det_out_format="01", obs_out_file=None)
+    assert det.read_text() == "\n"
+    stim_gb300.DetectorErrorModel("error(0) D0\nerror(1) D1 L2").compile_sampler(seed=0).sample_write(
+        5, det_out_file=str(det), det_out_format="01", obs_out_file=str(obs), obs_out_format="01")
+    assert det.read_text() == "01\n" * 5
+    assert obs.read_text() == "001\n" * 5
