@@ -63,3 +63,23 @@ def test_gpu_matches_reference_statistics(name, template, a, b, want, noise_mode
     d = s.sample(SHOTS, bit_packed=True)
     check_bins(d, want)
     np.testing.assert_array_equal(d, OracleCircuit(text).sample(SHOTS, 7, threads=8)[0])
+
+
+# src/stim/simulators/frame_simulator_pybind_test.py:406-414 (test_repro_heralded_pauli_channel_1_bug): a herald with
+# only the "heralded identity" and X branches set fires on some shots, and the unheralded qubit stays 0.
+HERALD_REPRO = "R 0 1\nHERALDED_PAULI_CHANNEL_1(0.2, 0.2, 0, 0) 1\nM 0"
+
+
+def test_oracle_heralded_pauli_channel_repro():
+    _, _, m = OracleCircuit(HERALD_REPRO).sample(1024, 9, dets=False, obs=False, meas=True)
+    r = np.unpackbits(m, axis=1, bitorder="little")[:, :2]
+    assert r[:, 0].sum() > 0 and r[:, 1].sum() == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("noise_mode", [0, 1], ids=["inline", "hit_lists"])
+def test_gpu_heralded_pauli_channel_repro(noise_mode):
+    s = stim_gb300.Circuit(HERALD_REPRO).compile_sampler(seed=9)
+    s.set_noise_mode(noise_mode)
+    r = s.sample(1024)
+    assert r[:, 0].sum() > 0 and r[:, 1].sum() == 0
