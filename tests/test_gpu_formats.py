@@ -145,15 +145,19 @@ def test_pipelined_chunks_equal_host_writer(fmt, layout, tmp_path):
     # observable layout, against the host writer on the same bits.
     from stim_gb300 import workloads
 
-    if layout == "prepend" and fmt == "dets":
-        pytest.skip("dets names prepended observables L0.. first; the host writer names row bits D then L")
     c = stim_gb300.Circuit(workloads.code_circuit("surface_code:rotated_memory_z", 7, 7, 0.01))
     D, O = c.num_detectors, c.num_observables
     shots = 9 * 1024 + 64
     s = c.compile_detector_sampler(seed=11)
     s.set_chunk_shots(1024)
     out = tmp_path / "dev"
-    if layout == "obs":
+    if layout == "prepend" and fmt == "dets":
+        # dets names prepended observables L0.. before the detectors, which the host writer's D-then-L rows cannot
+        # express: compare against one chunk of the same device path (pinned to the reference CLI's file above).
+        s.sample_write(shots, filepath=str(out), format=fmt, prepend_observables=True)
+        c.compile_detector_sampler(seed=11).sample_write(shots, filepath=str(tmp_path / "h"), format=fmt,
+                                                         prepend_observables=True)
+    elif layout == "obs":
         obs = tmp_path / "obs"
         s.sample_write(shots, filepath=str(out), format=fmt, obs_out_filepath=str(obs), obs_out_format=fmt)
         d, o = c.compile_detector_sampler(seed=11).sample(shots, bit_packed=True, separate_observables=True)
