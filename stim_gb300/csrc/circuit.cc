@@ -357,9 +357,11 @@ void parse_into(Circuit &circ, Reader &r, bool until_brace) {
                     buf.push_back((char)c);
                     c = r.get();
                 }
+                // An empty number reads as 0, as in the reference (circuit.h read_normal_double): "X_ERROR() 0" is
+                // X_ERROR(0) 0 and "H() 0" is H with one argument.
                 char *end = nullptr;
                 double v = std::strtod(buf.c_str(), &end);
-                if (buf.empty() || end != buf.c_str() + buf.size() || std::isinf(v) || std::isnan(v)) {
+                if (end != buf.c_str() + buf.size() || std::isinf(v) || std::isnan(v)) {
                     fail("Not a real number: " + buf);
                 }
                 op.args.push_back(v);

@@ -128,6 +128,17 @@ struct Lowerer {
         }
     }
 
+    // Whether every record target of a detector / observable instruction reads a result already recorded.
+    bool lookbacks_valid(const Instruction &op) const {
+        for (auto t : op.targets) {
+            const uint32_t k = t & GFS_T_VALUE_MASK;
+            if (((op.gate == GFS_DETECTOR) || (t & GFS_T_RECORD)) && (k == 0 || k > meas_seen)) {
+                return false;
+            }
+        }
+        return true;
+    }
+
     // ---- runs of distinct rows ----
     template <typename F>
     void distinct_runs(const std::vector<uint32_t> &rows, size_t stride, F flush) {
@@ -681,6 +692,12 @@ struct Lowerer {
     void lower_instruction(const Instruction &op, uint64_t inst) {
         gfs_gate g = op.gate;
         if (g == GFS_DETECTOR) {
+            // Sampling measurements, the reference never evaluates detectors or observables (frame_simulator.inl
+            // :222-252 keep no detection data), so one that reads a record before the beginning of time is left
+            // out instead of rejected; detection sampling rejects it as the reference does.
+            if (mode == SampleMode::MEASUREMENTS && !lookbacks_valid(op)) {
+                return;
+            }
             if (pending_dets.empty()) {
                 pending_inst = inst;
             }
@@ -709,6 +726,9 @@ struct Lowerer {
                 break;
         }
         if (g == GFS_OBSERVABLE_INCLUDE) {
+            if (mode == SampleMode::MEASUREMENTS && !lookbacks_valid(op)) {
+                return;  // as for detectors above
+            }
             uint32_t k_obs = (uint32_t)op.args[0];
             std::vector<uint32_t> terms;
             for (auto t : op.targets) {
@@ -1834,7 +1854,7 @@ struct Lowerer {
             throw std::invalid_argument("measurement record window too large for the GPU frame sampler");
         }
         prog.ring = (uint32_t)ring;
-        if (dets_unrolled != prog.stats.num_detectors) {
+        if (mode == SampleMode::DETECTIONS && dets_unrolled != prog.stats.num_detectors) {
             throw std::logic_error("detector count mismatch in lowering");
         }
         if (opts.no_randomization) {

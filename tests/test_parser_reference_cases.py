@@ -35,6 +35,8 @@ REJECTED = [
     # classical control of a qubit-only gate, zero repetitions, NaN, MPAD of a non-bit
     "M 0\nXCX rec[-1] 1", "REPEAT 0 {\n    M 0\n    OBSERVABLE_INCLUDE(0) rec[-1]\n}", "X_ERROR(nan) 0", "MPAD 2",
     "MPAD sweep[-1]",
+    # an empty argument reads as 0 (the reference's read_normal_double), which these gates cannot take
+    "H() 0", "TICK()", "H( ) 0", "X_ERROR(0.1,) 0",
 ]
 
 # (text, measurements it records)
@@ -56,6 +58,10 @@ ACCEPTED = [
     ("PAULI_CHANNEL_2(0,0,0,0,0,0,0,0,0,0,0,0,0,0,0) 1 2", 0),
     ("PAULI_CHANNEL_2(0.1,0,0,0,0,0,0,0,0,0,0.1,0,0,0,0.1) 1 2", 0),
     ("ZCX 0 1\nZCX rec[-1] 1\nZCY rec[-2] 1\nZCZ rec[-4] 1", 0), ("MPAD 0 1", 2), ("H 0\r\nH 1\r\n", 0),
+    # an empty argument reads as 0, as the reference's parser reads it (found by comparing acceptance with the
+    # reference's own `stim sample` / `stim detect` on random texts)
+    ("X_ERROR() 0", 0), ("X_ERROR( ) 0", 0), ("M() 0", 1), ("QUBIT_COORDS() 0", 0), ("DETECTOR()", 0),
+    ("MPP() X0", 1), ("PAULI_CHANNEL_1(,,) 0", 0), ("PAULI_CHANNEL_1(0.1,,) 0", 0), ("REPEAT() 2 {\n}", 0),
 ]
 
 
@@ -68,3 +74,14 @@ def test_rejected_like_the_reference(text):
 @pytest.mark.parametrize("text,measurements", ACCEPTED)
 def test_accepted_like_the_reference(text, measurements):
     assert stim_gb300.Circuit(text).num_measurements == measurements
+
+
+@pytest.mark.parametrize("text", ["M 0\nDETECTOR rec[-3]", "OBSERVABLE_INCLUDE(0) rec[-3]",
+                                  "REPEAT 3 {\n    M 0\n    DETECTOR rec[-2]\n}"])
+def test_unreadable_detectors_matter_only_to_detection_sampling(text):
+    # The reference's measurement sampler keeps no detection data (frame_simulator.inl:222-252), so `stim sample`
+    # takes these circuits while `stim detect` rejects them (std::out_of_range, IndexError in Python).
+    c = stim_gb300.Circuit(text)
+    c.program_info("measurements")
+    with pytest.raises(IndexError, match="before the beginning of time"):
+        c.program_info("detections")
