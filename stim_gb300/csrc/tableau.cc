@@ -15,6 +15,7 @@
 #include <stdexcept>
 #include <string>
 #include <unordered_map>
+#include <vector>
 
 namespace gfs {
 namespace {
@@ -310,6 +311,25 @@ class Runner {
         return rec_[rec_.size() - k];
     }
 
+    // The reference collapses the targets of an X- or Y-basis measurement or reset in ascending qubit order before it
+    // reads any result (tableau_simulator.inl collapse_x / collapse_y gather them in a std::set), and those of a
+    // Z-basis one in the order given (collapse_z).  The order decides which random outcome is the one forced to 0, so
+    // X / Y targets are collapsed here in that order first; the per-target reads that follow are then deterministic.
+    void collapse_sorted(const Instruction &op, gfs_gate basis) {
+        if (basis == GFS_M || basis == GFS_MR || basis == GFS_R || op.targets.size() < 2) {
+            return;
+        }
+        std::vector<uint32_t> vs;
+        for (uint32_t t : op.targets) {
+            vs.push_back(t & GFS_T_VALUE_MASK);
+        }
+        std::sort(vs.begin(), vs.end());
+        vs.erase(std::unique(vs.begin(), vs.end()), vs.end());
+        for (uint32_t v : vs) {
+            measure(v, basis, false, false);
+        }
+    }
+
     void measure(uint32_t t, gfs_gate basis, bool reset_after, bool record = true) {
         const uint32_t a = q(t);
         if (basis == GFS_MX || basis == GFS_RX || basis == GFS_MRX) tab_.apply(GFS_H, a);
@@ -327,9 +347,10 @@ class Runner {
 
     // One Pauli product with sign (-1)^sign: factors (qubit, x, z).  measure = true records its
     // eigenvalue bit (outcome forced to 0 when random); otherwise applies exp(-i pi/4 P) (dag: +).
-    void product(const std::vector<std::array<uint32_t, 3>> &f, bool sign, bool measure, bool dag) {
+    void product(const std::vector<std::array<uint32_t, 3>> &f, bool sign, bool measure, bool dag,
+                 bool record = true) {
         if (f.empty()) {
-            if (measure) {
+            if (measure && record) {
                 rec_.push_back(sign);
             }
             return;
@@ -351,7 +372,10 @@ class Runner {
         rotate();
         fold();
         if (measure) {
-            rec_.push_back((uint8_t)(tab_.measure_z(f[0][0]) ^ sign));
+            const bool m = tab_.measure_z(f[0][0]);
+            if (record) {
+                rec_.push_back((uint8_t)(m ^ sign));
+            }
         } else {
             tab_.apply((sign ^ dag) ? GFS_S_DAG : GFS_S, f[0][0]);
         }
@@ -450,16 +474,54 @@ class Runner {
         }
     }
 
+    // MXX / MYY / MZZ as the reference runs them (tableau_simulator.inl do_MXX and gate_decomposition.cc
+    // decompose_pair_instruction_into_disjoint_segments): the pairs split into runs on disjoint qubits, and within a
+    // run MXX / MYY collapse their pairs in ascending order of the first target's qubit, MZZ in the order given,
+    // before the results are read in the order given.
     void pair_measure(const Instruction &op) {
-        for (size_t k = 0; k + 1 < op.targets.size(); k += 2) {
+        const uint32_t x = op.gate == GFS_MZZ ? 0 : 1, z = op.gate == GFS_MXX ? 0 : 1;
+        auto pair_product = [&](size_t k, bool record) {
             const uint32_t a = op.targets[k], b = op.targets[k + 1];
-            const uint32_t x = op.gate == GFS_MZZ ? 0 : 1, z = op.gate == GFS_MXX ? 0 : 1;
             const bool sign = ((a ^ b) & GFS_T_INVERTED) != 0;
             if (q(a) == q(b)) {
-                rec_.push_back(sign);
-                continue;
+                if (record) {
+                    rec_.push_back(sign);
+                }
+                return;
             }
-            product({{q(a), x, z}, {q(b), x, z}}, sign, true, false);
+            product({{q(a), x, z}, {q(b), x, z}}, sign, true, false, record);
+        };
+        auto run = [&](size_t lo, size_t hi) {
+            if (op.gate != GFS_MZZ) {
+                std::vector<std::pair<uint32_t, size_t>> order;
+                for (size_t k = lo; k < hi; k += 2) {
+                    order.push_back({op.targets[k] & GFS_T_VALUE_MASK, k});
+                }
+                std::sort(order.begin(), order.end());
+                for (const auto &e : order) {
+                    pair_product(e.second, false);
+                }
+            }
+            for (size_t k = lo; k < hi; k += 2) {
+                pair_product(k, true);
+            }
+        };
+        std::vector<uint32_t> used;
+        size_t lo = 0;
+        const size_t n = op.targets.size() & ~(size_t)1;
+        for (size_t k = 0; k < n; k += 2) {
+            const uint32_t v0 = op.targets[k] & GFS_T_VALUE_MASK, v1 = op.targets[k + 1] & GFS_T_VALUE_MASK;
+            if (std::find(used.begin(), used.end(), v0) != used.end() ||
+                std::find(used.begin(), used.end(), v1) != used.end()) {
+                run(lo, k);
+                lo = k;
+                used.clear();
+            }
+            used.push_back(v0);
+            used.push_back(v1);
+        }
+        if (lo < n) {
+            run(lo, n);
         }
     }
 
@@ -470,16 +532,19 @@ class Runner {
             case GFS_M:
             case GFS_MX:
             case GFS_MY:
+                collapse_sorted(op, g);
                 for (uint32_t t : op.targets) measure(t, g, false);
                 return;
             case GFS_MR:
             case GFS_MRX:
             case GFS_MRY:
+                collapse_sorted(op, g);
                 for (uint32_t t : op.targets) measure(t, g, true);
                 return;
             case GFS_R:
             case GFS_RX:
             case GFS_RY:
+                collapse_sorted(op, g);
                 for (uint32_t t : op.targets) measure(t, g, true, false);
                 return;
             case GFS_MPAD:

@@ -12,6 +12,10 @@ It writes
                                   noise knobs at 0.001 (stim_gb300.workloads substitutes other p);
   * tests/golden/refsample_random.npz  reference samples (the reference's TableauSimulator) of 300 random
                                   small circuits mixing every sign-sensitive gate family;
+  * tests/golden/refsample_multi.npz   the same for 300 random circuits whose measurements, resets and pair
+                                  measurements take several targets at once (the reference collapses an
+                                  instruction's X / Y targets in ascending qubit order, which decides the
+                                  random outcomes forced to 0);
   * tests/golden/<case>.npz       for each case: the circuit text, seed, shot count, and the
                                   detection events, observable flips and measurement flips that the
                                   reference's FrameSimulator produced when fed the injected random
@@ -167,14 +171,56 @@ def random_small_circuit(rng, n=4, depth=25):
     return "\n".join(lines) + "\n"
 
 
-def refsample_fixtures(count=300, seed=3):
+def random_multi_target_circuit(rng, n=6, depth=14):
+    """A random circuit whose measurements, resets and pair measurements act on several (shuffled) targets of
+    entangled qubits at once, with MPP products in several disjoint and overlapping groups."""
+    g1 = ["H", "S", "SQRT_X", "C_XYZ", "H_YZ", "X", "Y"]
+    g2 = ["CX", "CZ", "CY", "ISWAP", "SQRT_XX", "XCY", "SWAP"]
+    lines = []
+    nmeas = 0
+    for _ in range(depth):
+        k = rng.randrange(8)
+        qs = list(range(n))
+        rng.shuffle(qs)
+        m = rng.randint(2, n)
+        if k == 0:
+            lines.append(f"{rng.choice(g1)} " + " ".join(map(str, qs[:m])))
+        elif k == 1:
+            lines.append(f"{rng.choice(g2)} " + " ".join(map(str, qs[:2 * (m // 2)])))
+        elif k == 2:
+            g = rng.choice(["M", "MX", "MY", "MR", "MRX", "MRY"])
+            lines.append(f"{g} " + " ".join(("!" if rng.random() < 0.3 else "") + str(q) for q in qs[:m]))
+            nmeas += m
+        elif k == 3:
+            lines.append(f"{rng.choice(['R', 'RX', 'RY'])} " + " ".join(map(str, qs[:m])))
+        elif k == 4:
+            pairs = qs[:2 * (m // 2)]
+            extra = rng.sample(range(n), 2)  # a repeated qubit starts a new disjoint run
+            tgts = pairs + extra
+            lines.append(f"{rng.choice(['MXX', 'MYY', 'MZZ'])} " + " ".join(map(str, tgts)))
+            nmeas += len(tgts) // 2
+        elif k == 5:
+            prods = []
+            for _ in range(rng.randint(2, 4)):
+                sub = rng.sample(range(n), rng.randint(1, 3))
+                prods.append("*".join(f"{rng.choice('XYZ')}{q}" for q in sub))
+            lines.append("MPP " + " ".join(prods))
+            nmeas += len(prods)
+        elif k == 6 and nmeas:
+            lines.append(f"{rng.choice(['CX', 'CZ', 'CY'])} rec[-{rng.randint(1, nmeas)}] {qs[0]}")
+        else:
+            lines.append(f"{rng.choice(['SPP', 'SPP_DAG'])} " + "*".join(f"{rng.choice('XYZ')}{q}" for q in qs[:3]))
+    return "\n".join(lines) + "\n"
+
+
+def refsample_fixtures(count=300, seed=3, make=random_small_circuit, name="refsample_random.npz"):
     """Reference samples (the reference's TableauSimulator) of random small circuits."""
     import random
 
     rng = random.Random(seed)
     texts, samples = [], []
     while len(texts) < count:
-        text = random_small_circuit(rng)
+        text = make(rng)
         try:
             out = run_ref(text, 1, 128)
         except subprocess.CalledProcessError:
@@ -186,13 +232,16 @@ def refsample_fixtures(count=300, seed=3):
     lengths = np.array([len(s) for s in samples], dtype=np.int64)
     for k, s in enumerate(samples):
         packed[k, :len(s)] = s
-    np.savez_compressed(os.path.join(HERE, "refsample_random.npz"), circuits=np.array(texts), samples=packed,
+    np.savez_compressed(os.path.join(HERE, name), circuits=np.array(texts), samples=packed,
                         lengths=lengths, seed=np.uint64(seed))
 
 
 def main():
     if "--refsample-only" in sys.argv:
         refsample_fixtures()
+        return
+    if "--refsample-multi-only" in sys.argv:
+        refsample_fixtures(seed=5, make=random_multi_target_circuit, name="refsample_multi.npz")
         return
     only = [a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")]
     if not only:
@@ -206,6 +255,7 @@ def main():
         print(name, out["num_detectors"], out["num_measurements"], shots)
     if not only:
         refsample_fixtures()
+        refsample_fixtures(seed=5, make=random_multi_target_circuit, name="refsample_multi.npz")
 
 
 if __name__ == "__main__":

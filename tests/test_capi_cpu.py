@@ -135,3 +135,13 @@ def test_reference_sample_random_small_circuits():
     for text, row, n in zip(d["circuits"], d["samples"], d["lengths"]):
         got = stim_gb300.Circuit(str(text)).reference_sample(bit_packed=True)
         np.testing.assert_array_equal(got, row[:n], err_msg=str(text))
+
+
+def test_reference_sample_multi_target_circuits():
+    # Measurements, resets and pair measurements on several entangled targets at once: which random outcome the
+    # reference forces to 0 depends on the order it collapses an instruction's targets in (X / Y bases ascending
+    # by qubit, Z in the order given; pair measurements per run of disjoint pairs).
+    d = np.load(os.path.join(GOLDEN_DIR, "refsample_multi.npz"))
+    for text, row, n in zip(d["circuits"], d["samples"], d["lengths"]):
+        got = stim_gb300.Circuit(str(text)).reference_sample(bit_packed=True)
+        np.testing.assert_array_equal(got, row[:n], err_msg=str(text))
