@@ -106,48 +106,64 @@ struct Parser {
             }
         }
     }
+    // Parenthesized arguments, as the reference reads them (circuit.h read_parens_arguments, shared with circuits):
+    // the '(' must follow the name or tag directly; numbers are runs of digits, '.', 'e', 'E', '+' and '-' (an
+    // empty one reads as 0), separated by ',' with spaces or tabs around.
     std::vector<double> read_args() {
         std::vector<double> args;
-        skip_spaces();
         if (peek() != '(') {
             return args;
         }
         k++;
-        skip_spaces();
-        if (peek() == ')') {
-            k++;
-            return args;
-        }
-        while (true) {
-            skip_spaces();
-            size_t start = k;
-            while (peek() != -1 && peek() != ',' && peek() != ')' && peek() != ' ' && peek() != '\n') {
+        auto blanks = [&]() {
+            while (peek() == ' ' || peek() == '\t') {
                 k++;
             }
-            std::string tok(s.substr(start, k - start));
+        };
+        auto number_char = [](int c) {
+            return (c >= '0' && c <= '9') || c == '.' || c == 'e' || c == 'E' || c == '+' || c == '-';
+        };
+        blanks();
+        while (true) {
+            std::string buf;
+            while (buf.size() < 63 && number_char(peek())) {
+                buf.push_back((char)get());
+            }
             char *end = nullptr;
-            double v = std::strtod(tok.c_str(), &end);
-            if (tok.empty() || end != tok.c_str() + tok.size() || std::isnan(v)) {
-                throw std::invalid_argument("Parsing a number failed: '" + tok + "'.");
+            const double v = std::strtod(buf.c_str(), &end);
+            if (end != buf.c_str() + buf.size() || std::isinf(v) || std::isnan(v)) {
+                throw std::invalid_argument("Not a real number: " + buf);
             }
             args.push_back(v);
-            skip_spaces();
-            int c = get();
-            if (c == ')') {
-                return args;
+            blanks();
+            if (peek() != ',') {
+                break;
             }
-            if (c != ',') {
-                throw std::invalid_argument("Expected ',' or ')' in instruction arguments.");
-            }
+            k++;
+            blanks();
         }
+        blanks();
+        if (get() != ')') {
+            throw std::invalid_argument("Parens arguments for 'detector error model instruction' didn't end with a ')'.");
+        }
+        return args;
     }
     // Targets until the end of the line, a comment, '{' or '}'.
+    // As the reference reads them (circuit.h read_until_next_line_arg): targets are separated from the instruction
+    // and from one another by spaces or tabs; the line ends at a newline, a comment or a block's '{', and a '}'
+    // closes a block only at the start of a line.
+    static bool ends_target(int c) {
+        return c == -1 || c == ' ' || c == '\t' || c == '\r' || c == '\n' || c == '#' || c == '{';
+    }
     std::vector<DemTarget> read_targets() {
         std::vector<DemTarget> t;
+        if (!ends_target(peek())) {
+            throw std::invalid_argument("Targets must be separated by spacing.");
+        }
         while (true) {
             skip_spaces();
             int c = peek();
-            if (c == -1 || c == '\n' || c == '#' || c == '{' || c == '}') {
+            if (c == -1 || c == '\n' || c == '#' || c == '{') {
                 return t;
             }
             if (c == 'D' || c == 'd') {
@@ -164,9 +180,8 @@ struct Parser {
             } else {
                 throw std::invalid_argument("Unrecognized target prefix '" + std::string(1, (char)c) + "'.");
             }
-            c = peek();
-            if (c != -1 && c != ' ' && c != '\t' && c != '\r' && c != '\n' && c != '#' && c != '{' && c != '}') {
-                throw std::invalid_argument("Target was not followed by a space.");
+            if (!ends_target(peek())) {
+                throw std::invalid_argument("Targets must be separated by spacing.");
             }
         }
     }
@@ -254,7 +269,9 @@ struct Parser {
             DemInst in;
             in.op = read_name();
             skip_tag();
-            in.args = read_args();
+            if (in.op != DemOp::REPEAT) {  // a repeat block takes no parenthesized arguments
+                in.args = read_args();
+            }
             in.targets = read_targets();
             skip_spaces();
             if (in.op == DemOp::REPEAT) {

@@ -69,3 +69,19 @@ def test_tagged_and_nested_models_parse():
         "error(0.125) D0\nerror(0.125) D5\nerror(0.25) D5 ^ L4\nshift_detectors(1.5, 2) 60\nrepeat 100 {\n"
         "    error(0.125) D0\n    error(0.125) D5\n    error(0.25) D5 ^ L4\n    shift_detectors(1.5, 2) 60\n}")
     assert (m.num_observables, m.num_errors) == (5, 303)
+
+
+# Spacing and argument rules of the reference's model parser (circuit.h read_parens_arguments and
+# read_until_next_line_arg, shared with circuits), found by comparing acceptance with the reference's own
+# `stim sample_dem` on random texts.
+@pytest.mark.parametrize("text", ["error() D0", "error( ) D0", "error(\t0.1\t) D0", "detector(1,,2) D0",
+                                  "error(0.1)", "error(0.1)#c", "repeat 2 {}", "repeat 2 { detector D0\n}"])
+def test_accepted_like_the_reference_parser(text):
+    stim_gb300.DetectorErrorModel(text)
+
+
+@pytest.mark.parametrize("text", ["error (0.1) D0", "error(0.1)D0", "repeat 2 {\ndetector D0 }",
+                                  "repeat 2 {\ndetector D0}", "repeat(2) 3 {\n}", "error(0.1x) D0", "error(inf) D0"])
+def test_rejected_like_the_reference_parser(text):
+    with pytest.raises(ValueError):
+        stim_gb300.DetectorErrorModel(text)
