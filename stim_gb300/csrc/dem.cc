@@ -148,10 +148,9 @@ struct Parser {
         }
         return args;
     }
-    // Targets until the end of the line, a comment, '{' or '}'.
-    // As the reference reads them (circuit.h read_until_next_line_arg): targets are separated from the instruction
-    // and from one another by spaces or tabs; the line ends at a newline, a comment or a block's '{', and a '}'
-    // closes a block only at the start of a line.
+    // Targets until the end of the line, as the reference reads them (circuit.h read_until_next_line_arg): they are
+    // separated from the instruction and from one another by spaces or tabs; the line ends at a newline, a comment
+    // or a block's '{', and a '}' closes a block only at the start of a line.
     static bool ends_target(int c) {
         return c == -1 || c == ' ' || c == '\t' || c == '\r' || c == '\n' || c == '#' || c == '{';
     }
