@@ -145,3 +145,22 @@ def test_reference_sample_multi_target_circuits():
     for text, row, n in zip(d["circuits"], d["samples"], d["lengths"]):
         got = stim_gb300.Circuit(str(text)).reference_sample(bit_packed=True)
         np.testing.assert_array_equal(got, row[:n], err_msg=str(text))
+
+
+def test_binding_example_compiles_and_runs(tmp_path):
+    # The host half of the binding the integration notes show (tests/binding_example.cc), compiled against
+    # include/stim_gb300.h and linked to the library: parse, counts, reference sample, and sampler creation, which
+    # without a GPU must fail with GFS_ERR_CUDA and a message.
+    import shutil
+    import subprocess
+
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    lib_dir = os.path.dirname(_native.lib()._name)
+    exe = tmp_path / "binding_example"
+    subprocess.run([cxx, "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "binding_example.cc"), "-L", lib_dir, "-lstim_gb300",
+                    f"-Wl,-rpath,{lib_dir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.strip()
+    assert re.fullmatch(r"measurements 4 reference 1000 sampler (0|3 message)", out), out
