@@ -6,7 +6,8 @@ where the reference has not been built into oracle/_ref by `make -C oracle ref`)
   per measurement (multi-target measurements, resets, pair measurements, products and feedback on entangled qubits);
 * detector error models: accepted / rejected as `stim sample_dem` accepts them, with the same detector and observable
   counts;
-* result files: this package's reader reads what `stim convert` writes, and its writer writes the same bytes.
+* result files: this package's reader reads what `stim convert` writes, and its writer writes the same bytes;
+  malformed files are rejected exactly when `stim convert` rejects them.
 
 The reference is run as the checker only; nothing here is on the product path."""
 
@@ -206,3 +207,45 @@ def test_result_files_match_reference_convert(tmp_path):
         np.testing.assert_array_equal(back, data)
         stim_gb300.write_shot_data_file(data=data, path=str(c), format=fout, **kw)
         assert c.read_bytes() == b.read_bytes(), (fin, fout, nm, shots, counts)
+
+
+def test_malformed_result_files_read_like_reference_convert(tmp_path):
+    # Random, often malformed files in every format: accepted or rejected as `stim convert` accepts them, and when
+    # accepted, read as the same bits.
+    r = random.Random(17)
+    a, b = tmp_path / "a", tmp_path / "b"
+
+    def make(fmt, nm):
+        if fmt == "01":
+            lines = ["".join(r.choice("01") for _ in range(nm + r.choice([0, 0, 0, -1, 1])))
+                     for _ in range(r.randint(0, 4))]
+            text = "\n".join(lines) + r.choice(["\n", "", "\n\n", "\r\n"])
+            return (text.replace("1", "2", 1) if r.random() < 0.1 else text).encode()
+        if fmt == "b8":
+            return bytes(r.randrange(256) for _ in range(r.randint(0, 3 * ((nm + 7) // 8) + 1)))
+        if fmt == "r8":
+            return bytes(r.choice([0, 1, 2, 5, 255, nm]) % 256 for _ in range(r.randint(0, 8)))
+        if fmt == "hits":
+            lines = [",".join(str(r.randrange(nm + 2)) for _ in range(r.randint(0, 3))) for _ in range(r.randint(0, 3))]
+            return ("\n".join(lines) + r.choice(["\n", ""])).encode()
+        if fmt == "dets":
+            lines = ["shot" + "".join(f" {r.choice('MDL')}{r.randrange(nm + 1)}" for _ in range(r.randint(0, 3)))
+                     for _ in range(r.randint(0, 3))]
+            return ("\n".join(lines) + r.choice(["\n", ""])).encode()
+        return bytes(r.randrange(256) for _ in range(8 * nm * r.randint(0, 2) + r.choice([0, 0, 3])))
+
+    for _ in range(300):
+        fmt = r.choice(["01", "b8", "r8", "hits", "dets", "ptb64"])
+        nm = r.choice([1, 3, 8, 9, 16, 17])
+        a.write_bytes(make(fmt, nm))
+        p = ref(["convert", "--in", str(a), "--in_format", fmt, "--out", str(b), "--out_format", "01",
+                 "--num_measurements", str(nm), "--num_detectors", "0", "--num_observables", "0"])
+        try:
+            got = stim_gb300.read_shot_data_file(path=str(a), format=fmt, num_measurements=nm)
+        except (ValueError, IndexError):
+            got = None
+        assert (p.returncode == 0) == (got is not None), (fmt, nm, a.read_bytes()[:60], p.stderr[:100])
+        if got is not None:
+            rows = [[ch == "1" for ch in ln] for ln in b.read_text().split("\n") if ln]
+            want = np.array(rows, dtype=np.bool_).reshape(-1, nm) if rows else np.zeros((0, nm), dtype=np.bool_)
+            np.testing.assert_array_equal(got, want)
