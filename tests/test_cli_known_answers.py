@@ -277,7 +277,8 @@ def dets_lines(d, o, append):
 def oracle_m2d_dets(text, data01, skip, append):
     c, o = stim_gb300.Circuit(text), OracleCircuit(text)
     ref = None if skip else c.reference_sample(bit_packed=True)
-    d, ob = o.m2d(np.packbits(parse01(data01), axis=1, bitorder="little"), ref if ref is not None and ref.size else None)
+    packed = np.packbits(parse01(data01), axis=1, bitorder="little")
+    d, ob = o.m2d(packed, ref if ref is not None and ref.size else None)
     d = np.unpackbits(d, axis=1, bitorder="little")[:, :o.num_detectors]
     ob = np.unpackbits(ob, axis=1, bitorder="little")[:, :o.num_observables]
     return d, ob

@@ -51,7 +51,8 @@ ACCEPTED = [
     ("H[test] 3 5", 0), ("H[] 3 5", 0), ("H[test \\B\\C\\r\\n] 3 5", 0),
     ("X_ERROR[test](0.125)\nX_ERROR[no_fuse](0.125) 1\nX_ERROR(0.125) 2\nX_ERROR[](0.125) 3\n"
      "REPEAT[looper] 5 {\n    CX[within] 0 1\n}", 0),
-    ("CNOT sweep[2] 5", 0), ("CNOT 0 1\nM !0\nM(0.125) !0", 2), ("CORRELATED_ERROR(0.1) X0\nCORRELATED_ERROR(0.1) Z0", 0),
+    ("CNOT sweep[2] 5", 0), ("CNOT 0 1\nM !0\nM(0.125) !0", 2),
+    ("CORRELATED_ERROR(0.1) X0\nCORRELATED_ERROR(0.1) Z0", 0),
     ("X_ERROR(0.5) 0", 0), ("X_ERROR(0) 1", 0), ("X_ERROR(0.1) 1", 0), ("X_ERROR(1) 1", 0),
     ("PAULI_CHANNEL_1(0,0,0) 1", 0), ("PAULI_CHANNEL_1(0.1,0.2,0.6) 1", 0), ("PAULI_CHANNEL_1(1,0,0) 1", 0),
     ("PAULI_CHANNEL_1(0.33333333334,0.33333333334,0.33333333334) 1", 0),
